@@ -1,0 +1,215 @@
+/*
+ * kestrel_gpu.h -- C ABI of the GB300 implementation of Kestrel's time-step hot path.
+ *
+ * The reference (Kestrel v1.1.1, serial Fortran 2008) has no plugin interface for its
+ * hot path: the module procedures below are called directly from `Run`
+ * (src/TimeStepper.f90:73) and `main` (src/main.f90:171).  This header is the drop-in
+ * boundary a Fortran host binds with ISO_C_BINDING, in the same way the reference already
+ * binds its C++ glue (src/GeoTiffRead.f90:43-100 <-> src/RasterData.h:181-,
+ * src/version.f90:25-33 <-> src/cversion.cpp:28-34).  The binding a maintainer adds is
+ * shown in INTEGRATION.md.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: 0 (KG_OK) or a negative KG_ERR_* code.  The
+ *    library never calls exit/abort and never traps on the device.  kg_last_error() gives
+ *    a one-line message for the last failure on a context.
+ *  - All pointers in signatures are HOST pointers; the context owns every device buffer.
+ *  - Indices are 1-based tile IDs exactly as in the reference (src/Grid.f90:260-267,
+ *    id = i + (j-1)*nXtiles, tiles numbered from the south-west corner).
+ *  - Per-tile cell arrays are nXpertile*nYpertile doubles, i (x) fastest, i.e. the
+ *    reference's u(d, :, :) slice for one field d (src/Grid.f90:83).
+ *  - One context = one simulation on one GPU and one CUDA stream; calls on the same
+ *    context are not thread-safe, separate contexts are independent.
+ */
+#ifndef KESTREL_GPU_H
+#define KESTREL_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (replace FatalErrorMessage / exit(1), src/Messages.f90:56-90) ---- */
+#define KG_OK                 0
+#define KG_ERR_PARAM         -1  /* invalid parameter value (src/Parameters.f90 FatalError_*) */
+#define KG_ERR_OOM           -2  /* device or host allocation failed */
+#define KG_ERR_HALT_EDGE     -3  /* flow reached the domain edge under 'halt' (src/UpdateTiles.f90:61-69) */
+#define KG_ERR_NAN           -4  /* non-finite state detected */
+#define KG_ERR_CUDA          -5  /* CUDA runtime error */
+#define KG_ERR_UNSUPPORTED   -6  /* configuration outside the implemented path (e.g. 1D grids) */
+#define KG_ERR_STATE         -7  /* call out of order (e.g. stepping before sources are loaded) */
+#define KG_ERR_DT            -8  /* time step collapsed (dt <= 0 or too many refinements) */
+#define KG_ERR_NOT_FOUND     -9  /* requested tile is not active */
+#define KG_ERR_TIMEOUT      -10  /* a bounded device wait expired */
+
+/* ---- runtime closure selections (procedure pointers in the reference) ---- */
+/* Drag: src/Parameters.f90:222-247, src/Closures.f90:365-558 */
+enum { KG_DRAG_CHEZY = 0, KG_DRAG_COULOMB = 1, KG_DRAG_VOELLMY = 2, KG_DRAG_POULIQUEN = 3,
+       KG_DRAG_EDWARDS2019 = 4, KG_DRAG_VARIABLE = 5, KG_DRAG_MANNING = 6 };
+/* Erosion: src/Parameters.f90:285-310, src/Closures.f90:566-675 */
+enum { KG_ERO_OFF = 0, KG_ERO_MIXED = 1, KG_ERO_SIMPLE = 2, KG_ERO_FLUID = 3, KG_ERO_GRANULAR = 4 };
+/* Deposition: src/Parameters.f90:163-176, src/Closures.f90:320-356 */
+enum { KG_DEP_NONE = 0, KG_DEP_SIMPLE = 1, KG_DEP_SPEARMAN_MANNING = 2 };
+/* Erosion transition: src/Closures.f90:684-732 */
+enum { KG_ETRANS_SMOOTH = 0, KG_ETRANS_STEP = 1, KG_ETRANS_OFF = 2 };
+/* Morphodynamic damping: src/Closures.f90:744-791 */
+enum { KG_DAMP_NONE = 0, KG_DAMP_TANH = 1, KG_DAMP_RAT3 = 2 };
+/* Switch function: src/Closures.f90:797-915 */
+enum { KG_SWITCH_TANH = 0, KG_SWITCH_RAT3 = 1, KG_SWITCH_COS = 2, KG_SWITCH_LINEAR = 3,
+       KG_SWITCH_EQUAL = 4, KG_SWITCH_ZERO = 5, KG_SWITCH_ONE = 6, KG_SWITCH_STEP = 7 };
+/* Slope limiter: src/SolverSettings.f90:102-126, src/Limiters.f90:83-184 */
+enum { KG_LIM_MINMOD1 = 0, KG_LIM_MINMOD2 = 1, KG_LIM_VANALBADA = 2, KG_LIM_WENO = 3, KG_LIM_NONE = 4 };
+/* Boundary conditions: src/DomainSettings.f90:108-120 */
+enum { KG_BC_HALT = 0, KG_BC_PERIODIC = 1, KG_BC_DIRICHLET = 2, KG_BC_SPONGE = 3 };
+/* Analytic topography (src/TopogFuncs.f90) or an uploaded vertex grid (kg_upload_b0). */
+enum { KG_TOPO_UPLOAD = 0, KG_TOPO_FLAT = 1, KG_TOPO_XSLOPE = 2, KG_TOPO_YSLOPE = 3,
+       KG_TOPO_XYSLOPE = 4, KG_TOPO_XSINSLOPE = 5, KG_TOPO_XYSINSLOPE = 6, KG_TOPO_XHUMP = 7,
+       KG_TOPO_XTANH = 8, KG_TOPO_XPARAB = 9, KG_TOPO_XYPARAB = 10 };
+/* Cap / cube shapes: src/InitConds.f90:499-510, :705-712 */
+enum { KG_SHAPE_FLAT = 0, KG_SHAPE_PARA = 1, KG_SHAPE_LEVEL = 2 };
+/* Arithmetic form of the GPU path. */
+enum { KG_PREC_FP64 = 0, KG_PREC_FP32 = 1 };
+
+#define KG_MAX_CAPS     16
+#define KG_MAX_CUBES    16
+#define KG_MAX_SOURCES  16
+#define KG_MAX_SERIES   64
+#define KG_MAX_TOPO_PARAMS 8
+
+typedef struct {                       /* src/InitConds.f90 type Caps */
+    double x, y, radius, height, psi, u, v;
+    int32_t shape, _pad;
+} kg_cap;
+
+typedef struct {                       /* src/InitConds.f90 type Cubes */
+    double x, y, length, width, height, psi, u, v;
+    int32_t shape, _pad;
+} kg_cube;
+
+typedef struct {                       /* src/InitConds.f90 type Sources */
+    double x, y, radius;
+    int32_t n_series, _pad;
+    double time[KG_MAX_SERIES];
+    double flux[KG_MAX_SERIES];
+    double psi[KG_MAX_SERIES];
+} kg_flux_source;
+
+/*
+ * Every numeric RunSet field the hot path reads (src/RunSettings.f90:161-340), with the
+ * reference's defaults applied by the host-side parser (kestrel_gb300/config.py).  The
+ * derived quantities (gred, Rep, ws0, nsettling, CriticalShields, diffusiveTimeScale,
+ * deltaX/Y; src/Parameters.f90:629-648, src/DomainSettings.f90:196-225) are computed by
+ * kg_create from these.
+ */
+typedef struct {
+    /* Domain block */
+    int32_t nXtiles, nYtiles, nXpertile, nYpertile;
+    double  Xtilesize, Ytilesize;
+    int32_t bcs, _pad0;
+    double  bcsHnval, bcsuval, bcsvval, bcspsival;
+    /* Parameters block */
+    int32_t geometric_factors, MorphodynamicsOn;
+    double  g, rhow, rhos;
+    double  ChezyCo, ManningCo, CoulombCo;
+    double  PouliquenMinSlope, PouliquenMaxSlope, PouliquenIntermediateSlope, PouliquenBeta;
+    double  Edwards2019betastar, Edwards2019kappa, Edwards2019Gamma;
+    double  VoellmySwitchRate, VoellmySwitchValue;
+    double  EroRate, EroRateGranular, EroDepth, EroCriticalHeight, BedPorosity;
+    double  maxPack, SolidDiameter, EddyViscosity;
+    int32_t ws0_given, _pad1;           /* 'Settling speed' key overrides the derived ws0 */
+    double  ws0;
+    int32_t drag, erosion, deposition, erosion_transition, morpho_damping, fswitch;
+    /* Solver block */
+    int32_t limiter, TileBuffer;
+    double  heightThreshold, cfl, maxdt, tstart, tend, SpongeStrength;
+    /* Output block: Nout fixes the IntegrateTo end points (src/TimeStepper.f90:97-103) */
+    int32_t Nout, _pad2;
+    /* Initial conditions */
+    int32_t nCaps, nCubes, nSources, _pad3;
+    kg_cap  caps[KG_MAX_CAPS];
+    kg_cube cubes[KG_MAX_CUBES];
+    kg_flux_source sources[KG_MAX_SOURCES];
+    /* Topog block */
+    int32_t topog, n_topog_params;
+    double  topog_params[KG_MAX_TOPO_PARAMS];
+} kg_params;
+
+/* Per-call statistics of kg_step / kg_integrate_to. */
+typedef struct {
+    double  t;                  /* simulation time after the call */
+    double  dt;                 /* last accepted hydraulic dt (dt_hydro) */
+    int64_t steps;              /* accepted steps taken by this call */
+    int64_t rejected;           /* dt refinements (rejected attempts) in this call */
+    int64_t cell_updates;       /* active cells x accepted hydraulic steps (H.M.H counts 2) */
+    int32_t n_active, n_ghost;  /* tile counts after the call */
+    int64_t kernel_launches;    /* device kernels launched by this call */
+} kg_step_stats;
+
+typedef struct kg_ctx kg_ctx;
+
+/* Library version string (src/version.f90 GetVersion analogue). */
+const char* kg_version(void);
+
+/* InitialiseGrid (src/Grid.f90:166) + topography set-up (src/dem.f90 LoadDEM). precision
+   selects the FP64 drop-in (KG_PREC_FP64) or the FP32 mixed form (KG_PREC_FP32). */
+int  kg_create(const kg_params* params, int32_t precision, kg_ctx** out);
+void kg_destroy(kg_ctx* ctx);
+const char* kg_last_error(const kg_ctx* ctx);
+
+/* Replaces GetTileHeights (src/dem.f90:395-416) with a global vertex grid of
+   (nXtiles*nXpertile+1) x (nYtiles*nYpertile+1) heights, x fastest, vertex (0,0) at the
+   south-west domain corner.  Must be called before kg_load_sources when topog==UPLOAD. */
+int  kg_upload_b0(kg_ctx* ctx, const double* b0_vertices, int64_t nx1, int64_t ny1);
+
+/* LoadSourceConditions (src/SetSources.f90:47-405): places caps, cubes and flux sources
+   and activates (AddTile) every tile that covers them. */
+int  kg_load_sources(kg_ctx* ctx);
+
+/* One accepted time step of IntegrateTo's loop (src/TimeStepper.f90:151-275), ending no
+   later than t_stop. */
+int  kg_step(kg_ctx* ctx, double t_stop, kg_step_stats* stats);
+
+/* IntegrateTo (src/TimeStepper.f90:116-277): step until t >= t_end. */
+int  kg_integrate_to(kg_ctx* ctx, double t_end, kg_step_stats* stats);
+
+/* Run (src/TimeStepper.f90:73-112) without the file output: integrate to each of the Nout
+   output times tstart + i*DeltaT in turn. */
+int  kg_run(kg_ctx* ctx, kg_step_stats* stats);
+
+/* CalculateHydraulicRHS (src/HydraulicRHS.f90:64-136) applied to the current solution
+   (the reference's tileContainer) at time t for the given substep (1..4).  Writes the
+   advised time step; the RHS itself is readable with kg_get_tile_rhs. */
+int  kg_hydraulic_rhs(kg_ctx* ctx, double t, int32_t substep, double* advised_dt);
+
+/* Sorted active tile list (src/Grid.f90:123 activeTiles%List) and ghost list (append
+   order).  *n is in/out: capacity on entry, count on exit. */
+int  kg_get_active_tiles(kg_ctx* ctx, int32_t* ids, int32_t* n);
+int  kg_get_ghost_tiles(kg_ctx* ctx, int32_t* ids, int32_t* n);
+
+/* One field (1..13, src/main.f90:116-141) of the current solution for an active tile,
+   nXpertile*nYpertile doubles.  Fields 5..9 are the desingularised variables as the
+   reference holds them in tileContainer after the last step. */
+int  kg_get_tile_field(kg_ctx* ctx, int32_t tile_id, int32_t field, double* out);
+/* Overwrite one of the conserved fields 1..4 of an active tile (tests, restarts). */
+int  kg_set_tile_field(kg_ctx* ctx, int32_t tile_id, int32_t field, const double* in);
+/* Vertex bed of an active tile, (nXpertile+1)*(nYpertile+1) doubles: which=0 b0, 1 bt. */
+int  kg_get_tile_vertex(kg_ctx* ctx, int32_t tile_id, int32_t which, double* out);
+/* ddtExplicit (k=1..4) / ddtImplicit (k=5, momenta) of the last kg_hydraulic_rhs call. */
+int  kg_get_tile_rhs(kg_ctx* ctx, int32_t tile_id, int32_t k, double* out);
+/* Running maxima (src/TimeStepper.f90:1155-1303): which = 0 Hnmax, 1 umax, 2 emax,
+   3 dmax, 4 psimax (value plane then time plane, 2*nX*nY doubles), 5 tfirst (nX*nY). */
+int  kg_get_tile_maxima(kg_ctx* ctx, int32_t tile_id, int32_t which, double* out);
+
+/* CalculateVolume (src/Output.f90:617-737): out = {volume, total_bed_volume, total_mass,
+   total_solids} before the rho multipliers, i.e. the four Kahan sums times dx*dy. */
+int  kg_volume(kg_ctx* ctx, double out[4]);
+
+/* Current time, last dt and the number of device kernels launched so far. */
+int  kg_get_time(kg_ctx* ctx, double* t, double* dt);
+int64_t kg_kernel_launches(const kg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KESTREL_GPU_H */

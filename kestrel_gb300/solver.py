@@ -1,0 +1,152 @@
+"""Host-side mirror of the reference's Run / IntegrateTo interface over the C ABI.
+
+``Simulation`` drives any library that exports the kg_ API of include/kestrel_gpu.h (the
+GPU library built from kestrel_gb300/csrc).  It follows the call order of
+src/main.f90:148-171: read input -> InitialiseGrid/LoadDEM (kg_create, kg_upload_b0) ->
+LoadSourceConditions (kg_load_sources) -> Run (kg_run / kg_integrate_to).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class KestrelError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{abi.KG_ERR.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Simulation:
+    """One simulation on one context.  ``lib``/``prefix`` select the implementation."""
+
+    def __init__(self, lib, prefix: str, params: abi.Params, precision: int = abi.PREC_FP64,
+                 b0: np.ndarray | None = None, load_sources: bool = True):
+        self.lib, self.pre = lib, prefix
+        self.params = params
+        self.nX, self.nY = params.nXpertile, params.nYpertile
+        h = C.c_void_p()
+        if prefix == "kg":
+            rc = self._f("create")(C.byref(params), precision, C.byref(h))
+        else:
+            rc = self._f("create")(C.byref(params), C.byref(h))
+        if rc != abi.KG_OK:
+            raise KestrelError(rc, "create failed")
+        self.h = h
+        if b0 is not None:
+            self.upload_b0(b0)
+        if load_sources:
+            self._check(self._f("load_sources")(self.h))
+
+    def _f(self, name):
+        return getattr(self.lib, f"{self.pre}_{name}")
+
+    def _check(self, rc):
+        if rc != abi.KG_OK:
+            msg = self._f("last_error")(self.h)
+            raise KestrelError(rc, msg.decode() if msg else "")
+        return rc
+
+    def close(self):
+        if self.h:
+            self._f("destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- set-up --------------------------------------------------------------------
+    def upload_b0(self, b0: np.ndarray):
+        b0 = np.ascontiguousarray(b0, dtype=np.float64)
+        ny1, nx1 = b0.shape
+        self._check(self._f("upload_b0")(self.h, b0.ctypes.data_as(C.POINTER(C.c_double)), nx1, ny1))
+
+    # -- stepping ------------------------------------------------------------------
+    def step(self, t_stop: float) -> abi.StepStats:
+        st = abi.StepStats()
+        self._check(self._f("step")(self.h, t_stop, C.byref(st)))
+        return st
+
+    def integrate_to(self, t_end: float) -> abi.StepStats:
+        st = abi.StepStats()
+        self._check(self._f("integrate_to")(self.h, t_end, C.byref(st)))
+        return st
+
+    def run(self) -> abi.StepStats:
+        st = abi.StepStats()
+        self._check(self._f("run")(self.h, C.byref(st)))
+        return st
+
+    def hydraulic_rhs(self, t: float, substep: int = 1) -> float:
+        adv = C.c_double()
+        self._check(self._f("hydraulic_rhs")(self.h, t, substep, C.byref(adv)))
+        return adv.value
+
+    # -- state access --------------------------------------------------------------
+    @property
+    def time(self):
+        t, dt = C.c_double(), C.c_double()
+        self._check(self._f("get_time")(self.h, C.byref(t), C.byref(dt)))
+        return t.value, dt.value
+
+    def _ids(self, name):
+        n = C.c_int32(0)
+        self._f(name)(self.h, None, C.byref(n))
+        buf = (C.c_int32 * max(n.value, 1))()
+        self._check(self._f(name)(self.h, buf, C.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def active_tiles(self):
+        return self._ids("get_active_tiles")
+
+    def ghost_tiles(self):
+        return self._ids("get_ghost_tiles")
+
+    def field(self, tile: int, field: int) -> np.ndarray:
+        out = np.empty(self.nX * self.nY, dtype=np.float64)
+        self._check(self._f("get_tile_field")(self.h, tile, field, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out.reshape(self.nY, self.nX)
+
+    def set_field(self, tile: int, field: int, values: np.ndarray):
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        self._check(self._f("set_tile_field")(self.h, tile, field, v.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def vertex(self, tile: int, which: int) -> np.ndarray:
+        out = np.empty((self.nX + 1) * (self.nY + 1), dtype=np.float64)
+        self._check(self._f("get_tile_vertex")(self.h, tile, which, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out.reshape(self.nY + 1, self.nX + 1)
+
+    def rhs(self, tile: int, k: int) -> np.ndarray:
+        out = np.empty(self.nX * self.nY, dtype=np.float64)
+        self._check(self._f("get_tile_rhs")(self.h, tile, k, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out.reshape(self.nY, self.nX)
+
+    def maxima(self, tile: int, which: int) -> np.ndarray:
+        n = self.nX * self.nY * (1 if which == 5 else 2)
+        out = np.empty(n, dtype=np.float64)
+        self._check(self._f("get_tile_maxima")(self.h, tile, which, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out.reshape(-1, self.nY, self.nX)
+
+    def volume(self) -> np.ndarray:
+        out = (C.c_double * 4)()
+        self._check(self._f("volume")(self.h, out))
+        return np.array(list(out))
+
+    def state(self, fields=range(1, 14)) -> dict:
+        """{tile_id: array (len(fields), nY, nX)} for every active tile."""
+        return {t: np.stack([self.field(t, f) for f in fields]) for t in self.active_tiles()}
+
+    def global_field(self, field: int, fill=np.nan) -> np.ndarray:
+        """Assemble one field over the whole domain (inactive tiles filled)."""
+        p = self.params
+        out = np.full((p.nYtiles * self.nY, p.nXtiles * self.nX), fill)
+        for t in self.active_tiles():
+            gi, gj = (t - 1) % p.nXtiles, (t - 1) // p.nXtiles
+            out[gj * self.nY:(gj + 1) * self.nY, gi * self.nX:(gi + 1) * self.nX] = self.field(t, field)
+        return out

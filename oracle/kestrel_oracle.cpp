@@ -1,0 +1,994 @@
+// kestrel_oracle.cpp -- TEST INFRASTRUCTURE (the oracle), not part of the product.
+//
+// CPU FP64 restatement of Kestrel v1.1.1's time stepper (src/TimeStepper.f90), excess-
+// deposition redistribution (src/Redistribute.f90), source placement (src/SetSources.f90),
+// volume accounting (src/Output.f90:617-737) and run-settings derivation
+// (src/Parameters.f90:629-648, src/DomainSettings.f90:185-225), exported as a C API with
+// the prefix ko_ so tests can drive it through ctypes beside the GPU library.
+//
+// Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg load this library.
+// Parity: pinned against the reference's invariant tests (tests/testlib.jl) on the
+// reference's input files; no golden vectors exist in the reference (see ko_model.hpp).
+#include "ko_step.hpp"
+#include <chrono>
+#include <cstdio>
+
+namespace ko {
+
+// ---------------------------------------------------------------- TimeStepper.f90
+static void CopyMutableTopographicData(const RunSet& rp, Grid& g, Tiles& from, Tiles& to) {  // :838-875
+    for (int id : g.activeTiles) {
+        Tile& F = TL(from, id);
+        Tile& T = TL(to, id);
+        int nX = rp.nXpertile, nY = rp.nYpertile;
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i) {
+                T.u(ibt, i, j) = F.u(ibt, i, j);
+                T.u(idbdx, i, j) = F.u(idbdx, i, j);
+                T.u(idbdy, i, j) = F.u(idbdy, i, j);
+            }
+        T.bt = F.bt;
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX + 1; ++i)
+                for (int d : {ibt, idbdx, idbdy}) {
+                    T.uPlusX(d, i, j) = F.uPlusX(d, i, j);
+                    T.uMinusX(d, i, j) = F.uMinusX(d, i, j);
+                }
+        for (int j = 1; j <= nY + 1; ++j)
+            for (int i = 1; i <= nX; ++i)
+                for (int d : {ibt, idbdx, idbdy}) {
+                    T.uPlusY(d, i, j) = F.uPlusY(d, i, j);
+                    T.uMinusY(d, i, j) = F.uMinusY(d, i, j);
+                }
+    }
+}
+static void CopySolutionData(const RunSet& rp, Grid& g, Tiles& from, Tiles& to) {  // :811-833
+    CopyMutableTopographicData(rp, g, from, to);
+    for (int id : g.activeTiles) {
+        Tile& F = TL(from, id);
+        Tile& T = TL(to, id);
+        T.u = F.u;
+        T.ddtExplicit = F.ddtExplicit;
+        T.ddtImplicit = F.ddtImplicit;
+        if (rp.MorphodynamicsOn) T.ddtExplicitBt = F.ddtExplicitBt;
+    }
+}
+static void InitialiseTimeSteppingArrays(Grid& g) {  // :785-808
+    for (int id : g.activeTiles) {
+        TL(g.intermed0, id) = g.tc(id);
+        TL(g.intermed1, id) = g.tc(id);
+        TL(g.intermed2, id) = g.tc(id);
+        TL(g.intermed3, id) = g.tc(id);
+    }
+    for (int id : g.ghostTiles) {
+        TL(g.intermed0, id) = g.tc(id);
+        TL(g.intermed1, id) = g.tc(id);
+        TL(g.intermed2, id) = g.tc(id);
+        TL(g.intermed3, id) = g.tc(id);
+    }
+}
+// ApplySpongeLayer, :879-920.  Its condition compares neighbour IDs with 0, which only
+// tiles 1 and nXtiles satisfy; those lie on the domain edge and are never active under
+// 'sponge', so this never fires.  The morphodynamic branch would index ddtExplicit(ibt)
+// past its 4 rows; it is unreachable for the same reason and is not restated.
+static void ApplySpongeLayer(const RunSet& rp, Grid& g, int ttk, Tiles& im, bool morpho) {
+    if (!rp.SpongeLayer || morpho) return;
+    Tile& C = g.tc(ttk);
+    if ((C.North() == 0 || C.South() == 0) || C.East() == 0 || C.West() == 0) {
+        Tile& T = TL(im, ttk);
+        for (int j = 1; j <= rp.nYpertile; ++j)
+            for (int i = 1; i <= rp.nXpertile; ++i)
+                for (int d = 1; d <= 4; ++d)
+                    T.ddtExplicit(d, i, j) = T.ddtExplicit(d, i, j) - rp.p.SpongeStrength * T.u(d, i, j);
+    }
+}
+
+static void UpdateMaxima(const RunSet& rp, Tile& T, double t) {  // :1155-1303
+    int nX = rp.nXpertile, nY = rp.nYpertile;
+    for (int jj = 1; jj <= nY; ++jj)
+        for (int ii = 1; ii <= nX; ++ii) {
+            double Hn = T.u(iHn, ii, jj);
+            if (Hn > rp.heightThreshold) {
+                if (T.tfirst(ii, jj) == -1) T.tfirst(ii, jj) = t;
+                if (Hn > T.Hnmax(ii, jj, 1)) { T.Hnmax(ii, jj, 1) = Hn; T.Hnmax(ii, jj, 2) = t; }
+            }
+        }
+    for (int jj = 1; jj <= nY; ++jj)
+        for (int ii = 1; ii <= nX; ++ii) {
+            double spd = std::sqrt(FlowSquaredSpeedSlopeAligned(rp, T.u.col(ii, jj)));
+            if ((spd > T.umax(ii, jj, 1)) && (T.u(iHn, ii, jj) > rp.heightThreshold)) {
+                T.umax(ii, jj, 1) = spd;
+                T.umax(ii, jj, 2) = t;
+            }
+        }
+    for (int jj = 1; jj <= nY; ++jj)
+        for (int ii = 1; ii <= nX; ++ii) {
+            double bt = T.u(ibt, ii, jj);
+            if (bt < 0 && -bt > T.emax(ii, jj, 1)) { T.emax(ii, jj, 1) = -bt; T.emax(ii, jj, 2) = t; }
+        }
+    for (int jj = 1; jj <= nY; ++jj)
+        for (int ii = 1; ii <= nX; ++ii) {
+            double bt = T.u(ibt, ii, jj);
+            if (bt > 0 && bt > T.dmax(ii, jj, 1)) { T.dmax(ii, jj, 1) = bt; T.dmax(ii, jj, 2) = t; }
+        }
+    for (int jj = 1; jj <= nY; ++jj)
+        for (int ii = 1; ii <= nX; ++ii) {
+            double psi = T.u(ipsi, ii, jj);
+            if (T.u(iHn, ii, jj) > rp.heightThreshold && psi > T.psimax(ii, jj, 1)) {
+                T.psimax(ii, jj, 1) = psi;
+                T.psimax(ii, jj, 2) = t;
+            }
+        }
+}
+
+struct Sim {
+    RunSet rp;
+    Grid g;
+    std::string err;
+    int64_t rejected = 0, steps = 0, cell_updates = 0;
+    double last_rhs_dt = 0.0;
+    bool sources_loaded = false;
+};
+
+// HydraulicTimeStepper, :333-527.
+static bool HydraulicTimeStepper(Sim& s, double& thisdt, double& nextT) {
+    RunSet& rp = s.rp;
+    Grid& g = s.g;
+    Tiles &im0 = g.intermed0, &im1 = g.intermed1, &im2 = g.intermed2, &im3 = g.intermed3;
+    int nX = rp.nXpertile, nY = rp.nYpertile;
+    double t = g.t;
+    nextT = g.t + thisdt;
+    g.dt = thisdt;
+    for (int ttk : g.activeTiles) {
+        ApplySpongeLayer(rp, g, ttk, im0, false);
+        Tile &A = TL(im0, ttk), &B = TL(im1, ttk);
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i)
+                for (int var = 1; var <= 4; ++var) {
+                    if (var == irhoHnu || var == irhoHnv)
+                        B.u(var, i, j) = (A.u(var, i, j) + thisdt * A.ddtExplicit(var, i, j)) /
+                                         (1.0 - thisdt * A.ddtImplicit(var, i, j));
+                    else
+                        B.u(var, i, j) = A.u(var, i, j) + thisdt * A.ddtExplicit(var, i, j);
+                }
+    }
+    double dt1 = CalculateHydraulicRHS(rp, g, im1, nextT, 2);
+    if (dt1 < thisdt) { thisdt = 0.9 * dt1; return true; }
+    for (int ttk : g.activeTiles) {
+        ApplySpongeLayer(rp, g, ttk, im1, false);
+        Tile &A = TL(im0, ttk), &B = TL(im1, ttk), &C = TL(im2, ttk);
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i)
+                for (int var = 1; var <= 4; ++var) {
+                    if (var == irhoHnu || var == irhoHnv) {
+                        C.u(var, i, j) = 0.75 * A.u(var, i, j) +
+                                         0.25 * (B.u(var, i, j) + thisdt * B.ddtExplicit(var, i, j)) /
+                                             (1.0 - thisdt * B.ddtImplicit(var, i, j));
+                    } else if (var == iw) {
+                        double hp_old = -A.u(ibt, i, j);
+                        hp_old = hp_old + (A.u(iw, i, j) - A.u(ib0, i, j));
+                        double hp_new = -B.u(ibt, i, j);
+                        hp_new = hp_new + (B.u(iw, i, j) - B.u(ib0, i, j));
+                        double w = A.u(ibt, i, j);
+                        w = w + 0.25 * hp_new;
+                        w = w + 0.75 * hp_old;
+                        w = w + 0.25 * thisdt * B.ddtExplicit(var, i, j);
+                        w = w + A.u(ib0, i, j);
+                        C.u(var, i, j) = w;
+                    } else {
+                        C.u(var, i, j) = 0.75 * A.u(var, i, j) + 0.25 * (B.u(var, i, j) + thisdt * B.ddtExplicit(var, i, j));
+                    }
+                }
+    }
+    double dt2 = CalculateHydraulicRHS(rp, g, im2, t + 0.5 * thisdt, 3);
+    if (dt2 < thisdt) { thisdt = 0.9 * dt2; return true; }
+    const double third = 1.0 / 3.0, twothird = 2.0 / 3.0;
+    for (int ttk : g.activeTiles) {
+        ApplySpongeLayer(rp, g, ttk, im2, false);
+        Tile &A = TL(im0, ttk), &C = TL(im2, ttk), &D = TL(im3, ttk);
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i)
+                for (int var = 1; var <= 4; ++var) {
+                    if (var == irhoHnu || var == irhoHnv) {
+                        D.u(var, i, j) = third * A.u(var, i, j) +
+                                         twothird * (C.u(var, i, j) + thisdt * C.ddtExplicit(var, i, j)) /
+                                             (1.0 - thisdt * C.ddtImplicit(var, i, j));
+                    } else if (var == iw) {
+                        double hp_old = -A.u(ibt, i, j);
+                        hp_old = hp_old + (A.u(iw, i, j) - A.u(ib0, i, j));
+                        double hp_new = -C.u(ibt, i, j);
+                        hp_new = hp_new + (C.u(iw, i, j) - C.u(ib0, i, j));
+                        double w = A.u(ibt, i, j);
+                        w = w + third * hp_old;
+                        w = w + twothird * hp_new;
+                        w = w + twothird * thisdt * C.ddtExplicit(var, i, j);
+                        w = w + A.u(ib0, i, j);
+                        D.u(var, i, j) = w;
+                    } else {
+                        D.u(var, i, j) = third * A.u(var, i, j) + twothird * (C.u(var, i, j) + thisdt * C.ddtExplicit(var, i, j));
+                    }
+                }
+    }
+    CalculateHydraulicRHS(rp, g, im3, nextT, 4);
+    for (int ttk : g.activeTiles) {
+        ApplySpongeLayer(rp, g, ttk, im3, false);
+        Tile& D = TL(im3, ttk);
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i)
+                for (int var : {irhoHnu, irhoHnv}) {
+                    D.u(var, i, j) = (D.u(var, i, j) - thisdt * thisdt * D.ddtExplicit(var, i, j) * D.ddtImplicit(var, i, j)) /
+                                     (1.0 + thisdt * thisdt * D.ddtImplicit(var, i, j) * D.ddtImplicit(var, i, j));
+                }
+        ComputeDesingularisedVariables(rp, g.tileContainer, ttk, true);
+        UpdateMaxima(rp, g.tc(ttk), nextT);
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------- Redistribute.f90
+struct RedistNode { int ttk, i, j; double excess_dep; };
+static void AddToRedistList(std::vector<RedistNode>& list, int ttk, int i, int j, double ex) {  // :69-101
+    RedistNode n{ttk, i, j, ex};
+    if (list.empty()) { list.push_back(n); return; }
+    if (list[0].excess_dep > ex) { list.insert(list.begin(), n); return; }
+    size_t p = 0;
+    while (true) {
+        if (p + 1 >= list.size()) break;
+        if (list[p + 1].excess_dep > ex) break;
+        p++;
+    }
+    list.insert(list.begin() + (long)(p + 1), n);
+}
+static void ExcessDeposition(const RunSet& rp, Tiles& before, Tiles& after, int ttk, int i, int j,
+                             double& excess_dep, double& deltaBt, double& psiold) {  // :158-198
+    Tile &B = TL(before, ttk), &A = TL(after, ttk);
+    double gamold = Gam(rp, B.u.col(i, j)), gamnew = Gam(rp, A.u.col(i, j));
+    double Hn_old = ComputeHn(B.u(iw, i, j), B.u(ib0, i, j), B.u(ibt, i, j), gamold);
+    double Hn_new = ComputeHn(A.u(iw, i, j), A.u(ib0, i, j), A.u(ibt, i, j), gamnew);
+    (void)Hn_new;
+    deltaBt = A.u(ibt, i, j) - B.u(ibt, i, j);
+    psiold = B.u(ipsi, i, j);
+    excess_dep = -(B.u(iHnpsi, i, j) * gamold / (1.0 - rp.p.BedPorosity) - deltaBt);
+    excess_dep = std::max(excess_dep, -(Hn_old * gamold - deltaBt));
+}
+static bool RedistributeCell(const RunSet& rp, Grid& g, int ttk, int i, int j, double corr) {  // :249-475
+    Tiles &im0 = g.intermed0, &im3 = g.intermed3;
+    int nX = rp.nXpertile, nY = rp.nYpertile;
+    int N = 0;
+    double sum_b_diff = 0.0, b_diff[4] = {0, 0, 0, 0};
+    int depi[4], depj[4];
+    const int ci4[4] = {i, i + 1, i, i + 1}, cj4[4] = {j, j, j + 1, j + 1};
+    for (int q = 0; q < 4; ++q) {
+        b_diff[N] = TL(im3, ttk).bt(ci4[q], cj4[q]) - TL(im0, ttk).bt(ci4[q], cj4[q]);
+        if (b_diff[N] > 0.0) {
+            depi[N] = ci4[q];
+            depj[N] = cj4[q];
+            sum_b_diff = sum_b_diff + b_diff[N];
+            N = N + 1;
+        }
+    }
+    if (N == 0) return false;
+    double delta = 4.0 * corr / sum_b_diff;
+    double Hnold = TL(im0, ttk).u(iHn, i, j);
+    double gamold = Gam(rp, TL(im0, ttk).u.col(i, j));
+    double db = TL(im3, ttk).u(ibt, i, j) - TL(im0, ttk).u(ibt, i, j);
+    double tol = EPS * TL(im3, ttk).u(iw, i, j) * 10.0;
+    double adjustment = 0.0;
+    {
+        double a[3] = {Hnold * gamold, -db, corr};
+        double discrepancy = KahanSumL(a);
+        if (std::fabs(discrepancy) < tol) {
+            double b[3] = {tol, -Hnold * gamold, db};
+            adjustment = KahanSumL(b);
+            adjustment = adjustment * (4.0 / sum_b_diff);
+            adjustment = adjustment - delta;
+            adjustment = std::max(adjustment, 0.0);
+        }
+    }
+    double Hngampsi = TL(im0, ttk).u(iHnpsi, i, j) * gamold / (1.0 - rp.p.BedPorosity);
+    tol = EPS * 10.0;
+    {
+        double a[3] = {Hngampsi, -db, corr};
+        double discrepancy = KahanSumL(a);
+        if (std::fabs(discrepancy) < tol) {
+            double b[3] = {tol, -Hngampsi, db};
+            double adjustment_psi = KahanSumL(b);
+            adjustment_psi = adjustment_psi * (4.0 / sum_b_diff);
+            adjustment_psi = adjustment_psi - delta;
+            adjustment = std::max(adjustment, adjustment_psi);
+        }
+    }
+    delta = delta + adjustment;
+    for (int k = 0; k < N; ++k) {
+        Tile& T3 = TL(im3, ttk);
+        T3.bt(depi[k], depj[k]) = T3.bt(depi[k], depj[k]) - delta * b_diff[k];
+        double v = T3.bt(depi[k], depj[k]);
+        if (depi[k] == 1) TL(im3, T3.West()).bt(nX + 1, depj[k]) = v;
+        else if (depi[k] == nX + 1) TL(im3, T3.East()).bt(1, depj[k]) = v;
+        if (depj[k] == 1) {
+            TL(im3, T3.South()).bt(depi[k], nY + 1) = v;
+            if (depi[k] == 1) TL(im3, TL(im3, T3.South()).West()).bt(nX + 1, nY + 1) = v;
+            if (depi[k] == nX + 1) TL(im3, TL(im3, T3.South()).East()).bt(1, nY + 1) = v;
+        }
+        if (depj[k] == nY + 1) {
+            TL(im3, T3.North()).bt(depi[k], 1) = v;
+            if (depi[k] == 1) TL(im3, TL(im3, T3.North()).West()).bt(nX + 1, 1) = v;
+            if (depi[k] == nX + 1) TL(im3, TL(im3, T3.North()).East()).bt(1, 1) = v;
+        }
+    }
+    // Update the (up to) 3x3 surrounding cell centres; the tile navigation is kept
+    // exactly as written (:404-448).
+    int cttk, ci, cj;
+    if (i == 1) { cttk = g.tc(ttk).West(); ci = nX; }
+    else { cttk = ttk; ci = i - 1; }
+    for (int k = -1; k <= 1; ++k) {
+        if (j == 1) { cttk = g.tc(cttk).South(); cj = nY; }
+        else cj = j - 1;
+        for (int l = -1; l <= 1; ++l) {
+            ComputeCellCentredTopographicDataIJ(rp, g, im3, cttk, ci, cj);
+            Tile &T3 = TL(im3, cttk), &T0 = TL(im0, cttk);
+            double dbc = T3.u(ibt, ci, cj) - T0.u(ibt, ci, cj);
+            double go = Gam(rp, T0.u.col(ci, cj)), gn = Gam(rp, T3.u.col(ci, cj));
+            double Hno = T0.u(iHn, ci, cj);
+            double w = T3.u(ibt, ci, cj);
+            w = w + (Hno * go / gn - dbc / gn) / gn;
+            w = w + T3.u(ib0, ci, cj);
+            T3.u(iw, ci, cj) = w;
+            double Hnpsiold = T0.u(iHnpsi, ci, cj);
+            T3.u(iHnpsi, ci, cj) = Hnpsiold * go / gn - (1.0 - rp.p.BedPorosity) * dbc / gn;
+            cj = cj + 1;
+            if (cj == nY + 1 && l < 1) { cttk = g.tc(cttk).North(); cj = 1; }
+        }
+        if (j + 1 > nY) cttk = g.tc(cttk).South();
+        ci = ci + 1;
+        if (ci == nX + 1) { cttk = g.tc(cttk).East(); ci = 1; }
+    }
+    return true;
+}
+static void RedistributeGrid(const RunSet& rp, Grid& g, std::vector<RedistNode>& list, bool& refine) {  // :203-244
+    for (size_t q = 0; q < list.size(); ++q) {
+        double ex, dBt, psiold;
+        ExcessDeposition(rp, g.intermed0, g.intermed3, list[q].ttk, list[q].i, list[q].j, ex, dBt, psiold);
+        if (ex > EPS) {
+            if (!RedistributeCell(rp, g, list[q].ttk, list[q].i, list[q].j, ex)) { refine = true; break; }
+        }
+    }
+    list.clear();
+}
+
+// MorphodynamicTimeStepper, :532-781.
+static bool MorphodynamicTimeStepper(Sim& s, double& thisdt) {
+    RunSet& rp = s.rp;
+    Grid& g = s.g;
+    Tiles &im0 = g.intermed0, &im1 = g.intermed1, &im2 = g.intermed2, &im3 = g.intermed3;
+    int nX = rp.nXpertile, nY = rp.nYpertile;
+    bool refine = false;
+    double relhdiffmax = 0.0;
+    double psib = 1.0 - rp.p.BedPorosity;
+    auto update_wHnpsi = [&](Tiles& imk) {
+        for (int ttk : g.activeTiles) {
+            ComputeCellCentredTopographicData(rp, g, imk, ttk);
+            Tile &A = TL(im0, ttk), &K = TL(imk, ttk);
+            for (int i = 1; i <= nX; ++i)
+                for (int j = 1; j <= nY; ++j) {
+                    double gamold = Gam(rp, A.u.col(i, j)), gamnew = Gam(rp, K.u.col(i, j));
+                    double Hn_old = ComputeHn(A.u(iw, i, j), A.u(ib0, i, j), A.u(ibt, i, j), gamold);
+                    double db = K.u(ibt, i, j) - A.u(ibt, i, j);
+                    double w = -db / gamnew / gamnew;
+                    w = w + K.u(ibt, i, j);
+                    w = w + Hn_old * gamold / gamnew / gamnew;
+                    w = w + K.u(ib0, i, j);
+                    K.u(iw, i, j) = w;
+                    double Hnpsi_old = A.u(iHnpsi, i, j);
+                    double Hnpsi = -(psib)*db / gamnew;
+                    Hnpsi = Hnpsi + Hnpsi_old * gamold / gamnew;
+                    K.u(iHnpsi, i, j) = Hnpsi;
+                }
+            ComputeDesingularisedVariables(rp, imk, ttk, false);
+        }
+    };
+    CalculateMorphodynamicRHS(rp, g, im0);
+    for (int ttk : g.activeTiles) {
+        ApplySpongeLayer(rp, g, ttk, im0, true);
+        Tile &A = TL(im0, ttk), &B = TL(im1, ttk);
+        for (int i = 1; i <= nX + 1; ++i)
+            for (int j = 1; j <= nY + 1; ++j)
+                B.bt(i, j) = std::max(-rp.p.EroDepth, A.bt(i, j) + thisdt * A.ddtExplicitBt(i, j));
+    }
+    update_wHnpsi(im1);
+    CalculateMorphodynamicRHS(rp, g, im1);
+    for (int ttk : g.activeTiles) {
+        ApplySpongeLayer(rp, g, ttk, im1, true);
+        Tile &A = TL(im0, ttk), &B = TL(im1, ttk), &C = TL(im2, ttk);
+        for (int i = 1; i <= nX + 1; ++i)
+            for (int j = 1; j <= nY + 1; ++j)
+                C.bt(i, j) = std::max(-rp.p.EroDepth, 0.75 * A.bt(i, j) + 0.25 * (B.bt(i, j) + thisdt * B.ddtExplicitBt(i, j)));
+    }
+    update_wHnpsi(im2);
+    CalculateMorphodynamicRHS(rp, g, im2);
+    for (int ttk : g.activeTiles) {
+        ApplySpongeLayer(rp, g, ttk, im2, true);
+        Tile &A = TL(im0, ttk), &C = TL(im2, ttk), &D = TL(im3, ttk);
+        for (int i = 1; i <= nX + 1; ++i)
+            for (int j = 1; j <= nY + 1; ++j)
+                D.bt(i, j) = std::max(-rp.p.EroDepth, (1.0 / 3.0) * A.bt(i, j) + (2.0 / 3.0) * (C.bt(i, j) + thisdt * C.ddtExplicitBt(i, j)));
+    }
+    update_wHnpsi(im3);
+    std::vector<RedistNode> redist;
+    // The Fortran 'exit' statements below leave only the innermost (i) loop.
+    for (int ttk : g.activeTiles) {
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i) {
+                Tile &A = TL(im0, ttk), &D = TL(im3, ttk);
+                double gamold = Gam(rp, A.u.col(i, j)), gamnew = Gam(rp, D.u.col(i, j));
+                double Hn_old = ComputeHn(A.u(iw, i, j), A.u(ib0, i, j), A.u(ibt, i, j), gamold);
+                double Hn_new = ComputeHn(D.u(iw, i, j), D.u(ib0, i, j), D.u(ibt, i, j), gamnew);
+                double ex, dBt, psiold;
+                ExcessDeposition(rp, im0, im3, ttk, i, j, ex, dBt, psiold);
+                if (!refine && ex > EPS && dBt > EPS && psiold > -EPS) {
+                    if (Hn_old < rp.p.EroCriticalHeight || std::fabs(Hn_new - Hn_old) < rp.p.EroCriticalHeight) {
+                        AddToRedistList(redist, ttk, i, j, ex);
+                    } else {
+                        refine = true;
+                        break;
+                    }
+                    continue;
+                }
+                if (Hn_old < rp.p.EroCriticalHeight) continue;
+                double relhdiff = std::fabs(Hn_new - Hn_old) / std::fabs(Hn_old);
+                if (relhdiff > 0.1 && relhdiff > relhdiffmax) {
+                    relhdiffmax = relhdiff;
+                    refine = true;
+                    break;
+                }
+            }
+    }
+    if (!redist.empty() && !refine) RedistributeGrid(rp, g, redist, refine);
+    if (refine) {
+        thisdt = 0.5 * thisdt;
+        return true;
+    }
+    for (int ttk : g.activeTiles) ComputeInterfacialTopographicData(rp, g, im3, ttk);
+    return false;
+}
+
+// ---------------------------------------------------------------- activation, :924-1150
+static void NearBoundary(Sim& s, char dir) {
+    RunSet& rp = s.rp;
+    Grid& g = s.g;
+    int nX = rp.nXpertile, nY = rp.nYpertile;
+    int size0 = (int)g.activeTiles.size();  // Fortran evaluates the loop bound once
+    for (int tt = 0; tt < size0; ++tt) {
+        int ttk = g.activeTiles[(size_t)tt];
+        Tile& T = g.tc(ttk);
+        if (dir == 'N') {
+            int ttN = T.North();
+            if (ttN > 0 && !g.tc(ttN).TileOn) {
+                int64_t ydist = 0;
+                for (int ii = 1; ii <= nX; ++ii) {
+                    for (int jj = nY; jj >= 1; --jj)
+                        if (g.tc(ttk).u(iHn, ii, jj) > rp.heightThreshold) { ydist = jj; break; }
+                    if (ydist > (nY - rp.TileBuffer)) { AddTile(g, ttN, rp); break; }
+                }
+            }
+        } else if (dir == 'E') {
+            int ttE = T.East();
+            if (ttE > 0 && !g.tc(ttE).TileOn) {
+                int64_t xdist = 0;
+                for (int jj = 1; jj <= nY; ++jj) {
+                    for (int ii = nX; ii >= 1; --ii)
+                        if (g.tc(ttk).u(iHn, ii, jj) > rp.heightThreshold) { xdist = ii; break; }
+                    if (xdist > (nX - rp.TileBuffer)) { AddTile(g, ttE, rp); break; }
+                }
+            }
+        } else if (dir == 'S') {
+            int ttS = T.South();
+            if (ttS > 0 && !g.tc(ttS).TileOn) {
+                int64_t ydist = nY;
+                for (int ii = 1; ii <= nX; ++ii) {
+                    for (int jj = 1; jj <= nY; ++jj)
+                        if (g.tc(ttk).u(iHn, ii, jj) > rp.heightThreshold) { ydist = jj; break; }
+                    if (ydist <= rp.TileBuffer) { AddTile(g, ttS, rp); break; }
+                }
+            }
+        } else {
+            int ttW = T.West();
+            if (ttW > 0 && !g.tc(ttW).TileOn) {
+                int64_t xdist = nX;
+                for (int jj = 1; jj <= nY; ++jj) {
+                    for (int ii = 1; ii <= nX; ++ii)
+                        if (g.tc(ttk).u(iHn, ii, jj) > rp.heightThreshold) { xdist = ii; break; }
+                    if (xdist <= rp.TileBuffer) { AddTile(g, ttW, rp); break; }
+                }
+            }
+        }
+    }
+}
+static void CheckIfNearBoundaries(Sim& s) {
+    NearBoundary(s, 'N');
+    NearBoundary(s, 'S');
+    NearBoundary(s, 'E');
+    NearBoundary(s, 'W');
+}
+
+// NextFluxSeriesTime, :281-305.
+static double NextFluxSeriesTime(const RunSet& rp, double t) {
+    double nextT = HUGE_, tdiff = HUGE_;
+    for (const FluxSrc& S : rp.FluxSources)
+        for (int j = 0; j < S.nFluxSeries; ++j) {
+            double tmp = S.time[j] - t;
+            if (tmp > 0.0 && tmp < tdiff) { tdiff = tmp; nextT = S.time[j]; }
+        }
+    return nextT;
+}
+
+// One pass of IntegrateTo's outer loop body (:151-275).
+static void IntegrateStep(Sim& s, double tend) {
+    RunSet& rp = s.rp;
+    Grid& g = s.g;
+    CheckIfNearBoundaries(s);
+    InitialiseTimeSteppingArrays(g);
+    double adv = CalculateHydraulicRHS(rp, g, g.tileContainer, g.t, 1);
+    double tmax = std::min(tend, NextFluxSeriesTime(rp, g.t));
+    if (!rp.MorphodynamicsOn) adv = std::min(adv, tmax - g.t);
+    else adv = std::min(adv, 0.5 * (tmax - g.t));
+    g.dt = adv;
+    double dt_hydro = adv, nextT = 0.0;
+    g.t0 = g.t;
+    int guard = 0;
+    while (true) {
+        if (++guard > 100000 || !(dt_hydro > 0.0)) throw KoError(KG_ERR_DT, "time step collapsed");
+        CopySolutionData(rp, g, g.tileContainer, g.intermed0);
+        CopyMutableTopographicData(rp, g, g.tileContainer, g.intermed1);
+        CopyMutableTopographicData(rp, g, g.tileContainer, g.intermed2);
+        CopySolutionData(rp, g, g.tileContainer, g.intermed3);
+        if (HydraulicTimeStepper(s, dt_hydro, nextT)) { s.rejected++; continue; }
+        if (!rp.MorphodynamicsOn) break;
+        CopySolutionData(rp, g, g.intermed3, g.intermed0);
+        CopySolutionData(rp, g, g.intermed3, g.intermed1);
+        CopySolutionData(rp, g, g.intermed3, g.intermed2);
+        double dt_morpho = 2.0 * dt_hydro;
+        if (MorphodynamicTimeStepper(s, dt_morpho)) {
+            s.rejected++;
+            dt_hydro = 0.5 * dt_morpho;
+            g.dt = dt_hydro;
+            continue;
+        }
+        CopySolutionData(rp, g, g.intermed3, g.intermed0);
+        CopyMutableTopographicData(rp, g, g.intermed3, g.intermed1);
+        CopyMutableTopographicData(rp, g, g.intermed3, g.intermed2);
+        g.t = g.t + dt_hydro;
+        adv = CalculateHydraulicRHS(rp, g, g.intermed0, g.t, 1);
+        if (adv < dt_hydro) {
+            if ((dt_hydro - adv) / dt_hydro < 0.1) dt_hydro = 0.9 * dt_hydro;
+            else dt_hydro = adv;
+            g.dt = dt_hydro;
+            g.t = g.t0;
+            s.rejected++;
+            continue;
+        }
+        if (!HydraulicTimeStepper(s, dt_hydro, nextT)) break;
+        g.t = g.t0;
+        s.rejected++;
+    }
+    CopySolutionData(rp, g, g.intermed3, g.tileContainer);
+    int64_t ncells = (int64_t)g.activeTiles.size() * rp.nXpertile * rp.nYpertile;
+    if (!rp.MorphodynamicsOn) {
+        g.t = g.t0 + dt_hydro;
+        s.cell_updates += ncells;
+    } else {
+        g.t = g.t0 + 2.0 * dt_hydro;
+        s.cell_updates += 2 * ncells;
+    }
+    g.dt = dt_hydro;
+    s.steps++;
+}
+
+// ---------------------------------------------------------------- SetSources.f90 (2D)
+static void LoadSourceConditions(Sim& s) {
+    RunSet& rp = s.rp;
+    Grid& g = s.g;
+    const kg_params& P = rp.p;
+    for (auto& S : rp.FluxSources) S.NumCellsInSrc = 0;
+    double rhow = rp.rhow, rhos = rp.rhos;
+    for (int i = 1; i <= rp.nXtiles; ++i)
+        for (int j = 1; j <= rp.nYtiles; ++j) {
+            int k = TileID(g, i, j);
+            for (int ii = 1; ii <= rp.nXpertile; ++ii)
+                for (int jj = 1; jj <= rp.nYpertile; ++jj) {
+                    double x, y;
+                    GridToPhysical(rp, g, i, j, ii, jj, x, y);
+                    for (int kk = 0; kk < P.nCaps; ++kk) {
+                        const kg_cap& C = P.caps[kk];
+                        double rho = rhow + (rhos - rhow) * C.psi;
+                        double Hn = C.height;
+                        double R2 = (x - C.x) * (x - C.x) + (y - C.y) * (y - C.y);
+                        if (R2 <= C.radius * C.radius) {
+                            if (!g.tc(k).TileOn) AddTile(g, k, rp);
+                            Tile& T = g.tc(k);
+                            if (T.TileOn) {
+                                double gam = Gam(rp, T.u.col(ii, jj));
+                                double Hn_orig = T.u(iHn, ii, jj), rho_orig = T.u(irho, ii, jj);
+                                if (C.shape == KG_SHAPE_FLAT) {
+                                    T.u(iw, ii, jj) = T.u(iw, ii, jj) + C.height / gam;
+                                    T.u(iHn, ii, jj) = T.u(iHn, ii, jj) + C.height;
+                                    T.Hnmax(ii, jj, 1) = T.Hnmax(ii, jj, 1) + C.height;
+                                    T.u(irhoHnu, ii, jj) = T.u(irhoHnu, ii, jj) + rho * C.height * C.u;
+                                    T.u(irhoHnv, ii, jj) = T.u(irhoHnv, ii, jj) + rho * C.height * C.v;
+                                    T.u(iHnpsi, ii, jj) = T.u(iHnpsi, ii, jj) + C.psi * C.height;
+                                } else if (C.shape == KG_SHAPE_PARA) {
+                                    double f = C.height * (1.0 - R2 / C.radius / C.radius);
+                                    T.u(iw, ii, jj) = T.u(iw, ii, jj) + f / gam;
+                                    T.u(iHn, ii, jj) = T.u(iHn, ii, jj) + f;
+                                    T.Hnmax(ii, jj, 1) = T.Hnmax(ii, jj, 1) + f;
+                                    T.u(irhoHnu, ii, jj) = T.u(irhoHnu, ii, jj) + rho * C.height * C.u;
+                                    T.u(irhoHnv, ii, jj) = T.u(irhoHnv, ii, jj) + rho * C.height * C.v;
+                                    T.u(iHnpsi, ii, jj) = T.u(iHnpsi, ii, jj) + C.psi * C.height * (1.0 - R2 / C.radius / C.radius);
+                                } else {
+                                    double hp = C.height - T.u(ib0, ii, jj);
+                                    Hn = hp * gam;
+                                    if (Hn > 0.0) {
+                                        T.u(iw, ii, jj) = T.u(iw, ii, jj) + hp;
+                                        T.u(iHn, ii, jj) = T.u(iHn, ii, jj) + Hn;
+                                        T.Hnmax(ii, jj, 1) = T.Hnmax(ii, jj, 1) + Hn;
+                                        T.u(irhoHnu, ii, jj) = T.u(irhoHnu, ii, jj) + rho * Hn * C.u;
+                                        T.u(irhoHnv, ii, jj) = T.u(irhoHnv, ii, jj) + rho * Hn * C.v;
+                                        T.u(iHnpsi, ii, jj) = T.u(iHnpsi, ii, jj) + C.psi * Hn;
+                                    }
+                                }
+                                T.u(irho, ii, jj) = (rho_orig * Hn_orig + rho * Hn) / (Hn_orig + Hn);
+                            }
+                        }
+                    }
+                    for (int kk = 0; kk < P.nCubes; ++kk) {
+                        const kg_cube& C = P.cubes[kk];
+                        double rho = rhow + (rhos - rhow) * C.psi;
+                        double Hn = C.height;
+                        if ((std::fabs(x - C.x) <= 0.5 * C.length) && (std::fabs(y - C.y) <= 0.5 * C.width)) {
+                            if (!g.tc(k).TileOn) AddTile(g, k, rp);
+                            Tile& T = g.tc(k);
+                            if (T.TileOn) {
+                                double gam = Gam(rp, T.u.col(ii, jj));
+                                double Hn_orig = T.u(iHn, ii, jj), rho_orig = T.u(irho, ii, jj);
+                                if (C.shape == KG_SHAPE_LEVEL) {
+                                    double hp = C.height - T.u(ib0, ii, jj);
+                                    Hn = hp * gam;
+                                    if (Hn > 0.0) {
+                                        T.u(iw, ii, jj) = T.u(iw, ii, jj) + hp;
+                                        T.u(iHn, ii, jj) = T.u(iHn, ii, jj) + Hn;
+                                        T.Hnmax(ii, jj, 1) = T.Hnmax(ii, jj, 1) + Hn;
+                                        T.u(iHnpsi, ii, jj) = T.u(iHnpsi, ii, jj) + Hn * C.psi;
+                                        T.u(irhoHnu, ii, jj) = T.u(irhoHnu, ii, jj) + 0.0;
+                                        T.u(irhoHnv, ii, jj) = T.u(irhoHnv, ii, jj) + 0.0;
+                                    }
+                                } else {
+                                    T.u(iw, ii, jj) = T.u(iw, ii, jj) + C.height / gam;
+                                    T.u(iHn, ii, jj) = T.u(iHn, ii, jj) + C.height;
+                                    T.Hnmax(ii, jj, 1) = T.Hnmax(ii, jj, 1) + C.height;
+                                    T.u(irhoHnu, ii, jj) = T.u(irhoHnu, ii, jj) + 0.0;
+                                    T.u(irhoHnv, ii, jj) = T.u(irhoHnv, ii, jj) + 0.0;
+                                    T.u(iHnpsi, ii, jj) = T.u(iHnpsi, ii, jj) + C.psi * C.height;
+                                }
+                                T.u(irho, ii, jj) = (rho_orig * Hn_orig + rho * Hn) / (Hn_orig + Hn);
+                            }
+                        }
+                    }
+                    for (size_t kk = 0; kk < rp.FluxSources.size(); ++kk) {
+                        FluxSrc& S = rp.FluxSources[kk];
+                        double R2 = (x - S.x) * (x - S.x) + (y - S.y) * (y - S.y);
+                        if (R2 <= S.Radius * S.Radius) {
+                            if (!g.tc(k).TileOn) AddTile(g, k, rp);
+                            g.tc(k).containsSource = true;
+                            S.NumCellsInSrc = S.NumCellsInSrc + 1;
+                        }
+                    }
+                }
+        }
+    for (int ttk : std::vector<int>(g.ghostTiles)) ReconstructwAtEdges(rp, g, g.tileContainer, ttk);
+}
+
+// CalculateVolume, src/Output.f90:617-737: the four compensated sums times dx*dy.
+static void CalculateVolume(Sim& s, double out[4]) {
+    RunSet& rp = s.rp;
+    Grid& g = s.g;
+    double vol = 0, mass = 0, bed = 0, solids = 0, cv = 0, cm = 0, cb = 0, cs = 0;
+    for (int ttk : g.activeTiles) {
+        Tile& T = g.tc(ttk);
+        for (int j = 1; j <= rp.nYpertile; ++j)
+            for (int i = 1; i <= rp.nXpertile; ++i) {
+                double gam = Gam(rp, T.u.col(i, j));
+                double Hn = T.u(iHn, i, j), rho = T.u(irho, i, j);
+                double dv = (T.u(iw, i, j) - T.u(ib0, i, j) - T.u(ibt, i, j)) * gam * gam;
+                KahanAdd(dv, vol, cv);
+                KahanAdd(rho * Hn * gam, mass, cm);
+                KahanAdd(T.u(ibt, i, j), bed, cb);
+                KahanAdd(T.u(iHnpsi, i, j) * gam, solids, cs);
+            }
+    }
+    out[0] = vol * g.deltaX * g.deltaY;
+    out[1] = bed * g.deltaX * g.deltaY;
+    out[2] = mass * g.deltaX * g.deltaY;
+    out[3] = solids * g.deltaX * g.deltaY;
+}
+
+// Run settings derivation (src/DomainSettings.f90:185-225, src/Parameters.f90:629-648,
+// src/OutputSettings.f90:286).
+static void Setup(Sim& s, const kg_params& p) {
+    RunSet& rp = s.rp;
+    rp.p = p;
+    if (p.nXtiles < 1 || p.nYtiles < 1 || p.nXpertile < 2 || p.nYpertile < 2)
+        throw KoError(KG_ERR_PARAM, "tile counts/sizes must be positive (nX/nYpertile >= 2)");
+    if (p.nYtiles * p.nYpertile == 1) throw KoError(KG_ERR_UNSUPPORTED, "1D grids are not implemented");
+    rp.nXpertile = p.nXpertile; rp.nYpertile = p.nYpertile;
+    rp.nXtiles = p.nXtiles; rp.nYtiles = p.nYtiles; rp.nTiles = p.nXtiles * p.nYtiles;
+    rp.Xtilesize = p.Xtilesize; rp.Ytilesize = p.Ytilesize;
+    rp.xSize = rp.nXtiles * rp.Xtilesize;
+    rp.ySize = rp.nYtiles * rp.Ytilesize;
+    rp.deltaX = rp.Xtilesize / (double)rp.nXpertile;
+    rp.deltaY = rp.Ytilesize / (double)rp.nYpertile;
+    rp.deltaXRecip = 1.0 / rp.deltaX;
+    rp.deltaYRecip = 1.0 / rp.deltaY;
+    rp.geometric_factors = p.geometric_factors != 0;
+    rp.MorphodynamicsOn = p.MorphodynamicsOn != 0;
+    rp.bcs = p.bcs;
+    rp.SpongeLayer = (p.bcs == KG_BC_SPONGE);
+    rp.g = p.g; rp.rhow = p.rhow; rp.rhos = p.rhos;
+    const double visc_w = 1.2e-6;
+    rp.gred = (rp.rhos / rp.rhow - 1.0) * rp.g;
+    rp.Rep = std::sqrt(rp.g * p.SolidDiameter) * p.SolidDiameter / visc_w;
+    double R = std::pow(rp.gred / visc_w / visc_w, 1.0 / 3.0) * p.SolidDiameter;
+    if (p.ws0_given) rp.ws0 = p.ws0;
+    else rp.ws0 = visc_w / p.SolidDiameter * (std::sqrt(10.36 * 10.36 + 1.048 * R * R * R) - 10.36);
+    rp.nsettling = (4.7 + 0.41 * std::pow(rp.Rep, 0.75)) / (1.0 + 0.175 * std::pow(rp.Rep, 0.75));
+    rp.CriticalShields = 0.3 / (1.0 + 1.2 * R) + 0.055 * (1.0 - std::exp(-0.02 * R));
+    rp.diffusiveTimeScale = HUGE_;
+    if (p.EddyViscosity > 0.0)
+        rp.diffusiveTimeScale = std::min(rp.deltaX * rp.deltaX / p.EddyViscosity, rp.deltaY * rp.deltaY / p.EddyViscosity);
+    rp.heightThreshold = p.heightThreshold; rp.cfl = p.cfl; rp.maxdt = p.maxdt;
+    rp.tstart = p.tstart; rp.tend = p.tend; rp.TileBuffer = p.TileBuffer;
+    rp.Nout = p.Nout > 0 ? p.Nout : 100;
+    rp.DeltaT = (rp.tend - rp.tstart) / (double)rp.Nout;
+    rp.tan1deg = std::tan(PI / 180.0);
+    rp.FluxSources.clear();
+    for (int k = 0; k < p.nSources; ++k) {
+        const kg_flux_source& S = p.sources[k];
+        FluxSrc F;
+        F.x = S.x; F.y = S.y; F.Radius = S.radius; F.nFluxSeries = S.n_series;
+        F.time.assign(S.time, S.time + S.n_series);
+        F.flux.assign(S.flux, S.flux + S.n_series);
+        F.psi.assign(S.psi, S.psi + S.n_series);
+        rp.FluxSources.push_back(F);
+    }
+    // InitialiseGrid, src/Grid.f90:166-226.
+    Grid& g = s.g;
+    g.dim = 2;
+    g.xmin = HUGE_; g.xmax = -HUGE_; g.ymin = HUGE_; g.ymax = -HUGE_;
+    g.nTiles = rp.nTiles; g.nXtiles = rp.nXtiles; g.nYtiles = rp.nYtiles;
+    g.deltaX = rp.deltaX; g.deltaY = rp.deltaY; g.deltaXRecip = rp.deltaXRecip; g.deltaYRecip = rp.deltaYRecip;
+    g.Xtilesize = rp.Xtilesize; g.Ytilesize = rp.Ytilesize;
+    g.tileContainer.assign((size_t)g.nTiles, Tile());
+    g.intermed0.assign((size_t)g.nTiles, Tile());
+    g.intermed1.assign((size_t)g.nTiles, Tile());
+    g.intermed2.assign((size_t)g.nTiles, Tile());
+    g.intermed3.assign((size_t)g.nTiles, Tile());
+    g.t = 0.0;  // InitialiseGrid starts every run at t = 0 (tstart only offsets the output times)
+    g.dt = 1.0e-5;
+    g.nx1 = (int64_t)rp.nXtiles * rp.nXpertile + 1;
+    g.ny1 = (int64_t)rp.nYtiles * rp.nYpertile + 1;
+}
+
+}  // namespace ko
+
+// ---------------------------------------------------------------- C API
+using ko::Sim;
+struct ko_ctx { Sim s; };
+
+#define KO_TRY(ctx, body)                                     \
+    try {                                                     \
+        body;                                                 \
+        return KG_OK;                                         \
+    } catch (const ko::KoError& e) {                          \
+        if (ctx) (ctx)->s.err = e.what();                     \
+        return e.code;                                        \
+    } catch (const std::exception& e) {                       \
+        if (ctx) (ctx)->s.err = e.what();                     \
+        return KG_ERR_PARAM;                                  \
+    }
+
+static int find_active(ko_ctx* c, int id) {
+    if (!c || id < 1 || id > c->s.g.nTiles) return 0;
+    return ko::InVector(c->s.g.activeTiles, id) ? 1 : 0;
+}
+
+extern "C" {
+
+int ko_create(const kg_params* p, ko_ctx** out) {
+    ko_ctx* c = new ko_ctx();
+    try {
+        ko::Setup(c->s, *p);
+    } catch (const ko::KoError& e) {
+        int code = e.code;
+        delete c;
+        *out = nullptr;
+        return code;
+    }
+    *out = c;
+    return KG_OK;
+}
+void ko_destroy(ko_ctx* c) { delete c; }
+const char* ko_last_error(ko_ctx* c) { return c ? c->s.err.c_str() : "null context"; }
+
+int ko_upload_b0(ko_ctx* c, const double* b0, int64_t nx1, int64_t ny1) {
+    if (nx1 != c->s.g.nx1 || ny1 != c->s.g.ny1) { c->s.err = "b0 grid has the wrong shape"; return KG_ERR_PARAM; }
+    c->s.g.b0_upload.assign(b0, b0 + nx1 * ny1);
+    return KG_OK;
+}
+int ko_load_sources(ko_ctx* c) {
+    if (c->s.rp.p.topog == KG_TOPO_UPLOAD && c->s.g.b0_upload.empty()) { c->s.err = "no topography uploaded"; return KG_ERR_STATE; }
+    KO_TRY(c, { ko::LoadSourceConditions(c->s); c->s.sources_loaded = true; })
+}
+int ko_step(ko_ctx* c, double t_stop, kg_step_stats* st) {
+    int64_t r0 = c->s.rejected, s0 = c->s.steps, cu0 = c->s.cell_updates;
+    int rc;
+    try {
+        ko::IntegrateStep(c->s, t_stop);
+        rc = KG_OK;
+    } catch (const ko::KoError& e) {
+        c->s.err = e.what();
+        rc = e.code;
+    }
+    if (st) {
+        st->t = c->s.g.t; st->dt = c->s.g.dt;
+        st->steps = c->s.steps - s0; st->rejected = c->s.rejected - r0;
+        st->cell_updates = c->s.cell_updates - cu0;
+        st->n_active = (int32_t)c->s.g.activeTiles.size();
+        st->n_ghost = (int32_t)c->s.g.ghostTiles.size();
+        st->kernel_launches = 0;
+    }
+    return rc;
+}
+int ko_integrate_to(ko_ctx* c, double tend, kg_step_stats* st) {
+    int64_t r0 = c->s.rejected, s0 = c->s.steps, cu0 = c->s.cell_updates;
+    int rc = KG_OK;
+    if (tend > c->s.g.t) {
+        try {
+            while (true) {
+                ko::IntegrateStep(c->s, tend);
+                if (c->s.g.t >= tend) break;
+            }
+        } catch (const ko::KoError& e) {
+            c->s.err = e.what();
+            rc = e.code;
+        }
+    }
+    if (st) {
+        st->t = c->s.g.t; st->dt = c->s.g.dt;
+        st->steps = c->s.steps - s0; st->rejected = c->s.rejected - r0;
+        st->cell_updates = c->s.cell_updates - cu0;
+        st->n_active = (int32_t)c->s.g.activeTiles.size();
+        st->n_ghost = (int32_t)c->s.g.ghostTiles.size();
+        st->kernel_launches = 0;
+    }
+    return rc;
+}
+int ko_run(ko_ctx* c, kg_step_stats* st) {
+    kg_step_stats acc{};
+    for (int i = 1; i <= c->s.rp.Nout; ++i) {
+        double t = c->s.rp.tstart + i * c->s.rp.DeltaT;
+        kg_step_stats one{};
+        int rc = ko_integrate_to(c, t, &one);
+        acc.steps += one.steps; acc.rejected += one.rejected; acc.cell_updates += one.cell_updates;
+        if (rc != KG_OK) { if (st) *st = acc; return rc; }
+    }
+    acc.t = c->s.g.t; acc.dt = c->s.g.dt;
+    acc.n_active = (int32_t)c->s.g.activeTiles.size();
+    acc.n_ghost = (int32_t)c->s.g.ghostTiles.size();
+    if (st) *st = acc;
+    return KG_OK;
+}
+int ko_hydraulic_rhs(ko_ctx* c, double t, int32_t substep, double* adv) {
+    KO_TRY(c, {
+        ko::InitialiseTimeSteppingArrays(c->s.g);
+        *adv = ko::CalculateHydraulicRHS(c->s.rp, c->s.g, c->s.g.tileContainer, t, substep);
+    })
+}
+int ko_get_active_tiles(ko_ctx* c, int32_t* ids, int32_t* n) {
+    int cap = *n;
+    *n = (int32_t)c->s.g.activeTiles.size();
+    for (int i = 0; i < std::min(cap, *n); ++i) ids[i] = c->s.g.activeTiles[(size_t)i];
+    return KG_OK;
+}
+int ko_get_ghost_tiles(ko_ctx* c, int32_t* ids, int32_t* n) {
+    int cap = *n;
+    *n = (int32_t)c->s.g.ghostTiles.size();
+    for (int i = 0; i < std::min(cap, *n); ++i) ids[i] = c->s.g.ghostTiles[(size_t)i];
+    return KG_OK;
+}
+int ko_get_tile_field(ko_ctx* c, int32_t id, int32_t field, double* out) {
+    if (!find_active(c, id)) return KG_ERR_NOT_FOUND;
+    if (field < 1 || field > 13) return KG_ERR_PARAM;
+    ko::Tile& T = c->s.g.tc(id);
+    int nX = c->s.rp.nXpertile, nY = c->s.rp.nYpertile;
+    for (int j = 1; j <= nY; ++j)
+        for (int i = 1; i <= nX; ++i) out[(i - 1) + nX * (j - 1)] = T.u(field, i, j);
+    return KG_OK;
+}
+int ko_set_tile_field(ko_ctx* c, int32_t id, int32_t field, const double* in) {
+    if (!find_active(c, id)) return KG_ERR_NOT_FOUND;
+    if (field < 1 || field > 4) return KG_ERR_PARAM;
+    ko::Tile& T = c->s.g.tc(id);
+    int nX = c->s.rp.nXpertile, nY = c->s.rp.nYpertile;
+    for (int j = 1; j <= nY; ++j)
+        for (int i = 1; i <= nX; ++i) T.u(field, i, j) = in[(i - 1) + nX * (j - 1)];
+    return KG_OK;
+}
+int ko_get_tile_vertex(ko_ctx* c, int32_t id, int32_t which, double* out) {
+    if (!find_active(c, id)) return KG_ERR_NOT_FOUND;
+    ko::Tile& T = c->s.g.tc(id);
+    ko::A2& A = which == 0 ? T.b0 : T.bt;
+    int nX = c->s.rp.nXpertile, nY = c->s.rp.nYpertile;
+    for (int j = 1; j <= nY + 1; ++j)
+        for (int i = 1; i <= nX + 1; ++i) out[(i - 1) + (nX + 1) * (j - 1)] = A(i, j);
+    return KG_OK;
+}
+int ko_get_tile_rhs(ko_ctx* c, int32_t id, int32_t k, double* out) {
+    if (!find_active(c, id)) return KG_ERR_NOT_FOUND;
+    if (k < 1 || k > 5) return KG_ERR_PARAM;
+    ko::Tile& T = c->s.g.tc(id);
+    int nX = c->s.rp.nXpertile, nY = c->s.rp.nYpertile;
+    for (int j = 1; j <= nY; ++j)
+        for (int i = 1; i <= nX; ++i)
+            out[(i - 1) + nX * (j - 1)] = k <= 4 ? T.ddtExplicit(k, i, j) : T.ddtImplicit(2, i, j);
+    return KG_OK;
+}
+int ko_get_tile_maxima(ko_ctx* c, int32_t id, int32_t which, double* out) {
+    if (!find_active(c, id)) return KG_ERR_NOT_FOUND;
+    ko::Tile& T = c->s.g.tc(id);
+    int nX = c->s.rp.nXpertile, nY = c->s.rp.nYpertile;
+    if (which == 5) {
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i) out[(i - 1) + nX * (j - 1)] = T.tfirst(i, j);
+        return KG_OK;
+    }
+    ko::A3* A[5] = {&T.Hnmax, &T.umax, &T.emax, &T.dmax, &T.psimax};
+    if (which < 0 || which > 4) return KG_ERR_PARAM;
+    for (int pl = 1; pl <= 2; ++pl)
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i) out[(size_t)(pl - 1) * nX * nY + (i - 1) + nX * (j - 1)] = (*A[which])(i, j, pl);
+    return KG_OK;
+}
+int ko_volume(ko_ctx* c, double out[4]) {
+    ko::CalculateVolume(c->s, out);
+    return KG_OK;
+}
+int ko_get_time(ko_ctx* c, double* t, double* dt) {
+    *t = c->s.g.t;
+    *dt = c->s.g.dt;
+    return KG_OK;
+}
+// Wall-clock seconds spent in ko_integrate_to for the CPU baseline (steady_clock).
+double ko_timed_integrate(ko_ctx* c, double tend, kg_step_stats* st, int32_t* rc) {
+    auto t0 = std::chrono::steady_clock::now();
+    *rc = ko_integrate_to(c, tend, st);
+    auto t1 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+double ko_timed_steps(ko_ctx* c, int32_t nsteps, kg_step_stats* st, int32_t* rc) {
+    auto t0 = std::chrono::steady_clock::now();
+    kg_step_stats acc{};
+    *rc = KG_OK;
+    for (int i = 0; i < nsteps; ++i) {
+        kg_step_stats one{};
+        *rc = ko_step(c, c->s.rp.tend, &one);
+        acc.steps += one.steps; acc.rejected += one.rejected; acc.cell_updates += one.cell_updates;
+        if (*rc != KG_OK || c->s.g.t >= c->s.rp.tend) break;
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    acc.t = c->s.g.t; acc.dt = c->s.g.dt;
+    acc.n_active = (int32_t)c->s.g.activeTiles.size();
+    acc.n_ghost = (int32_t)c->s.g.ghostTiles.size();
+    if (st) *st = acc;
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
+}  // extern "C"
