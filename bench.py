@@ -1,0 +1,299 @@
+"""Benchmark: cell-updates/s of the time-step hot path on one GB300.
+
+A step is one accepted time step of IntegrateTo (the fused hydraulic passes plus the
+activation check) over the whole active domain.  One cell-update is one active cell
+advanced by one accepted hydraulic dt (a morphodynamic Strang step counts 2).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+- value:   device-timed throughput (CUDA events on the library's stream around each
+           step; L2 flushed by a 256 MiB write between timed steps, outside the timed
+           intervals).
+- e2e:     the same metric through the public C ABI from host inputs to host outputs:
+           kg_create + kg_load_sources (inputs copied from host) + K steps (each returns
+           its statistics to the host) + reading the conserved fields of every active tile
+           back to host memory, timed on the host clock.
+- roofline: the fused hydraulic pass; algorithmic bytes per cell-update (FP64 hydraulic
+           step: 368 B over its 4 passes) over the measured pass time, against the
+           measured HBM copy bandwidth.
+- cpu_baseline: the CPU oracle (a serial C++ restatement of the reference; the Fortran
+           reference cannot be built here) on a bounded sample of the same workload.
+Under torchrun (N > 1) each rank advances an independent replica (replicas only).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG_BYTES = {"fp64_hydro": 368.0, "fp64_morpho": 512.0, "fp32_hydro": 252.0, "fp32_morpho": 366.0}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str, workload: str):
+    """dram bytes per pass from a committed ncu summary (profiles/<kernel>_<workload>.md)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"dram_bytes_per_pass:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+
+        def rd():
+            for line in self.proc.stdout:
+                self.samples.append([x.strip() for x in line.split(",")])
+
+        self.thread = threading.Thread(target=rd, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx = float(s[1])
+                for n, v in zip(names, s[2:6]):
+                    if v.lower() in ("active", "1", "yes"):
+                        reasons.add(n)
+            except Exception:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(params, seconds=15.0, max_steps=100000):
+    """Oracle timed on a bounded sample: accepted steps from t = 0 until ~`seconds`."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle
+    from kestrel_gb300 import abi
+    L = _oracle.load()
+    sim = _oracle.simulation(params)
+    total_cu, total_s, steps = 0, 0.0, 0
+    rc = C.c_int32(0)
+    while total_s < seconds and steps < max_steps:
+        st = abi.StepStats()
+        dt = L.ko_timed_steps(sim.h, 1, C.byref(st), C.byref(rc))
+        if rc.value != 0:
+            break
+        total_cu += st.cell_updates
+        total_s += dt
+        steps += st.steps
+        if sim.time[0] >= params.tend:
+            break
+    return {"value": total_cu / total_s if total_s > 0 else None, "unit": "cell-updates/s", "cores": 1,
+            "kind": "port", "sample": f"first {steps} accepted steps from t=0 (t_end {sim.time[0]:.3f} s), "
+            f"{total_cu} cell-updates in {total_s:.2f} s, serial C++ restatement (oracle)"}
+
+
+def run_reference(args, wl):
+    from kestrel_gb300 import abi  # noqa: F401
+    p = wl["params"]()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle
+    L = _oracle.load()
+    sim = _oracle.simulation(p)
+    rc = C.c_int32(0)
+    from kestrel_gb300 import abi as A
+    for _ in range(args.warmup):
+        st = A.StepStats()
+        L.ko_timed_steps(sim.h, 1, C.byref(st), C.byref(rc))
+    cu, secs, n = 0, 0.0, 0
+    for _ in range(args.steps):
+        st = A.StepStats()
+        secs += L.ko_timed_steps(sim.h, 1, C.byref(st), C.byref(rc))
+        cu += st.cell_updates
+        n += st.steps
+    v = cu / secs if secs > 0 else None
+    line = {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(n, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "desc": wl["desc"], "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                             "sample": f"{n} accepted steps after {args.warmup} warm-up steps, serial C++ restatement"},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cap_release_256_fp64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    from kestrel_gb300 import workloads
+    wl = workloads.WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, wl)
+        return
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from kestrel_gb300 import abi, lib
+    L = lib.load()
+    p = wl["params"]()
+
+    # ---- device-timed throughput ----
+    sim = lib.simulation(p, precision=wl["prec"])
+    stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    for _ in range(args.warmup):
+        sim.step(p.tend)
+    torch.cuda.synchronize()
+    L.kg_set_kernel_timing(sim.h, 1)
+    launches0 = L.kg_kernel_launches(sim.h)
+    clocks = ClockSampler(local)
+    if rank == 0:
+        clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    total_ms, cu, nsteps = 0.0, 0, 0
+    evs = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        st = sim.step(p.tend)
+        e1.record(stream)
+        evs.append((e0, e1))
+        cu += st.cell_updates
+        nsteps += st.steps
+        if sim.time[0] >= p.tend:
+            break
+    torch.cuda.synchronize()
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    if dist:
+        dist.barrier()
+    clk = clocks.stop() if rank == 0 else None
+    launches = L.kg_kernel_launches(sim.h) - launches0
+    kms, kpasses = C.c_double(), C.c_int64()
+    L.kg_get_kernel_time(sim.h, C.byref(kms), C.byref(kpasses))
+    t_s = total_ms / 1e3
+    if dist:
+        tt = torch.tensor([t_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_s = float(tt.item())
+        cc = torch.tensor([float(cu)], device="cuda")
+        dist.all_reduce(cc)
+        cu_all = float(cc.item())
+    else:
+        cu_all = float(cu)
+    value = cu_all / t_s
+    active_cells = len(sim.active_tiles()) * p.nXpertile * p.nYpertile
+    sim.close()
+
+    # ---- end to end through the C ABI ----
+    t0 = time.perf_counter()
+    sim2 = lib.simulation(p, precision=wl["prec"])
+    cu2, n2 = 0, 0
+    for _ in range(args.warmup + args.steps):
+        st = sim2.step(p.tend)
+        cu2 += st.cell_updates
+        n2 += st.steps
+        if sim2.time[0] >= p.tend:
+            break
+    d2h = 0
+    for t in sim2.active_tiles():
+        for f in (1, 2, 3, 4):
+            d2h += sim2.field(t, f).nbytes
+    e2e_s = time.perf_counter() - t0
+    h2d = C.sizeof(abi.Params) + 16 * 4 * n2
+    d2h += 16 * 4 * n2
+    sim2.close()
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    key = "fp64_hydro" if wl["prec"] == abi.PREC_FP64 else "fp32_hydro"
+    if p.MorphodynamicsOn:
+        key = key.replace("hydro", "morpho")
+    alg = ALG_BYTES[key]
+    pass_ms = kms.value / max(kpasses.value, 1)
+    # algorithmic bytes per pass: the per-cell-update figure over the 4 passes of a step
+    alg_pass = alg / 4.0 * (cu / max(nsteps, 1))
+    achieved = alg_pass / (pass_ms / 1e3) / 1e9 if pass_ms > 0 else None
+    peak, peak_kind = measured_peaks()
+    traffic = profile_traffic("k_hydro", args.workload)
+    line = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": nsteps,
+        "warmup": args.warmup, "ms_per_step": total_ms / max(nsteps, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if wl["prec"] == abi.PREC_FP64 else "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "desc": wl["desc"], "active_cells_end": active_cells,
+                   "l2": "flushed (256 MiB write) between timed steps, outside the timed intervals",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": cu2 / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / max(n2, 1),
+                "d2h_bytes_per_step": d2h / max(n2, 1)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "k_hydro", "pass_ms": pass_ms},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(p)
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

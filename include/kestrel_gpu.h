@@ -209,6 +209,15 @@ int  kg_volume(kg_ctx* ctx, double out[4]);
 int  kg_get_time(kg_ctx* ctx, double* t, double* dt);
 int64_t kg_kernel_launches(const kg_ctx* ctx);
 
+/* The cudaStream_t the context launches on, so a caller can order (or time) its own work
+   against the library's.  No reference counterpart (the reference has no device). */
+void* kg_stream(kg_ctx* ctx);
+/* When enabled, every fused hydraulic pass is bracketed by CUDA events on the context's
+   stream; kg_get_kernel_time returns the accumulated pass duration in ms and the count.
+   No reference counterpart. */
+int  kg_set_kernel_timing(kg_ctx* ctx, int32_t enable);
+int  kg_get_kernel_time(kg_ctx* ctx, double* ms, int64_t* passes);
+
 #ifdef __cplusplus
 }
 #endif

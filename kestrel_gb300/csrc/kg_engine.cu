@@ -1,0 +1,1224 @@
+// kg_engine.cu -- host engine and C ABI (include/kestrel_gpu.h).
+//
+// The context owns a pool of tile "slots" in HBM (layout in kg_engine.cuh), the reference's
+// tile bookkeeping (active list kept sorted, ghost list in append order, per-tile
+// neighbour IDs; src/Grid.f90, src/UpdateTiles.f90) and one CUDA stream.  Per accepted
+// step it launches the activation-flag kernel, then the fused hydraulic passes
+// (kg_hydro.cu) with the CFL minimum read back after each pass to take the reference's
+// accept / refine decisions (src/TimeStepper.f90:151-275).  Tile activation, which in the
+// reference mutates the active list while iterating over it, runs on the host from the
+// device flags, launching the per-tile set-up kernels (kg_tiles.cu) in the reference's
+// order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "kg_engine.cuh"
+
+namespace kg {
+// kg_hydro.cu
+size_t hydro_smem_bytes();
+cudaError_t set_constants(const DevParams& p, const DevSource* src, int nsrc, cudaStream_t st);
+cudaError_t launch_hydro(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st);
+// kg_tiles.cu
+cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, cudaStream_t st);
+cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, cudaStream_t st);
+cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, cudaStream_t st);
+cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, cudaStream_t st);
+cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, double u, double v, double psi, cudaStream_t st);
+cudaError_t launch_ghost_edges(const DevArrays& A, int slot, int mask, int qcur, cudaStream_t st);
+cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, cudaStream_t st);
+cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st);
+cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, const double* hn_over, int* d_flags,
+                             cudaStream_t st);
+cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, const double* hn, const double* rho,
+                          double* d_out, cudaStream_t st);
+}  // namespace kg
+
+using namespace kg;
+
+namespace {
+
+constexpr double HUGE_D = std::numeric_limits<double>::max();
+constexpr double PI_D = 3.141592653589793238462643383279502884;
+
+struct KgError : std::runtime_error {
+    int code;
+    KgError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            throw KgError(KG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct TileMeta {
+    int slot = -1;
+    bool on = false, ghost = false, src = false, maxima = false;
+    int nb[4] = {0, 0, 0, 0};   // W, E, N, S tile IDs
+    int cor[4] = {0, 0, 0, 0};  // SW, SE, NW, NE
+};
+
+struct HostSource {
+    double x, y, R;
+    int n, ncells;
+    std::vector<double> time, flux, psi;
+};
+
+}  // namespace
+
+struct kg_ctx {
+    kg_params p{};
+    int prec = KG_PREC_FP64;
+    DevParams dp{};
+    int nX = 0, nY = 0, nXt = 0, nYt = 0, nTiles = 0, SC = 0, SV = 0, SFX = 0, SFY = 0, nE = 0;
+    double xSize = 0, ySize = 0, DeltaT = 0;
+    std::vector<TileMeta> tiles;         // index = tile ID - 1
+    std::vector<int> active, ghost;      // tile IDs
+    std::vector<HostSource> srcs;
+    // per-slot host mirrors of the static bed: vertex b0 and face b0 (X, Y)
+    std::vector<std::vector<double>> hb0, hfx0, hfy0;
+    std::vector<int> slot_tile;
+    DevArrays A{};
+    int cap = 0, nslots = 0;
+    std::vector<BlockDesc> blocks;
+    BlockDesc* d_blocks = nullptr;
+    int d_blocks_cap = 0;
+    int* d_list = nullptr;               // scratch slot list
+    int d_list_cap = 0;
+    int* d_flags = nullptr;
+    unsigned long long* d_cfl = nullptr;
+    double* d_vol = nullptr;
+    unsigned long long* h_cfl = nullptr; // pinned
+    double* d_srcHn = nullptr;           // depth/density the sources set (valid until the first step)
+    double* d_srcRho = nullptr;
+    bool src_override = false;
+    std::vector<double> upload;          // global vertex grid (KG_TOPO_UPLOAD)
+    int64_t nx1 = 0, ny1 = 0;
+    bool sources_loaded = false;
+    int qcur = 0;
+    double t = 0.0, dt = 1.0e-5, t0 = 0.0;
+    int64_t launches = 0, steps = 0, rejected = 0, cell_updates = 0;
+    bool blocks_dirty = true;
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double kernel_ms = 0.0;
+    int64_t timed_passes = 0;
+    cudaStream_t st = nullptr;
+    std::string err;
+};
+
+namespace {
+
+size_t bytes_per_slot(const kg_ctx& c) {
+    size_t SC = c.SC;
+    return sizeof(double) * (4 * 4 * SC + 4 * SC + SC + 2 * SC + 4 * SC + 5 * (size_t)c.SFX + 5 * (size_t)c.SFY +
+                             2 * (size_t)c.SV + 9 * SC + GE_COUNT * (size_t)c.nE + 11 * SC + 2 * SC) +
+           8 * sizeof(int) + 2 + sizeof(int);
+}
+
+template <class T>
+void grow_array(T*& ptr, size_t old_n, size_t new_n, cudaStream_t st) {
+    T* np = nullptr;
+    CK(cudaMalloc(&np, new_n * sizeof(T)));
+    CK(cudaMemsetAsync(np, 0, new_n * sizeof(T), st));
+    if (ptr && old_n) CK(cudaMemcpyAsync(np, ptr, old_n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    if (ptr) {
+        CK(cudaStreamSynchronize(st));
+        CK(cudaFree(ptr));
+    }
+    ptr = np;
+}
+
+void ensure_cap(kg_ctx& c, int need) {
+    if (need <= c.cap) return;
+    int nc = std::max(need, std::max(16, c.cap * 2));
+    nc = std::min(nc, std::max(need, c.nTiles));
+    size_t o = c.cap, n = nc, SC = c.SC;
+    for (int b = 0; b < 4; ++b) grow_array(c.A.Q[b], o * 4 * SC, n * 4 * SC, c.st);
+    grow_array(c.A.E0, o * 4 * SC, n * 4 * SC, c.st);
+    grow_array(c.A.I0, o * SC, n * SC, c.st);
+    grow_array(c.A.UV, o * 2 * SC, n * 2 * SC, c.st);
+    grow_array(c.A.CT, o * 4 * SC, n * 4 * SC, c.st);
+    grow_array(c.A.FX, o * 5 * (size_t)c.SFX, n * 5 * (size_t)c.SFX, c.st);
+    grow_array(c.A.FY, o * 5 * (size_t)c.SFY, n * 5 * (size_t)c.SFY, c.st);
+    grow_array(c.A.BV, o * 2 * (size_t)c.SV, n * 2 * (size_t)c.SV, c.st);
+    grow_array(c.A.G9, o * 9 * SC, n * 9 * SC, c.st);
+    grow_array(c.A.GE, o * GE_COUNT * (size_t)c.nE, n * GE_COUNT * (size_t)c.nE, c.st);
+    grow_array(c.A.MX, o * 11 * SC, n * 11 * SC, c.st);
+    grow_array(c.A.nbr, o * 8, n * 8, c.st);
+    grow_array(c.A.kind, o, n, c.st);
+    grow_array(c.A.has_source, o, n, c.st);
+    grow_array(c.A.tile_of_slot, o, n, c.st);
+    grow_array(c.d_srcHn, o * SC, n * SC, c.st);
+    grow_array(c.d_srcRho, o * SC, n * SC, c.st);
+    c.cap = nc;
+    c.A.cap = nc;
+    c.hb0.resize(nc);
+    c.hfx0.resize(nc);
+    c.hfy0.resize(nc);
+    c.slot_tile.resize(nc, 0);
+}
+
+void ensure_list(kg_ctx& c, size_t n) {
+    if ((int)n <= c.d_list_cap) return;
+    int nc = std::max<int>((int)n, std::max(64, c.d_list_cap * 2));
+    if (c.d_list) CK(cudaFree(c.d_list));
+    if (c.d_flags) CK(cudaFree(c.d_flags));
+    CK(cudaMalloc(&c.d_list, nc * sizeof(int)));
+    CK(cudaMalloc(&c.d_flags, nc * sizeof(int)));
+    c.d_list_cap = nc;
+}
+
+void upload_list(kg_ctx& c, const std::vector<int>& slots) {
+    ensure_list(c, slots.size());
+    if (!slots.empty())
+        CK(cudaMemcpyAsync(c.d_list, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+}
+
+void sync(kg_ctx& c) { CK(cudaStreamSynchronize(c.st)); }
+
+// ---------------------------------------------------------------- grid navigation
+// src/Grid.f90:245-353
+int tile_col(const kg_ctx& c, int id) { return (id - 1) % c.nXt + 1; }
+int tile_row(const kg_ctx& c, int id) { return (id - 1) / c.nXt + 1; }
+int tile_id(const kg_ctx& c, int gi, int gj) { return gi + (gj - 1) * c.nXt; }
+bool in_bounds(const kg_ctx& c, int id) { return !(id < 1 || id > c.nTiles); }
+bool on_edge(const kg_ctx& c, int id) {
+    int i = tile_col(c, id), j = tile_row(c, id);
+    bool on = (i == 1 || i == c.nXt);
+    return on || (c.nYt > 1 && (j == 1 || j == c.nYt));
+}
+TileMeta& T(kg_ctx& c, int id) { return c.tiles[(size_t)id - 1]; }
+double cell_x(const kg_ctx& c, int gi, int ii) { return -0.5 * c.xSize + c.dp.dx * ((gi - 1.0) * c.nX + (ii - 0.5)); }
+double cell_y(const kg_ctx& c, int gj, int jj) { return -0.5 * c.ySize + c.dp.dy * ((gj - 1.0) * c.nY + (jj - 0.5)); }
+
+// SetTileBoundaries / SetPeriodicBoundaryConds, src/UpdateTiles.f90:487-566.
+void set_tile_boundaries(kg_ctx& c, int k) {
+    TileMeta& m = T(c, k);
+    int N = k + c.nXt, S = k - c.nXt;
+    m.nb[0] = k - 1; m.nb[1] = k + 1; m.nb[2] = N; m.nb[3] = S;
+    m.cor[0] = S - 1; m.cor[1] = S + 1; m.cor[2] = N - 1; m.cor[3] = N + 1;
+    if (c.p.bcs == KG_BC_PERIODIC) {
+        int gi = tile_col(c, k), gj = tile_row(c, k);
+        if (gi == 1) {
+            m.nb[0] = tile_id(c, c.nXt, gj);
+            if (gj > 1 && gj < c.nYt) { m.cor[0] = tile_id(c, c.nXt, gj - 1); m.cor[2] = tile_id(c, c.nXt, gj + 1); }
+            else if (gj == 1) { m.cor[0] = tile_id(c, c.nXt, c.nYt); m.cor[2] = tile_id(c, c.nXt, gj + 1); }
+            else if (gj == c.nYt) { m.cor[0] = tile_id(c, c.nXt, gj - 1); m.cor[2] = tile_id(c, c.nXt, 1); }
+        }
+        if (gi == c.nXt) {
+            m.nb[1] = tile_id(c, 1, gj);
+            if (gj > 1 && gj < c.nYt) { m.cor[1] = tile_id(c, 1, gj - 1); m.cor[3] = tile_id(c, 1, gj + 1); }
+            else if (gj == 1) { m.cor[1] = tile_id(c, 1, c.nYt); m.cor[3] = tile_id(c, 1, gj + 1); }
+            else if (gj == c.nYt) { m.cor[1] = tile_id(c, 1, gj - 1); m.cor[3] = tile_id(c, 1, 1); }
+        }
+        if (gj == 1) m.nb[3] = tile_id(c, gi, c.nYt);
+        if (gj == c.nYt) m.nb[2] = tile_id(c, gi, 1);
+    }
+}
+
+// Neighbour slot table entries of one tile (refreshed whenever a neighbour gets a slot).
+void push_nbr(kg_ctx& c, int id) {
+    TileMeta& m = T(c, id);
+    if (m.slot < 0) return;
+    int v[8];
+    const int order[8] = {m.nb[0], m.nb[1], m.nb[2], m.nb[3], m.cor[0], m.cor[1], m.cor[2], m.cor[3]};
+    for (int q = 0; q < 8; ++q) v[q] = in_bounds(c, order[q]) ? T(c, order[q]).slot : -1;
+    CK(cudaMemcpyAsync(c.A.nbr + (size_t)m.slot * 8, v, sizeof(v), cudaMemcpyHostToDevice, c.st));
+    sync(c);
+}
+void refresh_nbrs_around(kg_ctx& c, int id) {
+    push_nbr(c, id);
+    TileMeta& m = T(c, id);
+    for (int q = 0; q < 4; ++q)
+        if (in_bounds(c, m.nb[q])) push_nbr(c, m.nb[q]);
+    for (int q = 0; q < 4; ++q)
+        if (in_bounds(c, m.cor[q])) push_nbr(c, m.cor[q]);
+    // tiles that list this tile as a neighbour's neighbour (corner relations) are covered
+    // by refreshing all slots lazily before each step.
+}
+void refresh_all_nbrs(kg_ctx& c) {
+    std::vector<int> v((size_t)c.nslots * 8, -1);
+    for (int s = 0; s < c.nslots; ++s) {
+        int id = c.slot_tile[s];
+        if (id <= 0) continue;
+        TileMeta& m = T(c, id);
+        const int order[8] = {m.nb[0], m.nb[1], m.nb[2], m.nb[3], m.cor[0], m.cor[1], m.cor[2], m.cor[3]};
+        for (int q = 0; q < 8; ++q) v[(size_t)s * 8 + q] = in_bounds(c, order[q]) ? T(c, order[q]).slot : -1;
+    }
+    if (!v.empty()) CK(cudaMemcpyAsync(c.A.nbr, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+    sync(c);
+}
+
+int assign_slot(kg_ctx& c, int id) {
+    TileMeta& m = T(c, id);
+    if (m.slot >= 0) return m.slot;
+    ensure_cap(c, c.nslots + 1);
+    int s = c.nslots++;
+    m.slot = s;
+    c.slot_tile[s] = id;
+    int8_t z = SLOT_FREE;
+    CK(cudaMemcpyAsync(c.A.kind + s, &z, 1, cudaMemcpyHostToDevice, c.st));
+    CK(cudaMemcpyAsync(c.A.tile_of_slot + s, &id, sizeof(int), cudaMemcpyHostToDevice, c.st));
+    sync(c);
+    return s;
+}
+void set_kind(kg_ctx& c, int id, int8_t k) {
+    CK(cudaMemcpyAsync(c.A.kind + T(c, id).slot, &k, 1, cudaMemcpyHostToDevice, c.st));
+    sync(c);
+}
+
+// ---------------------------------------------------------------- bed set-up
+// GetHeights (src/dem.f90:360-391) with the analytic surfaces of src/TopogFuncs.f90 or the
+// uploaded vertex grid, evaluated at the vertex coordinates AllocateTopographicData builds
+// (src/UpdateTiles.f90:271-337).
+double topo_value(const kg_ctx& c, int id, int a, int b, double X, double Y) {
+    const double* P = c.p.topog_params;
+    switch (c.p.topog) {
+        case KG_TOPO_FLAT: return 0.0;
+        case KG_TOPO_XSLOPE: return P[0] * X;
+        case KG_TOPO_YSLOPE: return P[0] * Y;
+        case KG_TOPO_XYSLOPE: return P[0] * X + P[1] * Y;
+        case KG_TOPO_XSINSLOPE: {
+            double Lx = c.p.Xtilesize * c.nXt;
+            double k = 2.0 * PI_D / Lx;
+            return P[0] * std::sin(X * k);
+        }
+        case KG_TOPO_XYSINSLOPE: {
+            double Lx = c.p.Xtilesize * c.nXt, Ly = c.p.Ytilesize * c.nYt;
+            double kx = 2.0 * PI_D / Lx, ky = 2.0 * PI_D / Ly;
+            return P[0] * std::sin(X * kx) * std::sin(Y * ky);
+        }
+        case KG_TOPO_XHUMP: return ((X > -P[1]) && (X < P[1])) ? 0.5 * P[0] * (1.0 + std::cos(PI_D * X / P[1])) : 0.0;
+        case KG_TOPO_XTANH: return P[1] * (1.0 + std::tanh((X - P[0]) / P[2]));
+        case KG_TOPO_XPARAB: return P[0] * X * X;
+        case KG_TOPO_XYPARAB: return P[0] * X * X + P[1] * Y * Y;
+        default: {
+            int gi = tile_col(c, id), gj = tile_row(c, id);
+            int64_t vx = (int64_t)(gi - 1) * c.nX + a, vy = (int64_t)(gj - 1) * c.nY + b;
+            return c.upload[(size_t)(vx + c.nx1 * vy)];
+        }
+    }
+}
+void get_heights(kg_ctx& c, int id) {
+    int s = T(c, id).slot, nX = c.nX, nY = c.nY, gi = tile_col(c, id), gj = tile_row(c, id);
+    std::vector<double> xv(nX + 1), yv(nY + 1);
+    for (int ii = 1; ii <= nX; ++ii) xv[ii - 1] = cell_x(c, gi, ii) - 0.5 * c.dp.dx;
+    xv[nX] = cell_x(c, gi, nX) + 0.5 * c.dp.dx;
+    for (int jj = 1; jj <= nY; ++jj) yv[jj - 1] = cell_y(c, gj, jj) - 0.5 * c.dp.dy;
+    yv[nY] = cell_y(c, gj, nY) + 0.5 * c.dp.dy;
+    std::vector<double>& b0 = c.hb0[s];
+    b0.assign((size_t)c.SV, 0.0);
+    for (int b = 0; b <= nY; ++b)
+        for (int a = 0; a <= nX; ++a) b0[(size_t)b * (nX + 1) + a] = topo_value(c, id, a, b, xv[a], yv[b]);
+    c.hfx0[s].assign((size_t)c.SFX, 0.0);
+    c.hfy0[s].assign((size_t)c.SFY, 0.0);
+    for (int j = 0; j < nY; ++j)
+        for (int a = 0; a <= nX; ++a)
+            c.hfx0[s][(size_t)j * (nX + 1) + a] = 0.5 * (b0[(size_t)j * (nX + 1) + a] + b0[(size_t)(j + 1) * (nX + 1) + a]);
+    for (int a = 0; a <= nY; ++a)
+        for (int i = 0; i < nX; ++i)
+            c.hfy0[s][(size_t)a * nX + i] = 0.5 * (b0[(size_t)a * (nX + 1) + i] + b0[(size_t)a * (nX + 1) + i + 1]);
+}
+void push_bed(kg_ctx& c, int s) {
+    CK(cudaMemcpyAsync(c.A.BV + (size_t)s * 2 * c.SV, c.hb0[s].data(), (size_t)c.SV * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    CK(cudaMemcpyAsync(c.A.FX + (size_t)s * 5 * c.SFX, c.hfx0[s].data(), (size_t)c.SFX * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    CK(cudaMemcpyAsync(c.A.FY + (size_t)s * 5 * c.SFY, c.hfy0[s].data(), (size_t)c.SFY * sizeof(double), cudaMemcpyHostToDevice, c.st));
+}
+// ComputeCellCentredTopographicData for a tile after its vertex b0 changed; InterpolateB
+// is recomputed with it since the reference evaluates that from the vertices on use.
+void cell_topo(kg_ctx& c, int id) {
+    int s = T(c, id).slot;
+    push_bed(c, s);
+    std::vector<int> one{s};
+    upload_list(c, one);
+    CK(launch_cell_topo(c.A, c.d_list, 1, c.st));
+    CK(launch_face_bI(c.A, c.d_list, 1, c.st));
+    c.launches += 2;
+    sync(c);
+}
+bool in_list(const std::vector<int>& v, int x) { return std::find(v.begin(), v.end(), x) != v.end(); }
+bool is_active_ghost(kg_ctx& c, int id) { return in_list(c.ghost, id) && T(c, id).ghost; }
+
+// EqualiseTopographicBoundaryData, src/MorphodynamicRHS.f90:588-687 (vertex and face b0).
+void equalise(kg_ctx& c, int id) {
+    int nX = c.nX, nY = c.nY, V = nX + 1;
+    auto ok = [&](int t) { return in_bounds(c, t) && (in_list(c.active, t) || is_active_ghost(c, t)); };
+    auto B0 = [&](int t) -> std::vector<double>& { return c.hb0[T(c, t).slot]; };
+    auto FX0 = [&](int t) -> std::vector<double>& { return c.hfx0[T(c, t).slot]; };
+    auto FY0 = [&](int t) -> std::vector<double>& { return c.hfy0[T(c, t).slot]; };
+    bool sw_up = false, ne_up = false;
+    int tW = T(c, id).nb[0];
+    if (ok(tW)) {
+        for (int j = 0; j < nY; ++j) {
+            B0(tW)[(size_t)j * V + nX] = B0(id)[(size_t)j * V + 0];
+            FX0(tW)[(size_t)j * V + nX] = FX0(id)[(size_t)j * V + 0];
+        }
+        cell_topo(c, tW);
+        int tSW = T(c, tW).nb[3];
+        if (ok(tSW)) {
+            B0(tSW)[(size_t)nY * V + nX] = B0(id)[0];
+            sw_up = true;
+            cell_topo(c, tSW);
+        }
+    }
+    int tE = T(c, id).nb[1];
+    if (ok(tE)) {
+        for (int j = 0; j < nY; ++j) {
+            B0(id)[(size_t)j * V + nX] = B0(tE)[(size_t)j * V + 0];
+            FX0(id)[(size_t)j * V + nX] = FX0(tE)[(size_t)j * V + 0];
+        }
+        int tNE = T(c, tE).nb[2];
+        if (ok(tNE)) {
+            B0(id)[(size_t)nY * V + nX] = B0(tNE)[0];
+            ne_up = true;
+        }
+        cell_topo(c, id);
+    }
+    int tN = T(c, id).nb[2];
+    if (ok(tN)) {
+        for (int i = 0; i < nX; ++i) {
+            B0(id)[(size_t)nY * V + i] = B0(tN)[i];
+            FY0(id)[(size_t)nY * nX + i] = FY0(tN)[i];
+        }
+        if (!ne_up) {
+            int tNE = T(c, tN).nb[1];
+            if (ok(tNE)) B0(id)[(size_t)nY * V + nX] = B0(tNE)[0];
+        }
+        cell_topo(c, id);
+    }
+    int tS = T(c, id).nb[3];
+    if (ok(tS)) {
+        for (int i = 0; i < nX; ++i) {
+            B0(tS)[(size_t)nY * V + i] = B0(id)[i];
+            FY0(tS)[(size_t)nY * nX + i] = FY0(id)[i];
+        }
+        cell_topo(c, tS);
+        if (!sw_up) {
+            int tSW = T(c, tS).nb[0];
+            if (ok(tSW)) {
+                B0(tSW)[(size_t)nY * V + nX] = B0(id)[0];
+                cell_topo(c, tSW);
+            }
+        }
+    }
+}
+
+// ReconstructwAtEdges (src/UpdateTiles.f90:669-750) for a ghost tile: each edge whose
+// neighbour is on gets its limited w slope and face reconstructions from current data.
+void ghost_edges(kg_ctx& c, int gid) {
+    TileMeta& m = T(c, gid);
+    int mask = 0;
+    const int dirs[4] = {m.nb[0], m.nb[1], m.nb[3], m.nb[2]};  // W, E, S, N
+    for (int q = 0; q < 4; ++q)
+        if (in_bounds(c, dirs[q]) && T(c, dirs[q]).on) mask |= (1 << q);
+    if (!mask) return;
+    CK(launch_ghost_edges(c.A, m.slot, mask, c.qcur, c.st));
+    c.launches++;
+    sync(c);
+}
+
+// AllocateU + AllocateTopographicData + SetTileBoundaries + GetHeights + the cell data.
+void init_tile_geometry(kg_ctx& c, int id) {
+    assign_slot(c, id);
+    set_tile_boundaries(c, id);
+    refresh_nbrs_around(c, id);
+    get_heights(c, id);
+    cell_topo(c, id);
+}
+
+void add_tile(kg_ctx& c, int k);
+
+// AddGhostTiles, src/UpdateTiles.f90:389-481.
+void add_ghost_tiles(kg_ctx& c, int k) {
+    std::vector<int> fresh;
+    for (int i = 1; i <= 8; ++i) {
+        int tile;
+        if (i > 4) {
+            if (c.p.bcs == KG_BC_PERIODIC) break;
+            tile = T(c, k).cor[i - 5];
+        } else {
+            tile = T(c, k).nb[i - 1];
+        }
+        if (!in_bounds(c, tile)) throw KgError(KG_ERR_HALT_EDGE, "a ghost tile would lie outside the domain");
+        bool already = in_list(c.ghost, tile);
+        if (already) ghost_edges(c, tile);
+        else if (!T(c, tile).on && !in_list(fresh, tile)) fresh.push_back(tile);
+    }
+    if (fresh.empty()) return;
+    for (int t : fresh) c.ghost.push_back(t);
+    for (int t : fresh) {
+        init_tile_geometry(c, t);
+        int s = T(c, t).slot;
+        if (on_edge(c, t)) {
+            if (c.p.bcs == KG_BC_DIRICHLET)
+                CK(launch_ghost_dirichlet(c.A, s, c.p.bcsHnval, c.p.bcsuval, c.p.bcsvval, c.p.bcspsival, c.st));
+            else
+                CK(launch_ghost_default(c.A, s, c.p.bcs == KG_BC_PERIODIC ? 2 : 0, c.st));
+        } else {
+            CK(launch_ghost_default(c.A, s, 0, c.st));
+        }
+        c.launches++;
+        sync(c);
+        ghost_edges(c, t);
+        T(c, t).ghost = true;
+        set_kind(c, t, SLOT_GHOST);
+    }
+    for (int t : fresh) equalise(c, t);
+}
+
+// AddTile / AddToActiveTiles / AllocateTile / ActivateTile, src/UpdateTiles.f90:56-384.
+void add_tile(kg_ctx& c, int k) {
+    if (!in_bounds(c, k) || (on_edge(c, k) && c.p.bcs != KG_BC_PERIODIC)) {
+        if (c.p.bcs == KG_BC_HALT)
+            throw KgError(KG_ERR_HALT_EDGE, "tried to add a tile outside the domain (increase the domain size)");
+        return;
+    }
+    // AddToActiveTiles (sorted insert; a ghost tile leaves the ghost list).
+    if (!in_list(c.active, k)) {
+        auto pos = std::upper_bound(c.active.begin(), c.active.end(), k);
+        c.active.insert(pos, k);
+        auto it = std::find(c.ghost.begin(), c.ghost.end(), k);
+        if (it != c.ghost.end()) {
+            c.ghost.erase(it);
+            T(c, k).ghost = false;
+        }
+    }
+    // AllocateTile
+    TileMeta& m = T(c, k);
+    m.on = true;
+    init_tile_geometry(c, k);
+    if (!T(c, k).maxima) {
+        CK(launch_init_maxima(c.A, T(c, k).slot, c.st));
+        c.launches++;
+        T(c, k).maxima = true;
+    }
+    equalise(c, k);
+    T(c, k).src = false;
+    int8_t zero = 0;
+    CK(cudaMemcpyAsync(c.A.has_source + T(c, k).slot, &zero, 1, cudaMemcpyHostToDevice, c.st));
+    // ActivateTile
+    T(c, k).ghost = false;
+    set_kind(c, k, SLOT_ACTIVE);
+    CK(launch_activate(c.A, T(c, k).slot, c.qcur, c.st));
+    c.launches++;
+    sync(c);
+    add_ghost_tiles(c, k);
+    std::vector<int> one{T(c, k).slot};
+    upload_list(c, one);
+    CK(launch_face_topo(c.A, c.d_list, 1, c.st));
+    c.launches++;
+    sync(c);
+    c.blocks_dirty = true;
+}
+
+void rebuild_blocks(kg_ctx& c) {
+    if (!c.blocks_dirty) return;
+    refresh_all_nbrs(c);
+    c.blocks.clear();
+    const int BSZ = 16;
+    for (int id : c.active) {
+        int s = T(c, id).slot;
+        for (int y0 = 0; y0 < c.nY; y0 += BSZ)
+            for (int x0 = 0; x0 < c.nX; x0 += BSZ) c.blocks.push_back(BlockDesc{s, x0, y0, id});
+    }
+    if ((int)c.blocks.size() > c.d_blocks_cap) {
+        if (c.d_blocks) CK(cudaFree(c.d_blocks));
+        c.d_blocks_cap = std::max<int>((int)c.blocks.size(), 2 * c.d_blocks_cap);
+        CK(cudaMalloc(&c.d_blocks, (size_t)c.d_blocks_cap * sizeof(BlockDesc)));
+    }
+    if (!c.blocks.empty())
+        CK(cudaMemcpyAsync(c.d_blocks, c.blocks.data(), c.blocks.size() * sizeof(BlockDesc), cudaMemcpyHostToDevice, c.st));
+    sync(c);
+    c.blocks_dirty = false;
+}
+
+// CheckIfNearBoundaries, src/TimeStepper.f90:924-1150: device edge-band flags for the
+// tiles active at the start of the check, then the reference's four sweeps with the list
+// growing (and shifting) under the loop; tiles added during the sweeps are dry.
+void check_near_boundaries(kg_ctx& c) {
+    if (c.active.empty()) return;
+    std::vector<int> slots;
+    for (int id : c.active) slots.push_back(T(c, id).slot);
+    upload_list(c, slots);
+    CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), c.qcur, c.src_override ? c.d_srcHn : nullptr, c.d_flags, c.st));
+    c.launches++;
+    std::vector<int> fl(slots.size());
+    CK(cudaMemcpyAsync(fl.data(), c.d_flags, fl.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    sync(c);
+    std::vector<int> flag_of((size_t)c.nTiles + 1, -1);
+    for (size_t q = 0; q < slots.size(); ++q) flag_of[(size_t)c.active[q]] = fl[q];
+    int TB = c.p.TileBuffer;
+    int dry_flags = (0 > c.nY - TB ? 1 : 0) | (c.nY <= TB ? 2 : 0) | (0 > c.nX - TB ? 4 : 0) | (c.nX <= TB ? 8 : 0);
+    // Sweep order N, S, E, W with neighbour index 2, 3, 1, 0.
+    const int bit[4] = {1, 2, 4, 8}, nbi[4] = {2, 3, 1, 0};
+    for (int d = 0; d < 4; ++d) {
+        int size0 = (int)c.active.size();
+        for (int tt = 0; tt < size0; ++tt) {
+            int ttk = c.active[(size_t)tt];
+            int nbt = T(c, ttk).nb[nbi[d]];
+            if (nbt > 0 && in_bounds(c, nbt) && !T(c, nbt).on) {
+                int f = flag_of[(size_t)ttk];
+                if (f < 0) f = dry_flags;
+                if (f & bit[d]) add_tile(c, nbt);
+            }
+        }
+    }
+}
+
+// ComputeAdvisedTimeStep, src/HydraulicRHS.f90:141-174.
+double advised(kg_ctx& c, unsigned long long bits, int substep) {
+    double umin;
+    std::memcpy(&umin, &bits, sizeof(double));
+    if ((int)c.active.size() < c.nTiles) umin = mn(umin, c.p.maxdt);
+    double m = mn(c.p.cfl * umin, c.dp.diffusiveTimeScale);
+    m = mn(m, c.p.maxdt);
+    if (substep == 1) return 0.9 * m;
+    return m;
+}
+
+unsigned long long run_pass(kg_ctx& c, StepArgs S) {
+    *c.h_cfl = (unsigned long long)0x7FEFFFFFFFFFFFFFull;  // bits of huge(1.0_wp)
+    CK(cudaMemcpyAsync(c.d_cfl, c.h_cfl, sizeof(unsigned long long), cudaMemcpyHostToDevice, c.st));
+    S.cfl_min = c.d_cfl;
+    if (c.timing) CK(cudaEventRecord(c.ev0, c.st));
+    CK(launch_hydro(c.A, c.d_blocks, (int)c.blocks.size(), S, c.st));
+    if (c.timing) CK(cudaEventRecord(c.ev1, c.st));
+    c.launches++;
+    CK(cudaMemcpyAsync(c.h_cfl, c.d_cfl, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
+    sync(c);
+    if (c.timing) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+        c.kernel_ms += ms;
+        c.timed_passes++;
+    }
+    return *c.h_cfl;
+}
+
+double next_flux_time(const kg_ctx& c, double t) {  // NextFluxSeriesTime, src/TimeStepper.f90:281-305
+    double nextT = HUGE_D, tdiff = HUGE_D;
+    for (const HostSource& s : c.srcs)
+        for (int j = 0; j < s.n; ++j) {
+            double tmp = s.time[j] - t;
+            if (tmp > 0.0 && tmp < tdiff) { tdiff = tmp; nextT = s.time[j]; }
+        }
+    return nextT;
+}
+
+// HydraulicTimeStepper on the device; returns true when dt had to be refined.
+bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int q_out) {
+    double nextT = c.t + dt;
+    c.dt = dt;
+    StepArgs S{};
+    S.q_in = q_in; S.q_out = q_out; S.dt = dt; S.t_grid = c.t; S.do_maxima = 1;
+    S.mode = MODE_S1; S.t_rhs = nextT;
+    double dt1 = advised(c, run_pass(c, S), 2);
+    if (dt1 < dt) { dt = 0.9 * dt1; return true; }
+    S.mode = MODE_S2; S.t_rhs = c.t + 0.5 * dt;
+    double dt2 = advised(c, run_pass(c, S), 3);
+    if (dt2 < dt) { dt = 0.9 * dt2; return true; }
+    S.mode = MODE_S3; S.t_rhs = nextT; S.t_max = nextT;
+    run_pass(c, S);
+    return false;
+}
+
+// One accepted step of IntegrateTo (src/TimeStepper.f90:151-275).
+void integrate_step(kg_ctx& c, double tend) {
+    if (!c.sources_loaded) throw KgError(KG_ERR_STATE, "kg_load_sources must be called before stepping");
+    if (c.p.MorphodynamicsOn) throw KgError(KG_ERR_UNSUPPORTED, "the morphodynamic operator is not in this build");
+    check_near_boundaries(c);
+    rebuild_blocks(c);
+    StepArgs S{};
+    S.mode = MODE_RHS0; S.q_in = c.qcur; S.t_rhs = c.t; S.t_grid = c.t;
+    double adv = advised(c, run_pass(c, S), 1);
+    double tmax = mn(tend, next_flux_time(c, c.t));
+    adv = mn(adv, tmax - c.t);
+    c.dt = adv;
+    double dt = adv;
+    c.t0 = c.t;
+    int guard = 0;
+    while (true) {
+        if (++guard > 100000 || !(dt > 0.0)) throw KgError(KG_ERR_DT, "time step collapsed");
+        if (hydraulic_stepper(c, dt, c.qcur, 1 - c.qcur)) { c.rejected++; continue; }
+        break;
+    }
+    c.qcur = 1 - c.qcur;
+    c.t = c.t0 + dt;
+    c.dt = dt;
+    c.steps++;
+    c.cell_updates += (int64_t)c.active.size() * c.SC;
+    c.src_override = false;
+}
+
+// ---------------------------------------------------------------- sources
+// LoadSourceConditions, src/SetSources.f90:47-405 (2D).  Tiles are activated in the
+// reference's loop order; the cap/cube increments are then applied to the cells in the
+// same order, which gives the same state (activation only touches the new tile).
+struct CellMod { int id, ii, jj, kind, idx; double R2; };
+
+void load_sources(kg_ctx& c) {
+    for (auto& s : c.srcs) s.ncells = 0;
+    std::vector<CellMod> mods;
+    const kg_params& P = c.p;
+    // Bounding boxes to skip tiles far from every cap / cube / source.
+    auto near = [&](double xmin, double xmax, double ymin, double ymax) {
+        for (int k = 0; k < P.nCaps; ++k) {
+            const kg_cap& C = P.caps[k];
+            if (C.x + C.radius >= xmin && C.x - C.radius <= xmax && C.y + C.radius >= ymin && C.y - C.radius <= ymax) return true;
+        }
+        for (int k = 0; k < P.nCubes; ++k) {
+            const kg_cube& C = P.cubes[k];
+            if (C.x + 0.5 * C.length >= xmin && C.x - 0.5 * C.length <= xmax && C.y + 0.5 * C.width >= ymin &&
+                C.y - 0.5 * C.width <= ymax)
+                return true;
+        }
+        for (auto& s : c.srcs)
+            if (s.x + s.R >= xmin && s.x - s.R <= xmax && s.y + s.R >= ymin && s.y - s.R <= ymax) return true;
+        return false;
+    };
+    for (int i = 1; i <= c.nXt; ++i)
+        for (int j = 1; j <= c.nYt; ++j) {
+            int k = tile_id(c, i, j);
+            double x0 = cell_x(c, i, 1) - c.dp.dx, x1 = cell_x(c, i, c.nX) + c.dp.dx;
+            double y0 = cell_y(c, j, 1) - c.dp.dy, y1 = cell_y(c, j, c.nY) + c.dp.dy;
+            if (!near(x0, x1, y0, y1)) continue;
+            for (int ii = 1; ii <= c.nX; ++ii)
+                for (int jj = 1; jj <= c.nY; ++jj) {
+                    double x = cell_x(c, i, ii), y = cell_y(c, j, jj);
+                    for (int kk = 0; kk < P.nCaps; ++kk) {
+                        const kg_cap& C = P.caps[kk];
+                        double R2 = (x - C.x) * (x - C.x) + (y - C.y) * (y - C.y);
+                        if (R2 <= C.radius * C.radius) {
+                            if (!T(c, k).on) add_tile(c, k);
+                            if (T(c, k).on) mods.push_back(CellMod{k, ii, jj, 0, kk, R2});
+                        }
+                    }
+                    for (int kk = 0; kk < P.nCubes; ++kk) {
+                        const kg_cube& C = P.cubes[kk];
+                        if ((std::fabs(x - C.x) <= 0.5 * C.length) && (std::fabs(y - C.y) <= 0.5 * C.width)) {
+                            if (!T(c, k).on) add_tile(c, k);
+                            if (T(c, k).on) mods.push_back(CellMod{k, ii, jj, 1, kk, 0.0});
+                        }
+                    }
+                    for (size_t kk = 0; kk < c.srcs.size(); ++kk) {
+                        HostSource& S = c.srcs[kk];
+                        double R2 = (x - S.x) * (x - S.x) + (y - S.y) * (y - S.y);
+                        if (R2 <= S.R * S.R) {
+                            if (!T(c, k).on) add_tile(c, k);
+                            T(c, k).src = true;
+                            S.ncells = S.ncells + 1;
+                        }
+                    }
+                }
+        }
+    // Apply the cap/cube increments on the host copies of the touched tiles.
+    std::vector<int> touched;
+    for (auto& m : mods)
+        if (!in_list(touched, m.id)) touched.push_back(m.id);
+    int SC = c.SC;
+    struct Buf { std::vector<double> q, ct, hn, rho; };
+    std::vector<Buf> bufs(touched.size());
+    for (size_t q = 0; q < touched.size(); ++q) {
+        int s = T(c, touched[q]).slot;
+        bufs[q].q.resize((size_t)4 * SC);
+        bufs[q].ct.resize((size_t)4 * SC);
+        bufs[q].hn.assign((size_t)SC, 0.0);
+        bufs[q].rho.assign((size_t)SC, c.p.rhow);
+        CK(cudaMemcpyAsync(bufs[q].q.data(), c.A.Q[c.qcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(bufs[q].ct.data(), c.A.CT + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    }
+    sync(c);
+    double rhow = c.p.rhow, rhos = c.p.rhos;
+    for (auto& m : mods) {
+        size_t q = std::find(touched.begin(), touched.end(), m.id) - touched.begin();
+        Buf& B = bufs[q];
+        size_t cc = (size_t)(m.jj - 1) * c.nX + (m.ii - 1);
+        double* w = &B.q[cc];
+        double* m1 = &B.q[SC + cc];
+        double* m2 = &B.q[2 * (size_t)SC + cc];
+        double* hp = &B.q[3 * (size_t)SC + cc];
+        double b0c = B.ct[cc], dbx = B.ct[2 * (size_t)SC + cc], dby = B.ct[3 * (size_t)SC + cc];
+        double gam = gam_of(c.dp.geo, dbx, dby);
+        double Hn_orig = B.hn[cc], rho_orig = B.rho[cc];
+        if (m.kind == 0) {
+            const kg_cap& C = P.caps[m.idx];
+            double rho = rhow + (rhos - rhow) * C.psi;
+            double Hn = C.height;
+            if (C.shape == KG_SHAPE_FLAT) {
+                *w = *w + C.height / gam;
+                B.hn[cc] = B.hn[cc] + C.height;
+                *m1 = *m1 + rho * C.height * C.u;
+                *m2 = *m2 + rho * C.height * C.v;
+                *hp = *hp + C.psi * C.height;
+            } else if (C.shape == KG_SHAPE_PARA) {
+                double f = C.height * (1.0 - m.R2 / C.radius / C.radius);
+                *w = *w + f / gam;
+                B.hn[cc] = B.hn[cc] + f;
+                *m1 = *m1 + rho * C.height * C.u;
+                *m2 = *m2 + rho * C.height * C.v;
+                *hp = *hp + C.psi * C.height * (1.0 - m.R2 / C.radius / C.radius);
+            } else {
+                double hpv = C.height - b0c;
+                Hn = hpv * gam;
+                if (Hn > 0.0) {
+                    *w = *w + hpv;
+                    B.hn[cc] = B.hn[cc] + Hn;
+                    *m1 = *m1 + rho * Hn * C.u;
+                    *m2 = *m2 + rho * Hn * C.v;
+                    *hp = *hp + C.psi * Hn;
+                }
+            }
+            B.rho[cc] = (rho_orig * Hn_orig + rho * Hn) / (Hn_orig + Hn);
+        } else {
+            const kg_cube& C = P.cubes[m.idx];
+            double rho = rhow + (rhos - rhow) * C.psi;
+            double Hn = C.height;
+            if (C.shape == KG_SHAPE_LEVEL) {
+                double hpv = C.height - b0c;
+                Hn = hpv * gam;
+                if (Hn > 0.0) {
+                    *w = *w + hpv;
+                    B.hn[cc] = B.hn[cc] + Hn;
+                    *hp = *hp + Hn * C.psi;
+                    *m1 = *m1 + 0.0;
+                    *m2 = *m2 + 0.0;
+                }
+            } else {
+                *w = *w + C.height / gam;
+                B.hn[cc] = B.hn[cc] + C.height;
+                *m1 = *m1 + 0.0;
+                *m2 = *m2 + 0.0;
+                *hp = *hp + C.psi * C.height;
+            }
+            B.rho[cc] = (rho_orig * Hn_orig + rho * Hn) / (Hn_orig + Hn);
+        }
+    }
+    // Depth/density as the reference holds them after the sources: activation leaves
+    // Hn = 0 and rho = rhow everywhere, the cap/cube loops then overwrite cells.
+    {
+        std::vector<double> z((size_t)SC, 0.0), r((size_t)SC, rhow);
+        for (int id : c.active) {
+            int s = T(c, id).slot;
+            CK(cudaMemcpyAsync(c.d_srcHn + (size_t)s * SC, z.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+            CK(cudaMemcpyAsync(c.d_srcRho + (size_t)s * SC, r.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        }
+        sync(c);
+    }
+    for (size_t q = 0; q < touched.size(); ++q) {
+        int s = T(c, touched[q]).slot;
+        for (int b = 0; b < 2; ++b)
+            CK(cudaMemcpyAsync(c.A.Q[b] + (size_t)s * 4 * SC, bufs[q].q.data(), (size_t)4 * SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.d_srcHn + (size_t)s * SC, bufs[q].hn.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.d_srcRho + (size_t)s * SC, bufs[q].rho.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    }
+    sync(c);
+    // containsSource flags and the per-source cell counts.
+    for (int id : c.active) {
+        int8_t f = T(c, id).src ? 1 : 0;
+        CK(cudaMemcpyAsync(c.A.has_source + T(c, id).slot, &f, 1, cudaMemcpyHostToDevice, c.st));
+        sync(c);
+    }
+    std::vector<DevSource> ds(c.srcs.size());
+    for (size_t k = 0; k < c.srcs.size(); ++k) {
+        DevSource& d = ds[k];
+        std::memset(&d, 0, sizeof(d));
+        d.x = c.srcs[k].x; d.y = c.srcs[k].y; d.R = c.srcs[k].R; d.n = c.srcs[k].n; d.ncells = c.srcs[k].ncells;
+        for (int q = 0; q < d.n; ++q) { d.time[q] = c.srcs[k].time[q]; d.flux[q] = c.srcs[k].flux[q]; d.psi[q] = c.srcs[k].psi[q]; }
+    }
+    CK(set_constants(c.dp, ds.data(), (int)ds.size(), c.st));
+    sync(c);
+    for (int g : std::vector<int>(c.ghost)) ghost_edges(c, g);
+    c.src_override = true;
+    c.sources_loaded = true;
+    c.blocks_dirty = true;
+}
+
+// Run settings (src/DomainSettings.f90:185-225, src/Parameters.f90:629-648).
+void setup(kg_ctx& c, const kg_params& p) {
+    c.p = p;
+    if (p.nXtiles < 1 || p.nYtiles < 1 || p.nXpertile < 2 || p.nYpertile < 2)
+        throw KgError(KG_ERR_PARAM, "nXtiles/nYtiles must be >= 1 and nXpertile/nYpertile >= 2");
+    if (p.nYtiles * p.nYpertile == 1) throw KgError(KG_ERR_UNSUPPORTED, "1D grids are not implemented");
+    if (p.nSources > KG_MAX_SOURCES || p.nCaps > KG_MAX_CAPS || p.nCubes > KG_MAX_CUBES)
+        throw KgError(KG_ERR_PARAM, "too many caps, cubes or sources");
+    c.nX = p.nXpertile; c.nY = p.nYpertile; c.nXt = p.nXtiles; c.nYt = p.nYtiles; c.nTiles = c.nXt * c.nYt;
+    c.SC = c.nX * c.nY; c.SV = (c.nX + 1) * (c.nY + 1); c.SFX = (c.nX + 1) * c.nY; c.SFY = c.nX * (c.nY + 1);
+    c.nE = std::max(c.nX, c.nY);
+    DevParams& d = c.dp;
+    d.nX = c.nX; d.nY = c.nY; d.nXtiles = c.nXt; d.nYtiles = c.nYt;
+    c.xSize = c.nXt * p.Xtilesize;
+    c.ySize = c.nYt * p.Ytilesize;
+    d.xSize = c.xSize; d.ySize = c.ySize;
+    d.dx = p.Xtilesize / (double)c.nX;
+    d.dy = p.Ytilesize / (double)c.nY;
+    d.dxR = 1.0 / d.dx;
+    d.dyR = 1.0 / d.dy;
+    d.geo = p.geometric_factors != 0; d.morpho = p.MorphodynamicsOn != 0;
+    d.drag = p.drag; d.erosion = p.erosion; d.deposition = p.deposition; d.etrans = p.erosion_transition;
+    d.damping = p.morpho_damping; d.fswitch = p.fswitch; d.limiter = p.limiter; d.bcs = p.bcs;
+    d.TileBuffer = p.TileBuffer; d.nSources = p.nSources;
+    d.g = p.g; d.rhow = p.rhow; d.rhos = p.rhos;
+    const double visc_w = 1.2e-6;
+    d.gred = (p.rhos / p.rhow - 1.0) * p.g;
+    double Rep = std::sqrt(p.g * p.SolidDiameter) * p.SolidDiameter / visc_w;
+    double R = std::pow(d.gred / visc_w / visc_w, 1.0 / 3.0) * p.SolidDiameter;
+    d.ws0 = p.ws0_given ? p.ws0 : visc_w / p.SolidDiameter * (std::sqrt(10.36 * 10.36 + 1.048 * R * R * R) - 10.36);
+    d.nsettling = (4.7 + 0.41 * std::pow(Rep, 0.75)) / (1.0 + 0.175 * std::pow(Rep, 0.75));
+    d.CriticalShields = 0.3 / (1.0 + 1.2 * R) + 0.055 * (1.0 - std::exp(-0.02 * R));
+    d.ChezyCo = p.ChezyCo; d.ManningCo = p.ManningCo; d.CoulombCo = p.CoulombCo;
+    d.PMin = p.PouliquenMinSlope; d.PMax = p.PouliquenMaxSlope; d.PInt = p.PouliquenIntermediateSlope;
+    d.PBeta = p.PouliquenBeta; d.Ebetastar = p.Edwards2019betastar; d.Ekappa = p.Edwards2019kappa; d.EGamma = p.Edwards2019Gamma;
+    d.SwRate = p.VoellmySwitchRate; d.SwValue = p.VoellmySwitchValue;
+    d.EroRate = p.EroRate; d.EroRateGranular = p.EroRateGranular; d.EroDepth = p.EroDepth;
+    d.EroCriticalHeight = p.EroCriticalHeight; d.BedPorosity = p.BedPorosity;
+    d.maxPack = p.maxPack; d.SolidDiameter = p.SolidDiameter; d.nu = p.EddyViscosity; d.hThr = p.heightThreshold;
+    d.tan1deg = std::tan(PI_D / 180.0);
+    d.SpongeStrength = p.SpongeStrength;
+    d.cfl = p.cfl; d.maxdt = p.maxdt;
+    d.diffusiveTimeScale = HUGE_D;
+    if (p.EddyViscosity > 0.0)
+        d.diffusiveTimeScale = mn(d.dx * d.dx / p.EddyViscosity, d.dy * d.dy / p.EddyViscosity);
+    int Nout = p.Nout > 0 ? p.Nout : 100;
+    c.DeltaT = (p.tend - p.tstart) / (double)Nout;
+    for (int k = 0; k < p.nSources; ++k) {
+        const kg_flux_source& s = p.sources[k];
+        if (s.n_series < 1 || s.n_series > KG_MAX_SERIES) throw KgError(KG_ERR_PARAM, "bad flux series length");
+        HostSource h;
+        h.x = s.x; h.y = s.y; h.R = s.radius; h.n = s.n_series; h.ncells = 0;
+        h.time.assign(s.time, s.time + s.n_series);
+        h.flux.assign(s.flux, s.flux + s.n_series);
+        h.psi.assign(s.psi, s.psi + s.n_series);
+        c.srcs.push_back(h);
+    }
+    c.tiles.assign((size_t)c.nTiles, TileMeta());
+    c.nx1 = (int64_t)c.nXt * c.nX + 1;
+    c.ny1 = (int64_t)c.nYt * c.nY + 1;
+    c.t = 0.0;
+    c.A.nE = c.nE;
+    CK(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
+    CK(cudaMalloc(&c.d_cfl, sizeof(unsigned long long)));
+    CK(cudaMalloc(&c.d_vol, 4 * sizeof(double)));
+    CK(cudaMallocHost(&c.h_cfl, sizeof(unsigned long long)));
+    CK(set_constants(c.dp, nullptr, 0, c.st));
+    sync(c);
+}
+
+void free_ctx(kg_ctx* c) {
+    if (!c) return;
+    if (c->st) cudaStreamSynchronize(c->st);
+    for (int b = 0; b < 4; ++b) cudaFree(c->A.Q[b]);
+    void* ptrs[] = {c->A.E0, c->A.I0, c->A.UV, c->A.CT, c->A.FX, c->A.FY, c->A.BV, c->A.G9, c->A.GE, c->A.MX,
+                    c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
+                    c->d_cfl, c->d_vol, c->d_srcHn, c->d_srcRho};
+    for (void* q : ptrs) cudaFree(q);
+    if (c->h_cfl) cudaFreeHost(c->h_cfl);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+}
+
+int fail(kg_ctx* c, const KgError& e) {
+    if (c) c->err = e.what();
+    return e.code;
+}
+
+void fill_stats(kg_ctx* c, kg_step_stats* st, int64_t s0, int64_t r0, int64_t cu0, int64_t l0) {
+    if (!st) return;
+    st->t = c->t;
+    st->dt = c->dt;
+    st->steps = c->steps - s0;
+    st->rejected = c->rejected - r0;
+    st->cell_updates = c->cell_updates - cu0;
+    st->n_active = (int32_t)c->active.size();
+    st->n_ghost = (int32_t)c->ghost.size();
+    st->kernel_launches = c->launches - l0;
+}
+
+int active_slot(kg_ctx* c, int id) {
+    if (!c || id < 1 || id > c->nTiles || !in_list(c->active, id)) return -1;
+    return T(*c, id).slot;
+}
+
+std::vector<double> d2h(kg_ctx* c, const double* src, size_t n) {
+    std::vector<double> v(n);
+    CK(cudaMemcpyAsync(v.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    sync(*c);
+    return v;
+}
+
+}  // namespace
+
+#define KG_GUARD(c, ...)                                    \
+    try {                                                   \
+        __VA_ARGS__;                                        \
+    } catch (const KgError& e) {                            \
+        return fail(c, e);                                  \
+    } catch (const std::exception& e) {                     \
+        if (c) c->err = e.what();                           \
+        return KG_ERR_PARAM;                                \
+    }
+
+extern "C" {
+
+const char* kg_version(void) { return "kestrel_gb300 1.0 (sm_103a)"; }
+
+int kg_create(const kg_params* params, int32_t precision, kg_ctx** out) {
+    if (!params || !out) return KG_ERR_PARAM;
+    *out = nullptr;
+    if (precision != KG_PREC_FP64) return KG_ERR_UNSUPPORTED;
+    kg_ctx* c = new kg_ctx();
+    c->prec = precision;
+    try {
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess || n < 1) throw KgError(KG_ERR_CUDA, "no CUDA device is available");
+        setup(*c, *params);
+    } catch (const KgError& e) {
+        int code = e.code;
+        free_ctx(c);
+        return code;
+    }
+    *out = c;
+    return KG_OK;
+}
+
+void kg_destroy(kg_ctx* ctx) { free_ctx(ctx); }
+
+const char* kg_last_error(const kg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int kg_upload_b0(kg_ctx* c, const double* b0, int64_t nx1, int64_t ny1) {
+    if (!c || !b0) return KG_ERR_PARAM;
+    if (nx1 != c->nx1 || ny1 != c->ny1) {
+        c->err = "b0 grid must be (nXtiles*nXpertile+1) x (nYtiles*nYpertile+1)";
+        return KG_ERR_PARAM;
+    }
+    c->upload.assign(b0, b0 + nx1 * ny1);
+    return KG_OK;
+}
+
+int kg_load_sources(kg_ctx* c) {
+    if (!c) return KG_ERR_PARAM;
+    if (c->sources_loaded) { c->err = "sources already loaded"; return KG_ERR_STATE; }
+    if (c->p.topog == KG_TOPO_UPLOAD && c->upload.empty()) { c->err = "no topography uploaded"; return KG_ERR_STATE; }
+    KG_GUARD(c, load_sources(*c));
+    return KG_OK;
+}
+
+int kg_step(kg_ctx* c, double t_stop, kg_step_stats* st) {
+    if (!c) return KG_ERR_PARAM;
+    int64_t s0 = c->steps, r0 = c->rejected, cu0 = c->cell_updates, l0 = c->launches;
+    int rc = KG_OK;
+    try {
+        integrate_step(*c, t_stop);
+    } catch (const KgError& e) {
+        rc = fail(c, e);
+    }
+    fill_stats(c, st, s0, r0, cu0, l0);
+    return rc;
+}
+
+int kg_integrate_to(kg_ctx* c, double t_end, kg_step_stats* st) {
+    if (!c) return KG_ERR_PARAM;
+    int64_t s0 = c->steps, r0 = c->rejected, cu0 = c->cell_updates, l0 = c->launches;
+    int rc = KG_OK;
+    if (t_end > c->t) {
+        try {
+            while (true) {
+                integrate_step(*c, t_end);
+                if (c->t >= t_end) break;
+            }
+        } catch (const KgError& e) {
+            rc = fail(c, e);
+        }
+    }
+    fill_stats(c, st, s0, r0, cu0, l0);
+    return rc;
+}
+
+int kg_run(kg_ctx* c, kg_step_stats* st) {
+    if (!c) return KG_ERR_PARAM;
+    int64_t s0 = c->steps, r0 = c->rejected, cu0 = c->cell_updates, l0 = c->launches;
+    int Nout = c->p.Nout > 0 ? c->p.Nout : 100;
+    int rc = KG_OK;
+    for (int i = 1; i <= Nout && rc == KG_OK; ++i) rc = kg_integrate_to(c, c->p.tstart + i * c->DeltaT, nullptr);
+    fill_stats(c, st, s0, r0, cu0, l0);
+    return rc;
+}
+
+int kg_hydraulic_rhs(kg_ctx* c, double t, int32_t substep, double* advised_dt) {
+    if (!c || !advised_dt || substep < 1 || substep > 4) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        rebuild_blocks(*c);
+        StepArgs S{};
+        S.mode = MODE_RHS0; S.q_in = c->qcur; S.t_rhs = t; S.t_grid = c->t;
+        *advised_dt = advised(*c, run_pass(*c, S), substep);
+    });
+    return KG_OK;
+}
+
+int kg_get_active_tiles(kg_ctx* c, int32_t* ids, int32_t* n) {
+    if (!c || !n) return KG_ERR_PARAM;
+    int cap = *n;
+    *n = (int32_t)c->active.size();
+    for (int i = 0; ids && i < std::min(cap, *n); ++i) ids[i] = c->active[(size_t)i];
+    return KG_OK;
+}
+int kg_get_ghost_tiles(kg_ctx* c, int32_t* ids, int32_t* n) {
+    if (!c || !n) return KG_ERR_PARAM;
+    int cap = *n;
+    *n = (int32_t)c->ghost.size();
+    for (int i = 0; ids && i < std::min(cap, *n); ++i) ids[i] = c->ghost[(size_t)i];
+    return KG_OK;
+}
+
+int kg_get_tile_field(kg_ctx* c, int32_t id, int32_t field, double* out) {
+    int s = active_slot(c, id);
+    if (s < 0) return KG_ERR_NOT_FOUND;
+    if (field < 1 || field > 13 || !out) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        int SC = c->SC;
+        if (field <= 4) {
+            auto v = d2h(c, c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * SC, SC);
+            std::memcpy(out, v.data(), SC * sizeof(double));
+        } else if (field >= 10) {
+            auto v = d2h(c, c->A.CT + ((size_t)s * 4 + field - 10) * SC, SC);
+            std::memcpy(out, v.data(), SC * sizeof(double));
+        } else if (field == 6 || field == 7) {
+            auto v = d2h(c, c->A.UV + ((size_t)s * 2 + field - 6) * SC, SC);
+            std::memcpy(out, v.data(), SC * sizeof(double));
+        } else {
+            auto q = d2h(c, c->A.Q[c->qcur] + (size_t)s * 4 * SC, 4 * (size_t)SC);
+            auto ct = d2h(c, c->A.CT + (size_t)s * 4 * SC, 4 * (size_t)SC);
+            std::vector<double> hn, rh;
+            if (c->src_override) {
+                hn = d2h(c, c->d_srcHn + (size_t)s * SC, SC);
+                rh = d2h(c, c->d_srcRho + (size_t)s * SC, SC);
+            }
+            double e2 = c->dp.hThr * c->dp.hThr;
+            for (int k = 0; k < SC; ++k) {
+                double gam = gam_of(c->dp.geo, ct[2 * (size_t)SC + k], ct[3 * (size_t)SC + k]);
+                double Hn = compute_hn(q[k], ct[k], ct[(size_t)SC + k], gam);
+                if (Hn < 0.0) Hn = 0.0;
+                double pp = q[3 * (size_t)SC + k] < 0.0 ? 0.0 : q[3 * (size_t)SC + k];
+                double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), c->dp.maxPack);
+                double rho = density(c->dp, psi);
+                if (c->src_override) { Hn = hn[k]; rho = rh[k]; }
+                out[k] = field == 5 ? Hn : field == 8 ? psi : rho;
+            }
+        }
+    });
+    return KG_OK;
+}
+
+int kg_set_tile_field(kg_ctx* c, int32_t id, int32_t field, const double* in) {
+    int s = active_slot(c, id);
+    if (s < 0) return KG_ERR_NOT_FOUND;
+    if (field < 1 || field > 4 || !in) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        CK(cudaMemcpyAsync(c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * c->SC, in, (size_t)c->SC * sizeof(double),
+                           cudaMemcpyHostToDevice, c->st));
+        sync(*c);
+    });
+    return KG_OK;
+}
+
+int kg_get_tile_vertex(kg_ctx* c, int32_t id, int32_t which, double* out) {
+    int s = active_slot(c, id);
+    if (s < 0) return KG_ERR_NOT_FOUND;
+    if (which < 0 || which > 1 || !out) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        auto v = d2h(c, c->A.BV + ((size_t)s * 2 + which) * c->SV, c->SV);
+        std::memcpy(out, v.data(), (size_t)c->SV * sizeof(double));
+    });
+    return KG_OK;
+}
+
+int kg_get_tile_rhs(kg_ctx* c, int32_t id, int32_t k, double* out) {
+    int s = active_slot(c, id);
+    if (s < 0) return KG_ERR_NOT_FOUND;
+    if (k < 1 || k > 5 || !out) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        const double* src = k <= 4 ? c->A.E0 + ((size_t)s * 4 + k - 1) * c->SC : c->A.I0 + (size_t)s * c->SC;
+        auto v = d2h(c, src, c->SC);
+        std::memcpy(out, v.data(), (size_t)c->SC * sizeof(double));
+    });
+    return KG_OK;
+}
+
+int kg_get_tile_maxima(kg_ctx* c, int32_t id, int32_t which, double* out) {
+    int s = active_slot(c, id);
+    if (s < 0) return KG_ERR_NOT_FOUND;
+    if (which < 0 || which > 5 || !out) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        size_t SC = c->SC;
+        if (which == 5) {
+            auto v = d2h(c, c->A.MX + ((size_t)s * 11 + 10) * SC, SC);
+            std::memcpy(out, v.data(), SC * sizeof(double));
+        } else {
+            auto v = d2h(c, c->A.MX + ((size_t)s * 11 + 2 * which) * SC, 2 * SC);
+            std::memcpy(out, v.data(), 2 * SC * sizeof(double));
+        }
+    });
+    return KG_OK;
+}
+
+int kg_volume(kg_ctx* c, double out[4]) {
+    if (!c || !out) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        std::vector<int> slots;
+        for (int id : c->active) slots.push_back(T(*c, id).slot);
+        upload_list(*c, slots);
+        CK(launch_volume(c->A, c->d_list, (int)slots.size(), c->qcur, c->src_override ? c->d_srcHn : nullptr,
+                         c->src_override ? c->d_srcRho : nullptr, c->d_vol, c->st));
+        c->launches++;
+        auto v = d2h(c, c->d_vol, 4);
+        for (int k = 0; k < 4; ++k) out[k] = v[k];
+    });
+    return KG_OK;
+}
+
+int kg_get_time(kg_ctx* c, double* t, double* dt) {
+    if (!c || !t || !dt) return KG_ERR_PARAM;
+    *t = c->t;
+    *dt = c->dt;
+    return KG_OK;
+}
+
+int64_t kg_kernel_launches(const kg_ctx* c) { return c ? c->launches : 0; }
+
+void* kg_stream(kg_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+int kg_set_kernel_timing(kg_ctx* c, int32_t enable) {
+    if (!c) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        if (enable && !c->ev0) {
+            CK(cudaEventCreate(&c->ev0));
+            CK(cudaEventCreate(&c->ev1));
+        }
+        c->timing = enable != 0;
+        c->kernel_ms = 0.0;
+        c->timed_passes = 0;
+    });
+    return KG_OK;
+}
+
+int kg_get_kernel_time(kg_ctx* c, double* ms, int64_t* passes) {
+    if (!c || !ms || !passes) return KG_ERR_PARAM;
+    *ms = c->kernel_ms;
+    *passes = c->timed_passes;
+    return KG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+// kg_engine.cuh -- device data layout shared by the kernels and the host engine.
+//
+// HBM layout (one "slot" per allocated tile, active or ghost; fields of a slot are
+// contiguous planes, x fastest):
+//   state buffers  Q[buf][slot][4][nY][nX]    w, rhoHnu, rhoHnv, Hnpsi (buf: 0/1 ping-pong
+//                                             solution, 2/3 RK stage results)
+//   RHS of stage 1 E0[slot][4][nY][nX], I0[slot][nY][nX]
+//   velocities     UV[slot][2][nY][nX]        u, v as the reference leaves them after a step
+//   cell topo      CT[slot][4][nY][nX]        b0, bt, dbdx, dbdy at cell centres
+//   face topo X    FX[slot][5][nY][nX+1]      b0, bt, dbdx, dbdy, InterpolateB(b0,bt)
+//   face topo Y    FY[slot][5][nY+1][nX]
+//   vertices       BV[slot][2][nY+1][nX+1]    b0, bt (each tile keeps its own copy of its
+//                                             edge vertices, as the reference does)
+//   ghost data     G9[slot][9][nY][nX]        static u(1:9) of a ghost tile
+//                  GE[slot][12][nE]           its stale w reconstructions at the edges
+//   maxima         MX[slot][11][nY][nX]       Hnmax, umax, emax, dmax, psimax (value, time)
+//                                             and tfirst (src/Grid.f90:95-102)
+#pragma once
+#include "kg_physics.cuh"
+
+namespace kg {
+
+enum SlotKind : int8_t { SLOT_FREE = 0, SLOT_ACTIVE = 1, SLOT_GHOST = 2 };
+enum Nb { NB_W = 0, NB_E = 1, NB_N = 2, NB_S = 3, NB_SW = 4, NB_SE = 5, NB_NW = 6, NB_NE = 7 };
+// Ghost edge records (GE planes): uLimX(iw,1,:), uLimX(iw,nX,:), uLimY(iw,:,1),
+// uLimY(iw,:,nY), uPlusX(iw,1,:), uMinusX(iw,2,:), uPlusX(iw,nX,:), uMinusX(iw,nX+1,:),
+// uPlusY(iw,:,1), uMinusY(iw,:,2), uPlusY(iw,:,nY), uMinusY(iw,:,nY+1).
+enum GEdge { GE_LX1 = 0, GE_LXN, GE_LY1, GE_LYN, GE_PX1, GE_MX2, GE_PXN, GE_MXN1, GE_PY1, GE_MY2, GE_PYN, GE_MYN1, GE_COUNT };
+
+constexpr int MAX_SRC = KG_MAX_SOURCES;
+constexpr int MAX_SER = KG_MAX_SERIES;
+
+struct DevSource {
+    double x, y, R;
+    int n, ncells;
+    double time[MAX_SER], flux[MAX_SER], psi[MAX_SER];
+};
+
+struct BlockDesc {
+    int slot, x0, y0, tile;  // tile: 1-based reference tile ID
+};
+
+struct DevArrays {
+    int cap;                   // slot capacity
+    int nE;                    // max(nX, nY)
+    double* Q[4];
+    double* E0;
+    double* I0;
+    double* UV;
+    double* CT;
+    double* FX;
+    double* FY;
+    double* BV;
+    double* G9;
+    double* GE;
+    double* MX;
+    int* nbr;                  // [cap][8] neighbour slots (-1: none)
+    int8_t* kind;              // SlotKind per slot
+    int8_t* has_source;        // containsSource per slot
+    int* tile_of_slot;         // 1-based tile id
+};
+
+// Per-launch control for the fused hydraulic kernels.
+enum Mode { MODE_RHS0 = 0, MODE_S1 = 1, MODE_S2 = 2, MODE_S3 = 3 };
+struct StepArgs {
+    int mode;
+    int q_in;        // state buffer read as q0 (the reference's intermed0 / tileContainer)
+    int q_out;       // buffer written by S3 (the new solution)
+    double dt;       // hydraulic dt of this attempt
+    double t_rhs;    // time passed to ConstructHydraulicRHS
+    double t_grid;   // grid%t (for the flux-source end-point logic)
+    double t_max;    // nextT stamped into the maxima (S3)
+    int do_maxima;
+    unsigned long long* cfl_min;  // ordered-bits min of the tile CFL terms
+};
+
+}  // namespace kg

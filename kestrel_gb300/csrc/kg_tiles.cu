@@ -1,0 +1,355 @@
+// kg_tiles.cu -- tile set-up, activation and accounting kernels.
+//
+//   k_cell_topo     ComputeCellCentredTopographicData   src/MorphodynamicRHS.f90:308-366
+//   k_face_bI       InterpolateB at every face           src/HydraulicRHS.f90:741-753
+//   k_face_topo     ComputeInterfacialTopographicData    src/MorphodynamicRHS.f90:419-540
+//   k_ghost_bc      UpdateGhostTileBCs                   src/UpdateTiles.f90:571-664
+//   k_ghost_edges   ReconstructwAtEdges                  src/UpdateTiles.f90:669-750
+//   k_activate      ActivateTile's w = b, bt = 0         src/UpdateTiles.f90:342-370
+//   k_act_flags     the per-direction tests of CheckIfNearBoundaries
+//                                                        src/TimeStepper.f90:924-1150
+//   k_volume        CalculateVolume's four compensated sums, in the reference's order
+//                                                        src/Output.f90:617-737
+#include <cuda_runtime.h>
+#include "kg_engine.cuh"
+
+namespace kg {
+
+// cP (the run settings in constant memory) is defined in kg_hydro.cu; both files are
+// compiled as one translation unit through kg_lib.cu.
+
+__device__ __forceinline__ size_t pl(int slot, int nf, int f, int npl) { return ((size_t)slot * nf + f) * (size_t)npl; }
+
+// One CTA per listed slot.
+__global__ void k_cell_topo(DevArrays A, const int* __restrict__ slots) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
+    const double* b0 = A.BV + pl(s, 2, 0, SV);
+    const double* bt = A.BV + pl(s, 2, 1, SV);
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        int i = c % nX, j = c / nX;
+        int v00 = j * (nX + 1) + i, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
+        double b0c = 0.25 * kahan4(b0[v00], b0[v10], b0[v01], b0[v11]);
+        double btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
+        double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
+        double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
+        A.CT[pl(s, 4, 0, SC) + c] = b0c;
+        A.CT[pl(s, 4, 1, SC) + c] = btc;
+        A.CT[pl(s, 4, 2, SC) + c] = 0.5 * P.dxR * kahan8(ax);
+        A.CT[pl(s, 4, 3, SC) + c] = 0.5 * P.dyR * kahan8(ay);
+    }
+}
+
+__global__ void k_face_bI(DevArrays A, const int* __restrict__ slots) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int nX = P.nX, nY = P.nY, SV = (nX + 1) * (nY + 1), SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
+    const double* b0 = A.BV + pl(s, 2, 0, SV);
+    const double* bt = A.BV + pl(s, 2, 1, SV);
+    for (int f = threadIdx.x; f < SFX; f += blockDim.x) {
+        int a = f % (nX + 1), j = f / (nX + 1);
+        int v0 = j * (nX + 1) + a, v1 = v0 + (nX + 1);
+        A.FX[pl(s, 5, 4, SFX) + f] = interp_b(b0[v0], b0[v1], bt[v0], bt[v1]);
+    }
+    for (int f = threadIdx.x; f < SFY; f += blockDim.x) {
+        int i = f % nX, a = f / nX;
+        int v0 = a * (nX + 1) + i, v1 = v0 + 1;
+        A.FY[pl(s, 5, 4, SFY) + f] = interp_b(b0[v0], b0[v1], bt[v0], bt[v1]);
+    }
+}
+
+// Face bt and slopes of one tile from its own vertices and the adjacent column/row of
+// the W/E/S/N tiles' vertex copies.
+__global__ void k_face_topo(DevArrays A, const int* __restrict__ slots) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int nX = P.nX, nY = P.nY, SV = (nX + 1) * (nY + 1), SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
+    int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sS = A.nbr[s * 8 + NB_S], sN = A.nbr[s * 8 + NB_N];
+    const double* b0 = A.BV + pl(s, 2, 0, SV);
+    const double* bt = A.BV + pl(s, 2, 1, SV);
+    const int V = nX + 1;
+    for (int f = threadIdx.x; f < SFX; f += blockDim.x) {
+        int a = f % (nX + 1), j = f / (nX + 1);  // vertex column a, rows j..j+1
+        // d/dx from the vertex columns either side (the W/E tile's copy at the tile edge)
+        const double *lb0 = b0, *lbt = bt, *rb0 = b0, *rbt = bt;
+        int la = a - 1, ra = a + 1;
+        if (a == 0) { lb0 = A.BV + pl(sW, 2, 0, SV); lbt = A.BV + pl(sW, 2, 1, SV); la = nX - 1; }
+        if (a == nX) { rb0 = A.BV + pl(sE, 2, 0, SV); rbt = A.BV + pl(sE, 2, 1, SV); ra = 1; }
+        double ax[8] = {rb0[j * V + ra], rbt[j * V + ra], rb0[(j + 1) * V + ra], rbt[(j + 1) * V + ra],
+                        -lb0[j * V + la], -lbt[j * V + la], -lb0[(j + 1) * V + la], -lbt[(j + 1) * V + la]};
+        double dbdx = 0.25 * P.dxR * kahan8(ax);
+        int v0 = j * V + a, v1 = v0 + V;
+        double btf = 0.5 * (bt[v0] + bt[v1]);
+        double ay[4] = {b0[v1], bt[v1], -b0[v0], -bt[v0]};
+        double dbdy = P.dyR * kahan4(ay[0], ay[1], ay[2], ay[3]);
+        A.FX[pl(s, 5, 1, SFX) + f] = btf;
+        A.FX[pl(s, 5, 2, SFX) + f] = dbdx;
+        A.FX[pl(s, 5, 3, SFX) + f] = dbdy;
+    }
+    for (int f = threadIdx.x; f < SFY; f += blockDim.x) {
+        int i = f % nX, a = f / nX;  // vertex row a, columns i..i+1
+        int v0 = a * V + i, v1 = v0 + 1;
+        double btf = 0.5 * (bt[v0] + bt[v1]);
+        double axv[4] = {b0[v1], bt[v1], -b0[v0], -bt[v0]};
+        double dbdx = P.dxR * kahan4(axv[0], axv[1], axv[2], axv[3]);
+        const double *db0 = b0, *dbt = bt, *ub0 = b0, *ubt = bt;
+        int da = a - 1, ua = a + 1;
+        if (a == 0) { db0 = A.BV + pl(sS, 2, 0, SV); dbt = A.BV + pl(sS, 2, 1, SV); da = nY - 1; }
+        if (a == nY) { ub0 = A.BV + pl(sN, 2, 0, SV); ubt = A.BV + pl(sN, 2, 1, SV); ua = 1; }
+        double ay[8] = {ub0[ua * V + i + 1], ubt[ua * V + i + 1], ub0[ua * V + i], ubt[ua * V + i],
+                        -db0[da * V + i + 1], -dbt[da * V + i + 1], -db0[da * V + i], -dbt[da * V + i]};
+        double dbdy = 0.25 * P.dyR * kahan8(ay);
+        A.FY[pl(s, 5, 1, SFY) + f] = btf;
+        A.FY[pl(s, 5, 2, SFY) + f] = dbdx;
+        A.FY[pl(s, 5, 3, SFY) + f] = dbdy;
+    }
+}
+
+// mode 0: default data (w = b0, rho = rhow, rest 0; SetDefaultTileData); 2: a periodic
+// domain-edge ghost, which SetDomainBoundaryData leaves as allocated (zeros, rho = rhow).
+__global__ void k_ghost_bc(DevArrays A, int slot, int mode) {
+    const DevParams& P = cP;
+    int SC = P.nX * P.nY;
+    double* G = A.G9 + pl(slot, 9, 0, SC);
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        for (int f = 0; f < 8; ++f) G[f * (size_t)SC + c] = 0.0;
+        G[8 * (size_t)SC + c] = P.rhow;
+        if (mode == 0) G[c] = A.CT[pl(slot, 4, 0, SC) + c];
+    }
+}
+
+// Dirichlet data (SetDomainBoundaryData 'dirichlet', src/UpdateTiles.f90:614-638).
+__global__ void k_ghost_dirichlet(DevArrays A, int slot, double Hnval, double uval, double vval, double psival) {
+    const DevParams& P = cP;
+    int SC = P.nX * P.nY;
+    double* G = A.G9 + pl(slot, 9, 0, SC);
+    double rho = density(P, psival);
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        double b0 = A.CT[pl(slot, 4, 0, SC) + c], bt = A.CT[pl(slot, 4, 1, SC) + c];
+        double dbx = A.CT[pl(slot, 4, 2, SC) + c], dby = A.CT[pl(slot, 4, 3, SC) + c];
+        double hpval = Hnval / gam_of(P.geo, dbx, dby);
+        double w = bt + hpval;
+        w = w + b0;
+        G[c] = w;
+        G[1 * (size_t)SC + c] = rho * Hnval * uval;
+        G[2 * (size_t)SC + c] = rho * Hnval * vval;
+        G[3 * (size_t)SC + c] = Hnval * psival;
+        G[4 * (size_t)SC + c] = Hnval;
+        G[5 * (size_t)SC + c] = uval;
+        G[6 * (size_t)SC + c] = vval;
+        G[7 * (size_t)SC + c] = psival;
+        G[8 * (size_t)SC + c] = rho;
+    }
+}
+
+// ReconstructwAtEdges for one ghost slot; edge bit k set when that neighbour (W,E,S,N) is
+// an active tile whose current w lives in Q[qcur].
+__global__ void k_ghost_edges(DevArrays A, int slot, int mask, int qcur) {
+    const DevParams& P = cP;
+    int nX = P.nX, nY = P.nY, SC = nX * nY, nE = A.nE;
+    const double* w = A.G9 + pl(slot, 9, 0, SC);
+    double* GE = A.GE + pl(slot, GE_COUNT, 0, nE);
+    const double* Qc = A.Q[qcur];
+    int lim = P.limiter;
+    double dx = P.dx, dy = P.dy;
+    for (int k = threadIdx.x; k < nY; k += blockDim.x) {
+        int j = k;
+        if (mask & 1) {
+            int nb = A.nbr[slot * 8 + NB_W];
+            double uW = Qc[pl(nb, 4, 0, SC) + j * nX + nX - 1];
+            double l = P.dxR * limiter(lim, w[j * nX + 1] - w[j * nX], w[j * nX] - uW);
+            GE[GE_LX1 * nE + j] = l;
+            GE[GE_PX1 * nE + j] = w[j * nX] - l * 0.5 * dx;
+            GE[GE_MX2 * nE + j] = w[j * nX] + l * 0.5 * dx;
+        }
+        if (mask & 2) {
+            int nb = A.nbr[slot * 8 + NB_E];
+            double uE = Qc[pl(nb, 4, 0, SC) + j * nX + 0];
+            double l = P.dxR * limiter(lim, uE - w[j * nX + nX - 1], w[j * nX + nX - 1] - w[j * nX + nX - 2]);
+            GE[GE_LXN * nE + j] = l;
+            GE[GE_PXN * nE + j] = w[j * nX + nX - 1] - l * 0.5 * dx;
+            GE[GE_MXN1 * nE + j] = w[j * nX + nX - 1] + l * 0.5 * dx;
+        }
+    }
+    for (int i = threadIdx.x; i < nX; i += blockDim.x) {
+        if (mask & 4) {
+            int nb = A.nbr[slot * 8 + NB_S];
+            double uS = Qc[pl(nb, 4, 0, SC) + (nY - 1) * nX + i];
+            double l = P.dyR * limiter(lim, w[nX + i] - w[i], w[i] - uS);
+            GE[GE_LY1 * nE + i] = l;
+            GE[GE_PY1 * nE + i] = w[i] - l * 0.5 * dy;
+            GE[GE_MY2 * nE + i] = w[i] + l * 0.5 * dy;
+        }
+        if (mask & 8) {
+            int nb = A.nbr[slot * 8 + NB_N];
+            double uN = Qc[pl(nb, 4, 0, SC) + 0 * nX + i];
+            double wt = w[(nY - 1) * nX + i], wb = w[(nY - 2) * nX + i];
+            double l = P.dyR * limiter(lim, uN - wt, wt - wb);
+            GE[GE_LYN * nE + i] = l;
+            GE[GE_PYN * nE + i] = wt - l * 0.5 * dy;
+            GE[GE_MYN1 * nE + i] = wt + l * 0.5 * dy;
+        }
+    }
+}
+
+// ActivateTile: w = cell b0, cell bt = 0, momenta and Hnpsi as the tile held them (zero).
+__global__ void k_activate(DevArrays A, int slot, int qcur) {
+    const DevParams& P = cP;
+    int SC = P.nX * P.nY;
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        double b0 = A.CT[pl(slot, 4, 0, SC) + c];
+        A.CT[pl(slot, 4, 1, SC) + c] = 0.0;
+        for (int b = 0; b < 2; ++b) {
+            double* Q = A.Q[b == 0 ? qcur : 1 - qcur];
+            Q[pl(slot, 4, 0, SC) + c] = b0;
+            Q[pl(slot, 4, 1, SC) + c] = 0.0;
+            Q[pl(slot, 4, 2, SC) + c] = 0.0;
+            Q[pl(slot, 4, 3, SC) + c] = 0.0;
+        }
+        A.UV[pl(slot, 2, 0, SC) + c] = 0.0;
+        A.UV[pl(slot, 2, 1, SC) + c] = 0.0;
+    }
+}
+
+__global__ void k_init_maxima(DevArrays A, int slot) {
+    int SC = cP.nX * cP.nY;
+    double* M = A.MX + pl(slot, 11, 0, SC);
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        for (int f = 0; f < 10; ++f) M[f * (size_t)SC + c] = 0.0;
+        M[10 * (size_t)SC + c] = -1.0;
+    }
+}
+
+// Edge-band tests of NearNorth/South/East/WestBoundary for each listed active slot:
+// bit 0 N, 1 S, 2 E, 3 W.  hn_over (optional) replaces the depth computed from w (used
+// for the first check after the sources have set the depth field directly).
+__global__ void k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur, const double* __restrict__ hn_over,
+                            int* __restrict__ flags) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int nX = P.nX, nY = P.nY, SC = nX * nY, TB = P.TileBuffer;
+    const double* Q = A.Q[qcur];
+    int f = 0;
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        int i = c % nX, j = c / nX;
+        double Hn;
+        if (hn_over) {
+            Hn = hn_over[(size_t)s * SC + c];
+        } else {
+            double b0 = A.CT[pl(s, 4, 0, SC) + c], bt = A.CT[pl(s, 4, 1, SC) + c];
+            double gam = gam_of(P.geo, A.CT[pl(s, 4, 2, SC) + c], A.CT[pl(s, 4, 3, SC) + c]);
+            Hn = compute_hn(Q[pl(s, 4, 0, SC) + c], b0, bt, gam);
+            if (Hn < 0.0) Hn = 0.0;
+        }
+        if (Hn > P.hThr) {
+            int jj = j + 1, ii = i + 1;
+            if (jj > nY - TB) f |= 1;
+            if (jj <= TB) f |= 2;
+            if (ii > nX - TB) f |= 4;
+            if (ii <= TB) f |= 8;
+        }
+    }
+    // The reference's scans start from ydist = 0 (N, E) or nY/nX (S, W), so a buffer
+    // wider than the tile triggers without any wet cell.
+    if (threadIdx.x == 0) {
+        if (0 > nY - TB) f |= 1;
+        if (nY <= TB) f |= 2;
+        if (0 > nX - TB) f |= 4;
+        if (nX <= TB) f |= 8;
+    }
+    __shared__ int red;
+    if (threadIdx.x == 0) red = 0;
+    __syncthreads();
+    if (f) atomicOr(&red, f);
+    __syncthreads();
+    if (threadIdx.x == 0) flags[blockIdx.x] = red;
+}
+
+// Sequential compensated sums over the active tiles in list order (j outer, i inner).
+__global__ void k_volume(DevArrays A, const int* __restrict__ slots, int n, int qcur, const double* __restrict__ hn_over,
+                         const double* __restrict__ rho_over, double* out) {
+    const DevParams& P = cP;
+    int nX = P.nX, nY = P.nY, SC = nX * nY;
+    const double* Q = A.Q[qcur];
+    double vol = 0, mass = 0, bed = 0, sol = 0, cv = 0, cm = 0, cb = 0, cs = 0;
+    double e2 = P.hThr * P.hThr;
+    for (int k = 0; k < n; ++k) {
+        int s = slots[k];
+        for (int c = 0; c < SC; ++c) {
+            double w = Q[pl(s, 4, 0, SC) + c], p = Q[pl(s, 4, 3, SC) + c];
+            double b0 = A.CT[pl(s, 4, 0, SC) + c], bt = A.CT[pl(s, 4, 1, SC) + c];
+            double gam = gam_of(P.geo, A.CT[pl(s, 4, 2, SC) + c], A.CT[pl(s, 4, 3, SC) + c]);
+            double Hn, rho;
+            if (hn_over) {
+                Hn = hn_over[(size_t)s * SC + c];
+                rho = rho_over[(size_t)s * SC + c];
+            } else {
+                Hn = compute_hn(w, b0, bt, gam);
+                if (Hn < 0.0) Hn = 0.0;
+                double pp = p < 0.0 ? 0.0 : p;
+                double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
+                rho = density(P, psi);
+            }
+            double dv = (w - b0 - bt) * gam * gam;
+            kahan_add(dv, vol, cv);
+            kahan_add(rho * Hn * gam, mass, cm);
+            kahan_add(bt, bed, cb);
+            kahan_add(p * gam, sol, cs);
+        }
+    }
+    out[0] = vol * P.dx * P.dy;
+    out[1] = bed * P.dx * P.dy;
+    out[2] = mass * P.dx * P.dy;
+    out[3] = sol * P.dx * P.dy;
+}
+
+// ---- host launchers ----
+cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_cell_topo<<<n, 256, 0, st>>>(A, d_slots);
+    return cudaGetLastError();
+}
+cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_face_bI<<<n, 256, 0, st>>>(A, d_slots);
+    return cudaGetLastError();
+}
+cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_face_topo<<<n, 256, 0, st>>>(A, d_slots);
+    return cudaGetLastError();
+}
+cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, cudaStream_t st) {
+    k_ghost_bc<<<1, 256, 0, st>>>(A, slot, mode);
+    return cudaGetLastError();
+}
+cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, double u, double v, double psi, cudaStream_t st) {
+    k_ghost_dirichlet<<<1, 256, 0, st>>>(A, slot, H, u, v, psi);
+    return cudaGetLastError();
+}
+cudaError_t launch_ghost_edges(const DevArrays& A, int slot, int mask, int qcur, cudaStream_t st) {
+    k_ghost_edges<<<1, 256, 0, st>>>(A, slot, mask, qcur);
+    return cudaGetLastError();
+}
+cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, cudaStream_t st) {
+    k_activate<<<1, 256, 0, st>>>(A, slot, qcur);
+    return cudaGetLastError();
+}
+cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st) {
+    k_init_maxima<<<1, 256, 0, st>>>(A, slot);
+    return cudaGetLastError();
+}
+cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, const double* hn_over, int* d_flags,
+                             cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_act_flags<<<n, 256, 0, st>>>(A, d_slots, qcur, hn_over, d_flags);
+    return cudaGetLastError();
+}
+cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, const double* hn, const double* rho,
+                          double* d_out, cudaStream_t st) {
+    k_volume<<<1, 1, 0, st>>>(A, d_slots, n, qcur, hn, rho, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace kg

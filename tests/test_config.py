@@ -1,0 +1,56 @@
+"""Input-file parsing: the reference's keys and defaults (src/*Settings.f90, Parameters.f90)."""
+import math
+
+import pytest
+
+from kestrel_gb300 import abi, config
+
+
+def test_defaults_match_reference():
+    p = config.default_params()
+    assert p.limiter == abi.LIMITER["minmod2"] and p.heightThreshold == 1e-6 and p.TileBuffer == 1
+    assert p.cfl == 0.25 and p.SpongeStrength == 0.2 and p.g == 9.81 and p.ChezyCo == 0.01
+    assert p.ManningCo == 0.03 and p.CoulombCo == 0.1 and p.PouliquenBeta == 0.136
+    assert p.maxPack == 0.65 and p.rhow == 1000 and p.rhos == 2000 and p.BedPorosity == 0.35
+    assert p.SolidDiameter == 1e-3 and p.EddyViscosity == 0.0
+    # Erosion defaults to Mixed and switches morphodynamics on (src/Parameters.f90:573-577).
+    assert p.erosion == abi.EROSION["mixed"] and p.MorphodynamicsOn == 1
+
+
+def test_parse_reference_input():
+    import cases
+    p = cases.ref_input("flux_hydro_2d")
+    assert (p.nXtiles, p.nYtiles, p.nXpertile, p.nYpertile) == (40, 40, 50, 50)
+    assert p.Xtilesize == 50 and p.Ytilesize == 50
+    assert p.nSources == 1 and p.sources[0].n_series == 2 and p.sources[0].flux[1] == 10.0
+    assert p.drag == abi.DRAG["chezy"] and p.MorphodynamicsOn == 0
+    assert p.topog == abi.TOPO["xslope"] and p.topog_params[0] == -0.1
+
+
+def test_cap_volume_relations():
+    txt = """Domain:
+nXtiles = 4
+nYtiles = 4
+nXpertile = 8
+nYpertile = 8
+Xtilesize = 8
+Cap:
+  capX = 0
+  capY = 0
+  capRadius = 2
+  capVolume = 10
+  capShape = para
+Solver:
+T end = 1
+Topog:
+Type = Function
+Topog function = flat
+"""
+    p = config.parse(txt).params
+    assert math.isclose(p.caps[0].height, 2.0 * 10 / math.pi / 2 / 2)
+
+
+def test_rejects_unknown_drag():
+    with pytest.raises(config.InputError):
+        config.parse("Domain:\nnXtiles = 1\nnYtiles = 1\nnXpertile = 4\nnYpertile = 4\nXtilesize = 4\n"
+                     "Parameters:\nDrag = Bogus\nSolver:\nT end = 1\n")

@@ -1,0 +1,146 @@
+"""Pins the oracle to the reference's own test suite (tests/runall.jl, tests/testlib.jl).
+
+The reference ships no golden output vectors; its tests are invariant checks on full runs
+of its own input files.  Each check below restates one of them and runs it on the same
+input files (shortened end times where the full run would take minutes, noted inline):
+
+- check_conservativity   (testlib.jl:106-158)  relative volume/solids error <= 1e-10
+- check_positivity       (testlib.jl:286-302)  flow depth >= -1e-14
+- check_max_ero_depth    (testlib.jl:306-328)  bt >= -Erosion Depth
+- check_no_flow          (testlib.jl:332-358)  lake at rest: depth unchanged at print precision
+- check_identical_simulations (testlib.jl:363-407, runall.jl:45-46) tile-layout independence
+"""
+import numpy as np
+import pytest
+
+import _oracle
+import cases
+
+
+def integrate_source_time_series(t, Q, psi, tstart, tend):
+    """Trapezium/exact-product integral of the flux hydrograph (testlib.jl:231-281)."""
+    total = 0.0
+    solids = 0.0
+    if len(t) == 1 and t[0] < tend:
+        duration = min(tend - tstart, tend - t[0])
+        total = Q[0] * duration
+        solids = psi[0] * total
+    for i in range(len(t) - 1):
+        if t[i + 1] < tstart or t[i] > tend:
+            continue
+        dQdt = (Q[i + 1] - Q[i]) / (t[i + 1] - t[i])
+        dpdt = (psi[i + 1] - psi[i]) / (t[i + 1] - t[i])
+        tl, tu, Ql, Qu, pl, pu = t[i], t[i + 1], Q[i], Q[i + 1], psi[i], psi[i + 1]
+        if t[i] < tstart:
+            tl, Ql, pl = tstart, Q[i] + dQdt * (tstart - t[i]), psi[i] + dpdt * (tstart - t[i])
+        if t[i + 1] > tend:
+            tu, Qu, pu = tend, Q[i] + dQdt * (tend - t[i]), psi[i] + dpdt * (tend - t[i])
+        dt = tu - tl
+        total += dt * (Ql + Qu) / 2
+        solids += (dt / 6) * (Ql * pu + Qu * pl + 2 * (Ql * pl + Qu * pu))
+    return total, solids
+
+
+def flux_totals(p):
+    vol = sol = 0.0
+    for k in range(p.nSources):
+        s = p.sources[k]
+        n = s.n_series
+        a, b = integrate_source_time_series(list(s.time[:n]), list(s.flux[:n]), list(s.psi[:n]), p.tstart, p.tend)
+        vol += a
+        sol += b
+    return vol, sol
+
+
+def check_conservation(p, sim_factory):
+    sim = sim_factory(p)
+    v0 = sim.volume()
+    sim.run()
+    v1 = sim.volume()
+    fv, fs = flux_totals(p)
+    phi = p.BedPorosity
+    expected = fv + v0[0] + v0[1]
+    final = v1[0] + v1[1]
+    vol_err = abs((expected - final) / expected)
+    exp_s = fs + v0[3] + v0[1] * (1 - phi)
+    fin_s = v1[3] + v1[1] * (1 - phi)
+    sol_err = abs(exp_s - fin_s) if exp_s == 0.0 else abs((exp_s - fin_s) / exp_s)
+    return sim, vol_err, sol_err
+
+
+CONSERVATION = [
+    ("cap_dilute_2d", 8.0, 5),          # full run
+    ("cap_conc_2d", 2.0, 2),            # T end 4 in the reference
+    ("cap_morpho_2d", 1.0, 2),          # T end 5 in the reference
+    ("flux_hydro_2d", 3.0, 3),          # T end 10 in the reference
+    ("flux_edwards2019_2d", 3.0, 3),    # T end 10 in the reference
+    ("flux_morpho_2d", 2.0, 2),         # T end 5 in the reference
+    ("flat_depositional_2d", 2.0, 2),   # T end 100 in the reference
+]
+
+
+@pytest.mark.parametrize("name,tend,nout", CONSERVATION)
+def test_oracle_flow_consistency(name, tend, nout):
+    p = cases.ref_input(name, tend=tend, nout=nout)
+    sim, vol_err, sol_err = check_conservation(p, _oracle.simulation)
+    assert vol_err <= 1e-10, vol_err
+    assert sol_err <= 1e-10, sol_err
+    for t in sim.active_tiles():
+        assert sim.field(t, 5).min() >= -1e-14
+        if p.MorphodynamicsOn:
+            assert sim.field(t, 11).min() >= -p.EroDepth
+
+
+@pytest.mark.parametrize("name", ["lake_at_rest_hydro_2d", "lake_at_rest_morpho_2d"])
+def test_oracle_lake_at_rest(name):
+    p = cases.ref_input(name)  # full run (T end 5, 10 outputs)
+    sim = _oracle.simulation(p)
+    fmt = np.vectorize(lambda v: "%.10E" % v)
+    h0 = {t: fmt(sim.field(t, 5)) for t in sim.active_tiles()}
+    for i in range(1, p.Nout + 1):
+        sim.integrate_to(p.tstart + i * (p.tend - p.tstart) / p.Nout)
+        for t, ref in h0.items():
+            assert (fmt(sim.field(t, 5)) == ref).all()
+
+
+def _rows(sim):
+    rows = []
+    for t in sim.active_tiles():
+        rows.append(np.stack([sim.field(t, 5).ravel(), sim.field(t, 6).ravel(), sim.field(t, 4).ravel(),
+                              sim.field(t, 11).ravel()], 1))
+    return np.concatenate(rows)
+
+
+def _sorted(r):
+    return r[np.lexsort(r.T[::-1])]
+
+
+def _printed(r):
+    return np.array([[float("%.10E" % v) for v in row] for row in r])
+
+
+@pytest.mark.parametrize("a,b,tol,tend", [
+    ("tile_indep_static_100m", "tile_indep_static_50m", 1e-13, 0.3),    # T end 4 in the reference
+    ("tile_indep_dynamic_100m", "tile_indep_dynamic_20m", 1e-11, 1.0),  # T end 5 in the reference
+])
+def test_oracle_tile_independence(a, b, tol, tend):
+    ra, rb = [], []
+    for name, out in ((a, ra), (b, rb)):
+        p = cases.ref_input(name, tend=tend, nout=1)
+        sim = _oracle.simulation(p)
+        sim.run()
+        out.append(_rows(sim))
+    fa, fb = _sorted(_printed(ra[0])), _sorted(_printed(rb[0]))
+    n = min(len(fa), len(fb))
+    assert np.max(np.abs(fa[-n:] - fb[-n:])) <= tol
+
+
+def test_oracle_sources_and_activation_counts():
+    """Cap placement activates exactly the tiles the cap covers, and NumCellsInSrc counts
+    cell centres with R^2 <= r^2 (src/SetSources.f90:362-368)."""
+    p = cases.ref_input("flux_hydro_2d", tend=0.5, nout=1)
+    sim = _oracle.simulation(p)
+    act = sim.active_tiles()
+    assert act == sorted(act)
+    assert len(act) == 4
+    assert len(sim.ghost_tiles()) == 12
