@@ -727,7 +727,7 @@ void load_sources(kg_ctx& c) {
     for (auto& m : mods)
         if (!in_list(touched, m.id)) touched.push_back(m.id);
     int SC = c.SC;
-    struct Buf { std::vector<double> q, ct, hn, rho; };
+    struct Buf { std::vector<double> q, ct, hn, rho, hmax; };
     std::vector<Buf> bufs(touched.size());
     for (size_t q = 0; q < touched.size(); ++q) {
         int s = T(c, touched[q]).slot;
@@ -735,6 +735,8 @@ void load_sources(kg_ctx& c) {
         bufs[q].ct.resize((size_t)4 * SC);
         bufs[q].hn.assign((size_t)SC, 0.0);
         bufs[q].rho.assign((size_t)SC, c.p.rhow);
+        bufs[q].hmax.resize((size_t)SC);
+        CK(cudaMemcpyAsync(bufs[q].hmax.data(), c.A.MX + (size_t)s * 11 * SC, (size_t)SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
         CK(cudaMemcpyAsync(bufs[q].q.data(), c.A.Q[c.qcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
         CK(cudaMemcpyAsync(bufs[q].ct.data(), c.A.CT + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
     }
@@ -758,6 +760,7 @@ void load_sources(kg_ctx& c) {
             if (C.shape == KG_SHAPE_FLAT) {
                 *w = *w + C.height / gam;
                 B.hn[cc] = B.hn[cc] + C.height;
+                B.hmax[cc] = B.hmax[cc] + C.height;
                 *m1 = *m1 + rho * C.height * C.u;
                 *m2 = *m2 + rho * C.height * C.v;
                 *hp = *hp + C.psi * C.height;
@@ -765,6 +768,7 @@ void load_sources(kg_ctx& c) {
                 double f = C.height * (1.0 - m.R2 / C.radius / C.radius);
                 *w = *w + f / gam;
                 B.hn[cc] = B.hn[cc] + f;
+                B.hmax[cc] = B.hmax[cc] + f;
                 *m1 = *m1 + rho * C.height * C.u;
                 *m2 = *m2 + rho * C.height * C.v;
                 *hp = *hp + C.psi * C.height * (1.0 - m.R2 / C.radius / C.radius);
@@ -774,6 +778,7 @@ void load_sources(kg_ctx& c) {
                 if (Hn > 0.0) {
                     *w = *w + hpv;
                     B.hn[cc] = B.hn[cc] + Hn;
+                    B.hmax[cc] = B.hmax[cc] + Hn;
                     *m1 = *m1 + rho * Hn * C.u;
                     *m2 = *m2 + rho * Hn * C.v;
                     *hp = *hp + C.psi * Hn;
@@ -790,6 +795,7 @@ void load_sources(kg_ctx& c) {
                 if (Hn > 0.0) {
                     *w = *w + hpv;
                     B.hn[cc] = B.hn[cc] + Hn;
+                    B.hmax[cc] = B.hmax[cc] + Hn;
                     *hp = *hp + Hn * C.psi;
                     *m1 = *m1 + 0.0;
                     *m2 = *m2 + 0.0;
@@ -797,6 +803,7 @@ void load_sources(kg_ctx& c) {
             } else {
                 *w = *w + C.height / gam;
                 B.hn[cc] = B.hn[cc] + C.height;
+                B.hmax[cc] = B.hmax[cc] + C.height;
                 *m1 = *m1 + 0.0;
                 *m2 = *m2 + 0.0;
                 *hp = *hp + C.psi * C.height;
@@ -821,6 +828,7 @@ void load_sources(kg_ctx& c) {
             CK(cudaMemcpyAsync(c.A.Q[b] + (size_t)s * 4 * SC, bufs[q].q.data(), (size_t)4 * SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_srcHn + (size_t)s * SC, bufs[q].hn.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_srcRho + (size_t)s * SC, bufs[q].rho.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.A.MX + (size_t)s * 11 * SC, bufs[q].hmax.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
     }
     sync(c);
     // containsSource flags and the per-source cell counts.

@@ -146,17 +146,21 @@ def test_maxima_and_inundation_time():
             assert np.array_equal(g.maxima(t, w), o.maxima(t, w)), (t, w)
 
 
-def test_full_cap_release_to_30s_properties():
-    """The 256x256 cap release to t = 30 s: volume conserved to roundoff, depth >= 0,
-    and the GPU state equals the oracle's at an intermediate time (oracle checked to
-    t = 3 s to keep the CPU side short)."""
+def test_full_cap_release_to_30s():
+    """The 256x256 cap release to t = 30 s on the GPU.  Volume leaves through the sponge
+    edges (the cap's southern rim starts 8 m from the inactive edge row), so the check is
+    against the oracle: identical state and identical volume accounting at t = 3 s; then
+    the full run to 30 s keeps depth >= 0 and a finite state."""
+    p = cases.cap_release_256(tend=3.0, nout=3)
+    g, o = pair(p)
+    g.run()
+    o.run()
+    compare_state(g, o, what="cap_release_3s")
+    assert np.array_equal(g.volume(), o.volume())
     p = cases.cap_release_256(tend=30.0, nout=10)
     g = lib.simulation(p)
-    v0 = g.volume()
     g.run()
-    v1 = g.volume()
-    assert abs(v1[0] - v0[0]) / v0[0] <= 1e-12
+    assert g.time[0] == 30.0
     for t in g.active_tiles():
-        w, b = g.field(t, 1), g.field(t, 10)
         assert (g.field(t, 5) >= 0).all()
-        assert np.isfinite(w).all()
+        assert np.isfinite(g.field(t, 1)).all() and np.isfinite(g.field(t, 2)).all()
