@@ -105,13 +105,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(params, seconds=15.0, max_steps=100000):
+def cpu_baseline(params, b0=None, seconds=15.0, max_steps=100000):
     """Oracle timed on a bounded sample: accepted steps from t = 0 until ~`seconds`."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle
     from kestrel_gb300 import abi
     L = _oracle.load()
-    sim = _oracle.simulation(params)
+    sim = _oracle.simulation(params, b0=b0)
     total_cu, total_s, steps = 0, 0.0, 0
     rc = C.c_int32(0)
     while total_s < seconds and steps < max_steps:
@@ -131,11 +131,12 @@ def cpu_baseline(params, seconds=15.0, max_steps=100000):
 
 def run_reference(args, wl):
     from kestrel_gb300 import abi  # noqa: F401
-    p = wl["params"]()
+    made = wl["params"]()
+    p, b0 = made if isinstance(made, tuple) else (made, None)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle
     L = _oracle.load()
-    sim = _oracle.simulation(p)
+    sim = _oracle.simulation(p, b0=b0)
     rc = C.c_int32(0)
     from kestrel_gb300 import abi as A
     for _ in range(args.warmup):
@@ -187,10 +188,14 @@ def main():
         dist.init_process_group("nccl")
     from kestrel_gb300 import abi, lib
     L = lib.load()
-    p = wl["params"]()
+    made = wl["params"]()
+    p, b0 = made if isinstance(made, tuple) else (made, None)
 
     # ---- device-timed throughput ----
-    sim = lib.simulation(p, precision=wl["prec"])
+    sim = lib.simulation(p, precision=wl["prec"], b0=b0)
+    spin = wl.get("spinup", 0.0)
+    if spin > 0.0:
+        sim.integrate_to(spin)
     stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
     for _ in range(args.warmup):
@@ -242,8 +247,12 @@ def main():
 
     # ---- end to end through the C ABI ----
     t0 = time.perf_counter()
-    sim2 = lib.simulation(p, precision=wl["prec"])
+    sim2 = lib.simulation(p, precision=wl["prec"], b0=b0)
     cu2, n2 = 0, 0
+    if spin > 0.0:
+        st = sim2.integrate_to(spin)
+        cu2 += st.cell_updates
+        n2 += st.steps
     for _ in range(args.warmup + args.steps):
         st = sim2.step(p.tend)
         cu2 += st.cell_updates
@@ -255,7 +264,7 @@ def main():
         for f in (1, 2, 3, 4):
             d2h += sim2.field(t, f).nbytes
     e2e_s = time.perf_counter() - t0
-    h2d = C.sizeof(abi.Params) + 16 * 4 * n2
+    h2d = C.sizeof(abi.Params) + (b0.nbytes if b0 is not None else 0) + 16 * 4 * n2
     d2h += 16 * 4 * n2
     sim2.close()
 
@@ -289,7 +298,7 @@ def main():
         "clocks": clk,
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(p)
+        line["cpu_baseline"] = cpu_baseline(p, b0)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

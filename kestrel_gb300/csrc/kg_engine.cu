@@ -28,18 +28,28 @@ size_t hydro_smem_bytes();
 cudaError_t set_constants(const DevParams& p, const DevSource* src, int nsrc, cudaStream_t st);
 cudaError_t launch_hydro(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st);
 // kg_tiles.cu
-cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, cudaStream_t st);
-cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, cudaStream_t st);
-cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, cudaStream_t st);
-cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, cudaStream_t st);
-cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, double u, double v, double psi, cudaStream_t st);
+cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
+cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
+cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
+cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, int ts, cudaStream_t st);
+cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, double u, double v, double psi, int ts, cudaStream_t st);
 cudaError_t launch_ghost_edges(const DevArrays& A, int slot, int mask, int qcur, cudaStream_t st);
-cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, cudaStream_t st);
+cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, int ts, cudaStream_t st);
 cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st);
-cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, const double* hn_over, int* d_flags,
+cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn_over, int* d_flags,
                              cudaStream_t st);
-cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, const double* hn, const double* rho,
+cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
                           double* d_out, cudaStream_t st);
+// kg_morpho.cu
+cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, cudaStream_t st);
+cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int tnew, cudaStream_t st);
+cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int tcur, int tnew, int stage, double dt, cudaStream_t st);
+cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, cudaStream_t st);
+cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, int* flags,
+                           unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st);
+cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, int n, int qa, int tcur, int tnew, int* flags,
+                            cudaStream_t st);
+cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int qa, cudaStream_t st);
 }  // namespace kg
 
 using namespace kg;
@@ -105,7 +115,16 @@ struct kg_ctx {
     std::vector<double> upload;          // global vertex grid (KG_TOPO_UPLOAD)
     int64_t nx1 = 0, ny1 = 0;
     bool sources_loaded = false;
-    int qcur = 0;
+    int qcur = 0;                        // state buffer holding the solution (0..3)
+    int tcur = 0;                        // topography set of the solution (0..1)
+    std::vector<int> touched;            // slots whose step-start topography changed in set-up
+    int* d_mflags = nullptr;             // M-operator refine flag
+    int* d_ncand = nullptr;
+    unsigned long long* d_ckey = nullptr;
+    double* d_cex = nullptr;
+    int* d_rslot = nullptr;
+    int* d_rcell = nullptr;
+    int cand_cap = 0;
     double t = 0.0, dt = 1.0e-5, t0 = 0.0;
     int64_t launches = 0, steps = 0, rejected = 0, cell_updates = 0;
     bool blocks_dirty = true;
@@ -121,8 +140,8 @@ namespace {
 
 size_t bytes_per_slot(const kg_ctx& c) {
     size_t SC = c.SC;
-    return sizeof(double) * (4 * 4 * SC + 4 * SC + SC + 2 * SC + 4 * SC + 5 * (size_t)c.SFX + 5 * (size_t)c.SFY +
-                             2 * (size_t)c.SV + 9 * SC + GE_COUNT * (size_t)c.nE + 11 * SC + 2 * SC) +
+    return sizeof(double) * (4 * 4 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * (size_t)c.SFX + 5 * (size_t)c.SFY + 2 * (size_t)c.SV) +
+                             2 * SC + 5 * SC + SC + 9 * SC + GE_COUNT * (size_t)c.nE + 11 * SC + 2 * SC) +
            8 * sizeof(int) + 2 + sizeof(int);
 }
 
@@ -145,13 +164,17 @@ void ensure_cap(kg_ctx& c, int need) {
     nc = std::min(nc, std::max(need, c.nTiles));
     size_t o = c.cap, n = nc, SC = c.SC;
     for (int b = 0; b < 4; ++b) grow_array(c.A.Q[b], o * 4 * SC, n * 4 * SC, c.st);
-    grow_array(c.A.E0, o * 4 * SC, n * 4 * SC, c.st);
-    grow_array(c.A.I0, o * SC, n * SC, c.st);
+    for (int b = 0; b < 2; ++b) {
+        grow_array(c.A.E[b], o * 4 * SC, n * 4 * SC, c.st);
+        grow_array(c.A.I[b], o * SC, n * SC, c.st);
+        grow_array(c.A.CT[b], o * 4 * SC, n * 4 * SC, c.st);
+        grow_array(c.A.FX[b], o * 5 * (size_t)c.SFX, n * 5 * (size_t)c.SFX, c.st);
+        grow_array(c.A.FY[b], o * 5 * (size_t)c.SFY, n * 5 * (size_t)c.SFY, c.st);
+        grow_array(c.A.BV[b], o * 2 * (size_t)c.SV, n * 2 * (size_t)c.SV, c.st);
+    }
     grow_array(c.A.UV, o * 2 * SC, n * 2 * SC, c.st);
-    grow_array(c.A.CT, o * 4 * SC, n * 4 * SC, c.st);
-    grow_array(c.A.FX, o * 5 * (size_t)c.SFX, n * 5 * (size_t)c.SFX, c.st);
-    grow_array(c.A.FY, o * 5 * (size_t)c.SFY, n * 5 * (size_t)c.SFY, c.st);
-    grow_array(c.A.BV, o * 2 * (size_t)c.SV, n * 2 * (size_t)c.SV, c.st);
+    grow_array(c.A.MS, o * 5 * SC, n * 5 * SC, c.st);
+    grow_array(c.A.EMD, o * SC, n * SC, c.st);
     grow_array(c.A.G9, o * 9 * SC, n * 9 * SC, c.st);
     grow_array(c.A.GE, o * GE_COUNT * (size_t)c.nE, n * GE_COUNT * (size_t)c.nE, c.st);
     grow_array(c.A.MX, o * 11 * SC, n * 11 * SC, c.st);
@@ -331,9 +354,28 @@ void get_heights(kg_ctx& c, int id) {
             c.hfy0[s][(size_t)a * nX + i] = 0.5 * (b0[(size_t)a * (nX + 1) + i] + b0[(size_t)a * (nX + 1) + i + 1]);
 }
 void push_bed(kg_ctx& c, int s) {
-    CK(cudaMemcpyAsync(c.A.BV + (size_t)s * 2 * c.SV, c.hb0[s].data(), (size_t)c.SV * sizeof(double), cudaMemcpyHostToDevice, c.st));
-    CK(cudaMemcpyAsync(c.A.FX + (size_t)s * 5 * c.SFX, c.hfx0[s].data(), (size_t)c.SFX * sizeof(double), cudaMemcpyHostToDevice, c.st));
-    CK(cudaMemcpyAsync(c.A.FY + (size_t)s * 5 * c.SFY, c.hfy0[s].data(), (size_t)c.SFY * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    // b0 and the face b0 are static: both topography sets hold them.
+    for (int b = 0; b < 2; ++b) {
+        CK(cudaMemcpyAsync(c.A.BV[b] + (size_t)s * 2 * c.SV, c.hb0[s].data(), (size_t)c.SV * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.A.FX[b] + (size_t)s * 5 * c.SFX, c.hfx0[s].data(), (size_t)c.SFX * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.A.FY[b] + (size_t)s * 5 * c.SFY, c.hfy0[s].data(), (size_t)c.SFY * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    }
+}
+void touch(kg_ctx& c, int s) {
+    if (std::find(c.touched.begin(), c.touched.end(), s) == c.touched.end()) c.touched.push_back(s);
+}
+// The second topography set of a slot is scratch for active tiles during a step and a
+// copy of the first for ghost tiles; after set-up work the touched slots are mirrored.
+void mirror_touched(kg_ctx& c) {
+    int o = 1 - c.tcur;
+    for (int s : c.touched) {
+        CK(cudaMemcpyAsync(c.A.CT[o] + (size_t)s * 4 * c.SC, c.A.CT[c.tcur] + (size_t)s * 4 * c.SC, (size_t)4 * c.SC * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+        CK(cudaMemcpyAsync(c.A.FX[o] + (size_t)s * 5 * c.SFX, c.A.FX[c.tcur] + (size_t)s * 5 * c.SFX, (size_t)5 * c.SFX * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+        CK(cudaMemcpyAsync(c.A.FY[o] + (size_t)s * 5 * c.SFY, c.A.FY[c.tcur] + (size_t)s * 5 * c.SFY, (size_t)5 * c.SFY * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+        CK(cudaMemcpyAsync(c.A.BV[o] + (size_t)s * 2 * c.SV, c.A.BV[c.tcur] + (size_t)s * 2 * c.SV, (size_t)2 * c.SV * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+    }
+    c.touched.clear();
+    sync(c);
 }
 // ComputeCellCentredTopographicData for a tile after its vertex b0 changed; InterpolateB
 // is recomputed with it since the reference evaluates that from the vertices on use.
@@ -342,9 +384,10 @@ void cell_topo(kg_ctx& c, int id) {
     push_bed(c, s);
     std::vector<int> one{s};
     upload_list(c, one);
-    CK(launch_cell_topo(c.A, c.d_list, 1, c.st));
-    CK(launch_face_bI(c.A, c.d_list, 1, c.st));
+    CK(launch_cell_topo(c.A, c.d_list, 1, c.tcur, c.st));
+    CK(launch_face_bI(c.A, c.d_list, 1, c.tcur, c.st));
     c.launches += 2;
+    touch(c, s);
     sync(c);
 }
 bool in_list(const std::vector<int>& v, int x) { return std::find(v.begin(), v.end(), x) != v.end(); }
@@ -462,11 +505,11 @@ void add_ghost_tiles(kg_ctx& c, int k) {
         int s = T(c, t).slot;
         if (on_edge(c, t)) {
             if (c.p.bcs == KG_BC_DIRICHLET)
-                CK(launch_ghost_dirichlet(c.A, s, c.p.bcsHnval, c.p.bcsuval, c.p.bcsvval, c.p.bcspsival, c.st));
+                CK(launch_ghost_dirichlet(c.A, s, c.p.bcsHnval, c.p.bcsuval, c.p.bcsvval, c.p.bcspsival, c.tcur, c.st));
             else
-                CK(launch_ghost_default(c.A, s, c.p.bcs == KG_BC_PERIODIC ? 2 : 0, c.st));
+                CK(launch_ghost_default(c.A, s, c.p.bcs == KG_BC_PERIODIC ? 2 : 0, c.tcur, c.st));
         } else {
-            CK(launch_ghost_default(c.A, s, 0, c.st));
+            CK(launch_ghost_default(c.A, s, 0, c.tcur, c.st));
         }
         c.launches++;
         sync(c);
@@ -510,13 +553,14 @@ void add_tile(kg_ctx& c, int k) {
     // ActivateTile
     T(c, k).ghost = false;
     set_kind(c, k, SLOT_ACTIVE);
-    CK(launch_activate(c.A, T(c, k).slot, c.qcur, c.st));
+    CK(launch_activate(c.A, T(c, k).slot, c.qcur, c.tcur, c.st));
+    touch(c, T(c, k).slot);
     c.launches++;
     sync(c);
     add_ghost_tiles(c, k);
     std::vector<int> one{T(c, k).slot};
     upload_list(c, one);
-    CK(launch_face_topo(c.A, c.d_list, 1, c.st));
+    CK(launch_face_topo(c.A, c.d_list, 1, c.tcur, c.st));
     c.launches++;
     sync(c);
     c.blocks_dirty = true;
@@ -551,7 +595,7 @@ void check_near_boundaries(kg_ctx& c) {
     std::vector<int> slots;
     for (int id : c.active) slots.push_back(T(c, id).slot);
     upload_list(c, slots);
-    CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), c.qcur, c.src_override ? c.d_srcHn : nullptr, c.d_flags, c.st));
+    CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), c.qcur, c.tcur, c.src_override ? c.d_srcHn : nullptr, c.d_flags, c.st));
     c.launches++;
     std::vector<int> fl(slots.size());
     CK(cudaMemcpyAsync(fl.data(), c.d_flags, fl.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
@@ -574,6 +618,7 @@ void check_near_boundaries(kg_ctx& c) {
             }
         }
     }
+    if (!c.touched.empty()) mirror_touched(c);
 }
 
 // ComputeAdvisedTimeStep, src/HydraulicRHS.f90:141-174.
@@ -617,11 +662,13 @@ double next_flux_time(const kg_ctx& c, double t) {  // NextFluxSeriesTime, src/T
 }
 
 // HydraulicTimeStepper on the device; returns true when dt had to be refined.
-bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int q_out) {
+bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int e_set, int topo, int q_s1, int q_s2, int q_out) {
     double nextT = c.t + dt;
     c.dt = dt;
     StepArgs S{};
-    S.q_in = q_in; S.q_out = q_out; S.dt = dt; S.t_grid = c.t; S.do_maxima = 1;
+    S.q_in = q_in; S.q_s1 = q_s1; S.q_s2 = q_s2; S.q_out = q_out; S.e_set = e_set; S.topo = topo;
+    S.q_tc = c.qcur; S.topo_tc = c.tcur;
+    S.dt = dt; S.t_grid = c.t; S.do_maxima = 1;
     S.mode = MODE_S1; S.t_rhs = nextT;
     double dt1 = advised(c, run_pass(c, S), 2);
     if (dt1 < dt) { dt = 0.9 * dt1; return true; }
@@ -633,31 +680,143 @@ bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int q_out) {
     return false;
 }
 
-// One accepted step of IntegrateTo (src/TimeStepper.f90:151-275).
+// CalculateHydraulicRHS at substep 1 on state q_in / topography topo into E/I set e_set.
+double rhs0(kg_ctx& c, int q_in, int e_set, int topo, double t, int substep = 1) {
+    StepArgs S{};
+    S.mode = MODE_RHS0; S.q_in = q_in; S.e_set = e_set; S.topo = topo; S.t_rhs = t; S.t_grid = c.t;
+    S.q_tc = c.qcur; S.topo_tc = c.tcur;
+    return advised(c, run_pass(c, S), substep);
+}
+
+// MorphodynamicTimeStepper (src/TimeStepper.f90:532-781) on state qa (the first hydraulic
+// step's result); builds the new bed in set tnew.  Returns true when dt must be refined.
+bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
+    std::vector<int> slots;
+    for (int id : c.active) slots.push_back(T(c, id).slot);
+    int n = (int)slots.size();
+    upload_list(c, slots);
+    CK(launch_m_init(c.A, c.d_list, n, qa, c.tcur, tnew, c.st));
+    c.launches++;
+    for (int stage = 1; stage <= 3; ++stage) {
+        CK(launch_m_emd(c.A, c.d_list, n, tnew, c.st));
+        CK(launch_m_bt(c.A, c.d_list, n, c.tcur, tnew, stage, dt_m, c.st));
+        CK(launch_m_cells(c.A, c.d_list, n, qa, c.tcur, tnew, c.st));
+        c.launches += 3;
+    }
+    int need = n * c.SC;
+    if (need > c.cand_cap) {
+        cudaFree(c.d_ckey); cudaFree(c.d_cex); cudaFree(c.d_rslot); cudaFree(c.d_rcell);
+        c.cand_cap = std::max(need, 2 * c.cand_cap);
+        CK(cudaMalloc(&c.d_ckey, (size_t)c.cand_cap * sizeof(unsigned long long)));
+        CK(cudaMalloc(&c.d_cex, (size_t)c.cand_cap * sizeof(double)));
+        CK(cudaMalloc(&c.d_rslot, (size_t)c.cand_cap * sizeof(int)));
+        CK(cudaMalloc(&c.d_rcell, (size_t)c.cand_cap * sizeof(int)));
+    }
+    if (!c.d_mflags) {
+        CK(cudaMalloc(&c.d_mflags, sizeof(int)));
+        CK(cudaMalloc(&c.d_ncand, sizeof(int)));
+    }
+    CK(cudaMemsetAsync(c.d_mflags, 0, sizeof(int), c.st));
+    CK(cudaMemsetAsync(c.d_ncand, 0, sizeof(int), c.st));
+    CK(launch_m_check(c.A, c.d_list, n, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, c.st));
+    c.launches++;
+    int hf[2];
+    CK(cudaMemcpyAsync(&hf[0], c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    CK(cudaMemcpyAsync(&hf[1], c.d_ncand, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    sync(c);
+    bool refine = hf[0] != 0;
+    int ncand = hf[1];
+    if (!refine && ncand > 0) {
+        // AddToRedistList keeps the cells ordered by excess deposition, ties in loop order
+        // (src/Redistribute.f90:69-101); RedistributeGrid then walks that list.
+        std::vector<unsigned long long> key((size_t)ncand);
+        std::vector<double> ex((size_t)ncand);
+        CK(cudaMemcpyAsync(key.data(), c.d_ckey, (size_t)ncand * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(ex.data(), c.d_cex, (size_t)ncand * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        sync(c);
+        std::vector<int> ord((size_t)ncand);
+        for (int q = 0; q < ncand; ++q) ord[(size_t)q] = q;
+        std::sort(ord.begin(), ord.end(), [&](int a, int b) {
+            if (ex[(size_t)a] != ex[(size_t)b]) return ex[(size_t)a] < ex[(size_t)b];
+            return key[(size_t)a] < key[(size_t)b];
+        });
+        std::vector<int> ls((size_t)ncand), lc((size_t)ncand);
+        for (int q = 0; q < ncand; ++q) {
+            unsigned long long k = key[(size_t)ord[(size_t)q]];
+            ls[(size_t)q] = slots[(size_t)(k >> 32)];
+            lc[(size_t)q] = (int)(k & 0xffffffffull);
+        }
+        CK(cudaMemcpyAsync(c.d_rslot, ls.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, ncand, qa, c.tcur, tnew, c.d_mflags, c.st));
+        c.launches++;
+        CK(cudaMemcpyAsync(&hf[0], c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        sync(c);
+        refine = hf[0] != 0;
+    }
+    if (refine) {
+        dt_m = 0.5 * dt_m;
+        return true;
+    }
+    upload_list(c, slots);
+    CK(launch_face_topo(c.A, c.d_list, n, tnew, c.st));
+    CK(launch_face_bI(c.A, c.d_list, n, tnew, c.st));
+    CK(launch_m_finish(c.A, c.d_list, n, qa, c.st));
+    c.launches += 3;
+    return false;
+}
+
+// One accepted step of IntegrateTo (src/TimeStepper.f90:151-275): H(dt) alone, or the
+// Strang split H(dt) M(2 dt) H(dt) with morphodynamics, retried from the step-start state
+// until every part accepts its dt.
 void integrate_step(kg_ctx& c, double tend) {
     if (!c.sources_loaded) throw KgError(KG_ERR_STATE, "kg_load_sources must be called before stepping");
-    if (c.p.MorphodynamicsOn) throw KgError(KG_ERR_UNSUPPORTED, "the morphodynamic operator is not in this build");
     check_near_boundaries(c);
     rebuild_blocks(c);
-    StepArgs S{};
-    S.mode = MODE_RHS0; S.q_in = c.qcur; S.t_rhs = c.t; S.t_grid = c.t;
-    double adv = advised(c, run_pass(c, S), 1);
+    const bool morpho = c.p.MorphodynamicsOn != 0;
+    int o[3], k = 0;
+    for (int b = 0; b < 4; ++b)
+        if (b != c.qcur) o[k++] = b;
+    int tnew = 1 - c.tcur;
+    double adv = rhs0(c, c.qcur, 0, c.tcur, c.t);
     double tmax = mn(tend, next_flux_time(c, c.t));
-    adv = mn(adv, tmax - c.t);
+    if (!morpho) adv = mn(adv, tmax - c.t);
+    else adv = mn(adv, 0.5 * (tmax - c.t));
     c.dt = adv;
     double dt = adv;
     c.t0 = c.t;
-    int guard = 0;
+    int guard = 0, newcur = -1;
     while (true) {
         if (++guard > 100000 || !(dt > 0.0)) throw KgError(KG_ERR_DT, "time step collapsed");
-        if (hydraulic_stepper(c, dt, c.qcur, 1 - c.qcur)) { c.rejected++; continue; }
-        break;
+        if (hydraulic_stepper(c, dt, c.qcur, 0, c.tcur, o[0], o[1], o[0])) { c.rejected++; continue; }
+        if (!morpho) { newcur = o[0]; break; }
+        double dt_m = 2.0 * dt;
+        if (morpho_stepper(c, dt_m, o[0], tnew)) {
+            c.rejected++;
+            dt = 0.5 * dt_m;
+            c.dt = dt;
+            continue;
+        }
+        c.t = c.t0 + dt;
+        adv = rhs0(c, o[0], 1, tnew, c.t);
+        if (adv < dt) {
+            if ((dt - adv) / dt < 0.1) dt = 0.9 * dt;
+            else dt = adv;
+            c.dt = dt;
+            c.t = c.t0;
+            c.rejected++;
+            continue;
+        }
+        if (!hydraulic_stepper(c, dt, o[0], 1, tnew, o[1], o[2], o[1])) { newcur = o[1]; break; }
+        c.t = c.t0;
+        c.rejected++;
     }
-    c.qcur = 1 - c.qcur;
-    c.t = c.t0 + dt;
+    c.qcur = newcur;
+    if (morpho) c.tcur = tnew;
+    c.t = morpho ? c.t0 + 2.0 * dt : c.t0 + dt;
     c.dt = dt;
     c.steps++;
-    c.cell_updates += (int64_t)c.active.size() * c.SC;
+    c.cell_updates += (int64_t)c.active.size() * c.SC * (morpho ? 2 : 1);
     c.src_override = false;
 }
 
@@ -738,7 +897,7 @@ void load_sources(kg_ctx& c) {
         bufs[q].hmax.resize((size_t)SC);
         CK(cudaMemcpyAsync(bufs[q].hmax.data(), c.A.MX + (size_t)s * 11 * SC, (size_t)SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
         CK(cudaMemcpyAsync(bufs[q].q.data(), c.A.Q[c.qcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
-        CK(cudaMemcpyAsync(bufs[q].ct.data(), c.A.CT + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(bufs[q].ct.data(), c.A.CT[c.tcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
     }
     sync(c);
     double rhow = c.p.rhow, rhos = c.p.rhos;
@@ -824,8 +983,7 @@ void load_sources(kg_ctx& c) {
     }
     for (size_t q = 0; q < touched.size(); ++q) {
         int s = T(c, touched[q]).slot;
-        for (int b = 0; b < 2; ++b)
-            CK(cudaMemcpyAsync(c.A.Q[b] + (size_t)s * 4 * SC, bufs[q].q.data(), (size_t)4 * SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.A.Q[c.qcur] + (size_t)s * 4 * SC, bufs[q].q.data(), (size_t)4 * SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_srcHn + (size_t)s * SC, bufs[q].hn.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_srcRho + (size_t)s * SC, bufs[q].rho.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.A.MX + (size_t)s * 11 * SC, bufs[q].hmax.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
@@ -847,6 +1005,7 @@ void load_sources(kg_ctx& c) {
     CK(set_constants(c.dp, ds.data(), (int)ds.size(), c.st));
     sync(c);
     for (int g : std::vector<int>(c.ghost)) ghost_edges(c, g);
+    if (!c.touched.empty()) mirror_touched(c);
     c.src_override = true;
     c.sources_loaded = true;
     c.blocks_dirty = true;
@@ -926,9 +1085,13 @@ void free_ctx(kg_ctx* c) {
     if (!c) return;
     if (c->st) cudaStreamSynchronize(c->st);
     for (int b = 0; b < 4; ++b) cudaFree(c->A.Q[b]);
-    void* ptrs[] = {c->A.E0, c->A.I0, c->A.UV, c->A.CT, c->A.FX, c->A.FY, c->A.BV, c->A.G9, c->A.GE, c->A.MX,
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(c->A.E[b]); cudaFree(c->A.I[b]); cudaFree(c->A.CT[b]); cudaFree(c->A.FX[b]); cudaFree(c->A.FY[b]); cudaFree(c->A.BV[b]);
+    }
+    void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
-                    c->d_cfl, c->d_vol, c->d_srcHn, c->d_srcRho};
+                    c->d_cfl, c->d_vol, c->d_srcHn, c->d_srcRho, c->d_mflags, c->d_ncand, c->d_ckey, c->d_cex,
+                    c->d_rslot, c->d_rcell};
     for (void* q : ptrs) cudaFree(q);
     if (c->h_cfl) cudaFreeHost(c->h_cfl);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1069,9 +1232,7 @@ int kg_hydraulic_rhs(kg_ctx* c, double t, int32_t substep, double* advised_dt) {
     if (!c || !advised_dt || substep < 1 || substep > 4) return KG_ERR_PARAM;
     KG_GUARD(c, {
         rebuild_blocks(*c);
-        StepArgs S{};
-        S.mode = MODE_RHS0; S.q_in = c->qcur; S.t_rhs = t; S.t_grid = c->t;
-        *advised_dt = advised(*c, run_pass(*c, S), substep);
+        *advised_dt = rhs0(*c, c->qcur, 0, c->tcur, t, substep);
     });
     return KG_OK;
 }
@@ -1101,14 +1262,14 @@ int kg_get_tile_field(kg_ctx* c, int32_t id, int32_t field, double* out) {
             auto v = d2h(c, c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * SC, SC);
             std::memcpy(out, v.data(), SC * sizeof(double));
         } else if (field >= 10) {
-            auto v = d2h(c, c->A.CT + ((size_t)s * 4 + field - 10) * SC, SC);
+            auto v = d2h(c, c->A.CT[c->tcur] + ((size_t)s * 4 + field - 10) * SC, SC);
             std::memcpy(out, v.data(), SC * sizeof(double));
         } else if (field == 6 || field == 7) {
             auto v = d2h(c, c->A.UV + ((size_t)s * 2 + field - 6) * SC, SC);
             std::memcpy(out, v.data(), SC * sizeof(double));
         } else {
             auto q = d2h(c, c->A.Q[c->qcur] + (size_t)s * 4 * SC, 4 * (size_t)SC);
-            auto ct = d2h(c, c->A.CT + (size_t)s * 4 * SC, 4 * (size_t)SC);
+            auto ct = d2h(c, c->A.CT[c->tcur] + (size_t)s * 4 * SC, 4 * (size_t)SC);
             std::vector<double> hn, rh;
             if (c->src_override) {
                 hn = d2h(c, c->d_srcHn + (size_t)s * SC, SC);
@@ -1147,7 +1308,7 @@ int kg_get_tile_vertex(kg_ctx* c, int32_t id, int32_t which, double* out) {
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (which < 0 || which > 1 || !out) return KG_ERR_PARAM;
     KG_GUARD(c, {
-        auto v = d2h(c, c->A.BV + ((size_t)s * 2 + which) * c->SV, c->SV);
+        auto v = d2h(c, c->A.BV[c->tcur] + ((size_t)s * 2 + which) * c->SV, c->SV);
         std::memcpy(out, v.data(), (size_t)c->SV * sizeof(double));
     });
     return KG_OK;
@@ -1158,7 +1319,7 @@ int kg_get_tile_rhs(kg_ctx* c, int32_t id, int32_t k, double* out) {
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (k < 1 || k > 5 || !out) return KG_ERR_PARAM;
     KG_GUARD(c, {
-        const double* src = k <= 4 ? c->A.E0 + ((size_t)s * 4 + k - 1) * c->SC : c->A.I0 + (size_t)s * c->SC;
+        const double* src = k <= 4 ? c->A.E[0] + ((size_t)s * 4 + k - 1) * c->SC : c->A.I[0] + (size_t)s * c->SC;
         auto v = d2h(c, src, c->SC);
         std::memcpy(out, v.data(), (size_t)c->SC * sizeof(double));
     });
@@ -1188,7 +1349,7 @@ int kg_volume(kg_ctx* c, double out[4]) {
         std::vector<int> slots;
         for (int id : c->active) slots.push_back(T(*c, id).slot);
         upload_list(*c, slots);
-        CK(launch_volume(c->A, c->d_list, (int)slots.size(), c->qcur, c->src_override ? c->d_srcHn : nullptr,
+        CK(launch_volume(c->A, c->d_list, (int)slots.size(), c->qcur, c->tcur, c->src_override ? c->d_srcHn : nullptr,
                          c->src_override ? c->d_srcRho : nullptr, c->d_vol, c->st));
         c->launches++;
         auto v = d2h(c, c->d_vol, 4);

@@ -43,17 +43,19 @@ struct BlockDesc {
 struct DevArrays {
     int cap;                   // slot capacity
     int nE;                    // max(nX, nY)
-    double* Q[4];
-    double* E0;
-    double* I0;
+    double* Q[4];              // state buffers (the current solution is one of them)
+    double* E[2];              // RHS of stage 1 (two sets: step start, and after the M operator)
+    double* I[2];
     double* UV;
-    double* CT;
-    double* FX;
-    double* FY;
-    double* BV;
+    double* CT[2];             // topography sets: the step-start bed and the M-updated bed
+    double* FX[2];
+    double* FY[2];
+    double* BV[2];
     double* G9;
     double* GE;
     double* MX;
+    double* MS;                // [slot][5][nY][nX] M-operator stage state: w, Hnpsi, Hn, psi, rho
+    double* EMD;               // [slot][nY][nX] E - D of the current M stage (zero on ghosts)
     int* nbr;                  // [cap][8] neighbour slots (-1: none)
     int8_t* kind;              // SlotKind per slot
     int8_t* has_source;        // containsSource per slot
@@ -64,8 +66,13 @@ struct DevArrays {
 enum Mode { MODE_RHS0 = 0, MODE_S1 = 1, MODE_S2 = 2, MODE_S3 = 3 };
 struct StepArgs {
     int mode;
-    int q_in;        // state buffer read as q0 (the reference's intermed0 / tileContainer)
-    int q_out;       // buffer written by S3 (the new solution)
+    int q_in;        // q0 of the hydraulic step (the reference's intermed0)
+    int q_s1;        // S1 writes the stage-2 state here
+    int q_s2;        // S2 writes the stage-3 state here (S3 reads it)
+    int q_out;       // S3 writes the new solution here
+    int e_set;       // E/I set written by RHS0 and read by S1
+    int topo;        // topography set of this hydraulic step
+    int q_tc, topo_tc;  // the step-start solution (tileContainer) for the maxima
     double dt;       // hydraulic dt of this attempt
     double t_rhs;    // time passed to ConstructHydraulicRHS
     double t_grid;   // grid%t (for the flux-source end-point logic)

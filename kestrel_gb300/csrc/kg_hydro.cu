@@ -257,10 +257,12 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
     const int tid = threadIdx.x;
     const int nbW = A.nbr[slot * 8 + NB_W], nbE = A.nbr[slot * 8 + NB_E];
     const int nbN = A.nbr[slot * 8 + NB_N], nbS = A.nbr[slot * 8 + NB_S];
-    const double* __restrict__ Qin = (S.mode == MODE_RHS0) ? A.Q[S.q_in]
-                                   : (S.mode == MODE_S1)   ? A.Q[S.q_in]
-                                   : (S.mode == MODE_S2)   ? A.Q[2]
-                                                           : A.Q[3];
+    const double* __restrict__ Qin = (S.mode == MODE_RHS0 || S.mode == MODE_S1) ? A.Q[S.q_in]
+                                   : (S.mode == MODE_S2)                        ? A.Q[S.q_s1]
+                                                                                : A.Q[S.q_s2];
+    const double* __restrict__ CT = A.CT[S.topo];
+    const double* __restrict__ FX = A.FX[S.topo];
+    const double* __restrict__ FY = A.FY[S.topo];
 
     // ---- A: load the cross-shaped region and desingularise ----
     for (int r = tid; r < NR; r += NT) {
@@ -274,8 +276,8 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         else if (j < 0) { s = nbS; j += nY; }
         else if (j >= nY) { s = nbN; j -= nY; }
         int c = j * nX + i;
-        double b0 = A.CT[plane(s, 4, 0, SC) + c], bt = A.CT[plane(s, 4, 1, SC) + c];
-        double dbx = A.CT[plane(s, 4, 2, SC) + c], dby = A.CT[plane(s, 4, 3, SC) + c];
+        double b0 = CT[plane(s, 4, 0, SC) + c], bt = CT[plane(s, 4, 1, SC) + c];
+        double dbx = CT[plane(s, 4, 2, SC) + c], dby = CT[plane(s, 4, 3, SC) + c];
         sm.b0[r] = b0; sm.bt[r] = bt; sm.bx[r] = dbx; sm.by[r] = dby;
         if (A.kind[s] == SLOT_GHOST) {
             sm.w[r] = A.G9[plane(s, 9, 0, SC) + c];
@@ -295,9 +297,9 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
                 q0[f] = Qin[plane(s, 4, f, SC) + c];
-                E[f] = A.E0[plane(s, 4, f, SC) + c];
+                E[f] = A.E[S.e_set][plane(s, 4, f, SC) + c];
             }
-            stage1(q0, E, A.I0[plane(s, 1, 0, SC) + c], S.dt, q);
+            stage1(q0, E, A.I[S.e_set][plane(s, 1, 0, SC) + c], S.dt, q);
         } else {
 #pragma unroll
             for (int f = 0; f < 4; ++f) q[f] = Qin[plane(s, 4, f, SC) + c];
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         L.du = sm.lx[2][liL];
         L.dv = sm.lx[3][liL];
         if (fi == 0) {
-            const double* fxs = A.FX + plane(nbW, 5, 4, SFX);
+            const double* fxs = FX + plane(nbW, 5, 4, SFX);
             double bl = fxs[j * (nX + 1) + nX - 1], br = fxs[j * (nX + 1) + nX];
             if (A.kind[nbW] == SLOT_GHOST) {
                 const double* ge = A.GE + plane(nbW, GE_COUNT, 0, A.nE);
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
             }
             if (L.p < 0.0) L.p = sm.p[rL];
         } else {
-            const double* fxs = A.FX + plane(slot, 5, 4, SFX);
+            const double* fxs = FX + plane(slot, 5, 4, SFX);
             double bl = fxs[j * (nX + 1) + fi - 1], br = fxs[j * (nX + 1) + fi];
             double wl = sm.w[rL] - sw * hdx * dx, pl = sm.p[rL] - sp * hdx * dx;
             if (L.w < br || wl < bl) L.w = sm.w[rL] + 0.5 * (br - bl);
@@ -396,7 +398,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         R.du = sm.lx[2][liR];
         R.dv = sm.lx[3][liR];
         if (fi == nX) {
-            const double* fxs = A.FX + plane(nbE, 5, 4, SFX);
+            const double* fxs = FX + plane(nbE, 5, 4, SFX);
             double bl = fxs[j * (nX + 1) + 0], br = fxs[j * (nX + 1) + 1];
             if (A.kind[nbE] == SLOT_GHOST) {
                 const double* ge = A.GE + plane(nbE, GE_COUNT, 0, A.nE);
@@ -407,14 +409,14 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
             }
             if (R.p < 0.0) R.p = sm.p[rR];
         } else {
-            const double* fxs = A.FX + plane(slot, 5, 4, SFX);
+            const double* fxs = FX + plane(slot, 5, 4, SFX);
             double bl = fxs[j * (nX + 1) + fi], br = fxs[j * (nX + 1) + fi + 1];
             double wr = sm.w[rR] + sw * hdx * dx, pr = sm.p[rR] + sp * hdx * dx;
             if (wr < br || R.w < bl) R.w = sm.w[rR] + 0.5 * (bl - br);
             if (pr < 0.0 || R.p < 0.0) R.p = sm.p[rR];
         }
         size_t fo = (size_t)slot * 5 * SFX + (size_t)j * (nX + 1) + fi;
-        double b0f = A.FX[fo], btf = A.FX[fo + SFX], dbxf = A.FX[fo + 2 * (size_t)SFX], dbyf = A.FX[fo + 3 * (size_t)SFX];
+        double b0f = FX[fo], btf = FX[fo + SFX], dbxf = FX[fo + 2 * (size_t)SFX], dbyf = FX[fo + 3 * (size_t)SFX];
         double gamL = gam_of(P.geo, sm.bx[rL], sm.by[rL]), gamR = gam_of(P.geo, sm.bx[rR], sm.by[rR]);
         double out[7];
         face_flux(P, true, R, L, b0f, btf, dbxf, dbyf, gamL, gamR, dx, out, cfl);
@@ -437,7 +439,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         L.du = sm.ly[2][liL];
         L.dv = sm.ly[3][liL];
         if (fj == 0) {
-            const double* fys = A.FY + plane(nbS, 5, 4, SFY);
+            const double* fys = FY + plane(nbS, 5, 4, SFY);
             double bb = fys[(nY - 1) * nX + i], bt_ = fys[nY * nX + i];
             if (A.kind[nbS] == SLOT_GHOST) {
                 const double* ge = A.GE + plane(nbS, GE_COUNT, 0, A.nE);
@@ -448,7 +450,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
             }
             if (L.p < 0.0) L.p = sm.p[rL];
         } else {
-            const double* fys = A.FY + plane(slot, 5, 4, SFY);
+            const double* fys = FY + plane(slot, 5, 4, SFY);
             double bb = fys[(fj - 1) * nX + i], bt_ = fys[fj * nX + i];
             double wb = sm.w[rL] - sw * hdx * dy, pb = sm.p[rL] - sp * hdx * dy;
             if (L.w < bt_ || wb < bb) L.w = sm.w[rL] + 0.5 * (bt_ - bb);
@@ -464,7 +466,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         R.du = sm.ly[2][liR];
         R.dv = sm.ly[3][liR];
         if (fj == nY) {
-            const double* fys = A.FY + plane(nbN, 5, 4, SFY);
+            const double* fys = FY + plane(nbN, 5, 4, SFY);
             double bb = fys[0 * nX + i], bt_ = fys[1 * nX + i];
             if (A.kind[nbN] == SLOT_GHOST) {
                 const double* ge = A.GE + plane(nbN, GE_COUNT, 0, A.nE);
@@ -475,14 +477,14 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
             }
             if (R.p < 0.0) R.p = sm.p[rR];
         } else {
-            const double* fys = A.FY + plane(slot, 5, 4, SFY);
+            const double* fys = FY + plane(slot, 5, 4, SFY);
             double bb = fys[fj * nX + i], bt_ = fys[(fj + 1) * nX + i];
             double wt = sm.w[rR] + sw * hdx * dy, pt = sm.p[rR] + sp * hdx * dy;
             if (wt < bt_ || R.w < bb) R.w = sm.w[rR] + 0.5 * (bb - bt_);
             if (pt < 0.0 || R.p < 0.0) R.p = sm.p[rR];
         }
         size_t fo = (size_t)slot * 5 * SFY + (size_t)fj * nX + i;
-        double b0f = A.FY[fo], btf = A.FY[fo + SFY], dbxf = A.FY[fo + 2 * (size_t)SFY], dbyf = A.FY[fo + 3 * (size_t)SFY];
+        double b0f = FY[fo], btf = FY[fo + SFY], dbxf = FY[fo + 2 * (size_t)SFY], dbyf = FY[fo + 3 * (size_t)SFY];
         double gamL = gam_of(P.geo, sm.bx[rL], sm.by[rL]), gamR = gam_of(P.geo, sm.bx[rR], sm.by[rR]);
         double out[7];
         face_flux(P, false, R, L, b0f, btf, dbxf, dbyf, gamL, gamR, dy, out, cfl);
@@ -539,15 +541,15 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         double qk[4] = {sm.w[r], sm.m1[r], sm.m2[r], sm.p[r]};
         if (S.mode == MODE_RHS0) {
 #pragma unroll
-            for (int f = 0; f < 4; ++f) A.E0[plane(slot, 4, f, SC) + c] = E[f];
-            A.I0[plane(slot, 1, 0, SC) + c] = I;
+            for (int f = 0; f < 4; ++f) A.E[S.e_set][plane(slot, 4, f, SC) + c] = E[f];
+            A.I[S.e_set][plane(slot, 1, 0, SC) + c] = I;
         } else if (S.mode == MODE_S1 || S.mode == MODE_S2) {
             const double* q0p = A.Q[S.q_in];
             double q0[4], out[4];
 #pragma unroll
             for (int f = 0; f < 4; ++f) q0[f] = q0p[plane(slot, 4, f, SC) + c];
             stage23(S.mode == MODE_S1 ? 2 : 3, q0, qk, E, I, S.dt, b0, bt, b0, bt, out);
-            double* dst = A.Q[S.mode == MODE_S1 ? 2 : 3];
+            double* dst = A.Q[S.mode == MODE_S1 ? S.q_s1 : S.q_s2];
 #pragma unroll
             for (int f = 0; f < 4; ++f) dst[plane(slot, 4, f, SC) + c] = out[f];
         } else {
@@ -564,10 +566,17 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
             if (S.do_maxima) {
                 // UpdateMaximum* on the state at the start of the step
                 // (src/TimeStepper.f90:519-524, :1155-1303).
-                const double* q0p = A.Q[S.q_in];
+                const double* q0p = A.Q[S.q_tc];
+                const double* ct0 = A.CT[S.topo_tc];
+                double b0t = ct0[plane(slot, 4, 0, SC) + c], btt = ct0[plane(slot, 4, 1, SC) + c];
+                double dbxt = ct0[plane(slot, 4, 2, SC) + c], dbyt = ct0[plane(slot, 4, 3, SC) + c];
+                double gamt = gam_of(P.geo, dbxt, dbyt);
                 double Hn, psi, rho, u, v;
                 desing(P, q0p[plane(slot, 4, 0, SC) + c], q0p[plane(slot, 4, 1, SC) + c], q0p[plane(slot, 4, 2, SC) + c],
-                       q0p[plane(slot, 4, 3, SC) + c], b0, bt, gam, Hn, psi, rho, u, v);
+                       q0p[plane(slot, 4, 3, SC) + c], b0t, btt, gamt, Hn, psi, rho, u, v);
+                bt = btt;
+                dbdx = dbxt;
+                dbdy = dbyt;
                 double* M = A.MX + plane(slot, 11, 0, SC) + c;
                 double tt = S.t_max;
                 if (Hn > P.hThr) {

@@ -2,4 +2,6 @@
 // __constant__ run settings, so they are compiled together rather than with -rdc).
 #include "kg_hydro.cu"
 #include "kg_tiles.cu"
+
+#include "kg_morpho.cu"
 #include "kg_engine.cu"

@@ -1,0 +1,464 @@
+// kg_morpho.cu -- the morphodynamic operator M (MorphodynamicTimeStepper,
+// src/TimeStepper.f90:532-781) on sm_103a, FP64.
+//
+// M advances the vertex bed bt with the three-stage scheme and updates w and Hnpsi
+// conservatively from the change in the cell-centred bed.  Per stage k = 1..3:
+//   k_m_emd     E - D at every active cell of stage k-1, zero next to a dry cell
+//               (CalculateMorphodynamicRHS, src/MorphodynamicRHS.f90:72-149)
+//   k_m_bt      d(bt)/dt at every vertex of every active tile (BtSourceTerm, :154-305:
+//               each tile updates its own copy of its edge vertices, with the reference's
+//               Kahan orders, including the two pre-added entries at :210 and :266) and the
+//               clamped stage update of bt
+//   k_m_cells   cell-centred bed from the new vertices (ComputeCellCentredTopographicData),
+//               the w / Hnpsi update (src/TimeStepper.f90:584-609) and the depth, solids
+//               fraction and density of the stage (ComputeDesingularisedVariables without
+//               velocities: u and v stay those the first hydraulic step left)
+// then k_m_check evaluates the excess-deposition and 10 % depth-change tests (:709-753)
+// and k_m_redist runs RedistributeGrid's serial, ordered correction (src/Redistribute.f90)
+// on one thread.  Topography lives in two sets: the step-start bed (read-only here) and
+// the bed M builds, so a refined attempt restarts from the step-start set.
+#include <cuda_runtime.h>
+#include "kg_engine.cuh"
+
+namespace kg {
+
+// cP is defined in kg_hydro.cu (one translation unit through kg_lib.cu).
+
+__device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return ((size_t)slot * nf + f) * (size_t)npl; }
+
+// Copy the step-start bed into the M set and fill the stage state of im0 (the state the
+// first hydraulic step produced).
+__global__ void k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int SC = P.nX * P.nY, SV = (P.nX + 1) * (P.nY + 1);
+    for (int v = threadIdx.x; v < SV; v += blockDim.x) {
+        A.BV[tnew][mp(s, 2, 0, SV) + v] = A.BV[tcur][mp(s, 2, 0, SV) + v];
+        A.BV[tnew][mp(s, 2, 1, SV) + v] = A.BV[tcur][mp(s, 2, 1, SV) + v];
+    }
+    double e2 = P.hThr * P.hThr;
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        double ct[4];
+        for (int f = 0; f < 4; ++f) {
+            ct[f] = A.CT[tcur][mp(s, 4, f, SC) + c];
+            A.CT[tnew][mp(s, 4, f, SC) + c] = ct[f];
+        }
+        double w = A.Q[qa][mp(s, 4, 0, SC) + c], p = A.Q[qa][mp(s, 4, 3, SC) + c];
+        double gam = gam_of(P.geo, ct[2], ct[3]);
+        double Hn = compute_hn(w, ct[0], ct[1], gam);
+        if (Hn < 0.0) Hn = 0.0;
+        double pp = p < 0.0 ? 0.0 : p;
+        double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
+        double* M = A.MS + mp(s, 5, 0, SC) + c;
+        M[0] = w;
+        M[(size_t)SC] = p;
+        M[2 * (size_t)SC] = Hn;
+        M[3 * (size_t)SC] = psi;
+        M[4 * (size_t)SC] = density(P, psi);
+    }
+}
+
+// Depth of a cell of any tile as the M stage sees it: active tiles from the stage state,
+// ghost tiles from their static data.
+__device__ __forceinline__ double stage_hn(const DevArrays& A, int s, int c, int SC) {
+    return A.kind[s] == SLOT_GHOST ? A.G9[mp(s, 9, 4, SC) + c] : A.MS[mp(s, 5, 2, SC) + c];
+}
+
+__global__ void k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int nX = P.nX, nY = P.nY, SC = nX * nY;
+    int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sN = A.nbr[s * 8 + NB_N], sS = A.nbr[s * 8 + NB_S];
+    const double* CT = A.CT[tnew];
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        int i = c % nX, j = c / nX;
+        double Hn = A.MS[mp(s, 5, 2, SC) + c];
+        double HnW = (i == 0) ? stage_hn(A, sW, j * nX + nX - 1, SC) : A.MS[mp(s, 5, 2, SC) + c - 1];
+        double HnE = (i == nX - 1) ? stage_hn(A, sE, j * nX, SC) : A.MS[mp(s, 5, 2, SC) + c + 1];
+        double HnS = (j == 0) ? stage_hn(A, sS, (nY - 1) * nX + i, SC) : A.MS[mp(s, 5, 2, SC) + c - nX];
+        double HnN = (j == nY - 1) ? stage_hn(A, sN, i, SC) : A.MS[mp(s, 5, 2, SC) + c + nX];
+        double e = P.hThr;
+        double emd = 0.0;
+        if (!(Hn < e || HnW < e || HnE < e || HnS < e || HnN < e)) {
+            double dbx = CT[mp(s, 4, 2, SC) + c], dby = CT[mp(s, 4, 3, SC) + c];
+            Pt<double> pt{Hn, A.UV[mp(s, 2, 0, SC) + c], A.UV[mp(s, 2, 1, SC) + c], A.MS[mp(s, 5, 3, SC) + c],
+                          A.MS[mp(s, 5, 4, SC) + c], CT[mp(s, 4, 1, SC) + c], dbx, dby, gam_of(P.geo, dbx, dby)};
+            emd = erosion_minus_deposition(P, pt);
+        }
+        A.EMD[(size_t)s * SC + c] = emd;
+    }
+}
+
+// Cell value of one of the eight tiles around (and including) a tile: field f of CT
+// (2: dbdx, 3: dbdy) or EMD (f = -1) at tile-local (i, j).
+__device__ __forceinline__ double cellv(const DevArrays& A, const double* CT, int s, int f, int i, int j, int nX, int SC) {
+    if (s < 0) return 0.0;  // a diagonal tile that was never allocated (periodic corners)
+    size_t c = (size_t)j * nX + i;
+    return f < 0 ? A.EMD[(size_t)s * SC + c] : CT[mp(s, 4, f, SC) + c];
+}
+
+// Vertex source term and clamped stage update of bt (one CTA per tile).
+__global__ void k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
+    const double* CT = A.CT[tnew];
+    int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sN = A.nbr[s * 8 + NB_N], sS = A.nbr[s * 8 + NB_S];
+    int sSW = sW < 0 ? -1 : A.nbr[sW * 8 + NB_S], sSE = sE < 0 ? -1 : A.nbr[sE * 8 + NB_S];
+    int sNW = sW < 0 ? -1 : A.nbr[sW * 8 + NB_N], sNE = sE < 0 ? -1 : A.nbr[sE * 8 + NB_N];
+    double psib = 1.0 - P.BedPorosity;
+    for (int v = threadIdx.x; v < SV; v += blockDim.x) {
+        int a = v % (nX + 1), b = v / (nX + 1);  // vertex (a, b), 0-based
+        // The four cells around the vertex in the reference's list order, as (slot, i, j).
+        int cs[4], ci[4], cj[4];
+        int mode = 0;  // 0 plain, 1 west edge (E-D list pre-adds its last two), 2 NE corner (dbdx pre-add)
+        if (a > 0 && a < nX && b > 0 && b < nY) {
+            cs[0] = s; ci[0] = a - 1; cj[0] = b - 1;
+            cs[1] = s; ci[1] = a - 1; cj[1] = b;
+            cs[2] = s; ci[2] = a;     cj[2] = b - 1;
+            cs[3] = s; ci[3] = a;     cj[3] = b;
+        } else if (a == 0 && b > 0 && b < nY) {
+            cs[0] = sW; ci[0] = nX - 1; cj[0] = b - 1;
+            cs[1] = sW; ci[1] = nX - 1; cj[1] = b;
+            cs[2] = s;  ci[2] = 0;      cj[2] = b - 1;
+            cs[3] = s;  ci[3] = 0;      cj[3] = b;
+            mode = 1;
+        } else if (a == nX && b > 0 && b < nY) {
+            cs[0] = s;  ci[0] = nX - 1; cj[0] = b - 1;
+            cs[1] = s;  ci[1] = nX - 1; cj[1] = b;
+            cs[2] = sE; ci[2] = 0;      cj[2] = b - 1;
+            cs[3] = sE; ci[3] = 0;      cj[3] = b;
+        } else if (b == nY && a > 0 && a < nX) {
+            cs[0] = s;  ci[0] = a - 1; cj[0] = nY - 1;
+            cs[1] = sN; ci[1] = a - 1; cj[1] = 0;
+            cs[2] = s;  ci[2] = a;     cj[2] = nY - 1;
+            cs[3] = sN; ci[3] = a;     cj[3] = 0;
+        } else if (b == 0 && a > 0 && a < nX) {
+            cs[0] = sS; ci[0] = a - 1; cj[0] = nY - 1;
+            cs[1] = s;  ci[1] = a - 1; cj[1] = 0;
+            cs[2] = sS; ci[2] = a;     cj[2] = nY - 1;
+            cs[3] = s;  ci[3] = a;     cj[3] = 0;
+        } else if (a == 0 && b == 0) {
+            cs[0] = sSW; ci[0] = nX - 1; cj[0] = nY - 1;
+            cs[1] = sW;  ci[1] = nX - 1; cj[1] = 0;
+            cs[2] = sS;  ci[2] = 0;      cj[2] = nY - 1;
+            cs[3] = s;   ci[3] = 0;      cj[3] = 0;
+        } else if (a == nX && b == 0) {
+            cs[0] = sS;  ci[0] = nX - 1; cj[0] = nY - 1;
+            cs[1] = s;   ci[1] = nX - 1; cj[1] = 0;
+            cs[2] = sSE; ci[2] = 0;      cj[2] = nY - 1;
+            cs[3] = sE;  ci[3] = 0;      cj[3] = 0;
+        } else if (a == 0 && b == nY) {
+            cs[0] = sW;  ci[0] = nX - 1; cj[0] = nY - 1;
+            cs[1] = sNW; ci[1] = nX - 1; cj[1] = 0;
+            cs[2] = s;   ci[2] = 0;      cj[2] = nY - 1;
+            cs[3] = sN;  ci[3] = 0;      cj[3] = 0;
+        } else {  // NE
+            cs[0] = s;   ci[0] = nX - 1; cj[0] = nY - 1;
+            cs[1] = sN;  ci[1] = nX - 1; cj[1] = 0;
+            cs[2] = sE;  ci[2] = 0;      cj[2] = nY - 1;
+            cs[3] = sNE; ci[3] = 0;      cj[3] = 0;
+            mode = 2;
+        }
+        double x[4], y[4], e[4];
+        for (int q = 0; q < 4; ++q) {
+            x[q] = cellv(A, CT, cs[q], 2, ci[q], cj[q], nX, SC);
+            y[q] = cellv(A, CT, cs[q], 3, ci[q], cj[q], nX, SC);
+            e[q] = cellv(A, CT, cs[q], -1, ci[q], cj[q], nX, SC);
+        }
+        double kx = (mode == 2) ? kahan3(x[0], x[1], x[2] + x[3]) : kahan4(x[0], x[1], x[2], x[3]);
+        double ky = kahan4(y[0], y[1], y[2], y[3]);
+        double ke = (mode == 1) ? kahan3(e[0], e[1], e[2] + e[3]) : kahan4(e[0], e[1], e[2], e[3]);
+        double gam = gam_of(P.geo, 0.25 * kx, 0.25 * ky);
+        double ddt = -0.25 * gam / psib * ke;
+        double bt0 = A.BV[tcur][mp(s, 2, 1, SV) + v];
+        double btp = A.BV[tnew][mp(s, 2, 1, SV) + v];
+        double nb;
+        if (stage == 1) nb = bt0 + dt * ddt;
+        else if (stage == 2) nb = 0.75 * bt0 + 0.25 * (btp + dt * ddt);
+        else nb = (1.0 / 3.0) * bt0 + (2.0 / 3.0) * (btp + dt * ddt);
+        A.BV[tnew][mp(s, 2, 1, SV) + v] = mx(-P.EroDepth, nb);
+    }
+}
+
+// Cell-centred bed of stage k, the conservative w / Hnpsi update and the stage's depth,
+// solids fraction and density.
+__global__ void k_m_cells(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
+    const double* b0 = A.BV[tnew] + mp(s, 2, 0, SV);
+    const double* bt = A.BV[tnew] + mp(s, 2, 1, SV);
+    double psib = 1.0 - P.BedPorosity, e2 = P.hThr * P.hThr;
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        int i = c % nX, j = c / nX;
+        int v00 = j * (nX + 1) + i, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
+        double b0c = 0.25 * kahan4(b0[v00], b0[v10], b0[v01], b0[v11]);
+        double btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
+        double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
+        double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
+        double dbx = 0.5 * P.dxR * kahan8(ax), dby = 0.5 * P.dyR * kahan8(ay);
+        A.CT[tnew][mp(s, 4, 0, SC) + c] = b0c;
+        A.CT[tnew][mp(s, 4, 1, SC) + c] = btc;
+        A.CT[tnew][mp(s, 4, 2, SC) + c] = dbx;
+        A.CT[tnew][mp(s, 4, 3, SC) + c] = dby;
+        const double* C0 = A.CT[tcur];
+        double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+        double gamnew = gam_of(P.geo, dbx, dby);
+        double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
+        double Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
+        double db = btc - C0[mp(s, 4, 1, SC) + c];
+        double w = -db / gamnew / gamnew;
+        w = w + btc;
+        w = w + Hn_old * gamold / gamnew / gamnew;
+        w = w + b0c;
+        double Hnpsi = -(psib)*db / gamnew;
+        Hnpsi = Hnpsi + p0 * gamold / gamnew;
+        double Hn = compute_hn(w, b0c, btc, gamnew);
+        if (Hn < 0.0) Hn = 0.0;
+        double pp = Hnpsi < 0.0 ? 0.0 : Hnpsi;
+        double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
+        double* M = A.MS + mp(s, 5, 0, SC) + c;
+        M[0] = w;
+        M[(size_t)SC] = Hnpsi;
+        M[2 * (size_t)SC] = Hn;
+        M[3 * (size_t)SC] = psi;
+        M[4 * (size_t)SC] = density(P, psi);
+    }
+}
+
+// ExcessDeposition (src/Redistribute.f90:158-198) of cell (s, c) between im0 and im3.
+__device__ __forceinline__ void excess_deposition(const DevParams& P, const DevArrays& A, int s, int c, int qa, int tcur,
+                                                  int tnew, double& excess, double& deltaBt, double& psiold,
+                                                  double& Hn_old, double& Hn_new) {
+    int SC = P.nX * P.nY;
+    const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
+    double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+    double gamnew = gam_of(P.geo, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c]);
+    double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
+    Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
+    Hn_new = compute_hn(A.MS[mp(s, 5, 0, SC) + c], C3[mp(s, 4, 0, SC) + c], C3[mp(s, 4, 1, SC) + c], gamnew);
+    deltaBt = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
+    // im0's solids fraction as the first hydraulic step left it
+    double H0 = Hn_old < 0.0 ? 0.0 : Hn_old, pp = p0 < 0.0 ? 0.0 : p0, e2 = P.hThr * P.hThr;
+    psiold = mn(2.0 * H0 * pp / (H0 * H0 + mx(H0 * H0, e2)), P.maxPack);
+    excess = -(p0 * gamold / (1.0 - P.BedPorosity) - deltaBt);
+    excess = mx(excess, -(Hn_old * gamold - deltaBt));
+}
+
+// The two tests of src/TimeStepper.f90:709-753 for every active cell.  flags[0] is set
+// when the step must be refined; redistribution candidates are appended with their loop
+// position (tile position in the active list, then j, then i) so the host can order them.
+__global__ void k_m_check(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew, int* flags,
+                          unsigned long long* cand_key, double* cand_ex, int* ncand, int cand_cap) {
+    const DevParams& P = cP;
+    int s = slots[blockIdx.x];
+    int SC = P.nX * P.nY;
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        double ex, dBt, psiold, Hn_old, Hn_new;
+        excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Hn_old, Hn_new);
+        bool refine = false;
+        if (ex > kEPS && dBt > kEPS && psiold > -kEPS) {
+            if (Hn_old < P.EroCriticalHeight || fabs(Hn_new - Hn_old) < P.EroCriticalHeight) {
+                int k = atomicAdd(ncand, 1);
+                if (k < cand_cap) {
+                    cand_key[k] = ((unsigned long long)blockIdx.x << 32) | (unsigned long long)c;
+                    cand_ex[k] = ex;
+                }
+            } else {
+                refine = true;
+            }
+        } else if (!(Hn_old < P.EroCriticalHeight)) {
+            double rel = fabs(Hn_new - Hn_old) / fabs(Hn_old);
+            if (rel > 0.1) refine = true;
+        }
+        if (refine) atomicOr(flags, 1);
+    }
+}
+
+// Kahan-ordered cell-centred bed of one cell from the M set (ComputeCellCentredTopographic-
+// Data_ij, src/MorphodynamicRHS.f90:371-414: bt, dbdx, dbdy; b0 is left as it is).
+__device__ void cell_topo_ij(const DevParams& P, const DevArrays& A, int tnew, int s, int i, int j) {
+    int nX = P.nX, SC = nX * P.nY, SV = (nX + 1) * (P.nY + 1);
+    const double* b0 = A.BV[tnew] + mp(s, 2, 0, SV);
+    const double* bt = A.BV[tnew] + mp(s, 2, 1, SV);
+    int v00 = j * (nX + 1) + i, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
+    size_t c = (size_t)j * nX + i;
+    A.CT[tnew][mp(s, 4, 1, SC) + c] = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
+    double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
+    double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
+    A.CT[tnew][mp(s, 4, 2, SC) + c] = 0.5 * P.dxR * kahan8(ax);
+    A.CT[tnew][mp(s, 4, 3, SC) + c] = 0.5 * P.dyR * kahan8(ay);
+}
+
+__device__ __forceinline__ void set_bt(const DevArrays& A, int tnew, int s, int a, int b, double v, int SV, int nX) {
+    // Only active tiles' copies persist; a ghost tile keeps its static bed.
+    if (s >= 0 && A.kind[s] == SLOT_ACTIVE) A.BV[tnew][mp(s, 2, 1, SV) + (size_t)b * (nX + 1) + a] = v;
+}
+
+// RedistributeCell, src/Redistribute.f90:249-475.  Returns false when the cell borders no
+// depositional vertex.
+__device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int s, int i, int j,
+                                  double corr) {
+    int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
+    const double* bt0 = A.BV[tcur] + mp(s, 2, 1, SV);
+    double* bt3 = A.BV[tnew] + mp(s, 2, 1, SV);
+    int N = 0;
+    double sum = 0.0, bd[4] = {0, 0, 0, 0};
+    int di[4], dj[4];
+    const int ca[4] = {i, i + 1, i, i + 1}, cb[4] = {j, j, j + 1, j + 1};
+    for (int q = 0; q < 4; ++q) {
+        int v = cb[q] * (nX + 1) + ca[q];
+        bd[N] = bt3[v] - bt0[v];
+        if (bd[N] > 0.0) {
+            di[N] = ca[q];
+            dj[N] = cb[q];
+            sum = sum + bd[N];
+            N = N + 1;
+        }
+    }
+    if (N == 0) return false;
+    double delta = 4.0 * corr / sum;
+    const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
+    size_t c = (size_t)j * nX + i;
+    double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+    double w0 = A.Q[qa][mp(s, 4, 0, SC) + c];
+    double Hnold = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
+    if (Hnold < 0.0) Hnold = 0.0;
+    double db = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
+    double tol = kEPS * A.MS[mp(s, 5, 0, SC) + c] * 10.0;
+    double adjustment = 0.0;
+    double disc = kahan3(Hnold * gamold, -db, corr);
+    if (fabs(disc) < tol) {
+        adjustment = kahan3(tol, -Hnold * gamold, db);
+        adjustment = adjustment * (4.0 / sum);
+        adjustment = adjustment - delta;
+        adjustment = mx(adjustment, 0.0);
+    }
+    double Hgp = A.Q[qa][mp(s, 4, 3, SC) + c] * gamold / (1.0 - P.BedPorosity);
+    tol = kEPS * 10.0;
+    disc = kahan3(Hgp, -db, corr);
+    if (fabs(disc) < tol) {
+        double ap = kahan3(tol, -Hgp, db);
+        ap = ap * (4.0 / sum);
+        ap = ap - delta;
+        adjustment = mx(adjustment, ap);
+    }
+    delta = delta + adjustment;
+    int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sN = A.nbr[s * 8 + NB_N], sS = A.nbr[s * 8 + NB_S];
+    for (int k = 0; k < N; ++k) {
+        int v = dj[k] * (nX + 1) + di[k];
+        bt3[v] = bt3[v] - delta * bd[k];
+        double val = bt3[v];
+        if (di[k] == 0) set_bt(A, tnew, sW, nX, dj[k], val, SV, nX);
+        else if (di[k] == nX) set_bt(A, tnew, sE, 0, dj[k], val, SV, nX);
+        if (dj[k] == 0) {
+            set_bt(A, tnew, sS, di[k], nY, val, SV, nX);
+            if (di[k] == 0 && sS >= 0) set_bt(A, tnew, A.nbr[sS * 8 + NB_W], nX, nY, val, SV, nX);
+            if (di[k] == nX && sS >= 0) set_bt(A, tnew, A.nbr[sS * 8 + NB_E], 0, nY, val, SV, nX);
+        }
+        if (dj[k] == nY) {
+            set_bt(A, tnew, sN, di[k], 0, val, SV, nX);
+            if (di[k] == 0 && sN >= 0) set_bt(A, tnew, A.nbr[sN * 8 + NB_W], nX, 0, val, SV, nX);
+            if (di[k] == nX && sN >= 0) set_bt(A, tnew, A.nbr[sN * 8 + NB_E], 0, 0, val, SV, nX);
+        }
+    }
+    // The (up to) 3x3 surrounding cells, with the reference's tile navigation (:404-448);
+    // i, j here are 0-based cell indices.  Cells of tiles that are not active are skipped
+    // (the reference updates its intermediate copy of a ghost tile there, which only the
+    // last hydraulic RHS of the step would read).
+    auto nb = [&](int t, int d) { return t < 0 ? -1 : A.nbr[t * 8 + d]; };
+    int ct, ci, cj;
+    if (i == 0) { ct = sW; ci = nX - 1; }
+    else { ct = s; ci = i - 1; }
+    for (int k = -1; k <= 1; ++k) {
+        if (j == 0) { ct = nb(ct, NB_S); cj = nY - 1; }
+        else cj = j - 1;
+        for (int l = -1; l <= 1; ++l) {
+            if (ct >= 0 && A.kind[ct] == SLOT_ACTIVE) {
+                cell_topo_ij(P, A, tnew, ct, ci, cj);
+                size_t cc = (size_t)cj * nX + ci;
+                double dbc = C3[mp(ct, 4, 1, SC) + cc] - C0[mp(ct, 4, 1, SC) + cc];
+                double go = gam_of(P.geo, C0[mp(ct, 4, 2, SC) + cc], C0[mp(ct, 4, 3, SC) + cc]);
+                double gn = gam_of(P.geo, C3[mp(ct, 4, 2, SC) + cc], C3[mp(ct, 4, 3, SC) + cc]);
+                double Hno = compute_hn(A.Q[qa][mp(ct, 4, 0, SC) + cc], C0[mp(ct, 4, 0, SC) + cc], C0[mp(ct, 4, 1, SC) + cc], go);
+                if (Hno < 0.0) Hno = 0.0;
+                double w = C3[mp(ct, 4, 1, SC) + cc];
+                w = w + (Hno * go / gn - dbc / gn) / gn;
+                w = w + C3[mp(ct, 4, 0, SC) + cc];
+                A.MS[mp(ct, 5, 0, SC) + cc] = w;
+                double Hnpsiold = A.Q[qa][mp(ct, 4, 3, SC) + cc];
+                A.MS[mp(ct, 5, 1, SC) + cc] = Hnpsiold * go / gn - (1.0 - P.BedPorosity) * dbc / gn;
+            }
+            cj = cj + 1;
+            if (cj == nY && l < 1) { ct = nb(ct, NB_N); cj = 0; }
+        }
+        if (j + 1 > nY - 1) ct = nb(ct, NB_S);
+        ci = ci + 1;
+        if (ci == nX) { ct = nb(ct, NB_E); ci = 0; }
+    }
+    return true;
+}
+
+// RedistributeGrid (src/Redistribute.f90:203-244) over the ordered candidate list.
+__global__ void k_m_redist(DevArrays A, const int* __restrict__ list_slot, const int* __restrict__ list_cell, int n, int qa,
+                           int tcur, int tnew, int* flags) {
+    const DevParams& P = cP;
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int q = 0; q < n; ++q) {
+        int s = list_slot[q], c = list_cell[q];
+        double ex, dBt, psiold, Ho, Hn;
+        excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
+        if (ex > kEPS) {
+            if (!redistribute_cell(P, A, qa, tcur, tnew, s, c % P.nX, c / P.nX, ex)) {
+                atomicOr(flags, 1);
+                return;
+            }
+        }
+    }
+}
+
+// The M result becomes the input of the second hydraulic step: w and Hnpsi from the stage
+// state, momenta unchanged.
+__global__ void k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
+    int s = slots[blockIdx.x];
+    int SC = cP.nX * cP.nY;
+    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+        A.Q[qa][mp(s, 4, 0, SC) + c] = A.MS[mp(s, 5, 0, SC) + c];
+        A.Q[qa][mp(s, 4, 3, SC) + c] = A.MS[mp(s, 5, 1, SC) + c];
+    }
+}
+
+// ---- host launchers ----
+cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, cudaStream_t st) {
+    k_m_init<<<n, 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
+    return cudaGetLastError();
+}
+cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int tnew, cudaStream_t st) {
+    k_m_emd<<<n, 256, 0, st>>>(A, d_slots, tnew);
+    return cudaGetLastError();
+}
+cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int tcur, int tnew, int stage, double dt, cudaStream_t st) {
+    k_m_bt<<<n, 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
+    return cudaGetLastError();
+}
+cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, cudaStream_t st) {
+    k_m_cells<<<n, 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
+    return cudaGetLastError();
+}
+cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, int* flags,
+                           unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st) {
+    k_m_check<<<n, 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
+    return cudaGetLastError();
+}
+cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, int n, int qa, int tcur, int tnew, int* flags,
+                            cudaStream_t st) {
+    k_m_redist<<<1, 32, 0, st>>>(A, ls, lc, n, qa, tcur, tnew, flags);
+    return cudaGetLastError();
+}
+cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int qa, cudaStream_t st) {
+    k_m_finish<<<n, 256, 0, st>>>(A, d_slots, qa);
+    return cudaGetLastError();
+}
+
+}  // namespace kg

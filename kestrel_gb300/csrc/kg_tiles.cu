@@ -21,12 +21,13 @@ namespace kg {
 __device__ __forceinline__ size_t pl(int slot, int nf, int f, int npl) { return ((size_t)slot * nf + f) * (size_t)npl; }
 
 // One CTA per listed slot.
-__global__ void k_cell_topo(DevArrays A, const int* __restrict__ slots) {
+__global__ void k_cell_topo(DevArrays A, const int* __restrict__ slots, int ts) {
     const DevParams& P = cP;
     int s = slots[blockIdx.x];
     int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
-    const double* b0 = A.BV + pl(s, 2, 0, SV);
-    const double* bt = A.BV + pl(s, 2, 1, SV);
+    const double* b0 = A.BV[ts] + pl(s, 2, 0, SV);
+    const double* bt = A.BV[ts] + pl(s, 2, 1, SV);
+    double* CT = A.CT[ts];
     for (int c = threadIdx.x; c < SC; c += blockDim.x) {
         int i = c % nX, j = c / nX;
         int v00 = j * (nX + 1) + i, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
@@ -34,48 +35,51 @@ __global__ void k_cell_topo(DevArrays A, const int* __restrict__ slots) {
         double btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
         double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
         double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
-        A.CT[pl(s, 4, 0, SC) + c] = b0c;
-        A.CT[pl(s, 4, 1, SC) + c] = btc;
-        A.CT[pl(s, 4, 2, SC) + c] = 0.5 * P.dxR * kahan8(ax);
-        A.CT[pl(s, 4, 3, SC) + c] = 0.5 * P.dyR * kahan8(ay);
+        CT[pl(s, 4, 0, SC) + c] = b0c;
+        CT[pl(s, 4, 1, SC) + c] = btc;
+        CT[pl(s, 4, 2, SC) + c] = 0.5 * P.dxR * kahan8(ax);
+        CT[pl(s, 4, 3, SC) + c] = 0.5 * P.dyR * kahan8(ay);
     }
 }
 
-__global__ void k_face_bI(DevArrays A, const int* __restrict__ slots) {
+__global__ void k_face_bI(DevArrays A, const int* __restrict__ slots, int ts) {
     const DevParams& P = cP;
     int s = slots[blockIdx.x];
     int nX = P.nX, nY = P.nY, SV = (nX + 1) * (nY + 1), SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
-    const double* b0 = A.BV + pl(s, 2, 0, SV);
-    const double* bt = A.BV + pl(s, 2, 1, SV);
+    const double* b0 = A.BV[ts] + pl(s, 2, 0, SV);
+    const double* bt = A.BV[ts] + pl(s, 2, 1, SV);
     for (int f = threadIdx.x; f < SFX; f += blockDim.x) {
         int a = f % (nX + 1), j = f / (nX + 1);
         int v0 = j * (nX + 1) + a, v1 = v0 + (nX + 1);
-        A.FX[pl(s, 5, 4, SFX) + f] = interp_b(b0[v0], b0[v1], bt[v0], bt[v1]);
+        A.FX[ts][pl(s, 5, 4, SFX) + f] = interp_b(b0[v0], b0[v1], bt[v0], bt[v1]);
     }
     for (int f = threadIdx.x; f < SFY; f += blockDim.x) {
         int i = f % nX, a = f / nX;
         int v0 = a * (nX + 1) + i, v1 = v0 + 1;
-        A.FY[pl(s, 5, 4, SFY) + f] = interp_b(b0[v0], b0[v1], bt[v0], bt[v1]);
+        A.FY[ts][pl(s, 5, 4, SFY) + f] = interp_b(b0[v0], b0[v1], bt[v0], bt[v1]);
     }
 }
 
 // Face bt and slopes of one tile from its own vertices and the adjacent column/row of
 // the W/E/S/N tiles' vertex copies.
-__global__ void k_face_topo(DevArrays A, const int* __restrict__ slots) {
+__global__ void k_face_topo(DevArrays A, const int* __restrict__ slots, int ts) {
     const DevParams& P = cP;
     int s = slots[blockIdx.x];
     int nX = P.nX, nY = P.nY, SV = (nX + 1) * (nY + 1), SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
     int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sS = A.nbr[s * 8 + NB_S], sN = A.nbr[s * 8 + NB_N];
-    const double* b0 = A.BV + pl(s, 2, 0, SV);
-    const double* bt = A.BV + pl(s, 2, 1, SV);
+    const double* BV = A.BV[ts];
+    double* FXs = A.FX[ts];
+    double* FYs = A.FY[ts];
+    const double* b0 = BV + pl(s, 2, 0, SV);
+    const double* bt = BV + pl(s, 2, 1, SV);
     const int V = nX + 1;
     for (int f = threadIdx.x; f < SFX; f += blockDim.x) {
         int a = f % (nX + 1), j = f / (nX + 1);  // vertex column a, rows j..j+1
         // d/dx from the vertex columns either side (the W/E tile's copy at the tile edge)
         const double *lb0 = b0, *lbt = bt, *rb0 = b0, *rbt = bt;
         int la = a - 1, ra = a + 1;
-        if (a == 0) { lb0 = A.BV + pl(sW, 2, 0, SV); lbt = A.BV + pl(sW, 2, 1, SV); la = nX - 1; }
-        if (a == nX) { rb0 = A.BV + pl(sE, 2, 0, SV); rbt = A.BV + pl(sE, 2, 1, SV); ra = 1; }
+        if (a == 0) { lb0 = BV + pl(sW, 2, 0, SV); lbt = BV + pl(sW, 2, 1, SV); la = nX - 1; }
+        if (a == nX) { rb0 = BV + pl(sE, 2, 0, SV); rbt = BV + pl(sE, 2, 1, SV); ra = 1; }
         double ax[8] = {rb0[j * V + ra], rbt[j * V + ra], rb0[(j + 1) * V + ra], rbt[(j + 1) * V + ra],
                         -lb0[j * V + la], -lbt[j * V + la], -lb0[(j + 1) * V + la], -lbt[(j + 1) * V + la]};
         double dbdx = 0.25 * P.dxR * kahan8(ax);
@@ -83,9 +87,9 @@ __global__ void k_face_topo(DevArrays A, const int* __restrict__ slots) {
         double btf = 0.5 * (bt[v0] + bt[v1]);
         double ay[4] = {b0[v1], bt[v1], -b0[v0], -bt[v0]};
         double dbdy = P.dyR * kahan4(ay[0], ay[1], ay[2], ay[3]);
-        A.FX[pl(s, 5, 1, SFX) + f] = btf;
-        A.FX[pl(s, 5, 2, SFX) + f] = dbdx;
-        A.FX[pl(s, 5, 3, SFX) + f] = dbdy;
+        FXs[pl(s, 5, 1, SFX) + f] = btf;
+        FXs[pl(s, 5, 2, SFX) + f] = dbdx;
+        FXs[pl(s, 5, 3, SFX) + f] = dbdy;
     }
     for (int f = threadIdx.x; f < SFY; f += blockDim.x) {
         int i = f % nX, a = f / nX;  // vertex row a, columns i..i+1
@@ -95,39 +99,40 @@ __global__ void k_face_topo(DevArrays A, const int* __restrict__ slots) {
         double dbdx = P.dxR * kahan4(axv[0], axv[1], axv[2], axv[3]);
         const double *db0 = b0, *dbt = bt, *ub0 = b0, *ubt = bt;
         int da = a - 1, ua = a + 1;
-        if (a == 0) { db0 = A.BV + pl(sS, 2, 0, SV); dbt = A.BV + pl(sS, 2, 1, SV); da = nY - 1; }
-        if (a == nY) { ub0 = A.BV + pl(sN, 2, 0, SV); ubt = A.BV + pl(sN, 2, 1, SV); ua = 1; }
+        if (a == 0) { db0 = BV + pl(sS, 2, 0, SV); dbt = BV + pl(sS, 2, 1, SV); da = nY - 1; }
+        if (a == nY) { ub0 = BV + pl(sN, 2, 0, SV); ubt = BV + pl(sN, 2, 1, SV); ua = 1; }
         double ay[8] = {ub0[ua * V + i + 1], ubt[ua * V + i + 1], ub0[ua * V + i], ubt[ua * V + i],
                         -db0[da * V + i + 1], -dbt[da * V + i + 1], -db0[da * V + i], -dbt[da * V + i]};
         double dbdy = 0.25 * P.dyR * kahan8(ay);
-        A.FY[pl(s, 5, 1, SFY) + f] = btf;
-        A.FY[pl(s, 5, 2, SFY) + f] = dbdx;
-        A.FY[pl(s, 5, 3, SFY) + f] = dbdy;
+        FYs[pl(s, 5, 1, SFY) + f] = btf;
+        FYs[pl(s, 5, 2, SFY) + f] = dbdx;
+        FYs[pl(s, 5, 3, SFY) + f] = dbdy;
     }
 }
 
 // mode 0: default data (w = b0, rho = rhow, rest 0; SetDefaultTileData); 2: a periodic
 // domain-edge ghost, which SetDomainBoundaryData leaves as allocated (zeros, rho = rhow).
-__global__ void k_ghost_bc(DevArrays A, int slot, int mode) {
+__global__ void k_ghost_bc(DevArrays A, int slot, int mode, int ts) {
     const DevParams& P = cP;
     int SC = P.nX * P.nY;
     double* G = A.G9 + pl(slot, 9, 0, SC);
     for (int c = threadIdx.x; c < SC; c += blockDim.x) {
         for (int f = 0; f < 8; ++f) G[f * (size_t)SC + c] = 0.0;
         G[8 * (size_t)SC + c] = P.rhow;
-        if (mode == 0) G[c] = A.CT[pl(slot, 4, 0, SC) + c];
+        if (mode == 0) G[c] = A.CT[ts][pl(slot, 4, 0, SC) + c];
     }
 }
 
 // Dirichlet data (SetDomainBoundaryData 'dirichlet', src/UpdateTiles.f90:614-638).
-__global__ void k_ghost_dirichlet(DevArrays A, int slot, double Hnval, double uval, double vval, double psival) {
+__global__ void k_ghost_dirichlet(DevArrays A, int slot, double Hnval, double uval, double vval, double psival, int ts) {
     const DevParams& P = cP;
     int SC = P.nX * P.nY;
     double* G = A.G9 + pl(slot, 9, 0, SC);
     double rho = density(P, psival);
     for (int c = threadIdx.x; c < SC; c += blockDim.x) {
-        double b0 = A.CT[pl(slot, 4, 0, SC) + c], bt = A.CT[pl(slot, 4, 1, SC) + c];
-        double dbx = A.CT[pl(slot, 4, 2, SC) + c], dby = A.CT[pl(slot, 4, 3, SC) + c];
+        const double* CT = A.CT[ts];
+        double b0 = CT[pl(slot, 4, 0, SC) + c], bt = CT[pl(slot, 4, 1, SC) + c];
+        double dbx = CT[pl(slot, 4, 2, SC) + c], dby = CT[pl(slot, 4, 3, SC) + c];
         double hpval = Hnval / gam_of(P.geo, dbx, dby);
         double w = bt + hpval;
         w = w + b0;
@@ -194,21 +199,20 @@ __global__ void k_ghost_edges(DevArrays A, int slot, int mask, int qcur) {
 }
 
 // ActivateTile: w = cell b0, cell bt = 0, momenta and Hnpsi as the tile held them (zero).
-__global__ void k_activate(DevArrays A, int slot, int qcur) {
+__global__ void k_activate(DevArrays A, int slot, int qcur, int ts) {
     const DevParams& P = cP;
     int SC = P.nX * P.nY;
     for (int c = threadIdx.x; c < SC; c += blockDim.x) {
-        double b0 = A.CT[pl(slot, 4, 0, SC) + c];
-        A.CT[pl(slot, 4, 1, SC) + c] = 0.0;
-        for (int b = 0; b < 2; ++b) {
-            double* Q = A.Q[b == 0 ? qcur : 1 - qcur];
-            Q[pl(slot, 4, 0, SC) + c] = b0;
-            Q[pl(slot, 4, 1, SC) + c] = 0.0;
-            Q[pl(slot, 4, 2, SC) + c] = 0.0;
-            Q[pl(slot, 4, 3, SC) + c] = 0.0;
-        }
+        double b0 = A.CT[ts][pl(slot, 4, 0, SC) + c];
+        A.CT[ts][pl(slot, 4, 1, SC) + c] = 0.0;
+        double* Q = A.Q[qcur];
+        Q[pl(slot, 4, 0, SC) + c] = b0;
+        Q[pl(slot, 4, 1, SC) + c] = 0.0;
+        Q[pl(slot, 4, 2, SC) + c] = 0.0;
+        Q[pl(slot, 4, 3, SC) + c] = 0.0;
         A.UV[pl(slot, 2, 0, SC) + c] = 0.0;
         A.UV[pl(slot, 2, 1, SC) + c] = 0.0;
+        A.EMD[(size_t)slot * SC + c] = 0.0;
     }
 }
 
@@ -224,7 +228,7 @@ __global__ void k_init_maxima(DevArrays A, int slot) {
 // Edge-band tests of NearNorth/South/East/WestBoundary for each listed active slot:
 // bit 0 N, 1 S, 2 E, 3 W.  hn_over (optional) replaces the depth computed from w (used
 // for the first check after the sources have set the depth field directly).
-__global__ void k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur, const double* __restrict__ hn_over,
+__global__ void k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur, int ts, const double* __restrict__ hn_over,
                             int* __restrict__ flags) {
     const DevParams& P = cP;
     int s = slots[blockIdx.x];
@@ -237,8 +241,9 @@ __global__ void k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur
         if (hn_over) {
             Hn = hn_over[(size_t)s * SC + c];
         } else {
-            double b0 = A.CT[pl(s, 4, 0, SC) + c], bt = A.CT[pl(s, 4, 1, SC) + c];
-            double gam = gam_of(P.geo, A.CT[pl(s, 4, 2, SC) + c], A.CT[pl(s, 4, 3, SC) + c]);
+            const double* CT = A.CT[ts];
+            double b0 = CT[pl(s, 4, 0, SC) + c], bt = CT[pl(s, 4, 1, SC) + c];
+            double gam = gam_of(P.geo, CT[pl(s, 4, 2, SC) + c], CT[pl(s, 4, 3, SC) + c]);
             Hn = compute_hn(Q[pl(s, 4, 0, SC) + c], b0, bt, gam);
             if (Hn < 0.0) Hn = 0.0;
         }
@@ -267,7 +272,7 @@ __global__ void k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur
 }
 
 // Sequential compensated sums over the active tiles in list order (j outer, i inner).
-__global__ void k_volume(DevArrays A, const int* __restrict__ slots, int n, int qcur, const double* __restrict__ hn_over,
+__global__ void k_volume(DevArrays A, const int* __restrict__ slots, int n, int qcur, int ts, const double* __restrict__ hn_over,
                          const double* __restrict__ rho_over, double* out) {
     const DevParams& P = cP;
     int nX = P.nX, nY = P.nY, SC = nX * nY;
@@ -278,8 +283,9 @@ __global__ void k_volume(DevArrays A, const int* __restrict__ slots, int n, int 
         int s = slots[k];
         for (int c = 0; c < SC; ++c) {
             double w = Q[pl(s, 4, 0, SC) + c], p = Q[pl(s, 4, 3, SC) + c];
-            double b0 = A.CT[pl(s, 4, 0, SC) + c], bt = A.CT[pl(s, 4, 1, SC) + c];
-            double gam = gam_of(P.geo, A.CT[pl(s, 4, 2, SC) + c], A.CT[pl(s, 4, 3, SC) + c]);
+            const double* CT = A.CT[ts];
+            double b0 = CT[pl(s, 4, 0, SC) + c], bt = CT[pl(s, 4, 1, SC) + c];
+            double gam = gam_of(P.geo, CT[pl(s, 4, 2, SC) + c], CT[pl(s, 4, 3, SC) + c]);
             double Hn, rho;
             if (hn_over) {
                 Hn = hn_over[(size_t)s * SC + c];
@@ -305,50 +311,50 @@ __global__ void k_volume(DevArrays A, const int* __restrict__ slots, int n, int 
 }
 
 // ---- host launchers ----
-cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, cudaStream_t st) {
+cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_cell_topo<<<n, 256, 0, st>>>(A, d_slots);
+    k_cell_topo<<<n, 256, 0, st>>>(A, d_slots, ts);
     return cudaGetLastError();
 }
-cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, cudaStream_t st) {
+cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_face_bI<<<n, 256, 0, st>>>(A, d_slots);
+    k_face_bI<<<n, 256, 0, st>>>(A, d_slots, ts);
     return cudaGetLastError();
 }
-cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, cudaStream_t st) {
+cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_face_topo<<<n, 256, 0, st>>>(A, d_slots);
+    k_face_topo<<<n, 256, 0, st>>>(A, d_slots, ts);
     return cudaGetLastError();
 }
-cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, cudaStream_t st) {
-    k_ghost_bc<<<1, 256, 0, st>>>(A, slot, mode);
+cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, int ts, cudaStream_t st) {
+    k_ghost_bc<<<1, 256, 0, st>>>(A, slot, mode, ts);
     return cudaGetLastError();
 }
-cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, double u, double v, double psi, cudaStream_t st) {
-    k_ghost_dirichlet<<<1, 256, 0, st>>>(A, slot, H, u, v, psi);
+cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, double u, double v, double psi, int ts, cudaStream_t st) {
+    k_ghost_dirichlet<<<1, 256, 0, st>>>(A, slot, H, u, v, psi, ts);
     return cudaGetLastError();
 }
 cudaError_t launch_ghost_edges(const DevArrays& A, int slot, int mask, int qcur, cudaStream_t st) {
     k_ghost_edges<<<1, 256, 0, st>>>(A, slot, mask, qcur);
     return cudaGetLastError();
 }
-cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, cudaStream_t st) {
-    k_activate<<<1, 256, 0, st>>>(A, slot, qcur);
+cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, int ts, cudaStream_t st) {
+    k_activate<<<1, 256, 0, st>>>(A, slot, qcur, ts);
     return cudaGetLastError();
 }
 cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st) {
     k_init_maxima<<<1, 256, 0, st>>>(A, slot);
     return cudaGetLastError();
 }
-cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, const double* hn_over, int* d_flags,
+cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn_over, int* d_flags,
                              cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_act_flags<<<n, 256, 0, st>>>(A, d_slots, qcur, hn_over, d_flags);
+    k_act_flags<<<n, 256, 0, st>>>(A, d_slots, qcur, ts, hn_over, d_flags);
     return cudaGetLastError();
 }
-cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, const double* hn, const double* rho,
+cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
                           double* d_out, cudaStream_t st) {
-    k_volume<<<1, 1, 0, st>>>(A, d_slots, n, qcur, hn, rho, d_out);
+    k_volume<<<1, 1, 0, st>>>(A, d_slots, n, qcur, ts, hn, rho, d_out);
     return cudaGetLastError();
 }
 

@@ -164,3 +164,42 @@ def test_full_cap_release_to_30s():
     for t in g.active_tiles():
         assert (g.field(t, 5) >= 0).all()
         assert np.isfinite(g.field(t, 1)).all() and np.isfinite(g.field(t, 2)).all()
+
+
+# ---- morphodynamics: transcendental closures (tanh/log/pow) differ in the last bits ----
+
+@pytest.mark.parametrize("name,tend,nout", [
+    ("lake_at_rest_morpho_2d", 1.0, 2),   # periodic single tile, Variable drag, eddy viscosity
+    ("cap_morpho_2d", 0.5, 1),            # erosion/deposition with dt refinements
+    ("flux_morpho_2d", 2.0, 2),           # flux source, morphodynamics
+])
+def test_morpho_parity(name, tend, nout):
+    p = cases.ref_input(name, tend=tend, nout=nout)
+    g, o = pair(p)
+    sg, so = g.run(), o.run()
+    assert (sg.steps, sg.rejected) == (so.steps, so.rejected), (sg.steps, sg.rejected, so.steps, so.rejected)
+    compare_state(g, o, tol=1e-10, what=name)
+    for t in o.active_tiles():
+        assert rel_linf(g.vertex(t, 1), o.vertex(t, 1)) <= 1e-10 or np.max(np.abs(o.vertex(t, 1))) == 0.0
+
+
+def test_morpho_lake_at_rest_exact():
+    p = cases.ref_input("lake_at_rest_morpho_2d", tend=2.0, nout=4)
+    g = lib.simulation(p)
+    h0 = g.field(1, 5).copy()
+    g.run()
+    fmt = np.vectorize(lambda v: "%.10E" % v)
+    assert (fmt(g.field(1, 5)) == fmt(h0)).all()
+
+
+def test_morpho_conservation_gpu():
+    p = cases.ref_input("cap_morpho_2d", tend=1.0, nout=2)
+    g = lib.simulation(p)
+    v0 = g.volume()
+    g.run()
+    v1 = g.volume()
+    phi = p.BedPorosity
+    assert abs((v1[0] + v1[1]) - (v0[0] + v0[1])) / (v0[0] + v0[1]) <= 1e-10
+    assert abs((v1[3] + v1[1] * (1 - phi)) - (v0[3] + v0[1] * (1 - phi))) / (v0[3] + v0[1] * (1 - phi)) <= 1e-10
+    for t in g.active_tiles():
+        assert g.field(t, 11).min() >= -p.EroDepth
