@@ -167,6 +167,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cap_release_256_fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--spinup", type=float, default=None, help="override the workload's untimed spin-up (s)")
+    ap.add_argument("--profile", action="store_true", help="cudaProfilerStart/Stop around the timed steps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -193,7 +195,7 @@ def main():
 
     # ---- device-timed throughput ----
     sim = lib.simulation(p, precision=wl["prec"], b0=b0)
-    spin = wl.get("spinup", 0.0)
+    spin = wl.get("spinup", 0.0) if args.spinup is None else args.spinup
     if spin > 0.0:
         sim.integrate_to(spin)
     stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
@@ -209,6 +211,8 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    if args.profile:
+        torch.cuda.cudart().cudaProfilerStart()
     total_ms, cu, nsteps = 0.0, 0, 0
     evs = []
     for _ in range(args.steps):
@@ -224,6 +228,8 @@ def main():
         if sim.time[0] >= p.tend:
             break
     torch.cuda.synchronize()
+    if args.profile:
+        torch.cuda.cudart().cudaProfilerStop()
     total_ms = sum(a.elapsed_time(b) for a, b in evs)
     if dist:
         dist.barrier()
