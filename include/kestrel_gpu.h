@@ -218,6 +218,17 @@ void* kg_stream(kg_ctx* ctx);
 int  kg_set_kernel_timing(kg_ctx* ctx, int32_t enable);
 int  kg_get_kernel_time(kg_ctx* ctx, double* ms, int64_t* passes);
 
+/* Same as kg_hydraulic_rhs (substep 1..4, advised dt, ddtExplicit/ddtImplicit readable
+   with kg_get_tile_rhs) but allocates nothing: for hosts that own all device memory and do
+   not let a library call cudaMalloc once running.  The pass's scratch (its CFL-minimum
+   word and tile-block list) lives in one static device array of about 1 MiB that every
+   GPU loading the library keeps until exit; at most 65,536 blocks of 16x16 cells (about
+   16.7 M active cells) are accepted, more is KG_ERR_PARAM.  All calls share that array, so
+   calls that overlap on the GPU race.  The first call on a device looks up the array's
+   address (cudaGetSymbolAddress, once per device); make it before any stream capture.
+   No counterpart in the reference. */
+int  kg_hydraulic_rhs_noalloc(kg_ctx* ctx, double t, int32_t substep, double* advised_dt);
+
 #ifdef __cplusplus
 }
 #endif

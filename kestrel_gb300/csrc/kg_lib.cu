@@ -5,3 +5,4 @@
 
 #include "kg_morpho.cu"
 #include "kg_engine.cu"
+#include "kg_noalloc.cu"
