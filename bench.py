@@ -48,13 +48,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel: str, workload: str):
-    """dram bytes per pass from a committed ncu summary (profiles/<kernel>_<workload>.md)."""
+def profile_traffic(kernel: str, workload: str, cells: float):
+    """DRAM bytes per pass, scaled to `cells` active cells from the bytes per cell and pass
+    of a committed ncu capture (profiles/<kernel>_<workload>.md): the capture runs a
+    smaller active set of the same workload and traffic grows with the cells processed."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
         return None
-    m = re.search(r"dram_bytes_per_pass:\s*([0-9.eE+]+)", open(path).read())
-    return float(m.group(1)) if m else None
+    m = re.search(r"dram_bytes_per_cell_pass:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) * cells if m else None
 
 
 class ClockSampler:
@@ -287,7 +289,7 @@ def main():
     alg_pass = alg / 4.0 * (cu / max(nsteps, 1))
     achieved = alg_pass / (pass_ms / 1e3) / 1e9 if pass_ms > 0 else None
     peak, peak_kind = measured_peaks()
-    traffic = profile_traffic("k_hydro", args.workload)
+    traffic = profile_traffic("k_hydro", args.workload, cu / max(nsteps, 1) / (2.0 if p.MorphodynamicsOn else 1.0))
     line = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": nsteps,
         "warmup": args.warmup, "ms_per_step": total_ms / max(nsteps, 1), "higher_is_better": True, "scaling": "weak",
