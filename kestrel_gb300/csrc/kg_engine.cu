@@ -41,15 +41,16 @@ cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int 
 cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
                           double* d_out, cudaStream_t st);
 // kg_morpho.cu
-cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, cudaStream_t st);
-cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int tnew, cudaStream_t st);
-cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int tcur, int tnew, int stage, double dt, cudaStream_t st);
-cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, cudaStream_t st);
-cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, int* flags,
+cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, cudaStream_t st);
+cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, cudaStream_t st);
+cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
+                        cudaStream_t st);
+cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, cudaStream_t st);
+cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
                            unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st);
 cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, int n, int qa, int tcur, int tnew, int* flags,
                             cudaStream_t st);
-cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int qa, cudaStream_t st);
+cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st);
 }  // namespace kg
 
 using namespace kg;
@@ -695,12 +696,12 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
     for (int id : c.active) slots.push_back(T(c, id).slot);
     int n = (int)slots.size();
     upload_list(c, slots);
-    CK(launch_m_init(c.A, c.d_list, n, qa, c.tcur, tnew, c.st));
+    CK(launch_m_init(c.A, c.d_list, n, c.SV, qa, c.tcur, tnew, c.st));
     c.launches++;
     for (int stage = 1; stage <= 3; ++stage) {
-        CK(launch_m_emd(c.A, c.d_list, n, tnew, c.st));
-        CK(launch_m_bt(c.A, c.d_list, n, c.tcur, tnew, stage, dt_m, c.st));
-        CK(launch_m_cells(c.A, c.d_list, n, qa, c.tcur, tnew, c.st));
+        CK(launch_m_emd(c.A, c.d_list, n, c.SC, tnew, c.st));
+        CK(launch_m_bt(c.A, c.d_list, n, c.SV, c.tcur, tnew, stage, dt_m, c.st));
+        CK(launch_m_cells(c.A, c.d_list, n, c.SC, qa, c.tcur, tnew, c.st));
         c.launches += 3;
     }
     int need = n * c.SC;
@@ -718,7 +719,7 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
     }
     CK(cudaMemsetAsync(c.d_mflags, 0, sizeof(int), c.st));
     CK(cudaMemsetAsync(c.d_ncand, 0, sizeof(int), c.st));
-    CK(launch_m_check(c.A, c.d_list, n, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, c.st));
+    CK(launch_m_check(c.A, c.d_list, n, c.SC, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, c.st));
     c.launches++;
     int hf[2];
     CK(cudaMemcpyAsync(&hf[0], c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
@@ -761,7 +762,7 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
     upload_list(c, slots);
     CK(launch_face_topo(c.A, c.d_list, n, tnew, c.st));
     CK(launch_face_bI(c.A, c.d_list, n, tnew, c.st));
-    CK(launch_m_finish(c.A, c.d_list, n, qa, c.st));
+    CK(launch_m_finish(c.A, c.d_list, n, c.SC, qa, c.st));
     c.launches += 3;
     return false;
 }

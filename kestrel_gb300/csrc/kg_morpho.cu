@@ -28,16 +28,24 @@ __device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return 
 
 // Copy the step-start bed into the M set and fill the stage state of im0 (the state the
 // first hydraulic step produced).
-__global__ void k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
+// Grid: one thread per cell / vertex, `per` CTAs of 256 threads per listed tile.
+#define KG_TILE_THREAD(NITEMS)                              \
+    int per_ = ((NITEMS) + 255) / 256;                      \
+    int s = slots[blockIdx.x / per_];                       \
+    int item_ = (blockIdx.x % per_) * 256 + threadIdx.x;
+
+__global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
     const DevParams& P = cP;
-    int s = slots[blockIdx.x];
     int SC = P.nX * P.nY, SV = (P.nX + 1) * (P.nY + 1);
-    for (int v = threadIdx.x; v < SV; v += blockDim.x) {
+    KG_TILE_THREAD(SV)
+    if (item_ < SV) {
+        int v = item_;
         A.BV[tnew][mp(s, 2, 0, SV) + v] = A.BV[tcur][mp(s, 2, 0, SV) + v];
         A.BV[tnew][mp(s, 2, 1, SV) + v] = A.BV[tcur][mp(s, 2, 1, SV) + v];
     }
     double e2 = P.hThr * P.hThr;
-    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+    if (item_ < SC) {
+        int c = item_;
         double ct[4];
         for (int f = 0; f < 4; ++f) {
             ct[f] = A.CT[tcur][mp(s, 4, f, SC) + c];
@@ -64,13 +72,14 @@ __device__ __forceinline__ double stage_hn(const DevArrays& A, int s, int c, int
     return A.kind[s] == SLOT_GHOST ? A.G9[mp(s, 9, 4, SC) + c] : A.MS[mp(s, 5, 2, SC) + c];
 }
 
-__global__ void k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
+__global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
     const DevParams& P = cP;
-    int s = slots[blockIdx.x];
     int nX = P.nX, nY = P.nY, SC = nX * nY;
+    KG_TILE_THREAD(SC)
     int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sN = A.nbr[s * 8 + NB_N], sS = A.nbr[s * 8 + NB_S];
     const double* CT = A.CT[tnew];
-    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+    if (item_ < SC) {
+        int c = item_;
         int i = c % nX, j = c / nX;
         double Hn = A.MS[mp(s, 5, 2, SC) + c];
         double HnW = (i == 0) ? stage_hn(A, sW, j * nX + nX - 1, SC) : A.MS[mp(s, 5, 2, SC) + c - 1];
@@ -98,16 +107,17 @@ __device__ __forceinline__ double cellv(const DevArrays& A, const double* CT, in
 }
 
 // Vertex source term and clamped stage update of bt (one CTA per tile).
-__global__ void k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt) {
+__global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt) {
     const DevParams& P = cP;
-    int s = slots[blockIdx.x];
     int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
+    KG_TILE_THREAD(SV)
     const double* CT = A.CT[tnew];
     int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sN = A.nbr[s * 8 + NB_N], sS = A.nbr[s * 8 + NB_S];
     int sSW = sW < 0 ? -1 : A.nbr[sW * 8 + NB_S], sSE = sE < 0 ? -1 : A.nbr[sE * 8 + NB_S];
     int sNW = sW < 0 ? -1 : A.nbr[sW * 8 + NB_N], sNE = sE < 0 ? -1 : A.nbr[sE * 8 + NB_N];
     double psib = 1.0 - P.BedPorosity;
-    for (int v = threadIdx.x; v < SV; v += blockDim.x) {
+    if (item_ < SV) {
+        int v = item_;
         int a = v % (nX + 1), b = v / (nX + 1);  // vertex (a, b), 0-based
         // The four cells around the vertex in the reference's list order, as (slot, i, j).
         int cs[4], ci[4], cj[4];
@@ -183,14 +193,15 @@ __global__ void k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int
 
 // Cell-centred bed of stage k, the conservative w / Hnpsi update and the stage's depth,
 // solids fraction and density.
-__global__ void k_m_cells(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
+__global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
     const DevParams& P = cP;
-    int s = slots[blockIdx.x];
     int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
+    KG_TILE_THREAD(SC)
     const double* b0 = A.BV[tnew] + mp(s, 2, 0, SV);
     const double* bt = A.BV[tnew] + mp(s, 2, 1, SV);
     double psib = 1.0 - P.BedPorosity, e2 = P.hThr * P.hThr;
-    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+    if (item_ < SC) {
+        int c = item_;
         int i = c % nX, j = c / nX;
         int v00 = j * (nX + 1) + i, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
         double b0c = 0.25 * kahan4(b0[v00], b0[v10], b0[v01], b0[v11]);
@@ -249,12 +260,14 @@ __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevA
 // The two tests of src/TimeStepper.f90:709-753 for every active cell.  flags[0] is set
 // when the step must be refined; redistribution candidates are appended with their loop
 // position (tile position in the active list, then j, then i) so the host can order them.
-__global__ void k_m_check(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew, int* flags,
+__global__ void __launch_bounds__(256) k_m_check(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew, int* flags,
                           unsigned long long* cand_key, double* cand_ex, int* ncand, int cand_cap) {
     const DevParams& P = cP;
-    int s = slots[blockIdx.x];
     int SC = P.nX * P.nY;
-    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+    KG_TILE_THREAD(SC)
+    int pos = blockIdx.x / per_;
+    if (item_ < SC) {
+        int c = item_;
         double ex, dBt, psiold, Hn_old, Hn_new;
         excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Hn_old, Hn_new);
         bool refine = false;
@@ -262,7 +275,7 @@ __global__ void k_m_check(DevArrays A, const int* __restrict__ slots, int qa, in
             if (Hn_old < P.EroCriticalHeight || fabs(Hn_new - Hn_old) < P.EroCriticalHeight) {
                 int k = atomicAdd(ncand, 1);
                 if (k < cand_cap) {
-                    cand_key[k] = ((unsigned long long)blockIdx.x << 32) | (unsigned long long)c;
+                    cand_key[k] = ((unsigned long long)pos << 32) | (unsigned long long)c;
                     cand_ex[k] = ex;
                 }
             } else {
@@ -420,35 +433,39 @@ __global__ void k_m_redist(DevArrays A, const int* __restrict__ list_slot, const
 
 // The M result becomes the input of the second hydraulic step: w and Hnpsi from the stage
 // state, momenta unchanged.
-__global__ void k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
-    int s = slots[blockIdx.x];
+__global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
     int SC = cP.nX * cP.nY;
-    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+    KG_TILE_THREAD(SC)
+    if (item_ < SC) {
+        int c = item_;
         A.Q[qa][mp(s, 4, 0, SC) + c] = A.MS[mp(s, 5, 0, SC) + c];
         A.Q[qa][mp(s, 4, 3, SC) + c] = A.MS[mp(s, 5, 1, SC) + c];
     }
 }
 
-// ---- host launchers ----
-cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, cudaStream_t st) {
-    k_m_init<<<n, 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
+// ---- host launchers (cells/verts: items per tile) ----
+static inline int per_of(int items) { return (items + 255) / 256; }
+
+cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, cudaStream_t st) {
+    k_m_init<<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
     return cudaGetLastError();
 }
-cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int tnew, cudaStream_t st) {
-    k_m_emd<<<n, 256, 0, st>>>(A, d_slots, tnew);
+cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, cudaStream_t st) {
+    k_m_emd<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, tnew);
     return cudaGetLastError();
 }
-cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int tcur, int tnew, int stage, double dt, cudaStream_t st) {
-    k_m_bt<<<n, 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
+cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
+                        cudaStream_t st) {
+    k_m_bt<<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
     return cudaGetLastError();
 }
-cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, cudaStream_t st) {
-    k_m_cells<<<n, 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
+cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, cudaStream_t st) {
+    k_m_cells<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
     return cudaGetLastError();
 }
-cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int qa, int tcur, int tnew, int* flags,
+cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
                            unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st) {
-    k_m_check<<<n, 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
+    k_m_check<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
     return cudaGetLastError();
 }
 cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, int n, int qa, int tcur, int tnew, int* flags,
@@ -456,8 +473,8 @@ cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, in
     k_m_redist<<<1, 32, 0, st>>>(A, ls, lc, n, qa, tcur, tnew, flags);
     return cudaGetLastError();
 }
-cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int qa, cudaStream_t st) {
-    k_m_finish<<<n, 256, 0, st>>>(A, d_slots, qa);
+cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st) {
+    k_m_finish<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa);
     return cudaGetLastError();
 }
 
