@@ -217,6 +217,10 @@ void* kg_stream(kg_ctx* ctx);
    No reference counterpart. */
 int  kg_set_kernel_timing(kg_ctx* ctx, int32_t enable);
 int  kg_get_kernel_time(kg_ctx* ctx, double* ms, int64_t* passes);
+/* Redistribution work so far (RedistributeGrid, src/Redistribute.f90:203-244): the number
+   of listed cells walked, the dependency waves they were run in and the walks.  No
+   reference counterpart (the reference walks its list serially). */
+int  kg_redistribution_stats(kg_ctx* ctx, int64_t* cells, int64_t* waves, int64_t* walks);
 
 /* Same as kg_hydraulic_rhs (substep 1..4, advised dt, ddtExplicit/ddtImplicit readable
    with kg_get_tile_rhs) but allocates nothing: for hosts that own all device memory and do

@@ -109,6 +109,7 @@ def declare(lib, prefix):
         "get_tile_maxima": ([vp, C.c_int32, C.c_int32, P(C.c_double)], C.c_int),
         "volume": ([vp, P(C.c_double)], C.c_int),
         "get_time": ([vp, P(C.c_double), P(C.c_double)], C.c_int),
+        "redistribution_stats": ([vp, P(C.c_int64), P(C.c_int64), P(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, f"{prefix}_{name}")

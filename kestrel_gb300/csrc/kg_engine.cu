@@ -48,8 +48,8 @@ cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts
 cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, cudaStream_t st);
 cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
                            unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st);
-cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, int n, int qa, int tcur, int tnew, int* flags,
-                            cudaStream_t st);
+cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, int nwaves, int qa, int tcur,
+                            int tnew, int* flags, cudaStream_t st);
 cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st);
 }  // namespace kg
 
@@ -125,9 +125,12 @@ struct kg_ctx {
     double* d_cex = nullptr;
     int* d_rslot = nullptr;
     int* d_rcell = nullptr;
+    int* d_rwave = nullptr;              // wave offsets of the redistribution list
     int cand_cap = 0;
+    std::vector<std::vector<int>> redist_grid;  // per-tile wave tables of the redistribution scheduler
     double t = 0.0, dt = 1.0e-5, t0 = 0.0;
     int64_t launches = 0, steps = 0, rejected = 0, cell_updates = 0;
+    int64_t redist_cells = 0, redist_waves = 0, redist_walks = 0;
     bool blocks_dirty = true;
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -689,6 +692,67 @@ double rhs0(kg_ctx& c, int q_in, int e_set, int topo, double t, int substep = 1)
     return advised(c, run_pass(c, S), substep);
 }
 
+// Dependency waves of the ordered redistribution list (see k_m_redist): candidate q goes
+// to wave 1 + the largest wave among the earlier candidates whose cell lies within 2 cells
+// of its own (with wrap-around on periodic domains).  The lists come back grouped by wave,
+// list order kept inside each wave; woff holds the wave offsets.
+void redistribution_waves(kg_ctx& c, const std::vector<int>& slots, const std::vector<unsigned long long>& key,
+                          const std::vector<int>& ord, std::vector<int>& ls, std::vector<int>& lc, std::vector<int>& woff) {
+    const int n = (int)ord.size();
+    const long long NXc = (long long)c.p.nXtiles * c.nX, NYc = (long long)c.p.nYtiles * c.nY;
+    const bool per = c.p.bcs == KG_BC_PERIODIC;
+    std::vector<long long> gx((size_t)n), gy((size_t)n);
+    std::vector<int> qs((size_t)n), qc((size_t)n);
+    for (int q = 0; q < n; ++q) {
+        unsigned long long k = key[(size_t)ord[(size_t)q]];
+        int s = slots[(size_t)(k >> 32)], cell = (int)(k & 0xffffffffull);
+        int id = c.slot_tile[(size_t)s];
+        qs[(size_t)q] = s;
+        qc[(size_t)q] = cell;
+        gx[(size_t)q] = (long long)((id - 1) % c.p.nXtiles) * c.nX + cell % c.nX;
+        gy[(size_t)q] = (long long)((id - 1) / c.p.nXtiles) * c.nY + cell / c.nX;
+    }
+    // Wave of the latest candidate per cell, kept per tile (tables are allocated the first
+    // time a tile holds a candidate and are cleared again before returning).
+    auto& tab = c.redist_grid;
+    if (tab.size() != (size_t)c.p.nXtiles * c.p.nYtiles) tab.assign((size_t)c.p.nXtiles * c.p.nYtiles, std::vector<int>());
+    auto at = [&](long long x, long long y, bool make) -> int* {
+        if (per) { x = (x % NXc + NXc) % NXc; y = (y % NYc + NYc) % NYc; }
+        if (x < 0 || x >= NXc || y < 0 || y >= NYc) return nullptr;
+        std::vector<int>& t = tab[(size_t)((y / c.nY) * c.p.nXtiles + x / c.nX)];
+        if (t.empty()) {
+            if (!make) return nullptr;
+            t.assign((size_t)c.nX * c.nY, 0);
+        }
+        return &t[(size_t)((y % c.nY) * c.nX + x % c.nX)];
+    };
+    std::vector<int> wave((size_t)n);
+    int nw = 0;
+    for (int q = 0; q < n; ++q) {
+        int m = 0;
+        for (int dy = -2; dy <= 2; ++dy)
+            for (int dx = -2; dx <= 2; ++dx) {
+                const int* v = at(gx[(size_t)q] + dx, gy[(size_t)q] + dy, false);
+                if (v) m = std::max(m, *v);
+            }
+        wave[(size_t)q] = m + 1;
+        *at(gx[(size_t)q], gy[(size_t)q], true) = m + 1;
+        nw = std::max(nw, m + 1);
+    }
+    for (int q = 0; q < n; ++q) *at(gx[(size_t)q], gy[(size_t)q], true) = 0;
+    woff.assign((size_t)nw + 1, 0);
+    for (int q = 0; q < n; ++q) woff[(size_t)wave[(size_t)q]]++;
+    for (int w = 1; w <= nw; ++w) woff[(size_t)w] += woff[(size_t)w - 1];
+    std::vector<int> fill(woff.begin(), woff.end() - 1);
+    ls.assign((size_t)n, 0);
+    lc.assign((size_t)n, 0);
+    for (int q = 0; q < n; ++q) {
+        int at = fill[(size_t)wave[(size_t)q] - 1]++;
+        ls[(size_t)at] = qs[(size_t)q];
+        lc[(size_t)at] = qc[(size_t)q];
+    }
+}
+
 // MorphodynamicTimeStepper (src/TimeStepper.f90:532-781) on state qa (the first hydraulic
 // step's result); builds the new bed in set tnew.  Returns true when dt must be refined.
 bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
@@ -706,12 +770,13 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
     }
     int need = n * c.SC;
     if (need > c.cand_cap) {
-        cudaFree(c.d_ckey); cudaFree(c.d_cex); cudaFree(c.d_rslot); cudaFree(c.d_rcell);
+        cudaFree(c.d_ckey); cudaFree(c.d_cex); cudaFree(c.d_rslot); cudaFree(c.d_rcell); cudaFree(c.d_rwave);
         c.cand_cap = std::max(need, 2 * c.cand_cap);
         CK(cudaMalloc(&c.d_ckey, (size_t)c.cand_cap * sizeof(unsigned long long)));
         CK(cudaMalloc(&c.d_cex, (size_t)c.cand_cap * sizeof(double)));
         CK(cudaMalloc(&c.d_rslot, (size_t)c.cand_cap * sizeof(int)));
         CK(cudaMalloc(&c.d_rcell, (size_t)c.cand_cap * sizeof(int)));
+        CK(cudaMalloc(&c.d_rwave, ((size_t)c.cand_cap + 1) * sizeof(int)));
     }
     if (!c.d_mflags) {
         CK(cudaMalloc(&c.d_mflags, sizeof(int)));
@@ -741,15 +806,16 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
             if (ex[(size_t)a] != ex[(size_t)b]) return ex[(size_t)a] < ex[(size_t)b];
             return key[(size_t)a] < key[(size_t)b];
         });
-        std::vector<int> ls((size_t)ncand), lc((size_t)ncand);
-        for (int q = 0; q < ncand; ++q) {
-            unsigned long long k = key[(size_t)ord[(size_t)q]];
-            ls[(size_t)q] = slots[(size_t)(k >> 32)];
-            lc[(size_t)q] = (int)(k & 0xffffffffull);
-        }
+        std::vector<int> ls, lc, woff;
+        redistribution_waves(c, slots, key, ord, ls, lc, woff);
+        int nw = (int)woff.size() - 1;
+        c.redist_cells += ncand;
+        c.redist_waves += nw;
+        c.redist_walks++;
         CK(cudaMemcpyAsync(c.d_rslot, ls.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
-        CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, ncand, qa, c.tcur, tnew, c.d_mflags, c.st));
+        CK(cudaMemcpyAsync(c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, c.d_rwave, nw, qa, c.tcur, tnew, c.d_mflags, c.st));
         c.launches++;
         CK(cudaMemcpyAsync(&hf[0], c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
         sync(c);
@@ -1092,7 +1158,7 @@ void free_ctx(kg_ctx* c) {
     void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
                     c->d_cfl, c->d_vol, c->d_srcHn, c->d_srcRho, c->d_mflags, c->d_ncand, c->d_ckey, c->d_cex,
-                    c->d_rslot, c->d_rcell};
+                    c->d_rslot, c->d_rcell, c->d_rwave};
     for (void* q : ptrs) cudaFree(q);
     if (c->h_cfl) cudaFreeHost(c->h_cfl);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1367,6 +1433,14 @@ int kg_get_time(kg_ctx* c, double* t, double* dt) {
 }
 
 int64_t kg_kernel_launches(const kg_ctx* c) { return c ? c->launches : 0; }
+
+int kg_redistribution_stats(kg_ctx* c, int64_t* cells, int64_t* waves, int64_t* walks) {
+    if (!c || !cells || !waves || !walks) return KG_ERR_PARAM;
+    *cells = c->redist_cells;
+    *waves = c->redist_waves;
+    *walks = c->redist_walks;
+    return KG_OK;
+}
 
 void* kg_stream(kg_ctx* c) { return c ? (void*)c->st : nullptr; }
 

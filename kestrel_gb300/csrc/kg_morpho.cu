@@ -24,6 +24,8 @@ namespace kg {
 
 // cP is defined in kg_hydro.cu (one translation unit through kg_lib.cu).
 
+constexpr int REDIST_THREADS = 512;
+
 __device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return ((size_t)slot * nf + f) * (size_t)npl; }
 
 // Copy the step-start bed into the M set and fill the stage state of im0 (the state the
@@ -413,20 +415,37 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
     return true;
 }
 
-// RedistributeGrid (src/Redistribute.f90:203-244) over the ordered candidate list.
-__global__ void k_m_redist(DevArrays A, const int* __restrict__ list_slot, const int* __restrict__ list_cell, int n, int qa,
-                           int tcur, int tnew, int* flags) {
+// RedistributeGrid (src/Redistribute.f90:203-244) over the ordered candidate list, run as
+// dependency waves.  Candidate q touches the vertices of its own cell and the cell data of
+// its 3 x 3 neighbourhood, and reads the vertices of that neighbourhood, so two candidates
+// can only interact when their cells are within 2 cells of each other (Chebyshev distance,
+// across tile seams).  The host puts each candidate in wave 1 + the largest wave of the
+// earlier candidates it can interact with; inside a wave no two candidates interact, and
+// every interacting pair keeps the list order, so the result equals the serial walk.
+// One CTA walks the waves with a barrier between them (__syncthreads makes the global
+// writes of a wave visible to the whole CTA).  A cell with no depositional vertex sets
+// flags[0]; the remaining waves are then skipped, as the serial walk stops there.
+__global__ void __launch_bounds__(REDIST_THREADS) k_m_redist(DevArrays A, const int* __restrict__ list_slot,
+                                                             const int* __restrict__ list_cell,
+                                                             const int* __restrict__ wave_off, int nwaves, int qa, int tcur,
+                                                             int tnew, int* flags) {
     const DevParams& P = cP;
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int q = 0; q < n; ++q) {
-        int s = list_slot[q], c = list_cell[q];
-        double ex, dBt, psiold, Ho, Hn;
-        excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
-        if (ex > kEPS) {
-            if (!redistribute_cell(P, A, qa, tcur, tnew, s, c % P.nX, c / P.nX, ex)) {
-                atomicOr(flags, 1);
-                return;
+    __shared__ int failed;
+    if (threadIdx.x == 0) failed = 0;
+    __syncthreads();
+    for (int wv = 0; wv < nwaves; ++wv) {
+        for (int q = wave_off[wv] + threadIdx.x; q < wave_off[wv + 1]; q += blockDim.x) {
+            int s = list_slot[q], c = list_cell[q];
+            double ex, dBt, psiold, Ho, Hn;
+            excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
+            if (ex > kEPS) {
+                if (!redistribute_cell(P, A, qa, tcur, tnew, s, c % P.nX, c / P.nX, ex)) failed = 1;
             }
+        }
+        __syncthreads();
+        if (failed) {
+            if (threadIdx.x == 0) atomicOr(flags, 1);
+            return;
         }
     }
 }
@@ -468,9 +487,10 @@ cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int ce
     k_m_check<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
     return cudaGetLastError();
 }
-cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, int n, int qa, int tcur, int tnew, int* flags,
-                            cudaStream_t st) {
-    k_m_redist<<<1, 32, 0, st>>>(A, ls, lc, n, qa, tcur, tnew, flags);
+cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, int nwaves, int qa, int tcur,
+                            int tnew, int* flags, cudaStream_t st) {
+    if (nwaves == 0) return cudaSuccess;
+    k_m_redist<<<1, REDIST_THREADS, 0, st>>>(A, ls, lc, woff, nwaves, qa, tcur, tnew, flags);
     return cudaGetLastError();
 }
 cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st) {

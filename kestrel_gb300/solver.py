@@ -88,6 +88,12 @@ class Simulation:
         self._check(self._f("hydraulic_rhs")(self.h, t, substep, C.byref(adv)))
         return adv.value
 
+    def redistribution_stats(self):
+        """(cells walked, dependency waves, walks) of RedistributeGrid so far."""
+        v = [C.c_int64() for _ in range(3)]
+        self._check(self._f("redistribution_stats")(self.h, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
     # -- state access --------------------------------------------------------------
     @property
     def time(self):

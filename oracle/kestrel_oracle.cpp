@@ -126,6 +126,7 @@ struct Sim {
     Grid g;
     std::string err;
     int64_t rejected = 0, steps = 0, cell_updates = 0;
+    int64_t redist_cells = 0, redist_walks = 0;  // cells listed for RedistributeGrid, walks
     double last_rhs_dt = 0.0;
     bool sources_loaded = false;
 };
@@ -443,7 +444,11 @@ static bool MorphodynamicTimeStepper(Sim& s, double& thisdt) {
                 }
             }
     }
-    if (!redist.empty() && !refine) RedistributeGrid(rp, g, redist, refine);
+    if (!redist.empty() && !refine) {
+        s.redist_cells += (int64_t)redist.size();
+        s.redist_walks++;
+        RedistributeGrid(rp, g, redist, refine);
+    }
     if (refine) {
         thisdt = 0.5 * thisdt;
         return true;
@@ -961,6 +966,15 @@ int ko_volume(ko_ctx* c, double out[4]) {
     ko::CalculateVolume(c->s, out);
     return KG_OK;
 }
+// The serial walk runs every listed cell in its own wave.
+int ko_redistribution_stats(ko_ctx* c, int64_t* cells, int64_t* waves, int64_t* walks) {
+    if (!c || !cells || !waves || !walks) return KG_ERR_PARAM;
+    *cells = c->s.redist_cells;
+    *waves = c->s.redist_cells;
+    *walks = c->s.redist_walks;
+    return KG_OK;
+}
+
 int ko_get_time(ko_ctx* c, double* t, double* dt) {
     *t = c->s.g.t;
     *dt = c->s.g.dt;

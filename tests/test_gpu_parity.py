@@ -181,6 +181,12 @@ def test_morpho_parity(name, tend, nout):
     compare_state(g, o, tol=1e-10, what=name)
     for t in o.active_tiles():
         assert rel_linf(g.vertex(t, 1), o.vertex(t, 1)) <= 1e-10 or np.max(np.abs(o.vertex(t, 1))) == 0.0
+    # The GPU walks the same redistribution lists, in dependency waves.
+    cg, wg, kg = g.redistribution_stats()
+    co, _, ko = o.redistribution_stats()
+    assert (cg, kg) == (co, ko), (cg, kg, co, ko)
+    if name == "cap_morpho_2d":
+        assert co > 0 and wg < cg, (cg, wg)
 
 
 def test_morpho_lake_at_rest_exact():
