@@ -289,7 +289,8 @@ def main():
     alg_pass = alg / 4.0 * (cu / max(nsteps, 1))
     achieved = alg_pass / (pass_ms / 1e3) / 1e9 if pass_ms > 0 else None
     peak, peak_kind = measured_peaks()
-    traffic = profile_traffic("k_hydro", args.workload, cu / max(nsteps, 1) / (2.0 if p.MorphodynamicsOn else 1.0))
+    kname = "k_hydro" if wl["prec"] == abi.PREC_FP64 else "k_hydro32"
+    traffic = profile_traffic(kname, args.workload, cu / max(nsteps, 1) / (2.0 if p.MorphodynamicsOn else 1.0))
     line = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": nsteps,
         "warmup": args.warmup, "ms_per_step": total_ms / max(nsteps, 1), "higher_is_better": True, "scaling": "weak",
@@ -301,7 +302,7 @@ def main():
                 "d2h_bytes_per_step": d2h / max(n2, 1)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "k_hydro", "pass_ms": pass_ms},
+                     "kernel": kname, "pass_ms": pass_ms},
         "gpu_launches": launches,
         "clocks": clk,
     }

@@ -31,6 +31,9 @@ cudaError_t launch_hydro(const DevArrays& A, const BlockDesc* blocks, int nblock
 cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
 cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
 cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
+// kg_hydro32.cu
+cudaError_t launch_hydro32(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st);
+cudaError_t launch_topo32(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, cudaStream_t st);
 cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, int ts, cudaStream_t st);
 cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, double u, double v, double psi, int ts, cudaStream_t st);
 cudaError_t launch_ghost_edges(const DevArrays& A, int slot, int mask, int qcur, cudaStream_t st);
@@ -118,6 +121,9 @@ struct kg_ctx {
     bool sources_loaded = false;
     int qcur = 0;                        // state buffer holding the solution (0..3)
     int tcur = 0;                        // topography set of the solution (0..1)
+    bool tdirty[2] = {true, true};       // FP32 form: the set's factor cache needs a rebuild
+    int* d_tlist = nullptr;              // slot list of the cache rebuild
+    int d_tlist_cap = 0;
     std::vector<int> touched;            // slots whose step-start topography changed in set-up
     int* d_mflags = nullptr;             // M-operator refine flag
     int* d_ncand = nullptr;
@@ -175,6 +181,12 @@ void ensure_cap(kg_ctx& c, int need) {
         grow_array(c.A.FX[b], o * 5 * (size_t)c.SFX, n * 5 * (size_t)c.SFX, c.st);
         grow_array(c.A.FY[b], o * 5 * (size_t)c.SFY, n * 5 * (size_t)c.SFY, c.st);
         grow_array(c.A.BV[b], o * 2 * (size_t)c.SV, n * 2 * (size_t)c.SV, c.st);
+        if (c.prec == KG_PREC_FP32) {
+            grow_array(c.A.TD[b], o * 3 * SC, n * 3 * SC, c.st);
+            grow_array(c.A.TF[b], o * 6 * SC, n * 6 * SC, c.st);
+            grow_array(c.A.TFX[b], o * 2 * (size_t)c.SFX, n * 2 * (size_t)c.SFX, c.st);
+            grow_array(c.A.TFY[b], o * 2 * (size_t)c.SFY, n * 2 * (size_t)c.SFY, c.st);
+        }
     }
     grow_array(c.A.UV, o * 2 * SC, n * 2 * SC, c.st);
     grow_array(c.A.MS, o * 5 * SC, n * 5 * SC, c.st);
@@ -366,6 +378,7 @@ void push_bed(kg_ctx& c, int s) {
     }
 }
 void touch(kg_ctx& c, int s) {
+    c.tdirty[0] = c.tdirty[1] = true;
     if (std::find(c.touched.begin(), c.touched.end(), s) == c.touched.end()) c.touched.push_back(s);
 }
 // The second topography set of a slot is scratch for active tiles during a step and a
@@ -399,6 +412,7 @@ bool is_active_ghost(kg_ctx& c, int id) { return in_list(c.ghost, id) && T(c, id
 
 // EqualiseTopographicBoundaryData, src/MorphodynamicRHS.f90:588-687 (vertex and face b0).
 void equalise(kg_ctx& c, int id) {
+    c.tdirty[0] = c.tdirty[1] = true;
     int nX = c.nX, nY = c.nY, V = nX + 1;
     auto ok = [&](int t) { return in_bounds(c, t) && (in_list(c.active, t) || is_active_ghost(c, t)); };
     auto B0 = [&](int t) -> std::vector<double>& { return c.hb0[T(c, t).slot]; };
@@ -568,6 +582,7 @@ void add_tile(kg_ctx& c, int k) {
     c.launches++;
     sync(c);
     c.blocks_dirty = true;
+    c.tdirty[0] = c.tdirty[1] = true;
 }
 
 void rebuild_blocks(kg_ctx& c) {
@@ -636,12 +651,33 @@ double advised(kg_ctx& c, unsigned long long bits, int substep) {
     return m;
 }
 
+// FP32 form: rebuild the factor cache of topography set ts for every allocated tile.
+void refresh_topo32(kg_ctx& c, int ts) {
+    std::vector<int> slots;
+    for (int id : c.active) slots.push_back(T(c, id).slot);
+    for (int id : c.ghost) slots.push_back(T(c, id).slot);
+    if ((int)slots.size() > c.d_tlist_cap) {
+        if (c.d_tlist) CK(cudaFree(c.d_tlist));
+        c.d_tlist_cap = std::max<int>((int)slots.size(), 2 * c.d_tlist_cap);
+        CK(cudaMalloc(&c.d_tlist, (size_t)c.d_tlist_cap * sizeof(int)));
+    }
+    if (!slots.empty()) {
+        CK(cudaMemcpyAsync(c.d_tlist, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(launch_topo32(c.A, c.d_tlist, (int)slots.size(), ts, c.nX, c.nY, c.st));
+        c.launches++;
+    }
+    c.tdirty[ts] = false;
+}
+
 unsigned long long run_pass(kg_ctx& c, StepArgs S) {
     *c.h_cfl = (unsigned long long)0x7FEFFFFFFFFFFFFFull;  // bits of huge(1.0_wp)
     CK(cudaMemcpyAsync(c.d_cfl, c.h_cfl, sizeof(unsigned long long), cudaMemcpyHostToDevice, c.st));
     S.cfl_min = c.d_cfl;
+    const bool fp32 = c.prec == KG_PREC_FP32;
+    if (fp32 && c.tdirty[S.topo]) refresh_topo32(c, S.topo);
     if (c.timing) CK(cudaEventRecord(c.ev0, c.st));
-    CK(launch_hydro(c.A, c.d_blocks, (int)c.blocks.size(), S, c.st));
+    if (fp32) CK(launch_hydro32(c.A, c.d_blocks, (int)c.blocks.size(), S, c.st));
+    else CK(launch_hydro(c.A, c.d_blocks, (int)c.blocks.size(), S, c.st));
     if (c.timing) CK(cudaEventRecord(c.ev1, c.st));
     c.launches++;
     CK(cudaMemcpyAsync(c.h_cfl, c.d_cfl, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
@@ -830,6 +866,7 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
     CK(launch_face_bI(c.A, c.d_list, n, tnew, c.st));
     CK(launch_m_finish(c.A, c.d_list, n, c.SC, qa, c.st));
     c.launches += 3;
+    c.tdirty[tnew] = true;
     return false;
 }
 
@@ -1154,7 +1191,9 @@ void free_ctx(kg_ctx* c) {
     for (int b = 0; b < 4; ++b) cudaFree(c->A.Q[b]);
     for (int b = 0; b < 2; ++b) {
         cudaFree(c->A.E[b]); cudaFree(c->A.I[b]); cudaFree(c->A.CT[b]); cudaFree(c->A.FX[b]); cudaFree(c->A.FY[b]); cudaFree(c->A.BV[b]);
+        cudaFree(c->A.TD[b]); cudaFree(c->A.TF[b]); cudaFree(c->A.TFX[b]); cudaFree(c->A.TFY[b]);
     }
+    cudaFree(c->d_tlist);
     void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
                     c->d_cfl, c->d_vol, c->d_srcHn, c->d_srcRho, c->d_mflags, c->d_ncand, c->d_ckey, c->d_cex,
@@ -1215,7 +1254,7 @@ const char* kg_version(void) { return "kestrel_gb300 1.0 (sm_103a)"; }
 int kg_create(const kg_params* params, int32_t precision, kg_ctx** out) {
     if (!params || !out) return KG_ERR_PARAM;
     *out = nullptr;
-    if (precision != KG_PREC_FP64) return KG_ERR_UNSUPPORTED;
+    if (precision != KG_PREC_FP64 && precision != KG_PREC_FP32) return KG_ERR_UNSUPPORTED;
     kg_ctx* c = new kg_ctx();
     c->prec = precision;
     try {

@@ -15,6 +15,11 @@
 //                  GE[slot][12][nE]           its stale w reconstructions at the edges
 //   maxima         MX[slot][11][nY][nX]       Hnmax, umax, emax, dmax, psimax (value, time)
 //                                             and tfirst (src/Grid.f90:95-102)
+// FP32 form only (static per topography set, rebuilt when the set changes):
+//   cell factors   TD[slot][3][nY][nX]        b0+bt, 1/gam^2, 1/gam            (FP64)
+//                  TF[slot][6][nY][nX]        gam, dbdx, dbdy, gXp1, gXp2, gYp2 (FP32)
+//   face factors   TFX[slot][2][nY][nX+1]     gam, (1+dbdy^2)/gam^3            (FP32)
+//                  TFY[slot][2][nY+1][nX]     gam, (1+dbdx^2)/gam^3            (FP32)
 #pragma once
 #include "kg_physics.cuh"
 
@@ -56,6 +61,10 @@ struct DevArrays {
     double* MX;
     double* MS;                // [slot][5][nY][nX] M-operator stage state: w, Hnpsi, Hn, psi, rho
     double* EMD;               // [slot][nY][nX] E - D of the current M stage (zero on ghosts)
+    double* TD[2];             // FP32 form topography factors (null in the FP64 form)
+    float* TF[2];
+    float* TFX[2];
+    float* TFY[2];
     int* nbr;                  // [cap][8] neighbour slots (-1: none)
     int8_t* kind;              // SlotKind per slot
     int8_t* has_source;        // containsSource per slot

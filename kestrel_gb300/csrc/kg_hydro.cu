@@ -104,6 +104,42 @@ __device__ __forceinline__ void desing(const DevParams& P, double w, double m1, 
     v = 2.0 * Hn * m2 / (Hn * Hn + mx(Hn * Hn, e2)) / rho;
 }
 
+// Flux-source rates of ExplicitSourceTerms (src/Equations.f90:500-590) at cell centre
+// (x, y): s1 = sum of Q / (NumCellsInSrc dx dy), s3 = the same for psi Q.
+__device__ __forceinline__ void flux_source_rates(const DevParams& P, double t, double tg, double x, double y, double& s1,
+                                                  double& s3) {
+    for (int J = 0; J < P.nSources; ++J) {
+        const DevSource& S = cSrc[J];
+        double Qf = 0.0, psiQf = 0.0;
+        if (((x - S.x) * (x - S.x) + (y - S.y) * (y - S.y)) < S.R * S.R) {
+            int n = S.n;
+            if (n == 1) {
+                if (!(t < S.time[0] || (t == S.time[0] && tg < t))) {
+                    Qf = S.flux[0];
+                    psiQf = S.psi[0] * Qf;
+                }
+            } else {
+                if (!(t < S.time[0] || t > S.time[n - 1] || (t == S.time[0] && tg < t) || (t == S.time[n - 1] && tg == t))) {
+                    for (int K = 1; K < n; ++K) {
+                        if ((t >= S.time[K - 1]) && (t <= S.time[K])) {
+                            double Qa = S.flux[K - 1], psia = S.psi[K - 1], ta = S.time[K - 1];
+                            double Qb = S.flux[K], psib = S.psi[K], tb = S.time[K];
+                            Qf = Qa + (Qb - Qa) * (t - ta) / (tb - ta);
+                            double psif = psia + (psib - psia) * (t - ta) / (tb - ta);
+                            psiQf = psif * Qf;
+                        }
+                    }
+                }
+            }
+        }
+        double ncs = (double)S.ncells;
+        Qf = Qf / ncs / P.dx / P.dy;
+        psiQf = psiQf / ncs / P.dx / P.dy;
+        s1 = s1 + Qf;
+        s3 = s3 + psiQf;
+    }
+}
+
 // Flux-source and gravity terms of ExplicitSourceTerms (src/Equations.f90:456-620).
 __device__ __forceinline__ void explicit_sources(const DevParams& P, bool has_src, double t, double tg, double x, double y,
                                                  double w, double b0, double bt, double rho, double dbdx, double dbdy,
@@ -111,36 +147,7 @@ __device__ __forceinline__ void explicit_sources(const DevParams& P, bool has_sr
     double Qt = 0.0, psiQt = 0.0;
     if (has_src && P.nSources >= 1) {
         double s1 = 0.0, s3 = 0.0;
-        for (int J = 0; J < P.nSources; ++J) {
-            const DevSource& S = cSrc[J];
-            double Qf = 0.0, psiQf = 0.0;
-            if (((x - S.x) * (x - S.x) + (y - S.y) * (y - S.y)) < S.R * S.R) {
-                int n = S.n;
-                if (n == 1) {
-                    if (!(t < S.time[0] || (t == S.time[0] && tg < t))) {
-                        Qf = S.flux[0];
-                        psiQf = S.psi[0] * Qf;
-                    }
-                } else {
-                    if (!(t < S.time[0] || t > S.time[n - 1] || (t == S.time[0] && tg < t) || (t == S.time[n - 1] && tg == t))) {
-                        for (int K = 1; K < n; ++K) {
-                            if ((t >= S.time[K - 1]) && (t <= S.time[K])) {
-                                double Qa = S.flux[K - 1], psia = S.psi[K - 1], ta = S.time[K - 1];
-                                double Qb = S.flux[K], psib = S.psi[K], tb = S.time[K];
-                                Qf = Qa + (Qb - Qa) * (t - ta) / (tb - ta);
-                                double psif = psia + (psib - psia) * (t - ta) / (tb - ta);
-                                psiQf = psif * Qf;
-                            }
-                        }
-                    }
-                }
-            }
-            double ncs = (double)S.ncells;
-            Qf = Qf / ncs / P.dx / P.dy;
-            psiQf = psiQf / ncs / P.dx / P.dy;
-            s1 = s1 + Qf;
-            s3 = s3 + psiQf;
-        }
+        flux_source_rates(P, t, tg, x, y, s1, s3);
         Qt = Qt + s1;
         psiQt = psiQt + s3;
     }

@@ -1,0 +1,521 @@
+// kg_hydro32.cu -- the FP32 form of the fused hydraulic operator.
+//
+// Same passes, block decomposition, tile-seam rules and stage formulas as k_hydro (the
+// FP64 drop-in), with the arithmetic split by what needs FP64:
+//   FP64  the free surface w and everything that subtracts a bed from it (cell depth
+//         w - (b0+bt), the face offsets w - InterpolateB), the w and Hnpsi rows of the RHS
+//         (flux differences of FP32 fluxes taken in FP64, so the sums over cells still
+//         telescope and mass and solids are conserved to FP64 round-off), the w / Hnpsi
+//         stage updates, the flux-source rates and the CFL minimum across CTAs;
+//   FP32  reconstruction slopes, desingularised variables, wave speeds, the central-upwind
+//         fluxes, hydrostatic and diffusive fluxes, momentum RHS rows, drag closures and
+//         the momentum stage updates.
+// Static geometric factors (gam, 1/gam, 1/gam^2, the hydrostatic prefactors, the face gam
+// and wave-speed factor) come from the per-topography-set cache built by k_topo32, so a
+// pass takes no FP64 divide or square root.  At rest (w flat, zero momenta) every face
+// offset on both sides of a face is the same FP64 difference, so the state stays at rest.
+#include <cuda_runtime.h>
+#include "kg_engine.cuh"
+
+namespace kg {
+
+struct __align__(16) Hydro32Smem {
+    double w[NR];                // free surface
+    double p64[NR];              // Hnpsi as the stage update reads it
+    float m1[NR], m2[NR], p[NR];
+    float hp[NR], gam[NR], Hn[NR], rho[NR], u[NR], v[NR], psi[NR];
+    float dlo[2][NLX], dhi[2][NLX];  // w - InterpolateB at the cell's lower / upper face (x, y)
+    float lx[5][NLX], ly[5][NLX];
+    float fx[7][NFX], fy[7][NFX];
+    float red[NT / 32];
+};
+
+// Desingularised variables (src/HydraulicRHS.f90:762-878) in FP32 from the FP32 depth.
+__device__ __forceinline__ void desing32(const DevParams& P, float hp, float gam, float m1, float m2, float pp, float& Hn,
+                                         float& psi, float& rho, float& u, float& v) {
+    Hn = hp * gam;
+    if (Hn < 0.f) Hn = 0.f;
+    float Hnpsi = pp < 0.f ? 0.f : pp;
+    float e2 = (float)(P.hThr * P.hThr);
+    float den = Hn * Hn + fmaxf(Hn * Hn, e2);
+    float r2 = 2.f * Hn / den;
+    psi = fminf(r2 * Hnpsi, (float)P.maxPack);
+    rho = density<float>(P, psi);
+    float k = r2 / rho;
+    u = k * m1;
+    v = k * m2;
+}
+
+struct Side32 {
+    float hp, p, u, v, rho, du, dv;  // hp: face free surface minus InterpolateB at the face
+};
+
+// Central-upwind fluxes at one face in FP32 (CalculateFluxes, src/HydraulicRHS.f90:949-1064).
+// gamf and kf = (1 + b_t^2)/gamf^3 are the face's cached factors.
+__device__ __forceinline__ void face_flux32(const DevParams& P, bool xdir, const Side32& Pl, const Side32& Mi, float gamf,
+                                            float kf, float gamL, float gamR, float h, float out[7], float& cfl) {
+    const float g = (float)P.g;
+    float HnP = Pl.hp * gamf, HnM = Mi.hp * gamf;
+    float unP = xdir ? Pl.u : Pl.v, unM = xdir ? Mi.u : Mi.v;
+    float hP = HnP <= 0.f ? 0.f : HnP, hM = HnM <= 0.f ? 0.f : HnM;
+    float cP = sqrtf(g * hP * kf), cM = sqrtf(g * hM * kf);
+    float aPos = fmaxf(fmaxf(unP + cP, unM + cM), 0.f);
+    float aNeg = fminf(fminf(unP - cP, unM - cM), 0.f);
+    if (aPos > 0.f) {
+        float gr = fminf(gamL / gamf, 1.f);
+        cfl = fminf(gr * gr * h / aPos, cfl);
+    }
+    if (aNeg < 0.f) {
+        float gr = fminf(gamR / gamf, 1.f);
+        cfl = fminf(gr * gr * h / -aNeg, cfl);
+    }
+    float dif = aPos - aNeg;
+    if (dif < 1e-10f) {
+#pragma unroll
+        for (int k = 0; k < 7; ++k) out[k] = 0.f;
+        return;
+    }
+    float rdif = 1.f / dif;
+    float ap = aPos * rdif, an = aNeg * rdif, apn = aPos * aNeg * rdif;
+    float m1P = Pl.rho * HnP * Pl.u, m1M = Mi.rho * HnM * Mi.u;
+    float m2P = Pl.rho * HnP * Pl.v, m2M = Mi.rho * HnM * Mi.v;
+    out[0] = (HnP - HnM) * gamf * apn + gamf * (ap * HnM * unM - an * HnP * unP);
+    out[3] = (Pl.p - Mi.p) * gamf * apn + gamf * (ap * Mi.p * unM - an * Pl.p * unP);
+    out[1] = (m1P - m1M) * apn + (ap * m1M * unM - an * m1P * unP);
+    out[2] = (m2P - m2M) * apn + (ap * m2M * unM - an * m2P * unP);
+    float GP = 0.5f * g * Pl.rho * Pl.hp * Pl.hp, GM = 0.5f * g * Mi.rho * Mi.hp * Mi.hp;
+    out[4] = ap * GM - an * GP;
+    const float nu = (float)P.nu;
+    float dP1 = 0.f, dP2 = 0.f, dM1 = 0.f, dM2 = 0.f;
+    if (!(HnP < 0.f)) {
+        dP1 = nu * Pl.rho * HnP * Pl.du;
+        dP2 = nu * Pl.rho * HnP * Pl.dv;
+    }
+    if (!(HnM < 0.f)) {
+        dM1 = nu * Mi.rho * HnM * Mi.du;
+        dM2 = nu * Mi.rho * HnM * Mi.dv;
+    }
+    out[5] = 0.5f * (dP1 + dM1);
+    out[6] = 0.5f * (dP2 + dM2);
+}
+
+// Well-balancing and positivity corrections of one reconstructed face side
+// (CorrectSlopes, src/HydraulicRHS.f90:560-735) in offset form: dlo/dhi are w_c minus the
+// interpolated bed at the cell's lower/upper face, s the half-cell slope step of w.  The
+// side value at the upper face is dhi + s; at the lower face dlo - s; a corrected cell
+// takes w_c + (bhi - blo)/2 at both, i.e. (dlo + dhi)/2 above either face's bed.
+__device__ __forceinline__ float side_hp(float dlo, float dhi, float s, bool upper, bool corr) {
+    if (corr) return 0.5f * (dlo + dhi);
+    return upper ? dhi + s : dlo - s;
+}
+
+__global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __restrict__ blocks, StepArgs S) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
+    const DevParams& P = cP;
+    const BlockDesc bd = blocks[blockIdx.x];
+    const int nX = P.nX, nY = P.nY, SC = nX * nY, SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
+    const int slot = bd.slot;
+    const int bx = min(BS, nX - bd.x0), by = min(BS, nY - bd.y0);
+    const int tid = threadIdx.x;
+    const int nbW = A.nbr[slot * 8 + NB_W], nbE = A.nbr[slot * 8 + NB_E];
+    const int nbN = A.nbr[slot * 8 + NB_N], nbS = A.nbr[slot * 8 + NB_S];
+    const double* __restrict__ Qin = (S.mode == MODE_RHS0 || S.mode == MODE_S1) ? A.Q[S.q_in]
+                                   : (S.mode == MODE_S2)                        ? A.Q[S.q_s1]
+                                                                                : A.Q[S.q_s2];
+    const double* __restrict__ TD = A.TD[S.topo];
+    const float* __restrict__ TF = A.TF[S.topo];
+    const double* __restrict__ FX = A.FX[S.topo];
+    const double* __restrict__ FY = A.FY[S.topo];
+    const float dtf = (float)S.dt;
+
+    // ---- A: load the cross-shaped region, FP64 depth, FP32 desingularisation ----
+    for (int r = tid; r < NR; r += NT) {
+        int cx = r % RG - 2, cy = r / RG - 2;
+        bool inX = (cy >= 0 && cy < by && cx >= -2 && cx < bx + 2);
+        bool inY = (cx >= 0 && cx < bx && cy >= -2 && cy < by + 2);
+        if (!inX && !inY) continue;
+        int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
+        if (i < 0) { s = nbW; i += nX; }
+        else if (i >= nX) { s = nbE; i -= nX; }
+        else if (j < 0) { s = nbS; j += nY; }
+        else if (j >= nY) { s = nbN; j -= nY; }
+        int c = j * nX + i;
+        float gam = TF[plane(s, 6, 0, SC) + c];
+        sm.gam[r] = gam;
+        if (A.kind[s] == SLOT_GHOST) {
+            double w = A.G9[plane(s, 9, 0, SC) + c], pp = A.G9[plane(s, 9, 3, SC) + c];
+            sm.w[r] = w;
+            sm.p64[r] = pp;
+            sm.m1[r] = (float)A.G9[plane(s, 9, 1, SC) + c];
+            sm.m2[r] = (float)A.G9[plane(s, 9, 2, SC) + c];
+            sm.p[r] = (float)pp;
+            sm.hp[r] = (float)(w - TD[plane(s, 3, 0, SC) + c]);
+            sm.Hn[r] = (float)A.G9[plane(s, 9, 4, SC) + c];
+            sm.u[r] = (float)A.G9[plane(s, 9, 5, SC) + c];
+            sm.v[r] = (float)A.G9[plane(s, 9, 6, SC) + c];
+            sm.psi[r] = (float)A.G9[plane(s, 9, 7, SC) + c];
+            sm.rho[r] = (float)A.G9[plane(s, 9, 8, SC) + c];
+            continue;
+        }
+        double w, pp;
+        float m1, m2;
+        size_t q = plane(s, 4, 0, SC) + c;
+        if (S.mode == MODE_S1) {
+            // stage 1 on the fly (src/TimeStepper.f90:371-404): w, Hnpsi in FP64
+            const double* E = A.E[S.e_set];
+            float I = (float)A.I[S.e_set][plane(s, 1, 0, SC) + c];
+            w = Qin[q] + S.dt * E[q];
+            pp = Qin[q + 3 * (size_t)SC] + S.dt * E[q + 3 * (size_t)SC];
+            float den = 1.f / (1.f - dtf * I);
+            m1 = ((float)Qin[q + SC] + dtf * (float)E[q + SC]) * den;
+            m2 = ((float)Qin[q + 2 * (size_t)SC] + dtf * (float)E[q + 2 * (size_t)SC]) * den;
+        } else {
+            w = Qin[q];
+            m1 = (float)Qin[q + SC];
+            m2 = (float)Qin[q + 2 * (size_t)SC];
+            pp = Qin[q + 3 * (size_t)SC];
+        }
+        float hp = (float)(w - TD[plane(s, 3, 0, SC) + c]);
+        sm.w[r] = w; sm.p64[r] = pp; sm.m1[r] = m1; sm.m2[r] = m2; sm.p[r] = (float)pp; sm.hp[r] = hp;
+        float Hn, psi, rho, u, v;
+        desing32(P, hp, gam, m1, m2, (float)pp, Hn, psi, rho, u, v);
+        sm.Hn[r] = Hn; sm.psi[r] = psi; sm.rho[r] = rho; sm.u[r] = u; sm.v[r] = v;
+    }
+    __syncthreads();
+
+    // ---- B: limited slopes and face offsets ----
+    const int lim = P.limiter;
+    const float dxR = (float)P.dxR, dyR = (float)P.dyR;
+    for (int k = tid; k < (bx + 2) * by; k += NT) {
+        int cx = k % (bx + 2) - 1, cy = k / (bx + 2);
+        int r = (cy + 2) * RG + (cx + 2);
+        int li = cy * (BS + 2) + (cx + 1);
+        bool ghW = (cx < 0 && bd.x0 == 0 && A.kind[nbW] == SLOT_GHOST);
+        bool ghE = (cx >= bx && bd.x0 + bx == nX && A.kind[nbE] == SLOT_GHOST);
+        if (ghW || ghE) {
+            int gs = ghW ? nbW : nbE;
+            sm.lx[0][li] = (float)A.GE[plane(gs, GE_COUNT, ghW ? GE_LXN : GE_LX1, A.nE) + bd.y0 + cy];
+            sm.lx[1][li] = 0.f; sm.lx[2][li] = 0.f; sm.lx[3][li] = 0.f; sm.lx[4][li] = 0.f;
+        } else {
+            sm.lx[0][li] = dxR * limiter<float>(lim, (float)(sm.w[r + 1] - sm.w[r]), (float)(sm.w[r] - sm.w[r - 1]));
+            sm.lx[1][li] = dxR * limiter<float>(lim, sm.p[r + 1] - sm.p[r], sm.p[r] - sm.p[r - 1]);
+            sm.lx[2][li] = dxR * limiter<float>(lim, sm.u[r + 1] - sm.u[r], sm.u[r] - sm.u[r - 1]);
+            sm.lx[3][li] = dxR * limiter<float>(lim, sm.v[r + 1] - sm.v[r], sm.v[r] - sm.v[r - 1]);
+            sm.lx[4][li] = dxR * limiter<float>(lim, sm.rho[r + 1] - sm.rho[r], sm.rho[r] - sm.rho[r - 1]);
+        }
+        int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
+        if (i < 0) { s = nbW; i += nX; }
+        else if (i >= nX) { s = nbE; i -= nX; }
+        const double* bI = FX + plane(s, 5, 4, SFX) + (size_t)j * (nX + 1) + i;
+        sm.dlo[0][li] = (float)(sm.w[r] - bI[0]);
+        sm.dhi[0][li] = (float)(sm.w[r] - bI[1]);
+    }
+    for (int k = tid; k < (by + 2) * bx; k += NT) {
+        int cx = k % bx, cy = k / bx - 1;
+        int r = (cy + 2) * RG + (cx + 2);
+        int li = (cy + 1) * BS + cx;
+        bool ghS = (cy < 0 && bd.y0 == 0 && A.kind[nbS] == SLOT_GHOST);
+        bool ghN = (cy >= by && bd.y0 + by == nY && A.kind[nbN] == SLOT_GHOST);
+        if (ghS || ghN) {
+            int gs = ghS ? nbS : nbN;
+            sm.ly[0][li] = (float)A.GE[plane(gs, GE_COUNT, ghS ? GE_LYN : GE_LY1, A.nE) + bd.x0 + cx];
+            sm.ly[1][li] = 0.f; sm.ly[2][li] = 0.f; sm.ly[3][li] = 0.f; sm.ly[4][li] = 0.f;
+        } else {
+            sm.ly[0][li] = dyR * limiter<float>(lim, (float)(sm.w[r + RG] - sm.w[r]), (float)(sm.w[r] - sm.w[r - RG]));
+            sm.ly[1][li] = dyR * limiter<float>(lim, sm.p[r + RG] - sm.p[r], sm.p[r] - sm.p[r - RG]);
+            sm.ly[2][li] = dyR * limiter<float>(lim, sm.u[r + RG] - sm.u[r], sm.u[r] - sm.u[r - RG]);
+            sm.ly[3][li] = dyR * limiter<float>(lim, sm.v[r + RG] - sm.v[r], sm.v[r] - sm.v[r - RG]);
+            sm.ly[4][li] = dyR * limiter<float>(lim, sm.rho[r + RG] - sm.rho[r], sm.rho[r] - sm.rho[r - RG]);
+        }
+        int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
+        if (j < 0) { s = nbS; j += nY; }
+        else if (j >= nY) { s = nbN; j -= nY; }
+        const double* bI = FY + plane(s, 5, 4, SFY) + (size_t)j * nX + i;
+        sm.dlo[1][li] = (float)(sm.w[r] - bI[0]);
+        sm.dhi[1][li] = (float)(sm.w[r] - bI[nX]);
+    }
+    __syncthreads();
+
+    // ---- C: face states, corrections, fluxes, CFL ----
+    float cfl = 3.402823466e38f;
+    const float hdx = 0.5f * (float)P.dx, hdy = 0.5f * (float)P.dy;
+    const float* __restrict__ TFXs = A.TFX[S.topo] + (size_t)slot * 2 * SFX;
+    const float* __restrict__ TFYs = A.TFY[S.topo] + (size_t)slot * 2 * SFY;
+    for (int k = tid; k < (bx + 1) * by; k += NT) {
+        int fx = k % (bx + 1), cy = k / (bx + 1);
+        int fi = bd.x0 + fx, j = bd.y0 + cy;
+        int rL = (cy + 2) * RG + (fx + 1), rR = rL + 1;
+        int liL = cy * (BS + 2) + fx, liR = liL + 1;
+        Side32 L, R;
+        // Left state: the upper-face reconstruction of cell fx-1.
+        float s = sm.lx[0][liL] * hdx, sp = sm.lx[1][liL] * hdx;
+        bool corr;
+        if (fi == 0 && A.kind[nbW] == SLOT_GHOST) {
+            const double* fxs = FX + plane(nbW, 5, 4, SFX);
+            double bl = fxs[j * (nX + 1) + nX - 1], br = fxs[j * (nX + 1) + nX];
+            const double* ge = A.GE + plane(nbW, GE_COUNT, 0, A.nE);
+            corr = ge[GE_MXN1 * A.nE + j] < br || ge[GE_PXN * A.nE + j] < bl;
+        } else {
+            corr = (sm.dhi[0][liL] + s < 0.f) || (sm.dlo[0][liL] - s < 0.f);
+        }
+        L.hp = side_hp(sm.dlo[0][liL], sm.dhi[0][liL], s, true, corr);
+        L.p = sm.p[rL] + sp;
+        if (L.p < 0.f || (fi != 0 && sm.p[rL] - sp < 0.f)) L.p = sm.p[rL];
+        L.u = sm.u[rL] + sm.lx[2][liL] * hdx;
+        L.v = sm.v[rL] + sm.lx[3][liL] * hdx;
+        L.rho = sm.rho[rL] + sm.lx[4][liL] * hdx;
+        L.du = sm.lx[2][liL];
+        L.dv = sm.lx[3][liL];
+        // Right state: the lower-face reconstruction of cell fx.
+        s = sm.lx[0][liR] * hdx;
+        sp = sm.lx[1][liR] * hdx;
+        if (fi == nX && A.kind[nbE] == SLOT_GHOST) {
+            const double* fxs = FX + plane(nbE, 5, 4, SFX);
+            double bl = fxs[j * (nX + 1) + 0], br = fxs[j * (nX + 1) + 1];
+            const double* ge = A.GE + plane(nbE, GE_COUNT, 0, A.nE);
+            corr = ge[GE_MX2 * A.nE + j] < br || ge[GE_PX1 * A.nE + j] < bl;
+        } else {
+            corr = (sm.dhi[0][liR] + s < 0.f) || (sm.dlo[0][liR] - s < 0.f);
+        }
+        R.hp = side_hp(sm.dlo[0][liR], sm.dhi[0][liR], s, false, corr);
+        R.p = sm.p[rR] - sp;
+        if (R.p < 0.f || (fi != nX && sm.p[rR] + sp < 0.f)) R.p = sm.p[rR];
+        R.u = sm.u[rR] - sm.lx[2][liR] * hdx;
+        R.v = sm.v[rR] - sm.lx[3][liR] * hdx;
+        R.rho = sm.rho[rR] - sm.lx[4][liR] * hdx;
+        R.du = sm.lx[2][liR];
+        R.dv = sm.lx[3][liR];
+        int fo = j * (nX + 1) + fi;
+        float out[7];
+        face_flux32(P, true, R, L, TFXs[fo], TFXs[fo + SFX], sm.gam[rL], sm.gam[rR], (float)P.dx, out, cfl);
+        int fo2 = cy * (BS + 1) + fx;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) sm.fx[q][fo2] = out[q];
+    }
+    for (int k = tid; k < (by + 1) * bx; k += NT) {
+        int cx = k % bx, fy = k / bx;
+        int fj = bd.y0 + fy, i = bd.x0 + cx;
+        int rL = (fy + 1) * RG + (cx + 2), rR = rL + RG;
+        int liL = fy * BS + cx, liR = liL + BS;
+        Side32 L, R;
+        float s = sm.ly[0][liL] * hdy, sp = sm.ly[1][liL] * hdy;
+        bool corr;
+        if (fj == 0 && A.kind[nbS] == SLOT_GHOST) {
+            const double* fys = FY + plane(nbS, 5, 4, SFY);
+            double bb = fys[(nY - 1) * nX + i], bt_ = fys[nY * nX + i];
+            const double* ge = A.GE + plane(nbS, GE_COUNT, 0, A.nE);
+            corr = ge[GE_MYN1 * A.nE + i] < bt_ || ge[GE_PYN * A.nE + i] < bb;
+        } else {
+            corr = (sm.dhi[1][liL] + s < 0.f) || (sm.dlo[1][liL] - s < 0.f);
+        }
+        L.hp = side_hp(sm.dlo[1][liL], sm.dhi[1][liL], s, true, corr);
+        L.p = sm.p[rL] + sp;
+        if (L.p < 0.f || (fj != 0 && sm.p[rL] - sp < 0.f)) L.p = sm.p[rL];
+        L.u = sm.u[rL] + sm.ly[2][liL] * hdy;
+        L.v = sm.v[rL] + sm.ly[3][liL] * hdy;
+        L.rho = sm.rho[rL] + sm.ly[4][liL] * hdy;
+        L.du = sm.ly[2][liL];
+        L.dv = sm.ly[3][liL];
+        s = sm.ly[0][liR] * hdy;
+        sp = sm.ly[1][liR] * hdy;
+        if (fj == nY && A.kind[nbN] == SLOT_GHOST) {
+            const double* fys = FY + plane(nbN, 5, 4, SFY);
+            double bb = fys[0 * nX + i], bt_ = fys[1 * nX + i];
+            const double* ge = A.GE + plane(nbN, GE_COUNT, 0, A.nE);
+            corr = ge[GE_MY2 * A.nE + i] < bt_ || ge[GE_PY1 * A.nE + i] < bb;
+        } else {
+            corr = (sm.dhi[1][liR] + s < 0.f) || (sm.dlo[1][liR] - s < 0.f);
+        }
+        R.hp = side_hp(sm.dlo[1][liR], sm.dhi[1][liR], s, false, corr);
+        R.p = sm.p[rR] - sp;
+        if (R.p < 0.f || (fj != nY && sm.p[rR] + sp < 0.f)) R.p = sm.p[rR];
+        R.u = sm.u[rR] - sm.ly[2][liR] * hdy;
+        R.v = sm.v[rR] - sm.ly[3][liR] * hdy;
+        R.rho = sm.rho[rR] - sm.ly[4][liR] * hdy;
+        R.du = sm.ly[2][liR];
+        R.dv = sm.ly[3][liR];
+        int fo = fj * nX + i;
+        float out[7];
+        face_flux32(P, false, R, L, TFYs[fo], TFYs[fo + SFY], sm.gam[rL], sm.gam[rR], (float)P.dy, out, cfl);
+        int fo2 = fy * BS + cx;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) sm.fy[q][fo2] = out[q];
+    }
+    // CFL: warp then block min in FP32, the cross-CTA minimum on FP64 bits.
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cfl = fminf(cfl, __shfl_xor_sync(0xffffffffu, cfl, o));
+    if ((tid & 31) == 0) sm.red[tid >> 5] = cfl;
+    __syncthreads();
+    if (tid == 0) {
+        float m = sm.red[0];
+        for (int q = 1; q < NT / 32; ++q) m = fminf(m, sm.red[q]);
+        double md = m >= 3.402823466e38f ? 1.7976931348623157e308 : (double)m;
+        atomicMin(S.cfl_min, (unsigned long long)__double_as_longlong(md));
+    }
+
+    // ---- D: RHS assembly and stage update for the block's own cells ----
+    if (tid < bx * by) {
+        int cx = tid % bx, cy = tid / bx;
+        int i = bd.x0 + cx, j = bd.y0 + cy, c = j * nX + i;
+        int r = (cy + 2) * RG + (cx + 2);
+        const double* td = TD + plane(slot, 3, 0, SC) + c;
+        const float* tf = TF + plane(slot, 6, 0, SC) + c;
+        double ig2 = td[SC], ig = td[2 * (size_t)SC];
+        float gam = tf[0], dbdx = tf[SC], dbdy = tf[2 * (size_t)SC];
+        float gXp1 = tf[3 * (size_t)SC], gXp2 = tf[4 * (size_t)SC], gYp2 = tf[5 * (size_t)SC], gYp1 = gXp2;
+        int xl = cy * (BS + 1) + cx, xr = xl + 1;
+        int yb = cy * BS + cx, yt = yb + BS;
+        // w and Hnpsi rows in FP64 (the flux differences of FP32 values are exact or nearly so)
+        double E[4];
+        E[0] = (((double)sm.fx[0][xl] - (double)sm.fx[0][xr]) * P.dxR + ((double)sm.fy[0][yb] - (double)sm.fy[0][yt]) * P.dyR) * ig2;
+        E[3] = (((double)sm.fx[3][xl] - (double)sm.fx[3][xr]) * P.dxR + ((double)sm.fy[3][yb] - (double)sm.fy[3][yt]) * P.dyR) * ig;
+        float E1 = kahan3<float>(sm.fx[1][xl] - sm.fx[1][xr], (sm.fx[4][xl] - sm.fx[4][xr]) * gXp1, sm.fx[5][xr] - sm.fx[5][xl]) * dxR +
+                   kahan3<float>(sm.fy[1][yb] - sm.fy[1][yt], (sm.fy[4][yb] - sm.fy[4][yt]) * gYp1, sm.fy[5][yt] - sm.fy[5][yb]) * dyR;
+        float E2 = kahan3<float>(sm.fx[2][xl] - sm.fx[2][xr], (sm.fx[4][xl] - sm.fx[4][xr]) * gXp2, sm.fx[6][xr] - sm.fx[6][xl]) * dxR +
+                   kahan3<float>(sm.fy[2][yb] - sm.fy[2][yt], (sm.fy[4][yb] - sm.fy[4][yt]) * gYp2, sm.fy[6][yt] - sm.fy[6][yb]) * dyR;
+        // Sources (ExplicitSourceTerms, src/Equations.f90:456-620): flux sources in FP64,
+        // gravity in FP32 from the FP64 depth.
+        if (A.has_source[slot] != 0 && P.nSources >= 1) {
+            int gi = (bd.tile - 1) % P.nXtiles + 1, gj = (bd.tile - 1) / P.nXtiles + 1;
+            double x = -0.5 * P.xSize + P.dx * ((gi - 1.0) * P.nX + ((i + 1) - 0.5));
+            double y = -0.5 * P.ySize + P.dy * ((gj - 1.0) * P.nY + ((j + 1) - 0.5));
+            double s1 = 0.0, s3 = 0.0;
+            flux_source_rates(P, S.t_rhs, S.t_grid, x, y, s1, s3);
+            E[0] = E[0] + s1 * ig2;
+            E[3] = E[3] + s3 * ig;
+        }
+        float grho = (float)P.g * sm.rho[r] * sm.hp[r] / gam;
+        E1 = E1 - grho * dbdx;
+        E2 = E2 - grho * dbdy;
+        E[1] = E1;
+        E[2] = E2;
+        Pt<float> pt{sm.Hn[r], sm.u[r], sm.v[r], sm.psi[r], sm.rho[r], 0.f, dbdx, dbdy, gam};
+        float I = implicit_source<float>(P, pt, drag<float>(P, pt));
+        if (S.mode == MODE_RHS0) {
+#pragma unroll
+            for (int f = 0; f < 4; ++f) A.E[S.e_set][plane(slot, 4, f, SC) + c] = E[f];
+            A.I[S.e_set][plane(slot, 1, 0, SC) + c] = I;
+        } else if (S.mode == MODE_S1 || S.mode == MODE_S2) {
+            const double* q0p = A.Q[S.q_in] + plane(slot, 4, 0, SC) + c;
+            double b = td[0];
+            double hp_old = q0p[0] - b, hp_new = sm.w[r] - b;
+            double* dst = A.Q[S.mode == MODE_S1 ? S.q_s1 : S.q_s2] + plane(slot, 4, 0, SC) + c;
+            float den = 1.f / (1.f - dtf * I);
+            double a0, a1;
+            if (S.mode == MODE_S1) { a0 = 0.75; a1 = 0.25; }
+            else { a0 = 1.0 / 3.0; a1 = 2.0 / 3.0; }
+            dst[0] = b + (a0 * hp_old + a1 * (hp_new + S.dt * E[0]));
+            dst[SC] = (double)((float)a0 * (float)q0p[SC] + (float)a1 * (sm.m1[r] + dtf * E1) * den);
+            dst[2 * (size_t)SC] = (double)((float)a0 * (float)q0p[2 * (size_t)SC] + (float)a1 * (sm.m2[r] + dtf * E2) * den);
+            dst[3 * (size_t)SC] = a0 * q0p[3 * (size_t)SC] + a1 * (sm.p64[r] + S.dt * E[3]);
+        } else {
+            float dt2I = dtf * dtf * I;
+            float den = 1.f / (1.f + dt2I * I);
+            double* dst = A.Q[S.q_out] + plane(slot, 4, 0, SC) + c;
+            dst[0] = sm.w[r];
+            dst[SC] = (double)((sm.m1[r] - dt2I * E1) * den);
+            dst[2 * (size_t)SC] = (double)((sm.m2[r] - dt2I * E2) * den);
+            dst[3 * (size_t)SC] = sm.p64[r];
+            A.UV[plane(slot, 2, 0, SC) + c] = (double)sm.u[r];
+            A.UV[plane(slot, 2, 1, SC) + c] = (double)sm.v[r];
+            if (S.do_maxima) {
+                // UpdateMaximum* on the state at the start of the step
+                // (src/TimeStepper.f90:519-524, :1155-1303).
+                const double* q0p = A.Q[S.q_tc] + plane(slot, 4, 0, SC) + c;
+                const double* ct0 = A.CT[S.topo_tc] + plane(slot, 4, 0, SC) + c;
+                double btt = ct0[SC];
+                float bxt = (float)ct0[2 * (size_t)SC], byt = (float)ct0[3 * (size_t)SC];
+                float gamt = gam_of<float>(P.geo, bxt, byt);
+                float hpt = (float)((q0p[0] - ct0[0]) - btt);
+                float Hn, psi, rho, u, v;
+                desing32(P, hpt, gamt, (float)q0p[SC], (float)q0p[2 * (size_t)SC], (float)q0p[3 * (size_t)SC], Hn, psi, rho, u, v);
+                double* M = A.MX + plane(slot, 11, 0, SC) + c;
+                double tt = S.t_max;
+                double Hnd = Hn, psid = psi;
+                if (Hnd > P.hThr) {
+                    if (M[10 * (size_t)SC] == -1.0) M[10 * (size_t)SC] = tt;
+                    if (Hnd > M[0]) { M[0] = Hnd; M[(size_t)SC] = tt; }
+                }
+                double spd = sqrtf(modu2_of<float>(P.geo, u, v, bxt, byt));
+                if ((spd > M[2 * (size_t)SC]) && (Hnd > P.hThr)) { M[2 * (size_t)SC] = spd; M[3 * (size_t)SC] = tt; }
+                if (btt < 0.0 && -btt > M[4 * (size_t)SC]) { M[4 * (size_t)SC] = -btt; M[5 * (size_t)SC] = tt; }
+                if (btt > 0.0 && btt > M[6 * (size_t)SC]) { M[6 * (size_t)SC] = btt; M[7 * (size_t)SC] = tt; }
+                if (Hnd > P.hThr && psid > M[8 * (size_t)SC]) { M[8 * (size_t)SC] = psid; M[9 * (size_t)SC] = tt; }
+            }
+        }
+    }
+}
+
+// Topography factors of the FP32 form for the listed slots of set ts, from the FP64 cell
+// and face topography (gam = sqrt(1 + b_x^2 + b_y^2), src/Closures.f90:174-186; the
+// hydrostatic prefactors of ConstructHydraulicRHS, src/HydraulicRHS.f90:1236-1250; the
+// wave-speed factor (1 + b_t^2)/gam^3 of src/Equations.f90:249-381).
+__global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restrict__ slots, int ts, int per) {
+    const DevParams& P = cP;
+    const int nX = P.nX, nY = P.nY, SC = nX * nY, SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
+    int s = slots[blockIdx.x / per];
+    int k = (blockIdx.x % per) * 256 + threadIdx.x;
+    if (k < SC) {
+        const double* ct = A.CT[ts] + plane(s, 4, 0, SC) + k;
+        double b0 = ct[0], bt = ct[SC], bx = ct[2 * (size_t)SC], by = ct[3 * (size_t)SC];
+        double gam = gam_of(P.geo, bx, by);
+        double* td = A.TD[ts] + plane(s, 3, 0, SC) + k;
+        td[0] = b0 + bt;
+        td[SC] = 1.0 / (gam * gam);
+        td[2 * (size_t)SC] = 1.0 / gam;
+        float* tf = A.TF[ts] + plane(s, 6, 0, SC) + k;
+        tf[0] = (float)gam;
+        tf[SC] = (float)bx;
+        tf[2 * (size_t)SC] = (float)by;
+        if (P.geo) {
+            tf[3 * (size_t)SC] = (float)((1.0 + by * by) / gam);
+            tf[4 * (size_t)SC] = (float)(-bx * by / gam);
+            tf[5 * (size_t)SC] = (float)((1.0 + bx * bx) / gam);
+        } else {
+            tf[3 * (size_t)SC] = 1.f;
+            tf[4 * (size_t)SC] = 0.f;
+            tf[5 * (size_t)SC] = 1.f;
+        }
+    }
+    if (k < SFX) {
+        const double* fx = A.FX[ts] + plane(s, 5, 0, SFX) + k;
+        double bx = fx[2 * (size_t)SFX], by = fx[3 * (size_t)SFX];
+        double g = gam_of(P.geo, bx, by);
+        float* o = A.TFX[ts] + plane(s, 2, 0, SFX) + k;
+        o[0] = (float)g;
+        o[SFX] = P.geo ? (float)((1.0 + by * by) / (g * g * g)) : 1.f;
+    }
+    if (k < SFY) {
+        const double* fy = A.FY[ts] + plane(s, 5, 0, SFY) + k;
+        double bx = fy[2 * (size_t)SFY], by = fy[3 * (size_t)SFY];
+        double g = gam_of(P.geo, bx, by);
+        float* o = A.TFY[ts] + plane(s, 2, 0, SFY) + k;
+        o[0] = (float)g;
+        o[SFY] = P.geo ? (float)((1.0 + bx * bx) / (g * g * g)) : 1.f;
+    }
+}
+
+size_t hydro32_smem_bytes() { return sizeof(Hydro32Smem); }
+
+cudaError_t launch_hydro32(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_hydro32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Hydro32Smem));
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    if (nblocks == 0) return cudaSuccess;
+    k_hydro32<<<nblocks, NT, sizeof(Hydro32Smem), st>>>(A, blocks, S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_topo32(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, cudaStream_t st) {
+    int items = (nX + 1) * (nY + 1);
+    int per = (items + 255) / 256;
+    if (n == 0) return cudaSuccess;
+    k_topo32<<<n * per, 256, 0, st>>>(A, d_slots, ts, per);
+    return cudaGetLastError();
+}
+
+}  // namespace kg

@@ -1,6 +1,7 @@
 // kg_lib.cu -- single translation unit of the device library (the kernels share the
 // __constant__ run settings, so they are compiled together rather than with -rdc).
 #include "kg_hydro.cu"
+#include "kg_hydro32.cu"
 #include "kg_tiles.cu"
 
 #include "kg_morpho.cu"

@@ -131,4 +131,15 @@ WORKLOADS = {
              "(mu=0.1, xi=500), mixed erosion with 2 m erodible depth, eddy viscosity 1e-2, to t=600 s; "
              "FP64 plain; timed after a spin-up to t=120 s",
         params=morpho_flux_2048, prec=abi.PREC_FP64, spinup=120.0),
+    "cap_release_256_fp32": dict(
+        desc="2D hydraulic cap release, 256x256 cells, dx=1 m, 5 deg slope, cap r=40 m h=4 m at (128,64), Chezy "
+             "0.01, no erosion, CFL 0.25, to t=30 s (16x16 tiles of 16x16 cells); FP32 form (FP64 free surface, "
+             "bed, mass/solids rows and dt)",
+        params=cap_release_256, prec=abi.PREC_FP32, b0=None, spinup=0.0),
+    "morpho_flux_2048_fp32": dict(
+        desc="2D morphodynamic flux release, 2048x2048 cells at dx=5 m on seeded fractal terrain (k^-3, relief "
+             "0-800 m, 8 deg tilt), inflow r=6 m with hydrograph 0-200-0 m^3/s over 300 s (conc 0.3), Voellmy "
+             "(mu=0.1, xi=500), mixed erosion with 2 m erodible depth, eddy viscosity 1e-2, to t=600 s; "
+             "FP32 form (FP64 free surface, bed, mass/solids rows and dt); timed after a spin-up to t=120 s",
+        params=morpho_flux_2048, prec=abi.PREC_FP32, spinup=120.0),
 }
