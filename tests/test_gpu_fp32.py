@@ -1,0 +1,109 @@
+"""The FP32 form (KG_PREC_FP32) against the FP64 oracle on the same inputs.
+
+The FP32 form keeps the free surface, the bed, the depth differences w - b, the w and
+Hnpsi RHS rows, their stage updates and the dt reduction in FP64, and computes the
+reconstruction, fluxes, closures and momentum rows in FP32.  Its stated error against
+the FP64 oracle, per field, relative L-inf over the active cells (w: relative to the
+largest depth, the scale its error lives on):
+
+  hydraulic runs (cap release 3 s, reference cap/flux inputs)   w, Hn <= 2e-5, momenta <= 5e-5
+  morphodynamic reference inputs (cap_morpho 1 s, flux_morpho 2 s)  w, Hn, momenta <= 5e-4,
+                                                                   Hnpsi <= 2e-3, bt <= 2e-2
+Conservation of volume and solids stays at FP64 round-off (<= 1e-12, the reference's own
+bar is 1e-10), depth stays >= 0, a lake at rest stays at rest to |u| <= 1e-5 m/s, and the
+active and ghost tile sets are identical to the oracle's.
+"""
+import numpy as np
+import pytest
+
+import _oracle
+import cases
+import test_oracle
+from kestrel_gb300 import abi, lib
+
+pytestmark = pytest.mark.gpu
+
+
+def fp32(p, **kw):
+    return lib.simulation(p, precision=abi.PREC_FP32, **kw)
+
+
+def field_errors(g, o):
+    tiles = o.active_tiles()
+    get = lambda s, f: np.concatenate([s.field(t, f).ravel() for t in tiles])
+    depth = np.max(np.abs(get(o, 5)))
+    errs = {}
+    for f, name in ((1, "w"), (2, "rhoHnu"), (3, "rhoHnv"), (4, "Hnpsi"), (5, "Hn"), (11, "bt")):
+        a, b = get(g, f), get(o, f)
+        den = depth if f == 1 else np.max(np.abs(b))
+        errs[name] = float(np.max(np.abs(a - b)) / den) if den > 0 else float(np.max(np.abs(a - b)))
+    return errs
+
+
+HYDRO = [
+    ("cap_release_256", 3.0),
+    ("cap_dilute_2d", 8.0),
+    ("cap_conc_2d", 2.0),
+    ("flux_hydro_2d", 3.0),
+    ("flux_edwards2019_2d", 3.0),
+]
+
+
+@pytest.mark.parametrize("name,tend", HYDRO)
+def test_fp32_hydraulic_error(name, tend):
+    p = cases.cap_release_256(tend=tend, nout=1) if name == "cap_release_256" else cases.ref_input(name, tend=tend, nout=1)
+    g, o = fp32(p), _oracle.simulation(p)
+    sg, so = g.run(), o.run()
+    assert g.active_tiles() == o.active_tiles() and g.ghost_tiles() == o.ghost_tiles()
+    assert sg.steps == so.steps
+    e = field_errors(g, o)
+    assert e["w"] <= 2e-5 and e["Hn"] <= 2e-5, e
+    assert e["rhoHnu"] <= 5e-5 and e["rhoHnv"] <= 5e-5, e
+    assert e["Hnpsi"] <= 2e-5, e
+    for t in g.active_tiles():
+        assert (g.field(t, 5) >= 0).all()
+
+
+@pytest.mark.parametrize("name,tend", [("cap_morpho_2d", 1.0), ("flux_morpho_2d", 2.0)])
+def test_fp32_morphodynamic_error(name, tend):
+    p = cases.ref_input(name, tend=tend, nout=1)
+    g, o = fp32(p), _oracle.simulation(p)
+    g.run()
+    o.run()
+    assert g.active_tiles() == o.active_tiles() and g.ghost_tiles() == o.ghost_tiles()
+    e = field_errors(g, o)
+    assert max(e["w"], e["Hn"], e["rhoHnu"], e["rhoHnv"]) <= 5e-4, e
+    assert e["Hnpsi"] <= 2e-3 and e["bt"] <= 2e-2, e
+    for t in g.active_tiles():
+        assert g.field(t, 11).min() >= -p.EroDepth
+
+
+@pytest.mark.parametrize("name,tend,nout", test_oracle.CONSERVATION)
+def test_fp32_conservation(name, tend, nout):
+    p = cases.ref_input(name, tend=tend, nout=nout)
+    sim, vol_err, sol_err = test_oracle.check_conservation(p, fp32)
+    assert vol_err <= 1e-12 and sol_err <= 1e-12, (vol_err, sol_err)
+    for t in sim.active_tiles():
+        assert (sim.field(t, 5) >= -1e-14).all()
+
+
+@pytest.mark.parametrize("name", ["lake_at_rest_hydro_2d", "lake_at_rest_morpho_2d"])
+def test_fp32_lake_at_rest(name):
+    p = cases.ref_input(name, tend=2.0, nout=2)
+    g = fp32(p)
+    h0 = {t: g.field(t, 5).copy() for t in g.active_tiles()}
+    g.run()
+    for t in g.active_tiles():
+        assert np.max(np.abs(g.field(t, 6))) <= 1e-5 and np.max(np.abs(g.field(t, 7))) <= 1e-5
+        assert np.max(np.abs(g.field(t, 5) - h0[t])) <= 1e-6 * max(np.max(np.abs(h0[t])), 1.0)
+
+
+def test_fp32_rejects_noalloc_entry_point():
+    """The allocation-free RHS entry point serves FP64 contexts only."""
+    import ctypes as C
+    L = lib.load()
+    L.kg_hydraulic_rhs_noalloc.argtypes = [C.c_void_p, C.c_double, C.c_int32, C.POINTER(C.c_double)]
+    L.kg_hydraulic_rhs_noalloc.restype = C.c_int
+    g = fp32(cases.ref_input("flux_hydro_2d", tend=1.0, nout=1))
+    dt = C.c_double()
+    assert abi.KG_ERR[L.kg_hydraulic_rhs_noalloc(g.h, 0.0, 1, C.byref(dt))] == "KG_ERR_UNSUPPORTED"
