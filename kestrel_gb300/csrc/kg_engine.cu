@@ -122,6 +122,12 @@ struct kg_ctx {
     int qcur = 0;                        // state buffer holding the solution (0..3)
     int tcur = 0;                        // topography set of the solution (0..1)
     bool tdirty[2] = {true, true};       // FP32 form: the set's factor cache needs a rebuild
+    // Edge-band flags of the active tiles computed right after the last accepted hydraulic
+    // step on its result (state buffer act_q, topography set act_t), so the next
+    // CheckIfNearBoundaries needs no wait of its own; act_gen guards against host writes.
+    std::vector<int> act_flags, act_tmp;
+    int act_q = -1, act_t = -1;
+    int64_t gen = 0, act_gen = -1;
     int* d_tlist = nullptr;              // slot list of the cache rebuild
     int d_tlist_cap = 0;
     std::vector<int> touched;            // slots whose step-start topography changed in set-up
@@ -139,7 +145,7 @@ struct kg_ctx {
     int64_t redist_cells = 0, redist_waves = 0, redist_walks = 0;
     bool blocks_dirty = true;
     bool timing = false;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0[4] = {nullptr, nullptr, nullptr, nullptr}, ev1[4] = {nullptr, nullptr, nullptr, nullptr};
     double kernel_ms = 0.0;
     int64_t timed_passes = 0;
     cudaStream_t st = nullptr;
@@ -613,12 +619,18 @@ void check_near_boundaries(kg_ctx& c) {
     if (c.active.empty()) return;
     std::vector<int> slots;
     for (int id : c.active) slots.push_back(T(c, id).slot);
-    upload_list(c, slots);
-    CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), c.qcur, c.tcur, c.src_override ? c.d_srcHn : nullptr, c.d_flags, c.st));
-    c.launches++;
-    std::vector<int> fl(slots.size());
-    CK(cudaMemcpyAsync(fl.data(), c.d_flags, fl.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
-    sync(c);
+    std::vector<int> fl;
+    if (!c.src_override && c.act_q == c.qcur && c.act_t == c.tcur && c.act_gen == c.gen && c.act_flags.size() == slots.size()) {
+        fl = c.act_flags;
+    } else {
+        upload_list(c, slots);
+        CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), c.qcur, c.tcur, c.src_override ? c.d_srcHn : nullptr, c.d_flags, c.st));
+        c.launches++;
+        fl.resize(slots.size());
+        CK(cudaMemcpyAsync(fl.data(), c.d_flags, fl.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        sync(c);
+    }
+    c.act_q = -1;
     std::vector<int> flag_of((size_t)c.nTiles + 1, -1);
     for (size_t q = 0; q < slots.size(); ++q) flag_of[(size_t)c.active[q]] = fl[q];
     int TB = c.p.TileBuffer;
@@ -669,26 +681,48 @@ void refresh_topo32(kg_ctx& c, int ts) {
     c.tdirty[ts] = false;
 }
 
-unsigned long long run_pass(kg_ctx& c, StepArgs S) {
-    *c.h_cfl = (unsigned long long)0x7FEFFFFFFFFFFFFFull;  // bits of huge(1.0_wp)
-    CK(cudaMemcpyAsync(c.d_cfl, c.h_cfl, sizeof(unsigned long long), cudaMemcpyHostToDevice, c.st));
-    S.cfl_min = c.d_cfl;
+constexpr unsigned long long HUGE_BITS = 0x7FEFFFFFFFFFFFFFull;  // bits of huge(1.0_wp)
+
+// Queue one fused pass that reduces its CFL terms into word `word` of the context's CFL
+// array; nothing waits for it.
+void launch_pass(kg_ctx& c, StepArgs& S, int word) {
+    S.cfl_min = c.d_cfl + word;
+    S.partial = (int)c.active.size() < c.nTiles ? 1 : 0;
     const bool fp32 = c.prec == KG_PREC_FP32;
     if (fp32 && c.tdirty[S.topo]) refresh_topo32(c, S.topo);
-    if (c.timing) CK(cudaEventRecord(c.ev0, c.st));
+    if (c.timing) CK(cudaEventRecord(c.ev0[word], c.st));
     if (fp32) CK(launch_hydro32(c.A, c.d_blocks, (int)c.blocks.size(), S, c.st));
     else CK(launch_hydro(c.A, c.d_blocks, (int)c.blocks.size(), S, c.st));
-    if (c.timing) CK(cudaEventRecord(c.ev1, c.st));
+    if (c.timing) CK(cudaEventRecord(c.ev1[word], c.st));
     c.launches++;
-    CK(cudaMemcpyAsync(c.h_cfl, c.d_cfl, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
+}
+void reset_cfl(kg_ctx& c, int n) {
+    for (int k = 0; k < n; ++k) c.h_cfl[k] = HUGE_BITS;
+    CK(cudaMemcpyAsync(c.d_cfl, c.h_cfl, (size_t)n * sizeof(unsigned long long), cudaMemcpyHostToDevice, c.st));
+}
+// Read back the first n CFL words (one wait for the whole queue).
+void collect_cfl(kg_ctx& c, int n) {
+    CK(cudaMemcpyAsync(c.h_cfl, c.d_cfl, (size_t)n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
     sync(c);
-    if (c.timing) {
+}
+// Accumulate the event timing of the first n passes of the last queue (those that ran).
+void account_passes(kg_ctx& c, int n) {
+    if (!c.timing) return;
+    for (int k = 0; k < n; ++k) {
         float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+        CK(cudaEventElapsedTime(&ms, c.ev0[k], c.ev1[k]));
         c.kernel_ms += ms;
         c.timed_passes++;
     }
-    return *c.h_cfl;
+}
+
+unsigned long long run_pass(kg_ctx& c, StepArgs S) {
+    reset_cfl(c, 1);
+    S.ngate = 0;
+    launch_pass(c, S, 0);
+    collect_cfl(c, 1);
+    account_passes(c, 1);
+    return c.h_cfl[0];
 }
 
 double next_flux_time(const kg_ctx& c, double t) {  // NextFluxSeriesTime, src/TimeStepper.f90:281-305
@@ -701,7 +735,10 @@ double next_flux_time(const kg_ctx& c, double t) {  // NextFluxSeriesTime, src/T
     return nextT;
 }
 
-// HydraulicTimeStepper on the device; returns true when dt had to be refined.
+// HydraulicTimeStepper on the device; returns true when dt had to be refined.  The three
+// stages are queued back to back: stage 2 runs only if stage 1's advised dt accepts dt and
+// stage 3 only if both do (the same test the host applies afterwards to the CFL words), so
+// one wait serves the whole step and a refined attempt leaves no output behind.
 bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int e_set, int topo, int q_s1, int q_s2, int q_out) {
     double nextT = c.t + dt;
     c.dt = dt;
@@ -709,14 +746,31 @@ bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int e_set, int topo, int
     S.q_in = q_in; S.q_s1 = q_s1; S.q_s2 = q_s2; S.q_out = q_out; S.e_set = e_set; S.topo = topo;
     S.q_tc = c.qcur; S.topo_tc = c.tcur;
     S.dt = dt; S.t_grid = c.t; S.do_maxima = 1;
-    S.mode = MODE_S1; S.t_rhs = nextT;
-    double dt1 = advised(c, run_pass(c, S), 2);
-    if (dt1 < dt) { dt = 0.9 * dt1; return true; }
-    S.mode = MODE_S2; S.t_rhs = c.t + 0.5 * dt;
-    double dt2 = advised(c, run_pass(c, S), 3);
-    if (dt2 < dt) { dt = 0.9 * dt2; return true; }
-    S.mode = MODE_S3; S.t_rhs = nextT; S.t_max = nextT;
-    run_pass(c, S);
+    reset_cfl(c, 3);
+    S.mode = MODE_S1; S.t_rhs = nextT; S.ngate = 0;
+    launch_pass(c, S, 0);
+    S.mode = MODE_S2; S.t_rhs = c.t + 0.5 * dt; S.gate[0] = c.d_cfl; S.ngate = 1;
+    launch_pass(c, S, 1);
+    S.mode = MODE_S3; S.t_rhs = nextT; S.t_max = nextT; S.gate[1] = c.d_cfl + 1; S.ngate = 2;
+    launch_pass(c, S, 2);
+    // Edge-band flags of the candidate result for the next step's CheckIfNearBoundaries.
+    std::vector<int> slots;
+    for (int id : c.active) slots.push_back(T(c, id).slot);
+    upload_list(c, slots);
+    CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), q_out, topo, nullptr, c.d_flags, c.st));
+    c.launches++;
+    c.act_tmp.resize(slots.size());
+    CK(cudaMemcpyAsync(c.act_tmp.data(), c.d_flags, slots.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    collect_cfl(c, 3);
+    double dt1 = advised(c, c.h_cfl[0], 2);
+    if (dt1 < dt) { account_passes(c, 1); dt = 0.9 * dt1; return true; }
+    double dt2 = advised(c, c.h_cfl[1], 3);
+    if (dt2 < dt) { account_passes(c, 2); dt = 0.9 * dt2; return true; }
+    account_passes(c, 3);
+    c.act_flags.swap(c.act_tmp);
+    c.act_q = q_out;
+    c.act_t = topo;
+    c.act_gen = c.gen;
     return false;
 }
 
@@ -1178,9 +1232,9 @@ void setup(kg_ctx& c, const kg_params& p) {
     c.t = 0.0;
     c.A.nE = c.nE;
     CK(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
-    CK(cudaMalloc(&c.d_cfl, sizeof(unsigned long long)));
+    CK(cudaMalloc(&c.d_cfl, 4 * sizeof(unsigned long long)));
     CK(cudaMalloc(&c.d_vol, 4 * sizeof(double)));
-    CK(cudaMallocHost(&c.h_cfl, sizeof(unsigned long long)));
+    CK(cudaMallocHost(&c.h_cfl, 4 * sizeof(unsigned long long)));
     CK(set_constants(c.dp, nullptr, 0, c.st));
     sync(c);
 }
@@ -1200,8 +1254,10 @@ void free_ctx(kg_ctx* c) {
                     c->d_rslot, c->d_rcell, c->d_rwave};
     for (void* q : ptrs) cudaFree(q);
     if (c->h_cfl) cudaFreeHost(c->h_cfl);
-    if (c->ev0) cudaEventDestroy(c->ev0);
-    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (int k = 0; k < 4; ++k) {
+        if (c->ev0[k]) cudaEventDestroy(c->ev0[k]);
+        if (c->ev1[k]) cudaEventDestroy(c->ev1[k]);
+    }
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
 }
@@ -1289,6 +1345,7 @@ int kg_load_sources(kg_ctx* c) {
     if (!c) return KG_ERR_PARAM;
     if (c->sources_loaded) { c->err = "sources already loaded"; return KG_ERR_STATE; }
     if (c->p.topog == KG_TOPO_UPLOAD && c->upload.empty()) { c->err = "no topography uploaded"; return KG_ERR_STATE; }
+    c->gen++;
     KG_GUARD(c, load_sources(*c));
     return KG_OK;
 }
@@ -1401,6 +1458,7 @@ int kg_set_tile_field(kg_ctx* c, int32_t id, int32_t field, const double* in) {
     int s = active_slot(c, id);
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (field < 1 || field > 4 || !in) return KG_ERR_PARAM;
+    c->gen++;
     KG_GUARD(c, {
         CK(cudaMemcpyAsync(c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * c->SC, in, (size_t)c->SC * sizeof(double),
                            cudaMemcpyHostToDevice, c->st));
@@ -1486,9 +1544,11 @@ void* kg_stream(kg_ctx* c) { return c ? (void*)c->st : nullptr; }
 int kg_set_kernel_timing(kg_ctx* c, int32_t enable) {
     if (!c) return KG_ERR_PARAM;
     KG_GUARD(c, {
-        if (enable && !c->ev0) {
-            CK(cudaEventCreate(&c->ev0));
-            CK(cudaEventCreate(&c->ev1));
+        if (enable && !c->ev0[0]) {
+            for (int k = 0; k < 4; ++k) {
+                CK(cudaEventCreate(&c->ev0[k]));
+                CK(cudaEventCreate(&c->ev1[k]));
+            }
         }
         c->timing = enable != 0;
         c->kernel_ms = 0.0;

@@ -88,6 +88,12 @@ struct StepArgs {
     double t_max;    // nextT stamped into the maxima (S3)
     int do_maxima;
     unsigned long long* cfl_min;  // ordered-bits min of the tile CFL terms
+    // Stage gate: the CFL words of the earlier stages of this hydraulic step.  The pass does
+    // nothing when one of them advises a dt below `dt` (the host then refines dt), so the
+    // three stages can be queued without waiting for the host's test in between.
+    const unsigned long long* gate[2];
+    int ngate;
+    int partial;     // fewer active tiles than tiles: the advised dt is capped by maxdt
 };
 
 }  // namespace kg

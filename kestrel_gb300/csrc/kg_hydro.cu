@@ -253,7 +253,25 @@ __device__ __forceinline__ void face_flux(const DevParams& P, bool xdir, const S
     out[6] = 0.5 * (dP2 + dM2);
 }
 
+// The host's advised-dt test (ComputeAdvisedTimeStep, src/HydraulicRHS.f90:141-174, for
+// substeps 2 and 3; refinement at src/TimeStepper.f90:393-404 and :452-463) on the CFL words
+// of the earlier stages of this step, with the host's operation order.  False when one of
+// them would have refined dt: the pass then leaves every output untouched.
+__device__ __forceinline__ bool stage_gate_open(const StepArgs& S) {
+    const DevParams& P = cP;
+    for (int g = 0; g < S.ngate; ++g) {
+        unsigned long long bits = *(volatile const unsigned long long*)S.gate[g];
+        double umin = __longlong_as_double((long long)bits);
+        if (S.partial) umin = mn(umin, P.maxdt);
+        double m = mn(P.cfl * umin, P.diffusiveTimeScale);
+        m = mn(m, P.maxdt);
+        if (m < S.dt) return false;
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __restrict__ blocks, StepArgs S) {
+    if (S.ngate > 0 && !stage_gate_open(S)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     HydroSmem& sm = *reinterpret_cast<HydroSmem*>(smraw);
     const DevParams& P = cP;
