@@ -29,8 +29,8 @@ cudaError_t set_constants(const DevParams& p, const DevSource* src, int nsrc, cu
 cudaError_t launch_hydro(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st);
 // kg_tiles.cu
 cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
-cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
-cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
+cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, cudaStream_t st);
+cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, bool plain, cudaStream_t st);
 // kg_hydro32.cu
 cudaError_t launch_hydro32(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st);
 cudaError_t launch_topo32(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, cudaStream_t st);
@@ -40,15 +40,16 @@ cudaError_t launch_ghost_edges(const DevArrays& A, int slot, int mask, int qcur,
 cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, int ts, cudaStream_t st);
 cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st);
 cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn_over, int* d_flags,
-                             cudaStream_t st);
+                             int nX, int nY, cudaStream_t st);
 cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
                           double* d_out, cudaStream_t st);
 // kg_morpho.cu
 cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, cudaStream_t st);
-cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, cudaStream_t st);
+cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st);
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
-                        cudaStream_t st);
-cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, cudaStream_t st);
+                        bool fp32, cudaStream_t st);
+cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, bool fp32,
+                           cudaStream_t st);
 cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
                            unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st);
 cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, int nwaves, int qa, int tcur,
@@ -121,7 +122,7 @@ struct kg_ctx {
     bool sources_loaded = false;
     int qcur = 0;                        // state buffer holding the solution (0..3)
     int tcur = 0;                        // topography set of the solution (0..1)
-    bool tdirty[2] = {true, true};       // FP32 form: the set's factor cache needs a rebuild
+    int tdirty[2] = {2, 2};              // FP32 form factor cache of a set: 0 clean, 1 active tiles stale, 2 all stale
     // Edge-band flags of the active tiles computed right after the last accepted hydraulic
     // step on its result (state buffer act_q, topography set act_t), so the next
     // CheckIfNearBoundaries needs no wait of its own; act_gen guards against host writes.
@@ -384,7 +385,7 @@ void push_bed(kg_ctx& c, int s) {
     }
 }
 void touch(kg_ctx& c, int s) {
-    c.tdirty[0] = c.tdirty[1] = true;
+    c.tdirty[0] = c.tdirty[1] = 2;
     if (std::find(c.touched.begin(), c.touched.end(), s) == c.touched.end()) c.touched.push_back(s);
 }
 // The second topography set of a slot is scratch for active tiles during a step and a
@@ -408,7 +409,7 @@ void cell_topo(kg_ctx& c, int id) {
     std::vector<int> one{s};
     upload_list(c, one);
     CK(launch_cell_topo(c.A, c.d_list, 1, c.tcur, c.st));
-    CK(launch_face_bI(c.A, c.d_list, 1, c.tcur, c.st));
+    CK(launch_face_bI(c.A, c.d_list, 1, c.tcur, c.nX, c.nY, c.st));
     c.launches += 2;
     touch(c, s);
     sync(c);
@@ -418,7 +419,7 @@ bool is_active_ghost(kg_ctx& c, int id) { return in_list(c.ghost, id) && T(c, id
 
 // EqualiseTopographicBoundaryData, src/MorphodynamicRHS.f90:588-687 (vertex and face b0).
 void equalise(kg_ctx& c, int id) {
-    c.tdirty[0] = c.tdirty[1] = true;
+    c.tdirty[0] = c.tdirty[1] = 2;
     int nX = c.nX, nY = c.nY, V = nX + 1;
     auto ok = [&](int t) { return in_bounds(c, t) && (in_list(c.active, t) || is_active_ghost(c, t)); };
     auto B0 = [&](int t) -> std::vector<double>& { return c.hb0[T(c, t).slot]; };
@@ -584,11 +585,11 @@ void add_tile(kg_ctx& c, int k) {
     add_ghost_tiles(c, k);
     std::vector<int> one{T(c, k).slot};
     upload_list(c, one);
-    CK(launch_face_topo(c.A, c.d_list, 1, c.tcur, c.st));
+    CK(launch_face_topo(c.A, c.d_list, 1, c.tcur, c.nX, c.nY, false, c.st));
     c.launches++;
     sync(c);
     c.blocks_dirty = true;
-    c.tdirty[0] = c.tdirty[1] = true;
+    c.tdirty[0] = c.tdirty[1] = 2;
 }
 
 void rebuild_blocks(kg_ctx& c) {
@@ -624,7 +625,7 @@ void check_near_boundaries(kg_ctx& c) {
         fl = c.act_flags;
     } else {
         upload_list(c, slots);
-        CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), c.qcur, c.tcur, c.src_override ? c.d_srcHn : nullptr, c.d_flags, c.st));
+        CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), c.qcur, c.tcur, c.src_override ? c.d_srcHn : nullptr, c.d_flags, c.nX, c.nY, c.st));
         c.launches++;
         fl.resize(slots.size());
         CK(cudaMemcpyAsync(fl.data(), c.d_flags, fl.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
@@ -667,7 +668,8 @@ double advised(kg_ctx& c, unsigned long long bits, int substep) {
 void refresh_topo32(kg_ctx& c, int ts) {
     std::vector<int> slots;
     for (int id : c.active) slots.push_back(T(c, id).slot);
-    for (int id : c.ghost) slots.push_back(T(c, id).slot);
+    if (c.tdirty[ts] > 1)
+        for (int id : c.ghost) slots.push_back(T(c, id).slot);
     if ((int)slots.size() > c.d_tlist_cap) {
         if (c.d_tlist) CK(cudaFree(c.d_tlist));
         c.d_tlist_cap = std::max<int>((int)slots.size(), 2 * c.d_tlist_cap);
@@ -678,7 +680,7 @@ void refresh_topo32(kg_ctx& c, int ts) {
         CK(launch_topo32(c.A, c.d_tlist, (int)slots.size(), ts, c.nX, c.nY, c.st));
         c.launches++;
     }
-    c.tdirty[ts] = false;
+    c.tdirty[ts] = 0;
 }
 
 constexpr unsigned long long HUGE_BITS = 0x7FEFFFFFFFFFFFFFull;  // bits of huge(1.0_wp)
@@ -757,7 +759,7 @@ bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int e_set, int topo, int
     std::vector<int> slots;
     for (int id : c.active) slots.push_back(T(c, id).slot);
     upload_list(c, slots);
-    CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), q_out, topo, nullptr, c.d_flags, c.st));
+    CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), q_out, topo, nullptr, c.d_flags, c.nX, c.nY, c.st));
     c.launches++;
     c.act_tmp.resize(slots.size());
     CK(cudaMemcpyAsync(c.act_tmp.data(), c.d_flags, slots.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
@@ -853,9 +855,10 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
     CK(launch_m_init(c.A, c.d_list, n, c.SV, qa, c.tcur, tnew, c.st));
     c.launches++;
     for (int stage = 1; stage <= 3; ++stage) {
-        CK(launch_m_emd(c.A, c.d_list, n, c.SC, tnew, c.st));
-        CK(launch_m_bt(c.A, c.d_list, n, c.SV, c.tcur, tnew, stage, dt_m, c.st));
-        CK(launch_m_cells(c.A, c.d_list, n, c.SC, qa, c.tcur, tnew, c.st));
+        const bool fp32 = c.prec == KG_PREC_FP32;
+        CK(launch_m_emd(c.A, c.d_list, n, c.SC, tnew, fp32, c.st));
+        CK(launch_m_bt(c.A, c.d_list, n, c.SV, c.tcur, tnew, stage, dt_m, fp32, c.st));
+        CK(launch_m_cells(c.A, c.d_list, n, c.SC, qa, c.tcur, tnew, fp32, c.st));
         c.launches += 3;
     }
     int need = n * c.SC;
@@ -916,11 +919,11 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
         return true;
     }
     upload_list(c, slots);
-    CK(launch_face_topo(c.A, c.d_list, n, tnew, c.st));
-    CK(launch_face_bI(c.A, c.d_list, n, tnew, c.st));
+    CK(launch_face_topo(c.A, c.d_list, n, tnew, c.nX, c.nY, c.prec == KG_PREC_FP32, c.st));
+    CK(launch_face_bI(c.A, c.d_list, n, tnew, c.nX, c.nY, c.st));
     CK(launch_m_finish(c.A, c.d_list, n, c.SC, qa, c.st));
     c.launches += 3;
-    c.tdirty[tnew] = true;
+    c.tdirty[tnew] = std::max(c.tdirty[tnew], 1);
     return false;
 }
 

@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
 }
 
 // Topography factors of the FP32 form for the listed slots of set ts, from the FP64 cell
-// and face topography (gam = sqrt(1 + b_x^2 + b_y^2), src/Closures.f90:174-186; the
+// and face topography (FP32 factors from FP32 slopes; 1/gam^2 and 1/gam to FP64 accuracy) (gam = sqrt(1 + b_x^2 + b_y^2), src/Closures.f90:174-186; the
 // hydrostatic prefactors of ConstructHydraulicRHS, src/HydraulicRHS.f90:1236-1250; the
 // wave-speed factor (1 + b_t^2)/gam^3 of src/Equations.f90:249-381).
 __global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restrict__ slots, int ts, int per) {
@@ -460,20 +460,33 @@ __global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restri
     if (k < SC) {
         const double* ct = A.CT[ts] + plane(s, 4, 0, SC) + k;
         double b0 = ct[0], bt = ct[SC], bx = ct[2 * (size_t)SC], by = ct[3 * (size_t)SC];
-        double gam = gam_of(P.geo, bx, by);
         double* td = A.TD[ts] + plane(s, 3, 0, SC) + k;
-        td[0] = b0 + bt;
-        td[SC] = 1.0 / (gam * gam);
-        td[2 * (size_t)SC] = 1.0 / gam;
         float* tf = A.TF[ts] + plane(s, 6, 0, SC) + k;
-        tf[0] = (float)gam;
-        tf[SC] = (float)bx;
-        tf[2 * (size_t)SC] = (float)by;
+        td[0] = b0 + bt;
         if (P.geo) {
-            tf[3 * (size_t)SC] = (float)((1.0 + by * by) / gam);
-            tf[4 * (size_t)SC] = (float)(-bx * by / gam);
-            tf[5 * (size_t)SC] = (float)((1.0 + bx * bx) / gam);
+            // 1/gam^2 and 1/gam to FP64 accuracy: FP32 seeds refined by two Newton steps.
+            double g2 = 1.0 + (bx * bx + by * by);
+            double r = (double)(1.f / (float)g2);
+            r = r * (2.0 - g2 * r);
+            r = r * (2.0 - g2 * r);
+            double y = (double)rsqrtf((float)g2);
+            y = y * (1.5 - 0.5 * g2 * y * y);
+            y = y * (1.5 - 0.5 * g2 * y * y);
+            td[SC] = r;
+            td[2 * (size_t)SC] = y;
+            float bxf = (float)bx, byf = (float)by, igf = (float)y;
+            tf[0] = sqrtf((float)g2);
+            tf[SC] = bxf;
+            tf[2 * (size_t)SC] = byf;
+            tf[3 * (size_t)SC] = (1.f + byf * byf) * igf;
+            tf[4 * (size_t)SC] = -bxf * byf * igf;
+            tf[5 * (size_t)SC] = (1.f + bxf * bxf) * igf;
         } else {
+            td[SC] = 1.0;
+            td[2 * (size_t)SC] = 1.0;
+            tf[0] = 1.f;
+            tf[SC] = (float)bx;
+            tf[2 * (size_t)SC] = (float)by;
             tf[3 * (size_t)SC] = 1.f;
             tf[4 * (size_t)SC] = 0.f;
             tf[5 * (size_t)SC] = 1.f;
@@ -481,19 +494,19 @@ __global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restri
     }
     if (k < SFX) {
         const double* fx = A.FX[ts] + plane(s, 5, 0, SFX) + k;
-        double bx = fx[2 * (size_t)SFX], by = fx[3 * (size_t)SFX];
-        double g = gam_of(P.geo, bx, by);
+        float bx = (float)fx[2 * (size_t)SFX], by = (float)fx[3 * (size_t)SFX];
         float* o = A.TFX[ts] + plane(s, 2, 0, SFX) + k;
-        o[0] = (float)g;
-        o[SFX] = P.geo ? (float)((1.0 + by * by) / (g * g * g)) : 1.f;
+        float g = P.geo ? sqrtf(1.f + bx * bx + by * by) : 1.f;
+        o[0] = g;
+        o[SFX] = P.geo ? (1.f + by * by) / (g * g * g) : 1.f;
     }
     if (k < SFY) {
         const double* fy = A.FY[ts] + plane(s, 5, 0, SFY) + k;
-        double bx = fy[2 * (size_t)SFY], by = fy[3 * (size_t)SFY];
-        double g = gam_of(P.geo, bx, by);
+        float bx = (float)fy[2 * (size_t)SFY], by = (float)fy[3 * (size_t)SFY];
         float* o = A.TFY[ts] + plane(s, 2, 0, SFY) + k;
-        o[0] = (float)g;
-        o[SFY] = P.geo ? (float)((1.0 + bx * bx) / (g * g * g)) : 1.f;
+        float g = P.geo ? sqrtf(1.f + bx * bx + by * by) : 1.f;
+        o[0] = g;
+        o[SFY] = P.geo ? (1.f + bx * bx) / (g * g * g) : 1.f;
     }
 }
 

@@ -74,6 +74,9 @@ __device__ __forceinline__ double stage_hn(const DevArrays& A, int s, int c, int
     return A.kind[s] == SLOT_GHOST ? A.G9[mp(s, 9, 4, SC) + c] : A.MS[mp(s, 5, 2, SC) + c];
 }
 
+// R = double: the FP64 drop-in; R = float: the FP32 form's closures (the depth test and
+// the stored E - D stay FP64).
+template <class R>
 __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
     const DevParams& P = cP;
     int nX = P.nX, nY = P.nY, SC = nX * nY;
@@ -91,10 +94,10 @@ __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restric
         double e = P.hThr;
         double emd = 0.0;
         if (!(Hn < e || HnW < e || HnE < e || HnS < e || HnN < e)) {
-            double dbx = CT[mp(s, 4, 2, SC) + c], dby = CT[mp(s, 4, 3, SC) + c];
-            Pt<double> pt{Hn, A.UV[mp(s, 2, 0, SC) + c], A.UV[mp(s, 2, 1, SC) + c], A.MS[mp(s, 5, 3, SC) + c],
-                          A.MS[mp(s, 5, 4, SC) + c], CT[mp(s, 4, 1, SC) + c], dbx, dby, gam_of(P.geo, dbx, dby)};
-            emd = erosion_minus_deposition(P, pt);
+            R dbx = (R)CT[mp(s, 4, 2, SC) + c], dby = (R)CT[mp(s, 4, 3, SC) + c];
+            Pt<R> pt{(R)Hn, (R)A.UV[mp(s, 2, 0, SC) + c], (R)A.UV[mp(s, 2, 1, SC) + c], (R)A.MS[mp(s, 5, 3, SC) + c],
+                     (R)A.MS[mp(s, 5, 4, SC) + c], (R)CT[mp(s, 4, 1, SC) + c], dbx, dby, gam_of<R>(P.geo, dbx, dby)};
+            emd = (double)erosion_minus_deposition<R>(P, pt);
         }
         A.EMD[(size_t)s * SC + c] = emd;
     }
@@ -108,7 +111,9 @@ __device__ __forceinline__ double cellv(const DevArrays& A, const double* CT, in
     return f < 0 ? A.EMD[(size_t)s * SC + c] : CT[mp(s, 4, f, SC) + c];
 }
 
-// Vertex source term and clamped stage update of bt (one CTA per tile).
+// Vertex source term and clamped stage update of bt.  PLAIN (the FP32 form) sums the four
+// cell terms pairwise instead of the reference's compensated sums.
+template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt) {
     const DevParams& P = cP;
     int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
@@ -178,9 +183,16 @@ __global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict
             y[q] = cellv(A, CT, cs[q], 3, ci[q], cj[q], nX, SC);
             e[q] = cellv(A, CT, cs[q], -1, ci[q], cj[q], nX, SC);
         }
-        double kx = (mode == 2) ? kahan3(x[0], x[1], x[2] + x[3]) : kahan4(x[0], x[1], x[2], x[3]);
-        double ky = kahan4(y[0], y[1], y[2], y[3]);
-        double ke = (mode == 1) ? kahan3(e[0], e[1], e[2] + e[3]) : kahan4(e[0], e[1], e[2], e[3]);
+        double kx, ky, ke;
+        if (PLAIN) {
+            kx = (x[0] + x[1]) + (x[2] + x[3]);
+            ky = (y[0] + y[1]) + (y[2] + y[3]);
+            ke = (e[0] + e[1]) + (e[2] + e[3]);
+        } else {
+            kx = (mode == 2) ? kahan3(x[0], x[1], x[2] + x[3]) : kahan4(x[0], x[1], x[2], x[3]);
+            ky = kahan4(y[0], y[1], y[2], y[3]);
+            ke = (mode == 1) ? kahan3(e[0], e[1], e[2] + e[3]) : kahan4(e[0], e[1], e[2], e[3]);
+        }
         double gam = gam_of(P.geo, 0.25 * kx, 0.25 * ky);
         double ddt = -0.25 * gam / psib * ke;
         double bt0 = A.BV[tcur][mp(s, 2, 1, SV) + v];
@@ -194,7 +206,9 @@ __global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict
 }
 
 // Cell-centred bed of stage k, the conservative w / Hnpsi update and the stage's depth,
-// solids fraction and density.
+// solids fraction and density.  PLAIN (the FP32 form) takes the vertex sums pairwise
+// (differences first) and one divide per cell; every quantity stays FP64.
+template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
     const DevParams& P = cP;
     int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
@@ -206,11 +220,20 @@ __global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restr
         int c = item_;
         int i = c % nX, j = c / nX;
         int v00 = j * (nX + 1) + i, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
-        double b0c = 0.25 * kahan4(b0[v00], b0[v10], b0[v01], b0[v11]);
-        double btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
-        double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
-        double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
-        double dbx = 0.5 * P.dxR * kahan8(ax), dby = 0.5 * P.dyR * kahan8(ay);
+        double b0c, btc, dbx, dby;
+        if (PLAIN) {
+            b0c = 0.25 * ((b0[v00] + b0[v10]) + (b0[v01] + b0[v11]));
+            btc = 0.25 * ((bt[v00] + bt[v10]) + (bt[v01] + bt[v11]));
+            dbx = 0.5 * P.dxR * (((b0[v10] - b0[v00]) + (bt[v10] - bt[v00])) + ((b0[v11] - b0[v01]) + (bt[v11] - bt[v01])));
+            dby = 0.5 * P.dyR * (((b0[v01] - b0[v00]) + (bt[v01] - bt[v00])) + ((b0[v11] - b0[v10]) + (bt[v11] - bt[v10])));
+        } else {
+            b0c = 0.25 * kahan4(b0[v00], b0[v10], b0[v01], b0[v11]);
+            btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
+            double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
+            double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
+            dbx = 0.5 * P.dxR * kahan8(ax);
+            dby = 0.5 * P.dyR * kahan8(ay);
+        }
         A.CT[tnew][mp(s, 4, 0, SC) + c] = b0c;
         A.CT[tnew][mp(s, 4, 1, SC) + c] = btc;
         A.CT[tnew][mp(s, 4, 2, SC) + c] = dbx;
@@ -221,16 +244,27 @@ __global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restr
         double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
         double Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
         double db = btc - C0[mp(s, 4, 1, SC) + c];
-        double w = -db / gamnew / gamnew;
-        w = w + btc;
-        w = w + Hn_old * gamold / gamnew / gamnew;
-        w = w + b0c;
-        double Hnpsi = -(psib)*db / gamnew;
-        Hnpsi = Hnpsi + p0 * gamold / gamnew;
-        double Hn = compute_hn(w, b0c, btc, gamnew);
-        if (Hn < 0.0) Hn = 0.0;
-        double pp = Hnpsi < 0.0 ? 0.0 : Hnpsi;
-        double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
+        double w, Hnpsi, Hn, psi;
+        if (PLAIN) {
+            double ign = 1.0 / gamnew;
+            w = (b0c + btc) + (Hn_old * gamold - db) * (ign * ign);
+            Hnpsi = (p0 * gamold - psib * db) * ign;
+            Hn = ((w - b0c) - btc) * gamnew;
+            if (Hn < 0.0) Hn = 0.0;
+            float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi, e2f = (float)e2;
+            psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, e2f)), (float)P.maxPack);
+        } else {
+            w = -db / gamnew / gamnew;
+            w = w + btc;
+            w = w + Hn_old * gamold / gamnew / gamnew;
+            w = w + b0c;
+            Hnpsi = -(psib)*db / gamnew;
+            Hnpsi = Hnpsi + p0 * gamold / gamnew;
+            Hn = compute_hn(w, b0c, btc, gamnew);
+            if (Hn < 0.0) Hn = 0.0;
+            double pp = Hnpsi < 0.0 ? 0.0 : Hnpsi;
+            psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
+        }
         double* M = A.MS + mp(s, 5, 0, SC) + c;
         M[0] = w;
         M[(size_t)SC] = Hnpsi;
@@ -469,17 +503,21 @@ cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int ver
     k_m_init<<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
     return cudaGetLastError();
 }
-cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, cudaStream_t st) {
-    k_m_emd<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, tnew);
+cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st) {
+    if (fp32) k_m_emd<float><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, tnew);
+    else k_m_emd<double><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, tnew);
     return cudaGetLastError();
 }
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
-                        cudaStream_t st) {
-    k_m_bt<<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
+                        bool fp32, cudaStream_t st) {
+    if (fp32) k_m_bt<true><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
+    else k_m_bt<false><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
     return cudaGetLastError();
 }
-cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, cudaStream_t st) {
-    k_m_cells<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
+cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, bool fp32,
+                           cudaStream_t st) {
+    if (fp32) k_m_cells<true><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
+    else k_m_cells<false><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
     return cudaGetLastError();
 }
 cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,

@@ -42,18 +42,21 @@ __global__ void k_cell_topo(DevArrays A, const int* __restrict__ slots, int ts) 
     }
 }
 
-__global__ void k_face_bI(DevArrays A, const int* __restrict__ slots, int ts) {
+// Per-tile kernels over the faces / cells of the listed tiles run `per` CTAs of 256
+// threads per tile, one face (x and y) or cell per thread.
+__global__ void __launch_bounds__(256) k_face_bI(DevArrays A, const int* __restrict__ slots, int ts, int per) {
     const DevParams& P = cP;
-    int s = slots[blockIdx.x];
+    int s = slots[blockIdx.x / per];
+    int f = (blockIdx.x % per) * 256 + threadIdx.x;
     int nX = P.nX, nY = P.nY, SV = (nX + 1) * (nY + 1), SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
     const double* b0 = A.BV[ts] + pl(s, 2, 0, SV);
     const double* bt = A.BV[ts] + pl(s, 2, 1, SV);
-    for (int f = threadIdx.x; f < SFX; f += blockDim.x) {
+    if (f < SFX) {
         int a = f % (nX + 1), j = f / (nX + 1);
         int v0 = j * (nX + 1) + a, v1 = v0 + (nX + 1);
         A.FX[ts][pl(s, 5, 4, SFX) + f] = interp_b(b0[v0], b0[v1], bt[v0], bt[v1]);
     }
-    for (int f = threadIdx.x; f < SFY; f += blockDim.x) {
+    if (f < SFY) {
         int i = f % nX, a = f / nX;
         int v0 = a * (nX + 1) + i, v1 = v0 + 1;
         A.FY[ts][pl(s, 5, 4, SFY) + f] = interp_b(b0[v0], b0[v1], bt[v0], bt[v1]);
@@ -61,10 +64,13 @@ __global__ void k_face_bI(DevArrays A, const int* __restrict__ slots, int ts) {
 }
 
 // Face bt and slopes of one tile from its own vertices and the adjacent column/row of
-// the W/E/S/N tiles' vertex copies.
-__global__ void k_face_topo(DevArrays A, const int* __restrict__ slots, int ts) {
+// the W/E/S/N tiles' vertex copies.  PLAIN (the FP32 form) sums the vertex terms pairwise
+// in FP64, differences first, instead of the reference's compensated sums.
+template <bool PLAIN>
+__global__ void __launch_bounds__(256) k_face_topo(DevArrays A, const int* __restrict__ slots, int ts, int per) {
     const DevParams& P = cP;
-    int s = slots[blockIdx.x];
+    int s = slots[blockIdx.x / per];
+    int f = (blockIdx.x % per) * 256 + threadIdx.x;
     int nX = P.nX, nY = P.nY, SV = (nX + 1) * (nY + 1), SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
     int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sS = A.nbr[s * 8 + NB_S], sN = A.nbr[s * 8 + NB_N];
     const double* BV = A.BV[ts];
@@ -73,37 +79,51 @@ __global__ void k_face_topo(DevArrays A, const int* __restrict__ slots, int ts) 
     const double* b0 = BV + pl(s, 2, 0, SV);
     const double* bt = BV + pl(s, 2, 1, SV);
     const int V = nX + 1;
-    for (int f = threadIdx.x; f < SFX; f += blockDim.x) {
+    if (f < SFX) {
         int a = f % (nX + 1), j = f / (nX + 1);  // vertex column a, rows j..j+1
         // d/dx from the vertex columns either side (the W/E tile's copy at the tile edge)
         const double *lb0 = b0, *lbt = bt, *rb0 = b0, *rbt = bt;
         int la = a - 1, ra = a + 1;
         if (a == 0) { lb0 = BV + pl(sW, 2, 0, SV); lbt = BV + pl(sW, 2, 1, SV); la = nX - 1; }
         if (a == nX) { rb0 = BV + pl(sE, 2, 0, SV); rbt = BV + pl(sE, 2, 1, SV); ra = 1; }
-        double ax[8] = {rb0[j * V + ra], rbt[j * V + ra], rb0[(j + 1) * V + ra], rbt[(j + 1) * V + ra],
-                        -lb0[j * V + la], -lbt[j * V + la], -lb0[(j + 1) * V + la], -lbt[(j + 1) * V + la]};
-        double dbdx = 0.25 * P.dxR * kahan8(ax);
         int v0 = j * V + a, v1 = v0 + V;
         double btf = 0.5 * (bt[v0] + bt[v1]);
-        double ay[4] = {b0[v1], bt[v1], -b0[v0], -bt[v0]};
-        double dbdy = P.dyR * kahan4(ay[0], ay[1], ay[2], ay[3]);
+        double dbdx, dbdy;
+        if (PLAIN) {
+            dbdx = 0.25 * P.dxR * (((rb0[j * V + ra] - lb0[j * V + la]) + (rbt[j * V + ra] - lbt[j * V + la])) +
+                                   ((rb0[(j + 1) * V + ra] - lb0[(j + 1) * V + la]) + (rbt[(j + 1) * V + ra] - lbt[(j + 1) * V + la])));
+            dbdy = P.dyR * ((b0[v1] - b0[v0]) + (bt[v1] - bt[v0]));
+        } else {
+            double ax[8] = {rb0[j * V + ra], rbt[j * V + ra], rb0[(j + 1) * V + ra], rbt[(j + 1) * V + ra],
+                            -lb0[j * V + la], -lbt[j * V + la], -lb0[(j + 1) * V + la], -lbt[(j + 1) * V + la]};
+            dbdx = 0.25 * P.dxR * kahan8(ax);
+            double ay[4] = {b0[v1], bt[v1], -b0[v0], -bt[v0]};
+            dbdy = P.dyR * kahan4(ay[0], ay[1], ay[2], ay[3]);
+        }
         FXs[pl(s, 5, 1, SFX) + f] = btf;
         FXs[pl(s, 5, 2, SFX) + f] = dbdx;
         FXs[pl(s, 5, 3, SFX) + f] = dbdy;
     }
-    for (int f = threadIdx.x; f < SFY; f += blockDim.x) {
+    if (f < SFY) {
         int i = f % nX, a = f / nX;  // vertex row a, columns i..i+1
         int v0 = a * V + i, v1 = v0 + 1;
         double btf = 0.5 * (bt[v0] + bt[v1]);
-        double axv[4] = {b0[v1], bt[v1], -b0[v0], -bt[v0]};
-        double dbdx = P.dxR * kahan4(axv[0], axv[1], axv[2], axv[3]);
         const double *db0 = b0, *dbt = bt, *ub0 = b0, *ubt = bt;
         int da = a - 1, ua = a + 1;
         if (a == 0) { db0 = BV + pl(sS, 2, 0, SV); dbt = BV + pl(sS, 2, 1, SV); da = nY - 1; }
         if (a == nY) { ub0 = BV + pl(sN, 2, 0, SV); ubt = BV + pl(sN, 2, 1, SV); ua = 1; }
-        double ay[8] = {ub0[ua * V + i + 1], ubt[ua * V + i + 1], ub0[ua * V + i], ubt[ua * V + i],
-                        -db0[da * V + i + 1], -dbt[da * V + i + 1], -db0[da * V + i], -dbt[da * V + i]};
-        double dbdy = 0.25 * P.dyR * kahan8(ay);
+        double dbdx, dbdy;
+        if (PLAIN) {
+            dbdx = P.dxR * ((b0[v1] - b0[v0]) + (bt[v1] - bt[v0]));
+            dbdy = 0.25 * P.dyR * (((ub0[ua * V + i + 1] - db0[da * V + i + 1]) + (ubt[ua * V + i + 1] - dbt[da * V + i + 1])) +
+                                   ((ub0[ua * V + i] - db0[da * V + i]) + (ubt[ua * V + i] - dbt[da * V + i])));
+        } else {
+            double axv[4] = {b0[v1], bt[v1], -b0[v0], -bt[v0]};
+            dbdx = P.dxR * kahan4(axv[0], axv[1], axv[2], axv[3]);
+            double ay[8] = {ub0[ua * V + i + 1], ubt[ua * V + i + 1], ub0[ua * V + i], ubt[ua * V + i],
+                            -db0[da * V + i + 1], -dbt[da * V + i + 1], -db0[da * V + i], -dbt[da * V + i]};
+            dbdy = 0.25 * P.dyR * kahan8(ay);
+        }
         FYs[pl(s, 5, 1, SFY) + f] = btf;
         FYs[pl(s, 5, 2, SFY) + f] = dbdx;
         FYs[pl(s, 5, 3, SFY) + f] = dbdy;
@@ -228,14 +248,16 @@ __global__ void k_init_maxima(DevArrays A, int slot) {
 // Edge-band tests of NearNorth/South/East/WestBoundary for each listed active slot:
 // bit 0 N, 1 S, 2 E, 3 W.  hn_over (optional) replaces the depth computed from w (used
 // for the first check after the sources have set the depth field directly).
-__global__ void k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur, int ts, const double* __restrict__ hn_over,
-                            int* __restrict__ flags) {
+__global__ void __launch_bounds__(256) k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur, int ts,
+                                                    const double* __restrict__ hn_over, int* __restrict__ flags, int per) {
     const DevParams& P = cP;
-    int s = slots[blockIdx.x];
+    int pos = blockIdx.x / per, chunk = blockIdx.x % per;
+    int s = slots[pos];
     int nX = P.nX, nY = P.nY, SC = nX * nY, TB = P.TileBuffer;
     const double* Q = A.Q[qcur];
     int f = 0;
-    for (int c = threadIdx.x; c < SC; c += blockDim.x) {
+    int c = chunk * 256 + threadIdx.x;
+    if (c < SC) {
         int i = c % nX, j = c / nX;
         double Hn;
         if (hn_over) {
@@ -257,18 +279,14 @@ __global__ void k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur
     }
     // The reference's scans start from ydist = 0 (N, E) or nY/nX (S, W), so a buffer
     // wider than the tile triggers without any wet cell.
-    if (threadIdx.x == 0) {
+    if (chunk == 0 && threadIdx.x == 0) {
         if (0 > nY - TB) f |= 1;
         if (nY <= TB) f |= 2;
         if (0 > nX - TB) f |= 4;
         if (nX <= TB) f |= 8;
     }
-    __shared__ int red;
-    if (threadIdx.x == 0) red = 0;
-    __syncthreads();
-    if (f) atomicOr(&red, f);
-    __syncthreads();
-    if (threadIdx.x == 0) flags[blockIdx.x] = red;
+    f = __reduce_or_sync(0xffffffffu, f);
+    if ((threadIdx.x & 31) == 0 && f) atomicOr(&flags[pos], f);
 }
 
 // Sequential compensated sums over the active tiles in list order (j outer, i inner).
@@ -316,14 +334,18 @@ cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, int 
     k_cell_topo<<<n, 256, 0, st>>>(A, d_slots, ts);
     return cudaGetLastError();
 }
-cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st) {
+static inline int faces_per(int nX, int nY) { return (std::max((nX + 1) * nY, nX * (nY + 1)) + 255) / 256; }
+cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_face_bI<<<n, 256, 0, st>>>(A, d_slots, ts);
+    int per = faces_per(nX, nY);
+    k_face_bI<<<n * per, 256, 0, st>>>(A, d_slots, ts, per);
     return cudaGetLastError();
 }
-cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st) {
+cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, bool plain, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_face_topo<<<n, 256, 0, st>>>(A, d_slots, ts);
+    int per = faces_per(nX, nY);
+    if (plain) k_face_topo<true><<<n * per, 256, 0, st>>>(A, d_slots, ts, per);
+    else k_face_topo<false><<<n * per, 256, 0, st>>>(A, d_slots, ts, per);
     return cudaGetLastError();
 }
 cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, int ts, cudaStream_t st) {
@@ -347,9 +369,12 @@ cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn_over, int* d_flags,
-                             cudaStream_t st) {
+                             int nX, int nY, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_act_flags<<<n, 256, 0, st>>>(A, d_slots, qcur, ts, hn_over, d_flags);
+    cudaError_t e = cudaMemsetAsync(d_flags, 0, (size_t)n * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    int per = (nX * nY + 255) / 256;
+    k_act_flags<<<n * per, 256, 0, st>>>(A, d_slots, qcur, ts, hn_over, d_flags, per);
     return cudaGetLastError();
 }
 cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
