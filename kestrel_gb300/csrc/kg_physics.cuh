@@ -89,6 +89,12 @@ template <class R> struct Pt {
     R Hn, u, v, psi, rho, bt, dbdx, dbdy, gam;
 };
 
+// 0.5 (1 + tanh x), the smooth switch of several closures.  The FP64 form evaluates the
+// reference's expression; the FP32 form uses the equal logistic 1 / (1 + exp(-2x)), which
+// keeps its relative precision where 1 + tanh x cancels (x below about -9 in FP32).
+template <class R> KG_HD R half_one_plus_tanh(R x) { return R(0.5) * (R(1) + tanh(x)); }
+template <> KG_HD float half_one_plus_tanh<float>(float x) { return 1.f / (1.f + expf(-2.f * x)); }
+
 template <class R> KG_HD R pouliquen_mu(const DevParams& P, R gcos, R Hn, R modu) {
     R mu1 = R(P.PMin), mu2 = R(P.PMax), beta = R(P.PBeta);
     if (Hn > R(P.hThr)) {
@@ -101,7 +107,7 @@ template <class R> KG_HD R pouliquen_mu(const DevParams& P, R gcos, R Hn, R modu
 template <class R> KG_HD R fswitch(const DevParams& P, R psi) {
     R rate = R(P.SwRate), val = R(P.SwValue);
     switch (P.fswitch) {
-        case KG_SWITCH_TANH: return R(0.5) * (R(1) + tanh(rate * (psi - val)));
+        case KG_SWITCH_TANH: return half_one_plus_tanh<R>(rate * (psi - val));
         case KG_SWITCH_RAT3: {
             R a = val - R(1.5) / rate, b = val + R(1.5) / rate;
             if (psi <= a) return R(0);
@@ -235,7 +241,7 @@ template <class R> KG_HD R erosion_closure(const DevParams& P, const Pt<R>& s) {
 template <class R> KG_HD R erosion_transition(const DevParams& P, R bt) {
     R d = R(P.EroDepth);
     switch (P.etrans) {
-        case KG_ETRANS_SMOOTH: return R(0.5) * (R(1) + tanh(R(1e5) * (bt + d)));
+        case KG_ETRANS_SMOOTH: return half_one_plus_tanh<R>(R(1e5) * (bt + d));
         case KG_ETRANS_STEP: return (bt < -d) ? R(0) : R(1);
         default: return R(1);
     }
@@ -243,7 +249,7 @@ template <class R> KG_HD R erosion_transition(const DevParams& P, R bt) {
 template <class R> KG_HD R morpho_damping(const DevParams& P, R Hn) {
     R Hc = R(P.EroCriticalHeight);
     switch (P.damping) {
-        case KG_DAMP_TANH: return R(0.5) * (R(1) + tanh(R(10) * log(Hn / Hc)));
+        case KG_DAMP_TANH: return half_one_plus_tanh<R>(R(10) * log(Hn / Hc));
         case KG_DAMP_RAT3: {
             if (Hn < Hc) return R(0);
             if (Hn > R(2) * Hc) return R(1);
