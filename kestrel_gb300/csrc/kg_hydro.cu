@@ -29,6 +29,7 @@
 namespace kg {
 
 __constant__ DevParams cP;
+__constant__ DevParams32 cP32;  // FP32 copy for the FP32 form
 __constant__ DevSource cSrc[MAX_SRC];
 
 constexpr int BS = 16;
@@ -622,6 +623,10 @@ size_t hydro_smem_bytes() { return sizeof(HydroSmem); }
 
 cudaError_t set_constants(const DevParams& p, const DevSource* src, int nsrc, cudaStream_t st) {
     cudaError_t e = cudaMemcpyToSymbolAsync(cP, &p, sizeof(DevParams), 0, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    static DevParams32 p32;  // the copy is asynchronous: keep the source alive
+    p32 = params32(p);
+    e = cudaMemcpyToSymbolAsync(cP32, &p32, sizeof(DevParams32), 0, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     if (nsrc > 0) e = cudaMemcpyToSymbolAsync(cSrc, src, sizeof(DevSource) * nsrc, 0, cudaMemcpyHostToDevice, st);
     return e;

@@ -31,15 +31,14 @@ struct __align__(16) Hydro32Smem {
 };
 
 // Desingularised variables (src/HydraulicRHS.f90:762-878) in FP32 from the FP32 depth.
-__device__ __forceinline__ void desing32(const DevParams& P, float hp, float gam, float m1, float m2, float pp, float& Hn,
+__device__ __forceinline__ void desing32(const DevParams32& P, float hp, float gam, float m1, float m2, float pp, float& Hn,
                                          float& psi, float& rho, float& u, float& v) {
     Hn = hp * gam;
     if (Hn < 0.f) Hn = 0.f;
     float Hnpsi = pp < 0.f ? 0.f : pp;
-    float e2 = (float)(P.hThr * P.hThr);
-    float den = Hn * Hn + fmaxf(Hn * Hn, e2);
+    float den = Hn * Hn + fmaxf(Hn * Hn, P.hThr2);
     float r2 = 2.f * Hn / den;
-    psi = fminf(r2 * Hnpsi, (float)P.maxPack);
+    psi = fminf(r2 * Hnpsi, P.maxPack);
     rho = density<float>(P, psi);
     float k = r2 / rho;
     u = k * m1;
@@ -52,9 +51,9 @@ struct Side32 {
 
 // Central-upwind fluxes at one face in FP32 (CalculateFluxes, src/HydraulicRHS.f90:949-1064).
 // gamf and kf = (1 + b_t^2)/gamf^3 are the face's cached factors.
-__device__ __forceinline__ void face_flux32(const DevParams& P, bool xdir, const Side32& Pl, const Side32& Mi, float gamf,
+__device__ __forceinline__ void face_flux32(const DevParams32& P, bool xdir, const Side32& Pl, const Side32& Mi, float gamf,
                                             float kf, float gamL, float gamR, float h, float out[7], float& cfl) {
-    const float g = (float)P.g;
+    const float g = P.g;
     float HnP = Pl.hp * gamf, HnM = Mi.hp * gamf;
     float unP = xdir ? Pl.u : Pl.v, unM = xdir ? Mi.u : Mi.v;
     float hP = HnP <= 0.f ? 0.f : HnP, hM = HnM <= 0.f ? 0.f : HnM;
@@ -85,7 +84,7 @@ __device__ __forceinline__ void face_flux32(const DevParams& P, bool xdir, const
     out[2] = (m2P - m2M) * apn + (ap * m2M * unM - an * m2P * unP);
     float GP = 0.5f * g * Pl.rho * Pl.hp * Pl.hp, GM = 0.5f * g * Mi.rho * Mi.hp * Mi.hp;
     out[4] = ap * GM - an * GP;
-    const float nu = (float)P.nu;
+    const float nu = P.nu;
     float dP1 = 0.f, dP2 = 0.f, dM1 = 0.f, dM2 = 0.f;
     if (!(HnP < 0.f)) {
         dP1 = nu * Pl.rho * HnP * Pl.du;
@@ -114,6 +113,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
     extern __shared__ __align__(16) unsigned char smraw[];
     Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
     const DevParams& P = cP;
+    const DevParams32& F = cP32;
     const BlockDesc bd = blocks[blockIdx.x];
     const int nX = P.nX, nY = P.nY, SC = nX * nY, SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
     const int slot = bd.slot;
@@ -180,14 +180,14 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
         float hp = (float)(w - TD[plane(s, 3, 0, SC) + c]);
         sm.w[r] = w; sm.p64[r] = pp; sm.m1[r] = m1; sm.m2[r] = m2; sm.p[r] = (float)pp; sm.hp[r] = hp;
         float Hn, psi, rho, u, v;
-        desing32(P, hp, gam, m1, m2, (float)pp, Hn, psi, rho, u, v);
+        desing32(F, hp, gam, m1, m2, (float)pp, Hn, psi, rho, u, v);
         sm.Hn[r] = Hn; sm.psi[r] = psi; sm.rho[r] = rho; sm.u[r] = u; sm.v[r] = v;
     }
     __syncthreads();
 
     // ---- B: limited slopes and face offsets ----
     const int lim = P.limiter;
-    const float dxR = (float)P.dxR, dyR = (float)P.dyR;
+    const float dxR = F.dxR, dyR = F.dyR;
     for (int k = tid; k < (bx + 2) * by; k += NT) {
         int cx = k % (bx + 2) - 1, cy = k / (bx + 2);
         int r = (cy + 2) * RG + (cx + 2);
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
 
     // ---- C: face states, corrections, fluxes, CFL ----
     float cfl = 3.402823466e38f;
-    const float hdx = 0.5f * (float)P.dx, hdy = 0.5f * (float)P.dy;
+    const float hdx = 0.5f * F.dx, hdy = 0.5f * F.dy;
     const float* __restrict__ TFXs = A.TFX[S.topo] + (size_t)slot * 2 * SFX;
     const float* __restrict__ TFYs = A.TFY[S.topo] + (size_t)slot * 2 * SFY;
     for (int k = tid; k < (bx + 1) * by; k += NT) {
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
         R.dv = sm.lx[3][liR];
         int fo = j * (nX + 1) + fi;
         float out[7];
-        face_flux32(P, true, R, L, TFXs[fo], TFXs[fo + SFX], sm.gam[rL], sm.gam[rR], (float)P.dx, out, cfl);
+        face_flux32(F, true, R, L, TFXs[fo], TFXs[fo + SFX], sm.gam[rL], sm.gam[rR], F.dx, out, cfl);
         int fo2 = cy * (BS + 1) + fx;
 #pragma unroll
         for (int q = 0; q < 7; ++q) sm.fx[q][fo2] = out[q];
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
         R.dv = sm.ly[3][liR];
         int fo = fj * nX + i;
         float out[7];
-        face_flux32(P, false, R, L, TFYs[fo], TFYs[fo + SFY], sm.gam[rL], sm.gam[rR], (float)P.dy, out, cfl);
+        face_flux32(F, false, R, L, TFYs[fo], TFYs[fo + SFY], sm.gam[rL], sm.gam[rR], F.dy, out, cfl);
         int fo2 = fy * BS + cx;
 #pragma unroll
         for (int q = 0; q < 7; ++q) sm.fy[q][fo2] = out[q];
@@ -386,13 +386,13 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
             E[0] = E[0] + s1 * ig2;
             E[3] = E[3] + s3 * ig;
         }
-        float grho = (float)P.g * sm.rho[r] * sm.hp[r] / gam;
+        float grho = F.g * sm.rho[r] * sm.hp[r] / gam;
         E1 = E1 - grho * dbdx;
         E2 = E2 - grho * dbdy;
         E[1] = E1;
         E[2] = E2;
         Pt<float> pt{sm.Hn[r], sm.u[r], sm.v[r], sm.psi[r], sm.rho[r], 0.f, dbdx, dbdy, gam};
-        float I = implicit_source<float>(P, pt, drag<float>(P, pt));
+        float I = implicit_source<float>(F, pt, drag<float>(F, pt));
         if (S.mode == MODE_RHS0) {
 #pragma unroll
             for (int f = 0; f < 4; ++f) A.E[S.e_set][plane(slot, 4, f, SC) + c] = E[f];
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
                 float gamt = gam_of<float>(P.geo, bxt, byt);
                 float hpt = (float)((q0p[0] - ct0[0]) - btt);
                 float Hn, psi, rho, u, v;
-                desing32(P, hpt, gamt, (float)q0p[SC], (float)q0p[2 * (size_t)SC], (float)q0p[3 * (size_t)SC], Hn, psi, rho, u, v);
+                desing32(F, hpt, gamt, (float)q0p[SC], (float)q0p[2 * (size_t)SC], (float)q0p[3 * (size_t)SC], Hn, psi, rho, u, v);
                 double* M = A.MX + plane(slot, 11, 0, SC) + c;
                 double tt = S.t_max;
                 double Hnd = Hn, psid = psi;

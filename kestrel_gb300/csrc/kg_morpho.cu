@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restric
             R dbx = (R)CT[mp(s, 4, 2, SC) + c], dby = (R)CT[mp(s, 4, 3, SC) + c];
             Pt<R> pt{(R)Hn, (R)A.UV[mp(s, 2, 0, SC) + c], (R)A.UV[mp(s, 2, 1, SC) + c], (R)A.MS[mp(s, 5, 3, SC) + c],
                      (R)A.MS[mp(s, 5, 4, SC) + c], (R)CT[mp(s, 4, 1, SC) + c], dbx, dby, gam_of<R>(P.geo, dbx, dby)};
-            emd = (double)erosion_minus_deposition<R>(P, pt);
+            if constexpr (sizeof(R) == sizeof(float)) emd = (double)erosion_minus_deposition<R>(cP32, pt);
+            else emd = erosion_minus_deposition<R>(P, pt);
         }
         A.EMD[(size_t)s * SC + c] = emd;
     }
@@ -251,8 +252,8 @@ __global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restr
             Hnpsi = (p0 * gamold - psib * db) * ign;
             Hn = ((w - b0c) - btc) * gamnew;
             if (Hn < 0.0) Hn = 0.0;
-            float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi, e2f = (float)e2;
-            psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, e2f)), (float)P.maxPack);
+            float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi;
+            psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, cP32.hThr2)), cP32.maxPack);
         } else {
             w = -db / gamnew / gamnew;
             w = w + btc;

@@ -7,7 +7,7 @@
 // come from CUDA's math library (a few ulp from glibc's).
 //
 // The templates take a real type R: double for the FP64 drop-in, float for the flux and
-// closure arithmetic of the FP32 form.
+// closure arithmetic of the FP32 form; the settings struct PP is DevParams or DevParams32.
 #pragma once
 #include <cstdint>
 #include "../../include/kestrel_gpu.h"
@@ -31,6 +31,37 @@ struct DevParams {
     double maxPack, SolidDiameter, nu, hThr, tan1deg, SpongeStrength;
     double cfl, maxdt, diffusiveTimeScale;
 };
+
+// The same settings in FP32 for the FP32 form's arithmetic (a conversion from FP64 is an
+// FP64-pipe instruction on this GPU, so FP32 code reads these instead), plus hThr^2.
+#define KG_PARAMS_REALS(X)                                                                                          \
+    X(dx) X(dy) X(dxR) X(dyR) X(xSize) X(ySize) X(g) X(rhow) X(rhos) X(gred) X(ws0) X(nsettling) X(CriticalShields) \
+    X(ChezyCo) X(ManningCo) X(CoulombCo) X(PMin) X(PMax) X(PInt) X(PBeta) X(Ebetastar) X(Ekappa) X(EGamma)         \
+    X(SwRate) X(SwValue) X(EroRate) X(EroRateGranular) X(EroDepth) X(EroCriticalHeight) X(BedPorosity) X(maxPack)   \
+    X(SolidDiameter) X(nu) X(hThr) X(tan1deg) X(SpongeStrength) X(cfl) X(maxdt) X(diffusiveTimeScale)
+#define KG_PARAMS_INTS(X)                                                                                           \
+    X(nX) X(nY) X(nXtiles) X(nYtiles) X(geo) X(morpho) X(drag) X(erosion) X(deposition) X(etrans) X(damping)       \
+    X(fswitch) X(limiter) X(bcs) X(TileBuffer) X(nSources)
+struct DevParams32 {
+#define KG_F(n) float n;
+#define KG_I(n) int n;
+    KG_PARAMS_REALS(KG_F)
+    KG_PARAMS_INTS(KG_I)
+#undef KG_F
+#undef KG_I
+    float hThr2;
+};
+inline DevParams32 params32(const DevParams& d) {
+    DevParams32 f{};
+#define KG_F(n) f.n = (float)d.n;
+#define KG_I(n) f.n = d.n;
+    KG_PARAMS_REALS(KG_F)
+    KG_PARAMS_INTS(KG_I)
+#undef KG_F
+#undef KG_I
+    f.hThr2 = (float)(d.hThr * d.hThr);
+    return f;
+}
 
 constexpr double kPI = 3.141592653589793238462643383279502884;
 constexpr double kEPS = 2.220446049250313080847263336181640625e-16;  // epsilon(1.0_wp)
@@ -82,7 +113,7 @@ template <class R> KG_HD R modu2_of(int geo, R u, R v, R dbdx, R dbdy) {
     else m = m + v * v;
     return m;
 }
-template <class R> KG_HD R density(const DevParams& P, R psi) { return R(P.rhow) + (R(P.rhos) - R(P.rhow)) * psi; }
+template <class R, class PP> KG_HD R density(const PP& P, R psi) { return R(P.rhow) + (R(P.rhos) - R(P.rhow)) * psi; }
 
 // Cell / face state the closures read (a subset of the reference's 13-vector).
 template <class R> struct Pt {
@@ -95,7 +126,7 @@ template <class R> struct Pt {
 template <class R> KG_HD R half_one_plus_tanh(R x) { return R(0.5) * (R(1) + tanh(x)); }
 template <> KG_HD float half_one_plus_tanh<float>(float x) { return 1.f / (1.f + expf(-2.f * x)); }
 
-template <class R> KG_HD R pouliquen_mu(const DevParams& P, R gcos, R Hn, R modu) {
+template <class R, class PP> KG_HD R pouliquen_mu(const PP& P, R gcos, R Hn, R modu) {
     R mu1 = R(P.PMin), mu2 = R(P.PMax), beta = R(P.PBeta);
     if (Hn > R(P.hThr)) {
         R Fr = modu / sqrt(gcos * Hn);
@@ -104,7 +135,7 @@ template <class R> KG_HD R pouliquen_mu(const DevParams& P, R gcos, R Hn, R modu
     }
     return mu1;
 }
-template <class R> KG_HD R fswitch(const DevParams& P, R psi) {
+template <class R, class PP> KG_HD R fswitch(const PP& P, R psi) {
     R rate = R(P.SwRate), val = R(P.SwValue);
     switch (P.fswitch) {
         case KG_SWITCH_TANH: return half_one_plus_tanh<R>(rate * (psi - val));
@@ -129,14 +160,14 @@ template <class R> KG_HD R fswitch(const DevParams& P, R psi) {
         default: return (psi < val) ? R(0) : R(1);
     }
 }
-template <class R> KG_HD R chezy(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R chezy(const PP& P, const Pt<R>& s) {
     return R(P.ChezyCo) * modu2_of(P.geo, s.u, s.v, s.dbdx, s.dbdy);
 }
-template <class R> KG_HD R coulomb(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R coulomb(const PP& P, const Pt<R>& s) {
     R g = R(P.g) / s.gam;
     return R(P.CoulombCo) * g * s.Hn;
 }
-template <class R> KG_HD R pouliquen(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R pouliquen(const PP& P, const Pt<R>& s) {
     R g = R(P.g) / s.gam;
     R m2 = modu2_of(P.geo, s.u, s.v, s.dbdx, s.dbdy);
     R mu = pouliquen_mu(P, g, s.Hn, sqrt(m2));
@@ -144,7 +175,7 @@ template <class R> KG_HD R pouliquen(const DevParams& P, const Pt<R>& s) {
     return R(0);
 }
 // DragClosure dispatch (src/Parameters.f90:222-247).
-template <class R> KG_HD R drag(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R drag(const PP& P, const Pt<R>& s) {
     switch (P.drag) {
         case KG_DRAG_CHEZY: return chezy(P, s);
         case KG_DRAG_COULOMB: return coulomb(P, s);
@@ -179,7 +210,7 @@ template <class R> KG_HD R drag(const DevParams& P, const Pt<R>& s) {
     }
 }
 // ImplicitSourceTerms (src/Equations.f90:627-658): the value of both momentum rows.
-template <class R> KG_HD R implicit_source(const DevParams& P, const Pt<R>& s, R friction) {
+template <class R, class PP> KG_HD R implicit_source(const PP& P, const Pt<R>& s, R friction) {
     if (s.Hn > R(P.hThr)) {
         R modu = sqrt(modu2_of(P.geo, s.u, s.v, s.dbdx, s.dbdy));
         if (modu > R(1.0e-8)) {
@@ -191,16 +222,16 @@ template <class R> KG_HD R implicit_source(const DevParams& P, const Pt<R>& s, R
 }
 
 // -- erosion / deposition (src/Closures.f90:566-791, src/Equations.f90:385-448) --
-template <class R> KG_HD R shields(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R shields(const PP& P, const Pt<R>& s) {
     R gred = R(P.gred) / s.gam;
     R cf = R(P.ChezyCo) * modu2_of(P.geo, s.u, s.v, s.dbdx, s.dbdy);
     return cf / (gred * R(P.SolidDiameter));
 }
-template <class R> KG_HD R particle_speed(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R particle_speed(const PP& P, const Pt<R>& s) {
     R gred = R(P.gred) / s.gam;
     return sqrt(gred * R(P.SolidDiameter));
 }
-template <class R> KG_HD R fluid_erosion(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R fluid_erosion(const PP& P, const Pt<R>& s) {
     R sh = shields(P, s);
     if (sh > R(P.CriticalShields)) {
         R ero = R(P.EroRate) * (sh - R(P.CriticalShields));
@@ -208,7 +239,7 @@ template <class R> KG_HD R fluid_erosion(const DevParams& P, const Pt<R>& s) {
     }
     return R(0);
 }
-template <class R> KG_HD R granular_erosion(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R granular_erosion(const PP& P, const Pt<R>& s) {
     R m2 = modu2_of(P.geo, s.u, s.v, s.dbdx, s.dbdy);
     R mu1 = R(P.PMin), t1 = R(P.tan1deg);
     R stat = (mu1 + t1) / (R(1) - mu1 * t1);
@@ -222,7 +253,7 @@ template <class R> KG_HD R granular_erosion(const DevParams& P, const Pt<R>& s) 
     }
     return R(0);
 }
-template <class R> KG_HD R erosion_closure(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R erosion_closure(const PP& P, const Pt<R>& s) {
     switch (P.erosion) {
         case KG_ERO_MIXED: {
             R fc = fswitch(P, s.psi);
@@ -238,7 +269,7 @@ template <class R> KG_HD R erosion_closure(const DevParams& P, const Pt<R>& s) {
         default: return R(0);
     }
 }
-template <class R> KG_HD R erosion_transition(const DevParams& P, R bt) {
+template <class R, class PP> KG_HD R erosion_transition(const PP& P, R bt) {
     R d = R(P.EroDepth);
     switch (P.etrans) {
         case KG_ETRANS_SMOOTH: return half_one_plus_tanh<R>(R(1e5) * (bt + d));
@@ -246,7 +277,7 @@ template <class R> KG_HD R erosion_transition(const DevParams& P, R bt) {
         default: return R(1);
     }
 }
-template <class R> KG_HD R morpho_damping(const DevParams& P, R Hn) {
+template <class R, class PP> KG_HD R morpho_damping(const PP& P, R Hn) {
     R Hc = R(P.EroCriticalHeight);
     switch (P.damping) {
         case KG_DAMP_TANH: return half_one_plus_tanh<R>(R(10) * log(Hn / Hc));
@@ -259,7 +290,7 @@ template <class R> KG_HD R morpho_damping(const DevParams& P, R Hn) {
         default: return R(1);
     }
 }
-template <class R> KG_HD R deposition_closure(const DevParams& P, R psi) {
+template <class R, class PP> KG_HD R deposition_closure(const PP& P, R psi) {
     switch (P.deposition) {
         case KG_DEP_SIMPLE: return psi * (R(1) - psi / R(P.maxPack));
         case KG_DEP_SPEARMAN_MANNING: {
@@ -271,7 +302,7 @@ template <class R> KG_HD R deposition_closure(const DevParams& P, R psi) {
     }
 }
 // E - D with damping (ErosionDepositionTerms, src/Equations.f90:385-405).
-template <class R> KG_HD R erosion_minus_deposition(const DevParams& P, const Pt<R>& s) {
+template <class R, class PP> KG_HD R erosion_minus_deposition(const PP& P, const Pt<R>& s) {
     R E = erosion_closure(P, s) * erosion_transition(P, s.bt);
     R alpha;
     if (s.psi >= R(P.maxPack)) alpha = R(0);
