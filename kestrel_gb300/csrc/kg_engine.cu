@@ -33,6 +33,7 @@ cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts
 cudaError_t launch_face_topo(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, bool plain, cudaStream_t st);
 // kg_hydro32.cu
 cudaError_t launch_hydro32(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st);
+cudaError_t launch_dt(const unsigned long long* cfl, int partial, double cap, double* dtp, cudaStream_t st);
 cudaError_t launch_topo32(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, cudaStream_t st);
 cudaError_t launch_ghost_default(const DevArrays& A, int slot, int mode, int ts, cudaStream_t st);
 cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, double u, double v, double psi, int ts, cudaStream_t st);
@@ -114,6 +115,11 @@ struct kg_ctx {
     unsigned long long* d_cfl = nullptr;
     double* d_vol = nullptr;
     unsigned long long* h_cfl = nullptr; // pinned
+    double* d_dt = nullptr;              // the step's first dt, set on the device (k_dt)
+    double* h_dt = nullptr;              // pinned
+    int* h_mf = nullptr;                 // pinned: M-operator refine flag read back
+    int* h_act = nullptr;                // pinned: edge-band flags read back
+    int h_act_cap = 0;
     double* d_srcHn = nullptr;           // depth/density the sources set (valid until the first step)
     double* d_srcRho = nullptr;
     bool src_override = false;
@@ -684,12 +690,17 @@ void refresh_topo32(kg_ctx& c, int ts) {
 }
 
 constexpr unsigned long long HUGE_BITS = 0x7FEFFFFFFFFFFFFFull;  // bits of huge(1.0_wp)
+// CFL words of the context: the three RK stages of a hydraulic step, and the RHS pass that
+// sets or checks dt.
+enum { W_S1 = 0, W_S2 = 1, W_S3 = 2, W_RHS = 3 };
+
+int partial(const kg_ctx& c) { return (int)c.active.size() < c.nTiles ? 1 : 0; }
 
 // Queue one fused pass that reduces its CFL terms into word `word` of the context's CFL
 // array; nothing waits for it.
 void launch_pass(kg_ctx& c, StepArgs& S, int word) {
     S.cfl_min = c.d_cfl + word;
-    S.partial = (int)c.active.size() < c.nTiles ? 1 : 0;
+    S.partial = partial(c);
     const bool fp32 = c.prec == KG_PREC_FP32;
     if (fp32 && c.tdirty[S.topo]) refresh_topo32(c, S.topo);
     if (c.timing) CK(cudaEventRecord(c.ev0[word], c.st));
@@ -698,33 +709,31 @@ void launch_pass(kg_ctx& c, StepArgs& S, int word) {
     if (c.timing) CK(cudaEventRecord(c.ev1[word], c.st));
     c.launches++;
 }
-void reset_cfl(kg_ctx& c, int n) {
-    for (int k = 0; k < n; ++k) c.h_cfl[k] = HUGE_BITS;
-    CK(cudaMemcpyAsync(c.d_cfl, c.h_cfl, (size_t)n * sizeof(unsigned long long), cudaMemcpyHostToDevice, c.st));
+void reset_cfl(kg_ctx& c, int first, int n) {
+    for (int k = first; k < first + n; ++k) c.h_cfl[k] = HUGE_BITS;
+    CK(cudaMemcpyAsync(c.d_cfl + first, c.h_cfl + first, (size_t)n * sizeof(unsigned long long), cudaMemcpyHostToDevice, c.st));
 }
-// Read back the first n CFL words (one wait for the whole queue).
-void collect_cfl(kg_ctx& c, int n) {
-    CK(cudaMemcpyAsync(c.h_cfl, c.d_cfl, (size_t)n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
+// Read back the CFL words (and whatever else was queued for reading) with one wait.
+void collect_cfl(kg_ctx& c) {
+    CK(cudaMemcpyAsync(c.h_cfl, c.d_cfl, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
     sync(c);
 }
-// Accumulate the event timing of the first n passes of the last queue (those that ran).
-void account_passes(kg_ctx& c, int n) {
+// Accumulate the event timing of one pass of the last queue (one that ran).
+void account_pass(kg_ctx& c, int word) {
     if (!c.timing) return;
-    for (int k = 0; k < n; ++k) {
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, c.ev0[k], c.ev1[k]));
-        c.kernel_ms += ms;
-        c.timed_passes++;
-    }
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c.ev0[word], c.ev1[word]));
+    c.kernel_ms += ms;
+    c.timed_passes++;
 }
 
 unsigned long long run_pass(kg_ctx& c, StepArgs S) {
-    reset_cfl(c, 1);
+    reset_cfl(c, W_RHS, 1);
     S.ngate = 0;
-    launch_pass(c, S, 0);
-    collect_cfl(c, 1);
-    account_passes(c, 1);
-    return c.h_cfl[0];
+    launch_pass(c, S, W_RHS);
+    collect_cfl(c);
+    account_pass(c, W_RHS);
+    return c.h_cfl[W_RHS];
 }
 
 double next_flux_time(const kg_ctx& c, double t) {  // NextFluxSeriesTime, src/TimeStepper.f90:281-305
@@ -737,51 +746,81 @@ double next_flux_time(const kg_ctx& c, double t) {  // NextFluxSeriesTime, src/T
     return nextT;
 }
 
-// HydraulicTimeStepper on the device; returns true when dt had to be refined.  The three
-// stages are queued back to back: stage 2 runs only if stage 1's advised dt accepts dt and
-// stage 3 only if both do (the same test the host applies afterwards to the CFL words), so
-// one wait serves the whole step and a refined attempt leaves no output behind.
-bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int e_set, int topo, int q_s1, int q_s2, int q_out) {
+// Queue HydraulicTimeStepper's three stages back to back.  Stage 2 runs only if stage 1's
+// advised dt accepts dt and stage 3 only if both do (the test the host applies afterwards
+// to the CFL words), so one wait serves the whole step and a refined attempt leaves no
+// output behind.  dt comes from the host, or from the device (dtp: the step's first
+// attempt, see k_dt).  gflag / gs1 close all three stages: a refine flag that is set, and
+// the CFL word of an RHS check whose substep-1 advised dt is below dt.  flags_after queues
+// the edge-band flags of the result for the next CheckIfNearBoundaries.
+void queue_hydraulic(kg_ctx& c, double dt, const double* dtp, int q_in, int e_set, int topo, int q_s1, int q_s2, int q_out,
+                     const int* gflag, const unsigned long long* gs1, bool flags_after) {
     double nextT = c.t + dt;
-    c.dt = dt;
     StepArgs S{};
     S.q_in = q_in; S.q_s1 = q_s1; S.q_s2 = q_s2; S.q_out = q_out; S.e_set = e_set; S.topo = topo;
     S.q_tc = c.qcur; S.topo_tc = c.tcur;
-    S.dt = dt; S.t_grid = c.t; S.do_maxima = 1;
-    reset_cfl(c, 3);
-    S.mode = MODE_S1; S.t_rhs = nextT; S.ngate = 0;
-    launch_pass(c, S, 0);
-    S.mode = MODE_S2; S.t_rhs = c.t + 0.5 * dt; S.gate[0] = c.d_cfl; S.ngate = 1;
-    launch_pass(c, S, 1);
-    S.mode = MODE_S3; S.t_rhs = nextT; S.t_max = nextT; S.gate[1] = c.d_cfl + 1; S.ngate = 2;
-    launch_pass(c, S, 2);
-    // Edge-band flags of the candidate result for the next step's CheckIfNearBoundaries.
-    std::vector<int> slots;
-    for (int id : c.active) slots.push_back(T(c, id).slot);
-    upload_list(c, slots);
-    CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), q_out, topo, nullptr, c.d_flags, c.nX, c.nY, c.st));
-    c.launches++;
-    c.act_tmp.resize(slots.size());
-    CK(cudaMemcpyAsync(c.act_tmp.data(), c.d_flags, slots.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
-    collect_cfl(c, 3);
-    double dt1 = advised(c, c.h_cfl[0], 2);
-    if (dt1 < dt) { account_passes(c, 1); dt = 0.9 * dt1; return true; }
-    double dt2 = advised(c, c.h_cfl[1], 3);
-    if (dt2 < dt) { account_passes(c, 2); dt = 0.9 * dt2; return true; }
-    account_passes(c, 3);
-    c.act_flags.swap(c.act_tmp);
-    c.act_q = q_out;
-    c.act_t = topo;
-    c.act_gen = c.gen;
+    S.dt = dt; S.dtp = dtp; S.t_grid = c.t; S.do_maxima = 1;
+    S.gate_flag = gflag;
+    int g0 = 0;
+    if (gs1) { S.gate[0] = gs1; S.gate_s1[0] = 1; g0 = 1; }
+    reset_cfl(c, W_S1, 3);
+    S.mode = MODE_S1; S.t_rhs = nextT; S.tmode = 1; S.ngate = g0;
+    launch_pass(c, S, W_S1);
+    S.mode = MODE_S2; S.t_rhs = c.t + 0.5 * dt; S.tmode = 2;
+    S.gate[g0] = c.d_cfl + W_S1; S.gate_s1[g0] = 0; S.ngate = g0 + 1;
+    launch_pass(c, S, W_S2);
+    S.mode = MODE_S3; S.t_rhs = nextT; S.t_max = nextT; S.tmode = 1;
+    S.gate[g0 + 1] = c.d_cfl + W_S2; S.gate_s1[g0 + 1] = 0; S.ngate = g0 + 2;
+    launch_pass(c, S, W_S3);
+    if (flags_after) {
+        std::vector<int> slots;
+        for (int id : c.active) slots.push_back(T(c, id).slot);
+        upload_list(c, slots);
+        CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), q_out, topo, nullptr, c.d_flags, c.nX, c.nY, c.st));
+        c.launches++;
+        if ((int)slots.size() > c.h_act_cap) {
+            if (c.h_act) CK(cudaFreeHost(c.h_act));
+            c.h_act_cap = std::max<int>((int)slots.size(), 2 * c.h_act_cap);
+            CK(cudaMallocHost(&c.h_act, (size_t)c.h_act_cap * sizeof(int)));
+        }
+        CK(cudaMemcpyAsync(c.h_act, c.d_flags, slots.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    }
+}
+
+// The host's refinement tests of HydraulicTimeStepper (src/TimeStepper.f90:393-404,
+// :452-463) on the stage CFL words after the wait; true (and the refined dt) on rejection.
+bool finish_hydraulic(kg_ctx& c, double& dt, int q_out, int topo, bool flags_after) {
+    double dt1 = advised(c, c.h_cfl[W_S1], 2);
+    if (dt1 < dt) { account_pass(c, W_S1); dt = 0.9 * dt1; return true; }
+    double dt2 = advised(c, c.h_cfl[W_S2], 3);
+    if (dt2 < dt) { account_pass(c, W_S1); account_pass(c, W_S2); dt = 0.9 * dt2; return true; }
+    account_pass(c, W_S1); account_pass(c, W_S2); account_pass(c, W_S3);
+    if (flags_after) {
+        c.act_flags.assign(c.h_act, c.h_act + c.active.size());
+        c.act_q = q_out;
+        c.act_t = topo;
+        c.act_gen = c.gen;
+    }
     return false;
 }
 
+// HydraulicTimeStepper with a host dt; returns true when dt had to be refined.
+bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int e_set, int topo, int q_s1, int q_s2, int q_out, bool flags_after) {
+    c.dt = dt;
+    queue_hydraulic(c, dt, nullptr, q_in, e_set, topo, q_s1, q_s2, q_out, nullptr, nullptr, flags_after);
+    collect_cfl(c);
+    return finish_hydraulic(c, dt, q_out, topo, flags_after);
+}
+
 // CalculateHydraulicRHS at substep 1 on state q_in / topography topo into E/I set e_set.
-double rhs0(kg_ctx& c, int q_in, int e_set, int topo, double t, int substep = 1) {
+StepArgs rhs_args(const kg_ctx& c, int q_in, int e_set, int topo, double t) {
     StepArgs S{};
     S.mode = MODE_RHS0; S.q_in = q_in; S.e_set = e_set; S.topo = topo; S.t_rhs = t; S.t_grid = c.t;
     S.q_tc = c.qcur; S.topo_tc = c.tcur;
-    return advised(c, run_pass(c, S), substep);
+    return S;
+}
+double rhs0(kg_ctx& c, int q_in, int e_set, int topo, double t, int substep = 1) {
+    return advised(c, run_pass(c, rhs_args(c, q_in, e_set, topo, t)), substep);
 }
 
 // Dependency waves of the ordered redistribution list (see k_m_redist): candidate q goes
@@ -845,17 +884,25 @@ void redistribution_waves(kg_ctx& c, const std::vector<int>& slots, const std::v
     }
 }
 
-// MorphodynamicTimeStepper (src/TimeStepper.f90:532-781) on state qa (the first hydraulic
-// step's result); builds the new bed in set tnew.  Returns true when dt must be refined.
-bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
+// The Strang remainder M(2 dt) H(dt) of a step whose first H(dt) was accepted
+// (src/TimeStepper.f90:193-270): MorphodynamicTimeStepper (:532-781) on o[0], building the
+// new bed in set tnew, then the RHS check of the M result at t0 + dt and the second
+// HydraulicTimeStepper into o[1].  Waits: after the M checks (plus one to read the
+// redistribution list when there is one) and one at the end; the RHS check and the
+// second H are gated on the device by the redistribution's refine flag and the check's
+// advised dt.  Returns 0 accepted, 1 M refined, 2 the check cut dt, 3 H refined; dt is
+// updated as the reference updates it.
+int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
+    const int qa = o[0];
+    double dt_m = 2.0 * dt;
     std::vector<int> slots;
     for (int id : c.active) slots.push_back(T(c, id).slot);
     int n = (int)slots.size();
     upload_list(c, slots);
+    const bool fp32 = c.prec == KG_PREC_FP32;
     CK(launch_m_init(c.A, c.d_list, n, c.SV, qa, c.tcur, tnew, c.st));
     c.launches++;
     for (int stage = 1; stage <= 3; ++stage) {
-        const bool fp32 = c.prec == KG_PREC_FP32;
         CK(launch_m_emd(c.A, c.d_list, n, c.SC, tnew, fp32, c.st));
         CK(launch_m_bt(c.A, c.d_list, n, c.SV, c.tcur, tnew, stage, dt_m, fp32, c.st));
         CK(launch_m_cells(c.A, c.d_list, n, c.SC, qa, c.tcur, tnew, fp32, c.st));
@@ -883,9 +930,13 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
     CK(cudaMemcpyAsync(&hf[0], c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
     CK(cudaMemcpyAsync(&hf[1], c.d_ncand, sizeof(int), cudaMemcpyDeviceToHost, c.st));
     sync(c);
-    bool refine = hf[0] != 0;
     int ncand = hf[1];
-    if (!refine && ncand > 0) {
+    if (hf[0] != 0) {
+        dt_m = 0.5 * dt_m;
+        dt = 0.5 * dt_m;
+        return 1;
+    }
+    if (ncand > 0) {
         // AddToRedistList keeps the cells ordered by excess deposition, ties in loop order
         // (src/Redistribute.f90:69-101); RedistributeGrid then walks that list.
         std::vector<unsigned long long> key((size_t)ncand);
@@ -910,26 +961,47 @@ bool morpho_stepper(kg_ctx& c, double& dt_m, int qa, int tnew) {
         CK(cudaMemcpyAsync(c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, c.d_rwave, nw, qa, c.tcur, tnew, c.d_mflags, c.st));
         c.launches++;
-        CK(cudaMemcpyAsync(&hf[0], c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
-        sync(c);
-        refine = hf[0] != 0;
     }
-    if (refine) {
-        dt_m = 0.5 * dt_m;
-        return true;
-    }
+    // Interfacial topography of the new bed and the M result (both scratch until accepted).
     upload_list(c, slots);
-    CK(launch_face_topo(c.A, c.d_list, n, tnew, c.nX, c.nY, c.prec == KG_PREC_FP32, c.st));
+    CK(launch_face_topo(c.A, c.d_list, n, tnew, c.nX, c.nY, fp32, c.st));
     CK(launch_face_bI(c.A, c.d_list, n, tnew, c.nX, c.nY, c.st));
     CK(launch_m_finish(c.A, c.d_list, n, c.SC, qa, c.st));
     c.launches += 3;
     c.tdirty[tnew] = std::max(c.tdirty[tnew], 1);
-    return false;
+    // RHS check at t0 + dt, then H(dt) from the M result, gated by both tests.
+    c.t = c.t0 + dt;
+    StepArgs R = rhs_args(c, o[0], 1, tnew, c.t);
+    reset_cfl(c, W_RHS, 1);
+    R.ngate = 0;
+    launch_pass(c, R, W_RHS);
+    c.dt = dt;
+    queue_hydraulic(c, dt, nullptr, o[0], 1, tnew, o[1], o[2], o[1], c.d_mflags, c.d_cfl + W_RHS, true);
+    CK(cudaMemcpyAsync(c.h_mf, c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    collect_cfl(c);
+    if (*c.h_mf != 0) {
+        c.t = c.t0;
+        dt_m = 0.5 * dt_m;
+        dt = 0.5 * dt_m;
+        return 1;
+    }
+    account_pass(c, W_RHS);
+    double adv = advised(c, c.h_cfl[W_RHS], 1);
+    if (adv < dt) {
+        if ((dt - adv) / dt < 0.1) dt = 0.9 * dt;
+        else dt = adv;
+        c.t = c.t0;
+        return 2;
+    }
+    if (!finish_hydraulic(c, dt, o[1], tnew, true)) return 0;
+    c.t = c.t0;
+    return 3;
 }
 
 // One accepted step of IntegrateTo (src/TimeStepper.f90:151-275): H(dt) alone, or the
 // Strang split H(dt) M(2 dt) H(dt) with morphodynamics, retried from the step-start state
-// until every part accepts its dt.
+// until every part accepts its dt.  The RHS at t, the step's dt (k_dt, on the device) and
+// the first attempt of H(dt) are queued together behind one wait.
 void integrate_step(kg_ctx& c, double tend) {
     if (!c.sources_loaded) throw KgError(KG_ERR_STATE, "kg_load_sources must be called before stepping");
     check_near_boundaries(c);
@@ -939,38 +1011,40 @@ void integrate_step(kg_ctx& c, double tend) {
     for (int b = 0; b < 4; ++b)
         if (b != c.qcur) o[k++] = b;
     int tnew = 1 - c.tcur;
-    double adv = rhs0(c, c.qcur, 0, c.tcur, c.t);
     double tmax = mn(tend, next_flux_time(c, c.t));
-    if (!morpho) adv = mn(adv, tmax - c.t);
-    else adv = mn(adv, 0.5 * (tmax - c.t));
+    double cap = morpho ? 0.5 * (tmax - c.t) : tmax - c.t;
+    c.t0 = c.t;
+    StepArgs R = rhs_args(c, c.qcur, 0, c.tcur, c.t);
+    reset_cfl(c, W_RHS, 1);
+    launch_pass(c, R, W_RHS);
+    CK(launch_dt(c.d_cfl + W_RHS, partial(c), cap, c.d_dt, c.st));
+    c.launches++;
+    queue_hydraulic(c, 0.0, c.d_dt, c.qcur, 0, c.tcur, o[0], o[1], o[0], nullptr, nullptr, !morpho);
+    CK(cudaMemcpyAsync(c.h_dt, c.d_dt, sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    collect_cfl(c);
+    account_pass(c, W_RHS);
+    double adv = mn(advised(c, c.h_cfl[W_RHS], 1), cap);
+    if (!(adv == *c.h_dt) && !(adv != adv && *c.h_dt != *c.h_dt))
+        throw KgError(KG_ERR_CUDA, "device-side dt differs from the host's");
     c.dt = adv;
     double dt = adv;
-    c.t0 = c.t;
+    bool first = true;
     int guard = 0, newcur = -1;
     while (true) {
         if (++guard > 100000 || !(dt > 0.0)) throw KgError(KG_ERR_DT, "time step collapsed");
-        if (hydraulic_stepper(c, dt, c.qcur, 0, c.tcur, o[0], o[1], o[0])) { c.rejected++; continue; }
+        bool rej;
+        if (first) {
+            rej = finish_hydraulic(c, dt, o[0], c.tcur, !morpho);
+            first = false;
+        } else {
+            rej = hydraulic_stepper(c, dt, c.qcur, 0, c.tcur, o[0], o[1], o[0], !morpho);
+        }
+        if (rej) { c.rejected++; continue; }
         if (!morpho) { newcur = o[0]; break; }
-        double dt_m = 2.0 * dt;
-        if (morpho_stepper(c, dt_m, o[0], tnew)) {
-            c.rejected++;
-            dt = 0.5 * dt_m;
-            c.dt = dt;
-            continue;
-        }
-        c.t = c.t0 + dt;
-        adv = rhs0(c, o[0], 1, tnew, c.t);
-        if (adv < dt) {
-            if ((dt - adv) / dt < 0.1) dt = 0.9 * dt;
-            else dt = adv;
-            c.dt = dt;
-            c.t = c.t0;
-            c.rejected++;
-            continue;
-        }
-        if (!hydraulic_stepper(c, dt, o[0], 1, tnew, o[1], o[2], o[1])) { newcur = o[1]; break; }
-        c.t = c.t0;
+        int r = morpho_and_h2(c, dt, o, tnew);
+        if (r == 0) { newcur = o[1]; break; }
         c.rejected++;
+        c.dt = dt;
     }
     c.qcur = newcur;
     if (morpho) c.tcur = tnew;
@@ -1238,6 +1312,9 @@ void setup(kg_ctx& c, const kg_params& p) {
     CK(cudaMalloc(&c.d_cfl, 4 * sizeof(unsigned long long)));
     CK(cudaMalloc(&c.d_vol, 4 * sizeof(double)));
     CK(cudaMallocHost(&c.h_cfl, 4 * sizeof(unsigned long long)));
+    CK(cudaMalloc(&c.d_dt, sizeof(double)));
+    CK(cudaMallocHost(&c.h_dt, sizeof(double)));
+    CK(cudaMallocHost(&c.h_mf, sizeof(int)));
     CK(set_constants(c.dp, nullptr, 0, c.st));
     sync(c);
 }
@@ -1257,6 +1334,10 @@ void free_ctx(kg_ctx* c) {
                     c->d_rslot, c->d_rcell, c->d_rwave};
     for (void* q : ptrs) cudaFree(q);
     if (c->h_cfl) cudaFreeHost(c->h_cfl);
+    if (c->h_dt) cudaFreeHost(c->h_dt);
+    if (c->h_mf) cudaFreeHost(c->h_mf);
+    if (c->h_act) cudaFreeHost(c->h_act);
+    cudaFree(c->d_dt);
     for (int k = 0; k < 4; ++k) {
         if (c->ev0[k]) cudaEventDestroy(c->ev0[k]);
         if (c->ev1[k]) cudaEventDestroy(c->ev1[k]);

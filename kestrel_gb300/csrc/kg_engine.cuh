@@ -88,11 +88,20 @@ struct StepArgs {
     double t_max;    // nextT stamped into the maxima (S3)
     int do_maxima;
     unsigned long long* cfl_min;  // ordered-bits min of the tile CFL terms
-    // Stage gate: the CFL words of the earlier stages of this hydraulic step.  The pass does
-    // nothing when one of them advises a dt below `dt` (the host then refines dt), so the
-    // three stages can be queued without waiting for the host's test in between.
-    const unsigned long long* gate[2];
+    // dt from the device: when dtp is set the pass reads dt there (the advised dt of the
+    // step's first RHS evaluation, written by k_dt) and derives t_rhs / t_max from t_grid
+    // exactly as the host would (tmode 1: t_rhs = t_grid + dt, 2: t_grid + 0.5 dt;
+    // t_max = t_grid + dt).
+    const double* dtp;
+    int tmode;
+    // Stage gate: the pass does nothing when one of these says dt must be refined, so the
+    // stages of a step can be queued without waiting for the host's tests in between:
+    // gate[g] is a CFL word whose advised dt (with the substep-1 factor 0.9 when
+    // gate_s1[g]) falls below dt; gate_flag is a refine flag that is set.
+    const unsigned long long* gate[3];
+    int gate_s1[3];
     int ngate;
+    const int* gate_flag;
     int partial;     // fewer active tiles than tiles: the advised dt is capped by maxdt
 };
 

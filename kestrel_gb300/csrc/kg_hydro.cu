@@ -254,25 +254,52 @@ __device__ __forceinline__ void face_flux(const DevParams& P, bool xdir, const S
     out[6] = 0.5 * (dP2 + dM2);
 }
 
-// The host's advised-dt test (ComputeAdvisedTimeStep, src/HydraulicRHS.f90:141-174, for
-// substeps 2 and 3; refinement at src/TimeStepper.f90:393-404 and :452-463) on the CFL words
-// of the earlier stages of this step, with the host's operation order.  False when one of
-// them would have refined dt: the pass then leaves every output untouched.
-__device__ __forceinline__ bool stage_gate_open(const StepArgs& S) {
+// ComputeAdvisedTimeStep (src/HydraulicRHS.f90:141-174) before the substep-1 factor, with
+// the host's operation order.
+__device__ __forceinline__ double advised_m(unsigned long long bits, int partial) {
     const DevParams& P = cP;
+    double umin = __longlong_as_double((long long)bits);
+    if (partial) umin = mn(umin, P.maxdt);
+    double m = mn(P.cfl * umin, P.diffusiveTimeScale);
+    return mn(m, P.maxdt);
+}
+
+// Resolve a device-held dt into the pass arguments, then apply the stage gate: false when
+// an earlier test of this step would have refined dt (TimeStepper.f90:393-404, :452-463
+// and the 10% test of :235-248), so the pass leaves every output untouched.
+__device__ __forceinline__ bool stage_gate_open(StepArgs& S) {
+    if (S.dtp) {
+        S.dt = *(volatile const double*)S.dtp;
+        if (S.tmode == 1) S.t_rhs = S.t_grid + S.dt;
+        else if (S.tmode == 2) S.t_rhs = S.t_grid + 0.5 * S.dt;
+        S.t_max = S.t_grid + S.dt;
+    }
+    if (S.gate_flag && *(volatile const int*)S.gate_flag != 0) return false;
     for (int g = 0; g < S.ngate; ++g) {
-        unsigned long long bits = *(volatile const unsigned long long*)S.gate[g];
-        double umin = __longlong_as_double((long long)bits);
-        if (S.partial) umin = mn(umin, P.maxdt);
-        double m = mn(P.cfl * umin, P.diffusiveTimeScale);
-        m = mn(m, P.maxdt);
+        double m = advised_m(*(volatile const unsigned long long*)S.gate[g], S.partial);
+        if (S.gate_s1[g]) m = 0.9 * m;
         if (m < S.dt) return false;
     }
     return true;
 }
 
+// The first dt of a step on the device: IntegrateTo's min(advised dt of the RHS at t,
+// the distance to the next flux knot) (src/TimeStepper.f90:151-183), from the CFL word of
+// the RHS pass; cap is the host's (tmax - t) or (tmax - t)/2.
+__global__ void k_dt(const unsigned long long* __restrict__ cfl, int partial, double cap, double* dtp) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double adv = 0.9 * advised_m(*cfl, partial);
+        *dtp = mn(adv, cap);
+    }
+}
+
+cudaError_t launch_dt(const unsigned long long* cfl, int partial, double cap, double* dtp, cudaStream_t st) {
+    k_dt<<<1, 32, 0, st>>>(cfl, partial, cap, dtp);
+    return cudaGetLastError();
+}
+
 __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __restrict__ blocks, StepArgs S) {
-    if (S.ngate > 0 && !stage_gate_open(S)) return;
+    if (!stage_gate_open(S)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     HydroSmem& sm = *reinterpret_cast<HydroSmem*>(smraw);
     const DevParams& P = cP;

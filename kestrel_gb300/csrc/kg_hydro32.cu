@@ -109,7 +109,7 @@ __device__ __forceinline__ float side_hp(float dlo, float dhi, float s, bool upp
 }
 
 __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __restrict__ blocks, StepArgs S) {
-    if (S.ngate > 0 && !stage_gate_open(S)) return;
+    if (!stage_gate_open(S)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
     const DevParams& P = cP;
