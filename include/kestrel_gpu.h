@@ -221,6 +221,10 @@ int  kg_get_kernel_time(kg_ctx* ctx, double* ms, int64_t* passes);
    of listed cells walked, the dependency waves they were run in and the walks.  No
    reference counterpart (the reference walks its list serially). */
 int  kg_redistribution_stats(kg_ctx* ctx, int64_t* cells, int64_t* waves, int64_t* walks);
+/* Host wall time in seconds since creation: out[0] inside kg_step/kg_integrate_to steps,
+   out[1] of that blocked in stream synchronisations (the host waiting for the GPU),
+   out[2] planning redistribution walks.  No reference counterpart. */
+int  kg_host_times(kg_ctx* ctx, double out[3]);
 
 /* Same as kg_hydraulic_rhs (substep 1..4, advised dt, ddtExplicit/ddtImplicit readable
    with kg_get_tile_rhs) but allocates nothing: for hosts that own all device memory and do

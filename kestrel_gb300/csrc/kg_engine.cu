@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -150,6 +151,9 @@ struct kg_ctx {
     double t = 0.0, dt = 1.0e-5, t0 = 0.0;
     int64_t launches = 0, steps = 0, rejected = 0, cell_updates = 0;
     int64_t redist_cells = 0, redist_waves = 0, redist_walks = 0;
+    // Host wall time (s): whole steps, waiting in stream synchronisations, planning the
+    // redistribution walk (read-back of the list excluded).
+    double host_step_s = 0.0, host_wait_s = 0.0, host_plan_s = 0.0;
     bool blocks_dirty = true;
     bool timing = false;
     cudaEvent_t ev0[4] = {nullptr, nullptr, nullptr, nullptr}, ev1[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -237,7 +241,12 @@ void upload_list(kg_ctx& c, const std::vector<int>& slots) {
         CK(cudaMemcpyAsync(c.d_list, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
 }
 
-void sync(kg_ctx& c) { CK(cudaStreamSynchronize(c.st)); }
+double wall() { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); }
+void sync(kg_ctx& c) {
+    double t0 = wall();
+    CK(cudaStreamSynchronize(c.st));
+    c.host_wait_s += wall() - t0;
+}
 
 // ---------------------------------------------------------------- grid navigation
 // src/Grid.f90:245-353
@@ -944,6 +953,7 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         CK(cudaMemcpyAsync(key.data(), c.d_ckey, (size_t)ncand * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
         CK(cudaMemcpyAsync(ex.data(), c.d_cex, (size_t)ncand * sizeof(double), cudaMemcpyDeviceToHost, c.st));
         sync(c);
+        double tp0 = wall();
         std::vector<int> ord((size_t)ncand);
         for (int q = 0; q < ncand; ++q) ord[(size_t)q] = q;
         std::sort(ord.begin(), ord.end(), [&](int a, int b) {
@@ -956,6 +966,7 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         c.redist_cells += ncand;
         c.redist_waves += nw;
         c.redist_walks++;
+        c.host_plan_s += wall() - tp0;
         CK(cudaMemcpyAsync(c.d_rslot, ls.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
@@ -1002,7 +1013,13 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
 // Strang split H(dt) M(2 dt) H(dt) with morphodynamics, retried from the step-start state
 // until every part accepts its dt.  The RHS at t, the step's dt (k_dt, on the device) and
 // the first attempt of H(dt) are queued together behind one wait.
+void integrate_step_body(kg_ctx& c, double tend);
 void integrate_step(kg_ctx& c, double tend) {
+    double t0 = wall();
+    integrate_step_body(c, tend);
+    c.host_step_s += wall() - t0;
+}
+void integrate_step_body(kg_ctx& c, double tend) {
     if (!c.sources_loaded) throw KgError(KG_ERR_STATE, "kg_load_sources must be called before stepping");
     check_near_boundaries(c);
     rebuild_blocks(c);
@@ -1614,6 +1631,14 @@ int kg_get_time(kg_ctx* c, double* t, double* dt) {
 }
 
 int64_t kg_kernel_launches(const kg_ctx* c) { return c ? c->launches : 0; }
+
+int kg_host_times(kg_ctx* c, double out[3]) {
+    if (!c || !out) return KG_ERR_PARAM;
+    out[0] = c->host_step_s;
+    out[1] = c->host_wait_s;
+    out[2] = c->host_plan_s;
+    return KG_OK;
+}
 
 int kg_redistribution_stats(kg_ctx* c, int64_t* cells, int64_t* waves, int64_t* walks) {
     if (!c || !cells || !waves || !walks) return KG_ERR_PARAM;
