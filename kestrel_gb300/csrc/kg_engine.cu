@@ -46,7 +46,8 @@ cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int 
 cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
                           double* d_out, cudaStream_t st);
 // kg_morpho.cu
-cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, cudaStream_t st);
+cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, int* ctl_flags,
+                          cudaStream_t st);
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st);
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
                         bool fp32, cudaStream_t st);
@@ -113,13 +114,24 @@ struct kg_ctx {
     int* d_list = nullptr;               // scratch slot list
     int d_list_cap = 0;
     int* d_flags = nullptr;
-    unsigned long long* d_cfl = nullptr;
+    int d_flags_cap = 0;
+    // Control words the kernels write and the host reads back with one copy per wait:
+    // CFL words, the device-chosen dt, the M refine flag and the candidate count.
+    struct Ctl {
+        unsigned long long cfl[4];
+        double dt;
+        int mflag, ncand;
+    };
+    Ctl* d_ctl = nullptr;
+    Ctl* h_ctl = nullptr;                // pinned
+    unsigned long long* d_cfl = nullptr; // = d_ctl->cfl
+    int* d_active = nullptr;             // active slots then ghost slots, list order (device copy)
+    int d_active_cap = 0;
+    int n_active_dev = -1, n_ghost_dev = 0;
     double* d_vol = nullptr;
-    unsigned long long* h_cfl = nullptr; // pinned
-    double* d_dt = nullptr;              // the step's first dt, set on the device (k_dt)
-    double* h_dt = nullptr;              // pinned
-    int* h_mf = nullptr;                 // pinned: M-operator refine flag read back
-    int* h_act = nullptr;                // pinned: edge-band flags read back
+    unsigned long long* h_cfl = nullptr; // = h_ctl->cfl
+    double* d_dt = nullptr;              // = &d_ctl->dt
+    int* h_act = nullptr;                // pinned: edge-band flags read back (per tile chunk)
     int h_act_cap = 0;
     double* d_srcHn = nullptr;           // depth/density the sources set (valid until the first step)
     double* d_srcRho = nullptr;
@@ -139,8 +151,8 @@ struct kg_ctx {
     int* d_tlist = nullptr;              // slot list of the cache rebuild
     int d_tlist_cap = 0;
     std::vector<int> touched;            // slots whose step-start topography changed in set-up
-    int* d_mflags = nullptr;             // M-operator refine flag
-    int* d_ncand = nullptr;
+    int* d_mflags = nullptr;             // = &d_ctl->mflag
+    int* d_ncand = nullptr;              // = &d_ctl->ncand
     unsigned long long* d_ckey = nullptr;
     double* d_cex = nullptr;
     int* d_rslot = nullptr;
@@ -229,9 +241,7 @@ void ensure_list(kg_ctx& c, size_t n) {
     if ((int)n <= c.d_list_cap) return;
     int nc = std::max<int>((int)n, std::max(64, c.d_list_cap * 2));
     if (c.d_list) CK(cudaFree(c.d_list));
-    if (c.d_flags) CK(cudaFree(c.d_flags));
     CK(cudaMalloc(&c.d_list, nc * sizeof(int)));
-    CK(cudaMalloc(&c.d_flags, nc * sizeof(int)));
     c.d_list_cap = nc;
 }
 
@@ -242,6 +252,14 @@ void upload_list(kg_ctx& c, const std::vector<int>& slots) {
 }
 
 double wall() { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); }
+// Edge-band flags are written per (tile, 256-cell chunk).
+void ensure_flags(kg_ctx& c, size_t ntiles) {
+    size_t need = ntiles * (size_t)((c.SC + 255) / 256);
+    if ((int)need <= c.d_flags_cap) return;
+    if (c.d_flags) CK(cudaFree(c.d_flags));
+    c.d_flags_cap = std::max<int>((int)need, 2 * c.d_flags_cap);
+    CK(cudaMalloc(&c.d_flags, (size_t)c.d_flags_cap * sizeof(int)));
+}
 void sync(kg_ctx& c) {
     double t0 = wall();
     CK(cudaStreamSynchronize(c.st));
@@ -610,6 +628,18 @@ void add_tile(kg_ctx& c, int k) {
 void rebuild_blocks(kg_ctx& c) {
     if (!c.blocks_dirty) return;
     refresh_all_nbrs(c);
+    // Device copy of the slot lists: active tiles in list order, then the ghost tiles.
+    std::vector<int> all;
+    for (int id : c.active) all.push_back(T(c, id).slot);
+    for (int id : c.ghost) all.push_back(T(c, id).slot);
+    if ((int)all.size() > c.d_active_cap) {
+        if (c.d_active) CK(cudaFree(c.d_active));
+        c.d_active_cap = std::max<int>((int)all.size(), 2 * c.d_active_cap);
+        CK(cudaMalloc(&c.d_active, (size_t)c.d_active_cap * sizeof(int)));
+    }
+    if (!all.empty()) CK(cudaMemcpyAsync(c.d_active, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+    c.n_active_dev = (int)c.active.size();
+    c.n_ghost_dev = (int)c.ghost.size();
     c.blocks.clear();
     const int BSZ = 16;
     for (int id : c.active) {
@@ -640,11 +670,16 @@ void check_near_boundaries(kg_ctx& c) {
         fl = c.act_flags;
     } else {
         upload_list(c, slots);
+        ensure_flags(c, slots.size());
         CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), c.qcur, c.tcur, c.src_override ? c.d_srcHn : nullptr, c.d_flags, c.nX, c.nY, c.st));
         c.launches++;
-        fl.resize(slots.size());
-        CK(cudaMemcpyAsync(fl.data(), c.d_flags, fl.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        int per = (c.SC + 255) / 256;
+        std::vector<int> chunks(slots.size() * per);
+        CK(cudaMemcpyAsync(chunks.data(), c.d_flags, chunks.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
         sync(c);
+        fl.assign(slots.size(), 0);
+        for (size_t q = 0; q < slots.size(); ++q)
+            for (int k = 0; k < per; ++k) fl[q] |= chunks[q * per + k];
     }
     c.act_q = -1;
     std::vector<int> flag_of((size_t)c.nTiles + 1, -1);
@@ -681,6 +716,15 @@ double advised(kg_ctx& c, unsigned long long bits, int substep) {
 
 // FP32 form: rebuild the factor cache of topography set ts for every allocated tile.
 void refresh_topo32(kg_ctx& c, int ts) {
+    if (c.n_active_dev == (int)c.active.size() && c.n_ghost_dev == (int)c.ghost.size() && !c.blocks_dirty) {
+        int n = c.n_active_dev + (c.tdirty[ts] > 1 ? c.n_ghost_dev : 0);
+        if (n > 0) {
+            CK(launch_topo32(c.A, c.d_active, n, ts, c.nX, c.nY, c.st));
+            c.launches++;
+        }
+        c.tdirty[ts] = 0;
+        return;
+    }
     std::vector<int> slots;
     for (int id : c.active) slots.push_back(T(c, id).slot);
     if (c.tdirty[ts] > 1)
@@ -724,7 +768,7 @@ void reset_cfl(kg_ctx& c, int first, int n) {
 }
 // Read back the CFL words (and whatever else was queued for reading) with one wait.
 void collect_cfl(kg_ctx& c) {
-    CK(cudaMemcpyAsync(c.h_cfl, c.d_cfl, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
+    CK(cudaMemcpyAsync(c.h_ctl, c.d_ctl, sizeof(kg_ctx::Ctl), cudaMemcpyDeviceToHost, c.st));
     sync(c);
 }
 // Accumulate the event timing of one pass of the last queue (one that ran).
@@ -782,17 +826,16 @@ void queue_hydraulic(kg_ctx& c, double dt, const double* dtp, int q_in, int e_se
     S.gate[g0 + 1] = c.d_cfl + W_S2; S.gate_s1[g0 + 1] = 0; S.ngate = g0 + 2;
     launch_pass(c, S, W_S3);
     if (flags_after) {
-        std::vector<int> slots;
-        for (int id : c.active) slots.push_back(T(c, id).slot);
-        upload_list(c, slots);
-        CK(launch_act_flags(c.A, c.d_list, (int)slots.size(), q_out, topo, nullptr, c.d_flags, c.nX, c.nY, c.st));
+        int n = (int)c.active.size(), per = (c.SC + 255) / 256;
+        ensure_flags(c, (size_t)n);
+        CK(launch_act_flags(c.A, c.d_active, n, q_out, topo, nullptr, c.d_flags, c.nX, c.nY, c.st));
         c.launches++;
-        if ((int)slots.size() > c.h_act_cap) {
+        if (n * per > c.h_act_cap) {
             if (c.h_act) CK(cudaFreeHost(c.h_act));
-            c.h_act_cap = std::max<int>((int)slots.size(), 2 * c.h_act_cap);
+            c.h_act_cap = std::max<int>(n * per, 2 * c.h_act_cap);
             CK(cudaMallocHost(&c.h_act, (size_t)c.h_act_cap * sizeof(int)));
         }
-        CK(cudaMemcpyAsync(c.h_act, c.d_flags, slots.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(c.h_act, c.d_flags, (size_t)n * per * sizeof(int), cudaMemcpyDeviceToHost, c.st));
     }
 }
 
@@ -805,7 +848,10 @@ bool finish_hydraulic(kg_ctx& c, double& dt, int q_out, int topo, bool flags_aft
     if (dt2 < dt) { account_pass(c, W_S1); account_pass(c, W_S2); dt = 0.9 * dt2; return true; }
     account_pass(c, W_S1); account_pass(c, W_S2); account_pass(c, W_S3);
     if (flags_after) {
-        c.act_flags.assign(c.h_act, c.h_act + c.active.size());
+        int n = (int)c.active.size(), per = (c.SC + 255) / 256;
+        c.act_flags.assign((size_t)n, 0);
+        for (int q = 0; q < n; ++q)
+            for (int k = 0; k < per; ++k) c.act_flags[(size_t)q] |= c.h_act[q * per + k];
         c.act_q = q_out;
         c.act_t = topo;
         c.act_gen = c.gen;
@@ -907,14 +953,14 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
     std::vector<int> slots;
     for (int id : c.active) slots.push_back(T(c, id).slot);
     int n = (int)slots.size();
-    upload_list(c, slots);
+    const int* dl = c.d_active;
     const bool fp32 = c.prec == KG_PREC_FP32;
-    CK(launch_m_init(c.A, c.d_list, n, c.SV, qa, c.tcur, tnew, c.st));
+    CK(launch_m_init(c.A, dl, n, c.SV, qa, c.tcur, tnew, c.d_mflags, c.st));
     c.launches++;
     for (int stage = 1; stage <= 3; ++stage) {
-        CK(launch_m_emd(c.A, c.d_list, n, c.SC, tnew, fp32, c.st));
-        CK(launch_m_bt(c.A, c.d_list, n, c.SV, c.tcur, tnew, stage, dt_m, fp32, c.st));
-        CK(launch_m_cells(c.A, c.d_list, n, c.SC, qa, c.tcur, tnew, fp32, c.st));
+        CK(launch_m_emd(c.A, dl, n, c.SC, tnew, fp32, c.st));
+        CK(launch_m_bt(c.A, dl, n, c.SV, c.tcur, tnew, stage, dt_m, fp32, c.st));
+        CK(launch_m_cells(c.A, dl, n, c.SC, qa, c.tcur, tnew, fp32, c.st));
         c.launches += 3;
     }
     int need = n * c.SC;
@@ -927,20 +973,11 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         CK(cudaMalloc(&c.d_rcell, (size_t)c.cand_cap * sizeof(int)));
         CK(cudaMalloc(&c.d_rwave, ((size_t)c.cand_cap + 1) * sizeof(int)));
     }
-    if (!c.d_mflags) {
-        CK(cudaMalloc(&c.d_mflags, sizeof(int)));
-        CK(cudaMalloc(&c.d_ncand, sizeof(int)));
-    }
-    CK(cudaMemsetAsync(c.d_mflags, 0, sizeof(int), c.st));
-    CK(cudaMemsetAsync(c.d_ncand, 0, sizeof(int), c.st));
-    CK(launch_m_check(c.A, c.d_list, n, c.SC, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, c.st));
+    CK(launch_m_check(c.A, dl, n, c.SC, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, c.st));
     c.launches++;
-    int hf[2];
-    CK(cudaMemcpyAsync(&hf[0], c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
-    CK(cudaMemcpyAsync(&hf[1], c.d_ncand, sizeof(int), cudaMemcpyDeviceToHost, c.st));
-    sync(c);
-    int ncand = hf[1];
-    if (hf[0] != 0) {
+    collect_cfl(c);
+    int ncand = c.h_ctl->ncand;
+    if (c.h_ctl->mflag != 0) {
         dt_m = 0.5 * dt_m;
         dt = 0.5 * dt_m;
         return 1;
@@ -974,10 +1011,9 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         c.launches++;
     }
     // Interfacial topography of the new bed and the M result (both scratch until accepted).
-    upload_list(c, slots);
-    CK(launch_face_topo(c.A, c.d_list, n, tnew, c.nX, c.nY, fp32, c.st));
-    CK(launch_face_bI(c.A, c.d_list, n, tnew, c.nX, c.nY, c.st));
-    CK(launch_m_finish(c.A, c.d_list, n, c.SC, qa, c.st));
+    CK(launch_face_topo(c.A, dl, n, tnew, c.nX, c.nY, fp32, c.st));
+    CK(launch_face_bI(c.A, dl, n, tnew, c.nX, c.nY, c.st));
+    CK(launch_m_finish(c.A, dl, n, c.SC, qa, c.st));
     c.launches += 3;
     c.tdirty[tnew] = std::max(c.tdirty[tnew], 1);
     // RHS check at t0 + dt, then H(dt) from the M result, gated by both tests.
@@ -988,9 +1024,8 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
     launch_pass(c, R, W_RHS);
     c.dt = dt;
     queue_hydraulic(c, dt, nullptr, o[0], 1, tnew, o[1], o[2], o[1], c.d_mflags, c.d_cfl + W_RHS, true);
-    CK(cudaMemcpyAsync(c.h_mf, c.d_mflags, sizeof(int), cudaMemcpyDeviceToHost, c.st));
     collect_cfl(c);
-    if (*c.h_mf != 0) {
+    if (c.h_ctl->mflag != 0) {
         c.t = c.t0;
         dt_m = 0.5 * dt_m;
         dt = 0.5 * dt_m;
@@ -1037,11 +1072,11 @@ void integrate_step_body(kg_ctx& c, double tend) {
     CK(launch_dt(c.d_cfl + W_RHS, partial(c), cap, c.d_dt, c.st));
     c.launches++;
     queue_hydraulic(c, 0.0, c.d_dt, c.qcur, 0, c.tcur, o[0], o[1], o[0], nullptr, nullptr, !morpho);
-    CK(cudaMemcpyAsync(c.h_dt, c.d_dt, sizeof(double), cudaMemcpyDeviceToHost, c.st));
     collect_cfl(c);
     account_pass(c, W_RHS);
     double adv = mn(advised(c, c.h_cfl[W_RHS], 1), cap);
-    if (!(adv == *c.h_dt) && !(adv != adv && *c.h_dt != *c.h_dt))
+    double ddt = c.h_ctl->dt;
+    if (!(adv == ddt) && !(adv != adv && ddt != ddt))
         throw KgError(KG_ERR_CUDA, "device-side dt differs from the host's");
     c.dt = adv;
     double dt = adv;
@@ -1326,12 +1361,15 @@ void setup(kg_ctx& c, const kg_params& p) {
     c.t = 0.0;
     c.A.nE = c.nE;
     CK(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
-    CK(cudaMalloc(&c.d_cfl, 4 * sizeof(unsigned long long)));
+    CK(cudaMalloc(&c.d_ctl, sizeof(kg_ctx::Ctl)));
+    CK(cudaMemset(c.d_ctl, 0, sizeof(kg_ctx::Ctl)));
+    c.d_cfl = c.d_ctl->cfl;
+    c.d_dt = &c.d_ctl->dt;
+    c.d_mflags = &c.d_ctl->mflag;
+    c.d_ncand = &c.d_ctl->ncand;
     CK(cudaMalloc(&c.d_vol, 4 * sizeof(double)));
-    CK(cudaMallocHost(&c.h_cfl, 4 * sizeof(unsigned long long)));
-    CK(cudaMalloc(&c.d_dt, sizeof(double)));
-    CK(cudaMallocHost(&c.h_dt, sizeof(double)));
-    CK(cudaMallocHost(&c.h_mf, sizeof(int)));
+    CK(cudaMallocHost(&c.h_ctl, sizeof(kg_ctx::Ctl)));
+    c.h_cfl = c.h_ctl->cfl;
     CK(set_constants(c.dp, nullptr, 0, c.st));
     sync(c);
 }
@@ -1347,14 +1385,12 @@ void free_ctx(kg_ctx* c) {
     cudaFree(c->d_tlist);
     void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
-                    c->d_cfl, c->d_vol, c->d_srcHn, c->d_srcRho, c->d_mflags, c->d_ncand, c->d_ckey, c->d_cex,
+                    c->d_ctl, c->d_vol, c->d_srcHn, c->d_srcRho, c->d_ckey, c->d_cex,
                     c->d_rslot, c->d_rcell, c->d_rwave};
     for (void* q : ptrs) cudaFree(q);
-    if (c->h_cfl) cudaFreeHost(c->h_cfl);
-    if (c->h_dt) cudaFreeHost(c->h_dt);
-    if (c->h_mf) cudaFreeHost(c->h_mf);
+    if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->h_act) cudaFreeHost(c->h_act);
-    cudaFree(c->d_dt);
+    cudaFree(c->d_active);
     for (int k = 0; k < 4; ++k) {
         if (c->ev0[k]) cudaEventDestroy(c->ev0[k]);
         if (c->ev1[k]) cudaEventDestroy(c->ev1[k]);

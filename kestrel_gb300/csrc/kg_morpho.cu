@@ -36,8 +36,11 @@ __device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return 
     int s = slots[blockIdx.x / per_];                       \
     int item_ = (blockIdx.x % per_) * 256 + threadIdx.x;
 
-__global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
+// ctl_flags[0..1]: the M refine flag and the candidate count, zeroed here for k_m_check.
+__global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew,
+                                                int* ctl_flags) {
     const DevParams& P = cP;
+    if (blockIdx.x == 0 && threadIdx.x < 2) ctl_flags[threadIdx.x] = 0;
     int SC = P.nX * P.nY, SV = (P.nX + 1) * (P.nY + 1);
     KG_TILE_THREAD(SV)
     if (item_ < SV) {
@@ -500,8 +503,9 @@ __global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __rest
 // ---- host launchers (cells/verts: items per tile) ----
 static inline int per_of(int items) { return (items + 255) / 256; }
 
-cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, cudaStream_t st) {
-    k_m_init<<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
+cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, int* ctl_flags,
+                          cudaStream_t st) {
+    k_m_init<<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, ctl_flags);
     return cudaGetLastError();
 }
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st) {

@@ -285,8 +285,14 @@ __global__ void __launch_bounds__(256) k_act_flags(DevArrays A, const int* __res
         if (0 > nX - TB) f |= 4;
         if (nX <= TB) f |= 8;
     }
+    // One word per (tile, chunk): the host ORs a tile's chunks, so nothing needs zeroing.
+    __shared__ int red;
+    if (threadIdx.x == 0) red = 0;
+    __syncthreads();
     f = __reduce_or_sync(0xffffffffu, f);
-    if ((threadIdx.x & 31) == 0 && f) atomicOr(&flags[pos], f);
+    if ((threadIdx.x & 31) == 0 && f) atomicOr(&red, f);
+    __syncthreads();
+    if (threadIdx.x == 0) flags[blockIdx.x] = red;
 }
 
 // Sequential compensated sums over the active tiles in list order (j outer, i inner).
@@ -371,8 +377,6 @@ cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st) {
 cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn_over, int* d_flags,
                              int nX, int nY, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(d_flags, 0, (size_t)n * sizeof(int), st);
-    if (e != cudaSuccess) return e;
     int per = (nX * nY + 255) / 256;
     k_act_flags<<<n * per, 256, 0, st>>>(A, d_slots, qcur, ts, hn_over, d_flags, per);
     return cudaGetLastError();
