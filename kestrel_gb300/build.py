@@ -41,7 +41,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-O3", "-std=c++17", ARCH, "-lineinfo", "-fmad=false", "--extended-lambda",
+    # -fmad=false keeps FP64 roundings identical to the reference's; -prec-div/-prec-sqrt
+    # only touch single precision, which only the FP32 form uses (approximate FP32 divide
+    # and square root, 2 ulp, never an FP64-pipe slow path).
+    cmd = [nvcc(), "-O3", "-std=c++17", ARCH, "-lineinfo", "-fmad=false", "-prec-div=false", "-prec-sqrt=false",
+           "--extended-lambda",
            "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-shared",
            "-o", tmp, os.path.join(CSRC, "kg_lib.cu")]
     if verbose:

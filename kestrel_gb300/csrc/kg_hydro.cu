@@ -264,21 +264,33 @@ __device__ __forceinline__ double advised_m(unsigned long long bits, int partial
     return mn(m, P.maxdt);
 }
 
-// Resolve a device-held dt into the pass arguments, then apply the stage gate: false when
-// an earlier test of this step would have refined dt (TimeStepper.f90:393-404, :452-463
-// and the 10% test of :235-248), so the pass leaves every output untouched.
-__device__ __forceinline__ bool stage_gate_open(StepArgs& S) {
+// The dt and times one pass uses.
+struct StageTimes {
+    double dt, t_rhs, t_max;
+};
+
+// Resolve a device-held dt (and the times derived from it exactly as the host derives
+// them), then apply the stage gate: false when an earlier test of this step would have
+// refined dt (TimeStepper.f90:393-404, :452-463 and the 10% test of :235-248), so the pass
+// leaves every output untouched.  S stays in parameter space (constant indices only).
+__device__ __forceinline__ bool stage_gate_open(const StepArgs& S, StageTimes& T) {
+    T.dt = S.dt;
+    T.t_rhs = S.t_rhs;
+    T.t_max = S.t_max;
     if (S.dtp) {
-        S.dt = *(volatile const double*)S.dtp;
-        if (S.tmode == 1) S.t_rhs = S.t_grid + S.dt;
-        else if (S.tmode == 2) S.t_rhs = S.t_grid + 0.5 * S.dt;
-        S.t_max = S.t_grid + S.dt;
+        T.dt = *(volatile const double*)S.dtp;
+        if (S.tmode == 1) T.t_rhs = S.t_grid + T.dt;
+        else if (S.tmode == 2) T.t_rhs = S.t_grid + 0.5 * T.dt;
+        T.t_max = S.t_grid + T.dt;
     }
     if (S.gate_flag && *(volatile const int*)S.gate_flag != 0) return false;
-    for (int g = 0; g < S.ngate; ++g) {
-        double m = advised_m(*(volatile const unsigned long long*)S.gate[g], S.partial);
-        if (S.gate_s1[g]) m = 0.9 * m;
-        if (m < S.dt) return false;
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {
+        if (g < S.ngate) {
+            double m = advised_m(*(volatile const unsigned long long*)S.gate[g], S.partial);
+            if (S.gate_s1[g]) m = 0.9 * m;
+            if (m < T.dt) return false;
+        }
     }
     return true;
 }
@@ -298,8 +310,9 @@ cudaError_t launch_dt(const unsigned long long* cfl, int partial, double cap, do
     return cudaGetLastError();
 }
 
-__global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __restrict__ blocks, StepArgs S) {
-    if (!stage_gate_open(S)) return;
+__global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
+    StageTimes Tm;
+    if (!stage_gate_open(S, Tm)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     HydroSmem& sm = *reinterpret_cast<HydroSmem*>(smraw);
     const DevParams& P = cP;
@@ -352,7 +365,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
                 q0[f] = Qin[plane(s, 4, f, SC) + c];
                 E[f] = A.E[S.e_set][plane(s, 4, f, SC) + c];
             }
-            stage1(q0, E, A.I[S.e_set][plane(s, 1, 0, SC) + c], S.dt, q);
+            stage1(q0, E, A.I[S.e_set][plane(s, 1, 0, SC) + c], Tm.dt, q);
         } else {
 #pragma unroll
             for (int f = 0; f < 4; ++f) q[f] = Qin[plane(s, 4, f, SC) + c];
@@ -585,7 +598,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         double x = -0.5 * P.xSize + P.dx * ((gi - 1.0) * P.nX + ((i + 1) - 0.5));
         double y = -0.5 * P.ySize + P.dy * ((gj - 1.0) * P.nY + ((j + 1) - 0.5));
         double ste[4];
-        explicit_sources(P, A.has_source[slot] != 0, S.t_rhs, S.t_grid, x, y, sm.w[r], b0, bt, sm.rho[r], dbdx, dbdy, gam, ste);
+        explicit_sources(P, A.has_source[slot] != 0, Tm.t_rhs, S.t_grid, x, y, sm.w[r], b0, bt, sm.rho[r], dbdx, dbdy, gam, ste);
         double E[4];
 #pragma unroll
         for (int f = 0; f < 4; ++f) E[f] = STF[f] + ste[f];
@@ -601,12 +614,12 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
             double q0[4], out[4];
 #pragma unroll
             for (int f = 0; f < 4; ++f) q0[f] = q0p[plane(slot, 4, f, SC) + c];
-            stage23(S.mode == MODE_S1 ? 2 : 3, q0, qk, E, I, S.dt, b0, bt, b0, bt, out);
+            stage23(S.mode == MODE_S1 ? 2 : 3, q0, qk, E, I, Tm.dt, b0, bt, b0, bt, out);
             double* dst = A.Q[S.mode == MODE_S1 ? S.q_s1 : S.q_s2];
 #pragma unroll
             for (int f = 0; f < 4; ++f) dst[plane(slot, 4, f, SC) + c] = out[f];
         } else {
-            double dt = S.dt;
+            double dt = Tm.dt;
             double m1 = (qk[1] - dt * dt * E[1] * I) / (1.0 + dt * dt * I * I);
             double m2 = (qk[2] - dt * dt * E[2] * I) / (1.0 + dt * dt * I * I);
             double* dst = A.Q[S.q_out];
@@ -631,7 +644,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
                 dbdx = dbxt;
                 dbdy = dbyt;
                 double* M = A.MX + plane(slot, 11, 0, SC) + c;
-                double tt = S.t_max;
+                double tt = Tm.t_max;
                 if (Hn > P.hThr) {
                     if (M[10 * (size_t)SC] == -1.0) M[10 * (size_t)SC] = tt;
                     if (Hn > M[0]) { M[0] = Hn; M[(size_t)SC] = tt; }

@@ -49,10 +49,11 @@ struct Side32 {
     float hp, p, u, v, rho, du, dv;  // hp: face free surface minus InterpolateB at the face
 };
 
-// Central-upwind fluxes at one face in FP32 (CalculateFluxes, src/HydraulicRHS.f90:949-1064).
-// gamf and kf = (1 + b_t^2)/gamf^3 are the face's cached factors.
+// Central-upwind fluxes at one face in FP32 (CalculateFluxes, src/HydraulicRHS.f90:949-1064),
+// written to out[k * stride] (the shared-memory flux rows).  gamf and kf = (1 + b_t^2)/gamf^3
+// are the face's cached factors.
 __device__ __forceinline__ void face_flux32(const DevParams32& P, bool xdir, const Side32& Pl, const Side32& Mi, float gamf,
-                                            float kf, float gamL, float gamR, float h, float out[7], float& cfl) {
+                                            float kf, float gamL, float gamR, float h, float* out, int stride, float& cfl) {
     const float g = P.g;
     float HnP = Pl.hp * gamf, HnM = Mi.hp * gamf;
     float unP = xdir ? Pl.u : Pl.v, unM = xdir ? Mi.u : Mi.v;
@@ -71,7 +72,7 @@ __device__ __forceinline__ void face_flux32(const DevParams32& P, bool xdir, con
     float dif = aPos - aNeg;
     if (dif < 1e-10f) {
 #pragma unroll
-        for (int k = 0; k < 7; ++k) out[k] = 0.f;
+        for (int k = 0; k < 7; ++k) out[k * stride] = 0.f;
         return;
     }
     float rdif = 1.f / dif;
@@ -79,11 +80,11 @@ __device__ __forceinline__ void face_flux32(const DevParams32& P, bool xdir, con
     float m1P = Pl.rho * HnP * Pl.u, m1M = Mi.rho * HnM * Mi.u;
     float m2P = Pl.rho * HnP * Pl.v, m2M = Mi.rho * HnM * Mi.v;
     out[0] = (HnP - HnM) * gamf * apn + gamf * (ap * HnM * unM - an * HnP * unP);
-    out[3] = (Pl.p - Mi.p) * gamf * apn + gamf * (ap * Mi.p * unM - an * Pl.p * unP);
-    out[1] = (m1P - m1M) * apn + (ap * m1M * unM - an * m1P * unP);
-    out[2] = (m2P - m2M) * apn + (ap * m2M * unM - an * m2P * unP);
+    out[3 * stride] = (Pl.p - Mi.p) * gamf * apn + gamf * (ap * Mi.p * unM - an * Pl.p * unP);
+    out[stride] = (m1P - m1M) * apn + (ap * m1M * unM - an * m1P * unP);
+    out[2 * stride] = (m2P - m2M) * apn + (ap * m2M * unM - an * m2P * unP);
     float GP = 0.5f * g * Pl.rho * Pl.hp * Pl.hp, GM = 0.5f * g * Mi.rho * Mi.hp * Mi.hp;
-    out[4] = ap * GM - an * GP;
+    out[4 * stride] = ap * GM - an * GP;
     const float nu = P.nu;
     float dP1 = 0.f, dP2 = 0.f, dM1 = 0.f, dM2 = 0.f;
     if (!(HnP < 0.f)) {
@@ -94,8 +95,8 @@ __device__ __forceinline__ void face_flux32(const DevParams32& P, bool xdir, con
         dM1 = nu * Mi.rho * HnM * Mi.du;
         dM2 = nu * Mi.rho * HnM * Mi.dv;
     }
-    out[5] = 0.5f * (dP1 + dM1);
-    out[6] = 0.5f * (dP2 + dM2);
+    out[5 * stride] = 0.5f * (dP1 + dM1);
+    out[6 * stride] = 0.5f * (dP2 + dM2);
 }
 
 // Well-balancing and positivity corrections of one reconstructed face side
@@ -108,8 +109,9 @@ __device__ __forceinline__ float side_hp(float dlo, float dhi, float s, bool upp
     return upper ? dhi + s : dlo - s;
 }
 
-__global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __restrict__ blocks, StepArgs S) {
-    if (!stage_gate_open(S)) return;
+__global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
+    StageTimes Tm;
+    if (!stage_gate_open(S, Tm)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
     const DevParams& P = cP;
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
     const float* __restrict__ TF = A.TF[S.topo];
     const double* __restrict__ FX = A.FX[S.topo];
     const double* __restrict__ FY = A.FY[S.topo];
-    const float dtf = (float)S.dt;
+    const float dtf = (float)Tm.dt;
 
     // ---- A: load the cross-shaped region, FP64 depth, FP32 desingularisation ----
     for (int r = tid; r < NR; r += NT) {
@@ -166,8 +168,8 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
             // stage 1 on the fly (src/TimeStepper.f90:371-404): w, Hnpsi in FP64
             const double* E = A.E[S.e_set];
             float I = (float)A.I[S.e_set][plane(s, 1, 0, SC) + c];
-            w = Qin[q] + S.dt * E[q];
-            pp = Qin[q + 3 * (size_t)SC] + S.dt * E[q + 3 * (size_t)SC];
+            w = Qin[q] + Tm.dt * E[q];
+            pp = Qin[q + 3 * (size_t)SC] + Tm.dt * E[q + 3 * (size_t)SC];
             float den = 1.f / (1.f - dtf * I);
             m1 = ((float)Qin[q + SC] + dtf * (float)E[q + SC]) * den;
             m2 = ((float)Qin[q + 2 * (size_t)SC] + dtf * (float)E[q + 2 * (size_t)SC]) * den;
@@ -288,11 +290,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
         R.du = sm.lx[2][liR];
         R.dv = sm.lx[3][liR];
         int fo = j * (nX + 1) + fi;
-        float out[7];
-        face_flux32(F, true, R, L, TFXs[fo], TFXs[fo + SFX], sm.gam[rL], sm.gam[rR], F.dx, out, cfl);
-        int fo2 = cy * (BS + 1) + fx;
-#pragma unroll
-        for (int q = 0; q < 7; ++q) sm.fx[q][fo2] = out[q];
+        face_flux32(F, true, R, L, TFXs[fo], TFXs[fo + SFX], sm.gam[rL], sm.gam[rR], F.dx, &sm.fx[0][cy * (BS + 1) + fx], NFX, cfl);
     }
     for (int k = tid; k < (by + 1) * bx; k += NT) {
         int cx = k % bx, fy = k / bx;
@@ -337,11 +335,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
         R.du = sm.ly[2][liR];
         R.dv = sm.ly[3][liR];
         int fo = fj * nX + i;
-        float out[7];
-        face_flux32(F, false, R, L, TFYs[fo], TFYs[fo + SFY], sm.gam[rL], sm.gam[rR], F.dy, out, cfl);
-        int fo2 = fy * BS + cx;
-#pragma unroll
-        for (int q = 0; q < 7; ++q) sm.fy[q][fo2] = out[q];
+        face_flux32(F, false, R, L, TFYs[fo], TFYs[fo + SFY], sm.gam[rL], sm.gam[rR], F.dy, &sm.fy[0][fy * BS + cx], NFX, cfl);
     }
     // CFL: warp then block min in FP32, the cross-CTA minimum on FP64 bits.
 #pragma unroll
@@ -368,9 +362,8 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
         int xl = cy * (BS + 1) + cx, xr = xl + 1;
         int yb = cy * BS + cx, yt = yb + BS;
         // w and Hnpsi rows in FP64 (the flux differences of FP32 values are exact or nearly so)
-        double E[4];
-        E[0] = (((double)sm.fx[0][xl] - (double)sm.fx[0][xr]) * P.dxR + ((double)sm.fy[0][yb] - (double)sm.fy[0][yt]) * P.dyR) * ig2;
-        E[3] = (((double)sm.fx[3][xl] - (double)sm.fx[3][xr]) * P.dxR + ((double)sm.fy[3][yb] - (double)sm.fy[3][yt]) * P.dyR) * ig;
+        double E0 = (((double)sm.fx[0][xl] - (double)sm.fx[0][xr]) * P.dxR + ((double)sm.fy[0][yb] - (double)sm.fy[0][yt]) * P.dyR) * ig2;
+        double E3 = (((double)sm.fx[3][xl] - (double)sm.fx[3][xr]) * P.dxR + ((double)sm.fy[3][yb] - (double)sm.fy[3][yt]) * P.dyR) * ig;
         float E1 = kahan3<float>(sm.fx[1][xl] - sm.fx[1][xr], (sm.fx[4][xl] - sm.fx[4][xr]) * gXp1, sm.fx[5][xr] - sm.fx[5][xl]) * dxR +
                    kahan3<float>(sm.fy[1][yb] - sm.fy[1][yt], (sm.fy[4][yb] - sm.fy[4][yt]) * gYp1, sm.fy[5][yt] - sm.fy[5][yb]) * dyR;
         float E2 = kahan3<float>(sm.fx[2][xl] - sm.fx[2][xr], (sm.fx[4][xl] - sm.fx[4][xr]) * gXp2, sm.fx[6][xr] - sm.fx[6][xl]) * dxR +
@@ -382,20 +375,21 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
             double x = -0.5 * P.xSize + P.dx * ((gi - 1.0) * P.nX + ((i + 1) - 0.5));
             double y = -0.5 * P.ySize + P.dy * ((gj - 1.0) * P.nY + ((j + 1) - 0.5));
             double s1 = 0.0, s3 = 0.0;
-            flux_source_rates(P, S.t_rhs, S.t_grid, x, y, s1, s3);
-            E[0] = E[0] + s1 * ig2;
-            E[3] = E[3] + s3 * ig;
+            flux_source_rates(P, Tm.t_rhs, S.t_grid, x, y, s1, s3);
+            E0 = E0 + s1 * ig2;
+            E3 = E3 + s3 * ig;
         }
         float grho = F.g * sm.rho[r] * sm.hp[r] / gam;
         E1 = E1 - grho * dbdx;
         E2 = E2 - grho * dbdy;
-        E[1] = E1;
-        E[2] = E2;
         Pt<float> pt{sm.Hn[r], sm.u[r], sm.v[r], sm.psi[r], sm.rho[r], 0.f, dbdx, dbdy, gam};
         float I = implicit_source<float>(F, pt, drag<float>(F, pt));
         if (S.mode == MODE_RHS0) {
-#pragma unroll
-            for (int f = 0; f < 4; ++f) A.E[S.e_set][plane(slot, 4, f, SC) + c] = E[f];
+            double* Ed = A.E[S.e_set] + plane(slot, 4, 0, SC) + c;
+            Ed[0] = E0;
+            Ed[SC] = (double)E1;
+            Ed[2 * (size_t)SC] = (double)E2;
+            Ed[3 * (size_t)SC] = E3;
             A.I[S.e_set][plane(slot, 1, 0, SC) + c] = I;
         } else if (S.mode == MODE_S1 || S.mode == MODE_S2) {
             const double* q0p = A.Q[S.q_in] + plane(slot, 4, 0, SC) + c;
@@ -406,10 +400,10 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
             double a0, a1;
             if (S.mode == MODE_S1) { a0 = 0.75; a1 = 0.25; }
             else { a0 = 1.0 / 3.0; a1 = 2.0 / 3.0; }
-            dst[0] = b + (a0 * hp_old + a1 * (hp_new + S.dt * E[0]));
+            dst[0] = b + (a0 * hp_old + a1 * (hp_new + Tm.dt * E0));
             dst[SC] = (double)((float)a0 * (float)q0p[SC] + (float)a1 * (sm.m1[r] + dtf * E1) * den);
             dst[2 * (size_t)SC] = (double)((float)a0 * (float)q0p[2 * (size_t)SC] + (float)a1 * (sm.m2[r] + dtf * E2) * den);
-            dst[3 * (size_t)SC] = a0 * q0p[3 * (size_t)SC] + a1 * (sm.p64[r] + S.dt * E[3]);
+            dst[3 * (size_t)SC] = a0 * q0p[3 * (size_t)SC] + a1 * (sm.p64[r] + Tm.dt * E3);
         } else {
             float dt2I = dtf * dtf * I;
             float den = 1.f / (1.f + dt2I * I);
@@ -432,7 +426,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
                 float Hn, psi, rho, u, v;
                 desing32(F, hpt, gamt, (float)q0p[SC], (float)q0p[2 * (size_t)SC], (float)q0p[3 * (size_t)SC], Hn, psi, rho, u, v);
                 double* M = A.MX + plane(slot, 11, 0, SC) + c;
-                double tt = S.t_max;
+                double tt = Tm.t_max;
                 double Hnd = Hn, psid = psi;
                 if (Hnd > P.hThr) {
                     if (M[10 * (size_t)SC] == -1.0) M[10 * (size_t)SC] = tt;
