@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -172,10 +173,20 @@ struct kg_ctx {
     double kernel_ms = 0.0;
     int64_t timed_passes = 0;
     cudaStream_t st = nullptr;
+    std::vector<DevSource> dsrc;         // the source table as uploaded (for re-binding)
     std::string err;
 };
 
 namespace {
+
+// The run settings and source table live in the device's __constant__ bank, shared by
+// every context of the process.  The context whose settings are loaded owns it; another
+// context re-binds before it launches (after waiting for the owner's stream when the two
+// streams differ).  API calls on different contexts are serialised by one lock.
+kg_ctx* g_const_owner = nullptr;
+std::recursive_mutex g_api_mu;
+
+void bind_constants(kg_ctx& c);
 
 size_t bytes_per_slot(const kg_ctx& c) {
     size_t SC = c.SC;
@@ -712,6 +723,13 @@ double advised(kg_ctx& c, unsigned long long bits, int substep) {
     m = mn(m, c.p.maxdt);
     if (substep == 1) return 0.9 * m;
     return m;
+}
+
+void bind_constants(kg_ctx& c) {
+    if (g_const_owner == &c) return;
+    if (g_const_owner && g_const_owner->st != c.st) CK(cudaStreamSynchronize(g_const_owner->st));
+    CK(set_constants(c.dp, c.dsrc.empty() ? nullptr : c.dsrc.data(), (int)c.dsrc.size(), c.st));
+    g_const_owner = &c;
 }
 
 // FP32 form: rebuild the factor cache of topography set ts for every allocated tile.
@@ -1289,7 +1307,9 @@ void load_sources(kg_ctx& c) {
         d.x = c.srcs[k].x; d.y = c.srcs[k].y; d.R = c.srcs[k].R; d.n = c.srcs[k].n; d.ncells = c.srcs[k].ncells;
         for (int q = 0; q < d.n; ++q) { d.time[q] = c.srcs[k].time[q]; d.flux[q] = c.srcs[k].flux[q]; d.psi[q] = c.srcs[k].psi[q]; }
     }
+    c.dsrc = ds;
     CK(set_constants(c.dp, ds.data(), (int)ds.size(), c.st));
+    g_const_owner = &c;
     sync(c);
     for (int g : std::vector<int>(c.ghost)) ghost_edges(c, g);
     if (!c.touched.empty()) mirror_touched(c);
@@ -1371,11 +1391,13 @@ void setup(kg_ctx& c, const kg_params& p) {
     CK(cudaMallocHost(&c.h_ctl, sizeof(kg_ctx::Ctl)));
     c.h_cfl = c.h_ctl->cfl;
     CK(set_constants(c.dp, nullptr, 0, c.st));
+    g_const_owner = &c;
     sync(c);
 }
 
 void free_ctx(kg_ctx* c) {
     if (!c) return;
+    if (g_const_owner == c) g_const_owner = nullptr;
     if (c->st) cudaStreamSynchronize(c->st);
     for (int b = 0; b < 4; ++b) cudaFree(c->A.Q[b]);
     for (int b = 0; b < 2; ++b) {
@@ -1430,6 +1452,17 @@ std::vector<double> d2h(kg_ctx* c, const double* src, size_t n) {
 
 }  // namespace
 
+// Every entry point that touches the device holds the API lock and binds its settings.
+#define KG_ENTER(c)                                         \
+    std::lock_guard<std::recursive_mutex> kg_lock_(g_api_mu); \
+    if (c) {                                                \
+        try {                                               \
+            bind_constants(*c);                             \
+        } catch (const KgError& e) {                        \
+            return fail(c, e);                              \
+        }                                                   \
+    }
+
 #define KG_GUARD(c, ...)                                    \
     try {                                                   \
         __VA_ARGS__;                                        \
@@ -1446,6 +1479,7 @@ const char* kg_version(void) { return "kestrel_gb300 1.0 (sm_103a)"; }
 
 int kg_create(const kg_params* params, int32_t precision, kg_ctx** out) {
     if (!params || !out) return KG_ERR_PARAM;
+    std::lock_guard<std::recursive_mutex> lock(g_api_mu);
     *out = nullptr;
     if (precision != KG_PREC_FP64 && precision != KG_PREC_FP32) return KG_ERR_UNSUPPORTED;
     kg_ctx* c = new kg_ctx();
@@ -1464,7 +1498,10 @@ int kg_create(const kg_params* params, int32_t precision, kg_ctx** out) {
     return KG_OK;
 }
 
-void kg_destroy(kg_ctx* ctx) { free_ctx(ctx); }
+void kg_destroy(kg_ctx* ctx) {
+    std::lock_guard<std::recursive_mutex> lock(g_api_mu);
+    free_ctx(ctx);
+}
 
 const char* kg_last_error(const kg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
@@ -1480,6 +1517,7 @@ int kg_upload_b0(kg_ctx* c, const double* b0, int64_t nx1, int64_t ny1) {
 
 int kg_load_sources(kg_ctx* c) {
     if (!c) return KG_ERR_PARAM;
+    KG_ENTER(c);
     if (c->sources_loaded) { c->err = "sources already loaded"; return KG_ERR_STATE; }
     if (c->p.topog == KG_TOPO_UPLOAD && c->upload.empty()) { c->err = "no topography uploaded"; return KG_ERR_STATE; }
     c->gen++;
@@ -1489,6 +1527,7 @@ int kg_load_sources(kg_ctx* c) {
 
 int kg_step(kg_ctx* c, double t_stop, kg_step_stats* st) {
     if (!c) return KG_ERR_PARAM;
+    KG_ENTER(c);
     int64_t s0 = c->steps, r0 = c->rejected, cu0 = c->cell_updates, l0 = c->launches;
     int rc = KG_OK;
     try {
@@ -1502,6 +1541,7 @@ int kg_step(kg_ctx* c, double t_stop, kg_step_stats* st) {
 
 int kg_integrate_to(kg_ctx* c, double t_end, kg_step_stats* st) {
     if (!c) return KG_ERR_PARAM;
+    KG_ENTER(c);
     int64_t s0 = c->steps, r0 = c->rejected, cu0 = c->cell_updates, l0 = c->launches;
     int rc = KG_OK;
     if (t_end > c->t) {
@@ -1520,6 +1560,7 @@ int kg_integrate_to(kg_ctx* c, double t_end, kg_step_stats* st) {
 
 int kg_run(kg_ctx* c, kg_step_stats* st) {
     if (!c) return KG_ERR_PARAM;
+    KG_ENTER(c);
     int64_t s0 = c->steps, r0 = c->rejected, cu0 = c->cell_updates, l0 = c->launches;
     int Nout = c->p.Nout > 0 ? c->p.Nout : 100;
     int rc = KG_OK;
@@ -1530,6 +1571,7 @@ int kg_run(kg_ctx* c, kg_step_stats* st) {
 
 int kg_hydraulic_rhs(kg_ctx* c, double t, int32_t substep, double* advised_dt) {
     if (!c || !advised_dt || substep < 1 || substep > 4) return KG_ERR_PARAM;
+    KG_ENTER(c);
     KG_GUARD(c, {
         rebuild_blocks(*c);
         *advised_dt = rhs0(*c, c->qcur, 0, c->tcur, t, substep);
@@ -1553,6 +1595,7 @@ int kg_get_ghost_tiles(kg_ctx* c, int32_t* ids, int32_t* n) {
 }
 
 int kg_get_tile_field(kg_ctx* c, int32_t id, int32_t field, double* out) {
+    KG_ENTER(c);
     int s = active_slot(c, id);
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (field < 1 || field > 13 || !out) return KG_ERR_PARAM;
@@ -1592,6 +1635,7 @@ int kg_get_tile_field(kg_ctx* c, int32_t id, int32_t field, double* out) {
 }
 
 int kg_set_tile_field(kg_ctx* c, int32_t id, int32_t field, const double* in) {
+    KG_ENTER(c);
     int s = active_slot(c, id);
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (field < 1 || field > 4 || !in) return KG_ERR_PARAM;
@@ -1645,6 +1689,7 @@ int kg_get_tile_maxima(kg_ctx* c, int32_t id, int32_t which, double* out) {
 }
 
 int kg_volume(kg_ctx* c, double out[4]) {
+    KG_ENTER(c);
     if (!c || !out) return KG_ERR_PARAM;
     KG_GUARD(c, {
         std::vector<int> slots;

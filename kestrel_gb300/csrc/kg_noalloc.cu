@@ -62,6 +62,7 @@ int scratch_for_current_device(NoAllocScratch** out, std::string& err) {
 
 extern "C" int kg_hydraulic_rhs_noalloc(kg_ctx* c, double t, int32_t substep, double* advised_dt) {
     if (!c || !advised_dt || substep < 1 || substep > 4) return KG_ERR_PARAM;
+    KG_ENTER(c);
     if (c->prec != KG_PREC_FP64) {
         // The FP32 form's factor cache is rebuilt through context-owned scratch.
         c->err = "kg_hydraulic_rhs_noalloc: only FP64 contexts are supported";
