@@ -237,6 +237,30 @@ int  kg_host_times(kg_ctx* ctx, double out[3]);
    No counterpart in the reference. */
 int  kg_hydraulic_rhs_noalloc(kg_ctx* ctx, double t, int32_t substep, double* advised_dt);
 
+/* ---- Batched ensemble: many FP32-form simulations advanced together ----------------
+   The hydraulic passes of all members run as one persistent launch over their packed
+   tile blocks; each member keeps its own tiles, dt control and refinement history, so its
+   results do not depend on the other members.  No reference counterpart (the reference
+   runs one simulation per process). */
+typedef struct kg_batch kg_batch;
+int  kg_batch_create(int32_t max_members, kg_batch** out);
+void kg_batch_destroy(kg_batch* b);
+const char* kg_batch_last_error(const kg_batch* b);
+/* Add a member from its run settings (always the FP32 form); b0 is the vertex grid for
+   KG_TOPO_UPLOAD (else NULL); its sources are loaded.  id receives the member id. */
+int  kg_batch_add(kg_batch* b, const kg_params* params, const double* b0, int64_t nx1, int64_t ny1, int32_t* id);
+/* The member's context: the single-simulation getters (kg_get_tile_field, kg_volume,
+   kg_get_time, ...) work on it.  Do not step or destroy it directly. */
+kg_ctx* kg_batch_member(kg_batch* b, int32_t id);
+int  kg_batch_remove(kg_batch* b, int32_t id);
+/* One accepted step (IntegrateTo's, src/TimeStepper.f90:151-275) of every member that has
+   not reached its end time, through its output intervals as kg_run takes them; live
+   receives the number of members still running. */
+int  kg_batch_step(kg_batch* b, int32_t* live);
+int  kg_batch_finished(kg_batch* b, int32_t id, int32_t* finished);
+int  kg_batch_stats(kg_batch* b, int64_t* launches, int64_t* rounds);
+void* kg_batch_stream(kg_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

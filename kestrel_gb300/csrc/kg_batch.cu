@@ -1,0 +1,751 @@
+// kg_batch.cu -- many simulations advanced together (the batched ensemble form).
+//
+// A batch owns FP32-form simulations of any grid and tile size on one CUDA stream.
+// kg_batch_step advances every live member by one accepted step of IntegrateTo
+// (src/TimeStepper.f90:151-275).  The hydraulic passes of all members that are at the
+// same stage run as ONE persistent launch over the packed list of their tile blocks
+// (k_hydro32_batch: each CTA walks the list with a grid stride and finds its member by a
+// binary search of the block offsets); the step's dt selection and the edge-band flags are
+// batched the same way, and every wait serves all members at once.  Each member keeps its
+// own context (arrays, tiles, dt control, refinement history): its settings come from a
+// per-member table instead of the constant bank, and its arithmetic is the single
+// simulation's, so a member's results are identical alone and in any mix.
+//
+// Steps are driven phase by phase:
+//   prepare   per member: CheckIfNearBoundaries, block list, step targets
+//   H         batched: RHS at t + device dt (fresh steps), the three RK stages (fresh steps
+//             and refined retries), edge-band flags; one wait; the host's tests per member
+//   M         per member: the morphodynamic operator up to its checks (per-member
+//             launches, no wait in between); one wait; redistribution where listed; then
+//             batched: the RHS check and the second H, gated on the device; one wait
+// until every member has accepted its step.
+
+namespace kg {
+
+// Per-member settings and device lists the batched kernels read.
+struct SimStatic {
+    DevArrays A;
+    DevParams P;
+    DevParams32 F;
+    const DevSource* src;
+    const BlockDesc* blocks;
+    const int* slots;  // active slots in list order
+    int nblocks, nactive;
+};
+
+__global__ void __launch_bounds__(NT) k_hydro32_batch(const SimStatic* __restrict__ sims, const StepArgs* __restrict__ args,
+                                                      const int* __restrict__ member, const int* __restrict__ prefix,
+                                                      int njobs, int total) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
+    for (int b = blockIdx.x; b < total; b += gridDim.x) {
+        int lo = 0, hi = njobs - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (prefix[mid] <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        const SimStatic& X = sims[member[lo]];
+        const StepArgs& S = args[lo];
+        StageTimes Tm;
+        if (stage_gate_open(X.P, S, Tm)) hydro32_block(X.A, S, Tm, X.P, X.F, X.src, X.blocks[b - prefix[lo]], sm);
+        __syncthreads();
+    }
+}
+
+// The first dt of a step for each listed member (k_dt's rule with the member's settings).
+struct DtJob {
+    const unsigned long long* cfl;
+    double* dtp;
+    double cap;
+    int partial, member;
+};
+__global__ void k_dt_batch(const SimStatic* __restrict__ sims, const DtJob* __restrict__ jobs, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DtJob& J = jobs[i];
+    double adv = 0.9 * advised_m(sims[J.member].P, *J.cfl, J.partial);
+    *J.dtp = mn(adv, J.cap);
+}
+
+// Edge-band flags of each listed member's candidate result, one word per (tile, chunk) at
+// out + prefix[job].
+struct ActJob {
+    int member, q, topo, per;
+};
+__global__ void __launch_bounds__(256) k_act_flags_batch(const SimStatic* __restrict__ sims, const ActJob* __restrict__ jobs,
+                                                          const int* __restrict__ prefix, int njobs, int total, int* out) {
+    for (int b = blockIdx.x; b < total; b += gridDim.x) {
+        int lo = 0, hi = njobs - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (prefix[mid] <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        const ActJob& J = jobs[lo];
+        const SimStatic& X = sims[J.member];
+        int local = b - prefix[lo];
+        int f = block_or(act_bits(X.P, X.A, X.slots[local / J.per], J.q, J.topo, nullptr, local % J.per));
+        if (threadIdx.x == 0) out[b] = f;
+        __syncthreads();
+    }
+}
+
+}  // namespace kg
+
+namespace {
+
+enum MemberState { ST_FRESH, ST_H1, ST_M, ST_DONE };
+
+struct Member {
+    kg_ctx* c = nullptr;
+    int next_out = 1;        // the output interval being integrated (kg_run's loop)
+    bool finished = false;
+    // the step in progress
+    int state = ST_DONE;
+    bool morpho = false;
+    int o[3] = {0, 0, 0}, tnew = 0, guard = 0, ncand = 0;
+    double dt = 0.0, cap = 0.0, target = 0.0, dt_m = 0.0;
+    std::vector<int> slots;
+};
+
+}  // namespace
+
+struct kg_batch {
+    cudaStream_t st = nullptr;
+    int cap = 0;
+    std::vector<Member> mem;            // index = member id
+    kg_ctx::Ctl* d_ctl = nullptr;       // contiguous control blocks, one per member slot
+    kg_ctx::Ctl* h_ctl = nullptr;       // pinned mirror
+    kg::SimStatic* d_static = nullptr;
+    std::vector<kg::SimStatic> h_static, up_static;
+    // per-launch tables (pinned staging, device copies), sized for `cap` jobs per launch
+    static constexpr int NLAUNCH = 8;
+    kg::StepArgs* h_args = nullptr;
+    kg::StepArgs* d_args = nullptr;
+    int* h_idx = nullptr;  // member and prefix arrays: [launch][2][cap + 1]
+    int* d_idx = nullptr;
+    kg::DtJob* h_dt = nullptr;
+    kg::DtJob* d_dt = nullptr;
+    kg::ActJob* h_act = nullptr;
+    kg::ActJob* d_act = nullptr;
+    int* d_actout = nullptr;
+    int* h_actout = nullptr;
+    int actout_cap = 0;
+    int grid_hydro = 0, grid_act = 0;
+    int launch_no = 0;
+    int64_t launches = 0, rounds = 0;
+    std::string err;
+};
+
+namespace {
+
+using namespace kg;
+
+void batch_sync(kg_batch& b) { CK(cudaStreamSynchronize(b.st)); }
+
+// Rebuild the member table on the host and upload it when it changed.
+void refresh_static(kg_batch& b) {
+    b.h_static.assign((size_t)b.cap, SimStatic{});
+    for (int i = 0; i < b.cap; ++i) {
+        const Member& m = b.mem[(size_t)i];
+        if (!m.c) continue;
+        const kg_ctx& c = *m.c;
+        SimStatic& X = b.h_static[(size_t)i];
+        X.A = c.A;
+        X.P = c.dp;
+        X.F = params32(c.dp);
+        X.src = c.d_src;
+        X.blocks = c.d_blocks;
+        X.slots = c.d_active;
+        X.nblocks = (int)c.blocks.size();
+        X.nactive = (int)c.active.size();
+    }
+    if (b.up_static.size() == b.h_static.size() &&
+        std::memcmp(b.up_static.data(), b.h_static.data(), b.h_static.size() * sizeof(SimStatic)) == 0)
+        return;
+    CK(cudaMemcpyAsync(b.d_static, b.h_static.data(), b.h_static.size() * sizeof(SimStatic), cudaMemcpyHostToDevice, b.st));
+    batch_sync(b);  // the host table is the copy's source
+    b.up_static = b.h_static;
+}
+
+// One batched hydraulic pass over the listed (member, args) jobs.
+void launch_hydro_batch(kg_batch& b, const std::vector<int>& who, const std::vector<StepArgs>& args) {
+    int n = (int)who.size();
+    if (n == 0) return;
+    int L = b.launch_no++ % kg_batch::NLAUNCH;
+    StepArgs* ha = b.h_args + (size_t)L * b.cap;
+    int* hm = b.h_idx + (size_t)L * 2 * (b.cap + 1);
+    int* hp = hm + (b.cap + 1);
+    int total = 0;
+    for (int k = 0; k < n; ++k) {
+        ha[k] = args[(size_t)k];
+        hm[k] = who[(size_t)k];
+        hp[k] = total;
+        total += (int)b.mem[(size_t)who[(size_t)k]].c->blocks.size();
+    }
+    StepArgs* da = b.d_args + (size_t)L * b.cap;
+    int* dm = b.d_idx + (size_t)L * 2 * (b.cap + 1);
+    int* dp = dm + (b.cap + 1);
+    CK(cudaMemcpyAsync(da, ha, (size_t)n * sizeof(StepArgs), cudaMemcpyHostToDevice, b.st));
+    CK(cudaMemcpyAsync(dm, hm, (size_t)2 * (b.cap + 1) * sizeof(int), cudaMemcpyHostToDevice, b.st));
+    if (total == 0) return;
+    int grid = std::min(total, b.grid_hydro);
+    k_hydro32_batch<<<grid, NT, sizeof(Hydro32Smem), b.st>>>(b.d_static, da, dm, dp, n, total);
+    CK(cudaGetLastError());
+    b.launches++;
+}
+
+// The pass arguments a member's single-simulation path would launch with (launch_pass).
+StepArgs member_args(kg_ctx& c, StepArgs S, int word) {
+    S.cfl_min = c.d_cfl + word;
+    S.partial = partial(c);
+    return S;
+}
+
+// Queue the three RK stages for the listed members (the batched queue_hydraulic): fresh
+// members read their dt on the device, the others use the host dt; `m_gates` adds the
+// M-phase gates (refine flag and RHS check).
+void queue_stages_batch(kg_batch& b, const std::vector<int>& who, bool m_gates) {
+    std::vector<StepArgs> a1, a2, a3;
+    for (int id : who) {
+        Member& m = b.mem[(size_t)id];
+        kg_ctx& c = *m.c;
+        bool fresh = m.state == ST_FRESH;
+        int q_in = m_gates ? m.o[0] : c.qcur, e_set = m_gates ? 1 : 0, topo = m_gates ? m.tnew : c.tcur;
+        int q_s1 = m_gates ? m.o[1] : m.o[0], q_s2 = m_gates ? m.o[2] : m.o[1], q_out = m_gates ? m.o[1] : m.o[0];
+        double dt = fresh ? 0.0 : m.dt;
+        double nextT = c.t + dt;
+        StepArgs S{};
+        S.q_in = q_in; S.q_s1 = q_s1; S.q_s2 = q_s2; S.q_out = q_out; S.e_set = e_set; S.topo = topo;
+        S.q_tc = c.qcur; S.topo_tc = c.tcur;
+        S.dt = dt; S.dtp = fresh ? c.d_dt : nullptr; S.t_grid = c.t; S.do_maxima = 1;
+        int g0 = 0;
+        if (m_gates) {
+            S.gate_flag = c.d_mflags;
+            S.gate[0] = c.d_cfl + W_RHS;
+            S.gate_s1[0] = 1;
+            g0 = 1;
+        }
+        if (!fresh) c.dt = dt;
+        S.mode = MODE_S1; S.t_rhs = nextT; S.tmode = 1; S.ngate = g0;
+        a1.push_back(member_args(c, S, W_S1));
+        S.mode = MODE_S2; S.t_rhs = c.t + 0.5 * dt; S.tmode = 2;
+        S.gate[g0] = c.d_cfl + W_S1; S.gate_s1[g0] = 0; S.ngate = g0 + 1;
+        a2.push_back(member_args(c, S, W_S2));
+        S.mode = MODE_S3; S.t_rhs = nextT; S.t_max = nextT; S.tmode = 1;
+        S.gate[g0 + 1] = c.d_cfl + W_S2; S.gate_s1[g0 + 1] = 0; S.ngate = g0 + 2;
+        a3.push_back(member_args(c, S, W_S3));
+    }
+    launch_hydro_batch(b, who, a1);
+    launch_hydro_batch(b, who, a2);
+    launch_hydro_batch(b, who, a3);
+}
+
+// Edge-band flags of the listed members' results (q_out, topo) into the batch buffer;
+// offsets[k] is where member who[k]'s words start.
+void queue_flags_batch(kg_batch& b, const std::vector<int>& who, const std::vector<int>& q, const std::vector<int>& topo,
+                       std::vector<int>& offsets) {
+    int n = (int)who.size();
+    offsets.assign((size_t)n, 0);
+    if (n == 0) return;
+    int* hp = b.h_idx + (size_t)(kg_batch::NLAUNCH) * 2 * (b.cap + 1);  // the flags job prefix
+    int total = 0;
+    for (int k = 0; k < n; ++k) {
+        kg_ctx& c = *b.mem[(size_t)who[(size_t)k]].c;
+        int per = (c.SC + 255) / 256;
+        b.h_act[k] = ActJob{who[(size_t)k], q[(size_t)k], topo[(size_t)k], per};
+        hp[k] = total;
+        offsets[(size_t)k] = total;
+        total += (int)c.active.size() * per;
+    }
+    if (total > b.actout_cap) {
+        if (b.d_actout) CK(cudaFree(b.d_actout));
+        if (b.h_actout) CK(cudaFreeHost(b.h_actout));
+        b.actout_cap = std::max(total, 2 * b.actout_cap);
+        CK(cudaMalloc(&b.d_actout, (size_t)b.actout_cap * sizeof(int)));
+        CK(cudaMallocHost(&b.h_actout, (size_t)b.actout_cap * sizeof(int)));
+    }
+    int* dp = b.d_idx + (size_t)(kg_batch::NLAUNCH) * 2 * (b.cap + 1);
+    CK(cudaMemcpyAsync(b.d_act, b.h_act, (size_t)n * sizeof(ActJob), cudaMemcpyHostToDevice, b.st));
+    CK(cudaMemcpyAsync(dp, hp, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, b.st));
+    if (total == 0) return;
+    k_act_flags_batch<<<std::min(total, b.grid_act), 256, 0, b.st>>>(b.d_static, b.d_act, dp, n, total, b.d_actout);
+    CK(cudaGetLastError());
+    b.launches++;
+    CK(cudaMemcpyAsync(b.h_actout, b.d_actout, (size_t)total * sizeof(int), cudaMemcpyDeviceToHost, b.st));
+}
+
+// Reset every member's CFL words (one copy; the other control words are left to the
+// kernels that own them).
+void reset_ctl(kg_batch& b) {
+    for (int i = 0; i < b.cap; ++i)
+        for (int k = 0; k < 4; ++k) b.h_ctl[i].cfl[k] = HUGE_BITS;
+    CK(cudaMemcpyAsync(b.d_ctl, b.h_ctl, (size_t)b.cap * sizeof(kg_ctx::Ctl), cudaMemcpyHostToDevice, b.st));
+}
+void collect_ctl(kg_batch& b) {
+    CK(cudaMemcpyAsync(b.h_ctl, b.d_ctl, (size_t)b.cap * sizeof(kg_ctx::Ctl), cudaMemcpyDeviceToHost, b.st));
+    batch_sync(b);
+}
+
+// The end of an accepted step (the tail of integrate_step).
+void finish_step(Member& m, int newcur) {
+    kg_ctx& c = *m.c;
+    c.qcur = newcur;
+    if (m.morpho) c.tcur = m.tnew;
+    c.t = m.morpho ? c.t0 + 2.0 * m.dt : c.t0 + m.dt;
+    c.dt = m.dt;
+    c.steps++;
+    c.cell_updates += (int64_t)c.active.size() * c.SC * (m.morpho ? 2 : 1);
+    c.src_override = false;
+    m.state = ST_DONE;
+    if (c.t >= m.target) {
+        m.next_out++;
+        int Nout = c.p.Nout > 0 ? c.p.Nout : 100;
+        if (m.next_out > Nout) m.finished = true;
+    }
+}
+
+// A refused attempt: back to the first H with the refined dt (the loop of integrate_step).
+void refuse(Member& m) {
+    m.c->rejected++;
+    m.c->dt = m.dt;
+    m.state = ST_H1;
+}
+
+// Guard of each attempt (integrate_step's loop head).
+void guard(Member& m) {
+    if (++m.guard > 100000 || !(m.dt > 0.0)) throw KgError(KG_ERR_DT, "time step collapsed");
+}
+
+// Phase H: RHS + device dt for fresh members, the three stages for fresh and retrying
+// members, flags for hydraulic-only members; one wait; the host's tests.
+void phase_h(kg_batch& b, const std::vector<int>& who) {
+    reset_ctl(b);
+    std::vector<int> fresh;
+    std::vector<StepArgs> ra;
+    for (int id : who) {
+        Member& m = b.mem[(size_t)id];
+        kg_ctx& c = *m.c;
+        if (c.prec == KG_PREC_FP32 && c.tdirty[c.tcur]) {
+            bind_constants(c);
+            refresh_topo32(c, c.tcur);
+        }
+        if (m.state == ST_FRESH) {
+            fresh.push_back(id);
+            ra.push_back(member_args(c, rhs_args(c, c.qcur, 0, c.tcur, c.t), W_RHS));
+        }
+    }
+    launch_hydro_batch(b, fresh, ra);
+    if (!fresh.empty()) {
+        int n = (int)fresh.size();
+        for (int k = 0; k < n; ++k) {
+            Member& m = b.mem[(size_t)fresh[(size_t)k]];
+            b.h_dt[k] = DtJob{m.c->d_cfl + W_RHS, m.c->d_dt, m.cap, partial(*m.c), fresh[(size_t)k]};
+        }
+        CK(cudaMemcpyAsync(b.d_dt, b.h_dt, (size_t)n * sizeof(DtJob), cudaMemcpyHostToDevice, b.st));
+        k_dt_batch<<<(n + 127) / 128, 128, 0, b.st>>>(b.d_static, b.d_dt, n);
+        CK(cudaGetLastError());
+        b.launches++;
+    }
+    queue_stages_batch(b, who, false);
+    std::vector<int> fw, fq, ft, off;
+    for (int id : who)
+        if (!b.mem[(size_t)id].morpho) {
+            fw.push_back(id);
+            fq.push_back(b.mem[(size_t)id].o[0]);
+            ft.push_back(b.mem[(size_t)id].c->tcur);
+        }
+    queue_flags_batch(b, fw, fq, ft, off);
+    collect_ctl(b);
+    size_t fk = 0;
+    for (int id : who) {
+        Member& m = b.mem[(size_t)id];
+        kg_ctx& c = *m.c;
+        if (m.state == ST_FRESH) {
+            double adv = mn(advised(c, c.h_cfl[W_RHS], 1), m.cap);
+            double ddt = c.h_ctl->dt;
+            if (!(adv == ddt) && !(adv != adv && ddt != ddt)) throw KgError(KG_ERR_CUDA, "device-side dt differs from the host's");
+            c.dt = adv;
+            m.dt = adv;
+        }
+        guard(m);
+        const int* chunks = nullptr;
+        if (!m.morpho) {
+            while (fk < fw.size() && fw[fk] != id) ++fk;
+            chunks = b.h_actout + off[fk];
+        }
+        bool rej = finish_hydraulic(c, m.dt, m.o[0], c.tcur, !m.morpho, chunks);
+        if (rej) { refuse(m); continue; }
+        if (!m.morpho) finish_step(m, m.o[0]);
+        else m.state = ST_M;
+    }
+}
+
+// Phase M: the morphodynamic operator of every listed member, its checks and
+// redistribution, then the batched RHS check and second H.
+void phase_m(kg_batch& b, const std::vector<int>& who) {
+    reset_ctl(b);
+    for (int id : who) {
+        Member& m = b.mem[(size_t)id];
+        kg_ctx& c = *m.c;
+        bind_constants(c);
+        m.dt_m = 2.0 * m.dt;
+        m.slots.clear();
+        for (int t : c.active) m.slots.push_back(T(c, t).slot);
+        int n = (int)m.slots.size();
+        const bool fp32 = c.prec == KG_PREC_FP32;
+        CK(launch_m_init(c.A, c.d_active, n, c.SV, m.o[0], c.tcur, m.tnew, c.d_mflags, c.st));
+        for (int stage = 1; stage <= 3; ++stage) {
+            CK(launch_m_emd(c.A, c.d_active, n, c.SC, m.tnew, fp32, c.st));
+            CK(launch_m_bt(c.A, c.d_active, n, c.SV, c.tcur, m.tnew, stage, m.dt_m, fp32, c.st));
+            CK(launch_m_cells(c.A, c.d_active, n, c.SC, m.o[0], c.tcur, m.tnew, fp32, c.st));
+        }
+        int need = n * c.SC;
+        if (need > c.cand_cap) {
+            cudaFree(c.d_ckey); cudaFree(c.d_cex); cudaFree(c.d_rslot); cudaFree(c.d_rcell); cudaFree(c.d_rwave);
+            c.cand_cap = std::max(need, 2 * c.cand_cap);
+            CK(cudaMalloc(&c.d_ckey, (size_t)c.cand_cap * sizeof(unsigned long long)));
+            CK(cudaMalloc(&c.d_cex, (size_t)c.cand_cap * sizeof(double)));
+            CK(cudaMalloc(&c.d_rslot, (size_t)c.cand_cap * sizeof(int)));
+            CK(cudaMalloc(&c.d_rcell, (size_t)c.cand_cap * sizeof(int)));
+            CK(cudaMalloc(&c.d_rwave, ((size_t)c.cand_cap + 1) * sizeof(int)));
+        }
+        CK(launch_m_check(c.A, c.d_active, n, c.SC, m.o[0], c.tcur, m.tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, c.st));
+        c.launches += 11;
+        b.launches += 11;
+    }
+    collect_ctl(b);
+    std::vector<int> go, listed;
+    for (int id : who) {
+        Member& m = b.mem[(size_t)id];
+        kg_ctx& c = *m.c;
+        if (c.h_ctl->mflag != 0) {
+            m.dt_m = 0.5 * m.dt_m;
+            m.dt = 0.5 * m.dt_m;
+            refuse(m);
+            continue;
+        }
+        m.ncand = c.h_ctl->ncand;
+        go.push_back(id);
+        if (m.ncand > 0) listed.push_back(id);
+    }
+    // Redistribution lists of the members that have one (one wait for all read-backs).
+    std::vector<std::vector<unsigned long long>> keys(listed.size());
+    std::vector<std::vector<double>> exs(listed.size());
+    for (size_t k = 0; k < listed.size(); ++k) {
+        Member& m = b.mem[(size_t)listed[k]];
+        kg_ctx& c = *m.c;
+        keys[k].resize((size_t)m.ncand);
+        exs[k].resize((size_t)m.ncand);
+        CK(cudaMemcpyAsync(keys[k].data(), c.d_ckey, (size_t)m.ncand * sizeof(unsigned long long), cudaMemcpyDeviceToHost, b.st));
+        CK(cudaMemcpyAsync(exs[k].data(), c.d_cex, (size_t)m.ncand * sizeof(double), cudaMemcpyDeviceToHost, b.st));
+    }
+    if (!listed.empty()) batch_sync(b);
+    for (size_t k = 0; k < listed.size(); ++k) {
+        Member& m = b.mem[(size_t)listed[k]];
+        kg_ctx& c = *m.c;
+        bind_constants(c);
+        const auto& key = keys[k];
+        const auto& ex = exs[k];
+        int ncand = m.ncand;
+        std::vector<int> ord((size_t)ncand);
+        for (int q = 0; q < ncand; ++q) ord[(size_t)q] = q;
+        std::sort(ord.begin(), ord.end(), [&](int x, int y) {
+            if (ex[(size_t)x] != ex[(size_t)y]) return ex[(size_t)x] < ex[(size_t)y];
+            return key[(size_t)x] < key[(size_t)y];
+        });
+        std::vector<int> ls, lc, woff;
+        redistribution_waves(c, m.slots, key, ord, ls, lc, woff);
+        int nw = (int)woff.size() - 1;
+        c.redist_cells += ncand;
+        c.redist_waves += nw;
+        c.redist_walks++;
+        CK(cudaMemcpyAsync(c.d_rslot, ls.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, c.d_rwave, nw, m.o[0], c.tcur, m.tnew, c.d_mflags, c.st));
+        c.launches++;
+        b.launches++;
+    }
+    if (go.empty()) return;
+    std::vector<StepArgs> ra;
+    for (int id : go) {
+        Member& m = b.mem[(size_t)id];
+        kg_ctx& c = *m.c;
+        bind_constants(c);
+        int n = (int)m.slots.size();
+        const bool fp32 = c.prec == KG_PREC_FP32;
+        CK(launch_face_topo(c.A, c.d_active, n, m.tnew, c.nX, c.nY, fp32, c.st));
+        CK(launch_face_bI(c.A, c.d_active, n, m.tnew, c.nX, c.nY, c.st));
+        CK(launch_m_finish(c.A, c.d_active, n, c.SC, m.o[0], c.st));
+        c.launches += 3;
+        b.launches += 3;
+        c.tdirty[m.tnew] = std::max(c.tdirty[m.tnew], 1);
+        if (fp32) refresh_topo32(c, m.tnew);
+        c.t = c.t0 + m.dt;
+        c.dt = m.dt;
+        ra.push_back(member_args(c, rhs_args(c, m.o[0], 1, m.tnew, c.t), W_RHS));
+    }
+    launch_hydro_batch(b, go, ra);
+    queue_stages_batch(b, go, true);
+    std::vector<int> fq, ft, off;
+    for (int id : go) {
+        fq.push_back(b.mem[(size_t)id].o[1]);
+        ft.push_back(b.mem[(size_t)id].tnew);
+    }
+    queue_flags_batch(b, go, fq, ft, off);
+    collect_ctl(b);
+    for (size_t k = 0; k < go.size(); ++k) {
+        Member& m = b.mem[(size_t)go[k]];
+        kg_ctx& c = *m.c;
+        if (c.h_ctl->mflag != 0) {
+            c.t = c.t0;
+            m.dt_m = 0.5 * m.dt_m;
+            m.dt = 0.5 * m.dt_m;
+            refuse(m);
+            continue;
+        }
+        double adv = advised(c, c.h_cfl[W_RHS], 1);
+        if (adv < m.dt) {
+            if ((m.dt - adv) / m.dt < 0.1) m.dt = 0.9 * m.dt;
+            else m.dt = adv;
+            c.t = c.t0;
+            refuse(m);
+            continue;
+        }
+        if (!finish_hydraulic(c, m.dt, m.o[1], m.tnew, true, b.h_actout + off[k])) {
+            finish_step(m, m.o[1]);
+            continue;
+        }
+        c.t = c.t0;
+        refuse(m);
+    }
+}
+
+// Prepare one step of a member (the head of integrate_step).
+void prepare(kg_batch& b, Member& m) {
+    kg_ctx& c = *m.c;
+    bind_constants(c);
+    if (!c.sources_loaded) throw KgError(KG_ERR_STATE, "kg_load_sources must be called before stepping");
+    m.target = c.p.tstart + m.next_out * c.DeltaT;
+    check_near_boundaries(c);
+    rebuild_blocks(c);
+    m.morpho = c.p.MorphodynamicsOn != 0;
+    int k = 0;
+    for (int q = 0; q < 4; ++q)
+        if (q != c.qcur) m.o[k++] = q;
+    m.tnew = 1 - c.tcur;
+    double tmax = mn(m.target, next_flux_time(c, c.t));
+    m.cap = m.morpho ? 0.5 * (tmax - c.t) : tmax - c.t;
+    c.t0 = c.t;
+    m.guard = 0;
+    m.state = ST_FRESH;
+    (void)b;
+}
+
+// One accepted step of every live member.
+void batch_step(kg_batch& b) {
+    std::vector<int> live;
+    for (int i = 0; i < b.cap; ++i)
+        if (b.mem[(size_t)i].c && !b.mem[(size_t)i].finished) live.push_back(i);
+    for (int id : live) {
+        Member& m = b.mem[(size_t)id];
+        // kg_integrate_to skips an interval that is already reached
+        int Nout = m.c->p.Nout > 0 ? m.c->p.Nout : 100;
+        while (!m.finished && m.c->t >= m.c->p.tstart + m.next_out * m.c->DeltaT) {
+            m.next_out++;
+            if (m.next_out > Nout) m.finished = true;
+        }
+    }
+    std::vector<int> run;
+    for (int id : live)
+        if (!b.mem[(size_t)id].finished) {
+            prepare(b, b.mem[(size_t)id]);
+            run.push_back(id);
+        }
+    refresh_static(b);
+    while (true) {
+        std::vector<int> h, mm;
+        for (int id : run) {
+            int s = b.mem[(size_t)id].state;
+            if (s == ST_FRESH || s == ST_H1) h.push_back(id);
+            else if (s == ST_M) mm.push_back(id);
+        }
+        if (h.empty() && mm.empty()) break;
+        if (!h.empty()) phase_h(b, h);
+        if (!mm.empty()) phase_m(b, mm);
+        b.rounds++;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void kg_batch_destroy(kg_batch* b);
+
+int kg_batch_create(int32_t max_members, kg_batch** out) {
+    if (!out || max_members < 1) return KG_ERR_PARAM;
+    *out = nullptr;
+    std::lock_guard<std::recursive_mutex> lock(g_api_mu);
+    kg_batch* b = new kg_batch();
+    try {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) throw KgError(KG_ERR_CUDA, "no CUDA device is available");
+        b->cap = max_members;
+        b->mem.resize((size_t)max_members);
+        CK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+        CK(cudaMalloc(&b->d_ctl, (size_t)max_members * sizeof(kg_ctx::Ctl)));
+        CK(cudaMemset(b->d_ctl, 0, (size_t)max_members * sizeof(kg_ctx::Ctl)));
+        CK(cudaMallocHost(&b->h_ctl, (size_t)max_members * sizeof(kg_ctx::Ctl)));
+        CK(cudaMalloc(&b->d_static, (size_t)max_members * sizeof(SimStatic)));
+        CK(cudaMallocHost(&b->h_args, (size_t)kg_batch::NLAUNCH * max_members * sizeof(StepArgs)));
+        CK(cudaMalloc(&b->d_args, (size_t)kg_batch::NLAUNCH * max_members * sizeof(StepArgs)));
+        size_t nidx = (size_t)(kg_batch::NLAUNCH + 1) * 2 * (max_members + 1);
+        CK(cudaMallocHost(&b->h_idx, nidx * sizeof(int)));
+        CK(cudaMalloc(&b->d_idx, nidx * sizeof(int)));
+        CK(cudaMallocHost(&b->h_dt, (size_t)max_members * sizeof(DtJob)));
+        CK(cudaMalloc(&b->d_dt, (size_t)max_members * sizeof(DtJob)));
+        CK(cudaMallocHost(&b->h_act, (size_t)max_members * sizeof(ActJob)));
+        CK(cudaMalloc(&b->d_act, (size_t)max_members * sizeof(ActJob)));
+        CK(cudaFuncSetAttribute(k_hydro32_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Hydro32Smem)));
+        int dev = 0, sms = 0, occ = 0, occa = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_hydro32_batch, NT, sizeof(Hydro32Smem)));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occa, k_act_flags_batch, 256, 0));
+        b->grid_hydro = sms * std::max(occ, 1);
+        b->grid_act = sms * std::max(occa, 1);
+    } catch (const KgError& e) {
+        int code = e.code;
+        kg_batch_destroy(b);
+        return code;
+    }
+    *out = b;
+    return KG_OK;
+}
+
+const char* kg_batch_last_error(const kg_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int kg_batch_add(kg_batch* b, const kg_params* params, const double* b0, int64_t nx1, int64_t ny1, int32_t* id) {
+    if (!b || !params || !id) return KG_ERR_PARAM;
+    std::lock_guard<std::recursive_mutex> lock(g_api_mu);
+    int slot = -1;
+    for (int i = 0; i < b->cap; ++i)
+        if (!b->mem[(size_t)i].c) { slot = i; break; }
+    if (slot < 0) { b->err = "the batch is full"; return KG_ERR_STATE; }
+    kg_ctx* c = nullptr;
+    int rc = kg_create(params, KG_PREC_FP32, &c);
+    if (rc != KG_OK) { b->err = "kg_create failed"; return rc; }
+    try {
+        // the member runs on the batch stream and keeps its control words in the batch
+        CK(cudaStreamSynchronize(c->st));
+        CK(cudaStreamDestroy(c->st));
+        c->st = b->st;
+        c->own_stream = false;
+        CK(cudaFree(c->d_ctl));
+        CK(cudaFreeHost(c->h_ctl));
+        c->own_ctl = false;
+        c->d_ctl = b->d_ctl + slot;
+        c->h_ctl = b->h_ctl + slot;
+        c->d_cfl = c->d_ctl->cfl;
+        c->d_dt = &c->d_ctl->dt;
+        c->d_mflags = &c->d_ctl->mflag;
+        c->d_ncand = &c->d_ctl->ncand;
+        c->h_cfl = c->h_ctl->cfl;
+        g_const_owner = nullptr;
+        if (b0) {
+            rc = kg_upload_b0(c, b0, nx1, ny1);
+            if (rc != KG_OK) throw KgError(rc, c->err);
+        }
+        rc = kg_load_sources(c);
+        if (rc != KG_OK) throw KgError(rc, c->err);
+    } catch (const KgError& e) {
+        b->err = e.what();
+        kg_destroy(c);
+        return e.code;
+    }
+    b->mem[(size_t)slot] = Member{};
+    b->mem[(size_t)slot].c = c;
+    *id = slot;
+    return KG_OK;
+}
+
+kg_ctx* kg_batch_member(kg_batch* b, int32_t id) {
+    if (!b || id < 0 || id >= b->cap) return nullptr;
+    return b->mem[(size_t)id].c;
+}
+
+int kg_batch_remove(kg_batch* b, int32_t id) {
+    if (!b || id < 0 || id >= b->cap || !b->mem[(size_t)id].c) return KG_ERR_PARAM;
+    std::lock_guard<std::recursive_mutex> lock(g_api_mu);
+    cudaStreamSynchronize(b->st);
+    kg_destroy(b->mem[(size_t)id].c);
+    b->mem[(size_t)id] = Member{};
+    return KG_OK;
+}
+
+int kg_batch_step(kg_batch* b, int32_t* live) {
+    if (!b) return KG_ERR_PARAM;
+    std::lock_guard<std::recursive_mutex> lock(g_api_mu);
+    try {
+        batch_step(*b);
+    } catch (const KgError& e) {
+        b->err = e.what();
+        return e.code;
+    }
+    if (live) {
+        int n = 0;
+        for (int i = 0; i < b->cap; ++i)
+            if (b->mem[(size_t)i].c && !b->mem[(size_t)i].finished) ++n;
+        *live = n;
+    }
+    return KG_OK;
+}
+
+int kg_batch_finished(kg_batch* b, int32_t id, int32_t* finished) {
+    if (!b || !finished || id < 0 || id >= b->cap || !b->mem[(size_t)id].c) return KG_ERR_PARAM;
+    Member& m = b->mem[(size_t)id];
+    int Nout = m.c->p.Nout > 0 ? m.c->p.Nout : 100;
+    while (!m.finished && m.c->t >= m.c->p.tstart + m.next_out * m.c->DeltaT) {
+        m.next_out++;
+        if (m.next_out > Nout) m.finished = true;
+    }
+    *finished = m.finished ? 1 : 0;
+    return KG_OK;
+}
+
+int kg_batch_stats(kg_batch* b, int64_t* launches, int64_t* rounds) {
+    if (!b || !launches || !rounds) return KG_ERR_PARAM;
+    *launches = b->launches;
+    *rounds = b->rounds;
+    return KG_OK;
+}
+
+void* kg_batch_stream(kg_batch* b) { return b ? (void*)b->st : nullptr; }
+
+void kg_batch_destroy(kg_batch* b) {
+    if (!b) return;
+    std::lock_guard<std::recursive_mutex> lock(g_api_mu);
+    if (b->st) cudaStreamSynchronize(b->st);
+    for (Member& m : b->mem)
+        if (m.c) kg_destroy(m.c);
+    cudaFree(b->d_ctl);
+    cudaFree(b->d_static);
+    cudaFree(b->d_args);
+    cudaFree(b->d_idx);
+    cudaFree(b->d_dt);
+    cudaFree(b->d_act);
+    cudaFree(b->d_actout);
+    if (b->h_ctl) cudaFreeHost(b->h_ctl);
+    if (b->h_args) cudaFreeHost(b->h_args);
+    if (b->h_idx) cudaFreeHost(b->h_idx);
+    if (b->h_dt) cudaFreeHost(b->h_dt);
+    if (b->h_act) cudaFreeHost(b->h_act);
+    if (b->h_actout) cudaFreeHost(b->h_actout);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+}
+
+}  // extern "C"

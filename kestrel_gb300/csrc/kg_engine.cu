@@ -174,6 +174,8 @@ struct kg_ctx {
     int64_t timed_passes = 0;
     cudaStream_t st = nullptr;
     std::vector<DevSource> dsrc;         // the source table as uploaded (for re-binding)
+    DevSource* d_src = nullptr;          // device copy of the source table (batched passes)
+    bool own_stream = true, own_ctl = true;  // false for members of a batch
     std::string err;
 };
 
@@ -859,7 +861,7 @@ void queue_hydraulic(kg_ctx& c, double dt, const double* dtp, int q_in, int e_se
 
 // The host's refinement tests of HydraulicTimeStepper (src/TimeStepper.f90:393-404,
 // :452-463) on the stage CFL words after the wait; true (and the refined dt) on rejection.
-bool finish_hydraulic(kg_ctx& c, double& dt, int q_out, int topo, bool flags_after) {
+bool finish_hydraulic(kg_ctx& c, double& dt, int q_out, int topo, bool flags_after, const int* chunks = nullptr) {
     double dt1 = advised(c, c.h_cfl[W_S1], 2);
     if (dt1 < dt) { account_pass(c, W_S1); dt = 0.9 * dt1; return true; }
     double dt2 = advised(c, c.h_cfl[W_S2], 3);
@@ -869,7 +871,7 @@ bool finish_hydraulic(kg_ctx& c, double& dt, int q_out, int topo, bool flags_aft
         int n = (int)c.active.size(), per = (c.SC + 255) / 256;
         c.act_flags.assign((size_t)n, 0);
         for (int q = 0; q < n; ++q)
-            for (int k = 0; k < per; ++k) c.act_flags[(size_t)q] |= c.h_act[q * per + k];
+            for (int k = 0; k < per; ++k) c.act_flags[(size_t)q] |= (chunks ? chunks : c.h_act)[q * per + k];
         c.act_q = q_out;
         c.act_t = topo;
         c.act_gen = c.gen;
@@ -1308,6 +1310,10 @@ void load_sources(kg_ctx& c) {
         for (int q = 0; q < d.n; ++q) { d.time[q] = c.srcs[k].time[q]; d.flux[q] = c.srcs[k].flux[q]; d.psi[q] = c.srcs[k].psi[q]; }
     }
     c.dsrc = ds;
+    if (!ds.empty()) {
+        CK(cudaMalloc(&c.d_src, ds.size() * sizeof(DevSource)));
+        CK(cudaMemcpyAsync(c.d_src, ds.data(), ds.size() * sizeof(DevSource), cudaMemcpyHostToDevice, c.st));
+    }
     CK(set_constants(c.dp, ds.data(), (int)ds.size(), c.st));
     g_const_owner = &c;
     sync(c);
@@ -1407,17 +1413,20 @@ void free_ctx(kg_ctx* c) {
     cudaFree(c->d_tlist);
     void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
-                    c->d_ctl, c->d_vol, c->d_srcHn, c->d_srcRho, c->d_ckey, c->d_cex,
+                    c->d_vol, c->d_srcHn, c->d_srcRho, c->d_ckey, c->d_cex, c->d_src,
                     c->d_rslot, c->d_rcell, c->d_rwave};
     for (void* q : ptrs) cudaFree(q);
-    if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    if (c->own_ctl) {
+        cudaFree(c->d_ctl);
+        if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    }
     if (c->h_act) cudaFreeHost(c->h_act);
     cudaFree(c->d_active);
     for (int k = 0; k < 4; ++k) {
         if (c->ev0[k]) cudaEventDestroy(c->ev0[k]);
         if (c->ev1[k]) cudaEventDestroy(c->ev1[k]);
     }
-    if (c->st) cudaStreamDestroy(c->st);
+    if (c->st && c->own_stream) cudaStreamDestroy(c->st);
     delete c;
 }
 

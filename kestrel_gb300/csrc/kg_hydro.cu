@@ -107,10 +107,10 @@ __device__ __forceinline__ void desing(const DevParams& P, double w, double m1, 
 
 // Flux-source rates of ExplicitSourceTerms (src/Equations.f90:500-590) at cell centre
 // (x, y): s1 = sum of Q / (NumCellsInSrc dx dy), s3 = the same for psi Q.
-__device__ __forceinline__ void flux_source_rates(const DevParams& P, double t, double tg, double x, double y, double& s1,
-                                                  double& s3) {
+__device__ __forceinline__ void flux_source_rates(const DevParams& P, const DevSource* src, double t, double tg, double x,
+                                                  double y, double& s1, double& s3) {
     for (int J = 0; J < P.nSources; ++J) {
-        const DevSource& S = cSrc[J];
+        const DevSource& S = src[J];
         double Qf = 0.0, psiQf = 0.0;
         if (((x - S.x) * (x - S.x) + (y - S.y) * (y - S.y)) < S.R * S.R) {
             int n = S.n;
@@ -148,7 +148,7 @@ __device__ __forceinline__ void explicit_sources(const DevParams& P, bool has_sr
     double Qt = 0.0, psiQt = 0.0;
     if (has_src && P.nSources >= 1) {
         double s1 = 0.0, s3 = 0.0;
-        flux_source_rates(P, t, tg, x, y, s1, s3);
+        flux_source_rates(P, cSrc, t, tg, x, y, s1, s3);
         Qt = Qt + s1;
         psiQt = psiQt + s3;
     }
@@ -256,8 +256,7 @@ __device__ __forceinline__ void face_flux(const DevParams& P, bool xdir, const S
 
 // ComputeAdvisedTimeStep (src/HydraulicRHS.f90:141-174) before the substep-1 factor, with
 // the host's operation order.
-__device__ __forceinline__ double advised_m(unsigned long long bits, int partial) {
-    const DevParams& P = cP;
+__device__ __forceinline__ double advised_m(const DevParams& P, unsigned long long bits, int partial) {
     double umin = __longlong_as_double((long long)bits);
     if (partial) umin = mn(umin, P.maxdt);
     double m = mn(P.cfl * umin, P.diffusiveTimeScale);
@@ -273,7 +272,7 @@ struct StageTimes {
 // them), then apply the stage gate: false when an earlier test of this step would have
 // refined dt (TimeStepper.f90:393-404, :452-463 and the 10% test of :235-248), so the pass
 // leaves every output untouched.  S stays in parameter space (constant indices only).
-__device__ __forceinline__ bool stage_gate_open(const StepArgs& S, StageTimes& T) {
+__device__ __forceinline__ bool stage_gate_open(const DevParams& P, const StepArgs& S, StageTimes& T) {
     T.dt = S.dt;
     T.t_rhs = S.t_rhs;
     T.t_max = S.t_max;
@@ -287,7 +286,7 @@ __device__ __forceinline__ bool stage_gate_open(const StepArgs& S, StageTimes& T
 #pragma unroll
     for (int g = 0; g < 3; ++g) {
         if (g < S.ngate) {
-            double m = advised_m(*(volatile const unsigned long long*)S.gate[g], S.partial);
+            double m = advised_m(P, *(volatile const unsigned long long*)S.gate[g], S.partial);
             if (S.gate_s1[g]) m = 0.9 * m;
             if (m < T.dt) return false;
         }
@@ -300,7 +299,7 @@ __device__ __forceinline__ bool stage_gate_open(const StepArgs& S, StageTimes& T
 // the RHS pass; cap is the host's (tmax - t) or (tmax - t)/2.
 __global__ void k_dt(const unsigned long long* __restrict__ cfl, int partial, double cap, double* dtp) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double adv = 0.9 * advised_m(*cfl, partial);
+        double adv = 0.9 * advised_m(cP, *cfl, partial);
         *dtp = mn(adv, cap);
     }
 }
@@ -312,7 +311,7 @@ cudaError_t launch_dt(const unsigned long long* cfl, int partial, double cap, do
 
 __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
     StageTimes Tm;
-    if (!stage_gate_open(S, Tm)) return;
+    if (!stage_gate_open(cP, S, Tm)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     HydroSmem& sm = *reinterpret_cast<HydroSmem*>(smraw);
     const DevParams& P = cP;

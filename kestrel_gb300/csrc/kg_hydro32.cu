@@ -109,14 +109,12 @@ __device__ __forceinline__ float side_hp(float dlo, float dhi, float s, bool upp
     return upper ? dhi + s : dlo - s;
 }
 
-__global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
-    StageTimes Tm;
-    if (!stage_gate_open(S, Tm)) return;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
-    const DevParams& P = cP;
-    const DevParams32& F = cP32;
-    const BlockDesc bd = blocks[blockIdx.x];
+// One BS x BS block of one tile through one pass (the body shared by the single-simulation
+// kernel, whose settings live in constant memory, and the batched kernel, whose settings
+// come from a per-simulation table).
+__device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs& S, const StageTimes& Tm, const DevParams& P,
+                                              const DevParams32& F, const DevSource* src, const BlockDesc bd,
+                                              Hydro32Smem& sm) {
     const int nX = P.nX, nY = P.nY, SC = nX * nY, SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
     const int slot = bd.slot;
     const int bx = min(BS, nX - bd.x0), by = min(BS, nY - bd.y0);
@@ -375,7 +373,7 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
             double x = -0.5 * P.xSize + P.dx * ((gi - 1.0) * P.nX + ((i + 1) - 0.5));
             double y = -0.5 * P.ySize + P.dy * ((gj - 1.0) * P.nY + ((j + 1) - 0.5));
             double s1 = 0.0, s3 = 0.0;
-            flux_source_rates(P, Tm.t_rhs, S.t_grid, x, y, s1, s3);
+            flux_source_rates(P, src, Tm.t_rhs, S.t_grid, x, y, s1, s3);
             E0 = E0 + s1 * ig2;
             E3 = E3 + s3 * ig;
         }
@@ -440,6 +438,14 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
+    StageTimes Tm;
+    if (!stage_gate_open(cP, S, Tm)) return;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
+    hydro32_block(A, S, Tm, cP, cP32, cSrc, blocks[blockIdx.x], sm);
 }
 
 // Topography factors of the FP32 form for the listed slots of set ts, from the FP64 cell

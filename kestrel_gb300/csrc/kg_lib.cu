@@ -7,3 +7,4 @@
 #include "kg_morpho.cu"
 #include "kg_engine.cu"
 #include "kg_noalloc.cu"
+#include "kg_batch.cu"

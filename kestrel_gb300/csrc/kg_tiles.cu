@@ -245,14 +245,12 @@ __global__ void k_init_maxima(DevArrays A, int slot) {
     }
 }
 
-// Edge-band tests of NearNorth/South/East/WestBoundary for each listed active slot:
-// bit 0 N, 1 S, 2 E, 3 W.  hn_over (optional) replaces the depth computed from w (used
-// for the first check after the sources have set the depth field directly).
-__global__ void __launch_bounds__(256) k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur, int ts,
-                                                    const double* __restrict__ hn_over, int* __restrict__ flags, int per) {
-    const DevParams& P = cP;
-    int pos = blockIdx.x / per, chunk = blockIdx.x % per;
-    int s = slots[pos];
+// Edge-band tests of NearNorth/South/East/WestBoundary (src/TimeStepper.f90:924-1150):
+// bit 0 N, 1 S, 2 E, 3 W of one thread's cell in 256-cell chunk `chunk` of slot s.
+// hn_over (optional) replaces the depth computed from w (used for the first check after
+// the sources have set the depth field directly).
+__device__ __forceinline__ int act_bits(const DevParams& P, const DevArrays& A, int s, int qcur, int ts,
+                                        const double* __restrict__ hn_over, int chunk) {
     int nX = P.nX, nY = P.nY, SC = nX * nY, TB = P.TileBuffer;
     const double* Q = A.Q[qcur];
     int f = 0;
@@ -285,14 +283,25 @@ __global__ void __launch_bounds__(256) k_act_flags(DevArrays A, const int* __res
         if (0 > nX - TB) f |= 4;
         if (nX <= TB) f |= 8;
     }
-    // One word per (tile, chunk): the host ORs a tile's chunks, so nothing needs zeroing.
+    return f;
+}
+// OR of f over the CTA (256 threads), valid in thread 0.
+__device__ __forceinline__ int block_or(int f) {
     __shared__ int red;
     if (threadIdx.x == 0) red = 0;
     __syncthreads();
     f = __reduce_or_sync(0xffffffffu, f);
     if ((threadIdx.x & 31) == 0 && f) atomicOr(&red, f);
     __syncthreads();
-    if (threadIdx.x == 0) flags[blockIdx.x] = red;
+    return red;
+}
+
+// One word per (tile, chunk): the host ORs a tile's chunks, so nothing needs zeroing.
+__global__ void __launch_bounds__(256) k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur, int ts,
+                                                    const double* __restrict__ hn_over, int* __restrict__ flags, int per) {
+    int pos = blockIdx.x / per, chunk = blockIdx.x % per;
+    int f = block_or(act_bits(cP, A, slots[pos], qcur, ts, hn_over, chunk));
+    if (threadIdx.x == 0) flags[blockIdx.x] = f;
 }
 
 // Sequential compensated sums over the active tiles in list order (j outer, i inner).

@@ -41,6 +41,17 @@ class Simulation:
         if load_sources:
             self._check(self._f("load_sources")(self.h))
 
+    @classmethod
+    def view(cls, lib, handle, params: abi.Params):
+        """A non-owning view of a context owned elsewhere (a batch member): every getter
+        works; closing the view leaves the context alone."""
+        self = cls.__new__(cls)
+        self.lib, self.pre, self.params = lib, "kg", params
+        self.nX, self.nY = params.nXpertile, params.nYpertile
+        self.h = C.c_void_p(handle)
+        self._owned = False
+        return self
+
     def _f(self, name):
         return getattr(self.lib, f"{self.pre}_{name}")
 
@@ -51,9 +62,9 @@ class Simulation:
         return rc
 
     def close(self):
-        if self.h:
+        if self.h and getattr(self, "_owned", True):
             self._f("destroy")(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
