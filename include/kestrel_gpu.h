@@ -221,6 +221,11 @@ int  kg_get_kernel_time(kg_ctx* ctx, double* ms, int64_t* passes);
    of listed cells walked, the dependency waves they were run in and the walks.  No
    reference counterpart (the reference walks its list serially). */
 int  kg_redistribution_stats(kg_ctx* ctx, int64_t* cells, int64_t* waves, int64_t* walks);
+/* Accepted steps, refused attempts and cell-updates (active cells x accepted hydraulic
+   steps) so far; and the device bytes the context holds for its allocated tiles.  No
+   reference counterpart. */
+int  kg_get_counters(kg_ctx* ctx, int64_t out[3]);
+int64_t kg_device_bytes(kg_ctx* ctx);
 /* Host wall time in seconds since creation: out[0] inside kg_step/kg_integrate_to steps,
    out[1] of that blocked in stream synchronisations (the host waiting for the GPU),
    out[2] planning redistribution walks.  No reference counterpart. */

@@ -194,7 +194,10 @@ size_t bytes_per_slot(const kg_ctx& c) {
     size_t SC = c.SC;
     return sizeof(double) * (4 * 4 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * (size_t)c.SFX + 5 * (size_t)c.SFY + 2 * (size_t)c.SV) +
                              2 * SC + 5 * SC + SC + 9 * SC + GE_COUNT * (size_t)c.nE + 11 * SC + 2 * SC) +
-           8 * sizeof(int) + 2 + sizeof(int);
+           8 * sizeof(int) + 2 + sizeof(int) +
+           (c.prec == KG_PREC_FP32 ? 2 * (3 * sizeof(double) * SC + 6 * sizeof(float) * SC +
+                                          2 * sizeof(float) * ((size_t)c.SFX + (size_t)c.SFY))
+                                   : 0);
 }
 
 template <class T>
@@ -1721,6 +1724,19 @@ int kg_get_time(kg_ctx* c, double* t, double* dt) {
 }
 
 int64_t kg_kernel_launches(const kg_ctx* c) { return c ? c->launches : 0; }
+
+int kg_get_counters(kg_ctx* c, int64_t out[3]) {
+    if (!c || !out) return KG_ERR_PARAM;
+    out[0] = c->steps;
+    out[1] = c->rejected;
+    out[2] = c->cell_updates;
+    return KG_OK;
+}
+
+int64_t kg_device_bytes(kg_ctx* c) {
+    if (!c) return 0;
+    return (int64_t)bytes_per_slot(*c) * c->cap;
+}
 
 int kg_host_times(kg_ctx* c, double out[3]) {
     if (!c || !out) return KG_ERR_PARAM;

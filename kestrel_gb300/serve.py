@@ -1,0 +1,126 @@
+"""Served ensemble solves: a request loop with continuous batching over one Batch.
+
+Requests (run settings, terrain, arrival time) are admitted in arrival order while the
+batch has a free member slot and the HBM budget covers the request's worst-case device
+memory (every tile of its domain allocated); admitted requests join the running batch at
+the next step boundary, so their work overlaps on the device with the requests already
+there.  A finished request leaves the batch and returns its slot and budget.  Every
+member's arithmetic is independent of the others, so a request's result is the same
+alone and in any mix.
+"""
+from __future__ import annotations
+
+import collections
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .batch import Batch
+
+
+def slot_bytes(nX: int, nY: int, fp32: bool = True) -> int:
+    """Device bytes of one allocated tile (the engine's per-slot planes)."""
+    SC, SFX, SFY, SV, nE = nX * nY, (nX + 1) * nY, nX * (nY + 1), (nX + 1) * (nY + 1), max(nX, nY)
+    d = 16 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * SFX + 5 * SFY + 2 * SV) + 2 * SC + 5 * SC + SC + 9 * SC + 12 * nE + 11 * SC + 2 * SC
+    b = 8 * d + 8 * 4 + 2 + 4
+    if fp32:
+        b += 2 * (3 * 8 * SC + 6 * 4 * SC + 2 * 4 * (SFX + SFY))
+    return b
+
+
+def worst_case_bytes(p: abi.Params) -> int:
+    """Every tile allocated, plus the redistribution buffers and block lists (28 bytes per
+    cell) and 10% for the context's small arrays."""
+    n = p.nXtiles * p.nYtiles
+    cells = n * p.nXpertile * p.nYpertile
+    return int(1.1 * (n * slot_bytes(p.nXpertile, p.nYpertile) + 28 * cells))
+
+
+@dataclass
+class Request:
+    arrival: float
+    params: abi.Params
+    b0: np.ndarray | None = None
+    desc: dict = field(default_factory=dict)
+    admitted: float | None = None
+    done: float | None = None
+    result: dict | None = None
+    budget: int = 0
+
+
+def extract(sim) -> dict:
+    """The final state a request returns: time, volume sums, counters, and per active tile
+    the free surface, momenta, Hnpsi and bed."""
+    L = sim.lib
+    cnt = (C.c_int64 * 3)()
+    L.kg_get_counters(sim.h, cnt)
+    return {"time": sim.time[0], "volume": sim.volume(), "steps": cnt[0], "rejected": cnt[1], "cell_updates": cnt[2],
+            "state": {t: np.stack([sim.field(t, f) for f in (1, 2, 3, 4, 11)]) for t in sim.active_tiles()}}
+
+
+class Server:
+    def __init__(self, hbm_budget: float = 150e9, max_members: int = 256, clock=time.perf_counter, keep_state: bool = True):
+        self.budget = float(hbm_budget)
+        self.batch = Batch(max_members)
+        self.max_members = max_members
+        self.clock = clock
+        self.keep_state = keep_state
+
+    def run(self, requests: list[Request]) -> dict:
+        """Serve the requests (arrival times in seconds from now) to completion; returns the
+        report (latencies, throughput, occupancy)."""
+        b, L = self.batch, self.batch.L
+        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        queue: collections.deque = collections.deque()
+        running: dict[int, Request] = {}
+        used, peak_used, peak_members, steps = 0, 0, 0, 0
+        occupancy = []
+        t0 = self.clock()
+        while pending or queue or running:
+            now = self.clock() - t0
+            while pending and pending[0].arrival <= now:
+                queue.append(pending.popleft())
+            while queue and len(running) < self.max_members:
+                r = queue[0]
+                need = worst_case_bytes(r.params)
+                if need > self.budget:
+                    raise ValueError(f"a request needs {need / 1e9:.1f} GB, above the whole budget")
+                if used + need > self.budget:
+                    break
+                queue.popleft()
+                mid = b.add(r.params, r.b0)
+                r.admitted, r.budget = self.clock() - t0, need
+                running[mid] = r
+                used += need
+            peak_used = max(peak_used, used)
+            peak_members = max(peak_members, len(running))
+            if not running:
+                if pending:
+                    time.sleep(max(0.0, min(pending[0].arrival - (self.clock() - t0), 0.05)))
+                continue
+            b.step()
+            steps += 1
+            occupancy.append(len(running))
+            for mid in [m for m in running if b.finished(m)]:
+                r = running.pop(mid)
+                r.done = self.clock() - t0
+                res = extract(b.member(mid))
+                if not self.keep_state:
+                    res.pop("state")
+                r.result = res
+                b.remove(mid)
+                used -= r.budget
+        makespan = self.clock() - t0
+        lat = np.array([r.done - r.arrival for r in requests])
+        cu = sum(r.result["cell_updates"] for r in requests)
+        return {"requests": len(requests), "makespan_s": makespan, "latency_p50_s": float(np.percentile(lat, 50)),
+                "latency_p99_s": float(np.percentile(lat, 99)), "solves_per_s": len(requests) / makespan,
+                "cell_updates_per_s": cu / makespan, "cell_updates": cu, "batch_steps": steps,
+                "peak_members": peak_members, "peak_budget_gb": peak_used / 1e9,
+                "mean_members": float(np.mean(occupancy)) if occupancy else 0.0}
+
+    def close(self):
+        self.batch.close()

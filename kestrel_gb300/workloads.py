@@ -143,3 +143,112 @@ WORKLOADS = {
              "FP32 form (FP64 free surface, bed, mass/solids rows and dt); timed after a spin-up to t=120 s",
         params=morpho_flux_2048, prec=abi.PREC_FP32, spinup=120.0),
 }
+
+
+# ---- ensembles (the batched and served forms) ---------------------------------------
+
+DRAGS = ("Chezy", "Voellmy", "Manning")
+
+
+def ensemble_member(seed: int, side: int | None = None, tend: float | None = None, tile: int | None = None,
+                    side_range=(128, 1024), tend_range=(60.0, 600.0), dx: float = 5.0):
+    """One ensemble solve, drawn from `seed`: grid side log-uniform in side_range (rounded to
+    a multiple of 64 cells) unless given, dx = 5 m, its own seeded fractal terrain, a cap or
+    a flux source (half each) of volume log-uniform in [1e3, 1e6] m^3 placed 30% of the way
+    up the slope, drag drawn from Chezy / Voellmy / Manning with coefficients uniform over
+    physical ranges, morphodynamics on for half, sponge edges.  `tile` is the tile side (the
+    autotuner's choice; 64 by default).  Returns (params, b0, description dict)."""
+    rng = np.random.default_rng(seed)
+    if side is None:
+        side = int(round(math.exp(rng.uniform(math.log(side_range[0]), math.log(side_range[1]))) / 64.0)) * 64
+        side = max(64, side)
+    if tend is None:
+        tend = float(rng.uniform(*tend_range))
+    if not tile:
+        # largest tile side that leaves an interior of tiles (edge tiles never activate
+        # under sponge edges)
+        tile = max([t for t in (16, 32, 64) if side % t == 0 and side // t >= 4] or [16])
+    if side % tile:
+        raise ValueError(f"tile {tile} does not divide side {side}")
+    L = side * dx
+    volume = math.exp(rng.uniform(math.log(1e3), math.log(1e6)))
+    drag = DRAGS[int(rng.integers(0, 3))]
+    morpho = bool(rng.integers(0, 2))
+    y0 = -0.3 * L
+    if drag == "Chezy":
+        dtext = f"Drag = Chezy\nChezy Co = {rng.uniform(0.005, 0.05)!r}"
+    elif drag == "Voellmy":
+        dtext = f"Drag = Voellmy\nCoulomb Co = {rng.uniform(0.05, 0.3)!r}\nChezy Co = {9.81 / rng.uniform(200.0, 2000.0)!r}"
+    else:
+        dtext = f"Drag = Manning\nManning Co = {rng.uniform(0.02, 0.1)!r}"
+    if rng.integers(0, 2):
+        h = rng.uniform(1.0, 5.0)
+        r = math.sqrt(volume / (math.pi * h))
+        r = min(r, 0.12 * L)
+        h = volume / (math.pi * r * r)
+        stext = f"Cap:\n  capX = 0\n  capY = {y0!r}\n  capRadius = {r!r}\n  capHeight = {h!r}\n  capShape = flat\n  capConc = 0.2"
+        src = ("cap", r, h)
+    else:
+        T = rng.uniform(60.0, 300.0)
+        q = 2.0 * volume / T
+        stext = (f"Source:\n  sourceX = 0\n  sourceY = {y0!r}\n  sourceRadius = {2.5 * dx!r}\n"
+                 f"  sourceTime = (0,{T / 2!r},{T!r})\n  sourceFlux = (0,{q!r},0)\n  sourceConc = (0.2,0.2,0.2)")
+        src = ("flux", T, q)
+    mtext = (f"Erosion = On\nErosion Depth = {rng.uniform(0.5, 3.0)!r}" if morpho else "Erosion = Off")
+    text = f"""
+Domain:
+nXtiles = {side // tile}
+nYtiles = {side // tile}
+nXpertile = {tile}
+nYpertile = {tile}
+Xtilesize = {tile * dx!r}
+Boundary Conditions = sponge
+{stext}
+Parameters:
+{dtext}
+{mtext}
+Solver:
+T end = {tend!r}
+cfl = 0.25
+Output:
+N out = 1
+Topog:
+Type = Function
+Topog function = flat
+"""
+    p = config.parse(text).params
+    p.topog = abi.TOPO["upload"]
+    b0 = fractal_terrain(side + 1, side + 1, dx, seed + 7919)
+    return p, b0, dict(seed=seed, side=side, tile=tile, tend=tend, volume=volume, drag=drag, morpho=morpho, source=src)
+
+
+def ensemble(n: int = 256, seed: int = 2024, tiles=None, **kw):
+    """The batched ensemble of n members (seeds seed .. seed + n - 1); `tiles` maps a grid
+    side to its tile side (a dict, or a function such as the autotuner's choice)."""
+    out = []
+    for k in range(n):
+        side = None
+        rng = np.random.default_rng(seed + k)
+        lo, hi = kw.get("side_range", (128, 1024))
+        side = max(64, int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))) / 64.0)) * 64)
+        tile = tiles(side) if callable(tiles) else (tiles or {}).get(side)
+        out.append(ensemble_member(seed + k, side=side, tile=tile, **{k2: v for k2, v in kw.items() if k2 != "side_range"}))
+    return out
+
+
+def serve_requests(n: int, rate: float = 20.0, seed: int = 77, sides=(256, 512, 1024, 2048), tend_range=(60.0, 600.0),
+                   tiles=None):
+    """A served request stream: Poisson arrivals at `rate` per second, grid sides uniform
+    over `sides`, end times uniform over tend_range, everything else as the ensemble.
+    Returns [(arrival_s, params, b0, desc)]."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for k in range(n):
+        t += float(rng.exponential(1.0 / rate))
+        side = int(sides[int(rng.integers(0, len(sides)))])
+        tend = float(rng.uniform(*tend_range))
+        tile = tiles(side) if callable(tiles) else (tiles or {}).get(side)
+        p, b0, d = ensemble_member(seed * 1000 + k, side=side, tend=tend, tile=tile)
+        out.append((t, p, b0, d))
+    return out

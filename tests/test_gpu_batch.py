@@ -71,3 +71,30 @@ def test_batch_late_join_and_leave():
     same(snapshot(b.member(a0)), ref[0])
     same(snapshot(b.member(a2)), ref[2])
     b.close()
+
+
+def test_served_requests_same_alone_and_mixed():
+    """Continuous batching: requests arriving together overlap on the device, are admitted
+    as memory frees up (a budget that fits two at a time), and each result equals the same
+    request served alone."""
+    from kestrel_gb300 import serve, workloads
+    reqs = []
+    for k, (side, tend) in enumerate([(256, 6.0), (128, 4.0), (256, 3.0), (192, 5.0)]):
+        p, b0, d = workloads.ensemble_member(900 + k, side=side, tend=tend)
+        reqs.append(serve.Request(arrival=0.0, params=p, b0=b0, desc=d))
+    budget = 2.05 * max(serve.worst_case_bytes(r.params) for r in reqs)
+    srv = serve.Server(hbm_budget=budget, max_members=4)
+    rep = srv.run(reqs)
+    srv.close()
+    assert rep["peak_members"] <= 2 and rep["requests"] == 4
+    for r in reqs:
+        solo = serve.Server(hbm_budget=budget, max_members=1)
+        one = serve.Request(arrival=0.0, params=r.params, b0=r.b0)
+        solo.run([one])
+        solo.close()
+        a, b = r.result, one.result
+        assert a["time"] == b["time"] and a["steps"] == b["steps"] and a["rejected"] == b["rejected"]
+        assert np.array_equal(a["volume"], b["volume"])
+        assert a["state"].keys() == b["state"].keys()
+        for t in a["state"]:
+            assert np.array_equal(a["state"][t], b["state"][t])
