@@ -527,7 +527,7 @@ cudaError_t launch_hydro32(const DevArrays& A, const BlockDesc* blocks, int nblo
 cudaError_t launch_topo32(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, cudaStream_t st) {
     int items = (nX + 1) * (nY + 1);
     int per = (items + 255) / 256;
-    if (n == 0) return cudaSuccess;
+    if (n <= 0) return cudaSuccess;
     k_topo32<<<n * per, 256, 0, st>>>(A, d_slots, ts, per);
     return cudaGetLastError();
 }

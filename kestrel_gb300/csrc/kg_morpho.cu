@@ -505,28 +505,33 @@ static inline int per_of(int items) { return (items + 255) / 256; }
 
 cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, int* ctl_flags,
                           cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
     k_m_init<<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, ctl_flags);
     return cudaGetLastError();
 }
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
     if (fp32) k_m_emd<float><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, tnew);
     else k_m_emd<double><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, tnew);
     return cudaGetLastError();
 }
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
                         bool fp32, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
     if (fp32) k_m_bt<true><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
     else k_m_bt<false><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
     return cudaGetLastError();
 }
 cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, bool fp32,
                            cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
     if (fp32) k_m_cells<true><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
     else k_m_cells<false><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
     return cudaGetLastError();
 }
 cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
                            unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
     k_m_check<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
     return cudaGetLastError();
 }
@@ -537,6 +542,7 @@ cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, co
     return cudaGetLastError();
 }
 cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
     k_m_finish<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa);
     return cudaGetLastError();
 }

@@ -154,8 +154,8 @@ def ensemble_member(seed: int, side: int | None = None, tend: float | None = Non
                     side_range=(128, 1024), tend_range=(60.0, 600.0), dx: float = 5.0):
     """One ensemble solve, drawn from `seed`: grid side log-uniform in side_range (rounded to
     a multiple of 64 cells) unless given, dx = 5 m, its own seeded fractal terrain, a cap or
-    a flux source (half each) of volume log-uniform in [1e3, 1e6] m^3 placed 30% of the way
-    up the slope, drag drawn from Chezy / Voellmy / Manning with coefficients uniform over
+    a flux source (half each) of volume log-uniform in [1e3, 1e6] m^3 placed 20% of the way
+    from the centre to the upper (southern) edge, always inside an interior tile row, drag drawn from Chezy / Voellmy / Manning with coefficients uniform over
     physical ranges, morphodynamics on for half, sponge edges.  `tile` is the tile side (the
     autotuner's choice; 64 by default).  Returns (params, b0, description dict)."""
     rng = np.random.default_rng(seed)
@@ -174,7 +174,7 @@ def ensemble_member(seed: int, side: int | None = None, tend: float | None = Non
     volume = math.exp(rng.uniform(math.log(1e3), math.log(1e6)))
     drag = DRAGS[int(rng.integers(0, 3))]
     morpho = bool(rng.integers(0, 2))
-    y0 = -0.3 * L
+    y0 = -0.2 * L
     if drag == "Chezy":
         dtext = f"Drag = Chezy\nChezy Co = {rng.uniform(0.005, 0.05)!r}"
     elif drag == "Voellmy":
