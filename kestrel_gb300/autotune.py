@@ -26,10 +26,11 @@ def candidates(side: int):
     return [t for t in CANDIDATES if side % t == 0 and side // t >= 4]
 
 
-def trial(side: int, tile: int, t_sim: float = 10.0, seed: int = 4242) -> float:
-    """Wall seconds per simulated second of one representative member (cap of 1e5 m^3,
-    Voellmy drag, no erosion) integrated to t_sim."""
-    p, b0, _ = workloads.ensemble_member(seed, side=side, tend=t_sim, tile=tile)
+def trial(side: int, tile: int, t_sim: float = 10.0, seed: int = 4242, max_wall: float = 3.0) -> float:
+    """Wall seconds per simulated second of one representative member (a cap of 1e5 m^3,
+    Voellmy drag, no erosion), integrated towards t_sim for at most max_wall seconds."""
+    p, b0, _ = workloads.ensemble_member(seed, side=side, tend=t_sim, tile=tile, volume=1e5, drag="Voellmy",
+                                         morpho=False, kind="cap")
     b = Batch(1)
     try:
         b.add(p, b0)
@@ -37,7 +38,7 @@ def trial(side: int, tile: int, t_sim: float = 10.0, seed: int = 4242) -> float:
         t0 = time.perf_counter()
         sim = b.member(0)
         t_start = sim.time[0]
-        while b.step() > 0:
+        while b.step() > 0 and time.perf_counter() - t0 < max_wall:
             pass
         dt_sim = max(sim.time[0] - t_start, 1e-9)
         return (time.perf_counter() - t0) / dt_sim

@@ -151,13 +151,18 @@ DRAGS = ("Chezy", "Voellmy", "Manning")
 
 
 def ensemble_member(seed: int, side: int | None = None, tend: float | None = None, tile: int | None = None,
-                    side_range=(128, 1024), tend_range=(60.0, 600.0), dx: float = 5.0):
+                    side_range=(128, 1024), tend_range=(60.0, 600.0), dx: float = 5.0, volume: float | None = None,
+                    drag: str | None = None, morpho: bool | None = None, kind: str | None = None):
     """One ensemble solve, drawn from `seed`: grid side log-uniform in side_range (rounded to
     a multiple of 64 cells) unless given, dx = 5 m, its own seeded fractal terrain, a cap or
     a flux source (half each) of volume log-uniform in [1e3, 1e6] m^3 placed 20% of the way
     from the centre to the upper (southern) edge, always inside an interior tile row, drag drawn from Chezy / Voellmy / Manning with coefficients uniform over
-    physical ranges, morphodynamics on for half, sponge edges.  `tile` is the tile side (the
-    autotuner's choice; 64 by default).  Returns (params, b0, description dict)."""
+    physical ranges, morphodynamics on for half, sponge edges.  The terrain's relief scales
+    with the domain (800 m over the 10.24 km of the 2048^2 configuration; the 8-degree tilt
+    is kept), so every size sees the same slopes.  `tile` is the tile side (the
+    autotuner's choice; by default the largest that leaves interior tiles); volume / drag /
+    morpho / kind ("cap" or "flux") override the draws.  Returns (params, b0, description
+    dict)."""
     rng = np.random.default_rng(seed)
     if side is None:
         side = int(round(math.exp(rng.uniform(math.log(side_range[0]), math.log(side_range[1]))) / 64.0)) * 64
@@ -171,9 +176,12 @@ def ensemble_member(seed: int, side: int | None = None, tend: float | None = Non
     if side % tile:
         raise ValueError(f"tile {tile} does not divide side {side}")
     L = side * dx
-    volume = math.exp(rng.uniform(math.log(1e3), math.log(1e6)))
-    drag = DRAGS[int(rng.integers(0, 3))]
-    morpho = bool(rng.integers(0, 2))
+    v_draw = math.exp(rng.uniform(math.log(1e3), math.log(1e6)))
+    d_draw = DRAGS[int(rng.integers(0, 3))]
+    m_draw = bool(rng.integers(0, 2))
+    volume = v_draw if volume is None else volume
+    drag = d_draw if drag is None else drag
+    morpho = m_draw if morpho is None else morpho
     y0 = -0.2 * L
     if drag == "Chezy":
         dtext = f"Drag = Chezy\nChezy Co = {rng.uniform(0.005, 0.05)!r}"
@@ -181,7 +189,8 @@ def ensemble_member(seed: int, side: int | None = None, tend: float | None = Non
         dtext = f"Drag = Voellmy\nCoulomb Co = {rng.uniform(0.05, 0.3)!r}\nChezy Co = {9.81 / rng.uniform(200.0, 2000.0)!r}"
     else:
         dtext = f"Drag = Manning\nManning Co = {rng.uniform(0.02, 0.1)!r}"
-    if rng.integers(0, 2):
+    k_draw = "cap" if rng.integers(0, 2) else "flux"
+    if (kind or k_draw) == "cap":
         h = rng.uniform(1.0, 5.0)
         r = math.sqrt(volume / (math.pi * h))
         r = min(r, 0.12 * L)
@@ -218,7 +227,7 @@ Topog function = flat
 """
     p = config.parse(text).params
     p.topog = abi.TOPO["upload"]
-    b0 = fractal_terrain(side + 1, side + 1, dx, seed + 7919)
+    b0 = fractal_terrain(side + 1, side + 1, dx, seed + 7919, relief=800.0 * min(1.0, L / 10240.0))
     return p, b0, dict(seed=seed, side=side, tile=tile, tend=tend, volume=volume, drag=drag, morpho=morpho, source=src)
 
 

@@ -79,14 +79,14 @@ def test_served_requests_same_alone_and_mixed():
     request served alone."""
     from kestrel_gb300 import serve, workloads
     reqs = []
-    for k, (side, tend) in enumerate([(256, 6.0), (128, 4.0), (256, 3.0), (192, 5.0)]):
+    for k, (side, tend) in enumerate([(256, 6.0), (256, 4.0), (256, 3.0), (256, 5.0)]):
         p, b0, d = workloads.ensemble_member(900 + k, side=side, tend=tend)
         reqs.append(serve.Request(arrival=0.0, params=p, b0=b0, desc=d))
-    budget = 2.05 * max(serve.worst_case_bytes(r.params) for r in reqs)
+    budget = 2.05 * serve.worst_case_bytes(reqs[0].params)  # equal sides and tiles: two fit
     srv = serve.Server(hbm_budget=budget, max_members=4)
     rep = srv.run(reqs)
     srv.close()
-    assert rep["peak_members"] <= 2 and rep["requests"] == 4
+    assert rep["peak_members"] == 2 and rep["requests"] == 4, rep
     for r in reqs:
         solo = serve.Server(hbm_budget=budget, max_members=1)
         one = serve.Request(arrival=0.0, params=r.params, b0=r.b0)
