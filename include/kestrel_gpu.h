@@ -258,9 +258,10 @@ int  kg_batch_add(kg_batch* b, const kg_params* params, const double* b0, int64_
    kg_get_time, ...) work on it.  Do not step or destroy it directly. */
 kg_ctx* kg_batch_member(kg_batch* b, int32_t id);
 int  kg_batch_remove(kg_batch* b, int32_t id);
-/* One accepted step (IntegrateTo's, src/TimeStepper.f90:151-275) of every member that has
-   not reached its end time, through its output intervals as kg_run takes them; live
-   receives the number of members still running. */
+/* One round of every member that has not reached its end time: each advances its current
+   step (IntegrateTo's, src/TimeStepper.f90:151-275, through its output intervals as
+   kg_run takes them) by one phase, at most completing it; members at the same stage share
+   the batched launches.  live receives the number of members still running. */
 int  kg_batch_step(kg_batch* b, int32_t* live);
 int  kg_batch_finished(kg_batch* b, int32_t id, int32_t* finished);
 int  kg_batch_stats(kg_batch* b, int64_t* launches, int64_t* rounds);

@@ -26,7 +26,7 @@ def candidates(side: int):
     return [t for t in CANDIDATES if side % t == 0 and side // t >= 4]
 
 
-def trial(side: int, tile: int, t_sim: float = 10.0, seed: int = 4242, max_wall: float = 3.0) -> float:
+def trial(side: int, tile: int, t_sim: float = 30.0, seed: int = 4242, max_wall: float = 3.0) -> float:
     """Wall seconds per simulated second of one representative member (a cap of 1e5 m^3,
     Voellmy drag, no erosion), integrated towards t_sim for at most max_wall seconds."""
     p, b0, _ = workloads.ensemble_member(seed, side=side, tend=t_sim, tile=tile, volume=1e5, drag="Voellmy",
@@ -46,7 +46,7 @@ def trial(side: int, tile: int, t_sim: float = 10.0, seed: int = 4242, max_wall:
         b.close()
 
 
-def tune(classes=CLASSES, t_sim: float = 10.0, cache: str | None = None, log=None) -> dict:
+def tune(classes=CLASSES, t_sim: float = 30.0, cache: str | None = None, log=None) -> dict:
     """{class side: best tile side}; read from / written to `cache` (JSON) when given."""
     if cache and os.path.exists(cache):
         with open(cache) as f:

@@ -1,8 +1,8 @@
 // kg_batch.cu -- many simulations advanced together (the batched ensemble form).
 //
 // A batch owns FP32-form simulations of any grid and tile size on one CUDA stream.
-// kg_batch_step advances every live member by one accepted step of IntegrateTo
-// (src/TimeStepper.f90:151-275).  The hydraulic passes of all members that are at the
+// kg_batch_step advances every live member by one round of its current step of
+// IntegrateTo (src/TimeStepper.f90:151-275).  The hydraulic passes of all members that are at the
 // same stage run as ONE persistent launch over the packed list of their tile blocks
 // (k_hydro32_batch: each CTA walks the list with a grid stride and finds its member by a
 // binary search of the block offsets); the step's dt selection and the edge-band flags are
@@ -91,6 +91,71 @@ __global__ void __launch_bounds__(256) k_act_flags_batch(const SimStatic* __rest
     }
 }
 
+// The morphodynamic operator's per-tile steps for many members in one launch each: job j
+// covers member jobs[j].member's active tiles with `per` CTAs per tile (enough for its
+// vertices, cells and faces); each CTA runs the same per-item body the single-simulation
+// kernel runs, with the member's settings.
+struct MJob {
+    int member, per, qa, tcur, tnew, cap;
+    double dt;
+    int* flags;  // the member's M refine flag; the candidate count follows it
+    unsigned long long* keys;
+    double* ex;
+};
+enum MKind { MK_INIT, MK_EMD, MK_BT, MK_CELLS, MK_CHECK, MK_FACE, MK_BI, MK_FINISH, MK_TOPO };
+
+template <int K>
+__global__ void __launch_bounds__(256) k_m_batch(const SimStatic* __restrict__ sims, const MJob* __restrict__ jobs,
+                                                 const int* __restrict__ prefix, int njobs, int total, int stage) {
+    for (int b = blockIdx.x; b < total; b += gridDim.x) {
+        int lo = 0, hi = njobs - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (prefix[mid] <= b) lo = mid;
+            else hi = mid - 1;
+        }
+        const MJob& J = jobs[lo];
+        const SimStatic& X = sims[J.member];
+        int local = b - prefix[lo], pos = local / J.per, item = (local % J.per) * 256 + threadIdx.x;
+        int s = X.slots[pos];
+        if (K == MK_INIT) {
+            if (local == 0 && threadIdx.x < 2) J.flags[threadIdx.x] = 0;
+            m_init(X.P, X.A, s, item, J.qa, J.tcur, J.tnew);
+        } else if (K == MK_EMD) {
+            m_emd<float>(X.P, X.F, X.A, s, item, J.tnew);
+        } else if (K == MK_BT) {
+            m_bt<true>(X.P, X.A, s, item, J.tcur, J.tnew, stage, J.dt);
+        } else if (K == MK_CELLS) {
+            m_cells<true>(X.P, X.F, X.A, s, item, J.qa, J.tcur, J.tnew);
+        } else if (K == MK_CHECK) {
+            m_check(X.P, X.A, s, item, pos, J.qa, J.tcur, J.tnew, J.flags, J.keys, J.ex, J.flags + 1, J.cap);
+        } else if (K == MK_FACE) {
+            face_topo<true>(X.P, X.A, s, item, J.tnew);
+        } else if (K == MK_BI) {
+            face_bI(X.P, X.A, s, item, J.tnew);
+        } else if (K == MK_FINISH) {
+            m_finish(X.P, X.A, s, item, J.qa);
+        } else {
+            topo32(X.P, X.A, s, item, J.tnew);
+        }
+    }
+}
+
+// RedistributeGrid of every member that has a list: one CTA per member.
+struct RJob {
+    int member, qa, tcur, tnew, nwaves;
+    const int* list_slot;
+    const int* list_cell;
+    const int* wave_off;
+    int* flags;
+};
+__global__ void __launch_bounds__(REDIST_THREADS) k_m_redist_batch(const SimStatic* __restrict__ sims,
+                                                                   const RJob* __restrict__ jobs) {
+    const RJob& J = jobs[blockIdx.x];
+    const SimStatic& X = sims[J.member];
+    m_redist(X.P, X.A, J.list_slot, J.list_cell, J.wave_off, J.nwaves, J.qa, J.tcur, J.tnew, J.flags);
+}
+
 }  // namespace kg
 
 namespace {
@@ -129,6 +194,13 @@ struct kg_batch {
     kg::DtJob* d_dt = nullptr;
     kg::ActJob* h_act = nullptr;
     kg::ActJob* d_act = nullptr;
+    kg::MJob* h_mjob = nullptr;         // [2][cap]: the M jobs before and after the checks
+    kg::MJob* d_mjob = nullptr;
+    int* h_mpre = nullptr;              // [2][cap + 1]
+    int* d_mpre = nullptr;
+    kg::RJob* h_rjob = nullptr;
+    kg::RJob* d_rjob = nullptr;
+    int grid_m = 0;
     int* d_actout = nullptr;
     int* h_actout = nullptr;
     int actout_cap = 0;
@@ -382,26 +454,44 @@ void phase_h(kg_batch& b, const std::vector<int>& who) {
     }
 }
 
-// Phase M: the morphodynamic operator of every listed member, its checks and
-// redistribution, then the batched RHS check and second H.
+// Upload M job table t (0: the operator and its checks, 1: after the checks).
+int upload_mjobs(kg_batch& b, int t, const std::vector<int>& who) {
+    MJob* hj = b.h_mjob + (size_t)t * b.cap;
+    int* hp = b.h_mpre + (size_t)t * (b.cap + 1);
+    int total = 0;
+    for (size_t k = 0; k < who.size(); ++k) {
+        Member& m = b.mem[(size_t)who[k]];
+        kg_ctx& c = *m.c;
+        int per = (c.SV + 255) / 256;
+        hj[k] = MJob{who[k], per, m.o[0], c.tcur, m.tnew, c.cand_cap, m.dt_m, c.d_mflags, c.d_ckey, c.d_cex};
+        hp[k] = total;
+        total += (int)c.active.size() * per;
+    }
+    CK(cudaMemcpyAsync(b.d_mjob + (size_t)t * b.cap, hj, who.size() * sizeof(MJob), cudaMemcpyHostToDevice, b.st));
+    CK(cudaMemcpyAsync(b.d_mpre + (size_t)t * (b.cap + 1), hp, who.size() * sizeof(int), cudaMemcpyHostToDevice, b.st));
+    return total;
+}
+template <int K>
+void launch_m(kg_batch& b, int t, int n, int total, int stage = 0) {
+    if (n == 0 || total == 0) return;
+    k_m_batch<K><<<std::min(total, b.grid_m), 256, 0, b.st>>>(b.d_static, b.d_mjob + (size_t)t * b.cap,
+                                                             b.d_mpre + (size_t)t * (b.cap + 1), n, total, stage);
+    CK(cudaGetLastError());
+    b.launches++;
+}
+
+// Phase M: the morphodynamic operator of every listed member (one launch per step kind
+// for all of them), its checks and redistribution, then the batched RHS check and second
+// H.
 void phase_m(kg_batch& b, const std::vector<int>& who) {
     reset_ctl(b);
     for (int id : who) {
         Member& m = b.mem[(size_t)id];
         kg_ctx& c = *m.c;
-        bind_constants(c);
         m.dt_m = 2.0 * m.dt;
         m.slots.clear();
         for (int t : c.active) m.slots.push_back(T(c, t).slot);
-        int n = (int)m.slots.size();
-        const bool fp32 = c.prec == KG_PREC_FP32;
-        CK(launch_m_init(c.A, c.d_active, n, c.SV, m.o[0], c.tcur, m.tnew, c.d_mflags, c.st));
-        for (int stage = 1; stage <= 3; ++stage) {
-            CK(launch_m_emd(c.A, c.d_active, n, c.SC, m.tnew, fp32, c.st));
-            CK(launch_m_bt(c.A, c.d_active, n, c.SV, c.tcur, m.tnew, stage, m.dt_m, fp32, c.st));
-            CK(launch_m_cells(c.A, c.d_active, n, c.SC, m.o[0], c.tcur, m.tnew, fp32, c.st));
-        }
-        int need = n * c.SC;
+        int need = (int)m.slots.size() * c.SC;
         if (need > c.cand_cap) {
             cudaFree(c.d_ckey); cudaFree(c.d_cex); cudaFree(c.d_rslot); cudaFree(c.d_rcell); cudaFree(c.d_rwave);
             c.cand_cap = std::max(need, 2 * c.cand_cap);
@@ -411,10 +501,17 @@ void phase_m(kg_batch& b, const std::vector<int>& who) {
             CK(cudaMalloc(&c.d_rcell, (size_t)c.cand_cap * sizeof(int)));
             CK(cudaMalloc(&c.d_rwave, ((size_t)c.cand_cap + 1) * sizeof(int)));
         }
-        CK(launch_m_check(c.A, c.d_active, n, c.SC, m.o[0], c.tcur, m.tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, c.st));
         c.launches += 11;
-        b.launches += 11;
     }
+    int n = (int)who.size();
+    int total = upload_mjobs(b, 0, who);
+    launch_m<MK_INIT>(b, 0, n, total);
+    for (int stage = 1; stage <= 3; ++stage) {
+        launch_m<MK_EMD>(b, 0, n, total);
+        launch_m<MK_BT>(b, 0, n, total, stage);
+        launch_m<MK_CELLS>(b, 0, n, total);
+    }
+    launch_m<MK_CHECK>(b, 0, n, total);
     collect_ctl(b);
     std::vector<int> go, listed;
     for (int id : who) {
@@ -445,7 +542,6 @@ void phase_m(kg_batch& b, const std::vector<int>& who) {
     for (size_t k = 0; k < listed.size(); ++k) {
         Member& m = b.mem[(size_t)listed[k]];
         kg_ctx& c = *m.c;
-        bind_constants(c);
         const auto& key = keys[k];
         const auto& ex = exs[k];
         int ncand = m.ncand;
@@ -464,25 +560,41 @@ void phase_m(kg_batch& b, const std::vector<int>& who) {
         CK(cudaMemcpyAsync(c.d_rslot, ls.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
-        CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, c.d_rwave, nw, m.o[0], c.tcur, m.tnew, c.d_mflags, c.st));
+        b.h_rjob[k] = RJob{listed[k], m.o[0], c.tcur, m.tnew, nw, c.d_rslot, c.d_rcell, c.d_rwave, c.d_mflags};
         c.launches++;
+    }
+    if (!listed.empty()) {
+        CK(cudaMemcpyAsync(b.d_rjob, b.h_rjob, listed.size() * sizeof(RJob), cudaMemcpyHostToDevice, b.st));
+        k_m_redist_batch<<<(int)listed.size(), REDIST_THREADS, 0, b.st>>>(b.d_static, b.d_rjob);
+        CK(cudaGetLastError());
         b.launches++;
     }
     if (go.empty()) return;
+    // Interfacial topography of the new bed and the M result, for every member at once.
+    int ng = (int)go.size();
+    int tg = upload_mjobs(b, 1, go);
+    launch_m<MK_FACE>(b, 1, ng, tg);
+    launch_m<MK_BI>(b, 1, ng, tg);
+    launch_m<MK_FINISH>(b, 1, ng, tg);
+    std::vector<int> whole;
+    for (int id : go) {
+        Member& m = b.mem[(size_t)id];
+        kg_ctx& c = *m.c;
+        c.launches += 3;
+        c.tdirty[m.tnew] = std::max(c.tdirty[m.tnew], 1);
+        if (c.tdirty[m.tnew] > 1) whole.push_back(id);
+    }
+    launch_m<MK_TOPO>(b, 1, ng, tg);  // the active tiles' factors of every member
+    for (int id : whole) {            // ghost factors too where they were never built
+        kg_ctx& c = *b.mem[(size_t)id].c;
+        bind_constants(c);
+        refresh_topo32(c, b.mem[(size_t)id].tnew);
+    }
     std::vector<StepArgs> ra;
     for (int id : go) {
         Member& m = b.mem[(size_t)id];
         kg_ctx& c = *m.c;
-        bind_constants(c);
-        int n = (int)m.slots.size();
-        const bool fp32 = c.prec == KG_PREC_FP32;
-        CK(launch_face_topo(c.A, c.d_active, n, m.tnew, c.nX, c.nY, fp32, c.st));
-        CK(launch_face_bI(c.A, c.d_active, n, m.tnew, c.nX, c.nY, c.st));
-        CK(launch_m_finish(c.A, c.d_active, n, c.SC, m.o[0], c.st));
-        c.launches += 3;
-        b.launches += 3;
-        c.tdirty[m.tnew] = std::max(c.tdirty[m.tnew], 1);
-        if (fp32) refresh_topo32(c, m.tnew);
+        c.tdirty[m.tnew] = 0;
         c.t = c.t0 + m.dt;
         c.dt = m.dt;
         ra.push_back(member_args(c, rhs_args(c, m.o[0], 1, m.tnew, c.t), W_RHS));
@@ -544,39 +656,37 @@ void prepare(kg_batch& b, Member& m) {
     (void)b;
 }
 
-// One accepted step of every live member.
+// One round: every live member advances its own step by one phase.  A member whose
+// previous step is complete starts the next one (prepare), members at the first H (fresh
+// or retrying) share the batched H phase, and members whose first H was accepted share
+// the M phase; a member that completes its step starts the next one in the next round,
+// so no member waits for another's retries.
 void batch_step(kg_batch& b) {
     std::vector<int> live;
     for (int i = 0; i < b.cap; ++i)
         if (b.mem[(size_t)i].c && !b.mem[(size_t)i].finished) live.push_back(i);
     for (int id : live) {
         Member& m = b.mem[(size_t)id];
+        if (m.state != ST_DONE) continue;
         // kg_integrate_to skips an interval that is already reached
         int Nout = m.c->p.Nout > 0 ? m.c->p.Nout : 100;
         while (!m.finished && m.c->t >= m.c->p.tstart + m.next_out * m.c->DeltaT) {
             m.next_out++;
             if (m.next_out > Nout) m.finished = true;
         }
+        if (!m.finished) prepare(b, m);
     }
-    std::vector<int> run;
-    for (int id : live)
-        if (!b.mem[(size_t)id].finished) {
-            prepare(b, b.mem[(size_t)id]);
-            run.push_back(id);
-        }
     refresh_static(b);
-    while (true) {
-        std::vector<int> h, mm;
-        for (int id : run) {
-            int s = b.mem[(size_t)id].state;
-            if (s == ST_FRESH || s == ST_H1) h.push_back(id);
-            else if (s == ST_M) mm.push_back(id);
-        }
-        if (h.empty() && mm.empty()) break;
-        if (!h.empty()) phase_h(b, h);
-        if (!mm.empty()) phase_m(b, mm);
-        b.rounds++;
+    std::vector<int> h, mm;
+    for (int id : live) {
+        int s = b.mem[(size_t)id].state;
+        if (!b.mem[(size_t)id].finished && (s == ST_FRESH || s == ST_H1)) h.push_back(id);
     }
+    if (!h.empty()) phase_h(b, h);
+    for (int id : live)
+        if (b.mem[(size_t)id].state == ST_M) mm.push_back(id);
+    if (!mm.empty()) phase_m(b, mm);
+    b.rounds++;
 }
 
 }  // namespace
@@ -609,6 +719,12 @@ int kg_batch_create(int32_t max_members, kg_batch** out) {
         CK(cudaMalloc(&b->d_dt, (size_t)max_members * sizeof(DtJob)));
         CK(cudaMallocHost(&b->h_act, (size_t)max_members * sizeof(ActJob)));
         CK(cudaMalloc(&b->d_act, (size_t)max_members * sizeof(ActJob)));
+        CK(cudaMallocHost(&b->h_mjob, (size_t)2 * max_members * sizeof(MJob)));
+        CK(cudaMalloc(&b->d_mjob, (size_t)2 * max_members * sizeof(MJob)));
+        CK(cudaMallocHost(&b->h_mpre, (size_t)2 * (max_members + 1) * sizeof(int)));
+        CK(cudaMalloc(&b->d_mpre, (size_t)2 * (max_members + 1) * sizeof(int)));
+        CK(cudaMallocHost(&b->h_rjob, (size_t)max_members * sizeof(RJob)));
+        CK(cudaMalloc(&b->d_rjob, (size_t)max_members * sizeof(RJob)));
         CK(cudaFuncSetAttribute(k_hydro32_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Hydro32Smem)));
         int dev = 0, sms = 0, occ = 0, occa = 0;
         CK(cudaGetDevice(&dev));
@@ -616,6 +732,9 @@ int kg_batch_create(int32_t max_members, kg_batch** out) {
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_hydro32_batch, NT, sizeof(Hydro32Smem)));
         CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occa, k_act_flags_batch, 256, 0));
         b->grid_hydro = sms * std::max(occ, 1);
+        int occm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occm, k_m_batch<MK_CELLS>, 256, 0));
+        b->grid_m = sms * std::max(occm, 1);
         b->grid_act = sms * std::max(occa, 1);
     } catch (const KgError& e) {
         int code = e.code;
@@ -737,6 +856,12 @@ void kg_batch_destroy(kg_batch* b) {
     cudaFree(b->d_idx);
     cudaFree(b->d_dt);
     cudaFree(b->d_act);
+    cudaFree(b->d_mjob);
+    cudaFree(b->d_mpre);
+    cudaFree(b->d_rjob);
+    if (b->h_mjob) cudaFreeHost(b->h_mjob);
+    if (b->h_mpre) cudaFreeHost(b->h_mpre);
+    if (b->h_rjob) cudaFreeHost(b->h_rjob);
     cudaFree(b->d_actout);
     if (b->h_ctl) cudaFreeHost(b->h_ctl);
     if (b->h_args) cudaFreeHost(b->h_args);

@@ -452,11 +452,8 @@ __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __
 // and face topography (FP32 factors from FP32 slopes; 1/gam^2 and 1/gam to FP64 accuracy) (gam = sqrt(1 + b_x^2 + b_y^2), src/Closures.f90:174-186; the
 // hydrostatic prefactors of ConstructHydraulicRHS, src/HydraulicRHS.f90:1236-1250; the
 // wave-speed factor (1 + b_t^2)/gam^3 of src/Equations.f90:249-381).
-__global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restrict__ slots, int ts, int per) {
-    const DevParams& P = cP;
+__device__ __forceinline__ void topo32(const DevParams& P, const DevArrays& A, int s, int k, int ts) {
     const int nX = P.nX, nY = P.nY, SC = nX * nY, SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
-    int s = slots[blockIdx.x / per];
-    int k = (blockIdx.x % per) * 256 + threadIdx.x;
     if (k < SC) {
         const double* ct = A.CT[ts] + plane(s, 4, 0, SC) + k;
         double b0 = ct[0], bt = ct[SC], bx = ct[2 * (size_t)SC], by = ct[3 * (size_t)SC];
@@ -508,6 +505,10 @@ __global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restri
         o[0] = g;
         o[SFY] = P.geo ? (1.f + bx * bx) / (g * g * g) : 1.f;
     }
+}
+
+__global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restrict__ slots, int ts, int per) {
+    topo32(cP, A, slots[blockIdx.x / per], (blockIdx.x % per) * 256 + threadIdx.x, ts);
 }
 
 size_t hydro32_smem_bytes() { return sizeof(Hydro32Smem); }

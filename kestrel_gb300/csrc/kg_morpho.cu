@@ -28,21 +28,15 @@ constexpr int REDIST_THREADS = 512;
 
 __device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return ((size_t)slot * nf + f) * (size_t)npl; }
 
+// Each step below is a per-item body (settings P / F, arrays A, slot s, item item_ of
+// the tile, the tile's list position pos) called by a single-simulation kernel, which
+// reads the constant bank, and by the batched kernels of kg_batch.cu, which read a
+// per-member table.
+
 // Copy the step-start bed into the M set and fill the stage state of im0 (the state the
 // first hydraulic step produced).
-// Grid: one thread per cell / vertex, `per` CTAs of 256 threads per listed tile.
-#define KG_TILE_THREAD(NITEMS)                              \
-    int per_ = ((NITEMS) + 255) / 256;                      \
-    int s = slots[blockIdx.x / per_];                       \
-    int item_ = (blockIdx.x % per_) * 256 + threadIdx.x;
-
-// ctl_flags[0..1]: the M refine flag and the candidate count, zeroed here for k_m_check.
-__global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew,
-                                                int* ctl_flags) {
-    const DevParams& P = cP;
-    if (blockIdx.x == 0 && threadIdx.x < 2) ctl_flags[threadIdx.x] = 0;
+__device__ __forceinline__ void m_init(const DevParams& P, const DevArrays& A, int s, int item_, int qa, int tcur, int tnew) {
     int SC = P.nX * P.nY, SV = (P.nX + 1) * (P.nY + 1);
-    KG_TILE_THREAD(SV)
     if (item_ < SV) {
         int v = item_;
         A.BV[tnew][mp(s, 2, 0, SV) + v] = A.BV[tcur][mp(s, 2, 0, SV) + v];
@@ -80,10 +74,8 @@ __device__ __forceinline__ double stage_hn(const DevArrays& A, int s, int c, int
 // R = double: the FP64 drop-in; R = float: the FP32 form's closures (the depth test and
 // the stored E - D stay FP64).
 template <class R>
-__global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
-    const DevParams& P = cP;
+__device__ __forceinline__ void m_emd(const DevParams& P, const DevParams32& F, const DevArrays& A, int s, int item_, int tnew) {
     int nX = P.nX, nY = P.nY, SC = nX * nY;
-    KG_TILE_THREAD(SC)
     int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sN = A.nbr[s * 8 + NB_N], sS = A.nbr[s * 8 + NB_S];
     const double* CT = A.CT[tnew];
     if (item_ < SC) {
@@ -100,7 +92,7 @@ __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restric
             R dbx = (R)CT[mp(s, 4, 2, SC) + c], dby = (R)CT[mp(s, 4, 3, SC) + c];
             Pt<R> pt{(R)Hn, (R)A.UV[mp(s, 2, 0, SC) + c], (R)A.UV[mp(s, 2, 1, SC) + c], (R)A.MS[mp(s, 5, 3, SC) + c],
                      (R)A.MS[mp(s, 5, 4, SC) + c], (R)CT[mp(s, 4, 1, SC) + c], dbx, dby, gam_of<R>(P.geo, dbx, dby)};
-            if constexpr (sizeof(R) == sizeof(float)) emd = (double)erosion_minus_deposition<R>(cP32, pt);
+            if constexpr (sizeof(R) == sizeof(float)) emd = (double)erosion_minus_deposition<R>(F, pt);
             else emd = erosion_minus_deposition<R>(P, pt);
         }
         A.EMD[(size_t)s * SC + c] = emd;
@@ -118,10 +110,9 @@ __device__ __forceinline__ double cellv(const DevArrays& A, const double* CT, in
 // Vertex source term and clamped stage update of bt.  PLAIN (the FP32 form) sums the four
 // cell terms pairwise instead of the reference's compensated sums.
 template <bool PLAIN>
-__global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt) {
-    const DevParams& P = cP;
+__device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int s, int item_, int tcur, int tnew, int stage,
+                                     double dt) {
     int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
-    KG_TILE_THREAD(SV)
     const double* CT = A.CT[tnew];
     int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sN = A.nbr[s * 8 + NB_N], sS = A.nbr[s * 8 + NB_S];
     int sSW = sW < 0 ? -1 : A.nbr[sW * 8 + NB_S], sSE = sE < 0 ? -1 : A.nbr[sE * 8 + NB_S];
@@ -213,10 +204,9 @@ __global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict
 // solids fraction and density.  PLAIN (the FP32 form) takes the vertex sums pairwise
 // (differences first) and one divide per cell; every quantity stays FP64.
 template <bool PLAIN>
-__global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
-    const DevParams& P = cP;
+__device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F, const DevArrays& A, int s, int item_, int qa,
+                                        int tcur, int tnew) {
     int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
-    KG_TILE_THREAD(SC)
     const double* b0 = A.BV[tnew] + mp(s, 2, 0, SV);
     const double* bt = A.BV[tnew] + mp(s, 2, 1, SV);
     double psib = 1.0 - P.BedPorosity, e2 = P.hThr * P.hThr;
@@ -256,7 +246,7 @@ __global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restr
             Hn = ((w - b0c) - btc) * gamnew;
             if (Hn < 0.0) Hn = 0.0;
             float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi;
-            psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, cP32.hThr2)), cP32.maxPack);
+            psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, F.hThr2)), F.maxPack);
         } else {
             w = -db / gamnew / gamnew;
             w = w + btc;
@@ -300,12 +290,10 @@ __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevA
 // The two tests of src/TimeStepper.f90:709-753 for every active cell.  flags[0] is set
 // when the step must be refined; redistribution candidates are appended with their loop
 // position (tile position in the active list, then j, then i) so the host can order them.
-__global__ void __launch_bounds__(256) k_m_check(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew, int* flags,
-                          unsigned long long* cand_key, double* cand_ex, int* ncand, int cand_cap) {
-    const DevParams& P = cP;
+__device__ __forceinline__ void m_check(const DevParams& P, const DevArrays& A, int s, int item_, int pos, int qa, int tcur,
+                                        int tnew, int* flags, unsigned long long* cand_key, double* cand_ex, int* ncand,
+                                        int cand_cap) {
     int SC = P.nX * P.nY;
-    KG_TILE_THREAD(SC)
-    int pos = blockIdx.x / per_;
     if (item_ < SC) {
         int c = item_;
         double ex, dBt, psiold, Hn_old, Hn_new;
@@ -463,11 +451,9 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
 // One CTA walks the waves with a barrier between them (__syncthreads makes the global
 // writes of a wave visible to the whole CTA).  A cell with no depositional vertex sets
 // flags[0]; the remaining waves are then skipped, as the serial walk stops there.
-__global__ void __launch_bounds__(REDIST_THREADS) k_m_redist(DevArrays A, const int* __restrict__ list_slot,
-                                                             const int* __restrict__ list_cell,
-                                                             const int* __restrict__ wave_off, int nwaves, int qa, int tcur,
-                                                             int tnew, int* flags) {
-    const DevParams& P = cP;
+__device__ __forceinline__ void m_redist(const DevParams& P, const DevArrays& A, const int* __restrict__ list_slot,
+                                         const int* __restrict__ list_cell, const int* __restrict__ wave_off, int nwaves,
+                                         int qa, int tcur, int tnew, int* flags) {
     __shared__ int failed;
     if (threadIdx.x == 0) failed = 0;
     __syncthreads();
@@ -490,14 +476,59 @@ __global__ void __launch_bounds__(REDIST_THREADS) k_m_redist(DevArrays A, const 
 
 // The M result becomes the input of the second hydraulic step: w and Hnpsi from the stage
 // state, momenta unchanged.
-__global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
-    int SC = cP.nX * cP.nY;
-    KG_TILE_THREAD(SC)
+__device__ __forceinline__ void m_finish(const DevParams& P, const DevArrays& A, int s, int item_, int qa) {
+    int SC = P.nX * P.nY;
     if (item_ < SC) {
         int c = item_;
         A.Q[qa][mp(s, 4, 0, SC) + c] = A.MS[mp(s, 5, 0, SC) + c];
         A.Q[qa][mp(s, 4, 3, SC) + c] = A.MS[mp(s, 5, 1, SC) + c];
     }
+}
+
+// ---- single-simulation kernels: one thread per cell / vertex, `per` CTAs per listed tile ----
+#define KG_TILE_ITEMS(NITEMS)                               \
+    int per_ = ((NITEMS) + 255) / 256;                      \
+    int pos = blockIdx.x / per_;                            \
+    int s = slots[pos];                                     \
+    int item_ = (blockIdx.x % per_) * 256 + threadIdx.x;    \
+    (void)pos;
+
+// ctl_flags[0..1]: the M refine flag and the candidate count, zeroed here for k_m_check.
+__global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew,
+                                                int* ctl_flags) {
+    if (blockIdx.x == 0 && threadIdx.x < 2) ctl_flags[threadIdx.x] = 0;
+    KG_TILE_ITEMS((cP.nX + 1) * (cP.nY + 1))
+    m_init(cP, A, s, item_, qa, tcur, tnew);
+}
+template <class R>
+__global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
+    KG_TILE_ITEMS(cP.nX * cP.nY)
+    m_emd<R>(cP, cP32, A, s, item_, tnew);
+}
+template <bool PLAIN>
+__global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt) {
+    KG_TILE_ITEMS((cP.nX + 1) * (cP.nY + 1))
+    m_bt<PLAIN>(cP, A, s, item_, tcur, tnew, stage, dt);
+}
+template <bool PLAIN>
+__global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
+    KG_TILE_ITEMS(cP.nX * cP.nY)
+    m_cells<PLAIN>(cP, cP32, A, s, item_, qa, tcur, tnew);
+}
+__global__ void __launch_bounds__(256) k_m_check(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew, int* flags,
+                                                 unsigned long long* cand_key, double* cand_ex, int* ncand, int cand_cap) {
+    KG_TILE_ITEMS(cP.nX * cP.nY)
+    m_check(cP, A, s, item_, pos, qa, tcur, tnew, flags, cand_key, cand_ex, ncand, cand_cap);
+}
+__global__ void __launch_bounds__(REDIST_THREADS) k_m_redist(DevArrays A, const int* __restrict__ list_slot,
+                                                             const int* __restrict__ list_cell,
+                                                             const int* __restrict__ wave_off, int nwaves, int qa, int tcur,
+                                                             int tnew, int* flags) {
+    m_redist(cP, A, list_slot, list_cell, wave_off, nwaves, qa, tcur, tnew, flags);
+}
+__global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
+    KG_TILE_ITEMS(cP.nX * cP.nY)
+    m_finish(cP, A, s, item_, qa);
 }
 
 // ---- host launchers (cells/verts: items per tile) ----

@@ -44,10 +44,7 @@ __global__ void k_cell_topo(DevArrays A, const int* __restrict__ slots, int ts) 
 
 // Per-tile kernels over the faces / cells of the listed tiles run `per` CTAs of 256
 // threads per tile, one face (x and y) or cell per thread.
-__global__ void __launch_bounds__(256) k_face_bI(DevArrays A, const int* __restrict__ slots, int ts, int per) {
-    const DevParams& P = cP;
-    int s = slots[blockIdx.x / per];
-    int f = (blockIdx.x % per) * 256 + threadIdx.x;
+__device__ __forceinline__ void face_bI(const DevParams& P, const DevArrays& A, int s, int f, int ts) {
     int nX = P.nX, nY = P.nY, SV = (nX + 1) * (nY + 1), SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
     const double* b0 = A.BV[ts] + pl(s, 2, 0, SV);
     const double* bt = A.BV[ts] + pl(s, 2, 1, SV);
@@ -67,10 +64,7 @@ __global__ void __launch_bounds__(256) k_face_bI(DevArrays A, const int* __restr
 // the W/E/S/N tiles' vertex copies.  PLAIN (the FP32 form) sums the vertex terms pairwise
 // in FP64, differences first, instead of the reference's compensated sums.
 template <bool PLAIN>
-__global__ void __launch_bounds__(256) k_face_topo(DevArrays A, const int* __restrict__ slots, int ts, int per) {
-    const DevParams& P = cP;
-    int s = slots[blockIdx.x / per];
-    int f = (blockIdx.x % per) * 256 + threadIdx.x;
+__device__ __forceinline__ void face_topo(const DevParams& P, const DevArrays& A, int s, int f, int ts) {
     int nX = P.nX, nY = P.nY, SV = (nX + 1) * (nY + 1), SFX = (nX + 1) * nY, SFY = nX * (nY + 1);
     int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E], sS = A.nbr[s * 8 + NB_S], sN = A.nbr[s * 8 + NB_N];
     const double* BV = A.BV[ts];
@@ -128,6 +122,14 @@ __global__ void __launch_bounds__(256) k_face_topo(DevArrays A, const int* __res
         FYs[pl(s, 5, 2, SFY) + f] = dbdx;
         FYs[pl(s, 5, 3, SFY) + f] = dbdy;
     }
+}
+
+__global__ void __launch_bounds__(256) k_face_bI(DevArrays A, const int* __restrict__ slots, int ts, int per) {
+    face_bI(cP, A, slots[blockIdx.x / per], (blockIdx.x % per) * 256 + threadIdx.x, ts);
+}
+template <bool PLAIN>
+__global__ void __launch_bounds__(256) k_face_topo(DevArrays A, const int* __restrict__ slots, int ts, int per) {
+    face_topo<PLAIN>(cP, A, slots[blockIdx.x / per], (blockIdx.x % per) * 256 + threadIdx.x, ts);
 }
 
 // mode 0: default data (w = b0, rho = rhow, rest 0; SetDefaultTileData); 2: a periodic
