@@ -260,13 +260,49 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def fp64_plain(args, wname):
+    """The plain FP64 drop-in on the same configuration, device-timed the same way (for the
+    FP32-vs-FP64 comparison of the headline line)."""
+    import torch
+    from kestrel_gb300 import lib, workloads
+    L = lib.load()
+    wl = workloads.WORKLOADS[wname]
+    made = wl["params"]()
+    p, b0 = made if isinstance(made, tuple) else (made, None)
+    sim = lib.simulation(p, precision=wl["prec"], b0=b0)
+    spin = wl.get("spinup", 0.0) if args.spinup is None else args.spinup
+    if spin > 0.0:
+        sim.integrate_to(spin)
+    stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        sim.step(p.tend)
+    torch.cuda.synchronize()
+    evs, cu, n = [], 0, 0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        st = sim.step(p.tend)
+        e1.record(stream)
+        evs.append((e0, e1))
+        cu += st.cell_updates
+        n += st.steps
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    sim.close()
+    return {"workload": wname, "value": cu / (ms / 1e3), "unit": "cell-updates/s", "steps": n, "ms_per_step": ms / max(n, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cap_release_256_fp64")
+    ap.add_argument("--workload", default="morpho_flux_2048_fp32")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain measurement beside an FP32 workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spinup", type=float, default=None, help="override the workload's untimed spin-up (s)")
     ap.add_argument("--profile", action="store_true", help="cudaProfilerStart/Stop around the timed steps")
@@ -416,6 +452,12 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if wl["prec"] == abi.PREC_FP32 and not args.no_fp64:
+        twin = args.workload.replace("_fp32", "_fp64")
+        if twin in workloads.WORKLOADS:
+            f64 = fp64_plain(args, twin)
+            line["fp64_plain"] = f64
+            line["fp32_over_fp64"] = line["value"] / f64["value"] if f64["value"] else None
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(p, b0)
     print(json.dumps(line))
