@@ -133,9 +133,12 @@ __device__ __forceinline__ void flux_source_rates(const DevParams& P, const DevS
                 }
             }
         }
-        double ncs = (double)S.ncells;
-        Qf = Qf / ncs / P.dx / P.dy;
-        psiQf = psiQf / ncs / P.dx / P.dy;
+        // A cell outside the source adds +0 either way; skip its divides.
+        if (Qf != 0.0 || psiQf != 0.0) {
+            double ncs = (double)S.ncells;
+            Qf = Qf / ncs / P.dx / P.dy;
+            psiQf = psiQf / ncs / P.dx / P.dy;
+        }
         s1 = s1 + Qf;
         s3 = s3 + psiQf;
     }

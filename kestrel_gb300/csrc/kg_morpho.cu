@@ -14,8 +14,8 @@
 //               fraction and density of the stage (ComputeDesingularisedVariables without
 //               velocities: u and v stay those the first hydraulic step left)
 // then k_m_check evaluates the excess-deposition and 10 % depth-change tests (:709-753)
-// and k_m_redist runs RedistributeGrid's serial, ordered correction (src/Redistribute.f90)
-// on one thread.  Topography lives in two sets: the step-start bed (read-only here) and
+// and k_m_redist runs RedistributeGrid's ordered correction (src/Redistribute.f90) in
+// dependency waves, one warp per listed cell.  Topography lives in two sets: the step-start bed (read-only here) and
 // the bed M builds, so a refined attempt restarts from the step-start set.
 #include <cuda_runtime.h>
 #include "kg_engine.cuh"
@@ -337,7 +337,8 @@ __device__ __forceinline__ void set_bt(const DevArrays& A, int tnew, int s, int 
     if (s >= 0 && A.kind[s] == SLOT_ACTIVE) A.BV[tnew][mp(s, 2, 1, SV) + (size_t)b * (nX + 1) + a] = v;
 }
 
-// RedistributeCell, src/Redistribute.f90:249-475.  Returns false when the cell borders no
+// RedistributeCell, src/Redistribute.f90:249-475, up to the corrected vertices (:249-399);
+// the cells are updated by redist_cell.  Returns false when the cell borders no
 // depositional vertex.
 __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int s, int i, int j,
                                   double corr) {
@@ -404,33 +405,24 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
             if (di[k] == nX && sN >= 0) set_bt(A, tnew, A.nbr[sN * 8 + NB_E], 0, 0, val, SV, nX);
         }
     }
-    // The (up to) 3x3 surrounding cells, with the reference's tile navigation (:404-448);
-    // i, j here are 0-based cell indices.  Cells of tiles that are not active are skipped
-    // (the reference updates its intermediate copy of a ghost tile there, which only the
-    // last hydraulic RHS of the step would read).
+    return true;
+}
+
+// The 3 x 3 cells a redistribution at cell (s, i, j) updates, in the order of the
+// reference's tile navigation (:404-448; i, j 0-based): ct[k] = -1 where a tile is missing.
+__device__ __forceinline__ void redist_cells_of(const DevParams& P, const DevArrays& A, int s, int i, int j, int vt[9], int vi[9],
+                                                int vj[9]) {
+    int nX = P.nX, nY = P.nY;
     auto nb = [&](int t, int d) { return t < 0 ? -1 : A.nbr[t * 8 + d]; };
-    int ct, ci, cj;
+    int sW = A.nbr[s * 8 + NB_W];
+    int ct, ci, cj, n = 0;
     if (i == 0) { ct = sW; ci = nX - 1; }
     else { ct = s; ci = i - 1; }
     for (int k = -1; k <= 1; ++k) {
         if (j == 0) { ct = nb(ct, NB_S); cj = nY - 1; }
         else cj = j - 1;
         for (int l = -1; l <= 1; ++l) {
-            if (ct >= 0 && A.kind[ct] == SLOT_ACTIVE) {
-                cell_topo_ij(P, A, tnew, ct, ci, cj);
-                size_t cc = (size_t)cj * nX + ci;
-                double dbc = C3[mp(ct, 4, 1, SC) + cc] - C0[mp(ct, 4, 1, SC) + cc];
-                double go = gam_of(P.geo, C0[mp(ct, 4, 2, SC) + cc], C0[mp(ct, 4, 3, SC) + cc]);
-                double gn = gam_of(P.geo, C3[mp(ct, 4, 2, SC) + cc], C3[mp(ct, 4, 3, SC) + cc]);
-                double Hno = compute_hn(A.Q[qa][mp(ct, 4, 0, SC) + cc], C0[mp(ct, 4, 0, SC) + cc], C0[mp(ct, 4, 1, SC) + cc], go);
-                if (Hno < 0.0) Hno = 0.0;
-                double w = C3[mp(ct, 4, 1, SC) + cc];
-                w = w + (Hno * go / gn - dbc / gn) / gn;
-                w = w + C3[mp(ct, 4, 0, SC) + cc];
-                A.MS[mp(ct, 5, 0, SC) + cc] = w;
-                double Hnpsiold = A.Q[qa][mp(ct, 4, 3, SC) + cc];
-                A.MS[mp(ct, 5, 1, SC) + cc] = Hnpsiold * go / gn - (1.0 - P.BedPorosity) * dbc / gn;
-            }
+            vt[n] = ct; vi[n] = ci; vj[n] = cj; ++n;
             cj = cj + 1;
             if (cj == nY && l < 1) { ct = nb(ct, NB_N); cj = 0; }
         }
@@ -438,7 +430,29 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
         ci = ci + 1;
         if (ci == nX) { ct = nb(ct, NB_E); ci = 0; }
     }
-    return true;
+}
+
+// One of those cells: its bed from the corrected vertices and the conservative w / Hnpsi
+// (cells of tiles that are not active are skipped; the reference updates its intermediate
+// copy of a ghost tile there, which only the last hydraulic RHS of the step would read).
+__device__ __forceinline__ void redist_cell(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int ct, int ci,
+                                            int cj) {
+    if (ct < 0 || A.kind[ct] != SLOT_ACTIVE) return;
+    int nX = P.nX, SC = nX * P.nY;
+    const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
+    cell_topo_ij(P, A, tnew, ct, ci, cj);
+    size_t cc = (size_t)cj * nX + ci;
+    double dbc = C3[mp(ct, 4, 1, SC) + cc] - C0[mp(ct, 4, 1, SC) + cc];
+    double go = gam_of(P.geo, C0[mp(ct, 4, 2, SC) + cc], C0[mp(ct, 4, 3, SC) + cc]);
+    double gn = gam_of(P.geo, C3[mp(ct, 4, 2, SC) + cc], C3[mp(ct, 4, 3, SC) + cc]);
+    double Hno = compute_hn(A.Q[qa][mp(ct, 4, 0, SC) + cc], C0[mp(ct, 4, 0, SC) + cc], C0[mp(ct, 4, 1, SC) + cc], go);
+    if (Hno < 0.0) Hno = 0.0;
+    double w = C3[mp(ct, 4, 1, SC) + cc];
+    w = w + (Hno * go / gn - dbc / gn) / gn;
+    w = w + C3[mp(ct, 4, 0, SC) + cc];
+    A.MS[mp(ct, 5, 0, SC) + cc] = w;
+    double Hnpsiold = A.Q[qa][mp(ct, 4, 3, SC) + cc];
+    A.MS[mp(ct, 5, 1, SC) + cc] = Hnpsiold * go / gn - (1.0 - P.BedPorosity) * dbc / gn;
 }
 
 // RedistributeGrid (src/Redistribute.f90:203-244) over the ordered candidate list, run as
@@ -454,17 +468,33 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
 __device__ __forceinline__ void m_redist(const DevParams& P, const DevArrays& A, const int* __restrict__ list_slot,
                                          const int* __restrict__ list_cell, const int* __restrict__ wave_off, int nwaves,
                                          int qa, int tcur, int tnew, int* flags) {
+    // One warp per candidate: lane 0 runs the excess test and the vertex correction, then
+    // lanes 0..8 update the nine cells (distinct cells, no interaction between them).
     __shared__ int failed;
     if (threadIdx.x == 0) failed = 0;
     __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     for (int wv = 0; wv < nwaves; ++wv) {
-        for (int q = wave_off[wv] + threadIdx.x; q < wave_off[wv + 1]; q += blockDim.x) {
+        for (int q = wave_off[wv] + warp; q < wave_off[wv + 1]; q += nwarps) {
             int s = list_slot[q], c = list_cell[q];
-            double ex, dBt, psiold, Ho, Hn;
-            excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
-            if (ex > kEPS) {
-                if (!redistribute_cell(P, A, qa, tcur, tnew, s, c % P.nX, c / P.nX, ex)) failed = 1;
+            int i = c % P.nX, j = c / P.nX;
+            int go = 0;
+            if (lane == 0) {
+                double ex, dBt, psiold, Ho, Hn;
+                excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
+                if (ex > kEPS) {
+                    if (redistribute_cell(P, A, qa, tcur, tnew, s, i, j, ex)) go = 1;
+                    else failed = 1;
+                }
             }
+            go = __shfl_sync(0xffffffffu, go, 0);
+            __syncwarp();
+            if (go) {
+                int vt[9], vi[9], vj[9];
+                redist_cells_of(P, A, s, i, j, vt, vi, vj);
+                if (lane < 9) redist_cell(P, A, qa, tcur, tnew, vt[lane], vi[lane], vj[lane]);
+            }
+            __syncwarp();
         }
         __syncthreads();
         if (failed) {

@@ -176,7 +176,7 @@ def ensemble_member(seed: int, side: int | None = None, tend: float | None = Non
     if side % tile:
         raise ValueError(f"tile {tile} does not divide side {side}")
     L = side * dx
-    v_draw = math.exp(rng.uniform(math.log(1e3), math.log(1e6)))
+    v_draw = math.exp(float(rng.uniform(math.log(1e3), math.log(1e6))))
     d_draw = DRAGS[int(rng.integers(0, 3))]
     m_draw = bool(rng.integers(0, 2))
     volume = v_draw if volume is None else volume
@@ -184,26 +184,26 @@ def ensemble_member(seed: int, side: int | None = None, tend: float | None = Non
     morpho = m_draw if morpho is None else morpho
     y0 = -0.2 * L
     if drag == "Chezy":
-        dtext = f"Drag = Chezy\nChezy Co = {rng.uniform(0.005, 0.05)!r}"
+        dtext = f"Drag = Chezy\nChezy Co = {float(rng.uniform(0.005, 0.05))!r}"
     elif drag == "Voellmy":
-        dtext = f"Drag = Voellmy\nCoulomb Co = {rng.uniform(0.05, 0.3)!r}\nChezy Co = {9.81 / rng.uniform(200.0, 2000.0)!r}"
+        dtext = f"Drag = Voellmy\nCoulomb Co = {float(rng.uniform(0.05, 0.3))!r}\nChezy Co = {9.81 / float(rng.uniform(200.0, 2000.0))!r}"
     else:
-        dtext = f"Drag = Manning\nManning Co = {rng.uniform(0.02, 0.1)!r}"
+        dtext = f"Drag = Manning\nManning Co = {float(rng.uniform(0.02, 0.1))!r}"
     k_draw = "cap" if rng.integers(0, 2) else "flux"
     if (kind or k_draw) == "cap":
-        h = rng.uniform(1.0, 5.0)
+        h = float(rng.uniform(1.0, 5.0))
         r = math.sqrt(volume / (math.pi * h))
         r = min(r, 0.12 * L)
         h = volume / (math.pi * r * r)
         stext = f"Cap:\n  capX = 0\n  capY = {y0!r}\n  capRadius = {r!r}\n  capHeight = {h!r}\n  capShape = flat\n  capConc = 0.2"
         src = ("cap", r, h)
     else:
-        T = rng.uniform(60.0, 300.0)
+        T = float(rng.uniform(60.0, 300.0))
         q = 2.0 * volume / T
         stext = (f"Source:\n  sourceX = 0\n  sourceY = {y0!r}\n  sourceRadius = {2.5 * dx!r}\n"
                  f"  sourceTime = (0,{T / 2!r},{T!r})\n  sourceFlux = (0,{q!r},0)\n  sourceConc = (0.2,0.2,0.2)")
         src = ("flux", T, q)
-    mtext = (f"Erosion = On\nErosion Depth = {rng.uniform(0.5, 3.0)!r}" if morpho else "Erosion = Off")
+    mtext = (f"Erosion = On\nErosion Depth = {float(rng.uniform(0.5, 3.0))!r}" if morpho else "Erosion = Off")
     text = f"""
 Domain:
 nXtiles = {side // tile}
@@ -261,3 +261,59 @@ def serve_requests(n: int, rate: float = 20.0, seed: int = 77, sides=(256, 512, 
         p, b0, d = ensemble_member(seed * 1000 + k, side=side, tend=tend, tile=tile)
         out.append((t, p, b0, d))
     return out
+
+
+def sparse_tiles(size: int = 8192, tile: int = 64, dx: float = 2.0, tend: float = 300.0, nout: int = 1, seed: int = 31337):
+    """Large sparse tiled domain: size x size cells at dx (8192^2 at 2 m by default, in
+    tiles of tile^2 cells), the fractal terrain generator with its own seed (relief scaled
+    to the domain as in the ensemble), three flux sources at seeded positions in the
+    middle 60% of the domain with triangular hydrographs (peak 40-120 m^3/s over 100-300 s,
+    concentration 0.2-0.4), Pouliquen-Forterre drag with the reference's defaults,
+    morphodynamics on, sponge edges, to t = 300 s.  Returns (params, b0)."""
+    rng = np.random.default_rng(seed)
+    L = size * dx
+    srcs = []
+    for k in range(3):
+        x, y = (float(v) for v in rng.uniform(-0.3 * L, 0.3 * L, size=2))
+        T = float(rng.uniform(100.0, 300.0))
+        q = float(rng.uniform(40.0, 120.0))
+        cc = float(rng.uniform(0.2, 0.4))
+        srcs.append(f"Source:\n  sourceX = {x!r}\n  sourceY = {y!r}\n  sourceRadius = {3 * dx!r}\n"
+                    f"  sourceTime = (0,{T / 2!r},{T!r})\n  sourceFlux = (0,{q!r},0)\n  sourceConc = ({cc!r},{cc!r},{cc!r})")
+    text = f"""
+Domain:
+nXtiles = {size // tile}
+nYtiles = {size // tile}
+nXpertile = {tile}
+nYpertile = {tile}
+Xtilesize = {tile * dx!r}
+Boundary Conditions = sponge
+{chr(10).join(srcs)}
+Parameters:
+Drag = Pouliquen
+Erosion = On
+Solver:
+T end = {tend!r}
+cfl = 0.25
+Output:
+N out = {nout}
+Topog:
+Type = Function
+Topog function = flat
+"""
+    p = config.parse(text).params
+    p.topog = abi.TOPO["upload"]
+    b0 = fractal_terrain(size + 1, size + 1, dx, seed + 104729, relief=800.0 * min(1.0, L / 10240.0))
+    return p, b0
+
+
+WORKLOADS["sparse_8192_fp32"] = dict(
+    desc="large sparse tiled domain: 8192x8192 cells at dx=2 m (128x128 tiles of 64x64), seeded fractal terrain, "
+         "three seeded flux sources, Pouliquen-Forterre drag, morphodynamics on, to t=300 s; FP32 form; timed after "
+         "a spin-up to t=60 s",
+    params=sparse_tiles, prec=abi.PREC_FP32, spinup=60.0)
+WORKLOADS["sparse_8192_fp64"] = dict(
+    desc="large sparse tiled domain: 8192x8192 cells at dx=2 m (128x128 tiles of 64x64), seeded fractal terrain, "
+         "three seeded flux sources, Pouliquen-Forterre drag, morphodynamics on, to t=300 s; FP64 plain; timed after "
+         "a spin-up to t=60 s",
+    params=sparse_tiles, prec=abi.PREC_FP64, spinup=60.0)

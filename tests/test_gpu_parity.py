@@ -209,3 +209,22 @@ def test_morpho_conservation_gpu():
     assert abs((v1[3] + v1[1] * (1 - phi)) - (v0[3] + v0[1] * (1 - phi))) / (v0[3] + v0[1] * (1 - phi)) <= 1e-10
     for t in g.active_tiles():
         assert g.field(t, 11).min() >= -p.EroDepth
+
+
+def test_sparse_activation_bitexact_every_step():
+    """The large sparse configuration at reduced size (512^2 cells at dx = 2 m in 32 x 32
+    tiles of 16^2, three seeded flux sources, Pouliquen drag, morphodynamics on): the
+    sorted active list and the ghost list match the oracle's after every accepted step, and
+    the state stays within the morphodynamic tolerance."""
+    from kestrel_gb300 import workloads
+    p, b0 = workloads.sparse_tiles(size=512, tile=16, dx=2.0, tend=3.0)
+    g, o = lib.simulation(p, b0=b0), _oracle.simulation(p, b0=b0)
+    n = 0
+    while o.time[0] < p.tend and n < 80:
+        sg, so = g.step(p.tend), o.step(p.tend)
+        assert (sg.steps, sg.rejected) == (so.steps, so.rejected), n
+        assert g.active_tiles() == o.active_tiles(), n
+        assert g.ghost_tiles() == o.ghost_tiles(), n
+        n += 1
+    assert len(o.active_tiles()) > 3
+    compare_state(g, o, tol=1e-10, what="sparse")
