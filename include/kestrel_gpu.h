@@ -165,6 +165,14 @@ int  kg_upload_b0(kg_ctx* ctx, const double* b0_vertices, int64_t nx1, int64_t n
 /* LoadSourceConditions (src/SetSources.f90:47-405): places caps, cubes and flux sources
    and activates (AddTile) every tile that covers them. */
 int  kg_load_sources(kg_ctx* ctx);
+/* Restart from a saved state instead of loading the sources (LoadInitialCondition,
+   src/Restart.f90:55-328): activates tiles ids[0..n) (strictly increasing) in order and
+   sets, per tile k, the conserved fields state[k][4][nYpertile][nXpertile] (w, rhoHnu,
+   rhoHnv, Hnpsi) and, when bt_vertex is not NULL, the vertex bed change
+   bt_vertex[k][nYpertile+1][nXpertile+1]; the cell and interfacial topography, the ghost
+   tiles and the flux-source cell counts are rebuilt; the clock is set to t.  Use on a
+   context with nothing loaded (no kg_load_sources). */
+int  kg_load_state(kg_ctx* ctx, const int32_t* ids, int32_t n, const double* state, const double* bt_vertex, double t);
 
 /* One accepted time step of IntegrateTo's loop (src/TimeStepper.f90:151-275), ending no
    later than t_stop. */

@@ -1136,6 +1136,7 @@ void integrate_step_body(kg_ctx& c, double tend) {
 // same order, which gives the same state (activation only touches the new tile).
 struct CellMod { int id, ii, jj, kind, idx; double R2; };
 
+void upload_sources(kg_ctx& c);
 void load_sources(kg_ctx& c) {
     for (auto& s : c.srcs) s.ncells = 0;
     std::vector<CellMod> mods;
@@ -1299,7 +1300,16 @@ void load_sources(kg_ctx& c) {
         CK(cudaMemcpyAsync(c.A.MX + (size_t)s * 11 * SC, bufs[q].hmax.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
     }
     sync(c);
-    // containsSource flags and the per-source cell counts.
+    upload_sources(c);
+    for (int g : std::vector<int>(c.ghost)) ghost_edges(c, g);
+    if (!c.touched.empty()) mirror_touched(c);
+    c.src_override = true;
+    c.sources_loaded = true;
+    c.blocks_dirty = true;
+}
+
+// containsSource flags, the per-source cell counts and the device source table.
+void upload_sources(kg_ctx& c) {
     for (int id : c.active) {
         int8_t f = T(c, id).src ? 1 : 0;
         CK(cudaMemcpyAsync(c.A.has_source + T(c, id).slot, &f, 1, cudaMemcpyHostToDevice, c.st));
@@ -1320,11 +1330,62 @@ void load_sources(kg_ctx& c) {
     CK(set_constants(c.dp, ds.data(), (int)ds.size(), c.st));
     g_const_owner = &c;
     sync(c);
+}
+
+// LoadInitialCondition_txt + ActivateTile(restart) (src/Restart.f90:151-328,
+// src/UpdateTiles.f90:342-384): activate the listed tiles in order, then overwrite their
+// conserved fields (w, rhoHnu, rhoHnv, Hnpsi) and their vertex bt, and rebuild what the
+// reference rebuilds: cell and interfacial topography, the ghost tiles' edge data and the
+// flux-source cell counts (<=, src/Restart.f90:284-305).  The maxima start afresh.
+void load_state(kg_ctx& c, const int32_t* ids, int n, const double* state, const double* btv, double t) {
+    if (c.sources_loaded) throw KgError(KG_ERR_STATE, "kg_load_state needs a context with nothing loaded");
+    for (int k = 0; k < n; ++k) {
+        if (!in_bounds(c, ids[k])) throw KgError(KG_ERR_PARAM, "tile id out of range");
+        if (!T(c, ids[k]).on) add_tile(c, ids[k]);
+    }
+    int SC = c.SC, SV = c.SV;
+    std::vector<int> slots;
+    for (int k = 0; k < n; ++k) {
+        int s = T(c, ids[k]).slot;
+        slots.push_back(s);
+        CK(cudaMemcpyAsync(c.A.Q[c.qcur] + (size_t)s * 4 * SC, state + (size_t)k * 4 * SC, (size_t)4 * SC * sizeof(double),
+                           cudaMemcpyHostToDevice, c.st));
+        if (btv)
+            CK(cudaMemcpyAsync(c.A.BV[c.tcur] + ((size_t)s * 2 + 1) * SV, btv + (size_t)k * SV, (size_t)SV * sizeof(double),
+                               cudaMemcpyHostToDevice, c.st));
+        touch(c, s);
+    }
+    sync(c);
+    upload_list(c, slots);
+    CK(launch_cell_topo(c.A, c.d_list, n, c.tcur, c.st));
+    CK(launch_face_topo(c.A, c.d_list, n, c.tcur, c.nX, c.nY, false, c.st));
+    CK(launch_face_bI(c.A, c.d_list, n, c.tcur, c.nX, c.nY, c.st));
+    c.launches += 3;
+    sync(c);
+    for (auto& src : c.srcs) src.ncells = 0;
+    for (int id : c.active) {
+        int gi = tile_col(c, id), gj = tile_row(c, id);
+        for (int jj = 1; jj <= c.nY; ++jj)
+            for (int ii = 1; ii <= c.nX; ++ii) {
+                double x = cell_x(c, gi, ii), y = cell_y(c, gj, jj);
+                for (auto& src : c.srcs) {
+                    double R2 = (x - src.x) * (x - src.x) + (y - src.y) * (y - src.y);
+                    if (R2 <= src.R * src.R) {
+                        src.ncells = src.ncells + 1;
+                        T(c, id).src = true;
+                    }
+                }
+            }
+    }
+    upload_sources(c);
     for (int g : std::vector<int>(c.ghost)) ghost_edges(c, g);
     if (!c.touched.empty()) mirror_touched(c);
-    c.src_override = true;
+    c.t = t;
+    c.src_override = false;
     c.sources_loaded = true;
     c.blocks_dirty = true;
+    c.gen++;
+    c.tdirty[0] = c.tdirty[1] = 2;
 }
 
 // Run settings (src/DomainSettings.f90:185-225, src/Parameters.f90:629-648).
@@ -1534,6 +1595,15 @@ int kg_load_sources(kg_ctx* c) {
     if (c->p.topog == KG_TOPO_UPLOAD && c->upload.empty()) { c->err = "no topography uploaded"; return KG_ERR_STATE; }
     c->gen++;
     KG_GUARD(c, load_sources(*c));
+    return KG_OK;
+}
+
+int kg_load_state(kg_ctx* c, const int32_t* ids, int32_t n, const double* state, const double* bt_vertex, double t) {
+    if (!c || !ids || !state || n < 1) return KG_ERR_PARAM;
+    KG_ENTER(c);
+    for (int k = 1; k < n; ++k)
+        if (ids[k] <= ids[k - 1]) { c->err = "kg_load_state: tile ids must be strictly increasing"; return KG_ERR_PARAM; }
+    KG_GUARD(c, load_state(*c, ids, n, state, bt_vertex, t));
     return KG_OK;
 }
 

@@ -188,14 +188,30 @@ __device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int
             ky = kahan4(y[0], y[1], y[2], y[3]);
             ke = (mode == 1) ? kahan3(e[0], e[1], e[2] + e[3]) : kahan4(e[0], e[1], e[2], e[3]);
         }
-        double gam = gam_of(P.geo, 0.25 * kx, 0.25 * ky);
-        double ddt = -0.25 * gam / psib * ke;
         double bt0 = A.BV[tcur][mp(s, 2, 1, SV) + v];
         double btp = A.BV[tnew][mp(s, 2, 1, SV) + v];
         double nb;
-        if (stage == 1) nb = bt0 + dt * ddt;
-        else if (stage == 2) nb = 0.75 * bt0 + 0.25 * (btp + dt * ddt);
-        else nb = (1.0 / 3.0) * bt0 + (2.0 / 3.0) * (btp + dt * ddt);
+        if (PLAIN) {
+            // FP32 form: the rate in FP32 (its E - D terms come from FP32 closures), the
+            // stage update as bt0 + a (bt_k - bt0 + dt ddt) in FP64, so a vertex with no
+            // erosion or deposition around it keeps its bed exactly.
+            float ddt = 0.f;
+            if (ke != 0.0) {
+                float gx = 0.25f * (float)kx, gy = 0.25f * (float)ky;
+                float gam = P.geo ? sqrtf(1.f + gx * gx + gy * gy) : 1.f;
+                ddt = -0.25f * gam * (float)ke / (float)psib;
+            }
+            double inc = (btp - bt0) + dt * (double)ddt;
+            if (stage == 1) nb = bt0 + dt * (double)ddt;
+            else if (stage == 2) nb = bt0 + 0.25 * inc;
+            else nb = bt0 + (2.0 / 3.0) * inc;
+        } else {
+            double gam = gam_of(P.geo, 0.25 * kx, 0.25 * ky);
+            double ddt = -0.25 * gam / psib * ke;
+            if (stage == 1) nb = bt0 + dt * ddt;
+            else if (stage == 2) nb = 0.75 * bt0 + 0.25 * (btp + dt * ddt);
+            else nb = (1.0 / 3.0) * bt0 + (2.0 / 3.0) * (btp + dt * ddt);
+        }
         A.BV[tnew][mp(s, 2, 1, SV) + v] = mx(-P.EroDepth, nb);
     }
 }
@@ -214,6 +230,16 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
         int c = item_;
         int i = c % nX, j = c / nX;
         int v00 = j * (nX + 1) + i, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
+        if (PLAIN) {
+            // FP32 form: a cell whose four vertices kept their bed, and whose cell bed in
+            // the M set is still the step-start one, keeps its current stage state.
+            const double* bt0 = A.BV[tcur] + mp(s, 2, 1, SV);
+            const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
+            if (bt[v00] == bt0[v00] && bt[v10] == bt0[v10] && bt[v01] == bt0[v01] && bt[v11] == bt0[v11] &&
+                C3[mp(s, 4, 1, SC) + c] == C0[mp(s, 4, 1, SC) + c] && C3[mp(s, 4, 2, SC) + c] == C0[mp(s, 4, 2, SC) + c] &&
+                C3[mp(s, 4, 3, SC) + c] == C0[mp(s, 4, 3, SC) + c])
+                return;
+        }
         double b0c, btc, dbx, dby;
         if (PLAIN) {
             b0c = 0.25 * ((b0[v00] + b0[v10]) + (b0[v01] + b0[v11]));
