@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) k_m_batch(const SimStatic* __restrict__ s
         int s = X.slots[pos];
         if (K == MK_INIT) {
             if (local == 0 && threadIdx.x < 2) J.flags[threadIdx.x] = 0;
-            m_init(X.P, X.A, s, item, J.qa, J.tcur, J.tnew);
+            m_init<true>(X.P, X.A, s, item, J.qa, J.tcur, J.tnew);
         } else if (K == MK_EMD) {
             m_emd<float>(X.P, X.F, X.A, s, item, J.tnew);
         } else if (K == MK_BT) {
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) k_m_batch(const SimStatic* __restrict__ s
         } else if (K == MK_CELLS) {
             m_cells<true>(X.P, X.F, X.A, s, item, J.qa, J.tcur, J.tnew);
         } else if (K == MK_CHECK) {
-            m_check(X.P, X.A, s, item, pos, J.qa, J.tcur, J.tnew, J.flags, J.keys, J.ex, J.flags + 1, J.cap);
+            m_check<true>(X.P, X.A, s, item, pos, J.qa, J.tcur, J.tnew, J.flags, J.keys, J.ex, J.flags + 1, J.cap);
         } else if (K == MK_FACE) {
             face_topo<true>(X.P, X.A, s, item, J.tnew);
         } else if (K == MK_BI) {
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(REDIST_THREADS) k_m_redist_batch(const SimStat
                                                                    const RJob* __restrict__ jobs) {
     const RJob& J = jobs[blockIdx.x];
     const SimStatic& X = sims[J.member];
-    m_redist(X.P, X.A, J.list_slot, J.list_cell, J.wave_off, J.nwaves, J.qa, J.tcur, J.tnew, J.flags);
+    m_redist<true>(X.P, X.A, J.list_slot, J.list_cell, J.wave_off, J.nwaves, J.qa, J.tcur, J.tnew, J.flags);
 }
 
 }  // namespace kg

@@ -48,16 +48,16 @@ cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcu
                           double* d_out, cudaStream_t st);
 // kg_morpho.cu
 cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, int* ctl_flags,
-                          cudaStream_t st);
+                          bool fp32, cudaStream_t st);
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st);
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
                         bool fp32, cudaStream_t st);
 cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, bool fp32,
                            cudaStream_t st);
 cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
-                           unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st);
-cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, int nwaves, int qa, int tcur,
-                            int tnew, int* flags, cudaStream_t st);
+                           unsigned long long* keys, double* ex, int* ncand, int cap, bool fp32, cudaStream_t st);
+cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, const int* hwoff, int nwaves,
+                            int qa, int tcur, int tnew, int* flags, bool fp32, cudaStream_t st);
 cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st);
 }  // namespace kg
 
@@ -978,7 +978,9 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
     int n = (int)slots.size();
     const int* dl = c.d_active;
     const bool fp32 = c.prec == KG_PREC_FP32;
-    CK(launch_m_init(c.A, dl, n, c.SV, qa, c.tcur, tnew, c.d_mflags, c.st));
+    // The FP32 form's M kernels read gamma of the step-start topography from the cache.
+    if (fp32 && c.tdirty[c.tcur]) refresh_topo32(c, c.tcur);
+    CK(launch_m_init(c.A, dl, n, c.SV, qa, c.tcur, tnew, c.d_mflags, fp32, c.st));
     c.launches++;
     for (int stage = 1; stage <= 3; ++stage) {
         CK(launch_m_emd(c.A, dl, n, c.SC, tnew, fp32, c.st));
@@ -996,7 +998,7 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         CK(cudaMalloc(&c.d_rcell, (size_t)c.cand_cap * sizeof(int)));
         CK(cudaMalloc(&c.d_rwave, ((size_t)c.cand_cap + 1) * sizeof(int)));
     }
-    CK(launch_m_check(c.A, dl, n, c.SC, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, c.st));
+    CK(launch_m_check(c.A, dl, n, c.SC, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, fp32, c.st));
     c.launches++;
     collect_cfl(c);
     int ncand = c.h_ctl->ncand;
@@ -1030,8 +1032,8 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         CK(cudaMemcpyAsync(c.d_rslot, ls.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
-        CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, c.d_rwave, nw, qa, c.tcur, tnew, c.d_mflags, c.st));
-        c.launches++;
+        CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, c.d_rwave, woff.data(), nw, qa, c.tcur, tnew, c.d_mflags, fp32, c.st));
+        c.launches += nw <= 64 ? nw : 1;
     }
     // Interfacial topography of the new bed and the M result (both scratch until accepted).
     CK(launch_face_topo(c.A, dl, n, tnew, c.nX, c.nY, fp32, c.st));

@@ -28,6 +28,25 @@ constexpr int REDIST_THREADS = 512;
 
 __device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return ((size_t)slot * nf + f) * (size_t)npl; }
 
+// FP32 form: 1/sqrt(x) to FP64 accuracy from an FP32 seed and two Newton steps, and the
+// step-start gamma of a cell from the topography-factor cache (gamma = gamma^2 / gamma).
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y = (double)rsqrtf((float)x);
+    y = y * (1.5 - 0.5 * x * y * y);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y;
+}
+__device__ __forceinline__ double gam_cached(const DevParams& P, const DevArrays& A, int ts, int s, int c, double bx, double by) {
+    if (!P.geo) return 1.0;
+    int SC = P.nX * P.nY;
+    return (1.0 + (bx * bx + by * by)) * A.TD[ts][mp(s, 3, 2, SC) + c];
+}
+__device__ __forceinline__ double gam_nr(const DevParams& P, double bx, double by) {
+    if (!P.geo) return 1.0;
+    double g2 = 1.0 + (bx * bx + by * by);
+    return g2 * rsqrt_nr(g2);
+}
+
 // Each step below is a per-item body (settings P / F, arrays A, slot s, item item_ of
 // the tile, the tile's list position pos) called by a single-simulation kernel, which
 // reads the constant bank, and by the batched kernels of kg_batch.cu, which read a
@@ -35,6 +54,7 @@ __device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return 
 
 // Copy the step-start bed into the M set and fill the stage state of im0 (the state the
 // first hydraulic step produced).
+template <bool PLAIN>
 __device__ __forceinline__ void m_init(const DevParams& P, const DevArrays& A, int s, int item_, int qa, int tcur, int tnew) {
     int SC = P.nX * P.nY, SV = (P.nX + 1) * (P.nY + 1);
     if (item_ < SV) {
@@ -51,11 +71,17 @@ __device__ __forceinline__ void m_init(const DevParams& P, const DevArrays& A, i
             A.CT[tnew][mp(s, 4, f, SC) + c] = ct[f];
         }
         double w = A.Q[qa][mp(s, 4, 0, SC) + c], p = A.Q[qa][mp(s, 4, 3, SC) + c];
-        double gam = gam_of(P.geo, ct[2], ct[3]);
+        double gam = PLAIN ? gam_cached(P, A, tcur, s, c, ct[2], ct[3]) : gam_of(P.geo, ct[2], ct[3]);
         double Hn = compute_hn(w, ct[0], ct[1], gam);
         if (Hn < 0.0) Hn = 0.0;
         double pp = p < 0.0 ? 0.0 : p;
-        double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
+        double psi;
+        if (PLAIN) {
+            float Hf = (float)Hn, pf = (float)pp;
+            psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, (float)e2)), (float)P.maxPack);
+        } else {
+            psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
+        }
         double* M = A.MS + mp(s, 5, 0, SC) + c;
         M[0] = w;
         M[(size_t)SC] = p;
@@ -259,14 +285,25 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
         A.CT[tnew][mp(s, 4, 2, SC) + c] = dbx;
         A.CT[tnew][mp(s, 4, 3, SC) + c] = dby;
         const double* C0 = A.CT[tcur];
-        double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
-        double gamnew = gam_of(P.geo, dbx, dby);
+        double gamold, gamnew, ign = 1.0;
+        if (PLAIN) {
+            gamold = gam_cached(P, A, tcur, s, c, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+            if (P.geo) {
+                double g2 = 1.0 + (dbx * dbx + dby * dby);
+                ign = rsqrt_nr(g2);
+                gamnew = g2 * ign;
+            } else {
+                gamnew = 1.0;
+            }
+        } else {
+            gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+            gamnew = gam_of(P.geo, dbx, dby);
+        }
         double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
         double Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
         double db = btc - C0[mp(s, 4, 1, SC) + c];
         double w, Hnpsi, Hn, psi;
         if (PLAIN) {
-            double ign = 1.0 / gamnew;
             w = (b0c + btc) + (Hn_old * gamold - db) * (ign * ign);
             Hnpsi = (p0 * gamold - psib * db) * ign;
             Hn = ((w - b0c) - btc) * gamnew;
@@ -295,20 +332,29 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
 }
 
 // ExcessDeposition (src/Redistribute.f90:158-198) of cell (s, c) between im0 and im3.
+// PLAIN (the FP32 form) takes gamma from the factor cache / an FP32-seeded Newton step.
+template <bool PLAIN = false>
 __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevArrays& A, int s, int c, int qa, int tcur,
                                                   int tnew, double& excess, double& deltaBt, double& psiold,
                                                   double& Hn_old, double& Hn_new) {
     int SC = P.nX * P.nY;
     const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
-    double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
-    double gamnew = gam_of(P.geo, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c]);
+    double gamold = PLAIN ? gam_cached(P, A, tcur, s, c, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c])
+                          : gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+    double gamnew = PLAIN ? gam_nr(P, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c])
+                          : gam_of(P.geo, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c]);
     double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
     Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
     Hn_new = compute_hn(A.MS[mp(s, 5, 0, SC) + c], C3[mp(s, 4, 0, SC) + c], C3[mp(s, 4, 1, SC) + c], gamnew);
     deltaBt = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
     // im0's solids fraction as the first hydraulic step left it
     double H0 = Hn_old < 0.0 ? 0.0 : Hn_old, pp = p0 < 0.0 ? 0.0 : p0, e2 = P.hThr * P.hThr;
-    psiold = mn(2.0 * H0 * pp / (H0 * H0 + mx(H0 * H0, e2)), P.maxPack);
+    if (PLAIN) {
+        float Hf = (float)H0, pf = (float)pp;
+        psiold = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, (float)e2)), (float)P.maxPack);
+    } else {
+        psiold = mn(2.0 * H0 * pp / (H0 * H0 + mx(H0 * H0, e2)), P.maxPack);
+    }
     excess = -(p0 * gamold / (1.0 - P.BedPorosity) - deltaBt);
     excess = mx(excess, -(Hn_old * gamold - deltaBt));
 }
@@ -316,6 +362,7 @@ __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevA
 // The two tests of src/TimeStepper.f90:709-753 for every active cell.  flags[0] is set
 // when the step must be refined; redistribution candidates are appended with their loop
 // position (tile position in the active list, then j, then i) so the host can order them.
+template <bool PLAIN>
 __device__ __forceinline__ void m_check(const DevParams& P, const DevArrays& A, int s, int item_, int pos, int qa, int tcur,
                                         int tnew, int* flags, unsigned long long* cand_key, double* cand_ex, int* ncand,
                                         int cand_cap) {
@@ -323,7 +370,7 @@ __device__ __forceinline__ void m_check(const DevParams& P, const DevArrays& A, 
     if (item_ < SC) {
         int c = item_;
         double ex, dBt, psiold, Hn_old, Hn_new;
-        excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Hn_old, Hn_new);
+        excess_deposition<PLAIN>(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Hn_old, Hn_new);
         bool refine = false;
         if (ex > kEPS && dBt > kEPS && psiold > -kEPS) {
             if (Hn_old < P.EroCriticalHeight || fabs(Hn_new - Hn_old) < P.EroCriticalHeight) {
@@ -491,6 +538,7 @@ __device__ __forceinline__ void redist_cell(const DevParams& P, const DevArrays&
 // One CTA walks the waves with a barrier between them (__syncthreads makes the global
 // writes of a wave visible to the whole CTA).  A cell with no depositional vertex sets
 // flags[0]; the remaining waves are then skipped, as the serial walk stops there.
+template <bool PLAIN>
 __device__ __forceinline__ void m_redist(const DevParams& P, const DevArrays& A, const int* __restrict__ list_slot,
                                          const int* __restrict__ list_cell, const int* __restrict__ wave_off, int nwaves,
                                          int qa, int tcur, int tnew, int* flags) {
@@ -507,7 +555,7 @@ __device__ __forceinline__ void m_redist(const DevParams& P, const DevArrays& A,
             int go = 0;
             if (lane == 0) {
                 double ex, dBt, psiold, Ho, Hn;
-                excess_deposition(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
+                excess_deposition<PLAIN>(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
                 if (ex > kEPS) {
                     if (redistribute_cell(P, A, qa, tcur, tnew, s, i, j, ex)) go = 1;
                     else failed = 1;
@@ -550,11 +598,12 @@ __device__ __forceinline__ void m_finish(const DevParams& P, const DevArrays& A,
     (void)pos;
 
 // ctl_flags[0..1]: the M refine flag and the candidate count, zeroed here for k_m_check.
+template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew,
                                                 int* ctl_flags) {
     if (blockIdx.x == 0 && threadIdx.x < 2) ctl_flags[threadIdx.x] = 0;
     KG_TILE_ITEMS((cP.nX + 1) * (cP.nY + 1))
-    m_init(cP, A, s, item_, qa, tcur, tnew);
+    m_init<PLAIN>(cP, A, s, item_, qa, tcur, tnew);
 }
 template <class R>
 __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
@@ -571,17 +620,48 @@ __global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restr
     KG_TILE_ITEMS(cP.nX * cP.nY)
     m_cells<PLAIN>(cP, cP32, A, s, item_, qa, tcur, tnew);
 }
+template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_check(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew, int* flags,
                                                  unsigned long long* cand_key, double* cand_ex, int* ncand, int cand_cap) {
     KG_TILE_ITEMS(cP.nX * cP.nY)
-    m_check(cP, A, s, item_, pos, qa, tcur, tnew, flags, cand_key, cand_ex, ncand, cand_cap);
+    m_check<PLAIN>(cP, A, s, item_, pos, qa, tcur, tnew, flags, cand_key, cand_ex, ncand, cand_cap);
 }
+template <bool PLAIN>
 __global__ void __launch_bounds__(REDIST_THREADS) k_m_redist(DevArrays A, const int* __restrict__ list_slot,
                                                              const int* __restrict__ list_cell,
                                                              const int* __restrict__ wave_off, int nwaves, int qa, int tcur,
                                                              int tnew, int* flags) {
-    m_redist(cP, A, list_slot, list_cell, wave_off, nwaves, qa, tcur, tnew, flags);
+    m_redist<PLAIN>(cP, A, list_slot, list_cell, wave_off, nwaves, qa, tcur, tnew, flags);
 }
+// One wave of the ordered walk, one 32-thread CTA per listed cell, so the wave's FP64 work
+// spreads over every SM (an SM has 2 FP64 lanes per clock).  A wave does nothing once an
+// earlier wave found a cell without a depositional vertex (the serial walk stops there).
+template <bool PLAIN>
+__global__ void __launch_bounds__(32) k_m_redist_wave(DevArrays A, const int* __restrict__ list_slot,
+                                                      const int* __restrict__ list_cell, int qa, int tcur, int tnew,
+                                                      int* flags) {
+    if (*(volatile int*)flags != 0) return;
+    const int lane = threadIdx.x;
+    int s = list_slot[blockIdx.x], c = list_cell[blockIdx.x];
+    int i = c % cP.nX, j = c / cP.nX;
+    int go = 0;
+    if (lane == 0) {
+        double ex, dBt, psiold, Ho, Hn;
+        excess_deposition<PLAIN>(cP, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
+        if (ex > kEPS) {
+            if (redistribute_cell(cP, A, qa, tcur, tnew, s, i, j, ex)) go = 1;
+            else atomicOr(flags, 1);
+        }
+    }
+    go = __shfl_sync(0xffffffffu, go, 0);
+    __syncwarp();
+    if (go) {
+        int vt[9], vi[9], vj[9];
+        redist_cells_of(cP, A, s, i, j, vt, vi, vj);
+        if (lane < 9) redist_cell(cP, A, qa, tcur, tnew, vt[lane], vi[lane], vj[lane]);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
     KG_TILE_ITEMS(cP.nX * cP.nY)
     m_finish(cP, A, s, item_, qa);
@@ -591,9 +671,10 @@ __global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __rest
 static inline int per_of(int items) { return (items + 255) / 256; }
 
 cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, int* ctl_flags,
-                          cudaStream_t st) {
+                          bool fp32, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_m_init<<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, ctl_flags);
+    if (fp32) k_m_init<true><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, ctl_flags);
+    else k_m_init<false><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, ctl_flags);
     return cudaGetLastError();
 }
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st) {
@@ -617,16 +698,30 @@ cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int ce
     return cudaGetLastError();
 }
 cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
-                           unsigned long long* keys, double* ex, int* ncand, int cap, cudaStream_t st) {
+                           unsigned long long* keys, double* ex, int* ncand, int cap, bool fp32, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_m_check<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
+    if (fp32) k_m_check<true><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
+    else k_m_check<false><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
     return cudaGetLastError();
 }
-cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, int nwaves, int qa, int tcur,
-                            int tnew, int* flags, cudaStream_t st) {
+// hwoff: the wave offsets on the host (one launch per wave while the waves are few).
+cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, const int* hwoff, int nwaves,
+                            int qa, int tcur, int tnew, int* flags, bool fp32, cudaStream_t st) {
     if (nwaves == 0) return cudaSuccess;
-    k_m_redist<<<1, REDIST_THREADS, 0, st>>>(A, ls, lc, woff, nwaves, qa, tcur, tnew, flags);
-    return cudaGetLastError();
+    if (nwaves > 64) {
+        if (fp32) k_m_redist<true><<<1, REDIST_THREADS, 0, st>>>(A, ls, lc, woff, nwaves, qa, tcur, tnew, flags);
+        else k_m_redist<false><<<1, REDIST_THREADS, 0, st>>>(A, ls, lc, woff, nwaves, qa, tcur, tnew, flags);
+        return cudaGetLastError();
+    }
+    for (int w = 0; w < nwaves; ++w) {
+        int n = hwoff[w + 1] - hwoff[w];
+        if (n <= 0) continue;
+        if (fp32) k_m_redist_wave<true><<<n, 32, 0, st>>>(A, ls + hwoff[w], lc + hwoff[w], qa, tcur, tnew, flags);
+        else k_m_redist_wave<false><<<n, 32, 0, st>>>(A, ls + hwoff[w], lc + hwoff[w], qa, tcur, tnew, flags);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
