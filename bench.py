@@ -260,19 +260,54 @@ def run_serve(args):
     print(json.dumps(line))
 
 
-def fp64_plain(args, wname):
+def spin_up(sim, p, spin, every=None):
+    """Untimed integration to t = spin; with `every`, the active-tile count is recorded at
+    each multiple of `every` seconds: [[t, active tiles, percent of all tiles], ...]."""
+    out = []
+    if spin <= 0.0:
+        return out
+    if not every:
+        sim.integrate_to(spin)
+        return out
+    total = p.nXtiles * p.nYtiles
+    t = 0.0
+    while t < spin:
+        t = min(spin, t + every)
+        sim.integrate_to(t)
+        n = len(sim.active_tiles())
+        out.append([round(sim.time[0], 3), n, round(100.0 * n / total, 3)])
+    return out
+
+
+def take_snapshot(sim):
+    """(tile ids, state (n, 4, nY, nX), vertex bt (n, nY+1, nX+1), t) of a running simulation."""
+    import numpy as np
+    ids = sim.active_tiles()
+    state = np.stack([np.stack([sim.field(t, f) for f in (1, 2, 3, 4)]) for t in ids])
+    btv = np.stack([sim.vertex(t, 1) for t in ids])
+    return ids, state, btv, sim.time[0]
+
+
+def fp64_plain(args, wname, snapshot=None):
     """The plain FP64 drop-in on the same configuration, device-timed the same way (for the
-    FP32-vs-FP64 comparison of the headline line)."""
+    FP32-vs-FP64 comparison of the headline line).  With a snapshot, the FP64 context is
+    restarted from the FP32 run's state at the end of its spin-up (kg_load_state) instead of
+    integrating the spin-up again."""
     import torch
     from kestrel_gb300 import lib, workloads
+    from kestrel_gb300.solver import Simulation
     L = lib.load()
     wl = workloads.WORKLOADS[wname]
     made = wl["params"]()
     p, b0 = made if isinstance(made, tuple) else (made, None)
-    sim = lib.simulation(p, precision=wl["prec"], b0=b0)
-    spin = wl.get("spinup", 0.0) if args.spinup is None else args.spinup
-    if spin > 0.0:
-        sim.integrate_to(spin)
+    if snapshot is not None:
+        sim = Simulation(L, "kg", p, precision=wl["prec"], b0=b0, load_sources=False)
+        sim.load_state(*snapshot)
+    else:
+        sim = lib.simulation(p, precision=wl["prec"], b0=b0)
+        spin = wl.get("spinup", 0.0) if args.spinup is None else args.spinup
+        if spin > 0.0:
+            sim.integrate_to(spin)
     stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
@@ -291,8 +326,13 @@ def fp64_plain(args, wname):
         n += st.steps
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in evs)
+    active = len(sim.active_tiles())
     sim.close()
-    return {"workload": wname, "value": cu / (ms / 1e3), "unit": "cell-updates/s", "steps": n, "ms_per_step": ms / max(n, 1)}
+    out = {"workload": wname, "value": cu / (ms / 1e3), "unit": "cell-updates/s", "steps": n, "ms_per_step": ms / max(n, 1),
+           "active_tiles_end": active}
+    if snapshot is not None:
+        out["start"] = f"restarted from the FP32 run's state at t={snapshot[3]:.3f} s ({len(snapshot[0])} tiles)"
+    return out
 
 
 def main():
@@ -344,13 +384,13 @@ def main():
     # ---- device-timed throughput ----
     sim = lib.simulation(p, precision=wl["prec"], b0=b0)
     spin = wl.get("spinup", 0.0) if args.spinup is None else args.spinup
-    if spin > 0.0:
-        sim.integrate_to(spin)
+    timeline = spin_up(sim, p, spin, wl.get("timeline"))
     stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
     for _ in range(args.warmup):
         sim.step(p.tend)
     torch.cuda.synchronize()
+    snapshot = take_snapshot(sim) if wl.get("twin_restart") else None
     L.kg_set_kernel_timing(sim.h, 1)
     launches0 = L.kg_kernel_launches(sim.h)
     clocks = ClockSampler(local)
@@ -452,10 +492,12 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if timeline:
+        line["config"]["active_timeline"] = timeline
     if wl["prec"] == abi.PREC_FP32 and not args.no_fp64:
         twin = args.workload.replace("_fp32", "_fp64")
         if twin in workloads.WORKLOADS:
-            f64 = fp64_plain(args, twin)
+            f64 = fp64_plain(args, twin, snapshot)
             line["fp64_plain"] = f64
             line["fp32_over_fp64"] = line["value"] / f64["value"] if f64["value"] else None
     if not args.no_cpu_baseline:

@@ -54,9 +54,11 @@ Topog params = ({slope!r})
     return config.parse(text).params
 
 
-def fractal_terrain(nx1: int, ny1: int, dx: float, seed: int, relief: float = 800.0, tilt_deg: float = 8.0) -> np.ndarray:
+def fractal_terrain(nx1: int, ny1: int, dx: float, seed: int, relief: float = 800.0, tilt_deg: float = 8.0,
+                    smooth: float = 0.0) -> np.ndarray:
     """Vertex heights (ny1, nx1): spectral synthesis with P(k) ~ k^-3 (amplitude ~ k^-1.5),
-    min-max scaled to [0, relief], plus a planar tilt descending towards +y."""
+    optionally low-passed by a Gaussian of standard deviation `smooth` metres, min-max
+    scaled to [0, relief], plus a planar tilt descending towards +y."""
     rng = np.random.default_rng(seed)
     kx = np.fft.rfftfreq(nx1)
     ky = np.fft.fftfreq(ny1)
@@ -64,6 +66,8 @@ def fractal_terrain(nx1: int, ny1: int, dx: float, seed: int, relief: float = 80
     k[0, 0] = 1.0
     amp = k ** -1.5
     amp[0, 0] = 0.0
+    if smooth > 0.0:
+        amp = amp * np.exp(-2.0 * math.pi ** 2 * (smooth / dx) ** 2 * k ** 2)
     phase = rng.uniform(0.0, 2.0 * np.pi, size=amp.shape)
     spec = amp * (rng.standard_normal(amp.shape) + 0j) * np.exp(1j * phase)
     field = np.fft.irfft2(spec, s=(ny1, nx1))
@@ -263,22 +267,25 @@ def serve_requests(n: int, rate: float = 20.0, seed: int = 77, sides=(256, 512, 
     return out
 
 
-def sparse_tiles(size: int = 8192, tile: int = 64, dx: float = 2.0, tend: float = 300.0, nout: int = 1, seed: int = 31337):
+def sparse_tiles(size: int = 8192, tile: int = 64, dx: float = 2.0, tend: float = 300.0, nout: int = 1, seed: int = 31337,
+                 relief: float = 400.0, tilt_deg: float = 6.0, smooth: float = 20.0, radius: float = 40.0,
+                 qpeak: tuple = (2000.0, 6000.0)):
     """Large sparse tiled domain: size x size cells at dx (8192^2 at 2 m by default, in
-    tiles of tile^2 cells), the fractal terrain generator with its own seed (relief scaled
-    to the domain as in the ensemble), three flux sources at seeded positions in the
-    middle 60% of the domain with triangular hydrographs (peak 40-120 m^3/s over 100-300 s,
-    concentration 0.2-0.4), Pouliquen-Forterre drag with the reference's defaults,
-    morphodynamics on, sponge edges, to t = 300 s.  Returns (params, b0)."""
+    tiles of tile^2 cells) on fractal terrain with its own seed, low-passed at 20 m (relief
+    0-400 m plus a 6-degree tilt: median slope about 12 degrees, 99th percentile about 28),
+    three flux sources of radius 40 m at seeded positions in the middle 60% of the domain
+    with triangular hydrographs (peak 2000-6000 m^3/s over 100-300 s, concentration
+    0.2-0.4), Pouliquen-Forterre drag with the reference's defaults, morphodynamics on,
+    sponge edges, to t = 300 s.  Returns (params, b0)."""
     rng = np.random.default_rng(seed)
     L = size * dx
     srcs = []
     for k in range(3):
         x, y = (float(v) for v in rng.uniform(-0.3 * L, 0.3 * L, size=2))
         T = float(rng.uniform(100.0, 300.0))
-        q = float(rng.uniform(40.0, 120.0))
+        q = float(rng.uniform(*qpeak))
         cc = float(rng.uniform(0.2, 0.4))
-        srcs.append(f"Source:\n  sourceX = {x!r}\n  sourceY = {y!r}\n  sourceRadius = {3 * dx!r}\n"
+        srcs.append(f"Source:\n  sourceX = {x!r}\n  sourceY = {y!r}\n  sourceRadius = {float(radius)!r}\n"
                     f"  sourceTime = (0,{T / 2!r},{T!r})\n  sourceFlux = (0,{q!r},0)\n  sourceConc = ({cc!r},{cc!r},{cc!r})")
     text = f"""
 Domain:
@@ -303,17 +310,19 @@ Topog function = flat
 """
     p = config.parse(text).params
     p.topog = abi.TOPO["upload"]
-    b0 = fractal_terrain(size + 1, size + 1, dx, seed + 104729, relief=800.0 * min(1.0, L / 10240.0))
+    b0 = fractal_terrain(size + 1, size + 1, dx, seed + 104729, relief=relief, tilt_deg=tilt_deg, smooth=smooth)
     return p, b0
 
 
 WORKLOADS["sparse_8192_fp32"] = dict(
-    desc="large sparse tiled domain: 8192x8192 cells at dx=2 m (128x128 tiles of 64x64), seeded fractal terrain, "
-         "three seeded flux sources, Pouliquen-Forterre drag, morphodynamics on, to t=300 s; FP32 form; timed after "
-         "a spin-up to t=60 s",
-    params=sparse_tiles, prec=abi.PREC_FP32, spinup=60.0)
+    desc="large sparse tiled domain: 8192x8192 cells at dx=2 m (128x128 tiles of 64x64), seeded fractal terrain "
+         "(k^-3 low-passed at 20 m, relief 0-400 m, 6 deg tilt), three seeded flux sources (r=40 m, peak 2000-6000 "
+         "m^3/s over 100-300 s, conc 0.2-0.4), Pouliquen-Forterre drag, mixed erosion, to t=300 s; FP32 form; timed "
+         "after a spin-up to t=240 s",
+    params=sparse_tiles, prec=abi.PREC_FP32, spinup=240.0, timeline=20.0, twin_restart=True)
 WORKLOADS["sparse_8192_fp64"] = dict(
-    desc="large sparse tiled domain: 8192x8192 cells at dx=2 m (128x128 tiles of 64x64), seeded fractal terrain, "
-         "three seeded flux sources, Pouliquen-Forterre drag, morphodynamics on, to t=300 s; FP64 plain; timed after "
-         "a spin-up to t=60 s",
-    params=sparse_tiles, prec=abi.PREC_FP64, spinup=60.0)
+    desc="large sparse tiled domain: 8192x8192 cells at dx=2 m (128x128 tiles of 64x64), seeded fractal terrain "
+         "(k^-3 low-passed at 20 m, relief 0-400 m, 6 deg tilt), three seeded flux sources (r=40 m, peak 2000-6000 "
+         "m^3/s over 100-300 s, conc 0.2-0.4), Pouliquen-Forterre drag, mixed erosion, to t=300 s; FP64 plain; timed "
+         "after a spin-up to t=240 s",
+    params=sparse_tiles, prec=abi.PREC_FP64, spinup=240.0, timeline=20.0)
