@@ -65,7 +65,10 @@ enum { KG_BC_HALT = 0, KG_BC_PERIODIC = 1, KG_BC_DIRICHLET = 2, KG_BC_SPONGE = 3
 /* Analytic topography (src/TopogFuncs.f90) or an uploaded vertex grid (kg_upload_b0). */
 enum { KG_TOPO_UPLOAD = 0, KG_TOPO_FLAT = 1, KG_TOPO_XSLOPE = 2, KG_TOPO_YSLOPE = 3,
        KG_TOPO_XYSLOPE = 4, KG_TOPO_XSINSLOPE = 5, KG_TOPO_XYSINSLOPE = 6, KG_TOPO_XHUMP = 7,
-       KG_TOPO_XTANH = 8, KG_TOPO_XPARAB = 9, KG_TOPO_XYPARAB = 10 };
+       KG_TOPO_XTANH = 8, KG_TOPO_XPARAB = 9, KG_TOPO_XYPARAB = 10,
+       KG_TOPO_RASTER = 11 /* a georeferenced elevation raster (kg_upload_raster) */,
+       KG_TOPO_X2SLOPES = 12, KG_TOPO_USGS = 13, KG_TOPO_FLUME = 14, KG_TOPO_CHANNEL_POWERLAW = 15,
+       KG_TOPO_CHANNEL_TRAPEZIUM = 16, KG_TOPO_XBISLOPE = 17, KG_TOPO_XTRISLOPE = 18 };
 /* Cap / cube shapes: src/InitConds.f90:499-510, :705-712 */
 enum { KG_SHAPE_FLAT = 0, KG_SHAPE_PARA = 1, KG_SHAPE_LEVEL = 2 };
 /* Arithmetic form of the GPU path. */
@@ -161,6 +164,29 @@ const char* kg_last_error(const kg_ctx* ctx);
    (nXtiles*nXpertile+1) x (nYtiles*nYpertile+1) heights, x fastest, vertex (0,0) at the
    south-west domain corner.  Must be called before kg_load_sources when topog==UPLOAD. */
 int  kg_upload_b0(kg_ctx* ctx, const double* b0_vertices, int64_t nx1, int64_t ny1);
+
+/* Georeferencing of an elevation raster, as GDAL reports it for the reference's DEM.vrt
+   (src/RasterData.cpp:160-215): the geotransform's origin and pixel sizes (north-up:
+   pixel_w > 0, pixel_h < 0), the no-data value, and the projected coordinates of the
+   domain centre (RunParams%centerUTM, src/TopogSettings.f90:387). */
+typedef struct {
+    int64_t nx, ny;              /* RasterXSize, RasterYSize */
+    double origin_x, origin_y;   /* geotransform[0], geotransform[3]: upper-left corner */
+    double pixel_w, pixel_h;     /* geotransform[1], geotransform[5] */
+    double nodata;
+    double center_e, center_n;
+} kg_raster;
+
+/* Replaces the raster branch of GetTileHeights (TileHeightData and GetRasterData,
+   src/dem.f90:203-356, with Bicubic_r, src/Interp2d.f90:214-282): values are the raster's
+   ny x nx elevations, row 0 the top (north) row, x fastest (GDAL RasterIO order).  Each
+   tile's vertex heights are the mean of four bicubic samples at the vertex's surrounding
+   cell corners, taken from the tile's own raster section exactly as the reference takes
+   them; a tile whose section leaves the raster or holds the no-data value fails with
+   KG_ERR_PARAM when it is activated (the reference's fatal read errors,
+   src/GeoTiffRead.f90:213-214).  The heights of every tile are computed on the GPU at this
+   call.  Must be called before kg_load_sources when topog==RASTER. */
+int  kg_upload_raster(kg_ctx* ctx, const double* values, const kg_raster* geo);
 
 /* LoadSourceConditions (src/SetSources.f90:47-405): places caps, cubes and flux sources
    and activates (AddTile) every tile that covers them. */

@@ -23,7 +23,13 @@ SWITCH = {"tanh": 0, "rat3": 1, "cos": 2, "linear": 3, "equal": 4, "0.5": 4, "of
 LIMITER = {"minmod1": 0, "minmod2": 1, "van albada": 2, "albada": 2, "weno": 3, "none": 4}
 BCS = {"halt": 0, "periodic": 1, "dirichlet": 2, "sponge": 3}
 TOPO = {"upload": 0, "flat": 1, "xslope": 2, "yslope": 3, "xyslope": 4, "xsinslope": 5,
-        "xysinslope": 6, "xhump": 7, "xtanh": 8, "xparab": 9, "xyparab": 10}
+        "xysinslope": 6, "xhump": 7, "xtanh": 8, "xparab": 9, "xyparab": 10, "raster": 11,
+        "x2slopes": 12, "usgs": 13, "flume": 14, "channel power law": 15, "channel trapezium": 16,
+        "xbislope": 17, "xtrislope": 18}
+# Topog params each analytic surface needs (src/TopogSettings.f90:202-345).
+TOPO_NPARAMS = {"flat": 0, "xslope": 1, "yslope": 1, "xyslope": 2, "x2slopes": 3, "usgs": 2, "flume": 6,
+                "channel power law": 3, "channel trapezium": 3, "xbislope": 3, "xtrislope": 6, "xsinslope": 1,
+                "xysinslope": 1, "xhump": 2, "xtanh": 3, "xparab": 1, "xyparab": 2}
 SHAPE = {"flat": 0, "para": 1, "parabolic": 1, "level": 2}
 PREC_FP64, PREC_FP32 = 0, 1
 
@@ -86,6 +92,12 @@ class StepStats(C.Structure):
                 ("kernel_launches", C.c_int64)]
 
 
+class Raster(C.Structure):
+    """kg_raster: georeferencing of an elevation raster (north-up GDAL geotransform)."""
+    _fields_ = [("nx", C.c_int64), ("ny", C.c_int64)] + [
+        (n, C.c_double) for n in ("origin_x", "origin_y", "pixel_w", "pixel_h", "nodata", "center_e", "center_n")]
+
+
 def declare(lib, prefix):
     """Attach argtypes/restype for the kg_-style API under ``prefix`` ('kg' or 'ko')."""
     P = C.POINTER
@@ -95,6 +107,7 @@ def declare(lib, prefix):
         "destroy": ([vp], None),
         "last_error": ([vp], C.c_char_p),
         "upload_b0": ([vp, P(C.c_double), C.c_int64, C.c_int64], C.c_int),
+        "upload_raster": ([vp, P(C.c_double), P(Raster)], C.c_int),
         "load_sources": ([vp], C.c_int),
         "step": ([vp, C.c_double, P(StepStats)], C.c_int),
         "integrate_to": ([vp, C.c_double, P(StepStats)], C.c_int),

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libkestrel_gb300.so")
-SOURCES = ["kg_lib.cu", "kg_hydro.cu", "kg_hydro32.cu", "kg_tiles.cu", "kg_morpho.cu", "kg_engine.cu", "kg_noalloc.cu", "kg_batch.cu",
+SOURCES = ["kg_lib.cu", "kg_hydro.cu", "kg_hydro32.cu", "kg_tiles.cu", "kg_morpho.cu", "kg_engine.cu", "kg_noalloc.cu", "kg_batch.cu", "kg_dem.cu",
            "kg_engine.cuh", "kg_physics.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -27,6 +27,7 @@ class ParsedInput:
     params: abi.Params
     warnings: list = field(default_factory=list)
     output: dict = field(default_factory=dict)
+    topog: dict = field(default_factory=dict)  # raster inputs: type, raster file, dem directory
 
 
 def _list(v: str):
@@ -107,6 +108,7 @@ def default_params() -> abi.Params:
 def parse(text: str) -> ParsedInput:
     """Parse an input file's text into kg_params (2D runs)."""
     p = default_params()
+    topo = {}
     warn = []
     out = {}
     blocks = read_blocks(text)
@@ -161,7 +163,7 @@ def parse(text: str) -> ParsedInput:
         elif name == "Solver":
             _solver_block(p, kv, warn)
         elif name == "Topog":
-            _topog_block(p, kv, warn)
+            topo = _topog_block(p, kv, warn)
         elif name == "Output":
             for k, v in kv:
                 out[k.lower()] = v
@@ -181,7 +183,7 @@ def parse(text: str) -> ParsedInput:
     _caps(p, caps, warn)
     _cubes(p, cubes, warn)
     _sources(p, srcs, warn)
-    return ParsedInput(params=p, warnings=warn, output=out)
+    return ParsedInput(params=p, warnings=warn, output=out, topog=topo)
 
 
 def _params_block(p, kv, warn):
@@ -299,15 +301,22 @@ def _solver_block(p, kv, warn):
 
 
 def _topog_block(p, kv, warn):
+    """Topog block (src/TopogSettings.f90:88-140).  'Raster'/'DEM' selects the raster
+    topography (the file is read by kestrel_gb300.dem and passed to kg_upload_raster);
+    'SRTM' needs the SRTM tile mosaic built through GDAL and PROJ and is refused."""
     typ = None
+    extra = {}
     for k, v in kv:
         key = k.lower()
         if key == "type":
             typ = v.strip().lower()
+            extra["type"] = typ
+        elif key in ("raster file", "dem directory", "embed raster", "rebuild dem"):
+            extra[key] = v.strip()
         elif key == "topog function":
             name = v.strip().lower()
-            if name not in abi.TOPO:
-                raise InputError(f"Topog function {v!r} is not implemented")
+            if name not in abi.TOPO_NPARAMS:
+                raise InputError(f"the 'Topog function = {v.strip()}' is not recognized")
             p.topog = abi.TOPO[name]
         elif key == "topog params":
             vals = _list(v)
@@ -316,8 +325,20 @@ def _topog_block(p, kv, warn):
                 p.topog_params[i] = x
         else:
             warn.append(f"Topog: unrecognised {k}")
-    if typ not in (None, "function"):
-        raise InputError("only analytic ('Function') or uploaded topography is supported")
+    if typ in (None, "function"):
+        name = next((n for n, v in abi.TOPO.items() if v == p.topog), None)
+        need = abi.TOPO_NPARAMS.get(name, 0)
+        if p.n_topog_params < need:
+            words = {1: "one", 2: "two", 3: "three", 6: "six"}
+            raise InputError(f"{words.get(need, need)} 'Topog params' are needed for 'Topog function = {name}'; "
+                             f"received {p.n_topog_params}")
+    if typ in ("dem", "raster"):
+        p.topog = abi.TOPO["raster"]
+    elif typ == "srtm":
+        raise InputError("SRTM topography needs the SRTM mosaic built through GDAL and PROJ, which are not available")
+    elif typ not in (None, "function"):
+        raise InputError(f"Topog type {typ!r} is not recognised")
+    return extra
 
 
 def _cap_shape(v):

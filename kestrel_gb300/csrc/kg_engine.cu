@@ -29,6 +29,9 @@ namespace kg {
 size_t hydro_smem_bytes();
 cudaError_t set_constants(const DevParams& p, const DevSource* src, int nsrc, cudaStream_t st);
 cudaError_t launch_hydro(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st);
+// kg_dem.cu
+cudaError_t launch_raster_heights(const double* R, const RasterGeo& g, const double* XV, const double* YV, double* out, int* status,
+                                  cudaStream_t st);
 // kg_tiles.cu
 cudaError_t launch_cell_topo(const DevArrays& A, const int* d_slots, int n, int ts, cudaStream_t st);
 cudaError_t launch_face_bI(const DevArrays& A, const int* d_slots, int n, int ts, int nX, int nY, cudaStream_t st);
@@ -138,6 +141,8 @@ struct kg_ctx {
     double* d_srcRho = nullptr;
     bool src_override = false;
     std::vector<double> upload;          // global vertex grid (KG_TOPO_UPLOAD)
+    double* d_rb0 = nullptr;             // KG_TOPO_RASTER: every tile's vertex heights (device)
+    std::vector<int> raster_status;      // KG_TOPO_RASTER: per tile, 0 ok or the section's failure
     int64_t nx1 = 0, ny1 = 0;
     bool sources_loaded = false;
     int qcur = 0;                        // state buffer holding the solution (0..3)
@@ -377,6 +382,82 @@ void set_kind(kg_ctx& c, int id, int8_t k) {
 // GetHeights (src/dem.f90:360-391) with the analytic surfaces of src/TopogFuncs.f90 or the
 // uploaded vertex grid, evaluated at the vertex coordinates AllocateTopographicData builds
 // (src/UpdateTiles.f90:271-337).
+// The remaining analytic surfaces of src/TopogFuncs.f90 at one vertex (X, Y): x2slopes
+// (:101-135), usgs (:145-183), flume (:197-242), channel_powerlaw (:255-276),
+// channel_trapezium (:288-308), xbislope (:315-337), xtrislope (:346-388).
+inline double more_topo(int kind, const double* P, double X, double Y) {
+    const double pi = PI_D;
+    switch (kind) {
+        case KG_TOPO_X2SLOPES: {
+            double alpha = P[0], beta = P[1], R = P[2];
+            double xc0 = (std::sqrt(1.0 + alpha * alpha) - std::sqrt(1.0 + beta * beta)) * R / (alpha - beta);
+            double zc0 = (alpha * std::sqrt(1.0 + beta * beta) - beta * std::sqrt(1.0 + alpha * alpha)) * R / (alpha - beta);
+            double x1 = xc0 - alpha * R / std::sqrt(1.0 + alpha * alpha);
+            double x2 = xc0 - beta * R / std::sqrt(1.0 + beta * beta);
+            if (X < x1) return -alpha * X;
+            if (X > x2) return -beta * X;
+            return zc0 - std::sqrt(R * R - (X - xc0) * (X - xc0));
+        }
+        case KG_TOPO_USGS:
+        case KG_TOPO_FLUME: {
+            double th0 = 31.0, th1 = 2.4, xwall = 8.5, ww = 2.0, wallH = P[0], sigma = P[1];
+            if (kind == KG_TOPO_FLUME) { th0 = P[0]; th1 = P[1]; xwall = P[2]; ww = P[3]; wallH = P[4]; sigma = P[5]; }
+            double alpha = 8.5 / (std::asinh(-std::tan(4.0 * pi / 180.0)) - std::asinh(-std::tan(th0 * pi / 180.0)));
+            double xc0 = -alpha * std::asinh(-std::tan(th0 * pi / 180.0));
+            double zc0 = -alpha * std::cosh((-xc0) / alpha);
+            double x1 = xc0 + alpha * std::asinh(-std::tan(th1 * pi / 180.0));
+            double b;
+            if (X < 0.0) b = -std::tan(th0 * pi / 180.0) * X;
+            else if (X > x1) b = zc0 + alpha * std::cosh((x1 - xc0) / alpha) - std::tan(th1 * pi / 180.0) * (X - x1);
+            else b = zc0 + alpha * std::cosh((X - xc0) / alpha);
+            if (X < xwall) {
+                if (kind == KG_TOPO_USGS)
+                    b = b + 0.5 * wallH * (std::tanh(sigma * (Y - 1.0)) - std::tanh(sigma * (Y - 2.0)) + std::tanh(sigma * (Y + 2.0)) -
+                                           std::tanh(sigma * (Y + 1.0)));
+                else
+                    b = b + 0.5 * wallH * (std::tanh(sigma * (Y - 0.5 * ww)) - std::tanh(sigma * (Y - 1.5 * ww)) +
+                                           std::tanh(sigma * (Y + 1.5 * ww)) - std::tanh(sigma * (Y + 0.5 * ww)));
+            }
+            return b;
+        }
+        case KG_TOPO_CHANNEL_POWERLAW: {
+            double slope = P[0], W = P[1], alpha = P[2];
+            double costheta = std::cos(std::atan(slope));
+            return slope * X + costheta * std::pow(std::fabs(Y) / W, alpha);
+        }
+        case KG_TOPO_CHANNEL_TRAPEZIUM: {
+            double slope = P[0], W = P[1], Sb = P[2];
+            double costheta = std::cos(std::atan(slope));
+            return slope * X + costheta * std::max(0.0, Sb * (std::fabs(Y) - 0.5 * W));
+        }
+        case KG_TOPO_XBISLOPE: {
+            double phi1 = P[0] * pi / 180.0, phi2 = P[1] * pi / 180.0, lam = P[2];
+            double a1 = std::tan(phi1), a2 = std::tan(phi2);
+            return -0.5 * (a1 + a2) * X + 0.5 * (a1 - a2) * lam * std::log(std::cosh(X / lam));
+        }
+        case KG_TOPO_XTRISLOPE: {
+            double phi1 = P[0] * pi / 180.0, phi2 = P[1] * pi / 180.0, phi3 = P[2] * pi / 180.0;
+            double lam = P[3], x1 = P[4], x2 = P[5];
+            double s1 = std::tan(phi1), s2 = std::tan(phi2), s3 = std::tan(phi3);
+            double c2 = (x1 - 0.5 * lam) * 0.5 * (s1 - s2);
+            double c3 = (x1 + 0.5 * lam) * 0.5 * (s1 - s2) + c2;
+            double c4 = (x2 - 0.5 * lam) * 0.5 * (s2 - s3) + c3;
+            double c5 = (x2 + 0.5 * lam) * 0.5 * (s2 - s3) + c4;
+            if (X < x1 - 0.5 * lam) return s1 * X;
+            if (X < x1 + 0.5 * lam) {
+                double A = 0.5 * (s2 - s1) * lam / pi;
+                return A * std::sin((X - x1) * pi / lam - 0.5 * pi) + 0.5 * (s1 + s2) * X + c2;
+            }
+            if (X < x2 - 0.5 * lam) return s2 * X + c3;
+            if (X < x2 + 0.5 * lam) {
+                double A = 0.5 * (s3 - s2) * lam / pi;
+                return A * std::sin((X - x2) * pi / lam - 0.5 * pi) + 0.5 * (s2 + s3) * X + c4;
+            }
+            return s3 * X + c5;
+        }
+    }
+    return 0.0;
+}
 double topo_value(const kg_ctx& c, int id, int a, int b, double X, double Y) {
     const double* P = c.p.topog_params;
     switch (c.p.topog) {
@@ -398,6 +479,13 @@ double topo_value(const kg_ctx& c, int id, int a, int b, double X, double Y) {
         case KG_TOPO_XTANH: return P[1] * (1.0 + std::tanh((X - P[0]) / P[2]));
         case KG_TOPO_XPARAB: return P[0] * X * X;
         case KG_TOPO_XYPARAB: return P[0] * X * X + P[1] * Y * Y;
+        case KG_TOPO_X2SLOPES:
+        case KG_TOPO_USGS:
+        case KG_TOPO_FLUME:
+        case KG_TOPO_CHANNEL_POWERLAW:
+        case KG_TOPO_CHANNEL_TRAPEZIUM:
+        case KG_TOPO_XBISLOPE:
+        case KG_TOPO_XTRISLOPE: return more_topo(c.p.topog, P, X, Y);
         default: {
             int gi = tile_col(c, id), gj = tile_row(c, id);
             int64_t vx = (int64_t)(gi - 1) * c.nX + a, vy = (int64_t)(gj - 1) * c.nY + b;
@@ -405,17 +493,35 @@ double topo_value(const kg_ctx& c, int id, int a, int b, double X, double Y) {
         }
     }
 }
+// Vertex coordinates of tile column gi / row gj (x_vertex, y_vertex of
+// src/UpdateTiles.f90:308-325).
+void vertex_x(const kg_ctx& c, int gi, double* xv) {
+    for (int ii = 1; ii <= c.nX; ++ii) xv[ii - 1] = cell_x(c, gi, ii) - 0.5 * c.dp.dx;
+    xv[c.nX] = cell_x(c, gi, c.nX) + 0.5 * c.dp.dx;
+}
+void vertex_y(const kg_ctx& c, int gj, double* yv) {
+    for (int jj = 1; jj <= c.nY; ++jj) yv[jj - 1] = cell_y(c, gj, jj) - 0.5 * c.dp.dy;
+    yv[c.nY] = cell_y(c, gj, c.nY) + 0.5 * c.dp.dy;
+}
 void get_heights(kg_ctx& c, int id) {
     int s = T(c, id).slot, nX = c.nX, nY = c.nY, gi = tile_col(c, id), gj = tile_row(c, id);
     std::vector<double> xv(nX + 1), yv(nY + 1);
-    for (int ii = 1; ii <= nX; ++ii) xv[ii - 1] = cell_x(c, gi, ii) - 0.5 * c.dp.dx;
-    xv[nX] = cell_x(c, gi, nX) + 0.5 * c.dp.dx;
-    for (int jj = 1; jj <= nY; ++jj) yv[jj - 1] = cell_y(c, gj, jj) - 0.5 * c.dp.dy;
-    yv[nY] = cell_y(c, gj, nY) + 0.5 * c.dp.dy;
+    vertex_x(c, gi, xv.data());
+    vertex_y(c, gj, yv.data());
     std::vector<double>& b0 = c.hb0[s];
     b0.assign((size_t)c.SV, 0.0);
-    for (int b = 0; b <= nY; ++b)
-        for (int a = 0; a <= nX; ++a) b0[(size_t)b * (nX + 1) + a] = topo_value(c, id, a, b, xv[a], yv[b]);
+    if (c.p.topog == KG_TOPO_RASTER) {
+        // The raster section read fails as in GeoTiffArraySectionRead (src/GeoTiffRead.f90:213-214).
+        int st = c.raster_status[(size_t)id - 1];
+        if (st == 1) throw KgError(KG_ERR_PARAM, "Could not read raster file: the section of tile " + std::to_string(id) + " leaves the raster");
+        if (st == 2) throw KgError(KG_ERR_PARAM, "No-data value found in raster file (section of tile " + std::to_string(id) + ")");
+        if (st != 0) throw KgError(KG_ERR_PARAM, "raster section of tile " + std::to_string(id) + " too small for its bicubic samples");
+        CK(cudaMemcpyAsync(b0.data(), c.d_rb0 + (size_t)(id - 1) * c.SV, (size_t)c.SV * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        sync(c);
+    } else {
+        for (int b = 0; b <= nY; ++b)
+            for (int a = 0; a <= nX; ++a) b0[(size_t)b * (nX + 1) + a] = topo_value(c, id, a, b, xv[a], yv[b]);
+    }
     c.hfx0[s].assign((size_t)c.SFX, 0.0);
     c.hfy0[s].assign((size_t)c.SFY, 0.0);
     for (int j = 0; j < nY; ++j)
@@ -1477,6 +1583,7 @@ void free_ctx(kg_ctx* c) {
         cudaFree(c->A.TD[b]); cudaFree(c->A.TF[b]); cudaFree(c->A.TFX[b]); cudaFree(c->A.TFY[b]);
     }
     cudaFree(c->d_tlist);
+    cudaFree(c->d_rb0);
     void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
                     c->d_vol, c->d_srcHn, c->d_srcRho, c->d_ckey, c->d_cex, c->d_src,
@@ -1590,11 +1697,60 @@ int kg_upload_b0(kg_ctx* c, const double* b0, int64_t nx1, int64_t ny1) {
     return KG_OK;
 }
 
+// Every tile's vertex heights from the raster, on the GPU (kg_dem.cu), kept on the device
+// until the tiles are activated.
+void upload_raster(kg_ctx& c, const double* values, const kg_raster& g) {
+    RasterGeo G{g.nx, g.ny, g.origin_x, g.origin_y, g.pixel_w, g.pixel_h, g.nodata, g.center_e, g.center_n,
+                c.dp.dx, c.dp.dy, c.nX, c.nY, c.nXt, c.nYt};
+    std::vector<double> XV((size_t)c.nXt * (c.nX + 1)), YV((size_t)c.nYt * (c.nY + 1));
+    for (int gi = 1; gi <= c.nXt; ++gi) vertex_x(c, gi, XV.data() + (size_t)(gi - 1) * (c.nX + 1));
+    for (int gj = 1; gj <= c.nYt; ++gj) vertex_y(c, gj, YV.data() + (size_t)(gj - 1) * (c.nY + 1));
+    double *dR = nullptr, *dXV = nullptr, *dYV = nullptr;
+    int* dst = nullptr;
+    size_t nR = (size_t)g.nx * (size_t)g.ny;
+    auto release = [&]() { cudaFree(dR); cudaFree(dXV); cudaFree(dYV); cudaFree(dst); };
+    try {
+        if (!c.d_rb0) CK(cudaMalloc(&c.d_rb0, (size_t)c.nTiles * c.SV * sizeof(double)));
+        CK(cudaMalloc(&dR, nR * sizeof(double)));
+        CK(cudaMalloc(&dXV, XV.size() * sizeof(double)));
+        CK(cudaMalloc(&dYV, YV.size() * sizeof(double)));
+        CK(cudaMalloc(&dst, (size_t)c.nTiles * sizeof(int)));
+        CK(cudaMemcpyAsync(dR, values, nR * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(dXV, XV.data(), XV.size() * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(cudaMemcpyAsync(dYV, YV.data(), YV.size() * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(launch_raster_heights(dR, G, dXV, dYV, c.d_rb0, dst, c.st));
+        c.launches++;
+        c.raster_status.assign((size_t)c.nTiles, 0);
+        CK(cudaMemcpyAsync(c.raster_status.data(), dst, (size_t)c.nTiles * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        sync(c);
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
+}
+
+int kg_upload_raster(kg_ctx* c, const double* values, const kg_raster* geo) {
+    if (!c || !values || !geo) return KG_ERR_PARAM;
+    KG_ENTER(c);
+    if (c->p.topog != KG_TOPO_RASTER) { c->err = "topog is not RASTER"; return KG_ERR_STATE; }
+    if (c->sources_loaded) { c->err = "sources already loaded"; return KG_ERR_STATE; }
+    if (geo->nx < 1 || geo->ny < 1 || !(geo->pixel_w > 0.0) || !(geo->pixel_h < 0.0) || !std::isfinite(geo->origin_x) ||
+        !std::isfinite(geo->origin_y) || !std::isfinite(geo->pixel_w) || !std::isfinite(geo->pixel_h) ||
+        !std::isfinite(geo->center_e) || !std::isfinite(geo->center_n)) {
+        c->err = "raster needs nx, ny >= 1, finite georeferencing, pixel_w > 0 and pixel_h < 0 (north-up)";
+        return KG_ERR_PARAM;
+    }
+    KG_GUARD(c, upload_raster(*c, values, *geo));
+    return KG_OK;
+}
+
 int kg_load_sources(kg_ctx* c) {
     if (!c) return KG_ERR_PARAM;
     KG_ENTER(c);
     if (c->sources_loaded) { c->err = "sources already loaded"; return KG_ERR_STATE; }
     if (c->p.topog == KG_TOPO_UPLOAD && c->upload.empty()) { c->err = "no topography uploaded"; return KG_ERR_STATE; }
+    if (c->p.topog == KG_TOPO_RASTER && c->raster_status.empty()) { c->err = "no raster uploaded"; return KG_ERR_STATE; }
     c->gen++;
     KG_GUARD(c, load_sources(*c));
     return KG_OK;

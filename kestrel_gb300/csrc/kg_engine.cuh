@@ -105,4 +105,11 @@ struct StepArgs {
     int partial;     // fewer active tiles than tiles: the advised dt is capped by maxdt
 };
 
+// Georeferencing of an elevation raster for the vertex-height kernel (kg_dem.cu).
+struct RasterGeo {
+    long long nx, ny;
+    double ox, oy, pw, ph, nodata, ce, cn, dx, dy;
+    int nX, nY, nXt, nYt;
+};
+
 }  // namespace kg

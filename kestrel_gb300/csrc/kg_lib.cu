@@ -3,6 +3,7 @@
 #include "kg_hydro.cu"
 #include "kg_hydro32.cu"
 #include "kg_tiles.cu"
+#include "kg_dem.cu"
 
 #include "kg_morpho.cu"
 #include "kg_engine.cu"

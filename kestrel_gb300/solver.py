@@ -24,7 +24,7 @@ class Simulation:
     """One simulation on one context.  ``lib``/``prefix`` select the implementation."""
 
     def __init__(self, lib, prefix: str, params: abi.Params, precision: int = abi.PREC_FP64,
-                 b0: np.ndarray | None = None, load_sources: bool = True):
+                 b0: np.ndarray | None = None, load_sources: bool = True, raster: dict | None = None):
         self.lib, self.pre = lib, prefix
         self.params = params
         self.nX, self.nY = params.nXpertile, params.nYpertile
@@ -38,6 +38,8 @@ class Simulation:
         self.h = h
         if b0 is not None:
             self.upload_b0(b0)
+        if raster is not None:
+            self.upload_raster(**raster)
         if load_sources:
             self._check(self._f("load_sources")(self.h))
 
@@ -77,6 +79,16 @@ class Simulation:
         b0 = np.ascontiguousarray(b0, dtype=np.float64)
         ny1, nx1 = b0.shape
         self._check(self._f("upload_b0")(self.h, b0.ctypes.data_as(C.POINTER(C.c_double)), nx1, ny1))
+
+    def upload_raster(self, values: np.ndarray, origin, pixel, nodata: float, center=(0.0, 0.0)):
+        """kg_upload_raster: an elevation raster (ny, nx), row 0 the north row, with its
+        geotransform origin (x, y) of the upper-left corner, pixel sizes (w, h) with h < 0,
+        no-data value and the projected domain centre (E, N)."""
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        ny, nx = v.shape
+        g = abi.Raster(nx=nx, ny=ny, origin_x=float(origin[0]), origin_y=float(origin[1]), pixel_w=float(pixel[0]),
+                       pixel_h=float(pixel[1]), nodata=float(nodata), center_e=float(center[0]), center_n=float(center[1]))
+        self._check(self._f("upload_raster")(self.h, v.ctypes.data_as(C.POINTER(C.c_double)), C.byref(g)))
 
     def load_state(self, ids, state: np.ndarray, bt_vertex: np.ndarray | None, t: float):
         """kg_load_state: restart from saved tiles (state (n, 4, nY, nX): w, rhoHnu, rhoHnv,

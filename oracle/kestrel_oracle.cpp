@@ -828,8 +828,24 @@ int ko_upload_b0(ko_ctx* c, const double* b0, int64_t nx1, int64_t ny1) {
     c->s.g.b0_upload.assign(b0, b0 + nx1 * ny1);
     return KG_OK;
 }
+int ko_upload_raster(ko_ctx* c, const double* values, const kg_raster* geo) {
+    if (!c || !values || !geo) return KG_ERR_PARAM;
+    if (c->s.rp.p.topog != KG_TOPO_RASTER) { c->s.err = "topog is not RASTER"; return KG_ERR_STATE; }
+    if (geo->nx < 1 || geo->ny < 1 || !(geo->pixel_w > 0.0) || !(geo->pixel_h < 0.0)) {
+        c->s.err = "raster needs nx, ny >= 1, pixel_w > 0 and pixel_h < 0 (north-up)";
+        return KG_ERR_PARAM;
+    }
+    ko::Raster& R = c->s.g.raster;
+    R.values.assign(values, values + geo->nx * geo->ny);
+    R.nx = geo->nx; R.ny = geo->ny;
+    R.originX = geo->origin_x; R.originY = geo->origin_y;
+    R.pixelWidth = geo->pixel_w; R.pixelHeight = geo->pixel_h;
+    R.nodata = geo->nodata; R.centerE = geo->center_e; R.centerN = geo->center_n;
+    return KG_OK;
+}
 int ko_load_sources(ko_ctx* c) {
     if (c->s.rp.p.topog == KG_TOPO_UPLOAD && c->s.g.b0_upload.empty()) { c->s.err = "no topography uploaded"; return KG_ERR_STATE; }
+    if (c->s.rp.p.topog == KG_TOPO_RASTER && c->s.g.raster.values.empty()) { c->s.err = "no raster uploaded"; return KG_ERR_STATE; }
     KO_TRY(c, { ko::LoadSourceConditions(c->s); c->s.sources_loaded = true; })
 }
 int ko_step(ko_ctx* c, double t_stop, kg_step_stats* st) {

@@ -3,8 +3,23 @@
 // src/MorphodynamicRHS.f90 (topographic interpolation) and src/HydraulicRHS.f90.
 #pragma once
 #include "ko_model.hpp"
+#include <stdexcept>
 
 namespace ko {
+
+struct KoError : std::runtime_error {
+    int code;
+    KoError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// An elevation raster as GDAL presents the reference's DEM.vrt (src/RasterData.cpp:160-215):
+// values row-major from the top row, the geotransform origin and pixel sizes, the no-data
+// value, and the projected domain centre (RunParams%centerUTM).
+struct Raster {
+    std::vector<double> values;
+    int64_t nx = 0, ny = 0;
+    double originX = 0, originY = 0, pixelWidth = 0, pixelHeight = 0, nodata = 0, centerE = 0, centerN = 0;
+};
 
 typedef std::vector<Tile> Tiles;
 
@@ -19,6 +34,7 @@ struct Grid {
     double t = 0.0, t0 = 0.0, dt = 1.0e-5;
     std::vector<double> b0_upload;  // global vertex grid when topog == KG_TOPO_UPLOAD
     int64_t nx1 = 0, ny1 = 0;
+    Raster raster;                  // when topog == KG_TOPO_RASTER
     Tile& tc(int id) { return tileContainer[(size_t)id - 1]; }
 };
 inline Tile& TL(Tiles& t, int id) { return t[(size_t)id - 1]; }
@@ -57,6 +73,83 @@ inline bool IsActiveGhostTile(Grid& g, int id) {
 }
 
 // ---------------------------------------------------------------- topography
+// The remaining analytic surfaces of src/TopogFuncs.f90 at one vertex (X, Y): x2slopes
+// (:101-135), usgs (:145-183), flume (:197-242), channel_powerlaw (:255-276),
+// channel_trapezium (:288-308), xbislope (:315-337), xtrislope (:346-388).
+inline double OtherTopogFunc(int kind, const double* P, double X, double Y) {
+    const double pi = PI;
+    switch (kind) {
+        case KG_TOPO_X2SLOPES: {
+            double alpha = P[0], beta = P[1], R = P[2];
+            double xc0 = (std::sqrt(1.0 + alpha * alpha) - std::sqrt(1.0 + beta * beta)) * R / (alpha - beta);
+            double zc0 = (alpha * std::sqrt(1.0 + beta * beta) - beta * std::sqrt(1.0 + alpha * alpha)) * R / (alpha - beta);
+            double x1 = xc0 - alpha * R / std::sqrt(1.0 + alpha * alpha);
+            double x2 = xc0 - beta * R / std::sqrt(1.0 + beta * beta);
+            if (X < x1) return -alpha * X;
+            if (X > x2) return -beta * X;
+            return zc0 - std::sqrt(R * R - (X - xc0) * (X - xc0));
+        }
+        case KG_TOPO_USGS:
+        case KG_TOPO_FLUME: {
+            double th0 = 31.0, th1 = 2.4, xwall = 8.5, ww = 2.0, wallH = P[0], sigma = P[1];
+            if (kind == KG_TOPO_FLUME) { th0 = P[0]; th1 = P[1]; xwall = P[2]; ww = P[3]; wallH = P[4]; sigma = P[5]; }
+            double alpha = 8.5 / (std::asinh(-std::tan(4.0 * pi / 180.0)) - std::asinh(-std::tan(th0 * pi / 180.0)));
+            double xc0 = -alpha * std::asinh(-std::tan(th0 * pi / 180.0));
+            double zc0 = -alpha * std::cosh((-xc0) / alpha);
+            double x1 = xc0 + alpha * std::asinh(-std::tan(th1 * pi / 180.0));
+            double b;
+            if (X < 0.0) b = -std::tan(th0 * pi / 180.0) * X;
+            else if (X > x1) b = zc0 + alpha * std::cosh((x1 - xc0) / alpha) - std::tan(th1 * pi / 180.0) * (X - x1);
+            else b = zc0 + alpha * std::cosh((X - xc0) / alpha);
+            if (X < xwall) {
+                if (kind == KG_TOPO_USGS)
+                    b = b + 0.5 * wallH * (std::tanh(sigma * (Y - 1.0)) - std::tanh(sigma * (Y - 2.0)) + std::tanh(sigma * (Y + 2.0)) -
+                                           std::tanh(sigma * (Y + 1.0)));
+                else
+                    b = b + 0.5 * wallH * (std::tanh(sigma * (Y - 0.5 * ww)) - std::tanh(sigma * (Y - 1.5 * ww)) +
+                                           std::tanh(sigma * (Y + 1.5 * ww)) - std::tanh(sigma * (Y + 0.5 * ww)));
+            }
+            return b;
+        }
+        case KG_TOPO_CHANNEL_POWERLAW: {
+            double slope = P[0], W = P[1], alpha = P[2];
+            double costheta = std::cos(std::atan(slope));
+            return slope * X + costheta * std::pow(std::fabs(Y) / W, alpha);
+        }
+        case KG_TOPO_CHANNEL_TRAPEZIUM: {
+            double slope = P[0], W = P[1], Sb = P[2];
+            double costheta = std::cos(std::atan(slope));
+            return slope * X + costheta * std::max(0.0, Sb * (std::fabs(Y) - 0.5 * W));
+        }
+        case KG_TOPO_XBISLOPE: {
+            double phi1 = P[0] * pi / 180.0, phi2 = P[1] * pi / 180.0, lam = P[2];
+            double a1 = std::tan(phi1), a2 = std::tan(phi2);
+            return -0.5 * (a1 + a2) * X + 0.5 * (a1 - a2) * lam * std::log(std::cosh(X / lam));
+        }
+        case KG_TOPO_XTRISLOPE: {
+            double phi1 = P[0] * pi / 180.0, phi2 = P[1] * pi / 180.0, phi3 = P[2] * pi / 180.0;
+            double lam = P[3], x1 = P[4], x2 = P[5];
+            double s1 = std::tan(phi1), s2 = std::tan(phi2), s3 = std::tan(phi3);
+            double c2 = (x1 - 0.5 * lam) * 0.5 * (s1 - s2);
+            double c3 = (x1 + 0.5 * lam) * 0.5 * (s1 - s2) + c2;
+            double c4 = (x2 - 0.5 * lam) * 0.5 * (s2 - s3) + c3;
+            double c5 = (x2 + 0.5 * lam) * 0.5 * (s2 - s3) + c4;
+            if (X < x1 - 0.5 * lam) return s1 * X;
+            if (X < x1 + 0.5 * lam) {
+                double A = 0.5 * (s2 - s1) * lam / pi;
+                return A * std::sin((X - x1) * pi / lam - 0.5 * pi) + 0.5 * (s1 + s2) * X + c2;
+            }
+            if (X < x2 - 0.5 * lam) return s2 * X + c3;
+            if (X < x2 + 0.5 * lam) {
+                double A = 0.5 * (s3 - s2) * lam / pi;
+                return A * std::sin((X - x2) * pi / lam - 0.5 * pi) + 0.5 * (s2 + s3) * X + c4;
+            }
+            return s3 * X + c5;
+        }
+    }
+    return 0.0;
+}
+
 // TopogFuncs.f90 analytic surfaces evaluated on vertex coordinates (x, y), plus the
 // uploaded-grid replacement of GetTileHeights for the synthetic terrains.
 inline void TopogFunc(const RunSet& rp, const Grid& g, int tileid, const std::vector<double>& x,
@@ -89,6 +182,13 @@ inline void TopogFunc(const RunSet& rp, const Grid& g, int tileid, const std::ve
                 case KG_TOPO_XTANH: b = P[1] * (1.0 + std::tanh((X - P[0]) / P[2])); break;
                 case KG_TOPO_XPARAB: b = P[0] * X * X; break;
                 case KG_TOPO_XYPARAB: b = P[0] * X * X + P[1] * Y * Y; break;
+                case KG_TOPO_X2SLOPES:
+                case KG_TOPO_USGS:
+                case KG_TOPO_FLUME:
+                case KG_TOPO_CHANNEL_POWERLAW:
+                case KG_TOPO_CHANNEL_TRAPEZIUM:
+                case KG_TOPO_XBISLOPE:
+                case KG_TOPO_XTRISLOPE: b = OtherTopogFunc(rp.p.topog, P, X, Y); break;
                 case KG_TOPO_UPLOAD: {
                     int gi, gj;
                     GridCoords(tileid, g, gi, gj);
@@ -102,13 +202,118 @@ inline void TopogFunc(const RunSet& rp, const Grid& g, int tileid, const std::ve
         }
 }
 
+// A raster section read the way GetRasterData reads one (src/dem.f90:203-256):
+// bandSection(i, j) = pixel (xoff + i - 1, yoff + j - 1) of the full raster, with the
+// section's own geotransform origin (src/RasterData.cpp:190-199).
+struct BandSection {
+    int xoff, yoff, xsize, ysize;
+    double rOX, rOY;
+    const Raster* r;
+    double operator()(int i, int j) const { return r->values[(size_t)((int64_t)(yoff + j - 1) * r->nx + (xoff + i - 1))]; }
+};
+
+// Bicubic_r, src/Interp2d.f90:214-282 (coefficient matrix m at :53-70).
+inline double Bicubic(double x, double y, const BandSection& z) {
+    static const double m[16][16] = {
+        {1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
+        {0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0},
+        {-3, 0, 3, 0, 0, 0, 0, 0, -2, 0, -1, 0, 0, 0, 0, 0},
+        {2, 0, -2, 0, 0, 0, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0},
+        {0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
+        {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0},
+        {0, 0, 0, 0, -3, 0, 3, 0, 0, 0, 0, 0, -2, 0, -1, 0},
+        {0, 0, 0, 0, 2, 0, -2, 0, 0, 0, 0, 0, 1, 0, 1, 0},
+        {-3, 3, 0, 0, -2, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
+        {0, 0, 0, 0, 0, 0, 0, 0, -3, 3, 0, 0, -2, -1, 0, 0},
+        {9, -9, -9, 9, 6, 3, -6, -3, 6, -6, 3, -3, 4, 2, 2, 1},
+        {-6, 6, 6, -6, -4, -2, 4, 2, -3, 3, -3, 3, -2, -1, -2, -1},
+        {2, -2, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0},
+        {0, 0, 0, 0, 0, 0, 0, 0, 2, -2, 0, 0, 1, 1, 0, 0},
+        {-6, 6, 6, -6, -3, -3, 3, 3, -4, 4, -2, 2, -2, -2, -1, -1},
+        {4, -4, -4, 4, 2, 2, -2, -2, 2, -2, 2, -2, 1, 1, 1, 1}};
+    int x0 = (int)std::floor(x), x1 = (int)std::ceil(x), y0 = (int)std::floor(y), y1 = (int)std::ceil(y);
+    if (x0 - 1 < 1 || x1 + 1 > z.xsize || y0 - 1 < 1 || y1 + 1 > z.ysize)
+        throw KoError(KG_ERR_PARAM, "bicubic sample outside its raster section");
+    double fVec[16];
+    fVec[0] = z(x0, y0);
+    fVec[1] = z(x1, y0);
+    fVec[2] = z(x0, y1);
+    fVec[3] = z(x1, y1);
+    fVec[4] = (z(x1, y0) - z(x0 - 1, y0)) / (double)(x1 - x0 + 1);
+    fVec[5] = (z(x1 + 1, y0) - z(x0, y0)) / (double)(x1 + 1 - x0);
+    fVec[6] = (z(x1, y1) - z(x0 - 1, y1)) / (double)(x1 - x0 + 1);
+    fVec[7] = (z(x1 + 1, y1) - z(x0, y1)) / (double)(x1 + 1 - x0);
+    fVec[8] = (z(x0, y1) - z(x0, y0 - 1)) / (double)(y1 - y0 + 1);
+    fVec[9] = (z(x1, y1) - z(x1, y0 - 1)) / (double)(y1 - y0 + 1);
+    fVec[10] = (z(x0, y1 + 1) - z(x0, y0)) / (double)(y1 + 1 - y0);
+    fVec[11] = (z(x1, y1 + 1) - z(x1, y0)) / (double)(y1 + 1 - y0);
+    fVec[12] = ((z(x1, y1) - z(x0 - 1, y1)) - (z(x1, y0 - 1) - z(x0 - 1, y0 - 1))) / (double)(x1 - x0 + 1) / (double)(y1 - y0 + 1);
+    fVec[13] = ((z(x1 + 1, y1) - z(x0, y1)) - (z(x1 + 1, y0 - 1) - z(x0, y0 - 1))) / (double)(x1 + 1 - x0) / (double)(y1 - y0 + 1);
+    fVec[14] = ((z(x1, y1 + 1) - z(x0 - 1, y1 + 1)) - (z(x1, y0) - z(x0 - 1, y0))) / (double)(x1 - x0 + 1) / (double)(y1 + 1 - y0);
+    fVec[15] = ((z(x1 + 1, y1 + 1) - z(x0, y1 + 1)) - (z(x1 + 1, y0) - z(x0, y0))) / (double)(x1 + 1 - x0) / (double)(y1 + 1 - y0);
+    double aVec[16];
+    for (int i = 0; i < 16; ++i) {  // matmul(m, fVec)
+        aVec[i] = 0.0;
+        for (int j = 0; j < 16; ++j) aVec[i] = aVec[i] + m[i][j] * fVec[j];
+    }
+    double a[4][4];  // reshape(aVec, (/4,4/), order=(/2,1/))
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) a[i][j] = aVec[i * 4 + j];
+    double t = (x == (double)x0) ? 0.0 : (x - x0) / (double)(x1 - x0);
+    double u = (y == (double)y0) ? 0.0 : (y - y0) / (double)(y1 - y0);
+    double ans = 0.0;
+    for (int i = 3; i >= 0; --i) ans = t * ans + ((a[i][3] * u + a[i][2]) * u + a[i][1]) * u + a[i][0];
+    return ans;
+}
+
+// TileHeightData, src/dem.f90:260-356, with its raster read (GetRasterData, :203-256;
+// GeoTiffArraySectionRead's failures, src/GeoTiffRead.f90:213-214, become errors).
+inline void TileHeightData(const RunSet& rp, const Grid& g, const std::vector<double>& xtile, const std::vector<double>& ytile,
+                           A2& b0) {
+    const Raster& R = g.raster;
+    int nX = rp.nXpertile, nY = rp.nYpertile;
+    double nwE = R.centerE + (xtile[0] - 0.5 * g.deltaX), nwN = R.centerN + (ytile[nY] + 0.5 * g.deltaY);
+    double seE = R.centerE + (xtile[nX] + 0.5 * g.deltaX), seN = R.centerN + (ytile[0] - 0.5 * g.deltaY);
+    BandSection z;
+    z.r = &R;
+    double imgx = (nwE - R.originX) / R.pixelWidth, imgy = (nwN - R.originY) / R.pixelHeight;
+    z.xoff = (int)std::floor(imgx) - 2;
+    z.yoff = (int)std::floor(imgy) - 2;
+    z.xsize = (int)std::ceil((seE - nwE) / R.pixelWidth) + 5;
+    z.ysize = (int)std::ceil((seN - nwN) / R.pixelHeight) + 5;
+    if (z.xoff < 0 || z.yoff < 0 || z.xoff + (int64_t)z.xsize > R.nx || z.yoff + (int64_t)z.ysize > R.ny)
+        throw KoError(KG_ERR_PARAM, "Could not read raster file: tile section outside the raster");
+    z.rOX = R.originX + z.xoff * R.pixelWidth;
+    z.rOY = R.originY + z.yoff * R.pixelHeight;
+    for (int j = 1; j <= z.ysize; ++j)
+        for (int i = 1; i <= z.xsize; ++i)
+            if (z(i, j) == R.nodata) throw KoError(KG_ERR_PARAM, "No-data value found in raster file");
+    for (int i = 1; i <= nX + 1; ++i)
+        for (int j = 1; j <= nY + 1; ++j) {
+            double hcorner[4];
+            for (int ii = 1; ii <= 2; ++ii)
+                for (int jj = 1; jj <= 2; ++jj) {
+                    int k = jj + 2 * (ii - 1);
+                    double E = R.centerE + xtile[i - 1] + ((double)(ii - 1) - 0.5) * g.deltaX;
+                    double N = R.centerN + ytile[j - 1] + ((double)(jj - 1) - 0.5) * g.deltaY;
+                    double ix = (E - z.rOX) / R.pixelWidth + 1;
+                    double iy = (N - z.rOY) / R.pixelHeight + 1;
+                    hcorner[k - 1] = Bicubic(ix, iy, z);
+                }
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s = s + hcorner[k];
+            b0(i, j) = 0.25 * s;
+        }
+}
+
 // GetHeights, src/dem.f90:360-391 (2D branch).
 inline void GetHeights(const RunSet& rp, Grid& g, int tID) {
     Tile& T = g.tc(tID);
     int nX = rp.nXpertile, nY = rp.nYpertile;
     A2 b0;
     b0.allocate(nX + 1, nY + 1, 0.0);
-    TopogFunc(rp, g, tID, T.x_vertex, T.y_vertex, b0);
+    if (rp.p.topog == KG_TOPO_RASTER) TileHeightData(rp, g, T.x_vertex, T.y_vertex, b0);
+    else TopogFunc(rp, g, tID, T.x_vertex, T.y_vertex, b0);
     T.b0 = b0;
     for (int i = 1; i <= nY; ++i)
         for (int a = 1; a <= nX + 1; ++a) {

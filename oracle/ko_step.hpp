@@ -9,11 +9,6 @@
 
 namespace ko {
 
-struct KoError : std::runtime_error {
-    int code;
-    KoError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
-};
-
 // ExplicitSourceTerms, src/Equations.f90:456-620; writes ste[0..3] (w, rhoHnu, rhoHnv, Hnpsi).
 inline void ExplicitSourceTerms(const RunSet& rp, const Grid& g, double t, double x, double y, const double* uv,
                                 bool tile_has_source, double* ste) {

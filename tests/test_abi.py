@@ -37,8 +37,9 @@ def test_struct_sizes_match_c():
 #include <stdio.h>
 #include <stddef.h>
 #include "kestrel_gpu.h"
-int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(kg_params), sizeof(kg_cap), sizeof(kg_cube),
- sizeof(kg_flux_source), sizeof(kg_step_stats), offsetof(kg_params, sources), offsetof(kg_params, topog_params));return 0;}
+int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(kg_params), sizeof(kg_cap), sizeof(kg_cube),
+ sizeof(kg_flux_source), sizeof(kg_step_stats), offsetof(kg_params, sources), offsetof(kg_params, topog_params),
+ sizeof(kg_raster), offsetof(kg_raster, center_n));return 0;}
 '''
     with tempfile.TemporaryDirectory() as d:
         cpath, exe = os.path.join(d, "t.c"), os.path.join(d, "t")
@@ -47,7 +48,8 @@ int main(void){printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(kg_params), sizeof
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
     got = [int(x) for x in out]
     want = [C.sizeof(abi.Params), C.sizeof(abi.Cap), C.sizeof(abi.Cube), C.sizeof(abi.FluxSource),
-            C.sizeof(abi.StepStats), abi.Params.sources.offset, abi.Params.topog_params.offset]
+            C.sizeof(abi.StepStats), abi.Params.sources.offset, abi.Params.topog_params.offset,
+            C.sizeof(abi.Raster), abi.Raster.center_n.offset]
     assert got == want
 
 
