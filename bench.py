@@ -288,6 +288,79 @@ def take_snapshot(sim):
     return ids, state, btv, sim.time[0]
 
 
+def run_dem(args):
+    """Raster topography ingestion on the 2048^2 configuration: kg_upload_raster computes
+    every tile's vertex heights (1024 tiles x 65^2 vertices, four bicubic samples each)
+    from a 2.5 m raster of the domain (4128^2 pixels).  value = vertex heights per second
+    of device time (CUDA events on the context's stream around the call, which includes
+    the raster's host-to-device copy); e2e = the same through the host clock.  The CPU
+    baseline is the oracle computing the heights of the tiles its set-up activates."""
+    from kestrel_gb300 import abi, workloads
+    p, r = workloads.dem_2048()
+    nvt = (p.nXpertile + 1) * (p.nYpertile + 1)
+    if args.impl == "reference":
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import _oracle
+        t1 = time.perf_counter()
+        o = _oracle.simulation(p, raster=r)
+        secs = time.perf_counter() - t1
+        nt = len(o.active_tiles()) + len(o.ghost_tiles())
+        v = nt * nvt / secs
+        print(json.dumps({"metric": "vertex-heights/s", "value": v, "unit": "vertex-heights/s", "n_gpus": args.gpus,
+                          "steps": 1, "warmup": 0, "ms_per_step": 1e3 * secs, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                          "config": {"workload": "dem_2048"},
+                          "cpu_baseline": {"value": v, "unit": "vertex-heights/s", "cores": 1, "kind": "port",
+                                           "sample": f"oracle set-up: raster copy, sources and the heights of its {nt} active and ghost tiles"},
+                          "e2e": {"value": v, "unit": "vertex-heights/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    from kestrel_gb300 import lib
+    from kestrel_gb300.solver import Simulation
+    L = lib.load()
+    sim = Simulation(L, "kg", p, precision=abi.PREC_FP64, load_sources=False)
+    stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
+    for _ in range(args.warmup):
+        sim.upload_raster(**r)
+    torch.cuda.synchronize()
+    steps = min(args.steps, 20)
+    clocks = ClockSampler(0)
+    clocks.start()
+    evs, t0 = [], time.perf_counter()
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.upload_raster(**r)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    nv = p.nXtiles * p.nYtiles * nvt
+    sim.close()
+    line = {"metric": "vertex-heights/s", "value": nv * steps / (ms / 1e3), "unit": "vertex-heights/s", "n_gpus": 1,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "dem_2048", "raster": list(r["values"].shape), "pixel_m": r["pixel"][0],
+                       "tiles": p.nXtiles * p.nYtiles, "vertices_per_tile": (p.nXpertile + 1) * (p.nYpertile + 1),
+                       "l2": "inputs (136 MB raster) larger than L2; not flushed"},
+            "e2e": {"value": nv * steps / wall, "unit": "vertex-heights/s", "h2d_bytes_per_step": int(r["values"].nbytes),
+                    "d2h_bytes_per_step": 4 * p.nXtiles * p.nYtiles},
+            "gpu_launches": steps, "clocks": clk}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import _oracle
+        t1 = time.perf_counter()
+        o = _oracle.simulation(p, raster=r)
+        secs = time.perf_counter() - t1
+        nt = len(o.active_tiles()) + len(o.ghost_tiles())
+        line["cpu_baseline"] = {"value": nt * (p.nXpertile + 1) * (p.nYpertile + 1) / secs, "unit": "vertex-heights/s",
+                                "cores": 1, "kind": "port",
+                                "sample": f"oracle set-up: raster copy, sources and the heights of its {nt} active and ghost tiles, {secs:.2f} s"}
+    print(json.dumps(line))
+
+
 def fp64_plain(args, wname, snapshot=None):
     """The plain FP64 drop-in on the same configuration, device-timed the same way (for the
     FP32-vs-FP64 comparison of the headline line).  With a snapshot, the FP64 context is
@@ -360,6 +433,10 @@ def main():
         return run_ensemble(args)
     if args.workload == "serve_fp32" and args.impl == "ours":
         return run_serve(args)
+    if args.workload == "dem_2048":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        return run_dem(args)
     from kestrel_gb300 import workloads
     wl = workloads.WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))

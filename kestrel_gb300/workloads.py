@@ -326,3 +326,17 @@ WORKLOADS["sparse_8192_fp64"] = dict(
          "m^3/s over 100-300 s, conc 0.2-0.4), Pouliquen-Forterre drag, mixed erosion, to t=300 s; FP64 plain; timed "
          "after a spin-up to t=240 s",
     params=sparse_tiles, prec=abi.PREC_FP64, spinup=240.0, timeline=20.0)
+
+
+def dem_2048(seed: int = 1, pixel: float = 2.5, center=(500000.0, 4000000.0)):
+    """The 2048^2 morphodynamic configuration with its bed read from an elevation raster
+    (topog = raster): seeded fractal terrain (k^-3, relief 0-800 m, 8-degree tilt) sampled
+    at `pixel` metres over the domain plus a 40 m margin, north-up, centred on `center`.
+    Returns (params, raster keyword arguments of Simulation.upload_raster)."""
+    p, _ = morpho_flux_2048()
+    p.topog = abi.TOPO["raster"]
+    half = 0.5 * p.nXtiles * p.Xtilesize + 40.0
+    n = int(round(2.0 * half / pixel))
+    z = fractal_terrain(n, n, pixel, seed + 7, relief=800.0, tilt_deg=8.0)[::-1]  # north row first
+    return p, dict(values=np.ascontiguousarray(z), origin=(center[0] - half, center[1] + half), pixel=(pixel, -pixel),
+                   nodata=-9999.0, center=center)
