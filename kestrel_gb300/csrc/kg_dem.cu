@@ -12,7 +12,7 @@
 //
 // One CTA per tile, all tiles at once: a section is a few hundred pixels, read through
 // L1/L2 (neighbouring tiles' sections overlap by 5 pixels), and a vertex costs four
-// 16 x 16 coefficient products in FP64.  The FP64 arithmetic follows the reference's
+// bicubic patches in FP64 (the kernel is bound by the FP64 pipe).  The FP64 arithmetic follows the reference's
 // operation order with no contraction (-fmad=false), so the heights equal the host
 // restatement's bit for bit.
 #include <cuda_runtime.h>
@@ -22,26 +22,38 @@
 namespace kg {
 
 
-// Bicubic_r's coefficient matrix (src/Interp2d.f90:53-70): a = M f with
+// Bicubic_r's coefficients a = m f (src/Interp2d.f90:53-70, matmul order j = 1..16) with
 // f = (corner values, x-derivatives, y-derivatives, cross derivatives) at (0,0), (1,0),
-// (0,1), (1,1).  Stored row-major; the zeros are kept so the sums run in the same order.
-__constant__ double cBicubicM[256] = {
-    1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-    0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0,
-    -3, 0, 3, 0, 0, 0, 0, 0, -2, 0, -1, 0, 0, 0, 0, 0,
-    2, 0, -2, 0, 0, 0, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0,
-    0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0,
-    0, 0, 0, 0, -3, 0, 3, 0, 0, 0, 0, 0, -2, 0, -1, 0,
-    0, 0, 0, 0, 2, 0, -2, 0, 0, 0, 0, 0, 1, 0, 1, 0,
-    -3, 3, 0, 0, -2, -1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-    0, 0, 0, 0, 0, 0, 0, 0, -3, 3, 0, 0, -2, -1, 0, 0,
-    9, -9, -9, 9, 6, 3, -6, -3, 6, -6, 3, -3, 4, 2, 2, 1,
-    -6, 6, 6, -6, -4, -2, 4, 2, -3, 3, -3, 3, -2, -1, -2, -1,
-    2, -2, 0, 0, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-    0, 0, 0, 0, 0, 0, 0, 0, 2, -2, 0, 0, 1, 1, 0, 0,
-    -6, 6, 6, -6, -3, -3, 3, 3, -4, 4, -2, 2, -2, -2, -1, -1,
-    4, -4, -4, 4, 2, 2, -2, -2, 2, -2, 2, -2, 1, 1, 1, 1};
+// (0,1), (1,1).  Only the non-zero entries of m are summed: a product with a zero entry is
+// +-0 and adding it never changes a partial sum that starts at +0 (x + -x rounds to +0),
+// so for finite data the sums equal the full 16-term products bit for bit, at a third of
+// the FP64 operations.
+__device__ __forceinline__ void bicubic_coeffs(const double* f, double* a) {
+    a[0] = 0.0 + f[0];
+    a[1] = 0.0 + f[8];
+    a[2] = (((0.0 + -3.0 * f[0]) + 3.0 * f[2]) + -2.0 * f[8]) - f[10];
+    a[3] = (((0.0 + 2.0 * f[0]) + -2.0 * f[2]) + f[8]) + f[10];
+    a[4] = 0.0 + f[4];
+    a[5] = 0.0 + f[12];
+    a[6] = (((0.0 + -3.0 * f[4]) + 3.0 * f[6]) + -2.0 * f[12]) - f[14];
+    a[7] = (((0.0 + 2.0 * f[4]) + -2.0 * f[6]) + f[12]) + f[14];
+    a[8] = (((0.0 + -3.0 * f[0]) + 3.0 * f[1]) + -2.0 * f[4]) - f[5];
+    a[9] = (((0.0 + -3.0 * f[8]) + 3.0 * f[9]) + -2.0 * f[12]) - f[13];
+    a[10] = (((((((((((((((0.0 + 9.0 * f[0]) + -9.0 * f[1]) + -9.0 * f[2]) + 9.0 * f[3]) + 6.0 * f[4]) + 3.0 * f[5]) +
+                    -6.0 * f[6]) + -3.0 * f[7]) + 6.0 * f[8]) + -6.0 * f[9]) + 3.0 * f[10]) + -3.0 * f[11]) + 4.0 * f[12]) +
+              2.0 * f[13]) + 2.0 * f[14]) + f[15];
+    a[11] = (((((((((((((((0.0 + -6.0 * f[0]) + 6.0 * f[1]) + 6.0 * f[2]) + -6.0 * f[3]) + -4.0 * f[4]) + -2.0 * f[5]) +
+                    4.0 * f[6]) + 2.0 * f[7]) + -3.0 * f[8]) + 3.0 * f[9]) + -3.0 * f[10]) + 3.0 * f[11]) + -2.0 * f[12]) -
+              f[13]) + -2.0 * f[14]) - f[15];
+    a[12] = (((0.0 + 2.0 * f[0]) + -2.0 * f[1]) + f[4]) + f[5];
+    a[13] = (((0.0 + 2.0 * f[8]) + -2.0 * f[9]) + f[12]) + f[13];
+    a[14] = (((((((((((((((0.0 + -6.0 * f[0]) + 6.0 * f[1]) + 6.0 * f[2]) + -6.0 * f[3]) + -3.0 * f[4]) + -3.0 * f[5]) +
+                    3.0 * f[6]) + 3.0 * f[7]) + -4.0 * f[8]) + 4.0 * f[9]) + -2.0 * f[10]) + 2.0 * f[11]) + -2.0 * f[12]) +
+              -2.0 * f[13]) - f[14]) - f[15];
+    a[15] = (((((((((((((((0.0 + 4.0 * f[0]) + -4.0 * f[1]) + -4.0 * f[2]) + 4.0 * f[3]) + 2.0 * f[4]) + 2.0 * f[5]) +
+                    -2.0 * f[6]) + -2.0 * f[7]) + 2.0 * f[8]) + -2.0 * f[9]) + 2.0 * f[10]) + -2.0 * f[11]) + f[12]) +
+              f[13]) + f[14]) + f[15];
+}
 
 // Section of one tile (GetRasterData, src/dem.f90:203-256, and the section geotransform of
 // src/RasterData.cpp:190-199).
@@ -89,13 +101,7 @@ __device__ __forceinline__ bool bicubic(const double* __restrict__ R, long long 
     f[14] = ((z(x1, y1 + 1) - z(x0 - 1, y1 + 1)) - (z(x1, y0) - z(x0 - 1, y0))) / ex0 / ey1;
     f[15] = ((z(x1 + 1, y1 + 1) - z(x0, y1 + 1)) - (z(x1 + 1, y0) - z(x0, y0))) / ex1 / ey1;
     double a[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        double s = 0.0;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) s = s + cBicubicM[i * 16 + j] * f[j];
-        a[i] = s;
-    }
+    bicubic_coeffs(f, a);
     double t = (x == (double)x0) ? 0.0 : (x - x0) / (double)(x1 - x0);
     double u = (y == (double)y0) ? 0.0 : (y - y0) / (double)(y1 - y0);
     double ans = 0.0;
