@@ -81,29 +81,31 @@ __device__ __forceinline__ bool bicubic(const double* __restrict__ R, long long 
     int x0 = (int)floor(x), x1 = (int)ceil(x), y0 = (int)floor(y), y1 = (int)ceil(y);
     if (x0 - 1 < 1 || x1 + 1 > S.xsize || y0 - 1 < 1 || y1 + 1 > S.ysize) return false;
     auto z = [&](int i, int j) { return R[(long long)(S.yoff + j - 1) * nx + (S.xoff + i - 1)]; };
+    // The finite-difference spacings x1 - x0 + 1 and y1 - y0 + 1 are 1 (on a pixel line)
+    // or 2, and the patch width x1 - x0 is 1 off a pixel line: dividing by 1 or 2 is
+    // exactly multiplying by 1 or 0.5, so no FP64 divide is needed.
+    const double sx = (x1 == x0) ? 1.0 : 0.5, sy = (y1 == y0) ? 1.0 : 0.5;
     double f[16];
-    double ex0 = (double)(x1 - x0 + 1), ex1 = (double)(x1 + 1 - x0);
-    double ey0 = (double)(y1 - y0 + 1), ey1 = (double)(y1 + 1 - y0);
     f[0] = z(x0, y0);
     f[1] = z(x1, y0);
     f[2] = z(x0, y1);
     f[3] = z(x1, y1);
-    f[4] = (z(x1, y0) - z(x0 - 1, y0)) / ex0;
-    f[5] = (z(x1 + 1, y0) - z(x0, y0)) / ex1;
-    f[6] = (z(x1, y1) - z(x0 - 1, y1)) / ex0;
-    f[7] = (z(x1 + 1, y1) - z(x0, y1)) / ex1;
-    f[8] = (z(x0, y1) - z(x0, y0 - 1)) / ey0;
-    f[9] = (z(x1, y1) - z(x1, y0 - 1)) / ey0;
-    f[10] = (z(x0, y1 + 1) - z(x0, y0)) / ey1;
-    f[11] = (z(x1, y1 + 1) - z(x1, y0)) / ey1;
-    f[12] = ((z(x1, y1) - z(x0 - 1, y1)) - (z(x1, y0 - 1) - z(x0 - 1, y0 - 1))) / ex0 / ey0;
-    f[13] = ((z(x1 + 1, y1) - z(x0, y1)) - (z(x1 + 1, y0 - 1) - z(x0, y0 - 1))) / ex1 / ey0;
-    f[14] = ((z(x1, y1 + 1) - z(x0 - 1, y1 + 1)) - (z(x1, y0) - z(x0 - 1, y0))) / ex0 / ey1;
-    f[15] = ((z(x1 + 1, y1 + 1) - z(x0, y1 + 1)) - (z(x1 + 1, y0) - z(x0, y0))) / ex1 / ey1;
+    f[4] = (z(x1, y0) - z(x0 - 1, y0)) * sx;
+    f[5] = (z(x1 + 1, y0) - z(x0, y0)) * sx;
+    f[6] = (z(x1, y1) - z(x0 - 1, y1)) * sx;
+    f[7] = (z(x1 + 1, y1) - z(x0, y1)) * sx;
+    f[8] = (z(x0, y1) - z(x0, y0 - 1)) * sy;
+    f[9] = (z(x1, y1) - z(x1, y0 - 1)) * sy;
+    f[10] = (z(x0, y1 + 1) - z(x0, y0)) * sy;
+    f[11] = (z(x1, y1 + 1) - z(x1, y0)) * sy;
+    f[12] = ((z(x1, y1) - z(x0 - 1, y1)) - (z(x1, y0 - 1) - z(x0 - 1, y0 - 1))) * sx * sy;
+    f[13] = ((z(x1 + 1, y1) - z(x0, y1)) - (z(x1 + 1, y0 - 1) - z(x0, y0 - 1))) * sx * sy;
+    f[14] = ((z(x1, y1 + 1) - z(x0 - 1, y1 + 1)) - (z(x1, y0) - z(x0 - 1, y0))) * sx * sy;
+    f[15] = ((z(x1 + 1, y1 + 1) - z(x0, y1 + 1)) - (z(x1 + 1, y0) - z(x0, y0))) * sx * sy;
     double a[16];
     bicubic_coeffs(f, a);
-    double t = (x == (double)x0) ? 0.0 : (x - x0) / (double)(x1 - x0);
-    double u = (y == (double)y0) ? 0.0 : (y - y0) / (double)(y1 - y0);
+    double t = (x == (double)x0) ? 0.0 : (x - x0);
+    double u = (y == (double)y0) ? 0.0 : (y - y0);
     double ans = 0.0;
     for (int i = 3; i >= 0; --i) ans = t * ans + ((a[i * 4 + 3] * u + a[i * 4 + 2]) * u + a[i * 4 + 1]) * u + a[i * 4 + 0];
     h = ans;

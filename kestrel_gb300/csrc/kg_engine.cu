@@ -165,6 +165,11 @@ struct kg_ctx {
     int* d_rcell = nullptr;
     int* d_rwave = nullptr;              // wave offsets of the redistribution list
     int cand_cap = 0;
+    // Pinned copies of the leading candidates, read back with the control block so that a
+    // typical redistribution list needs no second wait; the prefix adapts to the counts seen.
+    unsigned long long* h_ckey = nullptr;
+    double* h_cex = nullptr;
+    int h_cand_cap = 0, cand_pre = 256;
     std::vector<std::vector<int>> redist_grid;  // per-tile wave tables of the redistribution scheduler
     double t = 0.0, dt = 1.0e-5, t0 = 0.0;
     int64_t launches = 0, steps = 0, rejected = 0, cell_updates = 0;
@@ -1106,8 +1111,21 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
     }
     CK(launch_m_check(c.A, dl, n, c.SC, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, fp32, c.st));
     c.launches++;
+    int pre = std::min(c.cand_pre, c.cand_cap);
+    if (pre > c.h_cand_cap) {
+        if (c.h_ckey) CK(cudaFreeHost(c.h_ckey));
+        if (c.h_cex) CK(cudaFreeHost(c.h_cex));
+        c.h_cand_cap = std::max(pre, 2 * c.h_cand_cap);
+        CK(cudaMallocHost(&c.h_ckey, (size_t)c.h_cand_cap * sizeof(unsigned long long)));
+        CK(cudaMallocHost(&c.h_cex, (size_t)c.h_cand_cap * sizeof(double)));
+    }
+    if (pre > 0) {
+        CK(cudaMemcpyAsync(c.h_ckey, c.d_ckey, (size_t)pre * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
+        CK(cudaMemcpyAsync(c.h_cex, c.d_cex, (size_t)pre * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    }
     collect_cfl(c);
     int ncand = c.h_ctl->ncand;
+    c.cand_pre = std::max(256, std::min(1 << 20, 2 * ncand));
     if (c.h_ctl->mflag != 0) {
         dt_m = 0.5 * dt_m;
         dt = 0.5 * dt_m;
@@ -1118,9 +1136,14 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         // (src/Redistribute.f90:69-101); RedistributeGrid then walks that list.
         std::vector<unsigned long long> key((size_t)ncand);
         std::vector<double> ex((size_t)ncand);
-        CK(cudaMemcpyAsync(key.data(), c.d_ckey, (size_t)ncand * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
-        CK(cudaMemcpyAsync(ex.data(), c.d_cex, (size_t)ncand * sizeof(double), cudaMemcpyDeviceToHost, c.st));
-        sync(c);
+        if (ncand <= pre) {
+            std::memcpy(key.data(), c.h_ckey, (size_t)ncand * sizeof(unsigned long long));
+            std::memcpy(ex.data(), c.h_cex, (size_t)ncand * sizeof(double));
+        } else {
+            CK(cudaMemcpyAsync(key.data(), c.d_ckey, (size_t)ncand * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
+            CK(cudaMemcpyAsync(ex.data(), c.d_cex, (size_t)ncand * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+            sync(c);
+        }
         double tp0 = wall();
         std::vector<int> ord((size_t)ncand);
         for (int q = 0; q < ncand; ++q) ord[(size_t)q] = q;
@@ -1139,7 +1162,7 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         CK(cudaMemcpyAsync(c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(cudaMemcpyAsync(c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
         CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, c.d_rwave, woff.data(), nw, qa, c.tcur, tnew, c.d_mflags, fp32, c.st));
-        c.launches += nw <= 64 ? nw : 1;
+        c.launches += nw <= KG_REDIST_WAVE_MAX ? nw : 1;
     }
     // Interfacial topography of the new bed and the M result (both scratch until accepted).
     CK(launch_face_topo(c.A, dl, n, tnew, c.nX, c.nY, fp32, c.st));
@@ -1594,6 +1617,8 @@ void free_ctx(kg_ctx* c) {
         if (c->h_ctl) cudaFreeHost(c->h_ctl);
     }
     if (c->h_act) cudaFreeHost(c->h_act);
+    if (c->h_ckey) cudaFreeHost(c->h_ckey);
+    if (c->h_cex) cudaFreeHost(c->h_cex);
     cudaFree(c->d_active);
     for (int k = 0; k < 4; ++k) {
         if (c->ev0[k]) cudaEventDestroy(c->ev0[k]);

@@ -23,6 +23,12 @@
 #pragma once
 #include "kg_physics.cuh"
 
+// Redistribution lists of at most this many dependency waves run as one launch per wave
+// (every SM takes part); longer ones are walked by a single CTA with barriers between waves.
+#ifndef KG_REDIST_WAVE_MAX
+#define KG_REDIST_WAVE_MAX 64
+#endif
+
 namespace kg {
 
 enum SlotKind : int8_t { SLOT_FREE = 0, SLOT_ACTIVE = 1, SLOT_GHOST = 2 };

@@ -708,7 +708,7 @@ cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int ce
 cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, const int* hwoff, int nwaves,
                             int qa, int tcur, int tnew, int* flags, bool fp32, cudaStream_t st) {
     if (nwaves == 0) return cudaSuccess;
-    if (nwaves > 64) {
+    if (nwaves > KG_REDIST_WAVE_MAX) {
         if (fp32) k_m_redist<true><<<1, REDIST_THREADS, 0, st>>>(A, ls, lc, woff, nwaves, qa, tcur, tnew, flags);
         else k_m_redist<false><<<1, REDIST_THREADS, 0, st>>>(A, ls, lc, woff, nwaves, qa, tcur, tnew, flags);
         return cudaGetLastError();
