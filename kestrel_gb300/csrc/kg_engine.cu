@@ -1557,6 +1557,7 @@ void setup(kg_ctx& c, const kg_params& p) {
     d.SwRate = p.VoellmySwitchRate; d.SwValue = p.VoellmySwitchValue;
     d.EroRate = p.EroRate; d.EroRateGranular = p.EroRateGranular; d.EroDepth = p.EroDepth;
     d.EroCriticalHeight = p.EroCriticalHeight; d.BedPorosity = p.BedPorosity;
+    d.invSolid = 1.0 / (1.0 - p.BedPorosity);
     d.maxPack = p.maxPack; d.SolidDiameter = p.SolidDiameter; d.nu = p.EddyViscosity; d.hThr = p.heightThreshold;
     d.tan1deg = std::tan(PI_D / 180.0);
     d.SpongeStrength = p.SpongeStrength;

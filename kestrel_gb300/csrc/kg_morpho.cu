@@ -28,14 +28,16 @@ constexpr int REDIST_THREADS = 512;
 
 __device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return ((size_t)slot * nf + f) * (size_t)npl; }
 
-// FP32 form: 1/sqrt(x) to FP64 accuracy from an FP32 seed and two Newton steps, and the
-// step-start gamma of a cell from the topography-factor cache (gamma = gamma^2 / gamma).
+// FP32 form: 1/sqrt(x) from an FP32 seed and one Newton step (relative error about 1e-13,
+// far below the form's FP32 error), and the step-start gamma of a cell from the
+// topography-factor cache (gamma = gamma^2 / gamma).
 __device__ __forceinline__ double rsqrt_nr(double x) {
     double y = (double)rsqrtf((float)x);
-    y = y * (1.5 - 0.5 * x * y * y);
-    y = y * (1.5 - 0.5 * x * y * y);
-    return y;
+    return y * (1.5 - 0.5 * x * y * y);
 }
+// Bitwise equality of two doubles on the integer pipe (FP64 compares use the FP64 pipe,
+// 1/64 of the FP32 rate on this GPU); differs from == only for +-0 and NaN.
+__device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
 __device__ __forceinline__ double gam_cached(const DevParams& P, const DevArrays& A, int ts, int s, int c, double bx, double by) {
     if (!P.geo) return 1.0;
     int SC = P.nX * P.nY;
@@ -261,9 +263,9 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
             // the M set is still the step-start one, keeps its current stage state.
             const double* bt0 = A.BV[tcur] + mp(s, 2, 1, SV);
             const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
-            if (bt[v00] == bt0[v00] && bt[v10] == bt0[v10] && bt[v01] == bt0[v01] && bt[v11] == bt0[v11] &&
-                C3[mp(s, 4, 1, SC) + c] == C0[mp(s, 4, 1, SC) + c] && C3[mp(s, 4, 2, SC) + c] == C0[mp(s, 4, 2, SC) + c] &&
-                C3[mp(s, 4, 3, SC) + c] == C0[mp(s, 4, 3, SC) + c])
+            if (same_bits(bt[v00], bt0[v00]) && same_bits(bt[v10], bt0[v10]) && same_bits(bt[v01], bt0[v01]) &&
+                same_bits(bt[v11], bt0[v11]) && same_bits(C3[mp(s, 4, 1, SC) + c], C0[mp(s, 4, 1, SC) + c]) &&
+                same_bits(C3[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 2, SC) + c]) && same_bits(C3[mp(s, 4, 3, SC) + c], C0[mp(s, 4, 3, SC) + c]))
                 return;
         }
         double b0c, btc, dbx, dby;
@@ -355,7 +357,7 @@ __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevA
     } else {
         psiold = mn(2.0 * H0 * pp / (H0 * H0 + mx(H0 * H0, e2)), P.maxPack);
     }
-    excess = -(p0 * gamold / (1.0 - P.BedPorosity) - deltaBt);
+    excess = PLAIN ? -(p0 * gamold * P.invSolid - deltaBt) : -(p0 * gamold / (1.0 - P.BedPorosity) - deltaBt);
     excess = mx(excess, -(Hn_old * gamold - deltaBt));
 }
 
@@ -383,8 +385,12 @@ __device__ __forceinline__ void m_check(const DevParams& P, const DevArrays& A, 
                 refine = true;
             }
         } else if (!(Hn_old < P.EroCriticalHeight)) {
-            double rel = fabs(Hn_new - Hn_old) / fabs(Hn_old);
-            if (rel > 0.1) refine = true;
+            if (PLAIN) {
+                if (fabs(Hn_new - Hn_old) > 0.1 * fabs(Hn_old)) refine = true;
+            } else {
+                double rel = fabs(Hn_new - Hn_old) / fabs(Hn_old);
+                if (rel > 0.1) refine = true;
+            }
         }
         if (refine) atomicOr(flags, 1);
     }
@@ -392,17 +398,20 @@ __device__ __forceinline__ void m_check(const DevParams& P, const DevArrays& A, 
 
 // Kahan-ordered cell-centred bed of one cell from the M set (ComputeCellCentredTopographic-
 // Data_ij, src/MorphodynamicRHS.f90:371-414: bt, dbdx, dbdy; b0 is left as it is).
-__device__ void cell_topo_ij(const DevParams& P, const DevArrays& A, int tnew, int s, int i, int j) {
+__device__ void cell_topo_ij(const DevParams& P, const DevArrays& A, int tnew, int s, int i, int j, double* out3 = nullptr) {
     int nX = P.nX, SC = nX * P.nY, SV = (nX + 1) * (P.nY + 1);
     const double* b0 = A.BV[tnew] + mp(s, 2, 0, SV);
     const double* bt = A.BV[tnew] + mp(s, 2, 1, SV);
     int v00 = j * (nX + 1) + i, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
     size_t c = (size_t)j * nX + i;
-    A.CT[tnew][mp(s, 4, 1, SC) + c] = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
+    double btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
     double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
     double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
-    A.CT[tnew][mp(s, 4, 2, SC) + c] = 0.5 * P.dxR * kahan8(ax);
-    A.CT[tnew][mp(s, 4, 3, SC) + c] = 0.5 * P.dyR * kahan8(ay);
+    double dbx = 0.5 * P.dxR * kahan8(ax), dby = 0.5 * P.dyR * kahan8(ay);
+    A.CT[tnew][mp(s, 4, 1, SC) + c] = btc;
+    A.CT[tnew][mp(s, 4, 2, SC) + c] = dbx;
+    A.CT[tnew][mp(s, 4, 3, SC) + c] = dby;
+    if (out3) { out3[0] = btc; out3[1] = dbx; out3[2] = dby; }
 }
 
 __device__ __forceinline__ void set_bt(const DevArrays& A, int tnew, int s, int a, int b, double v, int SV, int nX) {
@@ -508,24 +517,51 @@ __device__ __forceinline__ void redist_cells_of(const DevParams& P, const DevArr
 // One of those cells: its bed from the corrected vertices and the conservative w / Hnpsi
 // (cells of tiles that are not active are skipped; the reference updates its intermediate
 // copy of a ghost tile there, which only the last hydraulic RHS of the step would read).
+// Split in two so a warp can load the cell's step-start data (which the walk never
+// changes) while another lane is still correcting the vertices.
+struct RedistCell {
+    int ct, ci, cj;
+    bool on;
+    double b0n, b00, bt0, bx0, by0, w0, p0;
+};
+__device__ __forceinline__ void redist_cell_load(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int ct, int ci,
+                                                 int cj, RedistCell& r) {
+    r.ct = ct; r.ci = ci; r.cj = cj;
+    r.on = ct >= 0 && A.kind[ct] == SLOT_ACTIVE;
+    if (!r.on) return;
+    int SC = P.nX * P.nY;
+    size_t cc = (size_t)cj * P.nX + ci;
+    const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
+    r.b0n = C3[mp(ct, 4, 0, SC) + cc];
+    r.b00 = C0[mp(ct, 4, 0, SC) + cc];
+    r.bt0 = C0[mp(ct, 4, 1, SC) + cc];
+    r.bx0 = C0[mp(ct, 4, 2, SC) + cc];
+    r.by0 = C0[mp(ct, 4, 3, SC) + cc];
+    r.w0 = A.Q[qa][mp(ct, 4, 0, SC) + cc];
+    r.p0 = A.Q[qa][mp(ct, 4, 3, SC) + cc];
+}
+__device__ __forceinline__ void redist_cell_apply(const DevParams& P, const DevArrays& A, int tnew, const RedistCell& r) {
+    if (!r.on) return;
+    int SC = P.nX * P.nY;
+    size_t cc = (size_t)r.cj * P.nX + r.ci;
+    double c3[3];
+    cell_topo_ij(P, A, tnew, r.ct, r.ci, r.cj, c3);
+    double dbc = c3[0] - r.bt0;
+    double go = gam_of(P.geo, r.bx0, r.by0);
+    double gn = gam_of(P.geo, c3[1], c3[2]);
+    double Hno = compute_hn(r.w0, r.b00, r.bt0, go);
+    if (Hno < 0.0) Hno = 0.0;
+    double w = c3[0];
+    w = w + (Hno * go / gn - dbc / gn) / gn;
+    w = w + r.b0n;
+    A.MS[mp(r.ct, 5, 0, SC) + cc] = w;
+    A.MS[mp(r.ct, 5, 1, SC) + cc] = r.p0 * go / gn - (1.0 - P.BedPorosity) * dbc / gn;
+}
 __device__ __forceinline__ void redist_cell(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int ct, int ci,
                                             int cj) {
-    if (ct < 0 || A.kind[ct] != SLOT_ACTIVE) return;
-    int nX = P.nX, SC = nX * P.nY;
-    const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
-    cell_topo_ij(P, A, tnew, ct, ci, cj);
-    size_t cc = (size_t)cj * nX + ci;
-    double dbc = C3[mp(ct, 4, 1, SC) + cc] - C0[mp(ct, 4, 1, SC) + cc];
-    double go = gam_of(P.geo, C0[mp(ct, 4, 2, SC) + cc], C0[mp(ct, 4, 3, SC) + cc]);
-    double gn = gam_of(P.geo, C3[mp(ct, 4, 2, SC) + cc], C3[mp(ct, 4, 3, SC) + cc]);
-    double Hno = compute_hn(A.Q[qa][mp(ct, 4, 0, SC) + cc], C0[mp(ct, 4, 0, SC) + cc], C0[mp(ct, 4, 1, SC) + cc], go);
-    if (Hno < 0.0) Hno = 0.0;
-    double w = C3[mp(ct, 4, 1, SC) + cc];
-    w = w + (Hno * go / gn - dbc / gn) / gn;
-    w = w + C3[mp(ct, 4, 0, SC) + cc];
-    A.MS[mp(ct, 5, 0, SC) + cc] = w;
-    double Hnpsiold = A.Q[qa][mp(ct, 4, 3, SC) + cc];
-    A.MS[mp(ct, 5, 1, SC) + cc] = Hnpsiold * go / gn - (1.0 - P.BedPorosity) * dbc / gn;
+    RedistCell r;
+    redist_cell_load(P, A, qa, tcur, tnew, ct, ci, cj, r);
+    redist_cell_apply(P, A, tnew, r);
 }
 
 // RedistributeGrid (src/Redistribute.f90:203-244) over the ordered candidate list, run as
@@ -640,10 +676,25 @@ template <bool PLAIN>
 __global__ void __launch_bounds__(32) k_m_redist_wave(DevArrays A, const int* __restrict__ list_slot,
                                                       const int* __restrict__ list_cell, int qa, int tcur, int tnew,
                                                       int* flags) {
-    if (*(volatile int*)flags != 0) return;
     const int lane = threadIdx.x;
+    // The failure flag and the list entry are independent loads, issued together.
+    int failed = *(volatile int*)flags;
     int s = list_slot[blockIdx.x], c = list_cell[blockIdx.x];
+    if (failed != 0) return;
     int i = c % cP.nX, j = c / cP.nX;
+    // Lanes 1..9 find their neighbour cell and load its step-start data while lane 0 runs
+    // the excess test and the vertex correction.
+    RedistCell r;
+    r.on = false;
+    if (lane >= 1 && lane <= 9) {
+        int vt[9], vi[9], vj[9];
+        redist_cells_of(cP, A, s, i, j, vt, vi, vj);
+        int mt = -1, mi = 0, mj = 0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+            if (k == lane - 1) { mt = vt[k]; mi = vi[k]; mj = vj[k]; }
+        redist_cell_load(cP, A, qa, tcur, tnew, mt, mi, mj, r);
+    }
     int go = 0;
     if (lane == 0) {
         double ex, dBt, psiold, Ho, Hn;
@@ -654,12 +705,8 @@ __global__ void __launch_bounds__(32) k_m_redist_wave(DevArrays A, const int* __
         }
     }
     go = __shfl_sync(0xffffffffu, go, 0);
-    __syncwarp();
-    if (go) {
-        int vt[9], vi[9], vj[9];
-        redist_cells_of(cP, A, s, i, j, vt, vi, vj);
-        if (lane < 9) redist_cell(cP, A, qa, tcur, tnew, vt[lane], vi[lane], vj[lane]);
-    }
+    __syncwarp();  // lane 0's vertex writes are visible to the other lanes after this
+    if (go) redist_cell_apply(cP, A, tnew, r);
 }
 
 __global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {

@@ -30,6 +30,7 @@ struct DevParams {
     double EroRate, EroRateGranular, EroDepth, EroCriticalHeight, BedPorosity;
     double maxPack, SolidDiameter, nu, hThr, tan1deg, SpongeStrength;
     double cfl, maxdt, diffusiveTimeScale;
+    double invSolid;  // 1 / (1 - BedPorosity), for the FP32 form's multiplications
 };
 
 // The same settings in FP32 for the FP32 form's arithmetic (a conversion from FP64 is an
