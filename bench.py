@@ -517,26 +517,39 @@ def main():
     sim.close()
 
     # ---- end to end through the C ABI ----
-    t0 = time.perf_counter()
+    # (1) e2e: the same kind of steps as `value` (after the same untimed spin-up and
+    # warm-up), host clock around kg_step calls that return their statistics to the host
+    # every step, plus the read-back of the conserved fields of every active tile at the
+    # end; the bytes are the library's own count of its host<->device copies.
+    # (2) e2e_job: the whole job from kg_create (settings and the bed grid uploaded) through
+    # the spin-up and the same steps to the final read-back.
+    t_job = time.perf_counter()
     sim2 = lib.simulation(p, precision=wl["prec"], b0=b0)
-    cu2, n2 = 0, 0
+    cu_job = 0
     if spin > 0.0:
-        st = sim2.integrate_to(spin)
-        cu2 += st.cell_updates
-        n2 += st.steps
-    for _ in range(args.warmup + args.steps):
+        cu_job += sim2.integrate_to(spin).cell_updates
+    for _ in range(args.warmup):
+        cu_job += sim2.step(p.tend).cell_updates
+    xb0 = (C.c_int64 * 2)()
+    L.kg_get_transfer_bytes(sim2.h, xb0)
+    cu2, n2 = 0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
         st = sim2.step(p.tend)
         cu2 += st.cell_updates
         n2 += st.steps
         if sim2.time[0] >= p.tend:
             break
-    d2h = 0
+    fields_bytes = 0
     for t in sim2.active_tiles():
         for f in (1, 2, 3, 4):
-            d2h += sim2.field(t, f).nbytes
-    e2e_s = time.perf_counter() - t0
-    h2d = C.sizeof(abi.Params) + (b0.nbytes if b0 is not None else 0) + 16 * 4 * n2
-    d2h += 16 * 4 * n2
+            fields_bytes += sim2.field(t, f).nbytes
+    t1 = time.perf_counter()
+    xb1 = (C.c_int64 * 2)()
+    L.kg_get_transfer_bytes(sim2.h, xb1)
+    e2e_s = t1 - t0
+    job_s = t1 - t_job
+    cu_job += cu2
     sim2.close()
 
     if rank != 0:
@@ -561,8 +574,13 @@ def main():
         "config": {"workload": args.workload, "desc": wl["desc"], "active_cells_end": active_cells,
                    "l2": "flushed (256 MiB write) between timed steps, outside the timed intervals",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "e2e": {"value": cu2 / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / max(n2, 1),
-                "d2h_bytes_per_step": d2h / max(n2, 1)},
+        "e2e": {"value": cu2 / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": (xb1[0] - xb0[0]) / max(n2, 1),
+                "d2h_bytes_per_step": (xb1[1] - xb0[1]) / max(n2, 1),
+                "note": f"host clock around {n2} kg_step calls after the same spin-up, then the read-back of the "
+                        f"conserved fields ({fields_bytes} B, counted in d2h)"},
+        "e2e_job": {"value": cu_job / job_s, "unit": "cell-updates/s", "seconds": job_s,
+                    "note": "kg_create with the settings and bed grid uploaded, spin-up, warm-up and the same steps, "
+                            "final read-back"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": kname, "pass_ms": pass_ms},

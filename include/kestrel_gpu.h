@@ -260,6 +260,8 @@ int  kg_redistribution_stats(kg_ctx* ctx, int64_t* cells, int64_t* waves, int64_
    reference counterpart. */
 int  kg_get_counters(kg_ctx* ctx, int64_t out[3]);
 int64_t kg_device_bytes(kg_ctx* ctx);
+/* Bytes copied host->device (out[0]) and device->host (out[1]) by the context so far. */
+int  kg_get_transfer_bytes(kg_ctx* ctx, int64_t out[2]);
 /* Host wall time in seconds since creation: out[0] inside kg_step/kg_integrate_to steps,
    out[1] of that blocked in stream synchronisations (the host waiting for the GPU),
    out[2] planning redistribution walks.  No reference counterpart. */

@@ -173,6 +173,7 @@ struct kg_ctx {
     std::vector<std::vector<int>> redist_grid;  // per-tile wave tables of the redistribution scheduler
     double t = 0.0, dt = 1.0e-5, t0 = 0.0;
     int64_t launches = 0, steps = 0, rejected = 0, cell_updates = 0;
+    int64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device traffic of this context
     int64_t redist_cells = 0, redist_waves = 0, redist_walks = 0;
     // Host wall time (s): whole steps, waiting in stream synchronisations, planning the
     // redistribution walk (read-back of the list excluded).
@@ -188,6 +189,14 @@ struct kg_ctx {
     bool own_stream = true, own_ctl = true;  // false for members of a batch
     std::string err;
 };
+
+// Every host<->device copy of a context goes through here and is counted.
+cudaError_t kg_cpy(kg_ctx& c, void* dst, const void* src, size_t n, cudaMemcpyKind kind) {
+    if (kind == cudaMemcpyHostToDevice) c.h2d_bytes += (int64_t)n;
+    else if (kind == cudaMemcpyDeviceToHost) c.d2h_bytes += (int64_t)n;
+    return cudaMemcpyAsync(dst, src, n, kind, c.st);
+}
+
 
 namespace {
 
@@ -274,7 +283,7 @@ void ensure_list(kg_ctx& c, size_t n) {
 void upload_list(kg_ctx& c, const std::vector<int>& slots) {
     ensure_list(c, slots.size());
     if (!slots.empty())
-        CK(cudaMemcpyAsync(c.d_list, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.d_list, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice));
 }
 
 double wall() { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); }
@@ -339,7 +348,7 @@ void push_nbr(kg_ctx& c, int id) {
     int v[8];
     const int order[8] = {m.nb[0], m.nb[1], m.nb[2], m.nb[3], m.cor[0], m.cor[1], m.cor[2], m.cor[3]};
     for (int q = 0; q < 8; ++q) v[q] = in_bounds(c, order[q]) ? T(c, order[q]).slot : -1;
-    CK(cudaMemcpyAsync(c.A.nbr + (size_t)m.slot * 8, v, sizeof(v), cudaMemcpyHostToDevice, c.st));
+    CK(kg_cpy(c, c.A.nbr + (size_t)m.slot * 8, v, sizeof(v), cudaMemcpyHostToDevice));
     sync(c);
 }
 void refresh_nbrs_around(kg_ctx& c, int id) {
@@ -361,7 +370,7 @@ void refresh_all_nbrs(kg_ctx& c) {
         const int order[8] = {m.nb[0], m.nb[1], m.nb[2], m.nb[3], m.cor[0], m.cor[1], m.cor[2], m.cor[3]};
         for (int q = 0; q < 8; ++q) v[(size_t)s * 8 + q] = in_bounds(c, order[q]) ? T(c, order[q]).slot : -1;
     }
-    if (!v.empty()) CK(cudaMemcpyAsync(c.A.nbr, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+    if (!v.empty()) CK(kg_cpy(c, c.A.nbr, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice));
     sync(c);
 }
 
@@ -373,13 +382,13 @@ int assign_slot(kg_ctx& c, int id) {
     m.slot = s;
     c.slot_tile[s] = id;
     int8_t z = SLOT_FREE;
-    CK(cudaMemcpyAsync(c.A.kind + s, &z, 1, cudaMemcpyHostToDevice, c.st));
-    CK(cudaMemcpyAsync(c.A.tile_of_slot + s, &id, sizeof(int), cudaMemcpyHostToDevice, c.st));
+    CK(kg_cpy(c, c.A.kind + s, &z, 1, cudaMemcpyHostToDevice));
+    CK(kg_cpy(c, c.A.tile_of_slot + s, &id, sizeof(int), cudaMemcpyHostToDevice));
     sync(c);
     return s;
 }
 void set_kind(kg_ctx& c, int id, int8_t k) {
-    CK(cudaMemcpyAsync(c.A.kind + T(c, id).slot, &k, 1, cudaMemcpyHostToDevice, c.st));
+    CK(kg_cpy(c, c.A.kind + T(c, id).slot, &k, 1, cudaMemcpyHostToDevice));
     sync(c);
 }
 
@@ -521,7 +530,7 @@ void get_heights(kg_ctx& c, int id) {
         if (st == 1) throw KgError(KG_ERR_PARAM, "Could not read raster file: the section of tile " + std::to_string(id) + " leaves the raster");
         if (st == 2) throw KgError(KG_ERR_PARAM, "No-data value found in raster file (section of tile " + std::to_string(id) + ")");
         if (st != 0) throw KgError(KG_ERR_PARAM, "raster section of tile " + std::to_string(id) + " too small for its bicubic samples");
-        CK(cudaMemcpyAsync(b0.data(), c.d_rb0 + (size_t)(id - 1) * c.SV, (size_t)c.SV * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        CK(kg_cpy(c, b0.data(), c.d_rb0 + (size_t)(id - 1) * c.SV, (size_t)c.SV * sizeof(double), cudaMemcpyDeviceToHost));
         sync(c);
     } else {
         for (int b = 0; b <= nY; ++b)
@@ -539,9 +548,9 @@ void get_heights(kg_ctx& c, int id) {
 void push_bed(kg_ctx& c, int s) {
     // b0 and the face b0 are static: both topography sets hold them.
     for (int b = 0; b < 2; ++b) {
-        CK(cudaMemcpyAsync(c.A.BV[b] + (size_t)s * 2 * c.SV, c.hb0[s].data(), (size_t)c.SV * sizeof(double), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(c.A.FX[b] + (size_t)s * 5 * c.SFX, c.hfx0[s].data(), (size_t)c.SFX * sizeof(double), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(c.A.FY[b] + (size_t)s * 5 * c.SFY, c.hfy0[s].data(), (size_t)c.SFY * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.A.BV[b] + (size_t)s * 2 * c.SV, c.hb0[s].data(), (size_t)c.SV * sizeof(double), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, c.A.FX[b] + (size_t)s * 5 * c.SFX, c.hfx0[s].data(), (size_t)c.SFX * sizeof(double), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, c.A.FY[b] + (size_t)s * 5 * c.SFY, c.hfy0[s].data(), (size_t)c.SFY * sizeof(double), cudaMemcpyHostToDevice));
     }
 }
 void touch(kg_ctx& c, int s) {
@@ -553,10 +562,10 @@ void touch(kg_ctx& c, int s) {
 void mirror_touched(kg_ctx& c) {
     int o = 1 - c.tcur;
     for (int s : c.touched) {
-        CK(cudaMemcpyAsync(c.A.CT[o] + (size_t)s * 4 * c.SC, c.A.CT[c.tcur] + (size_t)s * 4 * c.SC, (size_t)4 * c.SC * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
-        CK(cudaMemcpyAsync(c.A.FX[o] + (size_t)s * 5 * c.SFX, c.A.FX[c.tcur] + (size_t)s * 5 * c.SFX, (size_t)5 * c.SFX * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
-        CK(cudaMemcpyAsync(c.A.FY[o] + (size_t)s * 5 * c.SFY, c.A.FY[c.tcur] + (size_t)s * 5 * c.SFY, (size_t)5 * c.SFY * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
-        CK(cudaMemcpyAsync(c.A.BV[o] + (size_t)s * 2 * c.SV, c.A.BV[c.tcur] + (size_t)s * 2 * c.SV, (size_t)2 * c.SV * sizeof(double), cudaMemcpyDeviceToDevice, c.st));
+        CK(kg_cpy(c, c.A.CT[o] + (size_t)s * 4 * c.SC, c.A.CT[c.tcur] + (size_t)s * 4 * c.SC, (size_t)4 * c.SC * sizeof(double), cudaMemcpyDeviceToDevice));
+        CK(kg_cpy(c, c.A.FX[o] + (size_t)s * 5 * c.SFX, c.A.FX[c.tcur] + (size_t)s * 5 * c.SFX, (size_t)5 * c.SFX * sizeof(double), cudaMemcpyDeviceToDevice));
+        CK(kg_cpy(c, c.A.FY[o] + (size_t)s * 5 * c.SFY, c.A.FY[c.tcur] + (size_t)s * 5 * c.SFY, (size_t)5 * c.SFY * sizeof(double), cudaMemcpyDeviceToDevice));
+        CK(kg_cpy(c, c.A.BV[o] + (size_t)s * 2 * c.SV, c.A.BV[c.tcur] + (size_t)s * 2 * c.SV, (size_t)2 * c.SV * sizeof(double), cudaMemcpyDeviceToDevice));
     }
     c.touched.clear();
     sync(c);
@@ -734,7 +743,7 @@ void add_tile(kg_ctx& c, int k) {
     equalise(c, k);
     T(c, k).src = false;
     int8_t zero = 0;
-    CK(cudaMemcpyAsync(c.A.has_source + T(c, k).slot, &zero, 1, cudaMemcpyHostToDevice, c.st));
+    CK(kg_cpy(c, c.A.has_source + T(c, k).slot, &zero, 1, cudaMemcpyHostToDevice));
     // ActivateTile
     T(c, k).ghost = false;
     set_kind(c, k, SLOT_ACTIVE);
@@ -764,7 +773,7 @@ void rebuild_blocks(kg_ctx& c) {
         c.d_active_cap = std::max<int>((int)all.size(), 2 * c.d_active_cap);
         CK(cudaMalloc(&c.d_active, (size_t)c.d_active_cap * sizeof(int)));
     }
-    if (!all.empty()) CK(cudaMemcpyAsync(c.d_active, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+    if (!all.empty()) CK(kg_cpy(c, c.d_active, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
     c.n_active_dev = (int)c.active.size();
     c.n_ghost_dev = (int)c.ghost.size();
     c.blocks.clear();
@@ -780,7 +789,7 @@ void rebuild_blocks(kg_ctx& c) {
         CK(cudaMalloc(&c.d_blocks, (size_t)c.d_blocks_cap * sizeof(BlockDesc)));
     }
     if (!c.blocks.empty())
-        CK(cudaMemcpyAsync(c.d_blocks, c.blocks.data(), c.blocks.size() * sizeof(BlockDesc), cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.d_blocks, c.blocks.data(), c.blocks.size() * sizeof(BlockDesc), cudaMemcpyHostToDevice));
     sync(c);
     c.blocks_dirty = false;
 }
@@ -802,7 +811,7 @@ void check_near_boundaries(kg_ctx& c) {
         c.launches++;
         int per = (c.SC + 255) / 256;
         std::vector<int> chunks(slots.size() * per);
-        CK(cudaMemcpyAsync(chunks.data(), c.d_flags, chunks.size() * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        CK(kg_cpy(c, chunks.data(), c.d_flags, chunks.size() * sizeof(int), cudaMemcpyDeviceToHost));
         sync(c);
         fl.assign(slots.size(), 0);
         for (size_t q = 0; q < slots.size(); ++q)
@@ -869,7 +878,7 @@ void refresh_topo32(kg_ctx& c, int ts) {
         CK(cudaMalloc(&c.d_tlist, (size_t)c.d_tlist_cap * sizeof(int)));
     }
     if (!slots.empty()) {
-        CK(cudaMemcpyAsync(c.d_tlist, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.d_tlist, slots.data(), slots.size() * sizeof(int), cudaMemcpyHostToDevice));
         CK(launch_topo32(c.A, c.d_tlist, (int)slots.size(), ts, c.nX, c.nY, c.st));
         c.launches++;
     }
@@ -898,11 +907,11 @@ void launch_pass(kg_ctx& c, StepArgs& S, int word) {
 }
 void reset_cfl(kg_ctx& c, int first, int n) {
     for (int k = first; k < first + n; ++k) c.h_cfl[k] = HUGE_BITS;
-    CK(cudaMemcpyAsync(c.d_cfl + first, c.h_cfl + first, (size_t)n * sizeof(unsigned long long), cudaMemcpyHostToDevice, c.st));
+    CK(kg_cpy(c, c.d_cfl + first, c.h_cfl + first, (size_t)n * sizeof(unsigned long long), cudaMemcpyHostToDevice));
 }
 // Read back the CFL words (and whatever else was queued for reading) with one wait.
 void collect_cfl(kg_ctx& c) {
-    CK(cudaMemcpyAsync(c.h_ctl, c.d_ctl, sizeof(kg_ctx::Ctl), cudaMemcpyDeviceToHost, c.st));
+    CK(kg_cpy(c, c.h_ctl, c.d_ctl, sizeof(kg_ctx::Ctl), cudaMemcpyDeviceToHost));
     sync(c);
 }
 // Accumulate the event timing of one pass of the last queue (one that ran).
@@ -969,7 +978,7 @@ void queue_hydraulic(kg_ctx& c, double dt, const double* dtp, int q_in, int e_se
             c.h_act_cap = std::max<int>(n * per, 2 * c.h_act_cap);
             CK(cudaMallocHost(&c.h_act, (size_t)c.h_act_cap * sizeof(int)));
         }
-        CK(cudaMemcpyAsync(c.h_act, c.d_flags, (size_t)n * per * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        CK(kg_cpy(c, c.h_act, c.d_flags, (size_t)n * per * sizeof(int), cudaMemcpyDeviceToHost));
     }
 }
 
@@ -1120,8 +1129,8 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         CK(cudaMallocHost(&c.h_cex, (size_t)c.h_cand_cap * sizeof(double)));
     }
     if (pre > 0) {
-        CK(cudaMemcpyAsync(c.h_ckey, c.d_ckey, (size_t)pre * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
-        CK(cudaMemcpyAsync(c.h_cex, c.d_cex, (size_t)pre * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        CK(kg_cpy(c, c.h_ckey, c.d_ckey, (size_t)pre * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        CK(kg_cpy(c, c.h_cex, c.d_cex, (size_t)pre * sizeof(double), cudaMemcpyDeviceToHost));
     }
     collect_cfl(c);
     int ncand = c.h_ctl->ncand;
@@ -1140,8 +1149,8 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
             std::memcpy(key.data(), c.h_ckey, (size_t)ncand * sizeof(unsigned long long));
             std::memcpy(ex.data(), c.h_cex, (size_t)ncand * sizeof(double));
         } else {
-            CK(cudaMemcpyAsync(key.data(), c.d_ckey, (size_t)ncand * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c.st));
-            CK(cudaMemcpyAsync(ex.data(), c.d_cex, (size_t)ncand * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+            CK(kg_cpy(c, key.data(), c.d_ckey, (size_t)ncand * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+            CK(kg_cpy(c, ex.data(), c.d_cex, (size_t)ncand * sizeof(double), cudaMemcpyDeviceToHost));
             sync(c);
         }
         double tp0 = wall();
@@ -1158,9 +1167,9 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         c.redist_waves += nw;
         c.redist_walks++;
         c.host_plan_s += wall() - tp0;
-        CK(cudaMemcpyAsync(c.d_rslot, ls.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.d_rslot, ls.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, c.d_rcell, lc.data(), (size_t)ncand * sizeof(int), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, c.d_rwave, woff.data(), woff.size() * sizeof(int), cudaMemcpyHostToDevice));
         CK(launch_m_redist(c.A, c.d_rslot, c.d_rcell, c.d_rwave, woff.data(), nw, qa, c.tcur, tnew, c.d_mflags, fp32, c.st));
         c.launches += nw <= KG_REDIST_WAVE_MAX ? nw : 1;
     }
@@ -1337,9 +1346,9 @@ void load_sources(kg_ctx& c) {
         bufs[q].hn.assign((size_t)SC, 0.0);
         bufs[q].rho.assign((size_t)SC, c.p.rhow);
         bufs[q].hmax.resize((size_t)SC);
-        CK(cudaMemcpyAsync(bufs[q].hmax.data(), c.A.MX + (size_t)s * 11 * SC, (size_t)SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
-        CK(cudaMemcpyAsync(bufs[q].q.data(), c.A.Q[c.qcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
-        CK(cudaMemcpyAsync(bufs[q].ct.data(), c.A.CT[c.tcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+        CK(kg_cpy(c, bufs[q].hmax.data(), c.A.MX + (size_t)s * 11 * SC, (size_t)SC * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(kg_cpy(c, bufs[q].q.data(), c.A.Q[c.qcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(kg_cpy(c, bufs[q].ct.data(), c.A.CT[c.tcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost));
     }
     sync(c);
     double rhow = c.p.rhow, rhos = c.p.rhos;
@@ -1418,17 +1427,17 @@ void load_sources(kg_ctx& c) {
         std::vector<double> z((size_t)SC, 0.0), r((size_t)SC, rhow);
         for (int id : c.active) {
             int s = T(c, id).slot;
-            CK(cudaMemcpyAsync(c.d_srcHn + (size_t)s * SC, z.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
-            CK(cudaMemcpyAsync(c.d_srcRho + (size_t)s * SC, r.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+            CK(kg_cpy(c, c.d_srcHn + (size_t)s * SC, z.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice));
+            CK(kg_cpy(c, c.d_srcRho + (size_t)s * SC, r.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice));
         }
         sync(c);
     }
     for (size_t q = 0; q < touched.size(); ++q) {
         int s = T(c, touched[q]).slot;
-        CK(cudaMemcpyAsync(c.A.Q[c.qcur] + (size_t)s * 4 * SC, bufs[q].q.data(), (size_t)4 * SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(c.d_srcHn + (size_t)s * SC, bufs[q].hn.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(c.d_srcRho + (size_t)s * SC, bufs[q].rho.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(c.A.MX + (size_t)s * 11 * SC, bufs[q].hmax.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.A.Q[c.qcur] + (size_t)s * 4 * SC, bufs[q].q.data(), (size_t)4 * SC * sizeof(double), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, c.d_srcHn + (size_t)s * SC, bufs[q].hn.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, c.d_srcRho + (size_t)s * SC, bufs[q].rho.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, c.A.MX + (size_t)s * 11 * SC, bufs[q].hmax.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice));
     }
     sync(c);
     upload_sources(c);
@@ -1443,7 +1452,7 @@ void load_sources(kg_ctx& c) {
 void upload_sources(kg_ctx& c) {
     for (int id : c.active) {
         int8_t f = T(c, id).src ? 1 : 0;
-        CK(cudaMemcpyAsync(c.A.has_source + T(c, id).slot, &f, 1, cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.A.has_source + T(c, id).slot, &f, 1, cudaMemcpyHostToDevice));
         sync(c);
     }
     std::vector<DevSource> ds(c.srcs.size());
@@ -1456,7 +1465,7 @@ void upload_sources(kg_ctx& c) {
     c.dsrc = ds;
     if (!ds.empty()) {
         CK(cudaMalloc(&c.d_src, ds.size() * sizeof(DevSource)));
-        CK(cudaMemcpyAsync(c.d_src, ds.data(), ds.size() * sizeof(DevSource), cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.d_src, ds.data(), ds.size() * sizeof(DevSource), cudaMemcpyHostToDevice));
     }
     CK(set_constants(c.dp, ds.data(), (int)ds.size(), c.st));
     g_const_owner = &c;
@@ -1479,11 +1488,11 @@ void load_state(kg_ctx& c, const int32_t* ids, int n, const double* state, const
     for (int k = 0; k < n; ++k) {
         int s = T(c, ids[k]).slot;
         slots.push_back(s);
-        CK(cudaMemcpyAsync(c.A.Q[c.qcur] + (size_t)s * 4 * SC, state + (size_t)k * 4 * SC, (size_t)4 * SC * sizeof(double),
-                           cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, c.A.Q[c.qcur] + (size_t)s * 4 * SC, state + (size_t)k * 4 * SC, (size_t)4 * SC * sizeof(double),
+                           cudaMemcpyHostToDevice));
         if (btv)
-            CK(cudaMemcpyAsync(c.A.BV[c.tcur] + ((size_t)s * 2 + 1) * SV, btv + (size_t)k * SV, (size_t)SV * sizeof(double),
-                               cudaMemcpyHostToDevice, c.st));
+            CK(kg_cpy(c, c.A.BV[c.tcur] + ((size_t)s * 2 + 1) * SV, btv + (size_t)k * SV, (size_t)SV * sizeof(double),
+                               cudaMemcpyHostToDevice));
         touch(c, s);
     }
     sync(c);
@@ -1653,7 +1662,7 @@ int active_slot(kg_ctx* c, int id) {
 
 std::vector<double> d2h(kg_ctx* c, const double* src, size_t n) {
     std::vector<double> v(n);
-    CK(cudaMemcpyAsync(v.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(kg_cpy(*c, v.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost));
     sync(*c);
     return v;
 }
@@ -1741,13 +1750,13 @@ void upload_raster(kg_ctx& c, const double* values, const kg_raster& g) {
         CK(cudaMalloc(&dXV, XV.size() * sizeof(double)));
         CK(cudaMalloc(&dYV, YV.size() * sizeof(double)));
         CK(cudaMalloc(&dst, (size_t)c.nTiles * sizeof(int)));
-        CK(cudaMemcpyAsync(dR, values, nR * sizeof(double), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(dXV, XV.data(), XV.size() * sizeof(double), cudaMemcpyHostToDevice, c.st));
-        CK(cudaMemcpyAsync(dYV, YV.data(), YV.size() * sizeof(double), cudaMemcpyHostToDevice, c.st));
+        CK(kg_cpy(c, dR, values, nR * sizeof(double), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, dXV, XV.data(), XV.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CK(kg_cpy(c, dYV, YV.data(), YV.size() * sizeof(double), cudaMemcpyHostToDevice));
         CK(launch_raster_heights(dR, G, dXV, dYV, c.d_rb0, dst, c.st));
         c.launches++;
         c.raster_status.assign((size_t)c.nTiles, 0);
-        CK(cudaMemcpyAsync(c.raster_status.data(), dst, (size_t)c.nTiles * sizeof(int), cudaMemcpyDeviceToHost, c.st));
+        CK(kg_cpy(c, c.raster_status.data(), dst, (size_t)c.nTiles * sizeof(int), cudaMemcpyDeviceToHost));
         sync(c);
     } catch (...) {
         release();
@@ -1907,8 +1916,8 @@ int kg_set_tile_field(kg_ctx* c, int32_t id, int32_t field, const double* in) {
     if (field < 1 || field > 4 || !in) return KG_ERR_PARAM;
     c->gen++;
     KG_GUARD(c, {
-        CK(cudaMemcpyAsync(c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * c->SC, in, (size_t)c->SC * sizeof(double),
-                           cudaMemcpyHostToDevice, c->st));
+        CK(kg_cpy(*c, c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * c->SC, in, (size_t)c->SC * sizeof(double),
+                           cudaMemcpyHostToDevice));
         sync(*c);
     });
     return KG_OK;
@@ -1984,6 +1993,13 @@ int kg_get_counters(kg_ctx* c, int64_t out[3]) {
     out[0] = c->steps;
     out[1] = c->rejected;
     out[2] = c->cell_updates;
+    return KG_OK;
+}
+
+int kg_get_transfer_bytes(kg_ctx* c, int64_t out[2]) {
+    if (!c || !out) return KG_ERR_PARAM;
+    out[0] = c->h2d_bytes;
+    out[1] = c->d2h_bytes;
     return KG_OK;
 }
 

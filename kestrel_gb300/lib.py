@@ -35,6 +35,8 @@ def load(auto_build: bool = True):
     lib.kg_get_kernel_time.restype = C.c_int
     lib.kg_get_counters.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     lib.kg_get_counters.restype = C.c_int
+    lib.kg_get_transfer_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    lib.kg_get_transfer_bytes.restype = C.c_int
     lib.kg_device_bytes.argtypes = [C.c_void_p]
     lib.kg_device_bytes.restype = C.c_int64
     lib.kg_host_times.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
