@@ -102,7 +102,7 @@ struct MJob {
     unsigned long long* keys;
     double* ex;
 };
-enum MKind { MK_INIT, MK_EMD, MK_BT, MK_CELLS, MK_CHECK, MK_FACE, MK_BI, MK_FINISH, MK_TOPO };
+enum MKind { MK_INIT, MK_EMD, MK_BT, MK_CELLS, MK_CHECK, MK_CLOSE };
 
 template <int K>
 __global__ void __launch_bounds__(256) k_m_batch(const SimStatic* __restrict__ sims, const MJob* __restrict__ jobs,
@@ -129,14 +129,8 @@ __global__ void __launch_bounds__(256) k_m_batch(const SimStatic* __restrict__ s
             m_cells<true>(X.P, X.F, X.A, s, item, J.qa, J.tcur, J.tnew);
         } else if (K == MK_CHECK) {
             m_check<true>(X.P, X.A, s, item, pos, J.qa, J.tcur, J.tnew, J.flags, J.keys, J.ex, J.flags + 1, J.cap);
-        } else if (K == MK_FACE) {
-            face_topo<true>(X.P, X.A, s, item, J.tnew);
-        } else if (K == MK_BI) {
-            face_bI(X.P, X.A, s, item, J.tnew);
-        } else if (K == MK_FINISH) {
-            m_finish(X.P, X.A, s, item, J.qa);
         } else {
-            topo32(X.P, X.A, s, item, J.tnew);
+            m_close<true>(X.P, X.A, s, item, J.qa, J.tnew);
         }
     }
 }
@@ -573,18 +567,15 @@ void phase_m(kg_batch& b, const std::vector<int>& who) {
     // Interfacial topography of the new bed and the M result, for every member at once.
     int ng = (int)go.size();
     int tg = upload_mjobs(b, 1, go);
-    launch_m<MK_FACE>(b, 1, ng, tg);
-    launch_m<MK_BI>(b, 1, ng, tg);
-    launch_m<MK_FINISH>(b, 1, ng, tg);
+    // interfacial topography, the M result and the active tiles' factor cache, fused
+    launch_m<MK_CLOSE>(b, 1, ng, tg);
     std::vector<int> whole;
     for (int id : go) {
         Member& m = b.mem[(size_t)id];
         kg_ctx& c = *m.c;
-        c.launches += 3;
-        c.tdirty[m.tnew] = std::max(c.tdirty[m.tnew], 1);
+        c.launches += 1;
         if (c.tdirty[m.tnew] > 1) whole.push_back(id);
     }
-    launch_m<MK_TOPO>(b, 1, ng, tg);  // the active tiles' factors of every member
     for (int id : whole) {            // ghost factors too where they were never built
         kg_ctx& c = *b.mem[(size_t)id].c;
         bind_constants(c);

@@ -62,6 +62,8 @@ cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int ce
 cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, const int* hwoff, int nwaves,
                             int qa, int tcur, int tnew, int* flags, bool fp32, cudaStream_t st);
 cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st);
+cudaError_t launch_m_close(const DevArrays& A, const int* d_slots, int n, int nX, int nY, int qa, int tnew, bool fp32,
+                           cudaStream_t st);
 }  // namespace kg
 
 using namespace kg;
@@ -1174,11 +1176,12 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         c.launches += nw <= KG_REDIST_WAVE_MAX ? nw : 1;
     }
     // Interfacial topography of the new bed and the M result (both scratch until accepted).
-    CK(launch_face_topo(c.A, dl, n, tnew, c.nX, c.nY, fp32, c.st));
-    CK(launch_face_bI(c.A, dl, n, tnew, c.nX, c.nY, c.st));
-    CK(launch_m_finish(c.A, dl, n, c.SC, qa, c.st));
-    c.launches += 3;
-    c.tdirty[tnew] = std::max(c.tdirty[tnew], 1);
+    CK(launch_m_close(c.A, dl, n, c.nX, c.nY, qa, tnew, fp32, c.st));
+    c.launches++;
+    // The fused launch rebuilt the active tiles' factor cache of the new set (FP32 form);
+    // ghost tiles' factors are rebuilt by the refresh when they were never built.
+    if (fp32) c.tdirty[tnew] = c.tdirty[tnew] > 1 ? 2 : 0;
+    else c.tdirty[tnew] = std::max(c.tdirty[tnew], 1);
     // RHS check at t0 + dt, then H(dt) from the M result, gated by both tests.
     c.t = c.t0 + dt;
     StepArgs R = rhs_args(c, o[0], 1, tnew, c.t);

@@ -709,6 +709,17 @@ __global__ void __launch_bounds__(32) k_m_redist_wave(DevArrays A, const int* __
     if (go) redist_cell_apply(cP, A, tnew, r);
 }
 
+template <bool PLAIN>
+__device__ __forceinline__ void m_close(const DevParams& P, const DevArrays& A, int s, int k, int qa, int tnew) {
+    face_topo<PLAIN>(P, A, s, k, tnew);
+    face_bI(P, A, s, k, tnew);
+    m_finish(P, A, s, k, qa);
+    if (PLAIN) topo32(P, A, s, k, tnew);
+}
+template <bool PLAIN>
+__global__ void __launch_bounds__(256) k_m_close(DevArrays A, const int* __restrict__ slots, int qa, int tnew, int per) {
+    m_close<PLAIN>(cP, A, slots[blockIdx.x / per], (blockIdx.x % per) * 256 + threadIdx.x, qa, tnew);
+}
 __global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
     KG_TILE_ITEMS(cP.nX * cP.nY)
     m_finish(cP, A, s, item_, qa);
@@ -773,6 +784,19 @@ cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, co
 cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     k_m_finish<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa);
+    return cudaGetLastError();
+}
+// The end of an M attempt in one launch: the interfacial topography of the new bed
+// (face_topo, face_bI), the M result into state qa (m_finish) and, in the FP32 form, the
+// factor cache of the new topography set for the listed tiles (topo32).  Every part works
+// on item k of the tile (face k, cell k) and reads only data written before the launch or
+// by the same thread, so the four kernels fuse without changing a result.
+cudaError_t launch_m_close(const DevArrays& A, const int* d_slots, int n, int nX, int nY, int qa, int tnew, bool fp32,
+                           cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    int per = per_of((nX + 1) * (nY + 1));
+    if (fp32) k_m_close<true><<<n * per, 256, 0, st>>>(A, d_slots, qa, tnew, per);
+    else k_m_close<false><<<n * per, 256, 0, st>>>(A, d_slots, qa, tnew, per);
     return cudaGetLastError();
 }
 
