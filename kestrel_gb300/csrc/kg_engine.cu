@@ -54,7 +54,7 @@ cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int ver
                           bool fp32, cudaStream_t st);
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st);
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
-                        bool fp32, cudaStream_t st);
+                        const double* dtp, bool fp32, cudaStream_t st);
 cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, bool fp32,
                            cudaStream_t st);
 cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
@@ -171,7 +171,7 @@ struct kg_ctx {
     // typical redistribution list needs no second wait; the prefix adapts to the counts seen.
     unsigned long long* h_ckey = nullptr;
     double* h_cex = nullptr;
-    int h_cand_cap = 0, cand_pre = 256;
+    int h_cand_cap = 0, cand_pre = 256, cand_pre_used = 0;
     std::vector<std::vector<int>> redist_grid;  // per-tile wave tables of the redistribution scheduler
     double t = 0.0, dt = 1.0e-5, t0 = 0.0;
     int64_t launches = 0, steps = 0, rejected = 0, cell_updates = 0;
@@ -1004,13 +1004,6 @@ bool finish_hydraulic(kg_ctx& c, double& dt, int q_out, int topo, bool flags_aft
     return false;
 }
 
-// HydraulicTimeStepper with a host dt; returns true when dt had to be refined.
-bool hydraulic_stepper(kg_ctx& c, double& dt, int q_in, int e_set, int topo, int q_s1, int q_s2, int q_out, bool flags_after) {
-    c.dt = dt;
-    queue_hydraulic(c, dt, nullptr, q_in, e_set, topo, q_s1, q_s2, q_out, nullptr, nullptr, flags_after);
-    collect_cfl(c);
-    return finish_hydraulic(c, dt, q_out, topo, flags_after);
-}
 
 // CalculateHydraulicRHS at substep 1 on state q_in / topography topo into E/I set e_set.
 StepArgs rhs_args(const kg_ctx& c, int q_in, int e_set, int topo, double t) {
@@ -1092,12 +1085,16 @@ void redistribution_waves(kg_ctx& c, const std::vector<int>& slots, const std::v
 // second H are gated on the device by the redistribution's refine flag and the check's
 // advised dt.  Returns 0 accepted, 1 M refined, 2 the check cut dt, 3 H refined; dt is
 // updated as the reference updates it.
-int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
+// Queues M on the first hydraulic half-step's result o[0]: init, the three stages, the
+// check and the read-back of the leading candidates, ready for one wait.  dtp: the
+// half-step's dt on the device (an M queued behind the first attempt of a step, before the
+// host has read that dt), else dt.  M writes only the scratch topography set, the M state
+// and the candidate list, so an M queued behind a half-step that is then refused is
+// simply discarded.
+void queue_morpho(kg_ctx& c, double dt, const double* dtp, const int o[3], int tnew) {
     const int qa = o[0];
     double dt_m = 2.0 * dt;
-    std::vector<int> slots;
-    for (int id : c.active) slots.push_back(T(c, id).slot);
-    int n = (int)slots.size();
+    int n = (int)c.active.size();
     const int* dl = c.d_active;
     const bool fp32 = c.prec == KG_PREC_FP32;
     // The FP32 form's M kernels read gamma of the step-start topography from the cache.
@@ -1106,12 +1103,13 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
     c.launches++;
     for (int stage = 1; stage <= 3; ++stage) {
         CK(launch_m_emd(c.A, dl, n, c.SC, tnew, fp32, c.st));
-        CK(launch_m_bt(c.A, dl, n, c.SV, c.tcur, tnew, stage, dt_m, fp32, c.st));
+        CK(launch_m_bt(c.A, dl, n, c.SV, c.tcur, tnew, stage, dt_m, dtp, fp32, c.st));
         CK(launch_m_cells(c.A, dl, n, c.SC, qa, c.tcur, tnew, fp32, c.st));
         c.launches += 3;
     }
     int need = n * c.SC;
     if (need > c.cand_cap) {
+        CK(cudaStreamSynchronize(c.st));
         cudaFree(c.d_ckey); cudaFree(c.d_cex); cudaFree(c.d_rslot); cudaFree(c.d_rcell); cudaFree(c.d_rwave);
         c.cand_cap = std::max(need, 2 * c.cand_cap);
         CK(cudaMalloc(&c.d_ckey, (size_t)c.cand_cap * sizeof(unsigned long long)));
@@ -1124,6 +1122,7 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
     c.launches++;
     int pre = std::min(c.cand_pre, c.cand_cap);
     if (pre > c.h_cand_cap) {
+        CK(cudaStreamSynchronize(c.st));
         if (c.h_ckey) CK(cudaFreeHost(c.h_ckey));
         if (c.h_cex) CK(cudaFreeHost(c.h_cex));
         c.h_cand_cap = std::max(pre, 2 * c.h_cand_cap);
@@ -1134,7 +1133,21 @@ int morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
         CK(kg_cpy(c, c.h_ckey, c.d_ckey, (size_t)pre * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
         CK(kg_cpy(c, c.h_cex, c.d_cex, (size_t)pre * sizeof(double), cudaMemcpyDeviceToHost));
     }
-    collect_cfl(c);
+    c.cand_pre_used = pre;
+}
+
+// After the wait that follows queue_morpho: the refinement tests, the ordered
+// redistribution, the closing launch, the RHS check at t0 + dt and the second half-step.
+// Returns 0 when the step is accepted, else the retry code with dt refined.
+int finish_morpho_and_h2(kg_ctx& c, double& dt, const int o[3], int tnew) {
+    const int qa = o[0];
+    double dt_m = 2.0 * dt;
+    std::vector<int> slots;
+    for (int id : c.active) slots.push_back(T(c, id).slot);
+    int n = (int)slots.size();
+    const int* dl = c.d_active;
+    const bool fp32 = c.prec == KG_PREC_FP32;
+    const int pre = c.cand_pre_used;
     int ncand = c.h_ctl->ncand;
     c.cand_pre = std::max(256, std::min(1 << 20, 2 * ncand));
     if (c.h_ctl->mflag != 0) {
@@ -1238,6 +1251,7 @@ void integrate_step_body(kg_ctx& c, double tend) {
     CK(launch_dt(c.d_cfl + W_RHS, partial(c), cap, c.d_dt, c.st));
     c.launches++;
     queue_hydraulic(c, 0.0, c.d_dt, c.qcur, 0, c.tcur, o[0], o[1], o[0], nullptr, nullptr, !morpho);
+    if (morpho) queue_morpho(c, 0.0, c.d_dt, o, tnew);
     collect_cfl(c);
     account_pass(c, W_RHS);
     double adv = mn(advised(c, c.h_cfl[W_RHS], 1), cap);
@@ -1250,16 +1264,20 @@ void integrate_step_body(kg_ctx& c, double tend) {
     int guard = 0, newcur = -1;
     while (true) {
         if (++guard > 100000 || !(dt > 0.0)) throw KgError(KG_ERR_DT, "time step collapsed");
-        bool rej;
-        if (first) {
-            rej = finish_hydraulic(c, dt, o[0], c.tcur, !morpho);
-            first = false;
-        } else {
-            rej = hydraulic_stepper(c, dt, c.qcur, 0, c.tcur, o[0], o[1], o[0], !morpho);
+        // Each attempt queues the first hydraulic half-step and, with morphodynamics, M on
+        // its result, and waits once for both (the first attempt was queued above with the
+        // device-computed dt).
+        if (!first) {
+            c.dt = dt;
+            queue_hydraulic(c, dt, nullptr, c.qcur, 0, c.tcur, o[0], o[1], o[0], nullptr, nullptr, !morpho);
+            if (morpho) queue_morpho(c, dt, nullptr, o, tnew);
+            collect_cfl(c);
         }
+        first = false;
+        bool rej = finish_hydraulic(c, dt, o[0], c.tcur, !morpho);
         if (rej) { c.rejected++; continue; }
         if (!morpho) { newcur = o[0]; break; }
-        int r = morpho_and_h2(c, dt, o, tnew);
+        int r = finish_morpho_and_h2(c, dt, o, tnew);
         if (r == 0) { newcur = o[1]; break; }
         c.rejected++;
         c.dt = dt;

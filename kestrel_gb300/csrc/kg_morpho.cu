@@ -647,9 +647,12 @@ __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restric
     m_emd<R>(cP, cP32, A, s, item_, tnew);
 }
 template <bool PLAIN>
-__global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt) {
+// dtp: when set, the M time step is twice the hydraulic dt the device computed (k_dt), for
+// an M queued before the host has read that dt back.
+__global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt,
+                                              const double* __restrict__ dtp) {
     KG_TILE_ITEMS((cP.nX + 1) * (cP.nY + 1))
-    m_bt<PLAIN>(cP, A, s, item_, tcur, tnew, stage, dt);
+    m_bt<PLAIN>(cP, A, s, item_, tcur, tnew, stage, dtp ? 2.0 * dtp[0] : dt);
 }
 template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
@@ -742,10 +745,10 @@ cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cell
     return cudaGetLastError();
 }
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
-                        bool fp32, cudaStream_t st) {
+                        const double* dtp, bool fp32, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (fp32) k_m_bt<true><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
-    else k_m_bt<false><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt);
+    if (fp32) k_m_bt<true><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt, dtp);
+    else k_m_bt<false><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt, dtp);
     return cudaGetLastError();
 }
 cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, bool fp32,
