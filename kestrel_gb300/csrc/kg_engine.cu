@@ -257,6 +257,7 @@ void ensure_cap(kg_ctx& c, int need) {
     grow_array(c.A.UV, o * 2 * SC, n * 2 * SC, c.st);
     grow_array(c.A.MS, o * 5 * SC, n * 5 * SC, c.st);
     grow_array(c.A.EMD, o * SC, n * SC, c.st);
+    grow_array(c.A.B0S, o * 2 * SC, n * 2 * SC, c.st);
     grow_array(c.A.G9, o * 9 * SC, n * 9 * SC, c.st);
     grow_array(c.A.GE, o * GE_COUNT * (size_t)c.nE, n * GE_COUNT * (size_t)c.nE, c.st);
     grow_array(c.A.MX, o * 11 * SC, n * 11 * SC, c.st);
@@ -1569,6 +1570,8 @@ void setup(kg_ctx& c, const kg_params& p) {
     d.dy = p.Ytilesize / (double)c.nY;
     d.dxR = 1.0 / d.dx;
     d.dyR = 1.0 / d.dy;
+    d.hdxR = 0.5 * d.dxR;
+    d.hdyR = 0.5 * d.dyR;
     d.geo = p.geometric_factors != 0; d.morpho = p.MorphodynamicsOn != 0;
     d.drag = p.drag; d.erosion = p.erosion; d.deposition = p.deposition; d.etrans = p.erosion_transition;
     d.damping = p.morpho_damping; d.fswitch = p.fswitch; d.limiter = p.limiter; d.bcs = p.bcs;
@@ -1638,7 +1641,7 @@ void free_ctx(kg_ctx* c) {
     }
     cudaFree(c->d_tlist);
     cudaFree(c->d_rb0);
-    void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.G9, c->A.GE, c->A.MX,
+    void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.B0S, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
                     c->d_vol, c->d_srcHn, c->d_srcRho, c->d_ckey, c->d_cex, c->d_src,
                     c->d_rslot, c->d_rcell, c->d_rwave};

@@ -67,6 +67,7 @@ struct DevArrays {
     double* MX;
     double* MS;                // [slot][5][nY][nX] M-operator stage state: w, Hnpsi, Hn, psi, rho
     double* EMD;               // [slot][nY][nX] E - D of the current M stage (zero on ghosts)
+    double* B0S;               // [slot][2][nY][nX] the static b0 parts of the cell slopes (FP32-form M stages)
     double* TD[2];             // FP32 form topography factors (null in the FP64 form)
     float* TF[2];
     float* TFX[2];

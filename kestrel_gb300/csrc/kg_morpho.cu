@@ -59,16 +59,18 @@ __device__ __forceinline__ double gam_nr(const DevParams& P, double bx, double b
 template <bool PLAIN>
 __device__ __forceinline__ void m_init(const DevParams& P, const DevArrays& A, int s, int item_, int qa, int tcur, int tnew) {
     int SC = P.nX * P.nY, SV = (P.nX + 1) * (P.nY + 1);
+    // b0 (vertex plane 0, cell plane 0) is static and both topography sets hold it: only
+    // the bed change and the slopes are carried into the M set.
     if (item_ < SV) {
         int v = item_;
-        A.BV[tnew][mp(s, 2, 0, SV) + v] = A.BV[tcur][mp(s, 2, 0, SV) + v];
         A.BV[tnew][mp(s, 2, 1, SV) + v] = A.BV[tcur][mp(s, 2, 1, SV) + v];
     }
     double e2 = P.hThr * P.hThr;
     if (item_ < SC) {
         int c = item_;
         double ct[4];
-        for (int f = 0; f < 4; ++f) {
+        ct[0] = A.CT[tcur][mp(s, 4, 0, SC) + c];
+        for (int f = 1; f < 4; ++f) {
             ct[f] = A.CT[tcur][mp(s, 4, f, SC) + c];
             A.CT[tnew][mp(s, 4, f, SC) + c] = ct[f];
         }
@@ -270,10 +272,13 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
         }
         double b0c, btc, dbx, dby;
         if (PLAIN) {
-            b0c = 0.25 * ((b0[v00] + b0[v10]) + (b0[v01] + b0[v11]));
+            // b0 is static: the cell b0 (the compensated sum of the set-up) and the b0 parts
+            // of the slopes come from the cache; only the bt terms are summed here.
+            b0c = A.CT[tcur][mp(s, 4, 0, SC) + c];
+            const double* B = A.B0S + mp(s, 2, 0, SC) + c;
             btc = 0.25 * ((bt[v00] + bt[v10]) + (bt[v01] + bt[v11]));
-            dbx = 0.5 * P.dxR * (((b0[v10] - b0[v00]) + (bt[v10] - bt[v00])) + ((b0[v11] - b0[v01]) + (bt[v11] - bt[v01])));
-            dby = 0.5 * P.dyR * (((b0[v01] - b0[v00]) + (bt[v01] - bt[v00])) + ((b0[v11] - b0[v10]) + (bt[v11] - bt[v10])));
+            dbx = B[0] + P.hdxR * ((bt[v10] - bt[v00]) + (bt[v11] - bt[v01]));
+            dby = B[(size_t)SC] + P.hdyR * ((bt[v01] - bt[v00]) + (bt[v11] - bt[v10]));
         } else {
             b0c = 0.25 * kahan4(b0[v00], b0[v10], b0[v01], b0[v11]);
             btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
@@ -282,7 +287,7 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
             dbx = 0.5 * P.dxR * kahan8(ax);
             dby = 0.5 * P.dyR * kahan8(ay);
         }
-        A.CT[tnew][mp(s, 4, 0, SC) + c] = b0c;
+        if (!PLAIN) A.CT[tnew][mp(s, 4, 0, SC) + c] = b0c;
         A.CT[tnew][mp(s, 4, 1, SC) + c] = btc;
         A.CT[tnew][mp(s, 4, 2, SC) + c] = dbx;
         A.CT[tnew][mp(s, 4, 3, SC) + c] = dby;

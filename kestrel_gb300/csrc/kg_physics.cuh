@@ -31,6 +31,7 @@ struct DevParams {
     double maxPack, SolidDiameter, nu, hThr, tan1deg, SpongeStrength;
     double cfl, maxdt, diffusiveTimeScale;
     double invSolid;  // 1 / (1 - BedPorosity), for the FP32 form's multiplications
+    double hdxR, hdyR;  // 0.5 / dx, 0.5 / dy
 };
 
 // The same settings in FP32 for the FP32 form's arithmetic (a conversion from FP64 is an

@@ -39,6 +39,9 @@ __global__ void k_cell_topo(DevArrays A, const int* __restrict__ slots, int ts) 
         CT[pl(s, 4, 1, SC) + c] = btc;
         CT[pl(s, 4, 2, SC) + c] = 0.5 * P.dxR * kahan8(ax);
         CT[pl(s, 4, 3, SC) + c] = 0.5 * P.dyR * kahan8(ay);
+        // The static b0 parts of the slopes, which the FP32 form's M stages add to the bt parts.
+        A.B0S[pl(s, 2, 0, SC) + c] = P.hdxR * ((b0[v10] - b0[v00]) + (b0[v11] - b0[v01]));
+        A.B0S[pl(s, 2, 1, SC) + c] = P.hdyR * ((b0[v01] - b0[v00]) + (b0[v11] - b0[v10]));
     }
 }
 
