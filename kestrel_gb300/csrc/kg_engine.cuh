@@ -119,4 +119,29 @@ struct RasterGeo {
     int nX, nY, nXt, nYt;
 };
 
+// Programmatic dependent launch: a kernel launched with kg_launch may be scheduled while
+// the previous kernel of the stream drains (hiding the launch gap between the short
+// kernels of a step); it calls kg_dep_wait() before touching memory, which returns once
+// that kernel has completed and its writes are visible (immediately for a plain launch).
+__device__ __forceinline__ void kg_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+#define KG_TRY_LAUNCH(x)                        \
+    do {                                        \
+        cudaError_t e_ = (x);                   \
+        if (e_ != cudaSuccess) return e_;       \
+    } while (0)
+template <typename... KArgs, typename... Args>
+inline cudaError_t kg_launch(void (*k)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 }  // namespace kg

@@ -301,6 +301,7 @@ __device__ __forceinline__ bool stage_gate_open(const DevParams& P, const StepAr
 // the distance to the next flux knot) (src/TimeStepper.f90:151-183), from the CFL word of
 // the RHS pass; cap is the host's (tmax - t) or (tmax - t)/2.
 __global__ void k_dt(const unsigned long long* __restrict__ cfl, int partial, double cap, double* dtp) {
+    kg_dep_wait();
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         double adv = 0.9 * advised_m(cP, *cfl, partial);
         *dtp = mn(adv, cap);
@@ -308,11 +309,12 @@ __global__ void k_dt(const unsigned long long* __restrict__ cfl, int partial, do
 }
 
 cudaError_t launch_dt(const unsigned long long* cfl, int partial, double cap, double* dtp, cudaStream_t st) {
-    k_dt<<<1, 32, 0, st>>>(cfl, partial, cap, dtp);
+    KG_TRY_LAUNCH(kg_launch(k_dt, 1, 32, 0, st, cfl, partial, cap, dtp));
     return cudaGetLastError();
 }
 
 __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
+    kg_dep_wait();
     StageTimes Tm;
     if (!stage_gate_open(cP, S, Tm)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -682,7 +684,7 @@ cudaError_t launch_hydro(const DevArrays& A, const BlockDesc* blocks, int nblock
         attr = true;
     }
     if (nblocks == 0) return cudaSuccess;
-    k_hydro<<<nblocks, NT, sizeof(HydroSmem), st>>>(A, blocks, S);
+    KG_TRY_LAUNCH(kg_launch(k_hydro, nblocks, NT, sizeof(HydroSmem), st, A, blocks, S));
     return cudaGetLastError();
 }
 

@@ -441,6 +441,7 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
 }
 
 __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
+    kg_dep_wait();
     StageTimes Tm;
     if (!stage_gate_open(cP, S, Tm)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -508,6 +509,7 @@ __device__ __forceinline__ void topo32(const DevParams& P, const DevArrays& A, i
 }
 
 __global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restrict__ slots, int ts, int per) {
+    kg_dep_wait();
     topo32(cP, A, slots[blockIdx.x / per], (blockIdx.x % per) * 256 + threadIdx.x, ts);
 }
 
@@ -521,7 +523,7 @@ cudaError_t launch_hydro32(const DevArrays& A, const BlockDesc* blocks, int nblo
         attr = true;
     }
     if (nblocks == 0) return cudaSuccess;
-    k_hydro32<<<nblocks, NT, sizeof(Hydro32Smem), st>>>(A, blocks, S);
+    KG_TRY_LAUNCH(kg_launch(k_hydro32, nblocks, NT, sizeof(Hydro32Smem), st, A, blocks, S));
     return cudaGetLastError();
 }
 
@@ -529,7 +531,7 @@ cudaError_t launch_topo32(const DevArrays& A, const int* d_slots, int n, int ts,
     int items = (nX + 1) * (nY + 1);
     int per = (items + 255) / 256;
     if (n <= 0) return cudaSuccess;
-    k_topo32<<<n * per, 256, 0, st>>>(A, d_slots, ts, per);
+    KG_TRY_LAUNCH(kg_launch(k_topo32, n * per, 256, 0, st, A, d_slots, ts, per));
     return cudaGetLastError();
 }
 

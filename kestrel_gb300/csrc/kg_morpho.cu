@@ -642,12 +642,14 @@ __device__ __forceinline__ void m_finish(const DevParams& P, const DevArrays& A,
 template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew,
                                                 int* ctl_flags) {
+    kg_dep_wait();
     if (blockIdx.x == 0 && threadIdx.x < 2) ctl_flags[threadIdx.x] = 0;
     KG_TILE_ITEMS((cP.nX + 1) * (cP.nY + 1))
     m_init<PLAIN>(cP, A, s, item_, qa, tcur, tnew);
 }
 template <class R>
 __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
+    kg_dep_wait();
     KG_TILE_ITEMS(cP.nX * cP.nY)
     m_emd<R>(cP, cP32, A, s, item_, tnew);
 }
@@ -656,17 +658,20 @@ template <bool PLAIN>
 // an M queued before the host has read that dt back.
 __global__ void __launch_bounds__(256) k_m_bt(DevArrays A, const int* __restrict__ slots, int tcur, int tnew, int stage, double dt,
                                               const double* __restrict__ dtp) {
+    kg_dep_wait();
     KG_TILE_ITEMS((cP.nX + 1) * (cP.nY + 1))
     m_bt<PLAIN>(cP, A, s, item_, tcur, tnew, stage, dtp ? 2.0 * dtp[0] : dt);
 }
 template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_cells(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew) {
+    kg_dep_wait();
     KG_TILE_ITEMS(cP.nX * cP.nY)
     m_cells<PLAIN>(cP, cP32, A, s, item_, qa, tcur, tnew);
 }
 template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_check(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew, int* flags,
                                                  unsigned long long* cand_key, double* cand_ex, int* ncand, int cand_cap) {
+    kg_dep_wait();
     KG_TILE_ITEMS(cP.nX * cP.nY)
     m_check<PLAIN>(cP, A, s, item_, pos, qa, tcur, tnew, flags, cand_key, cand_ex, ncand, cand_cap);
 }
@@ -675,6 +680,7 @@ __global__ void __launch_bounds__(REDIST_THREADS) k_m_redist(DevArrays A, const 
                                                              const int* __restrict__ list_cell,
                                                              const int* __restrict__ wave_off, int nwaves, int qa, int tcur,
                                                              int tnew, int* flags) {
+    kg_dep_wait();
     m_redist<PLAIN>(cP, A, list_slot, list_cell, wave_off, nwaves, qa, tcur, tnew, flags);
 }
 // One wave of the ordered walk, one 32-thread CTA per listed cell, so the wave's FP64 work
@@ -684,6 +690,7 @@ template <bool PLAIN>
 __global__ void __launch_bounds__(32) k_m_redist_wave(DevArrays A, const int* __restrict__ list_slot,
                                                       const int* __restrict__ list_cell, int qa, int tcur, int tnew,
                                                       int* flags) {
+    kg_dep_wait();
     const int lane = threadIdx.x;
     // The failure flag and the list entry are independent loads, issued together.
     int failed = *(volatile int*)flags;
@@ -726,6 +733,7 @@ __device__ __forceinline__ void m_close(const DevParams& P, const DevArrays& A, 
 }
 template <bool PLAIN>
 __global__ void __launch_bounds__(256) k_m_close(DevArrays A, const int* __restrict__ slots, int qa, int tnew, int per) {
+    kg_dep_wait();
     m_close<PLAIN>(cP, A, slots[blockIdx.x / per], (blockIdx.x % per) * 256 + threadIdx.x, qa, tnew);
 }
 __global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
@@ -739,35 +747,35 @@ static inline int per_of(int items) { return (items + 255) / 256; }
 cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, int* ctl_flags,
                           bool fp32, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (fp32) k_m_init<true><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, ctl_flags);
-    else k_m_init<false><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, ctl_flags);
+    if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_init<true>, n * per_of(verts), 256, 0, st, A, d_slots, qa, tcur, tnew, ctl_flags));
+    else KG_TRY_LAUNCH(kg_launch(k_m_init<false>, n * per_of(verts), 256, 0, st, A, d_slots, qa, tcur, tnew, ctl_flags));
     return cudaGetLastError();
 }
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (fp32) k_m_emd<float><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, tnew);
-    else k_m_emd<double><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, tnew);
+    if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_emd<float>, n * per_of(cells), 256, 0, st, A, d_slots, tnew));
+    else KG_TRY_LAUNCH(kg_launch(k_m_emd<double>, n * per_of(cells), 256, 0, st, A, d_slots, tnew));
     return cudaGetLastError();
 }
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
                         const double* dtp, bool fp32, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (fp32) k_m_bt<true><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt, dtp);
-    else k_m_bt<false><<<n * per_of(verts), 256, 0, st>>>(A, d_slots, tcur, tnew, stage, dt, dtp);
+    if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_bt<true>, n * per_of(verts), 256, 0, st, A, d_slots, tcur, tnew, stage, dt, dtp));
+    else KG_TRY_LAUNCH(kg_launch(k_m_bt<false>, n * per_of(verts), 256, 0, st, A, d_slots, tcur, tnew, stage, dt, dtp));
     return cudaGetLastError();
 }
 cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, bool fp32,
                            cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (fp32) k_m_cells<true><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
-    else k_m_cells<false><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew);
+    if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_cells<true>, n * per_of(cells), 256, 0, st, A, d_slots, qa, tcur, tnew));
+    else KG_TRY_LAUNCH(kg_launch(k_m_cells<false>, n * per_of(cells), 256, 0, st, A, d_slots, qa, tcur, tnew));
     return cudaGetLastError();
 }
 cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, int* flags,
                            unsigned long long* keys, double* ex, int* ncand, int cap, bool fp32, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (fp32) k_m_check<true><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
-    else k_m_check<false><<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap);
+    if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_check<true>, n * per_of(cells), 256, 0, st, A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap));
+    else KG_TRY_LAUNCH(kg_launch(k_m_check<false>, n * per_of(cells), 256, 0, st, A, d_slots, qa, tcur, tnew, flags, keys, ex, ncand, cap));
     return cudaGetLastError();
 }
 // hwoff: the wave offsets on the host (one launch per wave while the waves are few).
@@ -775,15 +783,15 @@ cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, co
                             int qa, int tcur, int tnew, int* flags, bool fp32, cudaStream_t st) {
     if (nwaves == 0) return cudaSuccess;
     if (nwaves > KG_REDIST_WAVE_MAX) {
-        if (fp32) k_m_redist<true><<<1, REDIST_THREADS, 0, st>>>(A, ls, lc, woff, nwaves, qa, tcur, tnew, flags);
-        else k_m_redist<false><<<1, REDIST_THREADS, 0, st>>>(A, ls, lc, woff, nwaves, qa, tcur, tnew, flags);
+        if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_redist<true>, 1, REDIST_THREADS, 0, st, A, ls, lc, woff, nwaves, qa, tcur, tnew, flags));
+        else KG_TRY_LAUNCH(kg_launch(k_m_redist<false>, 1, REDIST_THREADS, 0, st, A, ls, lc, woff, nwaves, qa, tcur, tnew, flags));
         return cudaGetLastError();
     }
     for (int w = 0; w < nwaves; ++w) {
         int n = hwoff[w + 1] - hwoff[w];
         if (n <= 0) continue;
-        if (fp32) k_m_redist_wave<true><<<n, 32, 0, st>>>(A, ls + hwoff[w], lc + hwoff[w], qa, tcur, tnew, flags);
-        else k_m_redist_wave<false><<<n, 32, 0, st>>>(A, ls + hwoff[w], lc + hwoff[w], qa, tcur, tnew, flags);
+        if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_redist_wave<true>, n, 32, 0, st, A, ls + hwoff[w], lc + hwoff[w], qa, tcur, tnew, flags));
+        else KG_TRY_LAUNCH(kg_launch(k_m_redist_wave<false>, n, 32, 0, st, A, ls + hwoff[w], lc + hwoff[w], qa, tcur, tnew, flags));
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -803,8 +811,8 @@ cudaError_t launch_m_close(const DevArrays& A, const int* d_slots, int n, int nX
                            cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     int per = per_of((nX + 1) * (nY + 1));
-    if (fp32) k_m_close<true><<<n * per, 256, 0, st>>>(A, d_slots, qa, tnew, per);
-    else k_m_close<false><<<n * per, 256, 0, st>>>(A, d_slots, qa, tnew, per);
+    if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_close<true>, n * per, 256, 0, st, A, d_slots, qa, tnew, per));
+    else KG_TRY_LAUNCH(kg_launch(k_m_close<false>, n * per, 256, 0, st, A, d_slots, qa, tnew, per));
     return cudaGetLastError();
 }
 

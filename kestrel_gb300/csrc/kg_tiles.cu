@@ -304,6 +304,7 @@ __device__ __forceinline__ int block_or(int f) {
 // One word per (tile, chunk): the host ORs a tile's chunks, so nothing needs zeroing.
 __global__ void __launch_bounds__(256) k_act_flags(DevArrays A, const int* __restrict__ slots, int qcur, int ts,
                                                     const double* __restrict__ hn_over, int* __restrict__ flags, int per) {
+    kg_dep_wait();
     int pos = blockIdx.x / per, chunk = blockIdx.x % per;
     int f = block_or(act_bits(cP, A, slots[pos], qcur, ts, hn_over, chunk));
     if (threadIdx.x == 0) flags[blockIdx.x] = f;
@@ -392,7 +393,7 @@ cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int 
                              int nX, int nY, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     int per = (nX * nY + 255) / 256;
-    k_act_flags<<<n * per, 256, 0, st>>>(A, d_slots, qcur, ts, hn_over, d_flags, per);
+    KG_TRY_LAUNCH(kg_launch(k_act_flags, n * per, 256, 0, st, A, d_slots, qcur, ts, hn_over, d_flags, per));
     return cudaGetLastError();
 }
 cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
