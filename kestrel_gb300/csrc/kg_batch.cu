@@ -36,6 +36,7 @@ struct SimStatic {
 __global__ void __launch_bounds__(NT) k_hydro32_batch(const SimStatic* __restrict__ sims, const StepArgs* __restrict__ args,
                                                       const int* __restrict__ member, const int* __restrict__ prefix,
                                                       int njobs, int total) {
+    kg_dep_wait();
     extern __shared__ __align__(16) unsigned char smraw[];
     Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
     for (int b = blockIdx.x; b < total; b += gridDim.x) {
@@ -61,6 +62,7 @@ struct DtJob {
     int partial, member;
 };
 __global__ void k_dt_batch(const SimStatic* __restrict__ sims, const DtJob* __restrict__ jobs, int n) {
+    kg_dep_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const DtJob& J = jobs[i];
@@ -75,6 +77,7 @@ struct ActJob {
 };
 __global__ void __launch_bounds__(256) k_act_flags_batch(const SimStatic* __restrict__ sims, const ActJob* __restrict__ jobs,
                                                           const int* __restrict__ prefix, int njobs, int total, int* out) {
+    kg_dep_wait();
     for (int b = blockIdx.x; b < total; b += gridDim.x) {
         int lo = 0, hi = njobs - 1;
         while (lo < hi) {
@@ -107,6 +110,7 @@ enum MKind { MK_INIT, MK_EMD, MK_BT, MK_CELLS, MK_CHECK, MK_CLOSE };
 template <int K>
 __global__ void __launch_bounds__(256) k_m_batch(const SimStatic* __restrict__ sims, const MJob* __restrict__ jobs,
                                                  const int* __restrict__ prefix, int njobs, int total, int stage) {
+    kg_dep_wait();
     for (int b = blockIdx.x; b < total; b += gridDim.x) {
         int lo = 0, hi = njobs - 1;
         while (lo < hi) {
@@ -145,6 +149,7 @@ struct RJob {
 };
 __global__ void __launch_bounds__(REDIST_THREADS) k_m_redist_batch(const SimStatic* __restrict__ sims,
                                                                    const RJob* __restrict__ jobs) {
+    kg_dep_wait();
     const RJob& J = jobs[blockIdx.x];
     const SimStatic& X = sims[J.member];
     m_redist<true>(X.P, X.A, J.list_slot, J.list_cell, J.wave_off, J.nwaves, J.qa, J.tcur, J.tnew, J.flags);
@@ -257,7 +262,7 @@ void launch_hydro_batch(kg_batch& b, const std::vector<int>& who, const std::vec
     CK(cudaMemcpyAsync(dm, hm, (size_t)2 * (b.cap + 1) * sizeof(int), cudaMemcpyHostToDevice, b.st));
     if (total == 0) return;
     int grid = std::min(total, b.grid_hydro);
-    k_hydro32_batch<<<grid, NT, sizeof(Hydro32Smem), b.st>>>(b.d_static, da, dm, dp, n, total);
+    CK(kg_launch(k_hydro32_batch, grid, NT, sizeof(Hydro32Smem), b.st, b.d_static, da, dm, dp, n, total));
     CK(cudaGetLastError());
     b.launches++;
 }
@@ -336,7 +341,7 @@ void queue_flags_batch(kg_batch& b, const std::vector<int>& who, const std::vect
     CK(cudaMemcpyAsync(b.d_act, b.h_act, (size_t)n * sizeof(ActJob), cudaMemcpyHostToDevice, b.st));
     CK(cudaMemcpyAsync(dp, hp, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, b.st));
     if (total == 0) return;
-    k_act_flags_batch<<<std::min(total, b.grid_act), 256, 0, b.st>>>(b.d_static, b.d_act, dp, n, total, b.d_actout);
+    CK(kg_launch(k_act_flags_batch, std::min(total, b.grid_act), 256, 0, b.st, b.d_static, b.d_act, dp, n, total, b.d_actout));
     CK(cudaGetLastError());
     b.launches++;
     CK(cudaMemcpyAsync(b.h_actout, b.d_actout, (size_t)total * sizeof(int), cudaMemcpyDeviceToHost, b.st));
@@ -410,7 +415,7 @@ void phase_h(kg_batch& b, const std::vector<int>& who) {
             b.h_dt[k] = DtJob{m.c->d_cfl + W_RHS, m.c->d_dt, m.cap, partial(*m.c), fresh[(size_t)k]};
         }
         CK(cudaMemcpyAsync(b.d_dt, b.h_dt, (size_t)n * sizeof(DtJob), cudaMemcpyHostToDevice, b.st));
-        k_dt_batch<<<(n + 127) / 128, 128, 0, b.st>>>(b.d_static, b.d_dt, n);
+        CK(kg_launch(k_dt_batch, (n + 127) / 128, 128, 0, b.st, b.d_static, b.d_dt, n));
         CK(cudaGetLastError());
         b.launches++;
     }
@@ -468,8 +473,8 @@ int upload_mjobs(kg_batch& b, int t, const std::vector<int>& who) {
 template <int K>
 void launch_m(kg_batch& b, int t, int n, int total, int stage = 0) {
     if (n == 0 || total == 0) return;
-    k_m_batch<K><<<std::min(total, b.grid_m), 256, 0, b.st>>>(b.d_static, b.d_mjob + (size_t)t * b.cap,
-                                                             b.d_mpre + (size_t)t * (b.cap + 1), n, total, stage);
+    CK(kg_launch(k_m_batch<K>, std::min(total, b.grid_m), 256, 0, b.st, b.d_static, b.d_mjob + (size_t)t * b.cap,
+                                                             b.d_mpre + (size_t)t * (b.cap + 1), n, total, stage));
     CK(cudaGetLastError());
     b.launches++;
 }
@@ -559,7 +564,7 @@ void phase_m(kg_batch& b, const std::vector<int>& who) {
     }
     if (!listed.empty()) {
         CK(cudaMemcpyAsync(b.d_rjob, b.h_rjob, listed.size() * sizeof(RJob), cudaMemcpyHostToDevice, b.st));
-        k_m_redist_batch<<<(int)listed.size(), REDIST_THREADS, 0, b.st>>>(b.d_static, b.d_rjob);
+        CK(kg_launch(k_m_redist_batch, (int)listed.size(), REDIST_THREADS, 0, b.st, b.d_static, b.d_rjob));
         CK(cudaGetLastError());
         b.launches++;
     }
