@@ -290,7 +290,10 @@ void queue_stages_batch(kg_batch& b, const std::vector<int>& who, bool m_gates) 
         StepArgs S{};
         S.q_in = q_in; S.q_s1 = q_s1; S.q_s2 = q_s2; S.q_out = q_out; S.e_set = e_set; S.topo = topo;
         S.q_tc = c.qcur; S.topo_tc = c.tcur;
-        S.dt = dt; S.dtp = fresh ? c.d_dt : nullptr; S.t_grid = c.t; S.do_maxima = 1;
+        // The running maxima change only in the first accepted half-step of a step (they read
+        // the step-start state with strict comparisons); later half-steps skip them.
+        if (fresh) c.maxima_done = false;
+        S.dt = dt; S.dtp = fresh ? c.d_dt : nullptr; S.t_grid = c.t; S.do_maxima = (m_gates || c.maxima_done) ? 0 : 1;
         int g0 = 0;
         if (m_gates) {
             S.gate_flag = c.d_mflags;
@@ -448,6 +451,7 @@ void phase_h(kg_batch& b, const std::vector<int>& who) {
         }
         bool rej = finish_hydraulic(c, m.dt, m.o[0], c.tcur, !m.morpho, chunks);
         if (rej) { refuse(m); continue; }
+        c.maxima_done = true;
         if (!m.morpho) finish_step(m, m.o[0]);
         else m.state = ST_M;
     }

@@ -176,6 +176,7 @@ struct kg_ctx {
     double t = 0.0, dt = 1.0e-5, t0 = 0.0;
     int64_t launches = 0, steps = 0, rejected = 0, cell_updates = 0;
     int64_t h2d_bytes = 0, d2h_bytes = 0;  // host<->device traffic of this context
+    bool maxima_done = false;              // the running maxima were updated in this step
     int64_t redist_cells = 0, redist_waves = 0, redist_walks = 0;
     // Host wall time (s): whole steps, waiting in stream synchronisations, planning the
     // redistribution walk (read-back of the list excluded).
@@ -958,7 +959,10 @@ void queue_hydraulic(kg_ctx& c, double dt, const double* dtp, int q_in, int e_se
     StepArgs S{};
     S.q_in = q_in; S.q_s1 = q_s1; S.q_s2 = q_s2; S.q_out = q_out; S.e_set = e_set; S.topo = topo;
     S.q_tc = c.qcur; S.topo_tc = c.tcur;
-    S.dt = dt; S.dtp = dtp; S.t_grid = c.t; S.do_maxima = 1;
+    // UpdateMaximum* reads the step-start state, so after the first accepted half-step of a
+    // step every later one (the second half-step, the half-steps of a retry) finds each
+    // maximum already taken with strict comparisons and changes nothing: it is skipped.
+    S.dt = dt; S.dtp = dtp; S.t_grid = c.t; S.do_maxima = c.maxima_done ? 0 : 1;
     S.gate_flag = gflag;
     int g0 = 0;
     if (gs1) { S.gate[0] = gs1; S.gate_s1[0] = 1; g0 = 1; }
@@ -1246,6 +1250,7 @@ void integrate_step_body(kg_ctx& c, double tend) {
     double tmax = mn(tend, next_flux_time(c, c.t));
     double cap = morpho ? 0.5 * (tmax - c.t) : tmax - c.t;
     c.t0 = c.t;
+    c.maxima_done = false;
     StepArgs R = rhs_args(c, c.qcur, 0, c.tcur, c.t);
     reset_cfl(c, W_RHS, 1);
     launch_pass(c, R, W_RHS);
@@ -1277,6 +1282,7 @@ void integrate_step_body(kg_ctx& c, double tend) {
         first = false;
         bool rej = finish_hydraulic(c, dt, o[0], c.tcur, !morpho);
         if (rej) { c.rejected++; continue; }
+        c.maxima_done = true;
         if (!morpho) { newcur = o[0]; break; }
         int r = finish_morpho_and_h2(c, dt, o, tnew);
         if (r == 0) { newcur = o[1]; break; }

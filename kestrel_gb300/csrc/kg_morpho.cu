@@ -38,6 +38,10 @@ __device__ __forceinline__ double rsqrt_nr(double x) {
 // Bitwise equality of two doubles on the integer pipe (FP64 compares use the FP64 pipe,
 // 1/64 of the FP32 rate on this GPU); differs from == only for +-0 and NaN.
 __device__ __forceinline__ bool same_bits(double a, double b) { return __double_as_longlong(a) == __double_as_longlong(b); }
+// x < e for e > 0 on the integer pipe: IEEE bit patterns of non-negative doubles order as
+// their values and negative ones compare below every positive pattern (only a NaN with the
+// sign bit set differs from the FP64 compare).
+__device__ __forceinline__ bool below_pos(double x, double e) { return __double_as_longlong(x) < __double_as_longlong(e); }
 __device__ __forceinline__ double gam_cached(const DevParams& P, const DevArrays& A, int ts, int s, int c, double bx, double by) {
     if (!P.geo) return 1.0;
     int SC = P.nX * P.nY;
@@ -118,7 +122,12 @@ __device__ __forceinline__ void m_emd(const DevParams& P, const DevParams32& F, 
         double HnN = (j == nY - 1) ? stage_hn(A, sN, i, SC) : A.MS[mp(s, 5, 2, SC) + c + nX];
         double e = P.hThr;
         double emd = 0.0;
-        if (!(Hn < e || HnW < e || HnE < e || HnS < e || HnN < e)) {
+        bool dry;
+        if constexpr (sizeof(R) == sizeof(float))
+            dry = below_pos(Hn, e) || below_pos(HnW, e) || below_pos(HnE, e) || below_pos(HnS, e) || below_pos(HnN, e);
+        else
+            dry = Hn < e || HnW < e || HnE < e || HnS < e || HnN < e;
+        if (!dry) {
             R dbx = (R)CT[mp(s, 4, 2, SC) + c], dby = (R)CT[mp(s, 4, 3, SC) + c];
             Pt<R> pt{(R)Hn, (R)A.UV[mp(s, 2, 0, SC) + c], (R)A.UV[mp(s, 2, 1, SC) + c], (R)A.MS[mp(s, 5, 3, SC) + c],
                      (R)A.MS[mp(s, 5, 4, SC) + c], (R)CT[mp(s, 4, 1, SC) + c], dbx, dby, gam_of<R>(P.geo, dbx, dby)};
@@ -203,17 +212,24 @@ __device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int
             mode = 2;
         }
         double x[4], y[4], e[4];
-        for (int q = 0; q < 4; ++q) {
-            x[q] = cellv(A, CT, cs[q], 2, ci[q], cj[q], nX, SC);
-            y[q] = cellv(A, CT, cs[q], 3, ci[q], cj[q], nX, SC);
-            e[q] = cellv(A, CT, cs[q], -1, ci[q], cj[q], nX, SC);
-        }
-        double kx, ky, ke;
+        for (int q = 0; q < 4; ++q) e[q] = cellv(A, CT, cs[q], -1, ci[q], cj[q], nX, SC);
+        double kx = 0.0, ky = 0.0, ke;
         if (PLAIN) {
-            kx = (x[0] + x[1]) + (x[2] + x[3]);
-            ky = (y[0] + y[1]) + (y[2] + y[3]);
+            // the slopes only matter where E - D is non-zero around the vertex
             ke = (e[0] + e[1]) + (e[2] + e[3]);
+            if (ke != 0.0) {
+                for (int q = 0; q < 4; ++q) {
+                    x[q] = cellv(A, CT, cs[q], 2, ci[q], cj[q], nX, SC);
+                    y[q] = cellv(A, CT, cs[q], 3, ci[q], cj[q], nX, SC);
+                }
+                kx = (x[0] + x[1]) + (x[2] + x[3]);
+                ky = (y[0] + y[1]) + (y[2] + y[3]);
+            }
         } else {
+            for (int q = 0; q < 4; ++q) {
+                x[q] = cellv(A, CT, cs[q], 2, ci[q], cj[q], nX, SC);
+                y[q] = cellv(A, CT, cs[q], 3, ci[q], cj[q], nX, SC);
+            }
             kx = (mode == 2) ? kahan3(x[0], x[1], x[2] + x[3]) : kahan4(x[0], x[1], x[2], x[3]);
             ky = kahan4(y[0], y[1], y[2], y[3]);
             ke = (mode == 1) ? kahan3(e[0], e[1], e[2] + e[3]) : kahan4(e[0], e[1], e[2], e[3]);
@@ -229,7 +245,7 @@ __device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int
             if (ke != 0.0) {
                 float gx = 0.25f * (float)kx, gy = 0.25f * (float)ky;
                 float gam = P.geo ? sqrtf(1.f + gx * gx + gy * gy) : 1.f;
-                ddt = -0.25f * gam * (float)ke / (float)psib;
+                ddt = -0.25f * gam * (float)ke * (float)P.invSolid;
             }
             double inc = (btp - bt0) + dt * (double)ddt;
             if (stage == 1) nb = bt0 + dt * (double)ddt;
