@@ -188,53 +188,56 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
     // ---- B: limited slopes and face offsets ----
     const int lim = P.limiter;
     const float dxR = F.dxR, dyR = F.dyR;
-    for (int k = tid; k < (bx + 2) * by; k += NT) {
-        int cx = k % (bx + 2) - 1, cy = k / (bx + 2);
-        int r = (cy + 2) * RG + (cx + 2);
-        int li = cy * (BS + 2) + (cx + 1);
-        bool ghW = (cx < 0 && bd.x0 == 0 && A.kind[nbW] == SLOT_GHOST);
-        bool ghE = (cx >= bx && bd.x0 + bx == nX && A.kind[nbE] == SLOT_GHOST);
-        if (ghW || ghE) {
-            int gs = ghW ? nbW : nbE;
-            sm.lx[0][li] = (float)A.GE[plane(gs, GE_COUNT, ghW ? GE_LXN : GE_LX1, A.nE) + bd.y0 + cy];
-            sm.lx[1][li] = 0.f; sm.lx[2][li] = 0.f; sm.lx[3][li] = 0.f; sm.lx[4][li] = 0.f;
+    for (int kk = tid; kk < (bx + 2) * by + (by + 2) * bx; kk += NT) {
+        if (kk < (bx + 2) * by) {
+            const int k = kk;
+            int cx = k % (bx + 2) - 1, cy = k / (bx + 2);
+            int r = (cy + 2) * RG + (cx + 2);
+            int li = cy * (BS + 2) + (cx + 1);
+            bool ghW = (cx < 0 && bd.x0 == 0 && A.kind[nbW] == SLOT_GHOST);
+            bool ghE = (cx >= bx && bd.x0 + bx == nX && A.kind[nbE] == SLOT_GHOST);
+            if (ghW || ghE) {
+                int gs = ghW ? nbW : nbE;
+                sm.lx[0][li] = (float)A.GE[plane(gs, GE_COUNT, ghW ? GE_LXN : GE_LX1, A.nE) + bd.y0 + cy];
+                sm.lx[1][li] = 0.f; sm.lx[2][li] = 0.f; sm.lx[3][li] = 0.f; sm.lx[4][li] = 0.f;
+            } else {
+                sm.lx[0][li] = dxR * limiter<float>(lim, (float)(sm.w[r + 1] - sm.w[r]), (float)(sm.w[r] - sm.w[r - 1]));
+                sm.lx[1][li] = dxR * limiter<float>(lim, sm.p[r + 1] - sm.p[r], sm.p[r] - sm.p[r - 1]);
+                sm.lx[2][li] = dxR * limiter<float>(lim, sm.u[r + 1] - sm.u[r], sm.u[r] - sm.u[r - 1]);
+                sm.lx[3][li] = dxR * limiter<float>(lim, sm.v[r + 1] - sm.v[r], sm.v[r] - sm.v[r - 1]);
+                sm.lx[4][li] = dxR * limiter<float>(lim, sm.rho[r + 1] - sm.rho[r], sm.rho[r] - sm.rho[r - 1]);
+            }
+            int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
+            if (i < 0) { s = nbW; i += nX; }
+            else if (i >= nX) { s = nbE; i -= nX; }
+            const double* bI = FX + plane(s, 5, 4, SFX) + (size_t)j * (nX + 1) + i;
+            sm.dlo[0][li] = (float)(sm.w[r] - bI[0]);
+            sm.dhi[0][li] = (float)(sm.w[r] - bI[1]);
         } else {
-            sm.lx[0][li] = dxR * limiter<float>(lim, (float)(sm.w[r + 1] - sm.w[r]), (float)(sm.w[r] - sm.w[r - 1]));
-            sm.lx[1][li] = dxR * limiter<float>(lim, sm.p[r + 1] - sm.p[r], sm.p[r] - sm.p[r - 1]);
-            sm.lx[2][li] = dxR * limiter<float>(lim, sm.u[r + 1] - sm.u[r], sm.u[r] - sm.u[r - 1]);
-            sm.lx[3][li] = dxR * limiter<float>(lim, sm.v[r + 1] - sm.v[r], sm.v[r] - sm.v[r - 1]);
-            sm.lx[4][li] = dxR * limiter<float>(lim, sm.rho[r + 1] - sm.rho[r], sm.rho[r] - sm.rho[r - 1]);
+            const int k = kk - ((bx + 2) * by);
+            int cx = k % bx, cy = k / bx - 1;
+            int r = (cy + 2) * RG + (cx + 2);
+            int li = (cy + 1) * BS + cx;
+            bool ghS = (cy < 0 && bd.y0 == 0 && A.kind[nbS] == SLOT_GHOST);
+            bool ghN = (cy >= by && bd.y0 + by == nY && A.kind[nbN] == SLOT_GHOST);
+            if (ghS || ghN) {
+                int gs = ghS ? nbS : nbN;
+                sm.ly[0][li] = (float)A.GE[plane(gs, GE_COUNT, ghS ? GE_LYN : GE_LY1, A.nE) + bd.x0 + cx];
+                sm.ly[1][li] = 0.f; sm.ly[2][li] = 0.f; sm.ly[3][li] = 0.f; sm.ly[4][li] = 0.f;
+            } else {
+                sm.ly[0][li] = dyR * limiter<float>(lim, (float)(sm.w[r + RG] - sm.w[r]), (float)(sm.w[r] - sm.w[r - RG]));
+                sm.ly[1][li] = dyR * limiter<float>(lim, sm.p[r + RG] - sm.p[r], sm.p[r] - sm.p[r - RG]);
+                sm.ly[2][li] = dyR * limiter<float>(lim, sm.u[r + RG] - sm.u[r], sm.u[r] - sm.u[r - RG]);
+                sm.ly[3][li] = dyR * limiter<float>(lim, sm.v[r + RG] - sm.v[r], sm.v[r] - sm.v[r - RG]);
+                sm.ly[4][li] = dyR * limiter<float>(lim, sm.rho[r + RG] - sm.rho[r], sm.rho[r] - sm.rho[r - RG]);
+            }
+            int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
+            if (j < 0) { s = nbS; j += nY; }
+            else if (j >= nY) { s = nbN; j -= nY; }
+            const double* bI = FY + plane(s, 5, 4, SFY) + (size_t)j * nX + i;
+            sm.dlo[1][li] = (float)(sm.w[r] - bI[0]);
+            sm.dhi[1][li] = (float)(sm.w[r] - bI[nX]);
         }
-        int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
-        if (i < 0) { s = nbW; i += nX; }
-        else if (i >= nX) { s = nbE; i -= nX; }
-        const double* bI = FX + plane(s, 5, 4, SFX) + (size_t)j * (nX + 1) + i;
-        sm.dlo[0][li] = (float)(sm.w[r] - bI[0]);
-        sm.dhi[0][li] = (float)(sm.w[r] - bI[1]);
-    }
-    for (int k = tid; k < (by + 2) * bx; k += NT) {
-        int cx = k % bx, cy = k / bx - 1;
-        int r = (cy + 2) * RG + (cx + 2);
-        int li = (cy + 1) * BS + cx;
-        bool ghS = (cy < 0 && bd.y0 == 0 && A.kind[nbS] == SLOT_GHOST);
-        bool ghN = (cy >= by && bd.y0 + by == nY && A.kind[nbN] == SLOT_GHOST);
-        if (ghS || ghN) {
-            int gs = ghS ? nbS : nbN;
-            sm.ly[0][li] = (float)A.GE[plane(gs, GE_COUNT, ghS ? GE_LYN : GE_LY1, A.nE) + bd.x0 + cx];
-            sm.ly[1][li] = 0.f; sm.ly[2][li] = 0.f; sm.ly[3][li] = 0.f; sm.ly[4][li] = 0.f;
-        } else {
-            sm.ly[0][li] = dyR * limiter<float>(lim, (float)(sm.w[r + RG] - sm.w[r]), (float)(sm.w[r] - sm.w[r - RG]));
-            sm.ly[1][li] = dyR * limiter<float>(lim, sm.p[r + RG] - sm.p[r], sm.p[r] - sm.p[r - RG]);
-            sm.ly[2][li] = dyR * limiter<float>(lim, sm.u[r + RG] - sm.u[r], sm.u[r] - sm.u[r - RG]);
-            sm.ly[3][li] = dyR * limiter<float>(lim, sm.v[r + RG] - sm.v[r], sm.v[r] - sm.v[r - RG]);
-            sm.ly[4][li] = dyR * limiter<float>(lim, sm.rho[r + RG] - sm.rho[r], sm.rho[r] - sm.rho[r - RG]);
-        }
-        int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
-        if (j < 0) { s = nbS; j += nY; }
-        else if (j >= nY) { s = nbN; j -= nY; }
-        const double* bI = FY + plane(s, 5, 4, SFY) + (size_t)j * nX + i;
-        sm.dlo[1][li] = (float)(sm.w[r] - bI[0]);
-        sm.dhi[1][li] = (float)(sm.w[r] - bI[nX]);
     }
     __syncthreads();
 
@@ -243,97 +246,100 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
     const float hdx = 0.5f * F.dx, hdy = 0.5f * F.dy;
     const float* __restrict__ TFXs = A.TFX[S.topo] + (size_t)slot * 2 * SFX;
     const float* __restrict__ TFYs = A.TFY[S.topo] + (size_t)slot * 2 * SFY;
-    for (int k = tid; k < (bx + 1) * by; k += NT) {
-        int fx = k % (bx + 1), cy = k / (bx + 1);
-        int fi = bd.x0 + fx, j = bd.y0 + cy;
-        int rL = (cy + 2) * RG + (fx + 1), rR = rL + 1;
-        int liL = cy * (BS + 2) + fx, liR = liL + 1;
-        Side32 L, R;
-        // Left state: the upper-face reconstruction of cell fx-1.
-        float s = sm.lx[0][liL] * hdx, sp = sm.lx[1][liL] * hdx;
-        bool corr;
-        if (fi == 0 && A.kind[nbW] == SLOT_GHOST) {
-            const double* fxs = FX + plane(nbW, 5, 4, SFX);
-            double bl = fxs[j * (nX + 1) + nX - 1], br = fxs[j * (nX + 1) + nX];
-            const double* ge = A.GE + plane(nbW, GE_COUNT, 0, A.nE);
-            corr = ge[GE_MXN1 * A.nE + j] < br || ge[GE_PXN * A.nE + j] < bl;
+    for (int kk = tid; kk < (bx + 1) * by + (by + 1) * bx; kk += NT) {
+        if (kk < (bx + 1) * by) {
+            const int k = kk;
+            int fx = k % (bx + 1), cy = k / (bx + 1);
+            int fi = bd.x0 + fx, j = bd.y0 + cy;
+            int rL = (cy + 2) * RG + (fx + 1), rR = rL + 1;
+            int liL = cy * (BS + 2) + fx, liR = liL + 1;
+            Side32 L, R;
+            // Left state: the upper-face reconstruction of cell fx-1.
+            float s = sm.lx[0][liL] * hdx, sp = sm.lx[1][liL] * hdx;
+            bool corr;
+            if (fi == 0 && A.kind[nbW] == SLOT_GHOST) {
+                const double* fxs = FX + plane(nbW, 5, 4, SFX);
+                double bl = fxs[j * (nX + 1) + nX - 1], br = fxs[j * (nX + 1) + nX];
+                const double* ge = A.GE + plane(nbW, GE_COUNT, 0, A.nE);
+                corr = ge[GE_MXN1 * A.nE + j] < br || ge[GE_PXN * A.nE + j] < bl;
+            } else {
+                corr = (sm.dhi[0][liL] + s < 0.f) || (sm.dlo[0][liL] - s < 0.f);
+            }
+            L.hp = side_hp(sm.dlo[0][liL], sm.dhi[0][liL], s, true, corr);
+            L.p = sm.p[rL] + sp;
+            if (L.p < 0.f || (fi != 0 && sm.p[rL] - sp < 0.f)) L.p = sm.p[rL];
+            L.u = sm.u[rL] + sm.lx[2][liL] * hdx;
+            L.v = sm.v[rL] + sm.lx[3][liL] * hdx;
+            L.rho = sm.rho[rL] + sm.lx[4][liL] * hdx;
+            L.du = sm.lx[2][liL];
+            L.dv = sm.lx[3][liL];
+            // Right state: the lower-face reconstruction of cell fx.
+            s = sm.lx[0][liR] * hdx;
+            sp = sm.lx[1][liR] * hdx;
+            if (fi == nX && A.kind[nbE] == SLOT_GHOST) {
+                const double* fxs = FX + plane(nbE, 5, 4, SFX);
+                double bl = fxs[j * (nX + 1) + 0], br = fxs[j * (nX + 1) + 1];
+                const double* ge = A.GE + plane(nbE, GE_COUNT, 0, A.nE);
+                corr = ge[GE_MX2 * A.nE + j] < br || ge[GE_PX1 * A.nE + j] < bl;
+            } else {
+                corr = (sm.dhi[0][liR] + s < 0.f) || (sm.dlo[0][liR] - s < 0.f);
+            }
+            R.hp = side_hp(sm.dlo[0][liR], sm.dhi[0][liR], s, false, corr);
+            R.p = sm.p[rR] - sp;
+            if (R.p < 0.f || (fi != nX && sm.p[rR] + sp < 0.f)) R.p = sm.p[rR];
+            R.u = sm.u[rR] - sm.lx[2][liR] * hdx;
+            R.v = sm.v[rR] - sm.lx[3][liR] * hdx;
+            R.rho = sm.rho[rR] - sm.lx[4][liR] * hdx;
+            R.du = sm.lx[2][liR];
+            R.dv = sm.lx[3][liR];
+            int fo = j * (nX + 1) + fi;
+            face_flux32(F, true, R, L, TFXs[fo], TFXs[fo + SFX], sm.gam[rL], sm.gam[rR], F.dx, &sm.fx[0][cy * (BS + 1) + fx], NFX, cfl);
         } else {
-            corr = (sm.dhi[0][liL] + s < 0.f) || (sm.dlo[0][liL] - s < 0.f);
+            const int k = kk - ((bx + 1) * by);
+            int cx = k % bx, fy = k / bx;
+            int fj = bd.y0 + fy, i = bd.x0 + cx;
+            int rL = (fy + 1) * RG + (cx + 2), rR = rL + RG;
+            int liL = fy * BS + cx, liR = liL + BS;
+            Side32 L, R;
+            float s = sm.ly[0][liL] * hdy, sp = sm.ly[1][liL] * hdy;
+            bool corr;
+            if (fj == 0 && A.kind[nbS] == SLOT_GHOST) {
+                const double* fys = FY + plane(nbS, 5, 4, SFY);
+                double bb = fys[(nY - 1) * nX + i], bt_ = fys[nY * nX + i];
+                const double* ge = A.GE + plane(nbS, GE_COUNT, 0, A.nE);
+                corr = ge[GE_MYN1 * A.nE + i] < bt_ || ge[GE_PYN * A.nE + i] < bb;
+            } else {
+                corr = (sm.dhi[1][liL] + s < 0.f) || (sm.dlo[1][liL] - s < 0.f);
+            }
+            L.hp = side_hp(sm.dlo[1][liL], sm.dhi[1][liL], s, true, corr);
+            L.p = sm.p[rL] + sp;
+            if (L.p < 0.f || (fj != 0 && sm.p[rL] - sp < 0.f)) L.p = sm.p[rL];
+            L.u = sm.u[rL] + sm.ly[2][liL] * hdy;
+            L.v = sm.v[rL] + sm.ly[3][liL] * hdy;
+            L.rho = sm.rho[rL] + sm.ly[4][liL] * hdy;
+            L.du = sm.ly[2][liL];
+            L.dv = sm.ly[3][liL];
+            s = sm.ly[0][liR] * hdy;
+            sp = sm.ly[1][liR] * hdy;
+            if (fj == nY && A.kind[nbN] == SLOT_GHOST) {
+                const double* fys = FY + plane(nbN, 5, 4, SFY);
+                double bb = fys[0 * nX + i], bt_ = fys[1 * nX + i];
+                const double* ge = A.GE + plane(nbN, GE_COUNT, 0, A.nE);
+                corr = ge[GE_MY2 * A.nE + i] < bt_ || ge[GE_PY1 * A.nE + i] < bb;
+            } else {
+                corr = (sm.dhi[1][liR] + s < 0.f) || (sm.dlo[1][liR] - s < 0.f);
+            }
+            R.hp = side_hp(sm.dlo[1][liR], sm.dhi[1][liR], s, false, corr);
+            R.p = sm.p[rR] - sp;
+            if (R.p < 0.f || (fj != nY && sm.p[rR] + sp < 0.f)) R.p = sm.p[rR];
+            R.u = sm.u[rR] - sm.ly[2][liR] * hdy;
+            R.v = sm.v[rR] - sm.ly[3][liR] * hdy;
+            R.rho = sm.rho[rR] - sm.ly[4][liR] * hdy;
+            R.du = sm.ly[2][liR];
+            R.dv = sm.ly[3][liR];
+            int fo = fj * nX + i;
+            face_flux32(F, false, R, L, TFYs[fo], TFYs[fo + SFY], sm.gam[rL], sm.gam[rR], F.dy, &sm.fy[0][fy * BS + cx], NFX, cfl);
         }
-        L.hp = side_hp(sm.dlo[0][liL], sm.dhi[0][liL], s, true, corr);
-        L.p = sm.p[rL] + sp;
-        if (L.p < 0.f || (fi != 0 && sm.p[rL] - sp < 0.f)) L.p = sm.p[rL];
-        L.u = sm.u[rL] + sm.lx[2][liL] * hdx;
-        L.v = sm.v[rL] + sm.lx[3][liL] * hdx;
-        L.rho = sm.rho[rL] + sm.lx[4][liL] * hdx;
-        L.du = sm.lx[2][liL];
-        L.dv = sm.lx[3][liL];
-        // Right state: the lower-face reconstruction of cell fx.
-        s = sm.lx[0][liR] * hdx;
-        sp = sm.lx[1][liR] * hdx;
-        if (fi == nX && A.kind[nbE] == SLOT_GHOST) {
-            const double* fxs = FX + plane(nbE, 5, 4, SFX);
-            double bl = fxs[j * (nX + 1) + 0], br = fxs[j * (nX + 1) + 1];
-            const double* ge = A.GE + plane(nbE, GE_COUNT, 0, A.nE);
-            corr = ge[GE_MX2 * A.nE + j] < br || ge[GE_PX1 * A.nE + j] < bl;
-        } else {
-            corr = (sm.dhi[0][liR] + s < 0.f) || (sm.dlo[0][liR] - s < 0.f);
-        }
-        R.hp = side_hp(sm.dlo[0][liR], sm.dhi[0][liR], s, false, corr);
-        R.p = sm.p[rR] - sp;
-        if (R.p < 0.f || (fi != nX && sm.p[rR] + sp < 0.f)) R.p = sm.p[rR];
-        R.u = sm.u[rR] - sm.lx[2][liR] * hdx;
-        R.v = sm.v[rR] - sm.lx[3][liR] * hdx;
-        R.rho = sm.rho[rR] - sm.lx[4][liR] * hdx;
-        R.du = sm.lx[2][liR];
-        R.dv = sm.lx[3][liR];
-        int fo = j * (nX + 1) + fi;
-        face_flux32(F, true, R, L, TFXs[fo], TFXs[fo + SFX], sm.gam[rL], sm.gam[rR], F.dx, &sm.fx[0][cy * (BS + 1) + fx], NFX, cfl);
-    }
-    for (int k = tid; k < (by + 1) * bx; k += NT) {
-        int cx = k % bx, fy = k / bx;
-        int fj = bd.y0 + fy, i = bd.x0 + cx;
-        int rL = (fy + 1) * RG + (cx + 2), rR = rL + RG;
-        int liL = fy * BS + cx, liR = liL + BS;
-        Side32 L, R;
-        float s = sm.ly[0][liL] * hdy, sp = sm.ly[1][liL] * hdy;
-        bool corr;
-        if (fj == 0 && A.kind[nbS] == SLOT_GHOST) {
-            const double* fys = FY + plane(nbS, 5, 4, SFY);
-            double bb = fys[(nY - 1) * nX + i], bt_ = fys[nY * nX + i];
-            const double* ge = A.GE + plane(nbS, GE_COUNT, 0, A.nE);
-            corr = ge[GE_MYN1 * A.nE + i] < bt_ || ge[GE_PYN * A.nE + i] < bb;
-        } else {
-            corr = (sm.dhi[1][liL] + s < 0.f) || (sm.dlo[1][liL] - s < 0.f);
-        }
-        L.hp = side_hp(sm.dlo[1][liL], sm.dhi[1][liL], s, true, corr);
-        L.p = sm.p[rL] + sp;
-        if (L.p < 0.f || (fj != 0 && sm.p[rL] - sp < 0.f)) L.p = sm.p[rL];
-        L.u = sm.u[rL] + sm.ly[2][liL] * hdy;
-        L.v = sm.v[rL] + sm.ly[3][liL] * hdy;
-        L.rho = sm.rho[rL] + sm.ly[4][liL] * hdy;
-        L.du = sm.ly[2][liL];
-        L.dv = sm.ly[3][liL];
-        s = sm.ly[0][liR] * hdy;
-        sp = sm.ly[1][liR] * hdy;
-        if (fj == nY && A.kind[nbN] == SLOT_GHOST) {
-            const double* fys = FY + plane(nbN, 5, 4, SFY);
-            double bb = fys[0 * nX + i], bt_ = fys[1 * nX + i];
-            const double* ge = A.GE + plane(nbN, GE_COUNT, 0, A.nE);
-            corr = ge[GE_MY2 * A.nE + i] < bt_ || ge[GE_PY1 * A.nE + i] < bb;
-        } else {
-            corr = (sm.dhi[1][liR] + s < 0.f) || (sm.dlo[1][liR] - s < 0.f);
-        }
-        R.hp = side_hp(sm.dlo[1][liR], sm.dhi[1][liR], s, false, corr);
-        R.p = sm.p[rR] - sp;
-        if (R.p < 0.f || (fj != nY && sm.p[rR] + sp < 0.f)) R.p = sm.p[rR];
-        R.u = sm.u[rR] - sm.ly[2][liR] * hdy;
-        R.v = sm.v[rR] - sm.ly[3][liR] * hdy;
-        R.rho = sm.rho[rR] - sm.ly[4][liR] * hdy;
-        R.du = sm.ly[2][liR];
-        R.dv = sm.ly[3][liR];
-        int fo = fj * nX + i;
-        face_flux32(F, false, R, L, TFYs[fo], TFYs[fo + SFY], sm.gam[rL], sm.gam[rR], F.dy, &sm.fy[0][fy * BS + cx], NFX, cfl);
     }
     // CFL: warp then block min in FP32, the cross-CTA minimum on FP64 bits.
 #pragma unroll
