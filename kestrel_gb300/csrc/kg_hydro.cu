@@ -383,40 +383,43 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
 
     // ---- B: limited slopes ----
     const int lim = P.limiter;
-    for (int k = tid; k < (bx + 2) * by; k += NT) {
-        int cx = k % (bx + 2) - 1, cy = k / (bx + 2);
-        int r = (cy + 2) * RG + (cx + 2);
-        int li = cy * (BS + 2) + (cx + 1);
-        bool ghW = (cx < 0 && bd.x0 == 0 && A.kind[nbW] == SLOT_GHOST);
-        bool ghE = (cx >= bx && bd.x0 + bx == nX && A.kind[nbE] == SLOT_GHOST);
-        if (ghW || ghE) {
-            int gs = ghW ? nbW : nbE;
-            sm.lx[0][li] = A.GE[plane(gs, GE_COUNT, ghW ? GE_LXN : GE_LX1, A.nE) + bd.y0 + cy];
-            sm.lx[1][li] = 0.0; sm.lx[2][li] = 0.0; sm.lx[3][li] = 0.0; sm.lx[4][li] = 0.0;
+    for (int kk = tid; kk < (bx + 2) * by + (by + 2) * bx; kk += NT) {
+        if (kk < (bx + 2) * by) {
+            const int k = kk;
+            int cx = k % (bx + 2) - 1, cy = k / (bx + 2);
+            int r = (cy + 2) * RG + (cx + 2);
+            int li = cy * (BS + 2) + (cx + 1);
+            bool ghW = (cx < 0 && bd.x0 == 0 && A.kind[nbW] == SLOT_GHOST);
+            bool ghE = (cx >= bx && bd.x0 + bx == nX && A.kind[nbE] == SLOT_GHOST);
+            if (ghW || ghE) {
+                int gs = ghW ? nbW : nbE;
+                sm.lx[0][li] = A.GE[plane(gs, GE_COUNT, ghW ? GE_LXN : GE_LX1, A.nE) + bd.y0 + cy];
+                sm.lx[1][li] = 0.0; sm.lx[2][li] = 0.0; sm.lx[3][li] = 0.0; sm.lx[4][li] = 0.0;
+            } else {
+                sm.lx[0][li] = P.dxR * limiter(lim, sm.w[r + 1] - sm.w[r], sm.w[r] - sm.w[r - 1]);
+                sm.lx[1][li] = P.dxR * limiter(lim, sm.p[r + 1] - sm.p[r], sm.p[r] - sm.p[r - 1]);
+                sm.lx[2][li] = P.dxR * limiter(lim, sm.u[r + 1] - sm.u[r], sm.u[r] - sm.u[r - 1]);
+                sm.lx[3][li] = P.dxR * limiter(lim, sm.v[r + 1] - sm.v[r], sm.v[r] - sm.v[r - 1]);
+                sm.lx[4][li] = P.dxR * limiter(lim, sm.rho[r + 1] - sm.rho[r], sm.rho[r] - sm.rho[r - 1]);
+            }
         } else {
-            sm.lx[0][li] = P.dxR * limiter(lim, sm.w[r + 1] - sm.w[r], sm.w[r] - sm.w[r - 1]);
-            sm.lx[1][li] = P.dxR * limiter(lim, sm.p[r + 1] - sm.p[r], sm.p[r] - sm.p[r - 1]);
-            sm.lx[2][li] = P.dxR * limiter(lim, sm.u[r + 1] - sm.u[r], sm.u[r] - sm.u[r - 1]);
-            sm.lx[3][li] = P.dxR * limiter(lim, sm.v[r + 1] - sm.v[r], sm.v[r] - sm.v[r - 1]);
-            sm.lx[4][li] = P.dxR * limiter(lim, sm.rho[r + 1] - sm.rho[r], sm.rho[r] - sm.rho[r - 1]);
-        }
-    }
-    for (int k = tid; k < (by + 2) * bx; k += NT) {
-        int cx = k % bx, cy = k / bx - 1;
-        int r = (cy + 2) * RG + (cx + 2);
-        int li = (cy + 1) * BS + cx;
-        bool ghS = (cy < 0 && bd.y0 == 0 && A.kind[nbS] == SLOT_GHOST);
-        bool ghN = (cy >= by && bd.y0 + by == nY && A.kind[nbN] == SLOT_GHOST);
-        if (ghS || ghN) {
-            int gs = ghS ? nbS : nbN;
-            sm.ly[0][li] = A.GE[plane(gs, GE_COUNT, ghS ? GE_LYN : GE_LY1, A.nE) + bd.x0 + cx];
-            sm.ly[1][li] = 0.0; sm.ly[2][li] = 0.0; sm.ly[3][li] = 0.0; sm.ly[4][li] = 0.0;
-        } else {
-            sm.ly[0][li] = P.dyR * limiter(lim, sm.w[r + RG] - sm.w[r], sm.w[r] - sm.w[r - RG]);
-            sm.ly[1][li] = P.dyR * limiter(lim, sm.p[r + RG] - sm.p[r], sm.p[r] - sm.p[r - RG]);
-            sm.ly[2][li] = P.dyR * limiter(lim, sm.u[r + RG] - sm.u[r], sm.u[r] - sm.u[r - RG]);
-            sm.ly[3][li] = P.dyR * limiter(lim, sm.v[r + RG] - sm.v[r], sm.v[r] - sm.v[r - RG]);
-            sm.ly[4][li] = P.dyR * limiter(lim, sm.rho[r + RG] - sm.rho[r], sm.rho[r] - sm.rho[r - RG]);
+            const int k = kk - ((bx + 2) * by);
+            int cx = k % bx, cy = k / bx - 1;
+            int r = (cy + 2) * RG + (cx + 2);
+            int li = (cy + 1) * BS + cx;
+            bool ghS = (cy < 0 && bd.y0 == 0 && A.kind[nbS] == SLOT_GHOST);
+            bool ghN = (cy >= by && bd.y0 + by == nY && A.kind[nbN] == SLOT_GHOST);
+            if (ghS || ghN) {
+                int gs = ghS ? nbS : nbN;
+                sm.ly[0][li] = A.GE[plane(gs, GE_COUNT, ghS ? GE_LYN : GE_LY1, A.nE) + bd.x0 + cx];
+                sm.ly[1][li] = 0.0; sm.ly[2][li] = 0.0; sm.ly[3][li] = 0.0; sm.ly[4][li] = 0.0;
+            } else {
+                sm.ly[0][li] = P.dyR * limiter(lim, sm.w[r + RG] - sm.w[r], sm.w[r] - sm.w[r - RG]);
+                sm.ly[1][li] = P.dyR * limiter(lim, sm.p[r + RG] - sm.p[r], sm.p[r] - sm.p[r - RG]);
+                sm.ly[2][li] = P.dyR * limiter(lim, sm.u[r + RG] - sm.u[r], sm.u[r] - sm.u[r - RG]);
+                sm.ly[3][li] = P.dyR * limiter(lim, sm.v[r + RG] - sm.v[r], sm.v[r] - sm.v[r - RG]);
+                sm.ly[4][li] = P.dyR * limiter(lim, sm.rho[r + RG] - sm.rho[r], sm.rho[r] - sm.rho[r - RG]);
+            }
         }
     }
     __syncthreads();
@@ -424,143 +427,146 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
     // ---- C: face states, corrections, fluxes, CFL ----
     double cfl = 1.7976931348623157e308;
     const double hdx = 0.5, dx = P.dx, dy = P.dy;
-    for (int k = tid; k < (bx + 1) * by; k += NT) {
-        int fx = k % (bx + 1), cy = k / (bx + 1);
-        int fi = bd.x0 + fx, j = bd.y0 + cy;
-        int rL = (cy + 2) * RG + (fx + 1), rR = rL + 1;
-        int liL = cy * (BS + 2) + fx, liR = liL + 1;
-        Side L, R;
-        // Left state: the right-face reconstruction of cell fx-1.
-        double sw = sm.lx[0][liL], sp = sm.lx[1][liL];
-        L.w = sm.w[rL] + sw * hdx * dx;
-        L.p = sm.p[rL] + sp * hdx * dx;
-        L.u = sm.u[rL] + sm.lx[2][liL] * hdx * dx;
-        L.v = sm.v[rL] + sm.lx[3][liL] * hdx * dx;
-        L.rho = sm.rho[rL] + sm.lx[4][liL] * hdx * dx;
-        L.du = sm.lx[2][liL];
-        L.dv = sm.lx[3][liL];
-        if (fi == 0) {
-            const double* fxs = FX + plane(nbW, 5, 4, SFX);
-            double bl = fxs[j * (nX + 1) + nX - 1], br = fxs[j * (nX + 1) + nX];
-            if (A.kind[nbW] == SLOT_GHOST) {
-                const double* ge = A.GE + plane(nbW, GE_COUNT, 0, A.nE);
-                if (ge[GE_MXN1 * A.nE + j] < br || ge[GE_PXN * A.nE + j] < bl) L.w = sm.w[rL] + 0.5 * (br - bl);
+    for (int kk = tid; kk < (bx + 1) * by + (by + 1) * bx; kk += NT) {
+        if (kk < (bx + 1) * by) {
+            const int k = kk;
+            int fx = k % (bx + 1), cy = k / (bx + 1);
+            int fi = bd.x0 + fx, j = bd.y0 + cy;
+            int rL = (cy + 2) * RG + (fx + 1), rR = rL + 1;
+            int liL = cy * (BS + 2) + fx, liR = liL + 1;
+            Side L, R;
+            // Left state: the right-face reconstruction of cell fx-1.
+            double sw = sm.lx[0][liL], sp = sm.lx[1][liL];
+            L.w = sm.w[rL] + sw * hdx * dx;
+            L.p = sm.p[rL] + sp * hdx * dx;
+            L.u = sm.u[rL] + sm.lx[2][liL] * hdx * dx;
+            L.v = sm.v[rL] + sm.lx[3][liL] * hdx * dx;
+            L.rho = sm.rho[rL] + sm.lx[4][liL] * hdx * dx;
+            L.du = sm.lx[2][liL];
+            L.dv = sm.lx[3][liL];
+            if (fi == 0) {
+                const double* fxs = FX + plane(nbW, 5, 4, SFX);
+                double bl = fxs[j * (nX + 1) + nX - 1], br = fxs[j * (nX + 1) + nX];
+                if (A.kind[nbW] == SLOT_GHOST) {
+                    const double* ge = A.GE + plane(nbW, GE_COUNT, 0, A.nE);
+                    if (ge[GE_MXN1 * A.nE + j] < br || ge[GE_PXN * A.nE + j] < bl) L.w = sm.w[rL] + 0.5 * (br - bl);
+                } else {
+                    double wl = sm.w[rL] - sw * hdx * dx;
+                    if (L.w < br || wl < bl) L.w = sm.w[rL] + 0.5 * (br - bl);
+                }
+                if (L.p < 0.0) L.p = sm.p[rL];
             } else {
-                double wl = sm.w[rL] - sw * hdx * dx;
+                const double* fxs = FX + plane(slot, 5, 4, SFX);
+                double bl = fxs[j * (nX + 1) + fi - 1], br = fxs[j * (nX + 1) + fi];
+                double wl = sm.w[rL] - sw * hdx * dx, pl = sm.p[rL] - sp * hdx * dx;
                 if (L.w < br || wl < bl) L.w = sm.w[rL] + 0.5 * (br - bl);
+                if (L.p < 0.0 || pl < 0.0) L.p = sm.p[rL];
             }
-            if (L.p < 0.0) L.p = sm.p[rL];
-        } else {
-            const double* fxs = FX + plane(slot, 5, 4, SFX);
-            double bl = fxs[j * (nX + 1) + fi - 1], br = fxs[j * (nX + 1) + fi];
-            double wl = sm.w[rL] - sw * hdx * dx, pl = sm.p[rL] - sp * hdx * dx;
-            if (L.w < br || wl < bl) L.w = sm.w[rL] + 0.5 * (br - bl);
-            if (L.p < 0.0 || pl < 0.0) L.p = sm.p[rL];
-        }
-        // Right state: the left-face reconstruction of cell fx.
-        sw = sm.lx[0][liR];
-        sp = sm.lx[1][liR];
-        R.w = sm.w[rR] - sw * hdx * dx;
-        R.p = sm.p[rR] - sp * hdx * dx;
-        R.u = sm.u[rR] - sm.lx[2][liR] * hdx * dx;
-        R.v = sm.v[rR] - sm.lx[3][liR] * hdx * dx;
-        R.rho = sm.rho[rR] - sm.lx[4][liR] * hdx * dx;
-        R.du = sm.lx[2][liR];
-        R.dv = sm.lx[3][liR];
-        if (fi == nX) {
-            const double* fxs = FX + plane(nbE, 5, 4, SFX);
-            double bl = fxs[j * (nX + 1) + 0], br = fxs[j * (nX + 1) + 1];
-            if (A.kind[nbE] == SLOT_GHOST) {
-                const double* ge = A.GE + plane(nbE, GE_COUNT, 0, A.nE);
-                if (ge[GE_MX2 * A.nE + j] < br || ge[GE_PX1 * A.nE + j] < bl) R.w = sm.w[rR] + 0.5 * (bl - br);
+            // Right state: the left-face reconstruction of cell fx.
+            sw = sm.lx[0][liR];
+            sp = sm.lx[1][liR];
+            R.w = sm.w[rR] - sw * hdx * dx;
+            R.p = sm.p[rR] - sp * hdx * dx;
+            R.u = sm.u[rR] - sm.lx[2][liR] * hdx * dx;
+            R.v = sm.v[rR] - sm.lx[3][liR] * hdx * dx;
+            R.rho = sm.rho[rR] - sm.lx[4][liR] * hdx * dx;
+            R.du = sm.lx[2][liR];
+            R.dv = sm.lx[3][liR];
+            if (fi == nX) {
+                const double* fxs = FX + plane(nbE, 5, 4, SFX);
+                double bl = fxs[j * (nX + 1) + 0], br = fxs[j * (nX + 1) + 1];
+                if (A.kind[nbE] == SLOT_GHOST) {
+                    const double* ge = A.GE + plane(nbE, GE_COUNT, 0, A.nE);
+                    if (ge[GE_MX2 * A.nE + j] < br || ge[GE_PX1 * A.nE + j] < bl) R.w = sm.w[rR] + 0.5 * (bl - br);
+                } else {
+                    double wr = sm.w[rR] + sw * hdx * dx;
+                    if (wr < br || R.w < bl) R.w = sm.w[rR] + 0.5 * (bl - br);
+                }
+                if (R.p < 0.0) R.p = sm.p[rR];
             } else {
-                double wr = sm.w[rR] + sw * hdx * dx;
+                const double* fxs = FX + plane(slot, 5, 4, SFX);
+                double bl = fxs[j * (nX + 1) + fi], br = fxs[j * (nX + 1) + fi + 1];
+                double wr = sm.w[rR] + sw * hdx * dx, pr = sm.p[rR] + sp * hdx * dx;
                 if (wr < br || R.w < bl) R.w = sm.w[rR] + 0.5 * (bl - br);
+                if (pr < 0.0 || R.p < 0.0) R.p = sm.p[rR];
             }
-            if (R.p < 0.0) R.p = sm.p[rR];
+            size_t fo = (size_t)slot * 5 * SFX + (size_t)j * (nX + 1) + fi;
+            double b0f = FX[fo], btf = FX[fo + SFX], dbxf = FX[fo + 2 * (size_t)SFX], dbyf = FX[fo + 3 * (size_t)SFX];
+            double gamL = gam_of(P.geo, sm.bx[rL], sm.by[rL]), gamR = gam_of(P.geo, sm.bx[rR], sm.by[rR]);
+            double out[7];
+            face_flux(P, true, R, L, b0f, btf, dbxf, dbyf, gamL, gamR, dx, out, cfl);
+            int fo2 = cy * (BS + 1) + fx;
+    #pragma unroll
+            for (int q = 0; q < 7; ++q) sm.fx[q][fo2] = out[q];
         } else {
-            const double* fxs = FX + plane(slot, 5, 4, SFX);
-            double bl = fxs[j * (nX + 1) + fi], br = fxs[j * (nX + 1) + fi + 1];
-            double wr = sm.w[rR] + sw * hdx * dx, pr = sm.p[rR] + sp * hdx * dx;
-            if (wr < br || R.w < bl) R.w = sm.w[rR] + 0.5 * (bl - br);
-            if (pr < 0.0 || R.p < 0.0) R.p = sm.p[rR];
-        }
-        size_t fo = (size_t)slot * 5 * SFX + (size_t)j * (nX + 1) + fi;
-        double b0f = FX[fo], btf = FX[fo + SFX], dbxf = FX[fo + 2 * (size_t)SFX], dbyf = FX[fo + 3 * (size_t)SFX];
-        double gamL = gam_of(P.geo, sm.bx[rL], sm.by[rL]), gamR = gam_of(P.geo, sm.bx[rR], sm.by[rR]);
-        double out[7];
-        face_flux(P, true, R, L, b0f, btf, dbxf, dbyf, gamL, gamR, dx, out, cfl);
-        int fo2 = cy * (BS + 1) + fx;
-#pragma unroll
-        for (int q = 0; q < 7; ++q) sm.fx[q][fo2] = out[q];
-    }
-    for (int k = tid; k < (by + 1) * bx; k += NT) {
-        int cx = k % bx, fy = k / bx;
-        int fj = bd.y0 + fy, i = bd.x0 + cx;
-        int rL = (fy + 1) * RG + (cx + 2), rR = rL + RG;
-        int liL = fy * BS + cx, liR = liL + BS;
-        Side L, R;
-        double sw = sm.ly[0][liL], sp = sm.ly[1][liL];
-        L.w = sm.w[rL] + sw * hdx * dy;
-        L.p = sm.p[rL] + sp * hdx * dy;
-        L.u = sm.u[rL] + sm.ly[2][liL] * hdx * dy;
-        L.v = sm.v[rL] + sm.ly[3][liL] * hdx * dy;
-        L.rho = sm.rho[rL] + sm.ly[4][liL] * hdx * dy;
-        L.du = sm.ly[2][liL];
-        L.dv = sm.ly[3][liL];
-        if (fj == 0) {
-            const double* fys = FY + plane(nbS, 5, 4, SFY);
-            double bb = fys[(nY - 1) * nX + i], bt_ = fys[nY * nX + i];
-            if (A.kind[nbS] == SLOT_GHOST) {
-                const double* ge = A.GE + plane(nbS, GE_COUNT, 0, A.nE);
-                if (ge[GE_MYN1 * A.nE + i] < bt_ || ge[GE_PYN * A.nE + i] < bb) L.w = sm.w[rL] + 0.5 * (bt_ - bb);
+            const int k = kk - ((bx + 1) * by);
+            int cx = k % bx, fy = k / bx;
+            int fj = bd.y0 + fy, i = bd.x0 + cx;
+            int rL = (fy + 1) * RG + (cx + 2), rR = rL + RG;
+            int liL = fy * BS + cx, liR = liL + BS;
+            Side L, R;
+            double sw = sm.ly[0][liL], sp = sm.ly[1][liL];
+            L.w = sm.w[rL] + sw * hdx * dy;
+            L.p = sm.p[rL] + sp * hdx * dy;
+            L.u = sm.u[rL] + sm.ly[2][liL] * hdx * dy;
+            L.v = sm.v[rL] + sm.ly[3][liL] * hdx * dy;
+            L.rho = sm.rho[rL] + sm.ly[4][liL] * hdx * dy;
+            L.du = sm.ly[2][liL];
+            L.dv = sm.ly[3][liL];
+            if (fj == 0) {
+                const double* fys = FY + plane(nbS, 5, 4, SFY);
+                double bb = fys[(nY - 1) * nX + i], bt_ = fys[nY * nX + i];
+                if (A.kind[nbS] == SLOT_GHOST) {
+                    const double* ge = A.GE + plane(nbS, GE_COUNT, 0, A.nE);
+                    if (ge[GE_MYN1 * A.nE + i] < bt_ || ge[GE_PYN * A.nE + i] < bb) L.w = sm.w[rL] + 0.5 * (bt_ - bb);
+                } else {
+                    double wb = sm.w[rL] - sw * hdx * dy;
+                    if (L.w < bt_ || wb < bb) L.w = sm.w[rL] + 0.5 * (bt_ - bb);
+                }
+                if (L.p < 0.0) L.p = sm.p[rL];
             } else {
-                double wb = sm.w[rL] - sw * hdx * dy;
+                const double* fys = FY + plane(slot, 5, 4, SFY);
+                double bb = fys[(fj - 1) * nX + i], bt_ = fys[fj * nX + i];
+                double wb = sm.w[rL] - sw * hdx * dy, pb = sm.p[rL] - sp * hdx * dy;
                 if (L.w < bt_ || wb < bb) L.w = sm.w[rL] + 0.5 * (bt_ - bb);
+                if (L.p < 0.0 || pb < 0.0) L.p = sm.p[rL];
             }
-            if (L.p < 0.0) L.p = sm.p[rL];
-        } else {
-            const double* fys = FY + plane(slot, 5, 4, SFY);
-            double bb = fys[(fj - 1) * nX + i], bt_ = fys[fj * nX + i];
-            double wb = sm.w[rL] - sw * hdx * dy, pb = sm.p[rL] - sp * hdx * dy;
-            if (L.w < bt_ || wb < bb) L.w = sm.w[rL] + 0.5 * (bt_ - bb);
-            if (L.p < 0.0 || pb < 0.0) L.p = sm.p[rL];
-        }
-        sw = sm.ly[0][liR];
-        sp = sm.ly[1][liR];
-        R.w = sm.w[rR] - sw * hdx * dy;
-        R.p = sm.p[rR] - sp * hdx * dy;
-        R.u = sm.u[rR] - sm.ly[2][liR] * hdx * dy;
-        R.v = sm.v[rR] - sm.ly[3][liR] * hdx * dy;
-        R.rho = sm.rho[rR] - sm.ly[4][liR] * hdx * dy;
-        R.du = sm.ly[2][liR];
-        R.dv = sm.ly[3][liR];
-        if (fj == nY) {
-            const double* fys = FY + plane(nbN, 5, 4, SFY);
-            double bb = fys[0 * nX + i], bt_ = fys[1 * nX + i];
-            if (A.kind[nbN] == SLOT_GHOST) {
-                const double* ge = A.GE + plane(nbN, GE_COUNT, 0, A.nE);
-                if (ge[GE_MY2 * A.nE + i] < bt_ || ge[GE_PY1 * A.nE + i] < bb) R.w = sm.w[rR] + 0.5 * (bb - bt_);
+            sw = sm.ly[0][liR];
+            sp = sm.ly[1][liR];
+            R.w = sm.w[rR] - sw * hdx * dy;
+            R.p = sm.p[rR] - sp * hdx * dy;
+            R.u = sm.u[rR] - sm.ly[2][liR] * hdx * dy;
+            R.v = sm.v[rR] - sm.ly[3][liR] * hdx * dy;
+            R.rho = sm.rho[rR] - sm.ly[4][liR] * hdx * dy;
+            R.du = sm.ly[2][liR];
+            R.dv = sm.ly[3][liR];
+            if (fj == nY) {
+                const double* fys = FY + plane(nbN, 5, 4, SFY);
+                double bb = fys[0 * nX + i], bt_ = fys[1 * nX + i];
+                if (A.kind[nbN] == SLOT_GHOST) {
+                    const double* ge = A.GE + plane(nbN, GE_COUNT, 0, A.nE);
+                    if (ge[GE_MY2 * A.nE + i] < bt_ || ge[GE_PY1 * A.nE + i] < bb) R.w = sm.w[rR] + 0.5 * (bb - bt_);
+                } else {
+                    double wt = sm.w[rR] + sw * hdx * dy;
+                    if (wt < bt_ || R.w < bb) R.w = sm.w[rR] + 0.5 * (bb - bt_);
+                }
+                if (R.p < 0.0) R.p = sm.p[rR];
             } else {
-                double wt = sm.w[rR] + sw * hdx * dy;
+                const double* fys = FY + plane(slot, 5, 4, SFY);
+                double bb = fys[fj * nX + i], bt_ = fys[(fj + 1) * nX + i];
+                double wt = sm.w[rR] + sw * hdx * dy, pt = sm.p[rR] + sp * hdx * dy;
                 if (wt < bt_ || R.w < bb) R.w = sm.w[rR] + 0.5 * (bb - bt_);
+                if (pt < 0.0 || R.p < 0.0) R.p = sm.p[rR];
             }
-            if (R.p < 0.0) R.p = sm.p[rR];
-        } else {
-            const double* fys = FY + plane(slot, 5, 4, SFY);
-            double bb = fys[fj * nX + i], bt_ = fys[(fj + 1) * nX + i];
-            double wt = sm.w[rR] + sw * hdx * dy, pt = sm.p[rR] + sp * hdx * dy;
-            if (wt < bt_ || R.w < bb) R.w = sm.w[rR] + 0.5 * (bb - bt_);
-            if (pt < 0.0 || R.p < 0.0) R.p = sm.p[rR];
+            size_t fo = (size_t)slot * 5 * SFY + (size_t)fj * nX + i;
+            double b0f = FY[fo], btf = FY[fo + SFY], dbxf = FY[fo + 2 * (size_t)SFY], dbyf = FY[fo + 3 * (size_t)SFY];
+            double gamL = gam_of(P.geo, sm.bx[rL], sm.by[rL]), gamR = gam_of(P.geo, sm.bx[rR], sm.by[rR]);
+            double out[7];
+            face_flux(P, false, R, L, b0f, btf, dbxf, dbyf, gamL, gamR, dy, out, cfl);
+            int fo2 = fy * BS + cx;
+    #pragma unroll
+            for (int q = 0; q < 7; ++q) sm.fy[q][fo2] = out[q];
         }
-        size_t fo = (size_t)slot * 5 * SFY + (size_t)fj * nX + i;
-        double b0f = FY[fo], btf = FY[fo + SFY], dbxf = FY[fo + 2 * (size_t)SFY], dbyf = FY[fo + 3 * (size_t)SFY];
-        double gamL = gam_of(P.geo, sm.bx[rL], sm.by[rL]), gamR = gam_of(P.geo, sm.bx[rR], sm.by[rR]);
-        double out[7];
-        face_flux(P, false, R, L, b0f, btf, dbxf, dbyf, gamL, gamR, dy, out, cfl);
-        int fo2 = fy * BS + cx;
-#pragma unroll
-        for (int q = 0; q < 7; ++q) sm.fy[q][fo2] = out[q];
     }
     // CFL: warp then block min, one atomic per CTA (ordered bits of a positive double).
 #pragma unroll
