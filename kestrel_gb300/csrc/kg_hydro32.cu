@@ -45,6 +45,24 @@ __device__ __forceinline__ void desing32(const DevParams32& P, float hp, float g
     v = k * m2;
 }
 
+// (a - b) + (c - d) of four FP32 fluxes in FP64 with two conversions instead of four: the
+// two differences and their sum are split error-free on the FP32 pipe (Knuth's TwoSum),
+// the leading part and the summed error parts are converted and added.  The result is the
+// exact sum to about 2^-47 relative (the FP32 rounding of the error sum), so the w and
+// Hnpsi rows still telescope to FP64 round-off, and it is exactly 0 when the four fluxes
+// cancel in pairs (a lake at rest).
+__device__ __forceinline__ double flux_sum4(float a, float b, float c, float d) {
+    float s1 = a - b, t = s1 - a, e1 = (a - (s1 - t)) + (-b - t);
+    float s2 = c - d;
+    t = s2 - c;
+    float e2 = (c - (s2 - t)) + (-d - t);
+    float S = s1 + s2;
+    t = S - s1;
+    float e3 = (s1 - (S - t)) + (s2 - t);
+    float E = (e1 + e2) + e3;
+    return (double)S + (double)E;
+}
+
 struct Side32 {
     float hp, p, u, v, rho, du, dv;  // hp: face free surface minus InterpolateB at the face
 };
@@ -366,8 +384,15 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
         int xl = cy * (BS + 1) + cx, xr = xl + 1;
         int yb = cy * BS + cx, yt = yb + BS;
         // w and Hnpsi rows in FP64 (the flux differences of FP32 values are exact or nearly so)
-        double E0 = (((double)sm.fx[0][xl] - (double)sm.fx[0][xr]) * P.dxR + ((double)sm.fy[0][yb] - (double)sm.fy[0][yt]) * P.dyR) * ig2;
-        double E3 = (((double)sm.fx[3][xl] - (double)sm.fx[3][xr]) * P.dxR + ((double)sm.fy[3][yb] - (double)sm.fy[3][yt]) * P.dyR) * ig;
+        double E0, E3;
+        if (P.dx == P.dy) {
+            // square cells: the four-flux sum once, from an error-free FP32 split
+            E0 = flux_sum4(sm.fx[0][xl], sm.fx[0][xr], sm.fy[0][yb], sm.fy[0][yt]) * P.dxR * ig2;
+            E3 = flux_sum4(sm.fx[3][xl], sm.fx[3][xr], sm.fy[3][yb], sm.fy[3][yt]) * P.dxR * ig;
+        } else {
+            E0 = (((double)sm.fx[0][xl] - (double)sm.fx[0][xr]) * P.dxR + ((double)sm.fy[0][yb] - (double)sm.fy[0][yt]) * P.dyR) * ig2;
+            E3 = (((double)sm.fx[3][xl] - (double)sm.fx[3][xr]) * P.dxR + ((double)sm.fy[3][yb] - (double)sm.fy[3][yt]) * P.dyR) * ig;
+        }
         float E1 = kahan3<float>(sm.fx[1][xl] - sm.fx[1][xr], (sm.fx[4][xl] - sm.fx[4][xr]) * gXp1, sm.fx[5][xr] - sm.fx[5][xl]) * dxR +
                    kahan3<float>(sm.fy[1][yb] - sm.fy[1][yt], (sm.fy[4][yb] - sm.fy[4][yt]) * gYp1, sm.fy[5][yt] - sm.fy[5][yb]) * dyR;
         float E2 = kahan3<float>(sm.fx[2][xl] - sm.fx[2][xr], (sm.fx[4][xl] - sm.fx[4][xr]) * gXp2, sm.fx[6][xr] - sm.fx[6][xl]) * dxR +

@@ -392,6 +392,16 @@ __device__ __forceinline__ void m_check(const DevParams& P, const DevArrays& A, 
     int SC = P.nX * P.nY;
     if (item_ < SC) {
         int c = item_;
+        if (PLAIN) {
+            // A cell whose bed, slopes and free surface M left as they were has no excess
+            // (its bed change is 0) and no depth change: neither test can fire.
+            const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
+            if (same_bits(C3[mp(s, 4, 1, SC) + c], C0[mp(s, 4, 1, SC) + c]) &&
+                same_bits(C3[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 2, SC) + c]) &&
+                same_bits(C3[mp(s, 4, 3, SC) + c], C0[mp(s, 4, 3, SC) + c]) &&
+                same_bits(A.MS[mp(s, 5, 0, SC) + c], A.Q[qa][mp(s, 4, 0, SC) + c]))
+                return;
+        }
         double ex, dBt, psiold, Hn_old, Hn_new;
         excess_deposition<PLAIN>(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Hn_old, Hn_new);
         bool refine = false;
