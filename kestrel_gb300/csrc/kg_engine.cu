@@ -215,7 +215,7 @@ void bind_constants(kg_ctx& c);
 size_t bytes_per_slot(const kg_ctx& c) {
     size_t SC = c.SC;
     return sizeof(double) * (4 * 4 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * (size_t)c.SFX + 5 * (size_t)c.SFY + 2 * (size_t)c.SV) +
-                             2 * SC + 5 * SC + SC + 9 * SC + GE_COUNT * (size_t)c.nE + 11 * SC + 2 * SC) +
+                             2 * SC + 5 * SC + SC + 2 * SC + 9 * SC + GE_COUNT * (size_t)c.nE + 11 * SC + 2 * SC) +
            8 * sizeof(int) + 2 + sizeof(int) +
            (c.prec == KG_PREC_FP32 ? 2 * (3 * sizeof(double) * SC + 6 * sizeof(float) * SC +
                                           2 * sizeof(float) * ((size_t)c.SFX + (size_t)c.SFY))

@@ -13,6 +13,7 @@
 //                                             edge vertices, as the reference does)
 //   ghost data     G9[slot][9][nY][nX]        static u(1:9) of a ghost tile
 //                  GE[slot][12][nE]           its stale w reconstructions at the edges
+//   static slopes  B0S[slot][2][nY][nX]       b0 parts of the cell slopes (FP32-form M stages)
 //   maxima         MX[slot][11][nY][nX]       Hnmax, umax, emax, dmax, psimax (value, time)
 //                                             and tfirst (src/Grid.f90:95-102)
 // FP32 form only (static per topography set, rebuilt when the set changes):
