@@ -453,6 +453,9 @@ __device__ __forceinline__ void set_bt(const DevArrays& A, int tnew, int s, int 
 // RedistributeCell, src/Redistribute.f90:249-475, up to the corrected vertices (:249-399);
 // the cells are updated by redist_cell.  Returns false when the cell borders no
 // depositional vertex.
+// PLAIN (the FP32 form) takes gamma from the factor cache, sums without compensation and
+// multiplies by 1 / (1 - porosity): a shorter FP64 chain for the serial walk.
+template <bool PLAIN>
 __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int s, int i, int j,
                                   double corr) {
     int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
@@ -476,25 +479,27 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
     double delta = 4.0 * corr / sum;
     const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
     size_t c = (size_t)j * nX + i;
-    double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+    double gamold = PLAIN ? gam_cached(P, A, tcur, s, c, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c])
+                          : gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
     double w0 = A.Q[qa][mp(s, 4, 0, SC) + c];
     double Hnold = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
     if (Hnold < 0.0) Hnold = 0.0;
     double db = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
     double tol = kEPS * A.MS[mp(s, 5, 0, SC) + c] * 10.0;
     double adjustment = 0.0;
-    double disc = kahan3(Hnold * gamold, -db, corr);
+    double disc = PLAIN ? (Hnold * gamold - db) + corr : kahan3(Hnold * gamold, -db, corr);
     if (fabs(disc) < tol) {
-        adjustment = kahan3(tol, -Hnold * gamold, db);
+        adjustment = PLAIN ? (tol - Hnold * gamold) + db : kahan3(tol, -Hnold * gamold, db);
         adjustment = adjustment * (4.0 / sum);
         adjustment = adjustment - delta;
         adjustment = mx(adjustment, 0.0);
     }
-    double Hgp = A.Q[qa][mp(s, 4, 3, SC) + c] * gamold / (1.0 - P.BedPorosity);
+    double Hgp = PLAIN ? A.Q[qa][mp(s, 4, 3, SC) + c] * gamold * P.invSolid
+                       : A.Q[qa][mp(s, 4, 3, SC) + c] * gamold / (1.0 - P.BedPorosity);
     tol = kEPS * 10.0;
-    disc = kahan3(Hgp, -db, corr);
+    disc = PLAIN ? (Hgp - db) + corr : kahan3(Hgp, -db, corr);
     if (fabs(disc) < tol) {
-        double ap = kahan3(tol, -Hgp, db);
+        double ap = PLAIN ? (tol - Hgp) + db : kahan3(tol, -Hgp, db);
         ap = ap * (4.0 / sum);
         ap = ap - delta;
         adjustment = mx(adjustment, ap);
@@ -571,10 +576,34 @@ __device__ __forceinline__ void redist_cell_load(const DevParams& P, const DevAr
     r.w0 = A.Q[qa][mp(ct, 4, 0, SC) + cc];
     r.p0 = A.Q[qa][mp(ct, 4, 3, SC) + cc];
 }
-__device__ __forceinline__ void redist_cell_apply(const DevParams& P, const DevArrays& A, int tnew, const RedistCell& r) {
+template <bool PLAIN>
+__device__ __forceinline__ void redist_cell_apply(const DevParams& P, const DevArrays& A, int tcur, int tnew, const RedistCell& r) {
     if (!r.on) return;
     int SC = P.nX * P.nY;
     size_t cc = (size_t)r.cj * P.nX + r.ci;
+    if (PLAIN) {
+        // the FP32 form's cell bed (as m_cells: static b0 parts from the cache, bt terms
+        // summed plainly) and its w / Hnpsi update with 1/gamma from an FP32-seeded Newton step
+        int nX = P.nX, SV = (nX + 1) * (P.nY + 1);
+        const double* bt = A.BV[tnew] + mp(r.ct, 2, 1, SV);
+        int v00 = r.cj * (nX + 1) + r.ci, v10 = v00 + 1, v01 = v00 + (nX + 1), v11 = v01 + 1;
+        const double* B = A.B0S + mp(r.ct, 2, 0, SC) + cc;
+        double btc = 0.25 * ((bt[v00] + bt[v10]) + (bt[v01] + bt[v11]));
+        double dbx = B[0] + P.hdxR * ((bt[v10] - bt[v00]) + (bt[v11] - bt[v01]));
+        double dby = B[(size_t)SC] + P.hdyR * ((bt[v01] - bt[v00]) + (bt[v11] - bt[v10]));
+        A.CT[tnew][mp(r.ct, 4, 1, SC) + cc] = btc;
+        A.CT[tnew][mp(r.ct, 4, 2, SC) + cc] = dbx;
+        A.CT[tnew][mp(r.ct, 4, 3, SC) + cc] = dby;
+        double dbc = btc - r.bt0;
+        double go = gam_cached(P, A, tcur, r.ct, (int)cc, r.bx0, r.by0);
+        double ign = 1.0;
+        if (P.geo) ign = rsqrt_nr(1.0 + (dbx * dbx + dby * dby));
+        double Hno = compute_hn(r.w0, r.b00, r.bt0, go);
+        if (Hno < 0.0) Hno = 0.0;
+        A.MS[mp(r.ct, 5, 0, SC) + cc] = (r.b0n + btc) + (Hno * go - dbc) * (ign * ign);
+        A.MS[mp(r.ct, 5, 1, SC) + cc] = (r.p0 * go - (1.0 - P.BedPorosity) * dbc) * ign;
+        return;
+    }
     double c3[3];
     cell_topo_ij(P, A, tnew, r.ct, r.ci, r.cj, c3);
     double dbc = c3[0] - r.bt0;
@@ -588,11 +617,12 @@ __device__ __forceinline__ void redist_cell_apply(const DevParams& P, const DevA
     A.MS[mp(r.ct, 5, 0, SC) + cc] = w;
     A.MS[mp(r.ct, 5, 1, SC) + cc] = r.p0 * go / gn - (1.0 - P.BedPorosity) * dbc / gn;
 }
+template <bool PLAIN>
 __device__ __forceinline__ void redist_cell(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int ct, int ci,
                                             int cj) {
     RedistCell r;
     redist_cell_load(P, A, qa, tcur, tnew, ct, ci, cj, r);
-    redist_cell_apply(P, A, tnew, r);
+    redist_cell_apply<PLAIN>(P, A, tcur, tnew, r);
 }
 
 // RedistributeGrid (src/Redistribute.f90:203-244) over the ordered candidate list, run as
@@ -624,7 +654,7 @@ __device__ __forceinline__ void m_redist(const DevParams& P, const DevArrays& A,
                 double ex, dBt, psiold, Ho, Hn;
                 excess_deposition<PLAIN>(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
                 if (ex > kEPS) {
-                    if (redistribute_cell(P, A, qa, tcur, tnew, s, i, j, ex)) go = 1;
+                    if (redistribute_cell<PLAIN>(P, A, qa, tcur, tnew, s, i, j, ex)) go = 1;
                     else failed = 1;
                 }
             }
@@ -633,7 +663,7 @@ __device__ __forceinline__ void m_redist(const DevParams& P, const DevArrays& A,
             if (go) {
                 int vt[9], vi[9], vj[9];
                 redist_cells_of(P, A, s, i, j, vt, vi, vj);
-                if (lane < 9) redist_cell(P, A, qa, tcur, tnew, vt[lane], vi[lane], vj[lane]);
+                if (lane < 9) redist_cell<PLAIN>(P, A, qa, tcur, tnew, vt[lane], vi[lane], vj[lane]);
             }
             __syncwarp();
         }
@@ -741,13 +771,13 @@ __global__ void __launch_bounds__(32) k_m_redist_wave(DevArrays A, const int* __
         double ex, dBt, psiold, Ho, Hn;
         excess_deposition<PLAIN>(cP, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Ho, Hn);
         if (ex > kEPS) {
-            if (redistribute_cell(cP, A, qa, tcur, tnew, s, i, j, ex)) go = 1;
+            if (redistribute_cell<PLAIN>(cP, A, qa, tcur, tnew, s, i, j, ex)) go = 1;
             else atomicOr(flags, 1);
         }
     }
     go = __shfl_sync(0xffffffffu, go, 0);
     __syncwarp();  // lane 0's vertex writes are visible to the other lanes after this
-    if (go) redist_cell_apply(cP, A, tnew, r);
+    if (go) redist_cell_apply<PLAIN>(cP, A, tcur, tnew, r);
 }
 
 template <bool PLAIN>
