@@ -583,7 +583,10 @@ def main():
                             "final read-back"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": kname, "pass_ms": pass_ms},
+                     "kernel": kname, "pass_ms": pass_ms,
+                     "note": "algorithmic bytes of the form over the measured pass time; the pass is bound by the FP64 "
+                             "pipe (2 lanes per SM per clock on GB300), not HBM: see profiles/" + kname + "_" +
+                             args.workload + ".md"},
         "gpu_launches": launches,
         "clocks": clk,
     }
