@@ -585,8 +585,8 @@ def main():
                      "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": kname, "pass_ms": pass_ms,
                      "note": "algorithmic bytes of the form over the measured pass time; the pass is bound by the FP64 "
-                             "pipe (2 lanes per SM per clock on GB300), not HBM: see profiles/" + kname + "_" +
-                             args.workload + ".md"},
+                             "pipe (2 lanes per SM per clock on GB300), not HBM: see profiles/" + kname +
+                             ("_morpho_flux_2048_fp64.md" if wl["prec"] == abi.PREC_FP64 else "_morpho_flux_2048_fp32.md")},
         "gpu_launches": launches,
         "clocks": clk,
     }
