@@ -61,7 +61,6 @@ cudaError_t launch_m_check(const DevArrays& A, const int* d_slots, int n, int ce
                            unsigned long long* keys, double* ex, int* ncand, int cap, bool fp32, cudaStream_t st);
 cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, const int* woff, const int* hwoff, int nwaves,
                             int qa, int tcur, int tnew, int* flags, bool fp32, cudaStream_t st);
-cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st);
 cudaError_t launch_m_close(const DevArrays& A, const int* d_slots, int n, int nX, int nY, int qa, int tnew, bool fp32,
                            cudaStream_t st);
 }  // namespace kg

@@ -13,10 +13,12 @@
 //               the w / Hnpsi update (src/TimeStepper.f90:584-609) and the depth, solids
 //               fraction and density of the stage (ComputeDesingularisedVariables without
 //               velocities: u and v stay those the first hydraulic step left)
-// then k_m_check evaluates the excess-deposition and 10 % depth-change tests (:709-753)
-// and k_m_redist runs RedistributeGrid's ordered correction (src/Redistribute.f90) in
-// dependency waves, one warp per listed cell.  Topography lives in two sets: the step-start bed (read-only here) and
-// the bed M builds, so a refined attempt restarts from the step-start set.
+// then k_m_check evaluates the excess-deposition and 10 % depth-change tests (:709-753),
+// k_m_redist_wave runs RedistributeGrid's ordered correction (src/Redistribute.f90) one
+// dependency wave per launch, one warp per listed cell, and k_m_close ends the attempt
+// (interfacial topography, M result, the FP32 form's factor cache).  Topography lives in
+// two sets: the step-start bed (read-only here) and the bed M builds, so a refined attempt
+// restarts from the step-start set.  The PLAIN / float instantiations are the FP32 form's.
 #include <cuda_runtime.h>
 #include "kg_engine.cuh"
 
@@ -792,10 +794,6 @@ __global__ void __launch_bounds__(256) k_m_close(DevArrays A, const int* __restr
     kg_dep_wait();
     m_close<PLAIN>(cP, A, slots[blockIdx.x / per], (blockIdx.x % per) * 256 + threadIdx.x, qa, tnew);
 }
-__global__ void __launch_bounds__(256) k_m_finish(DevArrays A, const int* __restrict__ slots, int qa) {
-    KG_TILE_ITEMS(cP.nX * cP.nY)
-    m_finish(cP, A, s, item_, qa);
-}
 
 // ---- host launchers (cells/verts: items per tile) ----
 static inline int per_of(int items) { return (items + 255) / 256; }
@@ -852,11 +850,6 @@ cudaError_t launch_m_redist(const DevArrays& A, const int* ls, const int* lc, co
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
-}
-cudaError_t launch_m_finish(const DevArrays& A, const int* d_slots, int n, int cells, int qa, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
-    k_m_finish<<<n * per_of(cells), 256, 0, st>>>(A, d_slots, qa);
-    return cudaGetLastError();
 }
 // The end of an M attempt in one launch: the interfacial topography of the new bed
 // (face_topo, face_bI), the M result into state qa (m_finish) and, in the FP32 form, the
