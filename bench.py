@@ -50,8 +50,9 @@ def measured_peaks():
 
 def profile_traffic(kernel: str, workload: str, cells: float):
     """DRAM bytes per pass, scaled to `cells` active cells from the bytes per cell and pass
-    of a committed ncu capture (profiles/<kernel>_<workload>.md): the capture runs a
-    smaller active set of the same workload and traffic grows with the cells processed."""
+    recorded in the committed ncu summary of this kernel and workload under profiles/
+    (the `dram_bytes_per_cell_pass:` line): the capture may run a smaller active set of the
+    same workload, and traffic grows with the cells processed."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
         return None
@@ -162,7 +163,7 @@ def run_reference(args, wl):
 
 
 def run_ensemble(args):
-    """configs[3]-style batched ensemble: N members (grid sides log-uniform in [128, 1024]
+    """The batched ensemble: N members (grid sides log-uniform in [128, 1024]
     at dx = 5 m, own fractal terrain, cap or flux source of 1e3-1e6 m^3, Chezy / Voellmy /
     Manning drag, morphodynamics on for half), tile sides from the autotuner, all advanced
     together; value = member cell-updates per second of device time over the timed batch
@@ -234,7 +235,7 @@ def run_ensemble(args):
 
 
 def run_serve(args):
-    """configs[4]-style served stream: requests arrive as a Poisson process (--rate per s),
+    """The served stream: requests arrive as a Poisson process (--rate per s),
     grid sides uniform over {256, 512, 1024, 2048}, end times uniform over
     [--tend-min, --tend-max] s, admitted by the HBM budget into one continuously batched
     engine; reports p50/p99 latency, solves/s and cell-updates/s (host clock)."""
@@ -585,8 +586,8 @@ def main():
                      "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": kname, "pass_ms": pass_ms,
                      "note": "algorithmic bytes of the form over the measured pass time; the pass is bound by the FP64 "
-                             "pipe (2 lanes per SM per clock on GB300), not HBM: see profiles/" + kname +
-                             ("_morpho_flux_2048_fp64.md" if wl["prec"] == abi.PREC_FP64 else "_morpho_flux_2048_fp32.md")},
+                             "pipe (2 lanes per SM per clock on GB300), not HBM, per the committed ncu capture of "
+                             + kname + " on the 2048^2 morphodynamic workload"},
         "gpu_launches": launches,
         "clocks": clk,
     }

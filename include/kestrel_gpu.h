@@ -6,8 +6,8 @@
  * (src/TimeStepper.f90:73) and `main` (src/main.f90:171).  This header is the drop-in
  * boundary a Fortran host binds with ISO_C_BINDING, in the same way the reference already
  * binds its C++ glue (src/GeoTiffRead.f90:43-100 <-> src/RasterData.h:181-,
- * src/version.f90:25-33 <-> src/cversion.cpp:28-34).  The binding a maintainer adds is
- * shown in INTEGRATION.md.
+ * src/version.f90:25-33 <-> src/cversion.cpp:28-34): one interface block per entry point,
+ * bind(C, name="kg_...") with value arguments for scalars and handles.
  *
  * Conventions
  *  - Every entry point returns an int status: 0 (KG_OK) or a negative KG_ERR_* code.  The

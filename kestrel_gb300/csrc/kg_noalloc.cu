@@ -1,7 +1,7 @@
 // kg_noalloc.cu -- kg_hydraulic_rhs_noalloc: the hydraulic RHS pass without any device
 // allocation in the call.
 //
-// Some hosts own all of the device memory themselves: a Fortran driver that reserves one
+// Some hosts own all of the device memory themselves: a Fortran host program that reserves one
 // device pool at start-up for its whole run, or a service that admits work against a fixed
 // HBM budget, may not let a library call cudaMalloc once it is running.  For them this
 // entry point evaluates one CalculateHydraulicRHS on a context created earlier (inputs:
