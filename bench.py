@@ -261,6 +261,20 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def reduce_replicas(seconds, cell_updates, dist=None, device="cpu"):
+    """Replicas (one simulation per rank, no exchange between them): the job's time is the
+    slowest rank's and its work the sum of the ranks' cell-updates.  Returns (seconds, cell
+    updates) for the whole job; without a process group, the rank's own."""
+    if not dist:
+        return float(seconds), float(cell_updates)
+    import torch
+    tt = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    cc = torch.tensor([float(cell_updates)], dtype=torch.float64, device=device)
+    dist.all_reduce(cc)
+    return float(tt.item()), float(cc.item())
+
+
 def spin_up(sim, p, spin, every=None):
     """Untimed integration to t = spin; with `every`, the active-tile count is recorded at
     each multiple of `every` seconds: [[t, active tiles, percent of all tiles], ...]."""
@@ -504,15 +518,7 @@ def main():
     kms, kpasses = C.c_double(), C.c_int64()
     L.kg_get_kernel_time(sim.h, C.byref(kms), C.byref(kpasses))
     t_s = total_ms / 1e3
-    if dist:
-        tt = torch.tensor([t_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_s = float(tt.item())
-        cc = torch.tensor([float(cu)], device="cuda")
-        dist.all_reduce(cc)
-        cu_all = float(cc.item())
-    else:
-        cu_all = float(cu)
+    t_s, cu_all = reduce_replicas(t_s, cu, dist, "cuda")
     value = cu_all / t_s
     active_cells = len(sim.active_tiles()) * p.nXpertile * p.nYpertile
     sim.close()
