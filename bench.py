@@ -162,6 +162,42 @@ def run_reference(args, wl):
     print(json.dumps(line))
 
 
+def run_reference_members(args):
+    """The reference arm for the batched and served forms: the oracle (serial, one core)
+    advancing the first members of the same ensemble or request stream one after another,
+    a bounded sample of about 20 s of CPU work; cell-updates per second over the sample."""
+    from kestrel_gb300 import abi as A, workloads
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle
+    L = _oracle.load()
+    if args.workload == "ensemble_fp32":
+        members = [(p, b0) for p, b0, _ in workloads.ensemble(8)]
+    else:
+        members = [(p, b0) for _, p, b0, _ in workloads.serve_requests(8, rate=args.rate,
+                                                                       tend_range=(args.tend_min, args.tend_max))]
+    rc = C.c_int32(0)
+    cu, secs, n, used = 0, 0.0, 0, 0
+    for p, b0 in members:
+        if secs >= 20.0:
+            break
+        sim = _oracle.simulation(p, b0=b0)
+        used += 1
+        while secs < 20.0 * used / len(members) and sim.time[0] < p.tend:
+            st = A.StepStats()
+            secs += L.ko_timed_steps(sim.h, 1, C.byref(st), C.byref(rc))
+            cu += st.cell_updates
+            n += st.steps
+        sim.close()
+    v = cu / secs if secs > 0 else None
+    sample = f"{n} accepted steps of the first {used} members, serial C++ restatement (oracle)"
+    print(json.dumps({"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
+                      "steps": n, "warmup": 0, "ms_per_step": 1e3 * secs / max(n, 1), "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                      "config": {"workload": args.workload},
+                      "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port", "sample": sample},
+                      "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
 def run_ensemble(args):
     """The batched ensemble: N members (grid sides log-uniform in [128, 1024]
     at dx = 5 m, own fractal terrain, cap or flux source of 1e3-1e6 m^3, Chezy / Voellmy /
@@ -444,6 +480,10 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
+    if args.workload in ("ensemble_fp32", "serve_fp32") and args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        return run_reference_members(args)
     if args.workload == "ensemble_fp32" and args.impl == "ours":
         return run_ensemble(args)
     if args.workload == "serve_fp32" and args.impl == "ours":
