@@ -48,16 +48,48 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel: str, workload: str, cells: float):
-    """DRAM bytes per pass, scaled to `cells` active cells from the bytes per cell and pass
-    recorded in the committed ncu summary of this kernel and workload under profiles/
-    (the `dram_bytes_per_cell_pass:` line): the capture may run a smaller active set of the
-    same workload, and traffic grows with the cells processed."""
+def measured_sm_max_mhz():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["sm_max_mhz"])
+    except Exception:
+        return 2070.0
+
+
+def profile_figure(kernel: str, workload: str, key: str):
+    """A per-cell figure (`key: value` line) from the committed ncu summary of this kernel
+    and workload under profiles/, or None."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
         return None
-    m = re.search(r"dram_bytes_per_cell_pass:\s*([0-9.eE+]+)", open(path).read())
-    return float(m.group(1)) * cells if m else None
+    m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def profile_traffic(kernel: str, workload: str, cells: float):
+    """DRAM bytes per pass, scaled to `cells` active cells from the bytes per cell and pass
+    recorded in the ncu summary (the `dram_bytes_per_cell_pass:` line): the capture may run
+    a smaller active set of the same workload, and traffic grows with the cells processed."""
+    per_cell = profile_figure(kernel, workload, "dram_bytes_per_cell_pass")
+    return per_cell * cells if per_cell is not None else None
+
+
+def fp64_pipe_roofline(kernel: str, workload: str, cells: float, pass_ms: float, sm_mhz, n_sm: int):
+    """The bound the pass actually meets on GB300: its FP64 pipe (2 FP64 lanes per SM per
+    clock).  `achieved` = the FP64-pipe busy cycles one pass needs (the per-cell figure from
+    the ncu capture, `fp64_pipe_cycles_per_cell_pass:`, times the cells of the pass) over
+    the measured pass time; `peak` = every SM's FP64 pipe busy every cycle at the median SM
+    clock sampled during the timed region."""
+    per_cell = profile_figure(kernel, workload, "fp64_pipe_cycles_per_cell_pass")
+    if per_cell is None or not pass_ms or not sm_mhz or not n_sm:
+        return None
+    achieved = per_cell * cells / (pass_ms / 1e3)
+    peak = n_sm * sm_mhz * 1e6
+    return {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "FP64-pipe cycles/s",
+            "frac": achieved / peak, "pipe_cycles_per_cell_pass": per_cell, "cells_per_pass": cells,
+            "sm_mhz": sm_mhz, "n_sm": n_sm, "kernel": kernel,
+            "source": f"profiles/{kernel}_{workload}.md (per-cell FP64-pipe cycles: sm__pipe_fp64_cycles_active "
+                      f"x sm__cycles_active over the SMs, divided by the cells of the captured launch)"}
 
 
 class ClockSampler:
@@ -613,7 +645,8 @@ def main():
     achieved = alg_pass / (pass_ms / 1e3) / 1e9 if pass_ms > 0 else None
     peak, peak_kind = measured_peaks()
     kname = "k_hydro" if wl["prec"] == abi.PREC_FP64 else "k_hydro32"
-    traffic = profile_traffic(kname, args.workload, cu / max(nsteps, 1) / (2.0 if p.MorphodynamicsOn else 1.0))
+    cells_pass = cu / max(nsteps, 1) / (2.0 if p.MorphodynamicsOn else 1.0)
+    traffic = profile_traffic(kname, args.workload, cells_pass)
     line = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": nsteps,
         "warmup": args.warmup, "ms_per_step": total_ms / max(nsteps, 1), "higher_is_better": True, "scaling": "weak",
@@ -633,10 +666,16 @@ def main():
                      "kernel": kname, "pass_ms": pass_ms,
                      "note": "algorithmic bytes of the form over the measured pass time; the pass is bound by the FP64 "
                              "pipe (2 lanes per SM per clock on GB300), not HBM, per the committed ncu capture of "
-                             + kname + " on the 2048^2 morphodynamic workload"},
+                             + kname + " on the 2048^2 morphodynamic workload (roofline_fp64 gives that bound)"},
         "gpu_launches": launches,
         "clocks": clk,
     }
+    try:
+        mhz = (clk or {}).get("sm_mhz") or measured_sm_max_mhz()
+        n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        line["roofline_fp64"] = fp64_pipe_roofline(kname, args.workload, cells_pass, pass_ms, mhz, n_sm)
+    except Exception as e:  # a secondary figure: never lose the bench line for it
+        line["roofline_fp64"] = {"error": repr(e)}
     if timeline:
         line["config"]["active_timeline"] = timeline
     if wl["prec"] == abi.PREC_FP32 and not args.no_fp64:
