@@ -12,7 +12,8 @@
  * Conventions
  *  - Every entry point returns an int status: 0 (KG_OK) or a negative KG_ERR_* code.  The
  *    library never calls exit/abort and never traps on the device.  kg_last_error() gives
- *    a one-line message for the last failure on a context.
+ *    a one-line message for the last failure on a context; kg_last_error(NULL) gives the
+ *    reason the calling thread's last kg_create failed.
  *  - All pointers in signatures are HOST pointers; the context owns every device buffer.
  *  - Indices are 1-based tile IDs exactly as in the reference (src/Grid.f90:260-267,
  *    id = i + (j-1)*nXtiles, tiles numbered from the south-west corner).
@@ -155,7 +156,11 @@ typedef struct kg_ctx kg_ctx;
 const char* kg_version(void);
 
 /* InitialiseGrid (src/Grid.f90:166) + topography set-up (src/dem.f90 LoadDEM). precision
-   selects the FP64 drop-in (KG_PREC_FP64) or the FP32 mixed form (KG_PREC_FP32). */
+   selects the FP64 drop-in (KG_PREC_FP64) or the FP32 mixed form (KG_PREC_FP32).
+   The struct is checked before the device is touched: tile counts and sizes, positive cfl,
+   heightThreshold and maxdt, counts of caps/cubes/sources and series lengths, and every
+   selector within its enum give KG_ERR_PARAM (a 1D grid KG_ERR_UNSUPPORTED); then no
+   device gives KG_ERR_CUDA.  On failure *out is NULL and kg_last_error(NULL) says why. */
 int  kg_create(const kg_params* params, int32_t precision, kg_ctx** out);
 void kg_destroy(kg_ctx* ctx);
 const char* kg_last_error(const kg_ctx* ctx);

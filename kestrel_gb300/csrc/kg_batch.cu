@@ -756,7 +756,7 @@ int kg_batch_add(kg_batch* b, const kg_params* params, const double* b0, int64_t
     if (slot < 0) { b->err = "the batch is full"; return KG_ERR_STATE; }
     kg_ctx* c = nullptr;
     int rc = kg_create(params, KG_PREC_FP32, &c);
-    if (rc != KG_OK) { b->err = "kg_create failed"; return rc; }
+    if (rc != KG_OK) { b->err = "kg_create failed: " + g_create_err; return rc; }
     try {
         // the member runs on the batch stream and keeps its control words in the batch
         CK(cudaStreamSynchronize(c->st));

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <limits>
 #include <mutex>
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -208,6 +209,8 @@ namespace {
 // streams differ).  API calls on different contexts are serialised by one lock.
 kg_ctx* g_const_owner = nullptr;
 std::recursive_mutex g_api_mu;
+// Why the calling thread's last kg_create failed (kg_last_error(NULL)); empty after a success.
+thread_local std::string g_create_err;
 
 void bind_constants(kg_ctx& c);
 
@@ -1555,14 +1558,41 @@ void load_state(kg_ctx& c, const int32_t* ids, int n, const double* state, const
     c.tdirty[0] = c.tdirty[1] = 2;
 }
 
+// Checks of a caller's kg_params before anything is allocated.  The input parser applies
+// the reference's own checks of the input file (src/Parameters.f90, src/SolverSettings.f90,
+// src/DomainSettings.f90); these keep a struct filled by any C caller inside what the
+// kernels index and branch on.
+void validate_params(const kg_params& p) {
+    auto bad = [](const char* m) { throw KgError(KG_ERR_PARAM, m); };
+    auto within = [](int32_t v, int32_t lo, int32_t hi) { return v >= lo && v <= hi; };
+    if (p.nYtiles == 1 && p.nYpertile == 1 && p.nXtiles >= 1 && p.nXpertile >= 1)
+        throw KgError(KG_ERR_UNSUPPORTED, "1D grids are not implemented");
+    if (p.nXtiles < 1 || p.nYtiles < 1 || p.nXpertile < 2 || p.nYpertile < 2)
+        bad("nXtiles/nYtiles must be >= 1 and nXpertile/nYpertile >= 2");
+    if ((int64_t)p.nXtiles * p.nYtiles > (int64_t)1 << 30 || (int64_t)p.nXpertile * p.nYpertile > (int64_t)1 << 24)
+        bad("more than 2^30 tiles or 2^24 cells per tile");
+    if (!(p.Xtilesize > 0.0) || !(p.Ytilesize > 0.0) || !std::isfinite(p.Xtilesize) || !std::isfinite(p.Ytilesize))
+        bad("Xtilesize and Ytilesize must be positive and finite");
+    if (!(p.cfl > 0.0) || !(p.heightThreshold > 0.0) || !(p.maxdt > 0.0))
+        bad("cfl, heightThreshold and maxdt must be positive");
+    if (p.TileBuffer < 0) bad("TileBuffer must be >= 0");
+    if (!within(p.nSources, 0, KG_MAX_SOURCES) || !within(p.nCaps, 0, KG_MAX_CAPS) || !within(p.nCubes, 0, KG_MAX_CUBES))
+        bad("nCaps, nCubes and nSources must lie in 0..16");
+    for (int k = 0; k < p.nSources; ++k)
+        if (!within(p.sources[k].n_series, 1, KG_MAX_SERIES)) bad("bad flux series length");
+    if (!within(p.drag, KG_DRAG_CHEZY, KG_DRAG_MANNING) || !within(p.erosion, KG_ERO_OFF, KG_ERO_GRANULAR) ||
+        !within(p.deposition, KG_DEP_NONE, KG_DEP_SPEARMAN_MANNING) ||
+        !within(p.erosion_transition, KG_ETRANS_SMOOTH, KG_ETRANS_OFF) ||
+        !within(p.morpho_damping, KG_DAMP_NONE, KG_DAMP_RAT3) || !within(p.fswitch, KG_SWITCH_TANH, KG_SWITCH_STEP) ||
+        !within(p.limiter, KG_LIM_MINMOD1, KG_LIM_NONE) || !within(p.bcs, KG_BC_HALT, KG_BC_SPONGE) ||
+        !within(p.topog, KG_TOPO_UPLOAD, KG_TOPO_XTRISLOPE))
+        bad("a closure, limiter, boundary or topography selector is out of range");
+}
+
 // Run settings (src/DomainSettings.f90:185-225, src/Parameters.f90:629-648).
 void setup(kg_ctx& c, const kg_params& p) {
     c.p = p;
-    if (p.nXtiles < 1 || p.nYtiles < 1 || p.nXpertile < 2 || p.nYpertile < 2)
-        throw KgError(KG_ERR_PARAM, "nXtiles/nYtiles must be >= 1 and nXpertile/nYpertile >= 2");
-    if (p.nYtiles * p.nYpertile == 1) throw KgError(KG_ERR_UNSUPPORTED, "1D grids are not implemented");
-    if (p.nSources > KG_MAX_SOURCES || p.nCaps > KG_MAX_CAPS || p.nCubes > KG_MAX_CUBES)
-        throw KgError(KG_ERR_PARAM, "too many caps, cubes or sources");
+    validate_params(p);
     c.nX = p.nXpertile; c.nY = p.nYpertile; c.nXt = p.nXtiles; c.nYt = p.nYtiles; c.nTiles = c.nXt * c.nYt;
     c.SC = c.nX * c.nY; c.SV = (c.nX + 1) * (c.nY + 1); c.SFX = (c.nX + 1) * c.nY; c.SFY = c.nX * (c.nY + 1);
     c.nE = std::max(c.nX, c.nY);
@@ -1724,22 +1754,35 @@ extern "C" {
 const char* kg_version(void) { return "kestrel_gb300 1.0 (sm_103a)"; }
 
 int kg_create(const kg_params* params, int32_t precision, kg_ctx** out) {
-    if (!params || !out) return KG_ERR_PARAM;
+    if (!params || !out) {
+        g_create_err = "kg_create: null params or out";
+        return KG_ERR_PARAM;
+    }
     std::lock_guard<std::recursive_mutex> lock(g_api_mu);
     *out = nullptr;
-    if (precision != KG_PREC_FP64 && precision != KG_PREC_FP32) return KG_ERR_UNSUPPORTED;
-    kg_ctx* c = new kg_ctx();
-    c->prec = precision;
+    if (precision != KG_PREC_FP64 && precision != KG_PREC_FP32) {
+        g_create_err = "precision must be KG_PREC_FP64 or KG_PREC_FP32";
+        return KG_ERR_UNSUPPORTED;
+    }
+    kg_ctx* c = nullptr;
     try {
+        validate_params(*params);
         int n = 0;
         cudaError_t e = cudaGetDeviceCount(&n);
         if (e != cudaSuccess || n < 1) throw KgError(KG_ERR_CUDA, "no CUDA device is available");
+        c = new kg_ctx();
+        c->prec = precision;
         setup(*c, *params);
     } catch (const KgError& e) {
-        int code = e.code;
+        g_create_err = e.what();
         free_ctx(c);
-        return code;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_create_err = "host allocation failed";
+        free_ctx(c);
+        return KG_ERR_OOM;
     }
+    g_create_err.clear();
     *out = c;
     return KG_OK;
 }
@@ -1749,7 +1792,7 @@ void kg_destroy(kg_ctx* ctx) {
     free_ctx(ctx);
 }
 
-const char* kg_last_error(const kg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+const char* kg_last_error(const kg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_err.c_str(); }
 
 int kg_upload_b0(kg_ctx* c, const double* b0, int64_t nx1, int64_t ny1) {
     if (!c || !b0) return KG_ERR_PARAM;

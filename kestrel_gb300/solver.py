@@ -34,7 +34,8 @@ class Simulation:
         else:
             rc = self._f("create")(C.byref(params), C.byref(h))
         if rc != abi.KG_OK:
-            raise KestrelError(rc, "create failed")
+            msg = self._f("last_error")(None)
+            raise KestrelError(rc, "create failed: " + (msg.decode() if msg else ""))
         self.h = h
         if b0 is not None:
             self.upload_b0(b0)

@@ -718,12 +718,39 @@ static void CalculateVolume(Sim& s, double out[4]) {
 
 // Run settings derivation (src/DomainSettings.f90:185-225, src/Parameters.f90:629-648,
 // src/OutputSettings.f90:286).
+// The checks of a caller's struct that the C entry points make (the input parser applies
+// the reference's own input-file checks); same codes as the GPU library.
+static void CheckParams(const kg_params& p) {
+    auto bad = [](const char* m) { throw KoError(KG_ERR_PARAM, m); };
+    auto within = [](int32_t v, int32_t lo, int32_t hi) { return v >= lo && v <= hi; };
+    if (p.nYtiles == 1 && p.nYpertile == 1 && p.nXtiles >= 1 && p.nXpertile >= 1)
+        throw KoError(KG_ERR_UNSUPPORTED, "1D grids are not implemented");
+    if (p.nXtiles < 1 || p.nYtiles < 1 || p.nXpertile < 2 || p.nYpertile < 2)
+        bad("nXtiles/nYtiles must be >= 1 and nXpertile/nYpertile >= 2");
+    if ((int64_t)p.nXtiles * p.nYtiles > (int64_t)1 << 30 || (int64_t)p.nXpertile * p.nYpertile > (int64_t)1 << 24)
+        bad("more than 2^30 tiles or 2^24 cells per tile");
+    if (!(p.Xtilesize > 0.0) || !(p.Ytilesize > 0.0) || !std::isfinite(p.Xtilesize) || !std::isfinite(p.Ytilesize))
+        bad("Xtilesize and Ytilesize must be positive and finite");
+    if (!(p.cfl > 0.0) || !(p.heightThreshold > 0.0) || !(p.maxdt > 0.0))
+        bad("cfl, heightThreshold and maxdt must be positive");
+    if (p.TileBuffer < 0) bad("TileBuffer must be >= 0");
+    if (!within(p.nSources, 0, KG_MAX_SOURCES) || !within(p.nCaps, 0, KG_MAX_CAPS) || !within(p.nCubes, 0, KG_MAX_CUBES))
+        bad("nCaps, nCubes and nSources must lie in 0..16");
+    for (int k = 0; k < p.nSources; ++k)
+        if (!within(p.sources[k].n_series, 1, KG_MAX_SERIES)) bad("bad flux series length");
+    if (!within(p.drag, KG_DRAG_CHEZY, KG_DRAG_MANNING) || !within(p.erosion, KG_ERO_OFF, KG_ERO_GRANULAR) ||
+        !within(p.deposition, KG_DEP_NONE, KG_DEP_SPEARMAN_MANNING) ||
+        !within(p.erosion_transition, KG_ETRANS_SMOOTH, KG_ETRANS_OFF) ||
+        !within(p.morpho_damping, KG_DAMP_NONE, KG_DAMP_RAT3) || !within(p.fswitch, KG_SWITCH_TANH, KG_SWITCH_STEP) ||
+        !within(p.limiter, KG_LIM_MINMOD1, KG_LIM_NONE) || !within(p.bcs, KG_BC_HALT, KG_BC_SPONGE) ||
+        !within(p.topog, KG_TOPO_UPLOAD, KG_TOPO_XTRISLOPE))
+        bad("a closure, limiter, boundary or topography selector is out of range");
+}
+
 static void Setup(Sim& s, const kg_params& p) {
     RunSet& rp = s.rp;
+    CheckParams(p);
     rp.p = p;
-    if (p.nXtiles < 1 || p.nYtiles < 1 || p.nXpertile < 2 || p.nYpertile < 2)
-        throw KoError(KG_ERR_PARAM, "tile counts/sizes must be positive (nX/nYpertile >= 2)");
-    if (p.nYtiles * p.nYpertile == 1) throw KoError(KG_ERR_UNSUPPORTED, "1D grids are not implemented");
     rp.nXpertile = p.nXpertile; rp.nYpertile = p.nYpertile;
     rp.nXtiles = p.nXtiles; rp.nYtiles = p.nYtiles; rp.nTiles = p.nXtiles * p.nYtiles;
     rp.Xtilesize = p.Xtilesize; rp.Ytilesize = p.Ytilesize;
@@ -807,21 +834,26 @@ static int find_active(ko_ctx* c, int id) {
 
 extern "C" {
 
+// Why the calling thread's last ko_create failed (ko_last_error(NULL)).
+static thread_local std::string g_create_err;
 int ko_create(const kg_params* p, ko_ctx** out) {
+    if (!p || !out) return KG_ERR_PARAM;
     ko_ctx* c = new ko_ctx();
     try {
         ko::Setup(c->s, *p);
     } catch (const ko::KoError& e) {
         int code = e.code;
+        g_create_err = e.what();
         delete c;
         *out = nullptr;
         return code;
     }
+    g_create_err.clear();
     *out = c;
     return KG_OK;
 }
 void ko_destroy(ko_ctx* c) { delete c; }
-const char* ko_last_error(ko_ctx* c) { return c ? c->s.err.c_str() : "null context"; }
+const char* ko_last_error(ko_ctx* c) { return c ? c->s.err.c_str() : g_create_err.c_str(); }
 
 int ko_upload_b0(ko_ctx* c, const double* b0, int64_t nx1, int64_t ny1) {
     if (nx1 != c->s.g.nx1 || ny1 != c->s.g.ny1) { c->s.err = "b0 grid has the wrong shape"; return KG_ERR_PARAM; }

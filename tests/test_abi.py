@@ -64,3 +64,77 @@ def test_create_without_gpu_fails_loudly():
     h = C.c_void_p()
     rc = L.kg_create(C.byref(cases.cap_release_256()), abi.PREC_FP64, C.byref(h))
     assert rc == -5 and not h.value
+
+
+def _bad_params():
+    """One caller error per case, each on a copy of a valid struct: (what, mutate, code)."""
+    def setf(name, value):
+        return lambda p: setattr(p, name, value)
+
+    def series(p):
+        p.nSources = 1
+        p.sources[0].n_series = 0
+
+    return [
+        ("zero tiles", setf("nXtiles", 0), "KG_ERR_PARAM"),
+        ("one cell per tile row", setf("nXpertile", 1), "KG_ERR_PARAM"),
+        ("1D grid", lambda p: (setattr(p, "nYtiles", 1), setattr(p, "nYpertile", 1)), "KG_ERR_UNSUPPORTED"),
+        ("too many tiles", lambda p: (setattr(p, "nXtiles", 1 << 16), setattr(p, "nYtiles", 1 << 15)), "KG_ERR_PARAM"),
+        ("negative tile size", setf("Xtilesize", -16.0), "KG_ERR_PARAM"),
+        ("NaN tile size", setf("Ytilesize", float("nan")), "KG_ERR_PARAM"),
+        ("zero cfl", setf("cfl", 0.0), "KG_ERR_PARAM"),
+        ("zero height threshold", setf("heightThreshold", 0.0), "KG_ERR_PARAM"),
+        ("NaN maxdt", setf("maxdt", float("nan")), "KG_ERR_PARAM"),
+        ("negative TileBuffer", setf("TileBuffer", -1), "KG_ERR_PARAM"),
+        ("17 caps", setf("nCaps", 17), "KG_ERR_PARAM"),
+        ("negative sources", setf("nSources", -1), "KG_ERR_PARAM"),
+        ("empty flux series", series, "KG_ERR_PARAM"),
+        ("drag id", setf("drag", 7), "KG_ERR_PARAM"),
+        ("erosion id", setf("erosion", -1), "KG_ERR_PARAM"),
+        ("limiter id", setf("limiter", 5), "KG_ERR_PARAM"),
+        ("boundary id", setf("bcs", 4), "KG_ERR_PARAM"),
+        ("topography id", setf("topog", 19), "KG_ERR_PARAM"),
+        ("switch id", setf("fswitch", 8), "KG_ERR_PARAM"),
+    ]
+
+
+@pytest.mark.parametrize("what,mutate,code", _bad_params(), ids=[c[0] for c in _bad_params()])
+def test_create_rejects_bad_params_before_the_device(what, mutate, code):
+    """A struct outside what the kernels index and branch on is refused by kg_create before
+    any device call (so the same status comes back on a machine without a GPU), with the
+    reason in kg_last_error(NULL); the oracle's C entry gives the same status and reason."""
+    import _oracle
+    from kestrel_gb300 import lib
+    import cases
+    p = cases.cap_release_256()
+    mutate(p)
+    L, O = lib.load(), _oracle.load()
+    h = C.c_void_p()
+    rc = L.kg_create(C.byref(p), abi.PREC_FP64, C.byref(h))
+    assert abi.KG_ERR.get(rc) == code and not h.value
+    msg = L.kg_last_error(None).decode()
+    assert msg
+    ho = C.c_void_p()
+    rco = O.ko_create(C.byref(p), C.byref(ho))
+    assert rco == rc and not ho.value
+    assert O.ko_last_error(None).decode() == msg
+
+
+def test_create_error_reaches_the_python_mirror():
+    from kestrel_gb300 import lib
+    from kestrel_gb300.solver import KestrelError
+    import cases
+    p = cases.cap_release_256()
+    p.cfl = -1.0
+    with pytest.raises(KestrelError, match="cfl, heightThreshold and maxdt must be positive") as ei:
+        lib.simulation(p)
+    assert abi.KG_ERR[ei.value.code] == "KG_ERR_PARAM"
+
+
+def test_create_rejects_an_unknown_precision():
+    from kestrel_gb300 import lib
+    import cases
+    L = lib.load()
+    h = C.c_void_p()
+    assert abi.KG_ERR[L.kg_create(C.byref(cases.cap_release_256()), 7, C.byref(h))] == "KG_ERR_UNSUPPORTED"
+    assert b"precision" in L.kg_last_error(None)
