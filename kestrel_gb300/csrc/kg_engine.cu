@@ -1942,6 +1942,7 @@ int kg_get_ghost_tiles(kg_ctx* c, int32_t* ids, int32_t* n) {
 }
 
 int kg_get_tile_field(kg_ctx* c, int32_t id, int32_t field, double* out) {
+    if (!c) return KG_ERR_PARAM;
     KG_ENTER(c);
     int s = active_slot(c, id);
     if (s < 0) return KG_ERR_NOT_FOUND;
@@ -1982,6 +1983,7 @@ int kg_get_tile_field(kg_ctx* c, int32_t id, int32_t field, double* out) {
 }
 
 int kg_set_tile_field(kg_ctx* c, int32_t id, int32_t field, const double* in) {
+    if (!c) return KG_ERR_PARAM;
     KG_ENTER(c);
     int s = active_slot(c, id);
     if (s < 0) return KG_ERR_NOT_FOUND;
@@ -1996,6 +1998,8 @@ int kg_set_tile_field(kg_ctx* c, int32_t id, int32_t field, const double* in) {
 }
 
 int kg_get_tile_vertex(kg_ctx* c, int32_t id, int32_t which, double* out) {
+    if (!c) return KG_ERR_PARAM;
+    std::lock_guard<std::recursive_mutex> kg_lock_(g_api_mu);
     int s = active_slot(c, id);
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (which < 0 || which > 1 || !out) return KG_ERR_PARAM;
@@ -2007,6 +2011,8 @@ int kg_get_tile_vertex(kg_ctx* c, int32_t id, int32_t which, double* out) {
 }
 
 int kg_get_tile_rhs(kg_ctx* c, int32_t id, int32_t k, double* out) {
+    if (!c) return KG_ERR_PARAM;
+    std::lock_guard<std::recursive_mutex> kg_lock_(g_api_mu);
     int s = active_slot(c, id);
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (k < 1 || k > 5 || !out) return KG_ERR_PARAM;
@@ -2019,6 +2025,8 @@ int kg_get_tile_rhs(kg_ctx* c, int32_t id, int32_t k, double* out) {
 }
 
 int kg_get_tile_maxima(kg_ctx* c, int32_t id, int32_t which, double* out) {
+    if (!c) return KG_ERR_PARAM;
+    std::lock_guard<std::recursive_mutex> kg_lock_(g_api_mu);
     int s = active_slot(c, id);
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (which < 0 || which > 5 || !out) return KG_ERR_PARAM;
@@ -2036,8 +2044,8 @@ int kg_get_tile_maxima(kg_ctx* c, int32_t id, int32_t which, double* out) {
 }
 
 int kg_volume(kg_ctx* c, double out[4]) {
-    KG_ENTER(c);
     if (!c || !out) return KG_ERR_PARAM;
+    KG_ENTER(c);
     KG_GUARD(c, {
         std::vector<int> slots;
         for (int id : c->active) slots.push_back(T(*c, id).slot);

@@ -138,3 +138,45 @@ def test_create_rejects_an_unknown_precision():
     h = C.c_void_p()
     assert abi.KG_ERR[L.kg_create(C.byref(cases.cap_release_256()), 7, C.byref(h))] == "KG_ERR_UNSUPPORTED"
     assert b"precision" in L.kg_last_error(None)
+
+
+def _header_prototypes():
+    """(return type, name, [parameter types]) of every function the header declares."""
+    txt = open(HEADER).read()
+    out = []
+    for m in re.finditer(r"^(const char\*|void\*|void|int64_t|int|kg_ctx\*)\s+(kg_[a-z0-9_]+)\(([^)]*)\);", txt, re.M):
+        params = [a.strip() for a in m.group(3).split(",")] if m.group(3).strip() != "void" else []
+        types = [re.sub(r"\s*\b[a-z_0-9]+(\[\d+\])?$", lambda q: "*" if q.group(1) else "", a).strip() for a in params]
+        out.append((m.group(1), m.group(2), types))
+    return out
+
+
+def test_every_entry_point_refuses_a_null_handle():
+    """Every function that takes a context or batch handle returns KG_ERR_PARAM (or NULL / 0
+    for the non-status getters, nothing for the destructors) when the handle is NULL, with
+    every other argument zero or NULL: the library never dereferences a caller's NULL."""
+    L = C.CDLL(build.build())  # its own function objects: the shared declarations stay as they are
+    protos = [p for p in _header_prototypes() if p[2] and p[2][0].replace("const ", "") in ("kg_ctx*", "kg_batch*")]
+    assert len(protos) >= 35
+    for ret, name, types in protos:
+        f = getattr(L, name)
+        args = []
+        for t in types:
+            if "*" in t:
+                args.append(C.c_void_p(None))
+            elif t == "double":
+                args.append(C.c_double(0.0))
+            elif t == "int64_t":
+                args.append(C.c_int64(0))
+            else:
+                args.append(C.c_int32(0))
+        f.argtypes = [type(a) for a in args]
+        f.restype = {"int": C.c_int, "int64_t": C.c_int64, "void": None, "const char*": C.c_char_p,
+                     "void*": C.c_void_p, "kg_ctx*": C.c_void_p}[ret]
+        got = f(*args)
+        if ret == "int":
+            assert abi.KG_ERR.get(got) == "KG_ERR_PARAM", (name, got)
+        elif ret in ("int64_t",):
+            assert got == 0, name
+        elif ret in ("void*", "kg_ctx*"):
+            assert got is None, name
