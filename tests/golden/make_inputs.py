@@ -9,7 +9,7 @@ import shutil
 import sys
 
 NAMES = ["cap_dilute_2d", "cap_conc_2d", "cap_morpho_2d", "flat_depositional_2d", "flux_edwards2019_2d",
-         "flux_hydro_2d", "flux_morpho_2d", "lake_at_rest_hydro_2d", "lake_at_rest_morpho_2d",
+         "flux_hydro_2d", "flux_morpho_2d", "flux_single_pt", "lake_at_rest_hydro_2d", "lake_at_rest_morpho_2d",
          "tile_indep_static_100m", "tile_indep_static_50m", "tile_indep_dynamic_100m", "tile_indep_dynamic_20m"]
 
 

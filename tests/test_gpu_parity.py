@@ -70,6 +70,7 @@ def test_steps_bitexact_cap_release():
     ("cap_dilute_2d", 2.0, 2),        # 50x50-cell tiles: partial 16x16 blocks, halt edges
     ("flux_hydro_2d", 2.0, 2),        # flux source with end-point logic, dt rejections
     ("cap_conc_2d", 1.0, 1),          # Pouliquen drag (sqrt/div only)
+    ("flux_single_pt", None, None),   # full run: one-point flux series from t = 0, T start = -1
 ])
 def test_reference_inputs_bitexact(name, tend, nout):
     p = cases.ref_input(name, tend=tend, nout=nout)

@@ -76,6 +76,7 @@ CONSERVATION = [
     ("flux_edwards2019_2d", 3.0, 3),    # T end 10 in the reference
     ("flux_morpho_2d", 2.0, 2),         # T end 5 in the reference
     ("flat_depositional_2d", 2.0, 2),   # T end 100 in the reference
+    ("flux_single_pt", None, None),     # full run: a one-point flux series starting after T start
 ]
 
 
