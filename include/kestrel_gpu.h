@@ -265,6 +265,10 @@ int  kg_redistribution_stats(kg_ctx* ctx, int64_t* cells, int64_t* waves, int64_
    reference counterpart. */
 int  kg_get_counters(kg_ctx* ctx, int64_t out[3]);
 int64_t kg_device_bytes(kg_ctx* ctx);
+/* Device bytes one allocated tile (active or ghost) costs for the given tile size and
+   form; host arithmetic only, no device needed (0 for invalid arguments).  A context's
+   tile memory is this times its slot capacity. */
+int64_t kg_slot_bytes(int32_t nXpertile, int32_t nYpertile, int32_t precision);
 /* Bytes copied host->device (out[0]) and device->host (out[1]) by the context so far. */
 int  kg_get_transfer_bytes(kg_ctx* ctx, int64_t out[2]);
 /* Host wall time in seconds since creation: out[0] inside kg_step/kg_integrate_to steps,

@@ -214,15 +214,18 @@ thread_local std::string g_create_err;
 
 void bind_constants(kg_ctx& c);
 
-size_t bytes_per_slot(const kg_ctx& c) {
-    size_t SC = c.SC;
-    return sizeof(double) * (4 * 4 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * (size_t)c.SFX + 5 * (size_t)c.SFY + 2 * (size_t)c.SV) +
-                             2 * SC + 5 * SC + SC + 2 * SC + 9 * SC + GE_COUNT * (size_t)c.nE + 11 * SC + 2 * SC) +
+// Device bytes of one slot: Q, E/I, CT/FX/FY/BV (two sets), UV, MS, EMD, B0S, G9, GE, MX,
+// the source-override Hn and rho planes, nbr/kind/has_source/tile_of_slot, and in the FP32
+// form TD/TF/TFX/TFY (two sets).
+size_t slot_bytes(size_t nX, size_t nY, int prec) {
+    size_t SC = nX * nY, SFX = (nX + 1) * nY, SFY = nX * (nY + 1), SV = (nX + 1) * (nY + 1), nE = std::max(nX, nY);
+    return sizeof(double) * (4 * 4 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * SFX + 5 * SFY + 2 * SV) +
+                             2 * SC + 5 * SC + SC + 2 * SC + 9 * SC + GE_COUNT * nE + 11 * SC + 2 * SC) +
            8 * sizeof(int) + 2 + sizeof(int) +
-           (c.prec == KG_PREC_FP32 ? 2 * (3 * sizeof(double) * SC + 6 * sizeof(float) * SC +
-                                          2 * sizeof(float) * ((size_t)c.SFX + (size_t)c.SFY))
-                                   : 0);
+           (prec == KG_PREC_FP32 ? 2 * (3 * sizeof(double) * SC + 6 * sizeof(float) * SC + 2 * sizeof(float) * (SFX + SFY))
+                                 : 0);
 }
+size_t bytes_per_slot(const kg_ctx& c) { return slot_bytes((size_t)c.nX, (size_t)c.nY, c.prec); }
 
 template <class T>
 void grow_array(T*& ptr, size_t old_n, size_t new_n, cudaStream_t st) {
@@ -2086,6 +2089,11 @@ int kg_get_transfer_bytes(kg_ctx* c, int64_t out[2]) {
 int64_t kg_device_bytes(kg_ctx* c) {
     if (!c) return 0;
     return (int64_t)bytes_per_slot(*c) * c->cap;
+}
+
+int64_t kg_slot_bytes(int32_t nXpertile, int32_t nYpertile, int32_t precision) {
+    if (nXpertile < 1 || nYpertile < 1 || (precision != KG_PREC_FP64 && precision != KG_PREC_FP32)) return 0;
+    return (int64_t)slot_bytes((size_t)nXpertile, (size_t)nYpertile, precision);
 }
 
 int kg_host_times(kg_ctx* c, double out[3]) {

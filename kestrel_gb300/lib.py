@@ -39,6 +39,8 @@ def load(auto_build: bool = True):
     lib.kg_get_transfer_bytes.restype = C.c_int
     lib.kg_device_bytes.argtypes = [C.c_void_p]
     lib.kg_device_bytes.restype = C.c_int64
+    lib.kg_slot_bytes.argtypes = [C.c_int32, C.c_int32, C.c_int32]
+    lib.kg_slot_bytes.restype = C.c_int64
     lib.kg_host_times.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     lib.kg_host_times.restype = C.c_int
     _lib = lib

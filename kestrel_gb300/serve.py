@@ -17,18 +17,17 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import abi
+from . import abi, lib
 from .batch import Batch
 
 
 def slot_bytes(nX: int, nY: int, fp32: bool = True) -> int:
-    """Device bytes of one allocated tile (the engine's per-slot planes)."""
-    SC, SFX, SFY, SV, nE = nX * nY, (nX + 1) * nY, nX * (nY + 1), (nX + 1) * (nY + 1), max(nX, nY)
-    d = 16 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * SFX + 5 * SFY + 2 * SV) + 2 * SC + 5 * SC + SC + 9 * SC + 12 * nE + 11 * SC + 2 * SC
-    b = 8 * d + 8 * 4 + 2 + 4
-    if fp32:
-        b += 2 * (3 * 8 * SC + 6 * 4 * SC + 2 * 4 * (SFX + SFY))
-    return b
+    """Device bytes of one allocated tile: the engine's own per-slot count (kg_slot_bytes,
+    host arithmetic, no device needed)."""
+    n = lib.load().kg_slot_bytes(nX, nY, abi.PREC_FP32 if fp32 else abi.PREC_FP64)
+    if n <= 0:
+        raise ValueError(f"invalid tile size {nX}x{nY}")
+    return int(n)
 
 
 def worst_case_bytes(p: abi.Params) -> int:

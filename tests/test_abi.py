@@ -180,3 +180,25 @@ def test_every_entry_point_refuses_a_null_handle():
             assert got == 0, name
         elif ret in ("void*", "kg_ctx*"):
             assert got is None, name
+
+
+@pytest.mark.parametrize("nx,ny", [(64, 64), (50, 50), (16, 8)])
+def test_slot_bytes_follow_the_layout(nx, ny):
+    """kg_slot_bytes (host arithmetic, no device) counts every per-slot array of the HBM
+    layout, and the serving loop's admission uses that count."""
+    from kestrel_gb300 import lib, serve
+    L = lib.load()
+    SC, SFX, SFY, SV, nE = nx * ny, (nx + 1) * ny, nx * (ny + 1), (nx + 1) * (ny + 1), max(nx, ny)
+    doubles = (4 * 4 * SC                                   # Q: 4 buffers of w, rhoHnu, rhoHnv, Hnpsi
+               + 2 * (4 * SC + SC)                          # E, I: two RHS sets
+               + 2 * (4 * SC + 5 * SFX + 5 * SFY + 2 * SV)  # CT, FX, FY, BV: two topography sets
+               + 2 * SC + 5 * SC + SC + 2 * SC              # UV, MS, EMD, B0S
+               + 9 * SC + 12 * nE + 11 * SC                 # G9, GE, MX
+               + 2 * SC)                                    # source-override Hn and rho
+    ints = 8 + 1                                            # nbr[8], tile_of_slot
+    fp32 = 2 * (3 * SC * 8 + 6 * SC * 4 + 2 * (SFX + SFY) * 4)  # TD, TF, TFX, TFY: two sets
+    base = 8 * doubles + 4 * ints + 2                       # + kind, has_source bytes
+    assert L.kg_slot_bytes(nx, ny, abi.PREC_FP64) == base
+    assert L.kg_slot_bytes(nx, ny, abi.PREC_FP32) == base + fp32
+    assert serve.slot_bytes(nx, ny) == base + fp32
+    assert L.kg_slot_bytes(0, ny, abi.PREC_FP64) == 0 and L.kg_slot_bytes(nx, ny, 9) == 0
