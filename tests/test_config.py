@@ -54,3 +54,38 @@ def test_rejects_unknown_drag():
     with pytest.raises(config.InputError):
         config.parse("Domain:\nnXtiles = 1\nnYtiles = 1\nnXpertile = 4\nnYpertile = 4\nXtilesize = 4\n"
                      "Parameters:\nDrag = Bogus\nSolver:\nT end = 1\n")
+
+
+def _all_inputs():
+    import glob
+    import os
+    import cases
+    return sorted(os.path.basename(f)[len("Input_"):-len(".txt")] for f in glob.glob(os.path.join(cases.INPUTS, "Input_*.txt")))
+
+
+def test_every_reference_input_parses_and_1d_grids_are_refused():
+    """Every input file of the reference's suite parses. Unknown labels are skipped with a
+    warning, as src/Messages.f90:299-304 does. The 2D inputs create an oracle context; the
+    1D ones (nYtiles = nYpertile = 1) get KG_ERR_UNSUPPORTED from the oracle and from the
+    GPU library, before any device call."""
+    import ctypes as C
+    import _oracle
+    import cases
+    from kestrel_gb300 import lib
+    L, O = lib.load(), _oracle.load()
+    names = _all_inputs()
+    assert len(names) >= 23
+    n1d = 0
+    for name in names:
+        p = cases.ref_input(name)
+        one_d = p.nYtiles * p.nYpertile == 1
+        n1d += one_d
+        h = C.c_void_p()
+        rc = O.ko_create(C.byref(p), C.byref(h))
+        if one_d:
+            assert abi.KG_ERR[rc] == "KG_ERR_UNSUPPORTED", name
+            assert abi.KG_ERR[L.kg_create(C.byref(p), abi.PREC_FP64, C.byref(C.c_void_p()))] == "KG_ERR_UNSUPPORTED", name
+        else:
+            assert rc == abi.KG_OK, (name, O.ko_last_error(None))
+            O.ko_destroy(h)
+    assert n1d == 9
