@@ -9,15 +9,18 @@ advanced by one accepted hydraulic dt (a morphodynamic Strang step counts 2).
 - value:   device-timed throughput (CUDA events on the library's stream around each
            step; L2 flushed by a 256 MiB write between timed steps, outside the timed
            intervals).
-- e2e:     the same metric through the public C ABI from host inputs to host outputs:
-           kg_create + kg_load_sources (inputs copied from host) + K steps (each returns
-           its statistics to the host) + reading the conserved fields of every active tile
-           back to host memory, timed on the host clock.
+- e2e:     the same metric through the public C ABI, host clock: K kg_step calls after
+           the same spin-up (each returns its statistics to the host, with the library's
+           own count of its host<->device bytes), then the conserved fields of every
+           active tile read back to host memory.  e2e_job: the whole job from kg_create
+           with the settings and bed uploaded, through the spin-up, to the read-back.
 - roofline: the fused hydraulic pass; algorithmic bytes per cell-update (FP64 hydraulic
            step: 368 B over its 4 passes) over the measured pass time, against the
-           measured HBM copy bandwidth.
-- cpu_baseline: the CPU oracle (a serial C++ restatement of the reference; the Fortran
-           reference cannot be built here) on a bounded sample of the same workload.
+           measured HBM copy bandwidth.  roofline_fp64: the same pass against its FP64
+           pipe, the bound it meets on GB300.
+- cpu_baseline: the CPU oracle (a serial C++ restatement of the reference, which is
+           itself serial; the Fortran cannot be built here) on a bounded sample of the
+           same workload, on one of the host's cores.
 Under torchrun (N > 1) each rank advances an independent replica (replicas only).
 """
 from __future__ import annotations
@@ -160,7 +163,7 @@ def cpu_baseline(params, b0=None, seconds=15.0, max_steps=100000):
         if sim.time[0] >= params.tend:
             break
     return {"value": total_cu / total_s if total_s > 0 else None, "unit": "cell-updates/s", "cores": 1,
-            "kind": "port", "sample": f"first {steps} accepted steps from t=0 (t_end {sim.time[0]:.3f} s), "
+            "host_cores": os.cpu_count(), "kind": "port", "sample": f"first {steps} accepted steps from t=0 (t_end {sim.time[0]:.3f} s), "
             f"{total_cu} cell-updates in {total_s:.2f} s, serial C++ restatement (oracle)"}
 
 
@@ -188,7 +191,7 @@ def run_reference(args, wl):
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(n, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": args.workload, "desc": wl["desc"], "l2": "n/a (CPU)"},
-            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
                              "sample": f"{n} accepted steps after {args.warmup} warm-up steps, serial C++ restatement"},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -226,7 +229,7 @@ def run_reference_members(args):
                       "steps": n, "warmup": 0, "ms_per_step": 1e3 * secs / max(n, 1), "higher_is_better": True,
                       "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
                       "config": {"workload": args.workload},
-                      "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port", "sample": sample},
+                      "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": 1, "host_cores": os.cpu_count(), "kind": "port", "sample": sample},
                       "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
@@ -393,7 +396,7 @@ def run_dem(args):
                           "steps": 1, "warmup": 0, "ms_per_step": 1e3 * secs, "higher_is_better": True, "scaling": "weak",
                           "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
                           "config": {"workload": "dem_2048"},
-                          "cpu_baseline": {"value": v, "unit": "vertex-heights/s", "cores": 1, "kind": "port",
+                          "cpu_baseline": {"value": v, "unit": "vertex-heights/s", "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
                                            "sample": f"oracle set-up: raster copy, sources and the heights of its {nt} active and ghost tiles"},
                           "e2e": {"value": v, "unit": "vertex-heights/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
@@ -439,7 +442,7 @@ def run_dem(args):
         secs = time.perf_counter() - t1
         nt = len(o.active_tiles()) + len(o.ghost_tiles())
         line["cpu_baseline"] = {"value": nt * (p.nXpertile + 1) * (p.nYpertile + 1) / secs, "unit": "vertex-heights/s",
-                                "cores": 1, "kind": "port",
+                                "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
                                 "sample": f"oracle set-up: raster copy, sources and the heights of its {nt} active and ghost tiles, {secs:.2f} s"}
     print(json.dumps(line))
 
