@@ -202,3 +202,38 @@ def test_slot_bytes_follow_the_layout(nx, ny):
     assert L.kg_slot_bytes(nx, ny, abi.PREC_FP32) == base + fp32
     assert serve.slot_bytes(nx, ny) == base + fp32
     assert L.kg_slot_bytes(0, ny, abi.PREC_FP64) == 0 and L.kg_slot_bytes(nx, ny, 9) == 0
+
+
+def _fortran_type_fields(text, name):
+    """[(field, fortran type)] of `type, bind(C) :: name` in a Fortran listing."""
+    m = re.search(r"type, bind\(C\) :: " + name + r"\b[^\n]*\n(.*?)\n\s*end type", text, re.S)
+    assert m, name
+    out = []
+    for line in m.group(1).splitlines():
+        line = line.split("!")[0].strip()
+        if not line:
+            continue
+        ftype, names = [x.strip() for x in line.split("::")]
+        for n in re.findall(r"[A-Za-z_0-9]+(?:\(\d+\))?", names):
+            out.append((n, ftype))
+    return out
+
+
+@pytest.mark.parametrize("name,cls", [("kg_params", "Params"), ("kg_cap", "Cap"), ("kg_cube", "Cube"),
+                                      ("kg_flux_source", "FluxSource"), ("kg_raster", "Raster"),
+                                      ("kg_step_stats", "StepStats")])
+def test_fortran_binding_matches_the_structs(name, cls):
+    """The bind(C) derived types of the Fortran binding list every field of the C struct, in
+    order, with the same kind and array bound (padding fields without their underscore)."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    got = _fortran_type_fields(text, name)
+    kinds = {C.c_double: "real(c_double)", C.c_int32: "integer(c_int32_t)", C.c_int64: "integer(c_int64_t)"}
+    subtypes = {abi.Cap: "type(kg_cap)", abi.Cube: "type(kg_cube)", abi.FluxSource: "type(kg_flux_source)"}
+    want = []
+    for fname, ft in getattr(abi, cls)._fields_:
+        if hasattr(ft, "_length_"):
+            base = ft._type_
+            want.append((f"{fname.lstrip('_')}({ft._length_})", subtypes.get(base) or kinds[base]))
+        else:
+            want.append((fname.lstrip("_"), kinds[ft]))
+    assert got == want
