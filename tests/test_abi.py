@@ -237,3 +237,26 @@ def test_fortran_binding_matches_the_structs(name, cls):
         else:
             want.append((fname.lstrip("_"), kinds[ft]))
     assert got == want
+
+
+def test_fortran_interfaces_match_the_header():
+    """Every bind(C) interface of the Fortran binding names a header function and takes its
+    number of arguments; value arguments are the header's scalars, the rest its pointers."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    protos = {n: types for _, n, types in _header_prototypes()}
+    blocks = re.findall(r"(?:function|subroutine) (kg_[a-z0-9_]+)\(([^)]*)\) bind\(C, name=\"(kg_[a-z0-9_]+)\"\)(.*?)end (?:function|subroutine)",
+                        text, re.S)
+    assert len(blocks) >= 9
+    for fname, args, cname, body in blocks:
+        assert fname == cname and cname in protos, cname
+        names = [a.strip() for a in args.split(",") if a.strip()]
+        types = protos[cname]
+        assert len(names) == len(types), cname
+        for a, t in zip(names, types):
+            decl = re.search(r"^\s*([^!\n]*)::[^!\n]*\b" + a + r"\b", body, re.M)
+            assert decl, (cname, a)
+            attrs = decl.group(1)
+            if "*" in t:  # a pointer: by reference, or an explicit c_ptr passed by value
+                assert "value" not in attrs or "type(c_ptr)" in attrs, (cname, a, t)
+            else:         # a scalar: by value
+                assert "value" in attrs and "type(c_ptr)" not in attrs, (cname, a, t)
