@@ -18,10 +18,10 @@ def load(auto_build: bool = True):
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB):
-        if not auto_build:
-            raise OSError(f"{LIB} is missing; run kestrel_gb300.build.build()")
-        build()
+    if auto_build:
+        build()  # compiles only when the library is missing or older than a source
+    elif not os.path.exists(LIB):
+        raise OSError(f"{LIB} is missing; run kestrel_gb300.build.build()")
     lib = C.CDLL(LIB)
     abi.declare(lib, "kg")
     lib.kg_version.restype = C.c_char_p
