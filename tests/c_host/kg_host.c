@@ -23,8 +23,9 @@ int main(int argc, char** argv) {
     kg_ctx* ctx = NULL;
     int rc = kg_create(&p, atoi(argv[2]), &ctx);
     if (rc != KG_OK) {
-        printf("create %d\n", rc);
-        return 0;  /* no GPU: the library refuses instead of computing on the host */
+        /* no GPU, or a struct the library refuses: the status and its reason, no host compute */
+        printf("create %d\n%s\n", rc, kg_last_error(NULL));
+        return 0;
     }
     rc = kg_load_sources(ctx);
     if (rc != KG_OK) {

@@ -24,22 +24,32 @@ def host_binary(tmp_path):
     return exe
 
 
-def run_host(tmp_path, p, precision=abi.PREC_FP64):
+def run_host(tmp_path, p, precision=abi.PREC_FP64, lines=False):
     path = str(tmp_path / "params.bin")
     with open(path, "wb") as f:
         f.write(bytes(p))
     out = subprocess.run([host_binary(tmp_path), path, str(precision)], capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stdout + out.stderr
-    return out.stdout.split()
+    return out.stdout.splitlines() if lines else out.stdout.split()
 
 
 def test_c_host_without_gpu(tmp_path):
     import torch
     if torch.cuda.is_available():
         pytest.skip("a GPU is present")
-    words = run_host(tmp_path, cases.ref_input("cap_dilute_2d", tend=0.5, nout=1))
+    out = run_host(tmp_path, cases.ref_input("cap_dilute_2d", tend=0.5, nout=1), lines=True)
     cuda_err = next(k for k, v in abi.KG_ERR.items() if v == "KG_ERR_CUDA")
-    assert words == ["create", str(cuda_err)]
+    assert out == [f"create {cuda_err}", "no CUDA device is available"]
+
+
+def test_c_host_bad_struct(tmp_path):
+    """A struct the library refuses gives the same status and reason to a C host, on any
+    machine (the check comes before the device)."""
+    p = cases.ref_input("cap_dilute_2d", tend=0.5, nout=1)
+    p.limiter = 99
+    out = run_host(tmp_path, p, lines=True)
+    param_err = next(k for k, v in abi.KG_ERR.items() if v == "KG_ERR_PARAM")
+    assert out == [f"create {param_err}", "a closure, limiter, boundary or topography selector is out of range"]
 
 
 @pytest.mark.gpu
