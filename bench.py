@@ -81,8 +81,9 @@ def fp64_pipe_roofline(kernel: str, workload: str, cells: float, pass_ms: float,
     """The bound the pass actually meets on GB300: its FP64 pipe (2 FP64 lanes per SM per
     clock).  `achieved` = the FP64-pipe busy cycles one pass needs (the per-cell figure from
     the ncu capture, `fp64_pipe_cycles_per_cell_pass:`, times the cells of the pass) over
-    the measured pass time; `peak` = every SM's FP64 pipe busy every cycle at the median SM
-    clock sampled during the timed region."""
+    the measured pass time; `peak` = every SM's FP64 pipe busy every cycle at `sm_mhz` (the
+    median SM clock sampled during the main timed region; the GPU's maximum clock for the
+    FP64 twin, which is not sampled)."""
     per_cell = profile_figure(kernel, workload, "fp64_pipe_cycles_per_cell_pass")
     if per_cell is None or not pass_ms or not sm_mhz or not n_sm:
         return None
@@ -472,6 +473,7 @@ def fp64_plain(args, wname, snapshot=None):
     for _ in range(args.warmup):
         sim.step(p.tend)
     torch.cuda.synchronize()
+    timed = L.kg_set_kernel_timing(sim.h, 1) == 0  # pass times, as in the main leg
     evs, cu, n = [], 0, 0
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
@@ -486,9 +488,20 @@ def fp64_plain(args, wname, snapshot=None):
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in evs)
     active = len(sim.active_tiles())
+    pass_ms = None
+    if timed:
+        kms, kpasses = C.c_double(), C.c_int64()
+        if L.kg_get_kernel_time(sim.h, C.byref(kms), C.byref(kpasses)) == 0 and kpasses.value > 0:
+            pass_ms = kms.value / kpasses.value
     sim.close()
     out = {"workload": wname, "value": cu / (ms / 1e3), "unit": "cell-updates/s", "steps": n, "ms_per_step": ms / max(n, 1),
-           "active_tiles_end": active}
+           "active_tiles_end": active, "pass_ms": pass_ms}
+    try:  # the FP64 pass against its FP64 pipe; the clock is the GPU's maximum (not sampled here)
+        cells = cu / max(n, 1) / (2.0 if p.MorphodynamicsOn else 1.0)
+        n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        out["roofline_fp64"] = fp64_pipe_roofline("k_hydro", wname, cells, pass_ms, measured_sm_max_mhz(), n_sm)
+    except Exception as e:
+        out["roofline_fp64"] = {"error": repr(e)}
     if snapshot is not None:
         out["start"] = f"restarted from the FP32 run's state at t={snapshot[3]:.3f} s ({len(snapshot[0])} tiles)"
     return out
