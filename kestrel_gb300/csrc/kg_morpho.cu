@@ -528,27 +528,28 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
     return true;
 }
 
-// The 3 x 3 cells a redistribution at cell (s, i, j) updates, in the order of the
-// reference's tile navigation (:404-448; i, j 0-based): ct[k] = -1 where a tile is missing.
+// The 3 x 3 cells a redistribution at cell (s, i, j) updates, column by column from the
+// west as the reference's navigation visits them (:404-448; i, j 0-based).  Each column's
+// tile is s or its west/east neighbour, and a cell above or below it lies in that tile's
+// north/south neighbour, which is what the reference's walk reaches when every tile
+// exists.  vt[k] = -1 for a cell whose tile was never allocated: on periodic domains the
+// diagonal tiles get no ghost copy (src/UpdateTiles.f90:415-418), and only that tile's
+// cells are skipped.
 __device__ __forceinline__ void redist_cells_of(const DevParams& P, const DevArrays& A, int s, int i, int j, int vt[9], int vi[9],
                                                 int vj[9]) {
     int nX = P.nX, nY = P.nY;
-    auto nb = [&](int t, int d) { return t < 0 ? -1 : A.nbr[t * 8 + d]; };
-    int sW = A.nbr[s * 8 + NB_W];
-    int ct, ci, cj, n = 0;
-    if (i == 0) { ct = sW; ci = nX - 1; }
-    else { ct = s; ci = i - 1; }
-    for (int k = -1; k <= 1; ++k) {
-        if (j == 0) { ct = nb(ct, NB_S); cj = nY - 1; }
-        else cj = j - 1;
-        for (int l = -1; l <= 1; ++l) {
+    int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E];
+    int n = 0;
+    for (int di = -1; di <= 1; ++di) {
+        int ci = i + di, col = s;
+        if (ci < 0) { col = sW; ci += nX; }
+        else if (ci >= nX) { col = sE; ci -= nX; }
+        for (int dj = -1; dj <= 1; ++dj) {
+            int cj = j + dj, ct = col;
+            if (cj < 0) { ct = col < 0 ? -1 : A.nbr[col * 8 + NB_S]; cj += nY; }
+            else if (cj >= nY) { ct = col < 0 ? -1 : A.nbr[col * 8 + NB_N]; cj -= nY; }
             vt[n] = ct; vi[n] = ci; vj[n] = cj; ++n;
-            cj = cj + 1;
-            if (cj == nY && l < 1) { ct = nb(ct, NB_N); cj = 0; }
         }
-        if (j + 1 > nY - 1) ct = nb(ct, NB_S);
-        ci = ci + 1;
-        if (ci == nX) { ct = nb(ct, NB_E); ci = 0; }
     }
 }
 

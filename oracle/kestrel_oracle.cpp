@@ -306,26 +306,37 @@ static bool RedistributeCell(const RunSet& rp, Grid& g, int ttk, int i, int j, d
         double v = T3.bt(depi[k], depj[k]);
         if (depi[k] == 1) TL(im3, T3.West()).bt(nX + 1, depj[k]) = v;
         else if (depi[k] == nX + 1) TL(im3, T3.East()).bt(1, depj[k]) = v;
+        // A diagonal tile that was never allocated (periodic domains) has no copy to patch.
+        auto put = [&](int id, int a, int b) {
+            if (TL(im3, id).bt.allocated()) TL(im3, id).bt(a, b) = v;
+        };
         if (depj[k] == 1) {
             TL(im3, T3.South()).bt(depi[k], nY + 1) = v;
-            if (depi[k] == 1) TL(im3, TL(im3, T3.South()).West()).bt(nX + 1, nY + 1) = v;
-            if (depi[k] == nX + 1) TL(im3, TL(im3, T3.South()).East()).bt(1, nY + 1) = v;
+            if (depi[k] == 1) put(TL(im3, T3.South()).West(), nX + 1, nY + 1);
+            if (depi[k] == nX + 1) put(TL(im3, T3.South()).East(), 1, nY + 1);
         }
         if (depj[k] == nY + 1) {
             TL(im3, T3.North()).bt(depi[k], 1) = v;
-            if (depi[k] == 1) TL(im3, TL(im3, T3.North()).West()).bt(nX + 1, 1) = v;
-            if (depi[k] == nX + 1) TL(im3, TL(im3, T3.North()).East()).bt(1, 1) = v;
+            if (depi[k] == 1) put(TL(im3, T3.North()).West(), nX + 1, 1);
+            if (depi[k] == nX + 1) put(TL(im3, T3.North()).East(), 1, 1);
         }
     }
-    // Update the (up to) 3x3 surrounding cell centres; the tile navigation is kept
-    // exactly as written (:404-448).
-    int cttk, ci, cj;
-    if (i == 1) { cttk = g.tc(ttk).West(); ci = nX; }
-    else { cttk = ttk; ci = i - 1; }
-    for (int k = -1; k <= 1; ++k) {
-        if (j == 1) { cttk = g.tc(cttk).South(); cj = nY; }
-        else cj = j - 1;
-        for (int l = -1; l <= 1; ++l) {
+    // Update the (up to) 3x3 surrounding cell centres, column by column from the west as
+    // the reference's navigation visits them (:404-448).  Each column's tile is ttk or its
+    // west/east neighbour, and a cell above or below it lies in that tile's north/south
+    // neighbour: the tiles the reference's walk reaches when every tile exists.  On
+    // periodic domains a diagonal tile may never have been allocated (no corner ghosts,
+    // src/UpdateTiles.f90:415-418), where the reference reads unallocated data; its cells
+    // are skipped here, as on the GPU.
+    for (int di = -1; di <= 1; ++di) {
+        int ci = i + di, col = ttk;
+        if (ci < 1) { col = g.tc(ttk).West(); ci = nX; }
+        else if (ci > nX) { col = g.tc(ttk).East(); ci = 1; }
+        for (int dj = -1; dj <= 1; ++dj) {
+            int cj = j + dj, cttk = col;
+            if (cj < 1) { cttk = g.tc(col).South(); cj = nY; }
+            else if (cj > nY) { cttk = g.tc(col).North(); cj = 1; }
+            if (!TL(im3, cttk).u.allocated()) continue;
             ComputeCellCentredTopographicDataIJ(rp, g, im3, cttk, ci, cj);
             Tile &T3 = TL(im3, cttk), &T0 = TL(im0, cttk);
             double dbc = T3.u(ibt, ci, cj) - T0.u(ibt, ci, cj);
@@ -337,12 +348,7 @@ static bool RedistributeCell(const RunSet& rp, Grid& g, int ttk, int i, int j, d
             T3.u(iw, ci, cj) = w;
             double Hnpsiold = T0.u(iHnpsi, ci, cj);
             T3.u(iHnpsi, ci, cj) = Hnpsiold * go / gn - (1.0 - rp.p.BedPorosity) * dbc / gn;
-            cj = cj + 1;
-            if (cj == nY + 1 && l < 1) { cttk = g.tc(cttk).North(); cj = 1; }
         }
-        if (j + 1 > nY) cttk = g.tc(cttk).South();
-        ci = ci + 1;
-        if (ci == nX + 1) { cttk = g.tc(cttk).East(); ci = 1; }
     }
     return true;
 }

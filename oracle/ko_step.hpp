@@ -168,6 +168,11 @@ inline void BtSourceTerm(const RunSet& rp, Grid& g, Tiles& tiles) {
             }
         int ttW = T.West(), ttE = T.East(), ttS = T.South(), ttN = T.North();
         Tile &W = TL(tiles, ttW), &E = TL(tiles, ttE), &S = TL(tiles, ttS), &N = TL(tiles, ttN);
+        // The diagonal tiles: on periodic domains one may never have been allocated (no
+        // corner ghosts, src/UpdateTiles.f90:415-418), where the reference reads unallocated
+        // data; it contributes zero here, as on the GPU.
+        auto du = [](const Tile& X, int f, int i, int j) { return X.u.allocated() ? X.u(f, i, j) : 0.0; };
+        auto de = [](const Tile& X, int i, int j) { return X.EminusD.allocated() ? X.EminusD(i, j) : 0.0; };
         Tile& SW = TL(tiles, W.South());
         Tile& SE = TL(tiles, E.South());
         Tile& NW = TL(tiles, W.North());
@@ -205,31 +210,31 @@ inline void BtSourceTerm(const RunSet& rp, Grid& g, Tiles& tiles) {
             }
         }
         {  // SW
-            double ax[4] = {SW.u(idbdx, nX, nY), W.u(idbdx, nX, 1), S.u(idbdx, 1, nY), T.u(idbdx, 1, 1)};
-            double ay[4] = {SW.u(idbdy, nX, nY), W.u(idbdy, nX, 1), S.u(idbdy, 1, nY), T.u(idbdy, 1, 1)};
+            double ax[4] = {du(SW, idbdx, nX, nY), W.u(idbdx, nX, 1), S.u(idbdx, 1, nY), T.u(idbdx, 1, 1)};
+            double ay[4] = {du(SW, idbdy, nX, nY), W.u(idbdy, nX, 1), S.u(idbdy, 1, nY), T.u(idbdy, 1, 1)};
             double gam = Gam_gradin(rp, 0.25 * KahanSumL(ax), 0.25 * KahanSumL(ay));
-            double ae[4] = {SW.EminusD(nX, nY), W.EminusD(nX, 1), S.EminusD(1, nY), T.EminusD(1, 1)};
+            double ae[4] = {de(SW, nX, nY), W.EminusD(nX, 1), S.EminusD(1, nY), T.EminusD(1, 1)};
             T.ddtExplicitBt(1, 1) = -0.25 * gam / psib * KahanSumL(ae);
         }
         {  // SE
-            double ax[4] = {S.u(idbdx, nX, nY), T.u(idbdx, nX, 1), SE.u(idbdx, 1, nY), E.u(idbdx, 1, 1)};
-            double ay[4] = {S.u(idbdy, nX, nY), T.u(idbdy, nX, 1), SE.u(idbdy, 1, nY), E.u(idbdy, 1, 1)};
+            double ax[4] = {S.u(idbdx, nX, nY), T.u(idbdx, nX, 1), du(SE, idbdx, 1, nY), E.u(idbdx, 1, 1)};
+            double ay[4] = {S.u(idbdy, nX, nY), T.u(idbdy, nX, 1), du(SE, idbdy, 1, nY), E.u(idbdy, 1, 1)};
             double gam = Gam_gradin(rp, 0.25 * KahanSumL(ax), 0.25 * KahanSumL(ay));
-            double ae[4] = {S.EminusD(nX, nY), T.EminusD(nX, 1), SE.EminusD(1, nY), E.EminusD(1, 1)};
+            double ae[4] = {S.EminusD(nX, nY), T.EminusD(nX, 1), de(SE, 1, nY), E.EminusD(1, 1)};
             T.ddtExplicitBt(nX + 1, 1) = -0.25 * gam / psib * KahanSumL(ae);
         }
         {  // NW
-            double ax[4] = {W.u(idbdx, nX, nY), NW.u(idbdx, nX, 1), T.u(idbdx, 1, nY), N.u(idbdx, 1, 1)};
-            double ay[4] = {W.u(idbdy, nX, nY), NW.u(idbdy, nX, 1), T.u(idbdy, 1, nY), N.u(idbdy, 1, 1)};
+            double ax[4] = {W.u(idbdx, nX, nY), du(NW, idbdx, nX, 1), T.u(idbdx, 1, nY), N.u(idbdx, 1, 1)};
+            double ay[4] = {W.u(idbdy, nX, nY), du(NW, idbdy, nX, 1), T.u(idbdy, 1, nY), N.u(idbdy, 1, 1)};
             double gam = Gam_gradin(rp, 0.25 * KahanSumL(ax), 0.25 * KahanSumL(ay));
-            double ae[4] = {W.EminusD(nX, nY), NW.EminusD(nX, 1), T.EminusD(1, nY), N.EminusD(1, 1)};
+            double ae[4] = {W.EminusD(nX, nY), de(NW, nX, 1), T.EminusD(1, nY), N.EminusD(1, 1)};
             T.ddtExplicitBt(1, nY + 1) = -0.25 * gam / psib * KahanSumL(ae);
         }
         {  // NE
-            double ax[3] = {T.u(idbdx, nX, nY), N.u(idbdx, nX, 1), E.u(idbdx, 1, nY) + NE.u(idbdx, 1, 1)};
-            double ay[4] = {T.u(idbdy, nX, nY), N.u(idbdy, nX, 1), E.u(idbdy, 1, nY), NE.u(idbdy, 1, 1)};
+            double ax[3] = {T.u(idbdx, nX, nY), N.u(idbdx, nX, 1), E.u(idbdx, 1, nY) + du(NE, idbdx, 1, 1)};
+            double ay[4] = {T.u(idbdy, nX, nY), N.u(idbdy, nX, 1), E.u(idbdy, 1, nY), du(NE, idbdy, 1, 1)};
             double gam = Gam_gradin(rp, 0.25 * KahanSumL(ax), 0.25 * KahanSumL(ay));
-            double ae[4] = {T.EminusD(nX, nY), N.EminusD(nX, 1), E.EminusD(1, nY), NE.EminusD(1, 1)};
+            double ae[4] = {T.EminusD(nX, nY), N.EminusD(nX, 1), E.EminusD(1, nY), de(NE, 1, 1)};
             T.ddtExplicitBt(nX + 1, nY + 1) = -0.25 * gam / psib * KahanSumL(ae);
         }
     }

@@ -145,3 +145,59 @@ def test_oracle_sources_and_activation_counts():
     assert act == sorted(act)
     assert len(act) == 4
     assert len(sim.ghost_tiles()) == 12
+
+
+def test_oracle_periodic_morphodynamics_missing_diagonal_tiles():
+    """Periodic domains get no corner ghost tiles (src/UpdateTiles.f90:415-418), yet the
+    vertex bed source and the redistribution reach the diagonal tile; the reference reads
+    unallocated data there. The oracle (like the GPU path) lets a missing diagonal tile
+    contribute nothing and skips its cells: a morphodynamic run whose active tiles have
+    missing diagonals completes with a finite, non-negative depth and bt above -EroDepth."""
+    from kestrel_gb300 import config
+    txt = """Domain:
+nXtiles = 6
+nYtiles = 6
+nXpertile = 8
+nYpertile = 8
+Xtilesize = 16
+Boundary Conditions = periodic
+Cap:
+  capX = -47.867778915771765
+  capY = -41.49383808639782
+  capRadius = 7.563777886388609
+  capHeight = 2.0165894394179498
+  capShape = para
+  capConc = 0.2917986243935994
+Parameters:
+Drag = Manning
+Erosion = On
+Eddy Viscosity = 0.01
+Solver:
+Limiter = WENO
+Tile Buffer = 3
+T end = 0.5
+Output:
+N out = 1
+Topog:
+Type = Function
+Topog function = flat
+"""
+    p = config.parse(txt).params
+    sim = _oracle.simulation(p)
+    sim.run()
+    act, gh = set(sim.active_tiles()), set(sim.ghost_tiles())
+
+    def wrap(i, j):
+        return (i - 1) % p.nXtiles + 1 + ((j - 1) % p.nYtiles) * p.nXtiles
+
+    missing = 0
+    for t in act:
+        i, j = (t - 1) % p.nXtiles + 1, (t - 1) // p.nXtiles + 1
+        missing += sum(wrap(i + a, j + b) not in act | gh for a in (-1, 1) for b in (-1, 1))
+    assert missing > 0  # the run exercised tiles whose diagonal neighbour was never allocated
+    assert sim.time[0] == p.tend
+    for t in act:
+        for f in (1, 2, 3, 4, 11):
+            assert np.isfinite(sim.field(t, f)).all()
+        assert sim.field(t, 5).min() >= -1e-14
+        assert sim.field(t, 11).min() >= -p.EroDepth
