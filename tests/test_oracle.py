@@ -201,3 +201,63 @@ Topog function = flat
             assert np.isfinite(sim.field(t, f)).all()
         assert sim.field(t, 5).min() >= -1e-14
         assert sim.field(t, 11).min() >= -p.EroDepth
+
+
+_SURFACES = [("flat", ()), ("xSlope", (-0.1,)), ("ySlope", (0.08,)), ("xySlope", (-0.1, 0.05)),
+             ("xSinSlope", (-0.1, 0.5, 0.02)), ("xHump", (-0.1, 1.0, 5.0)), ("xTanh", (-0.1, 1.0, 0.2)),
+             ("xParab", (0.002,)), ("xyParab", (0.002, 0.001))]
+
+
+def _random_input(seed):
+    """A small seeded configuration drawn over boundary conditions, cap or cube sources and
+    shapes, analytic surfaces, drag laws, erosion modes, limiters, tile sizes and buffers."""
+    rng = np.random.default_rng(seed)
+    pick = lambda xs: xs[int(rng.integers(len(xs)))]  # noqa: E731
+    surf, prm = pick(_SURFACES)
+    if rng.integers(2):
+        src = (f"Cap:\n  capX = {float(rng.uniform(-8, 8))!r}\n  capY = {float(rng.uniform(-8, 8))!r}\n"
+               f"  capRadius = {float(rng.uniform(2, 6))!r}\n  capHeight = {float(rng.uniform(0.5, 3))!r}\n"
+               f"  capShape = {pick(['flat', 'para', 'level'])}\n  capConc = {float(rng.uniform(0, 0.5))!r}")
+    else:
+        src = (f"Cube:\n  cubeX = {float(rng.uniform(-8, 8))!r}\n  cubeY = {float(rng.uniform(-8, 8))!r}\n"
+               f"  cubeLength = {float(rng.uniform(2, 8))!r}\n  cubeWidth = {float(rng.uniform(2, 8))!r}\n"
+               f"  cubeHeight = {float(rng.uniform(0.5, 3))!r}\n  cubeShape = {pick(['flat', 'level'])}\n"
+               f"  cubeConc = {float(rng.uniform(0, 0.5))!r}")
+    topog = f"Topog function = {surf}\n" + (f"Topog params = ({', '.join(repr(x) for x in prm)})\n" if prm else "")
+    return f"""Domain:
+nXtiles = 10
+nYtiles = 10
+nXpertile = {int(rng.choice([6, 8, 10]))}
+nYpertile = {int(rng.choice([6, 8, 10]))}
+Xtilesize = 12
+Boundary Conditions = {pick(['halt', 'dirichlet', 'sponge'])}
+{src}
+Parameters:
+Drag = {pick(['Chezy', 'Coulomb', 'Voellmy', 'Pouliquen', 'Edwards2019', 'Manning', 'Variable'])}
+Erosion = {pick(['Off', 'On', 'Simple', 'Fluid', 'Granular'])}
+Solver:
+Limiter = {pick(['Minmod1', 'Minmod2', 'Van Albada', 'WENO', 'None'])}
+Tile Buffer = {int(rng.integers(1, 4))}
+T end = 0.5
+Output:
+N out = 1
+Topog:
+Type = Function
+{topog}"""
+
+
+def test_oracle_random_configurations_complete():
+    """Seeded small configurations across the closure, limiter, boundary, source and surface
+    choices run to T end with a finite state, non-negative depth and bt above -EroDepth."""
+    from kestrel_gb300 import config
+    for seed in range(100, 124):
+        p = config.parse(_random_input(seed)).params
+        sim = _oracle.simulation(p)
+        sim.run()
+        assert sim.time[0] == p.tend, seed
+        for t in sim.active_tiles():
+            for f in (1, 2, 3, 4, 11):
+                assert np.isfinite(sim.field(t, f)).all(), (seed, t, f)
+            assert sim.field(t, 5).min() >= -1e-14, seed
+            if p.MorphodynamicsOn:
+                assert sim.field(t, 11).min() >= -p.EroDepth, seed
