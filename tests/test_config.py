@@ -1,5 +1,6 @@
 """Input-file parsing: the reference's keys and defaults (src/*Settings.f90, Parameters.f90)."""
 import math
+import os
 
 import pytest
 
@@ -89,3 +90,21 @@ def test_every_reference_input_parses_and_1d_grids_are_refused():
             assert rc == abi.KG_OK, (name, O.ko_last_error(None))
             O.ko_destroy(h)
     assert n1d == 9
+
+
+def test_reader_line_rules():
+    """The reference's reader rules (src/Input.f90:91-123, :205-212): leading blanks
+    ignored, '#' ends a line's content, lines starting with '%' or '#' are comments, a line
+    with ':' names a block (text after the colon dropped); CRLF files read the same."""
+    import cases
+    base = open(os.path.join(cases.INPUTS, "Input_flux_hydro_2d.txt")).read()
+    p0 = bytes(config.parse(base).params)
+    variants = [
+        base.replace("nXtiles = 40", "nXtiles = 40   # forty tiles").replace("Chezy Co = 0.04", "Chezy Co = 0.04 # drag"),
+        "# header\n% another\n" + base.replace("Domain:", "# the domain\nDomain:"),
+        base.replace("nXtiles = 40", "\t   nXtiles = 40").replace("Domain:", "   Domain:"),
+        base.replace("Domain:", "Domain: the grid"),
+        base.replace("\n", "\r\n"),
+    ]
+    for v in variants:
+        assert bytes(config.parse(v).params) == p0
