@@ -261,3 +261,46 @@ def test_oracle_random_configurations_complete():
             assert sim.field(t, 5).min() >= -1e-14, seed
             if p.MorphodynamicsOn:
                 assert sim.field(t, 11).min() >= -p.EroDepth, seed
+
+
+@pytest.mark.parametrize("drag,limiter,erosion", [("Edwards2019", "WENO", "On"), ("Pouliquen", "Van Albada", "On"),
+                                                  ("Manning", "None", "Off"), ("Voellmy", "Minmod2", "On")])
+def test_oracle_static_tile_independence(drag, limiter, erosion):
+    """check_identical_simulations (tests/testlib.jl:363-407) in its static form: with every
+    tile active from the start (a cap over the whole periodic domain) the printed state is
+    the same for 10- and 20-cell tiles, to the last printed digit (the reference asks 1e-13),
+    for every closure, limiter and erosion choice."""
+    from kestrel_gb300 import config
+    out = []
+    for ntiles, nper in ((8, 10), (4, 20)):
+        txt = f"""Domain:
+nXtiles = {ntiles}
+nYtiles = {ntiles}
+nXpertile = {nper}
+nYpertile = {nper}
+Xtilesize = {float(nper)}
+Boundary Conditions = periodic
+Cap:
+  capX = 0
+  capY = 0
+  capRadius = 100
+  capHeight = 1.3
+  capShape = para
+  capConc = 0.2
+Parameters:
+Drag = {drag}
+Erosion = {erosion}
+Solver:
+Limiter = {limiter}
+T end = 0.5
+Output:
+N out = 1
+Topog:
+Type = Function
+Topog function = flat
+"""
+        sim = _oracle.simulation(config.parse(txt).params)
+        sim.run()
+        assert len(sim.active_tiles()) == ntiles * ntiles
+        out.append(_sorted(_printed(_rows(sim))))
+    assert np.array_equal(out[0], out[1])
