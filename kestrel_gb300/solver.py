@@ -92,12 +92,12 @@ class Simulation:
         self._check(self._f("upload_raster")(self.h, v.ctypes.data_as(C.POINTER(C.c_double)), C.byref(g)))
 
     def load_state(self, ids, state: np.ndarray, bt_vertex: np.ndarray | None, t: float):
-        """kg_load_state: restart from saved tiles (state (n, 4, nY, nX): w, rhoHnu, rhoHnv,
+        """load_state: restart from saved tiles (state (n, 4, nY, nX): w, rhoHnu, rhoHnv,
         Hnpsi; bt_vertex (n, nY+1, nX+1) or None) at time t, instead of loading sources."""
         ids = (C.c_int32 * len(ids))(*ids)
         st = np.ascontiguousarray(state, dtype=np.float64)
         bt = None if bt_vertex is None else np.ascontiguousarray(bt_vertex, dtype=np.float64)
-        f = self.lib.kg_load_state
+        f = self._f("load_state")
         f.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                       C.c_double]
         f.restype = C.c_int

@@ -192,13 +192,15 @@ def read_snapshot(path: str, nX: int, nY: int):
     return out, topo
 
 
-def restart_from_snapshot(lib, params, path: str, t: float, precision: int = 0, b0: np.ndarray | None = None):
+def restart_from_snapshot(lib, params, path: str, t: float, precision: int = 0, b0: np.ndarray | None = None,
+                          prefix: str = "kg"):
     """A new simulation restarted from snapshot `path` (and `path`_topo) at time t, as
     LoadInitialCondition does (src/Restart.f90:55-328): the saved tiles are activated in
-    order with their w, momenta, Hnpsi and vertex bt; the running maxima start afresh."""
+    order with their w, momenta, Hnpsi and vertex bt; the running maxima start afresh.
+    `lib` is a loaded library (None: the GPU library) and `prefix` its entry-point prefix."""
     from . import lib as _lib
     sim = _lib.simulation(params, precision=precision, b0=b0, load_sources=False) if lib is None else \
-        Simulation(lib, "kg", params, precision=precision, b0=b0, load_sources=False)
+        Simulation(lib, prefix, params, precision=precision, b0=b0, load_sources=False)
     cells, topo = read_snapshot(path, params.nXpertile, params.nYpertile)
     ids = sorted(cells)
     state = np.stack([np.stack([cells[t_]["w"], cells[t_]["x_flux"], cells[t_]["y_flux"], cells[t_]["Hnpsi"]])

@@ -596,10 +596,11 @@ static void IntegrateStep(Sim& s, double tend) {
 }
 
 // ---------------------------------------------------------------- SetSources.f90 (2D)
-static void LoadSourceConditions(Sim& s) {
+static void LoadSourceConditions(Sim& s, bool restart = false) {
     RunSet& rp = s.rp;
     Grid& g = s.g;
-    const kg_params& P = rp.p;
+    kg_params P = rp.p;
+    if (restart) P.nCaps = P.nCubes = 0;  // caps and cubes are not placed again on a restart
     for (auto& S : rp.FluxSources) S.NumCellsInSrc = 0;
     double rhow = rp.rhow, rhos = rp.rhos;
     for (int i = 1; i <= rp.nXtiles; ++i)
@@ -699,6 +700,46 @@ static void LoadSourceConditions(Sim& s) {
 }
 
 // CalculateVolume, src/Output.f90:617-737: the four compensated sums times dx*dy.
+// LoadInitialCondition (src/Restart.f90:55-145, the txt reader :147-289) followed by the
+// restart pass of LoadSourceConditions (main.f90:124-126): the saved tiles are activated
+// in order with their conserved fields and vertex bt, then activated in restart mode (w
+// and bt kept), their interfacial topography rebuilt, and the flux sources flagged and
+// counted again.  The reference reads the cell bt and slopes from the file at print
+// precision; here they are rebuilt from the vertices, as the GPU engine's kg_load_state
+// does.  state[k][4][nY][nX] holds w, rhoHnu, rhoHnv, Hnpsi; btv[k][nY+1][nX+1] the
+// vertex bt (NULL keeps the set-up's zero).
+static void LoadState(Sim& s, const int32_t* ids, int n, const double* state, const double* btv, double t) {
+    RunSet& rp = s.rp;
+    Grid& g = s.g;
+    const int nX = rp.nXpertile, nY = rp.nYpertile;
+    const size_t SC = (size_t)nX * nY, SV = (size_t)(nX + 1) * (nY + 1);
+    for (int k = 0; k < n; ++k) {  // :190-201
+        if (!TileInBounds(g, ids[k])) throw KoError(KG_ERR_PARAM, "tile id out of range");
+        AddToActiveTiles(g, ids[k]);
+        AllocateTile(rp, g, ids[k]);
+    }
+    for (int k = 0; k < n; ++k) {  // :203-260 and :270-283
+        Tile& T = g.tc(ids[k]);
+        const double* q = state + (size_t)k * 4 * SC;
+        for (int j = 1; j <= nY; ++j)
+            for (int i = 1; i <= nX; ++i) {
+                size_t c = (size_t)(j - 1) * nX + (i - 1);
+                T.u(iw, i, j) = q[c];
+                T.u(irhoHnu, i, j) = q[SC + c];
+                T.u(irhoHnv, i, j) = q[2 * SC + c];
+                T.u(iHnpsi, i, j) = q[3 * SC + c];
+            }
+        if (btv)
+            for (int j = 1; j <= nY + 1; ++j)
+                for (int i = 1; i <= nX + 1; ++i) T.bt(i, j) = btv[(size_t)k * SV + (size_t)(j - 1) * (nX + 1) + (i - 1)];
+        ComputeCellCentredTopographicData(rp, g, g.tileContainer, ids[k]);
+    }
+    for (int id : std::vector<int>(g.activeTiles)) ActivateTile(rp, g, id, true);  // :286-289
+    for (int id : g.activeTiles) ComputeInterfacialTopographicData(rp, g, g.tileContainer, id);  // :140-143
+    LoadSourceConditions(s, true);
+    g.t = t;
+}
+
 static void CalculateVolume(Sim& s, double out[4]) {
     RunSet& rp = s.rp;
     Grid& g = s.g;
@@ -885,6 +926,15 @@ int ko_load_sources(ko_ctx* c) {
     if (c->s.rp.p.topog == KG_TOPO_UPLOAD && c->s.g.b0_upload.empty()) { c->s.err = "no topography uploaded"; return KG_ERR_STATE; }
     if (c->s.rp.p.topog == KG_TOPO_RASTER && c->s.g.raster.values.empty()) { c->s.err = "no raster uploaded"; return KG_ERR_STATE; }
     KO_TRY(c, { ko::LoadSourceConditions(c->s); c->s.sources_loaded = true; })
+}
+int ko_load_state(ko_ctx* c, const int32_t* ids, int32_t n, const double* state, const double* bt_vertex, double t) {
+    if (!c || !ids || !state || n < 1) return KG_ERR_PARAM;
+    if (c->s.sources_loaded) { c->s.err = "ko_load_state needs a context with nothing loaded"; return KG_ERR_STATE; }
+    for (int k = 1; k < n; ++k)
+        if (ids[k] <= ids[k - 1]) { c->s.err = "ko_load_state: tile ids must be strictly increasing"; return KG_ERR_PARAM; }
+    if (c->s.rp.p.topog == KG_TOPO_UPLOAD && c->s.g.b0_upload.empty()) { c->s.err = "no topography uploaded"; return KG_ERR_STATE; }
+    if (c->s.rp.p.topog == KG_TOPO_RASTER && c->s.g.raster.values.empty()) { c->s.err = "no raster uploaded"; return KG_ERR_STATE; }
+    KO_TRY(c, { ko::LoadState(c->s, ids, n, state, bt_vertex, t); c->s.sources_loaded = true; })
 }
 int ko_step(ko_ctx* c, double t_stop, kg_step_stats* st) {
     int64_t r0 = c->s.rejected, s0 = c->s.steps, cu0 = c->s.cell_updates;

@@ -586,14 +586,15 @@ inline void AddToActiveTiles(Grid& g, int k) {  // :81-117
         }
     }
 }
-inline void ActivateTile(const RunSet& rp, Grid& g, int k) {  // :342-384
+inline void ActivateTile(const RunSet& rp, Grid& g, int k, bool restart = false) {  // :342-384
     Tile& T = g.tc(k);
     T.isGhostTile = false;
-    for (int j = 1; j <= rp.nYpertile; ++j)
-        for (int i = 1; i <= rp.nXpertile; ++i) {
-            T.u(iw, i, j) = T.u(ib0, i, j);
-            T.u(ibt, i, j) = 0.0;
-        }
+    if (!restart)  // a restart keeps the loaded w and bt (:361-370)
+        for (int j = 1; j <= rp.nYpertile; ++j)
+            for (int i = 1; i <= rp.nXpertile; ++i) {
+                T.u(iw, i, j) = T.u(ib0, i, j);
+                T.u(ibt, i, j) = 0.0;
+            }
     AddGhostTiles(rp, g, k);
     Tiles& tc = g.tileContainer;
     ComputeInterfacialTopographicData(rp, g, tc, k);
