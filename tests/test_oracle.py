@@ -304,3 +304,46 @@ Topog function = flat
         assert len(sim.active_tiles()) == ntiles * ntiles
         out.append(_sorted(_printed(_rows(sim))))
     assert np.array_equal(out[0], out[1])
+
+
+def _halt_input(cap_x, tend):
+    return f"""Domain:
+nXtiles = 6
+nYtiles = 6
+nXpertile = 8
+nYpertile = 8
+Xtilesize = 8
+Boundary Conditions = halt
+Cap:
+  capX = {cap_x!r}
+  capY = 0
+  capRadius = 3
+  capHeight = 2
+  capShape = flat
+  capConc = 0
+Solver:
+T end = {tend!r}
+Tile Buffer = 2
+Output:
+N out = 1
+Topog:
+Type = Function
+Topog function = flat
+"""
+
+
+def test_oracle_halt_edge_is_fatal():
+    """Under 'halt', adding a tile on the domain edge is the reference's fatal error
+    (src/UpdateTiles.f90:61-69): KG_ERR_HALT_EDGE, whether the cap itself covers an edge
+    tile or the flow reaches one."""
+    from kestrel_gb300 import abi, config
+    from kestrel_gb300.solver import KestrelError
+    # the cap covers cells of the west edge tile: refused at source placement
+    with pytest.raises(KestrelError) as e:
+        _oracle.simulation(config.parse(_halt_input(-20.5, 1.0)).params)
+    assert abi.KG_ERR[e.value.code] == "KG_ERR_HALT_EDGE" and "outside the domain" in str(e.value)
+    # the cap sits in an interior tile next to the edge tile; the flow reaches it
+    sim = _oracle.simulation(config.parse(_halt_input(-13.0, 5.0)).params)
+    with pytest.raises(KestrelError) as e:
+        sim.run()
+    assert abi.KG_ERR[e.value.code] == "KG_ERR_HALT_EDGE"
