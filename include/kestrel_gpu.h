@@ -34,15 +34,17 @@ extern "C" {
 /* ---- status codes (replace FatalErrorMessage / exit(1), src/Messages.f90:56-90) ---- */
 #define KG_OK                 0
 #define KG_ERR_PARAM         -1  /* invalid parameter value (src/Parameters.f90 FatalError_*) */
-#define KG_ERR_OOM           -2  /* device or host allocation failed */
+#define KG_ERR_OOM           -2  /* device memory (cudaErrorMemoryAllocation) or host memory ran out */
 #define KG_ERR_HALT_EDGE     -3  /* flow reached the domain edge under 'halt' (src/UpdateTiles.f90:61-69) */
-#define KG_ERR_NAN           -4  /* non-finite state detected */
+#define KG_ERR_NAN           -4  /* reserved: like the reference, a step does not scan the state for
+                                     non-finite values; a non-finite advised dt gives KG_ERR_DT */
 #define KG_ERR_CUDA          -5  /* CUDA runtime error */
 #define KG_ERR_UNSUPPORTED   -6  /* configuration outside the implemented path (e.g. 1D grids) */
 #define KG_ERR_STATE         -7  /* call out of order (e.g. stepping before sources are loaded) */
-#define KG_ERR_DT            -8  /* time step collapsed (dt <= 0 or too many refinements) */
+#define KG_ERR_DT            -8  /* time step collapsed: dt <= 0 or not finite, or 100000
+                                     refinements of one step (the reference would loop on) */
 #define KG_ERR_NOT_FOUND     -9  /* requested tile is not active */
-#define KG_ERR_TIMEOUT      -10  /* a bounded device wait expired */
+#define KG_ERR_TIMEOUT      -10  /* reserved: no kernel of the library waits on a flag */
 
 /* ---- runtime closure selections (procedure pointers in the reference) ---- */
 /* Drag: src/Parameters.f90:222-247, src/Closures.f90:365-558 */

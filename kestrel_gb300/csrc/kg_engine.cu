@@ -78,11 +78,14 @@ struct KgError : std::runtime_error {
     KgError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
+// A failed CUDA call ends the entry point with its status: KG_ERR_OOM when device memory
+// ran out, KG_ERR_CUDA otherwise.
 #define CK(call)                                                                          \
     do {                                                                                  \
         cudaError_t e_ = (call);                                                          \
         if (e_ != cudaSuccess)                                                            \
-            throw KgError(KG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+            throw KgError(e_ == cudaErrorMemoryAllocation ? KG_ERR_OOM : KG_ERR_CUDA,     \
+                          std::string(#call) + ": " + cudaGetErrorString(e_));            \
     } while (0)
 
 struct TileMeta {
