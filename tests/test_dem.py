@@ -86,6 +86,20 @@ def test_ascii_grid_round_trip(tmp_path):
     assert back["center"] == (E0, N0)
 
 
+def test_ascii_grid_header_forms(tmp_path):
+    """The centre form of the ESRI header (xllcenter/yllcenter: half a cell inside the
+    corner), a grid without NODATA_value (NaN, which no value equals), and a grid whose
+    value count disagrees with its header."""
+    path = tmp_path / "c.asc"
+    path.write_text("ncols 3\nnrows 2\nxllcenter 101.0\nyllcenter 201.0\ncellsize 2.0\n1 2 3\n4 5 6\n")
+    r = dem.read_ascii_grid(str(path))
+    assert r["origin"] == (100.0, 204.0) and r["pixel"] == (2.0, -2.0)
+    assert np.isnan(r["nodata"]) and r["values"].tolist() == [[1, 2, 3], [4, 5, 6]]
+    path.write_text("ncols 3\nnrows 2\nxllcorner 0\nyllcorner 0\ncellsize 1\n1 2 3\n4 5\n")
+    with pytest.raises(ValueError, match="expected 6 values, found 5"):
+        dem.read_ascii_grid(str(path))
+
+
 def test_oracle_reproduces_a_plane():
     """Bicubic_r's finite-difference derivatives are exact for a linear surface and its
     Hermite patch is then that surface, so every vertex height is the plane at the vertex
