@@ -862,9 +862,15 @@ double advised(kg_ctx& c, unsigned long long bits, int substep) {
     return m;
 }
 
+// Before the constant bank is rewritten for context c, the kernels the previous owner
+// queued on another stream (which read the bank) must have finished.
+void wait_const_owner(kg_ctx& c) {
+    if (g_const_owner && g_const_owner != &c && g_const_owner->st != c.st) CK(cudaStreamSynchronize(g_const_owner->st));
+}
+
 void bind_constants(kg_ctx& c) {
     if (g_const_owner == &c) return;
-    if (g_const_owner && g_const_owner->st != c.st) CK(cudaStreamSynchronize(g_const_owner->st));
+    wait_const_owner(c);
     CK(set_constants(c.dp, c.dsrc.empty() ? nullptr : c.dsrc.data(), (int)c.dsrc.size(), c.st));
     g_const_owner = &c;
 }
@@ -1503,6 +1509,7 @@ void upload_sources(kg_ctx& c) {
         CK(cudaMalloc(&c.d_src, ds.size() * sizeof(DevSource)));
         CK(kg_cpy(c, c.d_src, ds.data(), ds.size() * sizeof(DevSource), cudaMemcpyHostToDevice));
     }
+    wait_const_owner(c);
     CK(set_constants(c.dp, ds.data(), (int)ds.size(), c.st));
     g_const_owner = &c;
     sync(c);
@@ -1666,6 +1673,7 @@ void setup(kg_ctx& c, const kg_params& p) {
     CK(cudaMalloc(&c.d_vol, 4 * sizeof(double)));
     CK(cudaMallocHost(&c.h_ctl, sizeof(kg_ctx::Ctl)));
     c.h_cfl = c.h_ctl->cfl;
+    wait_const_owner(c);
     CK(set_constants(c.dp, nullptr, 0, c.st));
     g_const_owner = &c;
     sync(c);

@@ -75,6 +75,11 @@ extern "C" int kg_hydraulic_rhs_noalloc(kg_ctx* c, double t, int32_t substep, do
     NoAllocScratch* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch, c->err);
     if (rc != KG_OK) return rc;
+    // The pass reads the neighbour-slot table.  After an activation or a load its corner
+    // entries are refreshed only lazily (before the next step); refresh the whole table
+    // now, the way the allocating entry point does.  This copies into the table the
+    // context already owns and allocates nothing on the device.
+    if (c->blocks_dirty) KG_GUARD(c, refresh_all_nbrs(*c));
     // The block list of the active tiles, built on the host exactly as the context's own
     // pass builds it.
     const int BSZ = 16;
@@ -93,8 +98,9 @@ extern "C" int kg_hydraulic_rhs_noalloc(kg_ctx* c, double t, int32_t substep, do
             for (int x0 = 0; x0 < c->nX; x0 += BSZ) host.push_back(kg::BlockDesc{s, x0, y0, id});
     }
     unsigned long long huge_bits = 0x7FEFFFFFFFFFFFFFull, bits = 0;
-    cudaError_t e = cudaMemcpyAsync(scratch->blocks, host.data(), host.size() * sizeof(kg::BlockDesc), cudaMemcpyHostToDevice, c->st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&scratch->cfl_min, &huge_bits, sizeof(huge_bits), cudaMemcpyHostToDevice, c->st);
+    // Copies go through kg_cpy so that kg_get_transfer_bytes counts them.
+    cudaError_t e = kg_cpy(*c, scratch->blocks, host.data(), host.size() * sizeof(kg::BlockDesc), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = kg_cpy(*c, &scratch->cfl_min, &huge_bits, sizeof(huge_bits), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         c->err = std::string("kg_hydraulic_rhs_noalloc: ") + cudaGetErrorString(e);
         return KG_ERR_CUDA;
@@ -110,7 +116,7 @@ extern "C" int kg_hydraulic_rhs_noalloc(kg_ctx* c, double t, int32_t substep, do
     S.t_grid = c->t;
     S.cfl_min = &scratch->cfl_min;
     e = kg::launch_hydro(c->A, scratch->blocks, (int)host.size(), S, c->st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, &scratch->cfl_min, sizeof(bits), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = kg_cpy(*c, &bits, &scratch->cfl_min, sizeof(bits), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     if (e != cudaSuccess) {
         c->err = std::string("kg_hydraulic_rhs_noalloc: ") + cudaGetErrorString(e);

@@ -124,6 +124,32 @@ Topog function = flat
     return p, b0
 
 
+def morpho_flux_window(size: int = 256, tile: int = 32, tend: float = 600.0, nout: int = 1, seed: int = 12345,
+                       src_from_south: float = 300.0):
+    """The 2048^2 morphodynamic flux release cut down to a size x size window of its own
+    terrain: the same seeded 2049^2 vertex grid (same dx = 5 m, relief, tilt), of which the
+    window holds the source with `src_from_south` metres of terrain south of it and the
+    rest downhill (north); the same source (radius 6 m, hydrograph 0 -> 200 -> 0 m^3/s over
+    300 s, concentration 0.3), Voellmy drag, mixed erosion with 2 m erodible depth, eddy
+    viscosity 1e-2, sponge edges, in tiles of tile^2 cells.  Returns (params, b0)."""
+    pf, bf = morpho_flux_2048(tend=tend, nout=nout, seed=seed)
+    dx = pf.Xtilesize / pf.nXpertile
+    half_full = 0.5 * pf.nXtiles * pf.Xtilesize
+    sx, sy = pf.sources[0].x, pf.sources[0].y
+    L = size * dx
+    x_lo, y_lo = sx - 0.5 * L, sy - src_from_south
+    c0, r0 = int(round((x_lo + half_full) / dx)), int(round((y_lo + half_full) / dx))
+    b0 = np.ascontiguousarray(bf[r0:r0 + size + 1, c0:c0 + size + 1])
+    p, _ = morpho_flux_2048(tend=tend, nout=nout, seed=seed)
+    p.nXtiles = p.nYtiles = size // tile
+    p.nXpertile = p.nYpertile = tile
+    p.Xtilesize = p.Ytilesize = tile * dx
+    # window centred at (0, 0): the source keeps its place on the terrain
+    p.sources[0].x = sx - (c0 * dx - half_full + 0.5 * L)
+    p.sources[0].y = sy - (r0 * dx - half_full + 0.5 * L)
+    return p, b0
+
+
 WORKLOADS = {
     "cap_release_256_fp64": dict(
         desc="plain FP64 2D hydraulic cap release, 256x256 cells, dx=1 m, 5 deg slope, cap r=40 m h=4 m at "
