@@ -39,7 +39,13 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# Algorithmic bytes per cell-update (minimal traffic: each stage's inputs read once, its
+# outputs written once; the bed is the two vertex fields).  A hydraulic step is 4 fused
+# passes over 46 field accesses per cell; a morphodynamic Strang step H.M.H counts 2
+# cell-updates and adds the 36 accesses of the M operator.
 ALG_BYTES = {"fp64_hydro": 368.0, "fp64_morpho": 512.0, "fp32_hydro": 252.0, "fp32_morpho": 366.0}
+# One fused hydraulic pass: a quarter of the hydraulic step, per cell of the pass.
+ALG_PASS_BYTES = {"fp64": ALG_BYTES["fp64_hydro"] / 4.0, "fp32": ALG_BYTES["fp32_hydro"] / 4.0}
 
 
 def measured_peaks():
@@ -144,13 +150,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(params, b0=None, seconds=15.0, max_steps=100000):
-    """Oracle timed on a bounded sample: accepted steps from t = 0 until ~`seconds`."""
+def cpu_baseline(params, b0=None, seconds=15.0, max_steps=100000, snapshot=None):
+    """Oracle timed on a bounded sample: accepted steps until ~`seconds`, from t = 0 or,
+    with a snapshot (the GPU run's state at the end of its spin-up), from that state."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle
     from kestrel_gb300 import abi
+    from kestrel_gb300.solver import Simulation
     L = _oracle.load()
-    sim = _oracle.simulation(params, b0=b0)
+    if snapshot is not None:
+        sim = Simulation(L, "ko", params, b0=b0, load_sources=False)
+        sim.load_state(*snapshot)
+    else:
+        sim = _oracle.simulation(params, b0=b0)
+    t_start = sim.time[0]
     total_cu, total_s, steps = 0, 0.0, 0
     rc = C.c_int32(0)
     while total_s < seconds and steps < max_steps:
@@ -164,7 +177,8 @@ def cpu_baseline(params, b0=None, seconds=15.0, max_steps=100000):
         if sim.time[0] >= params.tend:
             break
     return {"value": total_cu / total_s if total_s > 0 else None, "unit": "cell-updates/s", "cores": 1,
-            "host_cores": os.cpu_count(), "kind": "port", "sample": f"first {steps} accepted steps from t=0 (t_end {sim.time[0]:.3f} s), "
+            "host_cores": os.cpu_count(), "kind": "port", "sample": f"{steps} accepted steps from t={t_start:.3f} s to {sim.time[0]:.3f} s"
+            + (f" (from the GPU run's state at the end of its spin-up, {len(snapshot[0])} tiles)" if snapshot else "") + ", "
             f"{total_cu} cell-updates in {total_s:.2f} s, serial C++ restatement (oracle)"}
 
 
@@ -174,8 +188,31 @@ def run_reference(args, wl):
     p, b0 = made if isinstance(made, tuple) else (made, None)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle
+    from kestrel_gb300.solver import Simulation
     L = _oracle.load()
-    sim = _oracle.simulation(p, b0=b0)
+    spin = wl.get("spinup", 0.0) if args.spinup is None else args.spinup
+    start = "t=0"
+    snap = None
+    if spin > 0.0:
+        # The same window as the GPU arm: the state at the end of the spin-up, integrated by
+        # the GPU's FP64 plain path (equal to the oracle within 1e-10 on the parity tests),
+        # is loaded into the oracle (ko_load_state, LoadInitialCondition) and the oracle's
+        # own steps are timed from there.  Without a GPU the oracle starts at t = 0.
+        try:
+            from kestrel_gb300 import abi as A0, lib
+            g = lib.simulation(p, precision=A0.PREC_FP64, b0=b0)
+            g.integrate_to(spin)
+            snap = take_snapshot(g)
+            g.close()
+            start = (f"t={snap[3]:.3f} s ({len(snap[0])} tiles): the state integrated to the end of the spin-up by the "
+                     f"FP64 GPU path and loaded into the oracle")
+        except Exception as e:  # no GPU: time the same configuration from its start
+            start = f"t=0 (no spin-up state: {e!r})"
+    if snap is not None:
+        sim = Simulation(L, "ko", p, b0=b0, load_sources=False)
+        sim.load_state(*snap)
+    else:
+        sim = _oracle.simulation(p, b0=b0)
     rc = C.c_int32(0)
     from kestrel_gb300 import abi as A
     for _ in range(args.warmup):
@@ -191,9 +228,11 @@ def run_reference(args, wl):
     line = {"metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(n, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "desc": wl["desc"], "l2": "n/a (CPU)"},
+            "config": {"workload": args.workload, "desc": wl["desc"], "active_cells_end": len(sim.active_tiles()) * p.nXpertile * p.nYpertile,
+                       "l2": "n/a (CPU)", "parallelism": "single"},
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
-                             "sample": f"{n} accepted steps after {args.warmup} warm-up steps, serial C++ restatement"},
+                             "sample": f"{n} accepted steps after {args.warmup} warm-up steps from {start}, serial C++ "
+                                       f"restatement (oracle)"},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -302,8 +341,8 @@ def run_ensemble(args):
             "batch": {"kernel_launches_per_step": (l1 - l0) / args.steps, "rounds_per_step": (r1 - r0) / args.steps,
                       "device_gb": hbm / 1e9, "autotune_s": t_tune, "add_s": t_add},
             "clocks": clk}
-    print(json.dumps(line))
     b.close()
+    return line
 
 
 def run_serve(args):
@@ -330,7 +369,85 @@ def run_serve(args):
                        "tend_s": [args.tend_min, args.tend_max], "hbm_budget_gb": args.budget_gb,
                        "sides": [256, 512, 1024, 2048]},
             "serve": rep, "clocks": clk}
-    print(json.dumps(line))
+    return line
+
+
+def extras_ensemble(args):
+    """configs[3] beside the headline: the batched ensemble of --members members, its
+    device-timed and host-clock throughput and round shape."""
+    import copy
+    a = copy.copy(args)
+    a.steps, a.warmup = 20, 3
+    r = run_ensemble(a)
+    return {"workload": r["config"]["workload"], "value": r["value"], "unit": r["unit"], "e2e": r["e2e"]["value"],
+            "ms_per_round": r["ms_per_step"], "rounds": r["steps"], "members": r["config"]["members"],
+            "morpho_members": r["config"]["morpho_members"], "sides": r["config"]["sides"], "tiles": r["config"]["tiles"],
+            "batch": r["batch"], "dtype": "f32", "clocks": r.get("clocks")}
+
+
+def extras_serve(args):
+    """configs[4] beside the headline: the served request stream (Poisson arrivals at
+    --rate per s, sides 256-2048, HBM budget --budget-gb), with the end times scaled by
+    --serve-tend-scale so that the whole stream is served within the default run."""
+    import copy
+    a = copy.copy(args)
+    a.tend_min, a.tend_max = args.tend_min * args.serve_tend_scale, args.tend_max * args.serve_tend_scale
+    r = run_serve(a)
+    rep = r["serve"]
+    return {"workload": "serve_fp32", "requests": a.requests, "rate_per_s": a.rate,
+            "tend_s": [a.tend_min, a.tend_max], "tend_scale": args.serve_tend_scale,
+            "latency_p50_s": rep.get("latency_p50_s"), "latency_p99_s": rep.get("latency_p99_s"),
+            "solves_per_s": rep.get("solves_per_s"), "cell_updates_per_s": rep.get("cell_updates_per_s"),
+            "makespan_s": rep.get("makespan_s"), "peak_members": rep.get("peak_members"),
+            "peak_budget_gb": rep.get("peak_budget_gb"), "hbm_budget_gb": a.budget_gb, "dtype": "f32",
+            "note": "host clock from the first arrival; end times of the configuration ([60, 600] s) scaled by "
+                    f"{args.serve_tend_scale} so that the stream is served within the default run"}
+
+
+def run_sparse_window(args, t_window: float = 290.0, steps: int = 20):
+    """The large sparse configuration (8192^2 cells in 16,384 tiles of 64^2, three seeded
+    flux sources, Pouliquen drag, morphodynamics; FP32 form) timed near its end time:
+    an untimed spin-up to t_window (the active-tile count recorded every 20 s), then
+    `steps` accepted steps device-timed as the headline (CUDA events on the library's
+    stream, L2 flushed between steps)."""
+    import torch
+    from kestrel_gb300 import lib, workloads
+    L = lib.load()
+    wl = workloads.WORKLOADS["sparse_8192_fp32"]
+    p, b0 = wl["params"]()
+    t0 = time.perf_counter()
+    sim = lib.simulation(p, precision=wl["prec"], b0=b0)
+    timeline = spin_up(sim, p, t_window, 20.0)
+    spin_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        sim.step(p.tend)
+    torch.cuda.synchronize()
+    evs, cu, n = [], 0, 0
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        st = sim.step(p.tend)
+        e1.record(stream)
+        evs.append((e0, e1))
+        cu += st.cell_updates
+        n += st.steps
+        if sim.time[0] >= p.tend:
+            break
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    act = len(sim.active_tiles())
+    t_end = sim.time[0]
+    sim.close()
+    total = p.nXtiles * p.nYtiles
+    return {"workload": "sparse_8192_fp32", "value": cu / (ms / 1e3) if ms > 0 else None, "unit": "cell-updates/s",
+            "steps": n, "ms_per_step": ms / max(n, 1), "t_window": [t_window, round(t_end, 3)],
+            "active_tiles": act, "active_percent": round(100.0 * act / total, 3), "active_timeline": timeline,
+            "spinup_wall_s": spin_s, "dtype": "f32",
+            "note": "device-timed steps after an untimed spin-up to the window; L2 flushed between steps"}
 
 
 def reduce_replicas(seconds, cell_updates, dist=None, device="cpu"):
@@ -487,6 +604,22 @@ def fp64_plain(args, wname, snapshot=None):
         n += st.steps
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in evs)
+    # end to end through the C ABI: the same number of steps on the host clock (each
+    # returns its statistics), then the conserved fields of every active tile read back
+    xb0 = (C.c_int64 * 2)()
+    L.kg_get_transfer_bytes(sim.h, xb0)
+    cu_e, n_e = 0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = sim.step(p.tend)
+        cu_e += st.cell_updates
+        n_e += st.steps
+    for t in sim.active_tiles():
+        for f in (1, 2, 3, 4):
+            sim.field(t, f)
+    e2e_s = time.perf_counter() - t0
+    xb1 = (C.c_int64 * 2)()
+    L.kg_get_transfer_bytes(sim.h, xb1)
     active = len(sim.active_tiles())
     pass_ms = None
     if timed:
@@ -495,7 +628,10 @@ def fp64_plain(args, wname, snapshot=None):
             pass_ms = kms.value / kpasses.value
     sim.close()
     out = {"workload": wname, "value": cu / (ms / 1e3), "unit": "cell-updates/s", "steps": n, "ms_per_step": ms / max(n, 1),
-           "active_tiles_end": active, "pass_ms": pass_ms}
+           "active_tiles_end": active, "pass_ms": pass_ms,
+           "e2e": {"value": cu_e / e2e_s if e2e_s > 0 else None, "unit": "cell-updates/s",
+                   "h2d_bytes_per_step": (xb1[0] - xb0[0]) / max(n_e, 1), "d2h_bytes_per_step": (xb1[1] - xb0[1]) / max(n_e, 1),
+                   "note": f"host clock around {n_e} further kg_step calls, then the read-back of the conserved fields"}}
     try:  # the FP64 pass against its FP64 pipe; the clock is the GPU's maximum (not sampled here)
         cells = cu / max(n, 1) / (2.0 if p.MorphodynamicsOn else 1.0)
         n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
@@ -525,6 +661,8 @@ def main():
     ap.add_argument("--tend-min", type=float, default=60.0)
     ap.add_argument("--tend-max", type=float, default=600.0)
     ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-tend-scale", type=float, default=0.1, help="served stream beside the headline: end-time scale")
+    ap.add_argument("--no-extras", action="store_true", help="headline only (no sparse, ensemble and served keys)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -533,9 +671,11 @@ def main():
             return
         return run_reference_members(args)
     if args.workload == "ensemble_fp32" and args.impl == "ours":
-        return run_ensemble(args)
+        print(json.dumps(run_ensemble(args)))
+        return
     if args.workload == "serve_fp32" and args.impl == "ours":
-        return run_serve(args)
+        print(json.dumps(run_serve(args)))
+        return
     if args.workload == "dem_2048":
         if int(os.environ.get("RANK", "0")) != 0:
             return
@@ -570,7 +710,7 @@ def main():
     for _ in range(args.warmup):
         sim.step(p.tend)
     torch.cuda.synchronize()
-    snapshot = take_snapshot(sim) if wl.get("twin_restart") else None
+    snapshot = take_snapshot(sim) if (wl.get("twin_restart") or spin > 0.0) else None
     L.kg_set_kernel_timing(sim.h, 1)
     launches0 = L.kg_kernel_launches(sim.h)
     clocks = ClockSampler(local)
@@ -656,13 +796,16 @@ def main():
         key = key.replace("hydro", "morpho")
     alg = ALG_BYTES[key]
     pass_ms = kms.value / max(kpasses.value, 1)
-    # algorithmic bytes per pass: the per-cell-update figure over the 4 passes of a step
-    alg_pass = alg / 4.0 * (cu / max(nsteps, 1))
+    kname = "k_hydro" if wl["prec"] == abi.PREC_FP64 else "k_hydro32"
+    # cells of one pass: a Strang step advances each active cell by two cell-updates
+    cells_pass = cu / max(nsteps, 1) / (2.0 if p.MorphodynamicsOn else 1.0)
+    # algorithmic bytes of one pass: 92 B (FP64) or 63 B (FP32 form) per cell of the pass
+    alg_pass = ALG_PASS_BYTES["fp64" if wl["prec"] == abi.PREC_FP64 else "fp32"] * cells_pass
     achieved = alg_pass / (pass_ms / 1e3) / 1e9 if pass_ms > 0 else None
     peak, peak_kind = measured_peaks()
-    kname = "k_hydro" if wl["prec"] == abi.PREC_FP64 else "k_hydro32"
-    cells_pass = cu / max(nsteps, 1) / (2.0 if p.MorphodynamicsOn else 1.0)
     traffic = profile_traffic(kname, args.workload, cells_pass)
+    # the whole step: algorithmic bytes per cell-update times the cell-updates of a step
+    step_gbs = alg * (cu / max(nsteps, 1)) / (total_ms / max(nsteps, 1) / 1e3) / 1e9 if total_ms > 0 else None
     line = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": nsteps,
         "warmup": args.warmup, "ms_per_step": total_ms / max(nsteps, 1), "higher_is_better": True, "scaling": "weak",
@@ -679,10 +822,17 @@ def main():
                             "final read-back"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": kname, "pass_ms": pass_ms,
-                     "note": "algorithmic bytes of the form over the measured pass time; the pass is bound by the FP64 "
-                             "pipe (2 lanes per SM per clock on GB300), not HBM, per the committed ncu capture of "
-                             + kname + " on the 2048^2 morphodynamic workload (roofline_fp64 gives that bound)"},
+                     "kernel": kname, "pass_ms": pass_ms, "cells_per_pass": cells_pass,
+                     "alg_bytes_per_pass": alg_pass,
+                     "traffic_over_alg": traffic / alg_pass if traffic and alg_pass else None,
+                     "step": {"alg_bytes_per_cell_update": alg, "achieved": step_gbs,
+                              "frac": step_gbs / peak if step_gbs else None},
+                     "note": "achieved = algorithmic bytes of one fused hydraulic pass (" +
+                             f"{alg_pass / max(cells_pass, 1):.0f} B per cell of the pass: a quarter of the "
+                             "hydraulic step's bytes per cell-update) over the pass time from CUDA events on the "
+                             "library's stream; traffic = DRAM bytes per pass from the committed ncu capture, scaled "
+                             "to the pass's cells; step = the form's bytes per cell-update times the cell-updates of "
+                             "a step over the device-timed step"},
         "gpu_launches": launches,
         "clocks": clk,
     }
@@ -697,11 +847,21 @@ def main():
     if wl["prec"] == abi.PREC_FP32 and not args.no_fp64:
         twin = args.workload.replace("_fp32", "_fp64")
         if twin in workloads.WORKLOADS:
-            f64 = fp64_plain(args, twin, snapshot)
+            f64 = fp64_plain(args, twin, snapshot if wl.get("twin_restart") else None)
             line["fp64_plain"] = f64
             line["fp32_over_fp64"] = line["value"] / f64["value"] if f64["value"] else None
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(p, b0)
+        line["cpu_baseline"] = cpu_baseline(p, b0, snapshot=snapshot)
+    if args.workload == "morpho_flux_2048_fp32" and not args.no_extras:
+        # the other forms of the metric on their own configurations, under their own keys
+        # (secondary figures: an error in one never loses the headline line)
+        for key, fn in (("sparse_8192_fp32", lambda: run_sparse_window(args)),
+                        ("ensemble_fp32", lambda: extras_ensemble(args)),
+                        ("serve_fp32", lambda: extras_serve(args))):
+            try:
+                line[key] = fn()
+            except Exception as e:
+                line[key] = {"error": repr(e)}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

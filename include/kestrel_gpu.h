@@ -228,6 +228,16 @@ int  kg_hydraulic_rhs(kg_ctx* ctx, double t, int32_t substep, double* advised_dt
 int  kg_get_active_tiles(kg_ctx* ctx, int32_t* ids, int32_t* n);
 int  kg_get_ghost_tiles(kg_ctx* ctx, int32_t* ids, int32_t* n);
 
+/* The whole active state in one call, the counterpart of kg_load_state (the state the
+   reference's snapshot writers read from grid%tileContainer, src/Output.f90:754-931, and
+   its restart reader takes back, src/Restart.f90:55-328): the active tile ids in list
+   order, per tile k the conserved fields state[k][4][nYpertile][nXpertile] (w, rhoHnu,
+   rhoHnv, Hnpsi) and the vertex bed change bt_vertex[k][nYpertile+1][nXpertile+1].  One
+   device gather, one copy per array, one wait.  *n is in/out: capacity on entry, count
+   on exit; with ids, state and bt_vertex all NULL only the count is returned.  Any of the
+   three may be NULL.  KG_ERR_PARAM when the capacity is below the count. */
+int  kg_get_state(kg_ctx* ctx, int32_t* ids, int32_t* n, double* state, double* bt_vertex);
+
 /* One field (1..13, src/main.f90:116-141) of the current solution for an active tile,
    nXpertile*nYpertile doubles.  Fields 5..9 are the desingularised variables as the
    reference holds them in tileContainer after the last step. */

@@ -116,6 +116,7 @@ def declare(lib, prefix):
         "get_active_tiles": ([vp, P(C.c_int32), P(C.c_int32)], C.c_int),
         "get_ghost_tiles": ([vp, P(C.c_int32), P(C.c_int32)], C.c_int),
         "get_tile_field": ([vp, C.c_int32, C.c_int32, P(C.c_double)], C.c_int),
+        "get_state": ([vp, P(C.c_int32), P(C.c_int32), P(C.c_double), P(C.c_double)], C.c_int),
         "set_tile_field": ([vp, C.c_int32, C.c_int32, P(C.c_double)], C.c_int),
         "get_tile_vertex": ([vp, C.c_int32, C.c_int32, P(C.c_double)], C.c_int),
         "get_tile_rhs": ([vp, C.c_int32, C.c_int32, P(C.c_double)], C.c_int),

@@ -46,6 +46,8 @@ cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, doubl
 cudaError_t launch_ghost_edges(const DevArrays& A, int slot, int mask, int qcur, cudaStream_t st);
 cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, int ts, cudaStream_t st);
 cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st);
+cudaError_t launch_gather_state(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, int SC, int SV, double* u4,
+                                double* btv, cudaStream_t st);
 cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn_over, int* d_flags,
                              int nX, int nY, cudaStream_t st);
 cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
@@ -161,6 +163,8 @@ struct kg_ctx {
     int64_t gen = 0, act_gen = -1;
     int* d_tlist = nullptr;              // slot list of the cache rebuild
     int d_tlist_cap = 0;
+    double* d_gather = nullptr;          // packed state of the active tiles (kg_get_state)
+    size_t d_gather_cap = 0;
     std::vector<int> touched;            // slots whose step-start topography changed in set-up
     int* d_mflags = nullptr;             // = &d_ctl->mflag
     int* d_ncand = nullptr;              // = &d_ctl->ncand
@@ -1689,6 +1693,7 @@ void free_ctx(kg_ctx* c) {
         cudaFree(c->A.TD[b]); cudaFree(c->A.TF[b]); cudaFree(c->A.TFX[b]); cudaFree(c->A.TFY[b]);
     }
     cudaFree(c->d_tlist);
+    cudaFree(c->d_gather);
     cudaFree(c->d_rb0);
     void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.B0S, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
@@ -1992,6 +1997,41 @@ int kg_get_tile_field(kg_ctx* c, int32_t id, int32_t field, double* out) {
                 out[k] = field == 5 ? Hn : field == 8 ? psi : rho;
             }
         }
+    });
+    return KG_OK;
+}
+
+int kg_get_state(kg_ctx* c, int32_t* ids, int32_t* n, double* state, double* bt_vertex) {
+    if (!c || !n) return KG_ERR_PARAM;
+    KG_ENTER(c);
+    const int cap = *n, na = (int)c->active.size();
+    *n = (int32_t)na;
+    if (!ids && !state && !bt_vertex) return KG_OK;  // the count only
+    if (cap < na) {
+        c->err = "kg_get_state: room for " + std::to_string(cap) + " tiles, " + std::to_string(na) + " are active";
+        return KG_ERR_PARAM;
+    }
+    for (int k = 0; ids && k < na; ++k) ids[k] = c->active[(size_t)k];
+    if ((!state && !bt_vertex) || na == 0) return KG_OK;
+    KG_GUARD(c, {
+        const size_t SC = (size_t)c->SC, SV = (size_t)c->SV, need = (size_t)na * (4 * SC + SV);
+        if (need > c->d_gather_cap) {
+            if (c->d_gather) CK(cudaFree(c->d_gather));
+            c->d_gather = nullptr;
+            c->d_gather_cap = 0;
+            CK(cudaMalloc(&c->d_gather, need * sizeof(double)));
+            c->d_gather_cap = need;
+        }
+        std::vector<int> slots;
+        for (int id : c->active) slots.push_back(T(*c, id).slot);
+        upload_list(*c, slots);
+        double* du4 = c->d_gather;
+        double* dbt = c->d_gather + (size_t)na * 4 * SC;
+        CK(launch_gather_state(c->A, c->d_list, na, c->qcur, c->tcur, (int)SC, (int)SV, du4, dbt, c->st));
+        c->launches++;
+        if (state) CK(kg_cpy(*c, state, du4, (size_t)na * 4 * SC * sizeof(double), cudaMemcpyDeviceToHost));
+        if (bt_vertex) CK(kg_cpy(*c, bt_vertex, dbt, (size_t)na * SV * sizeof(double), cudaMemcpyDeviceToHost));
+        sync(*c);
     });
     return KG_OK;
 }

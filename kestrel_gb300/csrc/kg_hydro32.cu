@@ -24,8 +24,9 @@ struct __align__(16) Hydro32Smem {
     double p64[NR];              // Hnpsi as the stage update reads it
     float m1[NR], m2[NR], p[NR];
     float hp[NR], gam[NR], Hn[NR], rho[NR], u[NR], v[NR], psi[NR];
-    float dlo[2][NLX], dhi[2][NLX];  // w - InterpolateB at the cell's lower / upper face (x, y)
-    float lx[5][NLX], ly[5][NLX];
+    float hlo[2][NLX], hhi[2][NLX];  // face-side depths w_face - InterpolateB at the cell's lower / upper
+                                     // face (x, y), after the well-balancing correction
+    float lx[5][NLX], ly[5][NLX];    // slopes of (-, Hnpsi, u, v, rho); row 0 (w) is not used
     float fx[7][NFX], fy[7][NFX];
     float red[NT / 32];
 };
@@ -61,6 +62,52 @@ __device__ __forceinline__ double flux_sum4(float a, float b, float c, float d) 
     float e3 = (s1 - (S - t)) + (s2 - t);
     float E = (e1 + e2) + e3;
     return (double)S + (double)E;
+}
+
+// Half of the limited free-surface difference (the step from a cell centre to its face,
+// 0.5 dx * limiter(a/dx, b/dx) with a, b the forward and backward differences of w), in
+// FP64.  On steep beds a thin flow's face depth is the small difference of two large
+// terms, w - InterpolateB (metres) and this step (metres), so both stay in FP64 until the
+// depth itself is formed.  The minmod family and the unlimited slope select or average
+// the FP64 differences exactly as the limiters of src/Limiters.f90:68-184 do (the sign and
+// magnitude tests are taken on the bit patterns); van Albada and WENO take their weight in
+// FP32.
+__device__ __forceinline__ double half_step_w(int lim, double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & 0x7FFFFFFFFFFFFFFFll, mb = ib & 0x7FFFFFFFFFFFFFFFll;
+    switch (lim) {
+        case KG_LIM_MINMOD1:
+        case KG_LIM_MINMOD2: {
+            if ((ia ^ ib) < 0 || ma == 0 || mb == 0) return 0.0;  // a * b <= 0
+            const double m = ma < mb ? a : b;                    // the one nearer zero
+            if (lim == KG_LIM_MINMOD1) return 0.5 * m;
+            // min(theta a, theta b, (a + b)/2) of the same sign, halved (exactly: powers of 2)
+            const double t1 = (0.5 * 1.3) * m, t2 = 0.25 * (a + b);
+            return (__double_as_longlong(t1) & 0x7FFFFFFFFFFFFFFFll) < (__double_as_longlong(t2) & 0x7FFFFFFFFFFFFFFFll) ? t1 : t2;
+        }
+        case KG_LIM_NONE: return 0.25 * (a + b);
+        default: return 0.5 * (double)limiter<float>(lim, (float)a, (float)b);
+    }
+}
+
+// The two reconstructed face sides of a cell, as depths above the interpolated bed of each
+// face (CorrectSlopes, src/HydraulicRHS.f90:560-735): dlo/dhi are w_c minus the bed of the
+// lower/upper face, hs the half step of w.  A side below its bed corrects the cell: both
+// sides then take w_c + (b_hi - b_lo)/2, i.e. (dlo + dhi)/2 above either face's bed.
+// `corr_in` forces the correction (the ghost-tile rule, decided from stored records).
+__device__ __forceinline__ void face_sides(double dlo, double dhi, double hs, int corr_in, float& lo, float& hi) {
+    double up = dhi + hs, dn = dlo - hs;
+    // x < 0 on the bit pattern (sign set, not -0): integer work instead of FP64 compares
+    auto neg = [](double x) { long long b = __double_as_longlong(x); return b < 0 && b != (long long)0x8000000000000000ull; };
+    bool corr = corr_in > 0 || (corr_in < 0 && (neg(up) || neg(dn)));
+    if (corr) {
+        float c = (float)(0.5 * (dlo + dhi));
+        lo = c;
+        hi = c;
+    } else {
+        lo = (float)dn;
+        hi = (float)up;
+    }
 }
 
 struct Side32 {
@@ -115,16 +162,6 @@ __device__ __forceinline__ void face_flux32(const DevParams32& P, bool xdir, con
     }
     out[5 * stride] = 0.5f * (dP1 + dM1);
     out[6 * stride] = 0.5f * (dP2 + dM2);
-}
-
-// Well-balancing and positivity corrections of one reconstructed face side
-// (CorrectSlopes, src/HydraulicRHS.f90:560-735) in offset form: dlo/dhi are w_c minus the
-// interpolated bed at the cell's lower/upper face, s the half-cell slope step of w.  The
-// side value at the upper face is dhi + s; at the lower face dlo - s; a corrected cell
-// takes w_c + (bhi - blo)/2 at both, i.e. (dlo + dhi)/2 above either face's bed.
-__device__ __forceinline__ float side_hp(float dlo, float dhi, float s, bool upper, bool corr) {
-    if (corr) return 0.5f * (dlo + dhi);
-    return upper ? dhi + s : dlo - s;
 }
 
 // One BS x BS block of one tile through one pass (the body shared by the single-simulation
@@ -203,7 +240,7 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
     }
     __syncthreads();
 
-    // ---- B: limited slopes and face offsets ----
+    // ---- B: limited slopes; reconstructed, corrected face-side depths of w in FP64 ----
     const int lim = P.limiter;
     const float dxR = F.dxR, dyR = F.dyR;
     for (int kk = tid; kk < (bx + 2) * by + (by + 2) * bx; kk += NT) {
@@ -212,49 +249,58 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             int cx = k % (bx + 2) - 1, cy = k / (bx + 2);
             int r = (cy + 2) * RG + (cx + 2);
             int li = cy * (BS + 2) + (cx + 1);
+            int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
+            if (i < 0) { s = nbW; i += nX; }
+            else if (i >= nX) { s = nbE; i -= nX; }
+            const double* bI = FX + plane(s, 5, 4, SFX) + (size_t)j * (nX + 1) + i;
+            const double dlo = sm.w[r] - bI[0], dhi = sm.w[r] - bI[1];
             bool ghW = (cx < 0 && bd.x0 == 0 && A.kind[nbW] == SLOT_GHOST);
             bool ghE = (cx >= bx && bd.x0 + bx == nX && A.kind[nbE] == SLOT_GHOST);
+            double hs;
+            int corr_in = -1;
             if (ghW || ghE) {
-                int gs = ghW ? nbW : nbE;
-                sm.lx[0][li] = (float)A.GE[plane(gs, GE_COUNT, ghW ? GE_LXN : GE_LX1, A.nE) + bd.y0 + cy];
+                // a ghost neighbour: its stored slope and stale face reconstructions decide
+                const double* ge = A.GE + plane(ghW ? nbW : nbE, GE_COUNT, 0, A.nE);
+                hs = ge[(ghW ? GE_LXN : GE_LX1) * A.nE + j] * (0.5 * P.dx);
+                corr_in = ghW ? (ge[GE_MXN1 * A.nE + j] < bI[1] || ge[GE_PXN * A.nE + j] < bI[0])
+                              : (ge[GE_MX2 * A.nE + j] < bI[1] || ge[GE_PX1 * A.nE + j] < bI[0]);
                 sm.lx[1][li] = 0.f; sm.lx[2][li] = 0.f; sm.lx[3][li] = 0.f; sm.lx[4][li] = 0.f;
             } else {
-                sm.lx[0][li] = dxR * limiter<float>(lim, (float)(sm.w[r + 1] - sm.w[r]), (float)(sm.w[r] - sm.w[r - 1]));
+                hs = half_step_w(lim, sm.w[r + 1] - sm.w[r], sm.w[r] - sm.w[r - 1]);
                 sm.lx[1][li] = dxR * limiter<float>(lim, sm.p[r + 1] - sm.p[r], sm.p[r] - sm.p[r - 1]);
                 sm.lx[2][li] = dxR * limiter<float>(lim, sm.u[r + 1] - sm.u[r], sm.u[r] - sm.u[r - 1]);
                 sm.lx[3][li] = dxR * limiter<float>(lim, sm.v[r + 1] - sm.v[r], sm.v[r] - sm.v[r - 1]);
                 sm.lx[4][li] = dxR * limiter<float>(lim, sm.rho[r + 1] - sm.rho[r], sm.rho[r] - sm.rho[r - 1]);
             }
-            int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
-            if (i < 0) { s = nbW; i += nX; }
-            else if (i >= nX) { s = nbE; i -= nX; }
-            const double* bI = FX + plane(s, 5, 4, SFX) + (size_t)j * (nX + 1) + i;
-            sm.dlo[0][li] = (float)(sm.w[r] - bI[0]);
-            sm.dhi[0][li] = (float)(sm.w[r] - bI[1]);
+            face_sides(dlo, dhi, hs, corr_in, sm.hlo[0][li], sm.hhi[0][li]);
         } else {
             const int k = kk - ((bx + 2) * by);
             int cx = k % bx, cy = k / bx - 1;
             int r = (cy + 2) * RG + (cx + 2);
             int li = (cy + 1) * BS + cx;
+            int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
+            if (j < 0) { s = nbS; j += nY; }
+            else if (j >= nY) { s = nbN; j -= nY; }
+            const double* bI = FY + plane(s, 5, 4, SFY) + (size_t)j * nX + i;
+            const double dlo = sm.w[r] - bI[0], dhi = sm.w[r] - bI[nX];
             bool ghS = (cy < 0 && bd.y0 == 0 && A.kind[nbS] == SLOT_GHOST);
             bool ghN = (cy >= by && bd.y0 + by == nY && A.kind[nbN] == SLOT_GHOST);
+            double hs;
+            int corr_in = -1;
             if (ghS || ghN) {
-                int gs = ghS ? nbS : nbN;
-                sm.ly[0][li] = (float)A.GE[plane(gs, GE_COUNT, ghS ? GE_LYN : GE_LY1, A.nE) + bd.x0 + cx];
+                const double* ge = A.GE + plane(ghS ? nbS : nbN, GE_COUNT, 0, A.nE);
+                hs = ge[(ghS ? GE_LYN : GE_LY1) * A.nE + i] * (0.5 * P.dy);
+                corr_in = ghS ? (ge[GE_MYN1 * A.nE + i] < bI[nX] || ge[GE_PYN * A.nE + i] < bI[0])
+                              : (ge[GE_MY2 * A.nE + i] < bI[nX] || ge[GE_PY1 * A.nE + i] < bI[0]);
                 sm.ly[1][li] = 0.f; sm.ly[2][li] = 0.f; sm.ly[3][li] = 0.f; sm.ly[4][li] = 0.f;
             } else {
-                sm.ly[0][li] = dyR * limiter<float>(lim, (float)(sm.w[r + RG] - sm.w[r]), (float)(sm.w[r] - sm.w[r - RG]));
+                hs = half_step_w(lim, sm.w[r + RG] - sm.w[r], sm.w[r] - sm.w[r - RG]);
                 sm.ly[1][li] = dyR * limiter<float>(lim, sm.p[r + RG] - sm.p[r], sm.p[r] - sm.p[r - RG]);
                 sm.ly[2][li] = dyR * limiter<float>(lim, sm.u[r + RG] - sm.u[r], sm.u[r] - sm.u[r - RG]);
                 sm.ly[3][li] = dyR * limiter<float>(lim, sm.v[r + RG] - sm.v[r], sm.v[r] - sm.v[r - RG]);
                 sm.ly[4][li] = dyR * limiter<float>(lim, sm.rho[r + RG] - sm.rho[r], sm.rho[r] - sm.rho[r - RG]);
             }
-            int i = bd.x0 + cx, j = bd.y0 + cy, s = slot;
-            if (j < 0) { s = nbS; j += nY; }
-            else if (j >= nY) { s = nbN; j -= nY; }
-            const double* bI = FY + plane(s, 5, 4, SFY) + (size_t)j * nX + i;
-            sm.dlo[1][li] = (float)(sm.w[r] - bI[0]);
-            sm.dhi[1][li] = (float)(sm.w[r] - bI[nX]);
+            face_sides(dlo, dhi, hs, corr_in, sm.hlo[1][li], sm.hhi[1][li]);
         }
     }
     __syncthreads();
@@ -273,17 +319,8 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             int liL = cy * (BS + 2) + fx, liR = liL + 1;
             Side32 L, R;
             // Left state: the upper-face reconstruction of cell fx-1.
-            float s = sm.lx[0][liL] * hdx, sp = sm.lx[1][liL] * hdx;
-            bool corr;
-            if (fi == 0 && A.kind[nbW] == SLOT_GHOST) {
-                const double* fxs = FX + plane(nbW, 5, 4, SFX);
-                double bl = fxs[j * (nX + 1) + nX - 1], br = fxs[j * (nX + 1) + nX];
-                const double* ge = A.GE + plane(nbW, GE_COUNT, 0, A.nE);
-                corr = ge[GE_MXN1 * A.nE + j] < br || ge[GE_PXN * A.nE + j] < bl;
-            } else {
-                corr = (sm.dhi[0][liL] + s < 0.f) || (sm.dlo[0][liL] - s < 0.f);
-            }
-            L.hp = side_hp(sm.dlo[0][liL], sm.dhi[0][liL], s, true, corr);
+            float sp = sm.lx[1][liL] * hdx;
+            L.hp = sm.hhi[0][liL];
             L.p = sm.p[rL] + sp;
             if (L.p < 0.f || (fi != 0 && sm.p[rL] - sp < 0.f)) L.p = sm.p[rL];
             L.u = sm.u[rL] + sm.lx[2][liL] * hdx;
@@ -292,17 +329,8 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             L.du = sm.lx[2][liL];
             L.dv = sm.lx[3][liL];
             // Right state: the lower-face reconstruction of cell fx.
-            s = sm.lx[0][liR] * hdx;
             sp = sm.lx[1][liR] * hdx;
-            if (fi == nX && A.kind[nbE] == SLOT_GHOST) {
-                const double* fxs = FX + plane(nbE, 5, 4, SFX);
-                double bl = fxs[j * (nX + 1) + 0], br = fxs[j * (nX + 1) + 1];
-                const double* ge = A.GE + plane(nbE, GE_COUNT, 0, A.nE);
-                corr = ge[GE_MX2 * A.nE + j] < br || ge[GE_PX1 * A.nE + j] < bl;
-            } else {
-                corr = (sm.dhi[0][liR] + s < 0.f) || (sm.dlo[0][liR] - s < 0.f);
-            }
-            R.hp = side_hp(sm.dlo[0][liR], sm.dhi[0][liR], s, false, corr);
+            R.hp = sm.hlo[0][liR];
             R.p = sm.p[rR] - sp;
             if (R.p < 0.f || (fi != nX && sm.p[rR] + sp < 0.f)) R.p = sm.p[rR];
             R.u = sm.u[rR] - sm.lx[2][liR] * hdx;
@@ -319,17 +347,8 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             int rL = (fy + 1) * RG + (cx + 2), rR = rL + RG;
             int liL = fy * BS + cx, liR = liL + BS;
             Side32 L, R;
-            float s = sm.ly[0][liL] * hdy, sp = sm.ly[1][liL] * hdy;
-            bool corr;
-            if (fj == 0 && A.kind[nbS] == SLOT_GHOST) {
-                const double* fys = FY + plane(nbS, 5, 4, SFY);
-                double bb = fys[(nY - 1) * nX + i], bt_ = fys[nY * nX + i];
-                const double* ge = A.GE + plane(nbS, GE_COUNT, 0, A.nE);
-                corr = ge[GE_MYN1 * A.nE + i] < bt_ || ge[GE_PYN * A.nE + i] < bb;
-            } else {
-                corr = (sm.dhi[1][liL] + s < 0.f) || (sm.dlo[1][liL] - s < 0.f);
-            }
-            L.hp = side_hp(sm.dlo[1][liL], sm.dhi[1][liL], s, true, corr);
+            float sp = sm.ly[1][liL] * hdy;
+            L.hp = sm.hhi[1][liL];
             L.p = sm.p[rL] + sp;
             if (L.p < 0.f || (fj != 0 && sm.p[rL] - sp < 0.f)) L.p = sm.p[rL];
             L.u = sm.u[rL] + sm.ly[2][liL] * hdy;
@@ -337,17 +356,8 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             L.rho = sm.rho[rL] + sm.ly[4][liL] * hdy;
             L.du = sm.ly[2][liL];
             L.dv = sm.ly[3][liL];
-            s = sm.ly[0][liR] * hdy;
             sp = sm.ly[1][liR] * hdy;
-            if (fj == nY && A.kind[nbN] == SLOT_GHOST) {
-                const double* fys = FY + plane(nbN, 5, 4, SFY);
-                double bb = fys[0 * nX + i], bt_ = fys[1 * nX + i];
-                const double* ge = A.GE + plane(nbN, GE_COUNT, 0, A.nE);
-                corr = ge[GE_MY2 * A.nE + i] < bt_ || ge[GE_PY1 * A.nE + i] < bb;
-            } else {
-                corr = (sm.dhi[1][liR] + s < 0.f) || (sm.dlo[1][liR] - s < 0.f);
-            }
-            R.hp = side_hp(sm.dlo[1][liR], sm.dhi[1][liR], s, false, corr);
+            R.hp = sm.hlo[1][liR];
             R.p = sm.p[rR] - sp;
             if (R.p < 0.f || (fj != nY && sm.p[rR] + sp < 0.f)) R.p = sm.p[rR];
             R.u = sm.u[rR] - sm.ly[2][liR] * hdy;

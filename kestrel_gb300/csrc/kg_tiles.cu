@@ -385,6 +385,29 @@ cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, int ts, cuda
     k_activate<<<1, 256, 0, st>>>(A, slot, qcur, ts);
     return cudaGetLastError();
 }
+// The state of the listed tiles packed for one read-back: the four conserved planes of
+// each tile (w, rhoHnu, rhoHnv, Hnpsi, contiguous per slot) into u4[k][4][SC] and its
+// vertex bed change into btv[k][SV], k in list order.
+__global__ void __launch_bounds__(256) k_gather_state(DevArrays A, const int* __restrict__ slots, int n, int qcur, int ts,
+                                                      int SC, int SV, double* __restrict__ u4, double* __restrict__ btv) {
+    kg_dep_wait();
+    const long long per = 4LL * SC + SV, total = per * n;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        int k = (int)(e / per);
+        long long r = e - k * per;
+        int s = slots[k];
+        if (r < 4LL * SC) u4[(size_t)k * 4 * SC + r] = A.Q[qcur][(size_t)s * 4 * SC + r];
+        else btv[(size_t)k * SV + (r - 4LL * SC)] = A.BV[ts][((size_t)s * 2 + 1) * SV + (r - 4LL * SC)];
+    }
+}
+cudaError_t launch_gather_state(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, int SC, int SV, double* u4,
+                                double* btv, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    long long total = (4LL * SC + SV) * n;
+    int grid = (int)std::min<long long>((total + 255) / 256, 152LL * 8);
+    KG_TRY_LAUNCH(kg_launch(k_gather_state, grid, 256, 0, st, A, d_slots, n, qcur, ts, SC, SV, u4, btv));
+    return cudaGetLastError();
+}
 cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st) {
     k_init_maxima<<<1, 256, 0, st>>>(A, slot);
     return cudaGetLastError();

@@ -156,6 +156,19 @@ class Simulation:
         self._check(self._f("get_tile_field")(self.h, tile, field, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out.reshape(self.nY, self.nX)
 
+    def get_state(self):
+        """(tile ids, state (n, 4, nY, nX), vertex bt (n, nY+1, nX+1), t): the whole active
+        state in one call (kg_get_state), in the form load_state takes back."""
+        n = C.c_int32(0)
+        self._check(self._f("get_state")(self.h, None, C.byref(n), None, None))
+        na = n.value
+        ids = (C.c_int32 * max(na, 1))()
+        st = np.empty((na, 4, self.nY, self.nX), dtype=np.float64)
+        bt = np.empty((na, self.nY + 1, self.nX + 1), dtype=np.float64)
+        self._check(self._f("get_state")(self.h, ids, C.byref(n), st.ctypes.data_as(C.POINTER(C.c_double)),
+                                         bt.ctypes.data_as(C.POINTER(C.c_double))))
+        return [ids[i] for i in range(na)], st, bt, self.time[0]
+
     def set_field(self, tile: int, field: int, values: np.ndarray):
         v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
         self._check(self._f("set_tile_field")(self.h, tile, field, v.ctypes.data_as(C.POINTER(C.c_double))))

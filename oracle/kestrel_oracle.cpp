@@ -1022,6 +1022,33 @@ int ko_get_tile_field(ko_ctx* c, int32_t id, int32_t field, double* out) {
         for (int i = 1; i <= nX; ++i) out[(i - 1) + nX * (j - 1)] = T.u(field, i, j);
     return KG_OK;
 }
+// Test hook: one-ulp nudge of the closure transcendentals, process-wide (0 off, +1 up, -1
+// down, >= 2 a pseudo-random direction per call seeded by the mode).
+void ko_set_closure_nudge(int32_t mode) {
+    ko::closure_nudge() = mode;
+    ko::closure_nudge_state() = 0x9E3779B97F4A7C15ull * (uint64_t)(mode > 0 ? mode : 1);
+}
+
+// kg_get_state: the active tiles' conserved fields and vertex bed change, list order.
+int ko_get_state(ko_ctx* c, int32_t* ids, int32_t* n, double* state, double* bt_vertex) {
+    if (!c || !n) return KG_ERR_PARAM;
+    const int cap = *n, na = (int)c->s.g.activeTiles.size();
+    *n = (int32_t)na;
+    if (!ids && !state && !bt_vertex) return KG_OK;
+    if (cap < na) { c->s.err = "ko_get_state: capacity below the active tile count"; return KG_ERR_PARAM; }
+    const int nX = c->s.rp.nXpertile, nY = c->s.rp.nYpertile, SC = nX * nY, SV = (nX + 1) * (nY + 1);
+    for (int k = 0; k < na; ++k) {
+        int id = c->s.g.activeTiles[(size_t)k];
+        if (ids) ids[k] = id;
+        ko::Tile& T = c->s.g.tc(id);
+        for (int f = 1; f <= 4 && state; ++f)
+            for (int j = 1; j <= nY; ++j)
+                for (int i = 1; i <= nX; ++i) state[(size_t)k * 4 * SC + (size_t)(f - 1) * SC + (i - 1) + nX * (j - 1)] = T.u(f, i, j);
+        for (int j = 1; j <= nY + 1 && bt_vertex; ++j)
+            for (int i = 1; i <= nX + 1; ++i) bt_vertex[(size_t)k * SV + (i - 1) + (nX + 1) * (j - 1)] = T.bt(i, j);
+    }
+    return KG_OK;
+}
 int ko_set_tile_field(ko_ctx* c, int32_t id, int32_t field, const double* in) {
     if (!find_active(c, id)) return KG_ERR_NOT_FOUND;
     if (field < 1 || field > 4) return KG_ERR_PARAM;

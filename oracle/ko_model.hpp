@@ -180,6 +180,35 @@ inline double PouliquenFrictionCoefficient(const RunSet& rp, double gcostheta, d
     }
     return mu1;
 }
+// Test hook (off unless a test sets it through ko_set_closure_nudge): moves the result of
+// every closure transcendental (pow, tanh, log, cos) by one ulp: up (mode +1), down (-1),
+// or, for a mode >= 2, up, down or not at all per call from a pseudo-random sequence seeded
+// by the mode.  The GPU calls CUDA's functions, which differ from glibc's in the last bits
+// in either direction; the tests use the nudge to measure how far the reference's
+// algorithm itself moves under such differences.
+inline int& closure_nudge() {
+    static int d = 0;
+    return d;
+}
+inline uint64_t& closure_nudge_state() {
+    static uint64_t x = 0;
+    return x;
+}
+inline double nd(double v) {
+    const int d = closure_nudge();
+    if (d == 0) return v;
+    int dir = d;
+    if (d >= 2) {  // xorshift64
+        uint64_t& x = closure_nudge_state();
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        dir = (int)(x % 3) - 1;
+        if (dir == 0) return v;
+    }
+    return std::nextafter(v, dir > 0 ? HUGE_VAL : -HUGE_VAL);
+}
+
 inline double ChezyDrag(const RunSet& rp, const double* uv) {
     double modu2 = FlowSquaredSpeedSlopeAligned(rp, uv);
     return rp.p.ChezyCo * modu2;
@@ -212,7 +241,7 @@ inline double Edwards2019Drag(const RunSet& rp, const double* uv) {  // :471-506
     if (Fr > betastar) {
         friction = mu1 + (mu2 - mu1) / (1.0 + Hn * beta / (L * (Fr + capgam)));
     } else {
-        friction = (std::pow(Fr / betastar, kappa)) *
+        friction = (nd(std::pow(Fr / betastar, kappa))) *
                        (mu1 + (mu2 - mu1) / (1.0 + Hn * beta / (L * (betastar + capgam))) -
                         mu3 - (mu2 - mu1) / (1.0 + Hn / L)) +
                    mu3 + (mu2 - mu1) / (1.0 + Hn / L);
@@ -224,13 +253,13 @@ inline double ManningDrag(const RunSet& rp, const double* uv) {  // :510-532
     double gam = Gam(rp, uv);
     double g = rp.g / gam;
     double n = rp.p.ManningCo;
-    if (Hn > rp.heightThreshold) return g * n * n / (std::pow(Hn, 1.0 / 3.0));
+    if (Hn > rp.heightThreshold) return g * n * n / (nd(std::pow(Hn, 1.0 / 3.0)));
     return 0.0;
 }
 inline double fswitch(const RunSet& rp, double psi) {  // :797-915
     double rate = rp.p.VoellmySwitchRate, val = rp.p.VoellmySwitchValue;
     switch (rp.p.fswitch) {
-        case KG_SWITCH_TANH: return 0.5 * (1.0 + std::tanh(rate * (psi - val)));
+        case KG_SWITCH_TANH: return 0.5 * (1.0 + nd(std::tanh(rate * (psi - val))));
         case KG_SWITCH_RAT3: {
             double a = val - 1.5 / rate, b = val + 1.5 / rate;
             if (psi <= a) return 0.0;
@@ -244,7 +273,7 @@ inline double fswitch(const RunSet& rp, double psi) {  // :797-915
             if (psi <= a) return 0.0;
             if (psi >= b) return 1.0;
             double x = (psi - a) / (b - a);
-            return 0.5 * (1.0 - std::cos(PI * x));
+            return 0.5 * (1.0 - nd(std::cos(PI * x)));
         }
         case KG_SWITCH_LINEAR: return psi / rp.p.maxPack;
         case KG_SWITCH_EQUAL: return 0.5;
@@ -328,7 +357,7 @@ inline double ErosionTransition(const RunSet& rp, const double* uv) {  // :684-7
     double Bt = uv[ibt - 1];
     double eroDepth = rp.p.EroDepth;
     switch (rp.p.erosion_transition) {
-        case KG_ETRANS_SMOOTH: return 0.5 * (1.0 + std::tanh(1e5 * (Bt + eroDepth)));
+        case KG_ETRANS_SMOOTH: return 0.5 * (1.0 + nd(std::tanh(1e5 * (Bt + eroDepth))));
         case KG_ETRANS_STEP: return (Bt < -eroDepth) ? 0.0 : 1.0;
         default: return 1.0;
     }
@@ -336,7 +365,7 @@ inline double ErosionTransition(const RunSet& rp, const double* uv) {  // :684-7
 inline double MorphoDamping(const RunSet& rp, double Hn) {  // :744-791
     double Hncrit = rp.p.EroCriticalHeight;
     switch (rp.p.morpho_damping) {
-        case KG_DAMP_TANH: return 0.5 * (1.0 + std::tanh(10.0 * std::log(Hn / Hncrit)));
+        case KG_DAMP_TANH: return 0.5 * (1.0 + nd(std::tanh(10.0 * nd(std::log(Hn / Hncrit)))));
         case KG_DAMP_RAT3: {
             if (Hn < Hncrit) return 0.0;
             if (Hn > 2.0 * Hncrit) return 1.0;
@@ -353,7 +382,7 @@ inline double DepositionClosure(const RunSet& rp, double psi) {  // :320-356
         case KG_DEP_SPEARMAN_MANNING: {
             double a = 2.7 - 0.15 * rp.nsettling;
             double b = 0.62 * rp.nsettling - 1.46;
-            return psi * std::pow(1.0 - psi, a) * std::pow(1.0 - psi / rp.p.maxPack, b);
+            return psi * nd(std::pow(1.0 - psi, a)) * nd(std::pow(1.0 - psi / rp.p.maxPack, b));
         }
         default: return 0.0;
     }

@@ -225,7 +225,7 @@ def _fortran_type_fields(text, name):
 def test_fortran_binding_matches_the_structs(name, cls):
     """The bind(C) derived types of the Fortran binding list every field of the C struct, in
     order, with the same kind and array bound (padding fields without their underscore)."""
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    text = open(os.path.join(ROOT, "include", "kestrel_gpu.f90")).read()
     got = _fortran_type_fields(text, name)
     kinds = {C.c_double: "real(c_double)", C.c_int32: "integer(c_int32_t)", C.c_int64: "integer(c_int64_t)"}
     subtypes = {abi.Cap: "type(kg_cap)", abi.Cube: "type(kg_cube)", abi.FluxSource: "type(kg_flux_source)"}
@@ -242,11 +242,11 @@ def test_fortran_binding_matches_the_structs(name, cls):
 def test_fortran_interfaces_match_the_header():
     """Every bind(C) interface of the Fortran binding names a header function and takes its
     number of arguments; value arguments are the header's scalars, the rest its pointers."""
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    text = open(os.path.join(ROOT, "include", "kestrel_gpu.f90")).read()
     protos = {n: types for _, n, types in _header_prototypes()}
     blocks = re.findall(r"(?:function|subroutine) (kg_[a-z0-9_]+)\(([^)]*)\) bind\(C, name=\"(kg_[a-z0-9_]+)\"\)(.*?)end (?:function|subroutine)",
                         text, re.S)
-    assert len(blocks) >= 9
+    assert len(blocks) >= 20
     for fname, args, cname, body in blocks:
         assert fname == cname and cname in protos, cname
         names = [a.strip() for a in args.split(",") if a.strip()]
@@ -260,3 +260,26 @@ def test_fortran_interfaces_match_the_header():
                 assert "value" not in attrs or "type(c_ptr)" in attrs, (cname, a, t)
             else:         # a scalar: by value
                 assert "value" in attrs and "type(c_ptr)" not in attrs, (cname, a, t)
+
+
+def test_fortran_dropin_keeps_the_reference_interfaces():
+    """The drop-in module offers Run, IntegrateTo and CalculateHydraulicRHS with the
+    reference's argument lists (src/TimeStepper.f90:73,116, src/HydraulicRHS.f90:64-73) and
+    binds only functions the header declares; every entry point it calls is interfaced in
+    the binding module."""
+    text = open(os.path.join(ROOT, "include", "kestrel_gpu_dropin.f90")).read()
+    binding = open(os.path.join(ROOT, "include", "kestrel_gpu.f90")).read()
+    for sig in ("subroutine Run(RunParams, grid)", "subroutine IntegrateTo(RunParams, tend, grid)",
+                "subroutine CalculateHydraulicRHS(RunParams, grid, tileWorkspace, t, substep, advisedTimeStep)"):
+        assert sig in text, sig
+    header = {n for _, n, _ in _header_prototypes()}
+    bound = set(re.findall(r'bind\(C, name="(kg_[a-z0-9_]+)"\)', binding))
+    assert bound <= header, bound - header
+    called = set(re.findall(r"\b(kg_[a-z0-9_]+)\(", text)) - {"kg_check", "kg_params", "kg_raster", "kg_step_stats"}
+    assert called <= bound, called - bound
+    # every statement block the module opens is closed (comments left out)
+    lines = [line.split("!")[0].strip().lower() for line in text.splitlines()]
+    for kw in ("module", "subroutine", "function"):
+        closed = sum(1 for line in lines if re.match(r"end " + kw + r"\b", line))
+        opened = sum(1 for line in lines if not line.startswith("end") and re.match(r"(?:[a-z()_0-9, ]*\s)?" + kw + r"\s+[a-z_]", line))
+        assert opened == closed, (kw, opened, closed)

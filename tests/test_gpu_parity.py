@@ -229,3 +229,32 @@ def test_sparse_activation_bitexact_every_step():
         n += 1
     assert len(o.active_tiles()) > 3
     compare_state(g, o, tol=1e-10, what="sparse")
+
+
+def test_get_state_single_call():
+    """kg_get_state returns every active tile's conserved fields and vertex bed change in
+    one call, equal to the per-tile getters and to the oracle's state (morphodynamic run
+    within the morphodynamic bar); loading it into a fresh context (kg_load_state)
+    continues the run exactly as the uninterrupted context does."""
+    from kestrel_gb300.solver import Simulation
+    p = cases.ref_input("cap_morpho_2d", tend=0.5, nout=1)
+    g, o = pair(p)
+    g.run()
+    o.run()
+    ids, st, bt, t = g.get_state()
+    oids, ost, obt, ot = o.get_state()
+    assert ids == g.active_tiles() == oids and t == ot
+    for k, tile in enumerate(ids):
+        for f in range(4):
+            assert np.array_equal(st[k, f], g.field(tile, f + 1)), (tile, f)
+        assert np.array_equal(bt[k], g.vertex(tile, 1)), tile
+    assert rel_linf(st[:, 0], ost[:, 0]) <= 1e-10 and rel_linf(bt, obt) <= 1e-10
+    r = Simulation(lib.load(), "kg", p, load_sources=False)
+    r.load_state(ids, st, bt, t)
+    p.tend = 0.8
+    for s in (g, r):
+        s.integrate_to(0.8)
+    ids2, st2, bt2, t2 = g.get_state()
+    rids, rst, rbt, rt = r.get_state()
+    assert ids2 == rids and t2 == rt
+    assert np.array_equal(st2, rst) and np.array_equal(bt2, rbt)

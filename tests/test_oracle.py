@@ -347,3 +347,33 @@ def test_oracle_halt_edge_is_fatal():
     with pytest.raises(KestrelError) as e:
         sim.run()
     assert abi.KG_ERR[e.value.code] == "KG_ERR_HALT_EDGE"
+
+
+def test_oracle_get_state_matches_the_getters():
+    """ko_get_state (the oracle's kg_get_state) packs the per-tile getters' values."""
+    p = cases.ref_input("cap_morpho_2d", tend=0.3, nout=1)
+    sim = _oracle.simulation(p)
+    sim.run()
+    ids, st, bt, t = sim.get_state()
+    assert ids == sim.active_tiles() and t == sim.time[0] and len(ids) > 0
+    for k, tile in enumerate(ids):
+        for f in range(4):
+            assert np.array_equal(st[k, f], sim.field(tile, f + 1))
+        assert np.array_equal(bt[k], sim.vertex(tile, 1))
+
+
+def test_oracle_closure_sensitivity_to_last_bits():
+    """The reference's morphodynamic algorithm takes discrete decisions (the ordered
+    redistribution walk, src/Redistribute.f90:69-475; the refinement tests) on values that
+    come out of pow/tanh/log/cos.  Moving every closure transcendental by one ulp leaves the
+    tanh-switch case at round-off but moves the linear-switch case by about 1e-3: the bar a
+    GPU, whose math library differs from glibc's in the last bits, can be held to for such a
+    case is this spread, not 1e-10."""
+    from kestrel_gb300 import abi
+    p = cases.ref_input("cap_morpho_2d", tend=1.0, nout=1)
+    p.fswitch = abi.SWITCH["tanh"]
+    _, _, calm = _oracle.nudged_spread(p)
+    assert calm <= 1e-12, calm
+    p.fswitch = abi.SWITCH["linear"]
+    _, _, moved = _oracle.nudged_spread(p)
+    assert 1e-6 < moved < 1e-1, moved

@@ -66,15 +66,15 @@ def test_rhs_noalloc_matches_allocating_entry_point():
 
 def test_rhs_noalloc_after_load_and_after_activation():
     """On a fresh context straight after kg_load_sources, and straight after each step
-    that activated tiles (8x8-cell tiles, so the flow crosses many seams), the call equals
-    the oracle's CalculateHydraulicRHS; the runs then continue identically."""
+    that activated tiles (the 256^2 cap release on 16^2-cell tiles: the flow activates a
+    tile row every few steps), the call equals the oracle's CalculateHydraulicRHS; the runs
+    then continue identically."""
     L = noalloc()
-    p = cases.ref_input("cap_dilute_2d", tend=2.0, nout=1, nXtiles=30, nYtiles=30, nXpertile=8, nYpertile=8,
-                        Xtilesize=8.0, Ytilesize=8.0, TileBuffer=2)
+    p = cases.cap_release_256(tend=4.0)
     g, o = lib.simulation(p), _oracle.simulation(p)
     checked = 0
     n_prev = -1
-    for n in range(60):
+    for n in range(400):
         tiles = o.active_tiles()
         assert g.active_tiles() == tiles, n
         if len(tiles) != n_prev:
@@ -85,6 +85,8 @@ def test_rhs_noalloc_after_load_and_after_activation():
             same_planes(rhs_planes(g), rhs_planes(o), f"step {n}")
             checked += 1
             n_prev = len(tiles)
+        if o.time[0] >= p.tend:
+            break
         g.step(p.tend)
         o.step(p.tend)
     assert checked >= 3, checked
@@ -126,12 +128,13 @@ def test_rhs_noalloc_refuses_fp32_and_oversized_active_sets():
     g32 = lib.simulation(cases.ref_input("flux_hydro_2d", tend=1.0, nout=1), precision=abi.PREC_FP32)
     assert abi.KG_ERR[call(L, g32, 0.0)[0]] == "KG_ERR_UNSUPPORTED"
     g32.close()
-    # one periodic tile of 4112^2 cells: 257^2 = 66,049 blocks (about 12 GB in FP64)
-    n = 4112
-    p = cases.ref_input("lake_at_rest_hydro_2d", tend=1.0, nout=1, nXpertile=n, nYpertile=n, Xtilesize=float(n),
-                        Ytilesize=float(n))
-    p.cubes[0].length = float(n)
-    p.cubes[0].width = float(n)
+    # two periodic tiles of 4096 x 2064 cells (a tile holds at most 2^24 cells): 2 x 256 x
+    # 129 = 66,048 blocks, about 12 GB in FP64
+    nx, ny = 4096, 2064
+    p = cases.ref_input("lake_at_rest_hydro_2d", tend=1.0, nout=1, nXtiles=2, nYtiles=1, nXpertile=nx, nYpertile=ny,
+                        Xtilesize=float(nx), Ytilesize=float(ny))
+    p.cubes[0].length = float(2 * nx)
+    p.cubes[0].width = float(ny)
     big = lib.simulation(p)
     rc, _ = call(L, big, 0.0)
     assert abi.KG_ERR[rc] == "KG_ERR_PARAM", rc
