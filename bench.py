@@ -288,7 +288,7 @@ def run_ensemble(args):
     tuned = autotune.tune(cache=cache, log=lambda m: print(m, file=sys.stderr))
     t_tune = time.perf_counter() - t0
     members = workloads.ensemble(args.members, tiles=lambda side: autotune.tile_for(side, tuned))
-    b = Batch(args.members)
+    b = Batch(args.members, graphs=bool(args.batch_graphs))
     t1 = time.perf_counter()
     ids = [b.add(p, b0) for p, b0, _ in members]
     t_add = time.perf_counter() - t1
@@ -339,7 +339,8 @@ def run_ensemble(args):
             "e2e": {"value": cu / wall, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                     "note": "host clock around the same batch steps (control words only cross per step)"},
             "batch": {"kernel_launches_per_step": (l1 - l0) / args.steps, "rounds_per_step": (r1 - r0) / args.steps,
-                      "device_gb": hbm / 1e9, "autotune_s": t_tune, "add_s": t_add},
+                      "device_gb": hbm / 1e9, "autotune_s": t_tune, "add_s": t_add, "graphs": bool(args.batch_graphs),
+                      "graph_launches_updates_instantiations": list(b.graph_stats())},
             "clocks": clk}
     b.close()
     return line
@@ -663,6 +664,8 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-tend-scale", type=float, default=0.1, help="served stream beside the headline: end-time scale")
     ap.add_argument("--no-extras", action="store_true", help="headline only (no sparse, ensemble and served keys)")
+    ap.add_argument("--batch-graphs", type=int, default=1, help="ensemble / serve: replay the rounds through CUDA graphs")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -758,34 +761,38 @@ def main():
     # end; the bytes are the library's own count of its host<->device copies.
     # (2) e2e_job: the whole job from kg_create (settings and the bed grid uploaded) through
     # the spin-up and the same steps to the final read-back.
-    t_job = time.perf_counter()
-    sim2 = lib.simulation(p, precision=wl["prec"], b0=b0)
-    cu_job = 0
-    if spin > 0.0:
-        cu_job += sim2.integrate_to(spin).cell_updates
-    for _ in range(args.warmup):
-        cu_job += sim2.step(p.tend).cell_updates
-    xb0 = (C.c_int64 * 2)()
-    L.kg_get_transfer_bytes(sim2.h, xb0)
-    cu2, n2 = 0, 0
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        st = sim2.step(p.tend)
-        cu2 += st.cell_updates
-        n2 += st.steps
-        if sim2.time[0] >= p.tend:
-            break
-    fields_bytes = 0
-    for t in sim2.active_tiles():
-        for f in (1, 2, 3, 4):
-            fields_bytes += sim2.field(t, f).nbytes
-    t1 = time.perf_counter()
-    xb1 = (C.c_int64 * 2)()
-    L.kg_get_transfer_bytes(sim2.h, xb1)
-    e2e_s = t1 - t0
-    job_s = t1 - t_job
-    cu_job += cu2
-    sim2.close()
+    e2e_s = job_s = 0.0
+    cu2 = n2 = cu_job = fields_bytes = 0
+    xb0, xb1 = (C.c_int64 * 2)(), (C.c_int64 * 2)()
+    if not args.no_e2e:
+        t_job = time.perf_counter()
+        sim2 = lib.simulation(p, precision=wl["prec"], b0=b0)
+        cu_job = 0
+        if spin > 0.0:
+            cu_job += sim2.integrate_to(spin).cell_updates
+        for _ in range(args.warmup):
+            cu_job += sim2.step(p.tend).cell_updates
+        xb0 = (C.c_int64 * 2)()
+        L.kg_get_transfer_bytes(sim2.h, xb0)
+        cu2, n2 = 0, 0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st = sim2.step(p.tend)
+            cu2 += st.cell_updates
+            n2 += st.steps
+            if sim2.time[0] >= p.tend:
+                break
+        fields_bytes = 0
+        for t in sim2.active_tiles():
+            for f in (1, 2, 3, 4):
+                fields_bytes += sim2.field(t, f).nbytes
+        t1 = time.perf_counter()
+        xb1 = (C.c_int64 * 2)()
+        L.kg_get_transfer_bytes(sim2.h, xb1)
+        e2e_s = t1 - t0
+        job_s = t1 - t_job
+        cu_job += cu2
+        sim2.close()
 
     if rank != 0:
         if dist:
@@ -813,11 +820,11 @@ def main():
         "config": {"workload": args.workload, "desc": wl["desc"], "active_cells_end": active_cells,
                    "l2": "flushed (256 MiB write) between timed steps, outside the timed intervals",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "e2e": {"value": cu2 / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": (xb1[0] - xb0[0]) / max(n2, 1),
+        "e2e": {"value": cu2 / e2e_s if e2e_s > 0 else None, "unit": "cell-updates/s", "h2d_bytes_per_step": (xb1[0] - xb0[0]) / max(n2, 1),
                 "d2h_bytes_per_step": (xb1[1] - xb0[1]) / max(n2, 1),
                 "note": f"host clock around {n2} kg_step calls after the same spin-up, then the read-back of the "
                         f"conserved fields ({fields_bytes} B, counted in d2h)"},
-        "e2e_job": {"value": cu_job / job_s, "unit": "cell-updates/s", "seconds": job_s,
+        "e2e_job": {"value": cu_job / job_s if job_s > 0 else None, "unit": "cell-updates/s", "seconds": job_s,
                     "note": "kg_create with the settings and bed grid uploaded, spin-up, warm-up and the same steps, "
                             "final read-back"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

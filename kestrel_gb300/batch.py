@@ -24,6 +24,8 @@ def _declare(L):
         "kg_batch_finished": ([vp, C.c_int32, P(C.c_int32)], C.c_int),
         "kg_batch_stats": ([vp, P(C.c_int64), P(C.c_int64)], C.c_int),
         "kg_batch_stream": ([vp], vp),
+        "kg_batch_set_graphs": ([vp, C.c_int32], C.c_int),
+        "kg_batch_graph_stats": ([vp, P(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -33,7 +35,7 @@ def _declare(L):
 
 
 class Batch:
-    def __init__(self, max_members: int):
+    def __init__(self, max_members: int, graphs: bool = True):
         self.L = _declare(_lib.load())
         h = C.c_void_p()
         rc = self.L.kg_batch_create(max_members, C.byref(h))
@@ -41,6 +43,13 @@ class Batch:
             raise KestrelError(rc, "kg_batch_create failed")
         self.h = h
         self.params = {}
+        self._check(self.L.kg_batch_set_graphs(self.h, 1 if graphs else 0))
+
+    def graph_stats(self):
+        """(graph launches, in-place updates, instantiations) of the rounds so far."""
+        out = (C.c_int64 * 3)()
+        self._check(self.L.kg_batch_graph_stats(self.h, out))
+        return tuple(out)
 
     def _check(self, rc):
         if rc != abi.KG_OK:

@@ -206,6 +206,15 @@ struct kg_batch {
     int grid_hydro = 0, grid_act = 0;
     int launch_no = 0;
     int64_t launches = 0, rounds = 0;
+    // CUDA graphs: each device segment of a round (between two waits) is captured from the
+    // stream and replayed through one executable graph per segment kind, updated in place
+    // (cudaGraphExecUpdate) when the captured segment differs from the last one.
+    enum { SEG_H = 0, SEG_M1 = 1, SEG_M2 = 2, NSEG = 3 };
+    bool use_graphs = true;
+    bool capturing = false;
+    int seg = -1;
+    cudaGraphExec_t exec[NSEG] = {nullptr, nullptr, nullptr};
+    int64_t graph_launches = 0, graph_updates = 0, graph_instantiations = 0;
     std::string err;
 };
 
@@ -214,6 +223,78 @@ namespace {
 using namespace kg;
 
 void batch_sync(kg_batch& b) { CK(cudaStreamSynchronize(b.st)); }
+
+// Start capturing a segment of the round (everything queued on the batch stream until
+// seg_end); a no-op when graphs are off.
+void seg_begin(kg_batch& b, int seg) {
+    if (!b.use_graphs) return;
+    CK(cudaStreamBeginCapture(b.st, cudaStreamCaptureModeRelaxed));
+    b.capturing = true;
+    b.seg = seg;
+}
+// End the capture and launch it: the segment kind's executable graph is updated in place
+// when the new capture has the same shape, instantiated afresh otherwise.
+void seg_end(kg_batch& b) {
+    if (!b.capturing) return;
+    cudaGraph_t g = nullptr;
+    b.capturing = false;
+    CK(cudaStreamEndCapture(b.st, &g));
+    cudaGraphExec_t& x = b.exec[b.seg];
+    if (x) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(x, g, &info) == cudaSuccess) {
+            b.graph_updates++;
+        } else {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(x);
+            x = nullptr;
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (!x) {
+        e = cudaGraphInstantiate(&x, g, 0);
+        if (e == cudaSuccess) b.graph_instantiations++;
+    }
+    cudaGraphDestroy(g);
+    CK(e);
+    CK(cudaGraphLaunch(x, b.st));
+    b.graph_launches++;
+}
+// Leaves the stream out of capture mode when an error unwinds through a segment.
+struct SegGuard {
+    kg_batch& b;
+    ~SegGuard() {
+        if (!b.capturing) return;
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(b.st, &g);
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        b.capturing = false;
+    }
+};
+
+// Room for `total` edge-band words (grown before a capture starts: no allocation inside one).
+void ensure_actout(kg_batch& b, int total) {
+    if (total <= b.actout_cap) return;
+    batch_sync(b);
+    if (b.d_actout) CK(cudaFree(b.d_actout));
+    if (b.h_actout) CK(cudaFreeHost(b.h_actout));
+    b.d_actout = nullptr;
+    b.h_actout = nullptr;
+    b.actout_cap = 0;
+    int cap = std::max(total, 2 * b.actout_cap);
+    CK(cudaMalloc(&b.d_actout, (size_t)cap * sizeof(int)));
+    CK(cudaMallocHost(&b.h_actout, (size_t)cap * sizeof(int)));
+    b.actout_cap = cap;
+}
+int flags_total(kg_batch& b, const std::vector<int>& who) {
+    int total = 0;
+    for (int id : who) {
+        kg_ctx& c = *b.mem[(size_t)id].c;
+        total += (int)c.active.size() * ((c.SC + 255) / 256);
+    }
+    return total;
+}
 
 // Rebuild the member table on the host and upload it when it changed.
 void refresh_static(kg_batch& b) {
@@ -333,13 +414,7 @@ void queue_flags_batch(kg_batch& b, const std::vector<int>& who, const std::vect
         offsets[(size_t)k] = total;
         total += (int)c.active.size() * per;
     }
-    if (total > b.actout_cap) {
-        if (b.d_actout) CK(cudaFree(b.d_actout));
-        if (b.h_actout) CK(cudaFreeHost(b.h_actout));
-        b.actout_cap = std::max(total, 2 * b.actout_cap);
-        CK(cudaMalloc(&b.d_actout, (size_t)b.actout_cap * sizeof(int)));
-        CK(cudaMallocHost(&b.h_actout, (size_t)b.actout_cap * sizeof(int)));
-    }
+    if (total > b.actout_cap) throw KgError(KG_ERR_STATE, "edge-band buffer not sized before the segment");
     int* dp = b.d_idx + (size_t)(kg_batch::NLAUNCH) * 2 * (b.cap + 1);
     CK(cudaMemcpyAsync(b.d_act, b.h_act, (size_t)n * sizeof(ActJob), cudaMemcpyHostToDevice, b.st));
     CK(cudaMemcpyAsync(dp, hp, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, b.st));
@@ -357,8 +432,13 @@ void reset_ctl(kg_batch& b) {
         for (int k = 0; k < 4; ++k) b.h_ctl[i].cfl[k] = HUGE_BITS;
     CK(cudaMemcpyAsync(b.d_ctl, b.h_ctl, (size_t)b.cap * sizeof(kg_ctx::Ctl), cudaMemcpyHostToDevice, b.st));
 }
-void collect_ctl(kg_batch& b) {
+void read_ctl(kg_batch& b) {
     CK(cudaMemcpyAsync(b.h_ctl, b.d_ctl, (size_t)b.cap * sizeof(kg_ctx::Ctl), cudaMemcpyDeviceToHost, b.st));
+}
+// The end of a segment: the control words come back, the segment runs, one wait.
+void collect_ctl(kg_batch& b) {
+    read_ctl(b);
+    seg_end(b);
     batch_sync(b);
 }
 
@@ -395,7 +475,6 @@ void guard(Member& m) {
 // Phase H: RHS + device dt for fresh members, the three stages for fresh and retrying
 // members, flags for hydraulic-only members; one wait; the host's tests.
 void phase_h(kg_batch& b, const std::vector<int>& who) {
-    reset_ctl(b);
     std::vector<int> fresh;
     std::vector<StepArgs> ra;
     for (int id : who) {
@@ -410,6 +489,13 @@ void phase_h(kg_batch& b, const std::vector<int>& who) {
             ra.push_back(member_args(c, rhs_args(c, c.qcur, 0, c.tcur, c.t), W_RHS));
         }
     }
+    std::vector<int> hydro_only;
+    for (int id : who)
+        if (!b.mem[(size_t)id].morpho) hydro_only.push_back(id);
+    ensure_actout(b, flags_total(b, hydro_only));
+    SegGuard seg_guard{b};
+    seg_begin(b, kg_batch::SEG_H);
+    reset_ctl(b);
     launch_hydro_batch(b, fresh, ra);
     if (!fresh.empty()) {
         int n = (int)fresh.size();
@@ -487,7 +573,6 @@ void launch_m(kg_batch& b, int t, int n, int total, int stage = 0) {
 // for all of them), its checks and redistribution, then the batched RHS check and second
 // H.
 void phase_m(kg_batch& b, const std::vector<int>& who) {
-    reset_ctl(b);
     for (int id : who) {
         Member& m = b.mem[(size_t)id];
         kg_ctx& c = *m.c;
@@ -506,6 +591,9 @@ void phase_m(kg_batch& b, const std::vector<int>& who) {
         }
         c.launches += 11;
     }
+    SegGuard seg_guard{b};
+    seg_begin(b, kg_batch::SEG_M1);
+    reset_ctl(b);
     int n = (int)who.size();
     int total = upload_mjobs(b, 0, who);
     launch_m<MK_INIT>(b, 0, n, total);
@@ -574,10 +662,6 @@ void phase_m(kg_batch& b, const std::vector<int>& who) {
     }
     if (go.empty()) return;
     // Interfacial topography of the new bed and the M result, for every member at once.
-    int ng = (int)go.size();
-    int tg = upload_mjobs(b, 1, go);
-    // interfacial topography, the M result and the active tiles' factor cache, fused
-    launch_m<MK_CLOSE>(b, 1, ng, tg);
     std::vector<int> whole;
     for (int id : go) {
         Member& m = b.mem[(size_t)id];
@@ -585,6 +669,14 @@ void phase_m(kg_batch& b, const std::vector<int>& who) {
         c.launches += 1;
         if (c.tdirty[m.tnew] > 1) whole.push_back(id);
     }
+    ensure_actout(b, flags_total(b, go));
+    // A member whose ghost tiles never had the factors of this topography set rebuilds them
+    // through context-owned lists (host copies), so that segment is not captured.
+    if (whole.empty()) seg_begin(b, kg_batch::SEG_M2);
+    int ng = (int)go.size();
+    int tg = upload_mjobs(b, 1, go);
+    // interfacial topography, the M result and the active tiles' factor cache, fused
+    launch_m<MK_CLOSE>(b, 1, ng, tg);
     for (int id : whole) {            // ghost factors too where they were never built
         kg_ctx& c = *b.mem[(size_t)id].c;
         bind_constants(c);
@@ -844,10 +936,27 @@ int kg_batch_stats(kg_batch* b, int64_t* launches, int64_t* rounds) {
 
 void* kg_batch_stream(kg_batch* b) { return b ? (void*)b->st : nullptr; }
 
+int kg_batch_set_graphs(kg_batch* b, int32_t enable) {
+    if (!b) return KG_ERR_PARAM;
+    std::lock_guard<std::recursive_mutex> lock(g_api_mu);
+    b->use_graphs = enable != 0;
+    return KG_OK;
+}
+
+int kg_batch_graph_stats(kg_batch* b, int64_t out[3]) {
+    if (!b || !out) return KG_ERR_PARAM;
+    out[0] = b->graph_launches;
+    out[1] = b->graph_updates;
+    out[2] = b->graph_instantiations;
+    return KG_OK;
+}
+
 void kg_batch_destroy(kg_batch* b) {
     if (!b) return;
     std::lock_guard<std::recursive_mutex> lock(g_api_mu);
     if (b->st) cudaStreamSynchronize(b->st);
+    for (cudaGraphExec_t& x : b->exec)
+        if (x) cudaGraphExecDestroy(x);
     for (Member& m : b->mem)
         if (m.c) kg_destroy(m.c);
     cudaFree(b->d_ctl);

@@ -57,6 +57,28 @@ def test_batch_members_match_alone():
     b.close()
 
 
+def test_batch_graphs_on_and_off_identical():
+    """The rounds replayed through CUDA graphs (the default) and launched directly on the
+    stream give bit-identical members; with graphs on, every segment ran as a graph and
+    most rounds updated an existing executable graph in place."""
+    ps = [f() for f in INPUTS]
+    out = {}
+    for graphs in (True, False):
+        b = Batch(8, graphs=graphs)
+        ids = [b.add(p) for p in ps]
+        b.run()
+        out[graphs] = [snapshot(b.member(i)) for i in ids]
+        gl, gu, gi = b.graph_stats()
+        _, rounds = b.stats()
+        if graphs:
+            assert gl >= rounds and gu > gi > 0, (gl, gu, gi, rounds)
+        else:
+            assert gl == 0
+        b.close()
+    for x, y in zip(out[True], out[False]):
+        same(x, y)
+
+
 def test_batch_late_join_and_leave():
     ps = [f() for f in INPUTS[:3]]
     ref = [alone(p) for p in ps]

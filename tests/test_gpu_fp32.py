@@ -6,9 +6,11 @@ reconstruction, fluxes, closures and momentum rows in FP32.  Its stated error ag
 the FP64 oracle, per field, relative L-inf over the active cells (w: relative to the
 largest depth, the scale its error lives on):
 
-  hydraulic runs (cap release 3 s, reference cap/flux inputs)   w, Hn <= 2e-5, momenta <= 5e-5
-  morphodynamic reference inputs (cap_morpho 1 s, flux_morpho 2 s)  w, Hn, momenta <= 5e-4,
-                                                                   Hnpsi <= 2e-3, bt <= 2e-2
+  hydraulic runs (cap release 3 s, reference cap/flux inputs)   w, Hn <= 5e-6, momenta <= 2e-5,
+                                                                Hnpsi <= 1e-6
+  morphodynamic reference inputs (cap_morpho 1 s, flux_morpho 2 s)  every field <= 1e-5
+  the 2048^2 morphodynamic configuration on a 256^2 window of its terrain, 750 steps:
+                                                                w, Hn <= 1e-5, bt <= 1e-4
 Conservation of volume and solids stays at FP64 round-off (<= 1e-12, the reference's own
 bar is 1e-10), depth stays >= 0, a lake at rest stays at rest to |u| <= 1e-5 m/s, and the
 active and ghost tile sets are identical to the oracle's.
@@ -57,9 +59,9 @@ def test_fp32_hydraulic_error(name, tend):
     assert g.active_tiles() == o.active_tiles() and g.ghost_tiles() == o.ghost_tiles()
     assert sg.steps == so.steps
     e = field_errors(g, o)
-    assert e["w"] <= 2e-5 and e["Hn"] <= 2e-5, e
-    assert e["rhoHnu"] <= 5e-5 and e["rhoHnv"] <= 5e-5, e
-    assert e["Hnpsi"] <= 2e-5, e
+    assert e["w"] <= 5e-6 and e["Hn"] <= 5e-6, e
+    assert e["rhoHnu"] <= 2e-5 and e["rhoHnv"] <= 2e-5, e
+    assert e["Hnpsi"] <= 1e-6, e
     for t in g.active_tiles():
         assert (g.field(t, 5) >= 0).all()
 
@@ -72,8 +74,8 @@ def test_fp32_morphodynamic_error(name, tend):
     o.run()
     assert g.active_tiles() == o.active_tiles() and g.ghost_tiles() == o.ghost_tiles()
     e = field_errors(g, o)
-    assert max(e["w"], e["Hn"], e["rhoHnu"], e["rhoHnv"]) <= 5e-4, e
-    assert e["Hnpsi"] <= 2e-3 and e["bt"] <= 2e-2, e
+    assert max(e["w"], e["Hn"], e["rhoHnu"], e["rhoHnv"]) <= 1e-5, e
+    assert e["Hnpsi"] <= 1e-5 and e["bt"] <= 1e-5, e
     for t in g.active_tiles():
         assert g.field(t, 11).min() >= -p.EroDepth
 
@@ -112,3 +114,23 @@ def test_fp32_rejects_noalloc_entry_point():
     g = fp32(cases.ref_input("flux_hydro_2d", tend=1.0, nout=1))
     dt = C.c_double()
     assert abi.KG_ERR[L.kg_hydraulic_rhs_noalloc(g.h, 0.0, 1, C.byref(dt))] == "KG_ERR_UNSUPPORTED"
+
+
+def test_fp32_morpho_flux_window_depth_error():
+    """The 2048^2 morphodynamic configuration's own terrain, source and closures (Voellmy,
+    mixed erosion with 2 m erodible depth, eddy viscosity 1e-2) on a 256^2 window of its
+    terrain in 32^2 tiles (workloads.morpho_flux_window): after 750 accepted steps (t = 15 s,
+    with about 2,400 refused attempts) the FP32 form's depth is within 1e-5 of the largest
+    depth of the FP64 oracle's, relative L-inf, with identical step and refusal counts and
+    identical active tiles (measured: 4.3e-6).  On this rough terrain the error then grows as wet/dry fronts move apart (3.6e-5 at t = 20 s), while the
+    oracle's own result moves by only about 1e-10 when its transcendentals are nudged."""
+    from kestrel_gb300 import workloads
+    p, b0 = workloads.morpho_flux_window(tend=15.0)
+    g, o = fp32(p, b0=b0), _oracle.simulation(p, b0=b0)
+    sg, so = g.integrate_to(15.0), o.integrate_to(15.0)
+    assert (sg.steps, sg.rejected) == (so.steps, so.rejected), (sg.steps, sg.rejected, so.steps, so.rejected)
+    assert sg.steps >= 600
+    assert g.active_tiles() == o.active_tiles()
+    e = field_errors(g, o)
+    assert e["Hn"] <= 1e-5 and e["w"] <= 1e-5, e
+    assert e["bt"] <= 1e-4, e
