@@ -674,8 +674,9 @@ size_t hydro_smem_bytes() { return sizeof(HydroSmem); }
 cudaError_t set_constants(const DevParams& p, const DevSource* src, int nsrc, cudaStream_t st) {
     cudaError_t e = cudaMemcpyToSymbolAsync(cP, &p, sizeof(DevParams), 0, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
-    static DevParams32 p32;  // the copy is asynchronous: keep the source alive
-    p32 = params32(p);
+    // A copy from pageable host memory is staged before the call returns, so a local
+    // source is safe.
+    const DevParams32 p32 = params32(p);
     e = cudaMemcpyToSymbolAsync(cP32, &p32, sizeof(DevParams32), 0, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     if (nsrc > 0) e = cudaMemcpyToSymbolAsync(cSrc, src, sizeof(DevSource) * nsrc, 0, cudaMemcpyHostToDevice, st);
@@ -683,11 +684,16 @@ cudaError_t set_constants(const DevParams& p, const DevSource* src, int nsrc, cu
 }
 
 cudaError_t launch_hydro(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_hydro, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(HydroSmem));
+    // the shared-memory opt-in is a per-device function attribute: set once per device
+    static bool attr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!attr[dev]) {
+        e = cudaFuncSetAttribute(k_hydro, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(HydroSmem));
         if (e != cudaSuccess) return e;
-        attr = true;
+        attr[dev] = true;
     }
     if (nblocks == 0) return cudaSuccess;
     KG_TRY_LAUNCH(kg_launch(k_hydro, nblocks, NT, sizeof(HydroSmem), st, A, blocks, S));

@@ -72,6 +72,16 @@ __device__ __forceinline__ double flux_sum4(float a, float b, float c, float d) 
 // the FP64 differences exactly as the limiters of src/Limiters.f90:68-184 do (the sign and
 // magnitude tests are taken on the bit patterns); van Albada and WENO take their weight in
 // FP32.
+// x * 2^-k (k = 1, 2) on the integer pipe: the exponent field of a normal, finite double
+// is lowered by k (exact); zeros, subnormals near the bottom and non-finite values take the
+// FP64 multiply.
+__device__ __forceinline__ double scale_down_pow2(double x, int k) {
+    const int hi = __double2hiint(x);
+    const int e = (hi >> 20) & 0x7FF;
+    if (e > k && e < 0x7FF) return __hiloint2double(hi - (k << 20), __double2loint(x));
+    return x * (k == 1 ? 0.5 : 0.25);
+}
+
 __device__ __forceinline__ double half_step_w(int lim, double a, double b) {
     const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
     const long long ma = ia & 0x7FFFFFFFFFFFFFFFll, mb = ib & 0x7FFFFFFFFFFFFFFFll;
@@ -80,12 +90,12 @@ __device__ __forceinline__ double half_step_w(int lim, double a, double b) {
         case KG_LIM_MINMOD2: {
             if ((ia ^ ib) < 0 || ma == 0 || mb == 0) return 0.0;  // a * b <= 0
             const double m = ma < mb ? a : b;                    // the one nearer zero
-            if (lim == KG_LIM_MINMOD1) return 0.5 * m;
+            if (lim == KG_LIM_MINMOD1) return scale_down_pow2(m, 1);
             // min(theta a, theta b, (a + b)/2) of the same sign, halved (exactly: powers of 2)
-            const double t1 = (0.5 * 1.3) * m, t2 = 0.25 * (a + b);
+            const double t1 = (0.5 * 1.3) * m, t2 = scale_down_pow2(a + b, 2);
             return (__double_as_longlong(t1) & 0x7FFFFFFFFFFFFFFFll) < (__double_as_longlong(t2) & 0x7FFFFFFFFFFFFFFFll) ? t1 : t2;
         }
-        case KG_LIM_NONE: return 0.25 * (a + b);
+        case KG_LIM_NONE: return scale_down_pow2(a + b, 2);
         default: return 0.5 * (double)limiter<float>(lim, (float)a, (float)b);
     }
 }
@@ -557,11 +567,16 @@ __global__ void __launch_bounds__(256) k_topo32(DevArrays A, const int* __restri
 size_t hydro32_smem_bytes() { return sizeof(Hydro32Smem); }
 
 cudaError_t launch_hydro32(const DevArrays& A, const BlockDesc* blocks, int nblocks, const StepArgs& S, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_hydro32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Hydro32Smem));
+    // the shared-memory opt-in is a per-device function attribute: set once per device
+    static bool attr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!attr[dev]) {
+        e = cudaFuncSetAttribute(k_hydro32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Hydro32Smem));
         if (e != cudaSuccess) return e;
-        attr = true;
+        attr[dev] = true;
     }
     if (nblocks == 0) return cudaSuccess;
     KG_TRY_LAUNCH(kg_launch(k_hydro32, nblocks, NT, sizeof(Hydro32Smem), st, A, blocks, S));
