@@ -79,3 +79,12 @@ def test_autotune_candidates_and_mapping(tmp_path):
     cache.write_text('{"256": 32, "1024": 64}')
     assert autotune.tune(cache=str(cache)) == {256: 32, 1024: 64}  # read back without trials
     assert math.isfinite(autotune.tile_for(300, autotune.tune(cache=str(cache))))
+
+
+def test_autotune_choice_is_stable_within_the_noise():
+    """Candidates within 5% of the fastest resolve to the largest of them; a smaller tile
+    wins only when it is faster by more than that."""
+    assert autotune.choose({16: 1.00, 32: 0.97, 64: 1.00}) == 64
+    assert autotune.choose({16: 1.00, 32: 0.90, 64: 1.00}) == 32
+    assert autotune.choose({32: 2.0, 64: 2.08}) == 64
+    assert autotune.choose({32: 2.0, 64: 2.2}) == 32
