@@ -754,6 +754,11 @@ void prepare(kg_batch& b, Member& m) {
 // the M phase; a member that completes its step starts the next one in the next round,
 // so no member waits for another's retries.
 void batch_step(kg_batch& b) {
+    // A round makes at most NLAUNCH (8) batched hydraulic launches: the RHS and three stages
+    // of H, the RHS check and three stages of the second H.  Numbering them from 0 every round
+    // gives each position the same table slot, so a segment captured in one round has the
+    // same kernel arguments as the last one whenever its jobs are unchanged.
+    b.launch_no = 0;
     std::vector<int> live;
     for (int i = 0; i < b.cap; ++i)
         if (b.mem[(size_t)i].c && !b.mem[(size_t)i].finished) live.push_back(i);
