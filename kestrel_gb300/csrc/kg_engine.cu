@@ -46,8 +46,8 @@ cudaError_t launch_ghost_dirichlet(const DevArrays& A, int slot, double H, doubl
 cudaError_t launch_ghost_edges(const DevArrays& A, int slot, int mask, int qcur, cudaStream_t st);
 cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, int ts, cudaStream_t st);
 cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st);
-cudaError_t launch_gather_state(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, int SC, int SV, double* u4,
-                                double* btv, cudaStream_t st);
+cudaError_t launch_gather_state(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, int SC, int SV, bool mom32,
+                                double* u4, double* btv, cudaStream_t st);
 cudaError_t launch_act_flags(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn_over, int* d_flags,
                              int nX, int nY, cudaStream_t st);
 cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, const double* hn, const double* rho,
@@ -209,6 +209,42 @@ cudaError_t kg_cpy(kg_ctx& c, void* dst, const void* src, size_t n, cudaMemcpyKi
 
 
 namespace {
+
+// The FP32 form keeps the momenta of a slot's state in FP32: its momentum plane (plane 1
+// of the slot's four) holds rhoHnu as SC floats followed by rhoHnv as SC floats, and plane
+// 2 is unused; the FP64 form keeps four FP64 planes.  These convert one slot's four
+// planes between the host's FP64 layout and the context's.
+void pack_state(const kg_ctx& c, const double* in, double* out) {
+    const size_t SC = (size_t)c.SC;
+    if (c.prec != KG_PREC_FP32) {
+        std::memmove(out, in, 4 * SC * sizeof(double));
+        return;
+    }
+    std::vector<float> m(2 * SC);
+    for (size_t k = 0; k < SC; ++k) {
+        m[k] = (float)in[SC + k];
+        m[SC + k] = (float)in[2 * SC + k];
+    }
+    std::memmove(out, in, SC * sizeof(double));
+    std::memmove(out + 3 * SC, in + 3 * SC, SC * sizeof(double));
+    std::memcpy(out + SC, m.data(), 2 * SC * sizeof(float));
+    std::fill(out + 2 * SC, out + 3 * SC, 0.0);
+}
+void unpack_state(const kg_ctx& c, const double* in, double* out) {
+    const size_t SC = (size_t)c.SC;
+    if (c.prec != KG_PREC_FP32) {
+        std::memmove(out, in, 4 * SC * sizeof(double));
+        return;
+    }
+    std::vector<float> m(2 * SC);
+    std::memcpy(m.data(), in + SC, 2 * SC * sizeof(float));
+    std::memmove(out, in, SC * sizeof(double));
+    std::memmove(out + 3 * SC, in + 3 * SC, SC * sizeof(double));
+    for (size_t k = 0; k < SC; ++k) {
+        out[SC + k] = (double)m[k];
+        out[2 * SC + k] = (double)m[SC + k];
+    }
+}
 
 // The run settings and source table live in the device's __constant__ bank, shared by
 // every context of the process.  The context whose settings are loaded owns it; another
@@ -1397,6 +1433,7 @@ void load_sources(kg_ctx& c) {
         CK(kg_cpy(c, bufs[q].ct.data(), c.A.CT[c.tcur] + (size_t)s * 4 * SC, (size_t)4 * SC * sizeof(double), cudaMemcpyDeviceToHost));
     }
     sync(c);
+    for (auto& B : bufs) unpack_state(c, B.q.data(), B.q.data());
     double rhow = c.p.rhow, rhos = c.p.rhos;
     for (auto& m : mods) {
         size_t q = std::find(touched.begin(), touched.end(), m.id) - touched.begin();
@@ -1480,6 +1517,7 @@ void load_sources(kg_ctx& c) {
     }
     for (size_t q = 0; q < touched.size(); ++q) {
         int s = T(c, touched[q]).slot;
+        pack_state(c, bufs[q].q.data(), bufs[q].q.data());
         CK(kg_cpy(c, c.A.Q[c.qcur] + (size_t)s * 4 * SC, bufs[q].q.data(), (size_t)4 * SC * sizeof(double), cudaMemcpyHostToDevice));
         CK(kg_cpy(c, c.d_srcHn + (size_t)s * SC, bufs[q].hn.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice));
         CK(kg_cpy(c, c.d_srcRho + (size_t)s * SC, bufs[q].rho.data(), (size_t)SC * sizeof(double), cudaMemcpyHostToDevice));
@@ -1532,11 +1570,13 @@ void load_state(kg_ctx& c, const int32_t* ids, int n, const double* state, const
     }
     int SC = c.SC, SV = c.SV;
     std::vector<int> slots;
+    std::vector<double> packed((size_t)n * 4 * SC);
     for (int k = 0; k < n; ++k) {
         int s = T(c, ids[k]).slot;
         slots.push_back(s);
-        CK(kg_cpy(c, c.A.Q[c.qcur] + (size_t)s * 4 * SC, state + (size_t)k * 4 * SC, (size_t)4 * SC * sizeof(double),
-                           cudaMemcpyHostToDevice));
+        double* pk = packed.data() + (size_t)k * 4 * SC;
+        pack_state(c, state + (size_t)k * 4 * SC, pk);
+        CK(kg_cpy(c, c.A.Q[c.qcur] + (size_t)s * 4 * SC, pk, (size_t)4 * SC * sizeof(double), cudaMemcpyHostToDevice));
         if (btv)
             CK(kg_cpy(c, c.A.BV[c.tcur] + ((size_t)s * 2 + 1) * SV, btv + (size_t)k * SV, (size_t)SV * sizeof(double),
                                cudaMemcpyHostToDevice));
@@ -1968,7 +2008,11 @@ int kg_get_tile_field(kg_ctx* c, int32_t id, int32_t field, double* out) {
     if (field < 1 || field > 13 || !out) return KG_ERR_PARAM;
     KG_GUARD(c, {
         int SC = c->SC;
-        if (field <= 4) {
+        if ((field == 2 || field == 3) && c->prec == KG_PREC_FP32) {
+            auto v = d2h(c, c->A.Q[c->qcur] + ((size_t)s * 4 + 1) * SC, SC);
+            const float* m = reinterpret_cast<const float*>(v.data()) + (field == 3 ? SC : 0);
+            for (int k = 0; k < SC; ++k) out[k] = (double)m[k];
+        } else if (field <= 4) {
             auto v = d2h(c, c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * SC, SC);
             std::memcpy(out, v.data(), SC * sizeof(double));
         } else if (field >= 10) {
@@ -2027,7 +2071,7 @@ int kg_get_state(kg_ctx* c, int32_t* ids, int32_t* n, double* state, double* bt_
         upload_list(*c, slots);
         double* du4 = c->d_gather;
         double* dbt = c->d_gather + (size_t)na * 4 * SC;
-        CK(launch_gather_state(c->A, c->d_list, na, c->qcur, c->tcur, (int)SC, (int)SV, du4, dbt, c->st));
+        CK(launch_gather_state(c->A, c->d_list, na, c->qcur, c->tcur, (int)SC, (int)SV, c->prec == KG_PREC_FP32, du4, dbt, c->st));
         c->launches++;
         if (state) CK(kg_cpy(*c, state, du4, (size_t)na * 4 * SC * sizeof(double), cudaMemcpyDeviceToHost));
         if (bt_vertex) CK(kg_cpy(*c, bt_vertex, dbt, (size_t)na * SV * sizeof(double), cudaMemcpyDeviceToHost));
@@ -2044,8 +2088,17 @@ int kg_set_tile_field(kg_ctx* c, int32_t id, int32_t field, const double* in) {
     if (field < 1 || field > 4 || !in) return KG_ERR_PARAM;
     c->gen++;
     KG_GUARD(c, {
-        CK(kg_cpy(*c, c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * c->SC, in, (size_t)c->SC * sizeof(double),
-                           cudaMemcpyHostToDevice));
+        if ((field == 2 || field == 3) && c->prec == KG_PREC_FP32) {
+            // the FP32 form's momentum plane holds both momenta as floats
+            double* pl = c->A.Q[c->qcur] + ((size_t)s * 4 + 1) * c->SC;
+            auto v = d2h(c, pl, (size_t)c->SC);
+            float* m = reinterpret_cast<float*>(v.data()) + (field == 3 ? c->SC : 0);
+            for (int k = 0; k < c->SC; ++k) m[k] = (float)in[k];
+            CK(kg_cpy(*c, pl, v.data(), (size_t)c->SC * sizeof(double), cudaMemcpyHostToDevice));
+        } else {
+            CK(kg_cpy(*c, c->A.Q[c->qcur] + ((size_t)s * 4 + field - 1) * c->SC, in, (size_t)c->SC * sizeof(double),
+                               cudaMemcpyHostToDevice));
+        }
         sync(*c);
     });
     return KG_OK;
@@ -2071,9 +2124,17 @@ int kg_get_tile_rhs(kg_ctx* c, int32_t id, int32_t k, double* out) {
     if (s < 0) return KG_ERR_NOT_FOUND;
     if (k < 1 || k > 5 || !out) return KG_ERR_PARAM;
     KG_GUARD(c, {
-        const double* src = k <= 4 ? c->A.E[0] + ((size_t)s * 4 + k - 1) * c->SC : c->A.I[0] + (size_t)s * c->SC;
-        auto v = d2h(c, src, c->SC);
-        std::memcpy(out, v.data(), (size_t)c->SC * sizeof(double));
+        if (c->prec == KG_PREC_FP32 && (k == 2 || k == 3 || k == 5)) {
+            // the FP32 form's momentum rows and ddtImplicit are stored as floats
+            const double* src = k == 5 ? c->A.I[0] + (size_t)s * c->SC : c->A.E[0] + ((size_t)s * 4 + 1) * c->SC;
+            auto v = d2h(c, src, c->SC);
+            const float* f = reinterpret_cast<const float*>(v.data()) + (k == 3 ? c->SC : 0);
+            for (int q = 0; q < c->SC; ++q) out[q] = (double)f[q];
+        } else {
+            const double* src = k <= 4 ? c->A.E[0] + ((size_t)s * 4 + k - 1) * c->SC : c->A.I[0] + (size_t)s * c->SC;
+            auto v = d2h(c, src, c->SC);
+            std::memcpy(out, v.data(), (size_t)c->SC * sizeof(double));
+        }
     });
     return KG_OK;
 }

@@ -120,6 +120,19 @@ __device__ __forceinline__ void face_sides(double dlo, double dhi, double hs, in
     }
 }
 
+// The FP32 form stores the momenta in FP32: the state's momentum plane (plane 1 of a slot's
+// four) holds rhoHnu as SC floats followed by rhoHnv as SC floats (plane 2 is unused); the
+// momentum rows of ddtExplicit are packed the same way and ddtImplicit holds SC floats.
+// The FP64 free surface and Hnpsi keep their planes.
+__device__ __forceinline__ float* mom32(double* Q, int s, int SC) { return reinterpret_cast<float*>(Q + plane(s, 4, 1, SC)); }
+__device__ __forceinline__ const float* mom32(const double* Q, int s, int SC) {
+    return reinterpret_cast<const float*>(Q + plane(s, 4, 1, SC));
+}
+__device__ __forceinline__ float* imp32(double* I, int s, int SC) { return reinterpret_cast<float*>(I + plane(s, 1, 0, SC)); }
+__device__ __forceinline__ const float* imp32(const double* I, int s, int SC) {
+    return reinterpret_cast<const float*>(I + plane(s, 1, 0, SC));
+}
+
 struct Side32 {
     float hp, p, u, v, rho, du, dv;  // hp: face free surface minus InterpolateB at the face
 };
@@ -227,19 +240,21 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
         double w, pp;
         float m1, m2;
         size_t q = plane(s, 4, 0, SC) + c;
+        const float* Qm = mom32(Qin, s, SC);
         if (S.mode == MODE_S1) {
             // stage 1 on the fly (src/TimeStepper.f90:371-404): w, Hnpsi in FP64
             const double* E = A.E[S.e_set];
-            float I = (float)A.I[S.e_set][plane(s, 1, 0, SC) + c];
+            const float* Em = mom32(E, s, SC);
+            float I = imp32(A.I[S.e_set], s, SC)[c];
             w = Qin[q] + Tm.dt * E[q];
             pp = Qin[q + 3 * (size_t)SC] + Tm.dt * E[q + 3 * (size_t)SC];
             float den = 1.f / (1.f - dtf * I);
-            m1 = ((float)Qin[q + SC] + dtf * (float)E[q + SC]) * den;
-            m2 = ((float)Qin[q + 2 * (size_t)SC] + dtf * (float)E[q + 2 * (size_t)SC]) * den;
+            m1 = (Qm[c] + dtf * Em[c]) * den;
+            m2 = (Qm[SC + c] + dtf * Em[SC + c]) * den;
         } else {
             w = Qin[q];
-            m1 = (float)Qin[q + SC];
-            m2 = (float)Qin[q + 2 * (size_t)SC];
+            m1 = Qm[c];
+            m2 = Qm[SC + c];
             pp = Qin[q + 3 * (size_t)SC];
         }
         float hp = (float)(w - TD[plane(s, 3, 0, SC) + c]);
@@ -436,10 +451,11 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
         if (S.mode == MODE_RHS0) {
             double* Ed = A.E[S.e_set] + plane(slot, 4, 0, SC) + c;
             Ed[0] = E0;
-            Ed[SC] = (double)E1;
-            Ed[2 * (size_t)SC] = (double)E2;
+            float* Edm = mom32(A.E[S.e_set], slot, SC);
+            Edm[c] = E1;
+            Edm[SC + c] = E2;
             Ed[3 * (size_t)SC] = E3;
-            A.I[S.e_set][plane(slot, 1, 0, SC) + c] = I;
+            imp32(A.I[S.e_set], slot, SC)[c] = I;
         } else if (S.mode == MODE_S1 || S.mode == MODE_S2) {
             const double* q0p = A.Q[S.q_in] + plane(slot, 4, 0, SC) + c;
             double b = td[0];
@@ -450,16 +466,19 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             if (S.mode == MODE_S1) { a0 = 0.75; a1 = 0.25; }
             else { a0 = 1.0 / 3.0; a1 = 2.0 / 3.0; }
             dst[0] = b + (a0 * hp_old + a1 * (hp_new + Tm.dt * E0));
-            dst[SC] = (double)((float)a0 * (float)q0p[SC] + (float)a1 * (sm.m1[r] + dtf * E1) * den);
-            dst[2 * (size_t)SC] = (double)((float)a0 * (float)q0p[2 * (size_t)SC] + (float)a1 * (sm.m2[r] + dtf * E2) * den);
+            const float* q0m = mom32(A.Q[S.q_in], slot, SC);
+            float* dm = mom32(A.Q[S.mode == MODE_S1 ? S.q_s1 : S.q_s2], slot, SC);
+            dm[c] = (float)a0 * q0m[c] + (float)a1 * (sm.m1[r] + dtf * E1) * den;
+            dm[SC + c] = (float)a0 * q0m[SC + c] + (float)a1 * (sm.m2[r] + dtf * E2) * den;
             dst[3 * (size_t)SC] = a0 * q0p[3 * (size_t)SC] + a1 * (sm.p64[r] + Tm.dt * E3);
         } else {
             float dt2I = dtf * dtf * I;
             float den = 1.f / (1.f + dt2I * I);
             double* dst = A.Q[S.q_out] + plane(slot, 4, 0, SC) + c;
             dst[0] = sm.w[r];
-            dst[SC] = (double)((sm.m1[r] - dt2I * E1) * den);
-            dst[2 * (size_t)SC] = (double)((sm.m2[r] - dt2I * E2) * den);
+            float* dm = mom32(A.Q[S.q_out], slot, SC);
+            dm[c] = (sm.m1[r] - dt2I * E1) * den;
+            dm[SC + c] = (sm.m2[r] - dt2I * E2) * den;
             dst[3 * (size_t)SC] = sm.p64[r];
             A.UV[plane(slot, 2, 0, SC) + c] = (double)sm.u[r];
             A.UV[plane(slot, 2, 1, SC) + c] = (double)sm.v[r];
@@ -473,7 +492,8 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
                 float gamt = gam_of<float>(P.geo, bxt, byt);
                 float hpt = (float)((q0p[0] - ct0[0]) - btt);
                 float Hn, psi, rho, u, v;
-                desing32(F, hpt, gamt, (float)q0p[SC], (float)q0p[2 * (size_t)SC], (float)q0p[3 * (size_t)SC], Hn, psi, rho, u, v);
+                const float* q0m = mom32(A.Q[S.q_tc], slot, SC);
+                desing32(F, hpt, gamt, q0m[c], q0m[SC + c], (float)q0p[3 * (size_t)SC], Hn, psi, rho, u, v);
                 double* M = A.MX + plane(slot, 11, 0, SC) + c;
                 double tt = Tm.t_max;
                 double Hnd = Hn, psid = psi;

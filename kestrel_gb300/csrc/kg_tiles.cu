@@ -388,24 +388,34 @@ cudaError_t launch_activate(const DevArrays& A, int slot, int qcur, int ts, cuda
 // The state of the listed tiles packed for one read-back: the four conserved planes of
 // each tile (w, rhoHnu, rhoHnv, Hnpsi, contiguous per slot) into u4[k][4][SC] and its
 // vertex bed change into btv[k][SV], k in list order.
+// (In the FP32 form, mom32, the momentum plane holds both momenta as floats; they are
+// widened into planes 1 and 2 of the packed state.)
 __global__ void __launch_bounds__(256) k_gather_state(DevArrays A, const int* __restrict__ slots, int n, int qcur, int ts,
-                                                      int SC, int SV, double* __restrict__ u4, double* __restrict__ btv) {
+                                                      int SC, int SV, int mom32, double* __restrict__ u4,
+                                                      double* __restrict__ btv) {
     kg_dep_wait();
     const long long per = 4LL * SC + SV, total = per * n;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
         int k = (int)(e / per);
         long long r = e - k * per;
         int s = slots[k];
-        if (r < 4LL * SC) u4[(size_t)k * 4 * SC + r] = A.Q[qcur][(size_t)s * 4 * SC + r];
-        else btv[(size_t)k * SV + (r - 4LL * SC)] = A.BV[ts][((size_t)s * 2 + 1) * SV + (r - 4LL * SC)];
+        if (r < 4LL * SC) {
+            const double* q = A.Q[qcur] + (size_t)s * 4 * SC;
+            double v;
+            if (mom32 && r >= SC && r < 3LL * SC) v = (double)reinterpret_cast<const float*>(q + SC)[r - SC];
+            else v = q[r];
+            u4[(size_t)k * 4 * SC + r] = v;
+        } else {
+            btv[(size_t)k * SV + (r - 4LL * SC)] = A.BV[ts][((size_t)s * 2 + 1) * SV + (r - 4LL * SC)];
+        }
     }
 }
-cudaError_t launch_gather_state(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, int SC, int SV, double* u4,
-                                double* btv, cudaStream_t st) {
+cudaError_t launch_gather_state(const DevArrays& A, const int* d_slots, int n, int qcur, int ts, int SC, int SV, bool mom32,
+                                double* u4, double* btv, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     long long total = (4LL * SC + SV) * n;
     int grid = (int)std::min<long long>((total + 255) / 256, 152LL * 8);
-    KG_TRY_LAUNCH(kg_launch(k_gather_state, grid, 256, 0, st, A, d_slots, n, qcur, ts, SC, SV, u4, btv));
+    KG_TRY_LAUNCH(kg_launch(k_gather_state, grid, 256, 0, st, A, d_slots, n, qcur, ts, SC, SV, mom32 ? 1 : 0, u4, btv));
     return cudaGetLastError();
 }
 cudaError_t launch_init_maxima(const DevArrays& A, int slot, cudaStream_t st) {
