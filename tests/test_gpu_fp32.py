@@ -134,3 +134,33 @@ def test_fp32_morpho_flux_window_depth_error():
     e = field_errors(g, o)
     assert e["Hn"] <= 1e-5 and e["w"] <= 1e-5, e
     assert e["bt"] <= 1e-4, e
+
+
+def test_fp32_state_round_trip():
+    """The FP32 form stores its momenta as floats packed in the momentum plane: the
+    per-tile getters, kg_get_state and kg_set_tile_field convert, and a context restarted
+    from kg_get_state (kg_load_state) continues bit for bit with the uninterrupted one."""
+    from kestrel_gb300.solver import Simulation
+    p = cases.ref_input("cap_morpho_2d", tend=0.5, nout=1)
+    g = fp32(p)
+    g.run()
+    ids, st, bt, t = g.get_state()
+    for k, tile in enumerate(ids):
+        for f in range(4):
+            assert np.array_equal(st[k, f], g.field(tile, f + 1)), (tile, f)
+        m = st[k, 1]
+        assert np.array_equal(m, m.astype(np.float32).astype(np.float64))  # FP32 values
+    r = Simulation(lib.load(), "kg", p, precision=abi.PREC_FP32, load_sources=False)
+    r.load_state(ids, st, bt, t)
+    for s in (g, r):
+        s.integrate_to(0.8)
+    a, b = g.get_state(), r.get_state()
+    assert a[0] == b[0] and a[3] == b[3]
+    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    # writing one momentum leaves the other and the free surface alone
+    tile = ids[0]
+    w0, m2 = g.field(tile, 1).copy(), g.field(tile, 3).copy()
+    new = np.full_like(m2, 0.125)
+    g.set_field(tile, 2, new)
+    assert np.array_equal(g.field(tile, 2), new)
+    assert np.array_equal(g.field(tile, 3), m2) and np.array_equal(g.field(tile, 1), w0)
