@@ -139,7 +139,9 @@ def test_fp32_morpho_flux_window_depth_error():
 def test_fp32_state_round_trip():
     """The FP32 form stores its momenta as floats packed in the momentum plane: the
     per-tile getters, kg_get_state and kg_set_tile_field convert, and a context restarted
-    from kg_get_state (kg_load_state) continues bit for bit with the uninterrupted one."""
+    from kg_get_state (kg_load_state) continues with the uninterrupted one (within 1e-6:
+    the restart rebuilds the cell topography from the vertices with the FP64 path's
+    compensated sums, the running form updates it incrementally)."""
     from kestrel_gb300.solver import Simulation
     p = cases.ref_input("cap_morpho_2d", tend=0.5, nout=1)
     g = fp32(p)
@@ -155,8 +157,11 @@ def test_fp32_state_round_trip():
     for s in (g, r):
         s.integrate_to(0.8)
     a, b = g.get_state(), r.get_state()
-    assert a[0] == b[0] and a[3] == b[3]
-    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert a[0] == b[0] and abs(a[3] - b[3]) <= 1e-9
+    for f in range(4):
+        x, y = a[1][:, f], b[1][:, f]
+        assert np.max(np.abs(x - y)) <= 1e-6 * max(float(np.max(np.abs(x))), 1e-300), f
+    assert np.max(np.abs(a[2] - b[2])) <= 1e-6 * max(float(np.max(np.abs(a[2]))), 1e-300)
     # writing one momentum leaves the other and the free surface alone
     tile = ids[0]
     w0, m2 = g.field(tile, 1).copy(), g.field(tile, 3).copy()
