@@ -294,15 +294,16 @@ def serve_requests(n: int, rate: float = 20.0, seed: int = 77, sides=(256, 512, 
 
 
 def sparse_tiles(size: int = 8192, tile: int = 64, dx: float = 2.0, tend: float = 300.0, nout: int = 1, seed: int = 31337,
-                 relief: float = 400.0, tilt_deg: float = 6.0, smooth: float = 20.0, radius: float = 40.0,
-                 qpeak: tuple = (2000.0, 6000.0)):
+                 relief: float = 400.0, tilt_deg: float = 6.0, smooth: float = 20.0, radius: float = 100.0,
+                 qpeak: tuple = (20000.0, 60000.0)):
     """Large sparse tiled domain: size x size cells at dx (8192^2 at 2 m by default, in
     tiles of tile^2 cells) on fractal terrain with its own seed, low-passed at 20 m (relief
     0-400 m plus a 6-degree tilt: median slope about 12 degrees, 99th percentile about 28),
-    three flux sources of radius 40 m at seeded positions in the middle 60% of the domain
-    with triangular hydrographs (peak 2000-6000 m^3/s over 100-300 s, concentration
-    0.2-0.4), Pouliquen-Forterre drag with the reference's defaults, morphodynamics on,
-    sponge edges, to t = 300 s.  Returns (params, b0)."""
+    three flux sources of radius 100 m at seeded positions in the middle 60% of the domain
+    with triangular hydrographs (peak 20,000-60,000 m^3/s over 100-300 s, concentration
+    0.2-0.4: large enough that the flows cover about 5% of the tiles by t = 300 s),
+    Pouliquen-Forterre drag with the reference's defaults, morphodynamics on, sponge edges,
+    to t = 300 s.  Returns (params, b0)."""
     rng = np.random.default_rng(seed)
     L = size * dx
     srcs = []
@@ -342,16 +343,16 @@ Topog function = flat
 
 WORKLOADS["sparse_8192_fp32"] = dict(
     desc="large sparse tiled domain: 8192x8192 cells at dx=2 m (128x128 tiles of 64x64), seeded fractal terrain "
-         "(k^-3 low-passed at 20 m, relief 0-400 m, 6 deg tilt), three seeded flux sources (r=40 m, peak 2000-6000 "
-         "m^3/s over 100-300 s, conc 0.2-0.4), Pouliquen-Forterre drag, mixed erosion, to t=300 s; FP32 form; timed "
-         "after a spin-up to t=240 s",
-    params=sparse_tiles, prec=abi.PREC_FP32, spinup=240.0, timeline=20.0, twin_restart=True)
+         "(k^-3 low-passed at 20 m, relief 0-400 m, 6 deg tilt), three seeded flux sources (r=100 m, peak "
+         "20000-60000 m^3/s over 100-300 s, conc 0.2-0.4), Pouliquen-Forterre drag, mixed erosion, to t=300 s; FP32 "
+         "form; timed after a spin-up to t=290 s",
+    params=sparse_tiles, prec=abi.PREC_FP32, spinup=290.0, timeline=20.0, twin_restart=True)
 WORKLOADS["sparse_8192_fp64"] = dict(
     desc="large sparse tiled domain: 8192x8192 cells at dx=2 m (128x128 tiles of 64x64), seeded fractal terrain "
-         "(k^-3 low-passed at 20 m, relief 0-400 m, 6 deg tilt), three seeded flux sources (r=40 m, peak 2000-6000 "
-         "m^3/s over 100-300 s, conc 0.2-0.4), Pouliquen-Forterre drag, mixed erosion, to t=300 s; FP64 plain; timed "
-         "after a spin-up to t=240 s",
-    params=sparse_tiles, prec=abi.PREC_FP64, spinup=240.0, timeline=20.0)
+         "(k^-3 low-passed at 20 m, relief 0-400 m, 6 deg tilt), three seeded flux sources (r=100 m, peak "
+         "20000-60000 m^3/s over 100-300 s, conc 0.2-0.4), Pouliquen-Forterre drag, mixed erosion, to t=300 s; FP64 "
+         "plain; timed after a spin-up to t=290 s",
+    params=sparse_tiles, prec=abi.PREC_FP64, spinup=290.0, timeline=20.0)
 
 
 def dem_2048(seed: int = 1, pixel: float = 2.5, center=(500000.0, 4000000.0)):

@@ -218,7 +218,7 @@ def test_sparse_activation_bitexact_every_step():
     sorted active list and the ghost list match the oracle's after every accepted step, and
     the state stays within the morphodynamic tolerance."""
     from kestrel_gb300 import workloads
-    p, b0 = workloads.sparse_tiles(size=512, tile=16, dx=2.0, tend=3.0)
+    p, b0 = workloads.sparse_tiles(size=512, tile=16, dx=2.0, tend=3.0, radius=40.0, qpeak=(2000.0, 6000.0))
     g, o = lib.simulation(p, b0=b0), _oracle.simulation(p, b0=b0)
     n = 0
     while o.time[0] < p.tend and n < 80:
