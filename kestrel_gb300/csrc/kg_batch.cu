@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(NT) k_hydro32_batch(const SimStatic* __restric
         const SimStatic& X = sims[member[lo]];
         const StepArgs& S = args[lo];
         StageTimes Tm;
-        if (stage_gate_open(X.P, S, Tm)) hydro32_block(X.A, S, Tm, X.P, X.F, X.src, X.blocks[b - prefix[lo]], sm);
+        if (stage_gate_open_warp(X.P, S, Tm)) hydro32_block(X.A, S, Tm, X.P, X.F, X.src, X.blocks[b - prefix[lo]], sm);
         __syncthreads();
     }
 }

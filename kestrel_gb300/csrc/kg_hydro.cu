@@ -297,6 +297,19 @@ __device__ __forceinline__ bool stage_gate_open(const DevParams& P, const StepAr
     return true;
 }
 
+// The gate and times are the same for every thread of a launch; lane 0 of each warp
+// evaluates them (FP64 work, 1/64 of the FP32 rate on this GPU) and the warp takes them
+// from it.  Every lane of the warp must call this.
+__device__ __forceinline__ bool stage_gate_open_warp(const DevParams& P, const StepArgs& S, StageTimes& T) {
+    int open = 0;
+    if ((threadIdx.x & 31) == 0) open = stage_gate_open(P, S, T) ? 1 : 0;
+    open = __shfl_sync(0xffffffffu, open, 0);
+    T.dt = __shfl_sync(0xffffffffu, T.dt, 0);
+    T.t_rhs = __shfl_sync(0xffffffffu, T.t_rhs, 0);
+    T.t_max = __shfl_sync(0xffffffffu, T.t_max, 0);
+    return open != 0;
+}
+
 // The first dt of a step on the device: IntegrateTo's min(advised dt of the RHS at t,
 // the distance to the next flux knot) (src/TimeStepper.f90:151-183), from the CFL word of
 // the RHS pass; cap is the host's (tmax - t) or (tmax - t)/2.
@@ -316,7 +329,7 @@ cudaError_t launch_dt(const unsigned long long* cfl, int partial, double cap, do
 __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
     kg_dep_wait();
     StageTimes Tm;
-    if (!stage_gate_open(cP, S, Tm)) return;
+    if (!stage_gate_open_warp(cP, S, Tm)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     HydroSmem& sm = *reinterpret_cast<HydroSmem*>(smraw);
     const DevParams& P = cP;

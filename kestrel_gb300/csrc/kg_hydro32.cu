@@ -420,7 +420,7 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
         int yb = cy * BS + cx, yt = yb + BS;
         // w and Hnpsi rows in FP64 (the flux differences of FP32 values are exact or nearly so)
         double E0, E3;
-        if (P.dx == P.dy) {
+        if (__double_as_longlong(P.dx) == __double_as_longlong(P.dy)) {  // square cells (an integer test)
             // square cells: the four-flux sum once, from an error-free FP32 split
             E0 = flux_sum4(sm.fx[0][xl], sm.fx[0][xr], sm.fy[0][yb], sm.fy[0][yt]) * P.dxR * ig2;
             E3 = flux_sum4(sm.fx[3][xl], sm.fx[3][xr], sm.fy[3][yb], sm.fy[3][yt]) * P.dxR * ig;
@@ -462,15 +462,18 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             double hp_old = q0p[0] - b, hp_new = sm.w[r] - b;
             double* dst = A.Q[S.mode == MODE_S1 ? S.q_s1 : S.q_s2] + plane(slot, 4, 0, SC) + c;
             float den = 1.f / (1.f - dtf * I);
-            double a0, a1;
-            if (S.mode == MODE_S1) { a0 = 0.75; a1 = 0.25; }
-            else { a0 = 1.0 / 3.0; a1 = 2.0 / 3.0; }
-            dst[0] = b + (a0 * hp_old + a1 * (hp_new + Tm.dt * E0));
+            // stage weights (3/4, 1/4) and (1/3, 2/3); the FP32 copies are constants, and
+            // the stage-2 quarter is an exact exponent shift on the integer pipe
+            const bool s1 = S.mode == MODE_S1;
+            const double a0 = s1 ? 0.75 : 1.0 / 3.0, a1 = s1 ? 0.25 : 2.0 / 3.0;
+            const float a0f = s1 ? 0.75f : (float)(1.0 / 3.0), a1f = s1 ? 0.25f : (float)(2.0 / 3.0);
+            const double wn = hp_new + Tm.dt * E0, pn = sm.p64[r] + Tm.dt * E3;
+            dst[0] = b + (a0 * hp_old + (s1 ? scale_down_pow2(wn, 2) : a1 * wn));
             const float* q0m = mom32(A.Q[S.q_in], slot, SC);
-            float* dm = mom32(A.Q[S.mode == MODE_S1 ? S.q_s1 : S.q_s2], slot, SC);
-            dm[c] = (float)a0 * q0m[c] + (float)a1 * (sm.m1[r] + dtf * E1) * den;
-            dm[SC + c] = (float)a0 * q0m[SC + c] + (float)a1 * (sm.m2[r] + dtf * E2) * den;
-            dst[3 * (size_t)SC] = a0 * q0p[3 * (size_t)SC] + a1 * (sm.p64[r] + Tm.dt * E3);
+            float* dm = mom32(A.Q[s1 ? S.q_s1 : S.q_s2], slot, SC);
+            dm[c] = a0f * q0m[c] + a1f * (sm.m1[r] + dtf * E1) * den;
+            dm[SC + c] = a0f * q0m[SC + c] + a1f * (sm.m2[r] + dtf * E2) * den;
+            dst[3 * (size_t)SC] = a0 * q0p[3 * (size_t)SC] + (s1 ? scale_down_pow2(pn, 2) : a1 * pn);
         } else {
             float dt2I = dtf * dtf * I;
             float den = 1.f / (1.f + dt2I * I);
@@ -514,7 +517,7 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
 __global__ void __launch_bounds__(NT) k_hydro32(DevArrays A, const BlockDesc* __restrict__ blocks, const StepArgs S) {
     kg_dep_wait();
     StageTimes Tm;
-    if (!stage_gate_open(cP, S, Tm)) return;
+    if (!stage_gate_open_warp(cP, S, Tm)) return;
     extern __shared__ __align__(16) unsigned char smraw[];
     Hydro32Smem& sm = *reinterpret_cast<Hydro32Smem*>(smraw);
     hydro32_block(A, S, Tm, cP, cP32, cSrc, blocks[blockIdx.x], sm);
