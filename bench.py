@@ -340,7 +340,7 @@ def run_ensemble(args):
                     "note": "host clock around the same batch steps (control words only cross per step)"},
             "batch": {"kernel_launches_per_step": (l1 - l0) / args.steps, "rounds_per_step": (r1 - r0) / args.steps,
                       "device_gb": hbm / 1e9, "autotune_s": t_tune, "add_s": t_add, "graphs": bool(args.batch_graphs),
-                      "graph_launches_updates_instantiations": list(b.graph_stats())},
+                      "graph_launches_updates_instantiations_replays": list(b.graph_stats())},
             "clocks": clk}
     b.close()
     return line

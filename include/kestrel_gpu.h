@@ -325,12 +325,15 @@ int  kg_batch_stats(kg_batch* b, int64_t* launches, int64_t* rounds);
 void* kg_batch_stream(kg_batch* b);
 /* CUDA graphs for the rounds (on by default): each device segment of a round between two
    waits -- the batched H phase, the M operator up to its checks, the closing launch with the
-   RHS check and second H -- is captured from the batch stream and replayed through one
-   executable graph per segment kind, updated in place when its shape is unchanged.
-   enable = 0 launches the same work directly on the stream. */
+   RHS check and second H -- runs as one executable graph per segment kind: launched as it
+   is when the segment's launches and copies carry the same parameters as last time (the
+   tables they read are refreshed in pinned memory), else captured from the batch stream
+   and updated in place, or instantiated when its shape changed.  enable = 0 launches the
+   same work directly on the stream. */
 int  kg_batch_set_graphs(kg_batch* b, int32_t enable);
-/* out[0] graph launches, out[1] in-place updates, out[2] instantiations so far. */
-int  kg_batch_graph_stats(kg_batch* b, int64_t out[3]);
+/* out[0] graph launches, out[1] in-place updates, out[2] instantiations, out[3] launches
+   of an unchanged graph without a capture, so far. */
+int  kg_batch_graph_stats(kg_batch* b, int64_t out[4]);
 
 #ifdef __cplusplus
 }

@@ -46,8 +46,9 @@ class Batch:
         self._check(self.L.kg_batch_set_graphs(self.h, 1 if graphs else 0))
 
     def graph_stats(self):
-        """(graph launches, in-place updates, instantiations) of the rounds so far."""
-        out = (C.c_int64 * 3)()
+        """(graph launches, in-place updates, instantiations, launches of an unchanged graph
+        without a capture) of the rounds so far."""
+        out = (C.c_int64 * 4)()
         self._check(self.L.kg_batch_graph_stats(self.h, out))
         return tuple(out)
 

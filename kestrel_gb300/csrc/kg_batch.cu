@@ -1,3 +1,4 @@
+#include <functional>
 // kg_batch.cu -- many simulations advanced together (the batched ensemble form).
 //
 // A batch owns FP32-form simulations of any grid and tile size on one CUDA stream.
@@ -209,12 +210,19 @@ struct kg_batch {
     // CUDA graphs: each device segment of a round (between two waits) is captured from the
     // stream and replayed through one executable graph per segment kind, updated in place
     // (cudaGraphExecUpdate) when the captured segment differs from the last one.
+    // A segment's enqueues are first recorded with a byte signature of their parameters
+    // (kernel, grid, arguments; copy addresses and sizes): when the signature equals that of
+    // the segment kind's executable graph, the graph is launched as it is (the copies read
+    // the pinned tables at execution time); otherwise the recorded enqueues are captured
+    // and the executable graph updated or instantiated.
     enum { SEG_H = 0, SEG_M1 = 1, SEG_M2 = 2, NSEG = 3 };
     bool use_graphs = true;
-    bool capturing = false;
+    bool capturing = false, recording = false;
     int seg = -1;
     cudaGraphExec_t exec[NSEG] = {nullptr, nullptr, nullptr};
-    int64_t graph_launches = 0, graph_updates = 0, graph_instantiations = 0;
+    std::vector<std::function<void()>> ops;
+    std::vector<unsigned char> sig_cur, sig[NSEG];
+    int64_t graph_launches = 0, graph_updates = 0, graph_instantiations = 0, graph_replays = 0;
     std::string err;
 };
 
@@ -224,22 +232,71 @@ using namespace kg;
 
 void batch_sync(kg_batch& b) { CK(cudaStreamSynchronize(b.st)); }
 
-// Start capturing a segment of the round (everything queued on the batch stream until
-// seg_end); a no-op when graphs are off.
+// Start a segment of the round (every batched enqueue until seg_end); without graphs the
+// enqueues are issued as they come.
 void seg_begin(kg_batch& b, int seg) {
     if (!b.use_graphs) return;
+    b.recording = true;
+    b.seg = seg;
+    b.ops.clear();
+    b.sig_cur.clear();
+}
+template <class T>
+void sig_add(kg_batch& b, const T& v) {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(&v);
+    b.sig_cur.insert(b.sig_cur.end(), p, p + sizeof(T));
+}
+// One batched kernel launch of the round: issued now, or recorded into the segment.
+template <typename... KArgs, typename... Args>
+void enq_kernel(kg_batch& b, void (*k)(KArgs...), int grid, int block, size_t smem, Args... args) {
+    if (!b.recording) {
+        CK(kg_launch(k, grid, block, smem, b.st, args...));
+        CK(cudaGetLastError());
+        return;
+    }
+    sig_add(b, (const void*)k);
+    sig_add(b, grid);
+    sig_add(b, block);
+    sig_add(b, smem);
+    (sig_add(b, args), ...);
+    cudaStream_t st = b.st;
+    b.ops.push_back([=]() {
+        CK(kg_launch(k, grid, block, smem, st, args...));
+        CK(cudaGetLastError());
+    });
+}
+// One copy of the round (pinned host tables and device buffers only).
+void enq_copy(kg_batch& b, void* dst, const void* src, size_t n, cudaMemcpyKind kind) {
+    if (!b.recording) {
+        CK(cudaMemcpyAsync(dst, src, n, kind, b.st));
+        return;
+    }
+    sig_add(b, dst);
+    sig_add(b, src);
+    sig_add(b, n);
+    sig_add(b, (int)kind);
+    cudaStream_t st = b.st;
+    b.ops.push_back([=]() { CK(cudaMemcpyAsync(dst, src, n, kind, st)); });
+}
+// End the segment and launch it: the segment kind's executable graph as it is when the
+// recorded enqueues carry its signature, else the enqueues captured from the stream and the
+// executable graph updated in place (or instantiated when its shape changed).
+void seg_end(kg_batch& b) {
+    if (!b.recording) return;
+    b.recording = false;
+    cudaGraphExec_t& x = b.exec[b.seg];
+    if (x && b.sig_cur == b.sig[b.seg]) {
+        CK(cudaGraphLaunch(x, b.st));
+        b.graph_launches++;
+        b.graph_replays++;
+        return;
+    }
     CK(cudaStreamBeginCapture(b.st, cudaStreamCaptureModeRelaxed));
     b.capturing = true;
-    b.seg = seg;
-}
-// End the capture and launch it: the segment kind's executable graph is updated in place
-// when the new capture has the same shape, instantiated afresh otherwise.
-void seg_end(kg_batch& b) {
-    if (!b.capturing) return;
+    for (auto& op : b.ops) op();
     cudaGraph_t g = nullptr;
     b.capturing = false;
     CK(cudaStreamEndCapture(b.st, &g));
-    cudaGraphExec_t& x = b.exec[b.seg];
     if (x) {
         cudaGraphExecUpdateResultInfo info;
         if (cudaGraphExecUpdate(x, g, &info) == cudaSuccess) {
@@ -257,19 +314,24 @@ void seg_end(kg_batch& b) {
     }
     cudaGraphDestroy(g);
     CK(e);
+    b.sig[b.seg] = b.sig_cur;
     CK(cudaGraphLaunch(x, b.st));
     b.graph_launches++;
 }
-// Leaves the stream out of capture mode when an error unwinds through a segment.
+// Leaves the stream out of capture mode and drops a half-recorded segment when an error
+// unwinds through it.
 struct SegGuard {
     kg_batch& b;
     ~SegGuard() {
+        b.recording = false;
+        b.ops.clear();
         if (!b.capturing) return;
         cudaGraph_t g = nullptr;
         cudaStreamEndCapture(b.st, &g);
         if (g) cudaGraphDestroy(g);
         (void)cudaGetLastError();
         b.capturing = false;
+        if (b.seg >= 0) b.sig[b.seg].clear();
     }
 };
 
@@ -339,12 +401,12 @@ void launch_hydro_batch(kg_batch& b, const std::vector<int>& who, const std::vec
     StepArgs* da = b.d_args + (size_t)L * b.cap;
     int* dm = b.d_idx + (size_t)L * 2 * (b.cap + 1);
     int* dp = dm + (b.cap + 1);
-    CK(cudaMemcpyAsync(da, ha, (size_t)n * sizeof(StepArgs), cudaMemcpyHostToDevice, b.st));
-    CK(cudaMemcpyAsync(dm, hm, (size_t)2 * (b.cap + 1) * sizeof(int), cudaMemcpyHostToDevice, b.st));
+    enq_copy(b, da, ha, (size_t)n * sizeof(StepArgs), cudaMemcpyHostToDevice);
+    enq_copy(b, dm, hm, (size_t)2 * (b.cap + 1) * sizeof(int), cudaMemcpyHostToDevice);
     if (total == 0) return;
     int grid = std::min(total, b.grid_hydro);
-    CK(kg_launch(k_hydro32_batch, grid, NT, sizeof(Hydro32Smem), b.st, b.d_static, da, dm, dp, n, total));
-    CK(cudaGetLastError());
+    enq_kernel(b, k_hydro32_batch, grid, NT, sizeof(Hydro32Smem), (const SimStatic*)b.d_static, (const StepArgs*)da,
+               (const int*)dm, (const int*)dp, n, total);
     b.launches++;
 }
 
@@ -416,13 +478,13 @@ void queue_flags_batch(kg_batch& b, const std::vector<int>& who, const std::vect
     }
     if (total > b.actout_cap) throw KgError(KG_ERR_STATE, "edge-band buffer not sized before the segment");
     int* dp = b.d_idx + (size_t)(kg_batch::NLAUNCH) * 2 * (b.cap + 1);
-    CK(cudaMemcpyAsync(b.d_act, b.h_act, (size_t)n * sizeof(ActJob), cudaMemcpyHostToDevice, b.st));
-    CK(cudaMemcpyAsync(dp, hp, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, b.st));
+    enq_copy(b, b.d_act, b.h_act, (size_t)n * sizeof(ActJob), cudaMemcpyHostToDevice);
+    enq_copy(b, dp, hp, (size_t)n * sizeof(int), cudaMemcpyHostToDevice);
     if (total == 0) return;
-    CK(kg_launch(k_act_flags_batch, std::min(total, b.grid_act), 256, 0, b.st, b.d_static, b.d_act, dp, n, total, b.d_actout));
-    CK(cudaGetLastError());
+    enq_kernel(b, k_act_flags_batch, std::min(total, b.grid_act), 256, 0, (const SimStatic*)b.d_static, (const ActJob*)b.d_act,
+               (const int*)dp, n, total, b.d_actout);
     b.launches++;
-    CK(cudaMemcpyAsync(b.h_actout, b.d_actout, (size_t)total * sizeof(int), cudaMemcpyDeviceToHost, b.st));
+    enq_copy(b, b.h_actout, b.d_actout, (size_t)total * sizeof(int), cudaMemcpyDeviceToHost);
 }
 
 // Reset every member's CFL words (one copy; the other control words are left to the
@@ -430,10 +492,10 @@ void queue_flags_batch(kg_batch& b, const std::vector<int>& who, const std::vect
 void reset_ctl(kg_batch& b) {
     for (int i = 0; i < b.cap; ++i)
         for (int k = 0; k < 4; ++k) b.h_ctl[i].cfl[k] = HUGE_BITS;
-    CK(cudaMemcpyAsync(b.d_ctl, b.h_ctl, (size_t)b.cap * sizeof(kg_ctx::Ctl), cudaMemcpyHostToDevice, b.st));
+    enq_copy(b, b.d_ctl, b.h_ctl, (size_t)b.cap * sizeof(kg_ctx::Ctl), cudaMemcpyHostToDevice);
 }
 void read_ctl(kg_batch& b) {
-    CK(cudaMemcpyAsync(b.h_ctl, b.d_ctl, (size_t)b.cap * sizeof(kg_ctx::Ctl), cudaMemcpyDeviceToHost, b.st));
+    enq_copy(b, b.h_ctl, b.d_ctl, (size_t)b.cap * sizeof(kg_ctx::Ctl), cudaMemcpyDeviceToHost);
 }
 // The end of a segment: the control words come back, the segment runs, one wait.
 void collect_ctl(kg_batch& b) {
@@ -503,9 +565,8 @@ void phase_h(kg_batch& b, const std::vector<int>& who) {
             Member& m = b.mem[(size_t)fresh[(size_t)k]];
             b.h_dt[k] = DtJob{m.c->d_cfl + W_RHS, m.c->d_dt, m.cap, partial(*m.c), fresh[(size_t)k]};
         }
-        CK(cudaMemcpyAsync(b.d_dt, b.h_dt, (size_t)n * sizeof(DtJob), cudaMemcpyHostToDevice, b.st));
-        CK(kg_launch(k_dt_batch, (n + 127) / 128, 128, 0, b.st, b.d_static, b.d_dt, n));
-        CK(cudaGetLastError());
+        enq_copy(b, b.d_dt, b.h_dt, (size_t)n * sizeof(DtJob), cudaMemcpyHostToDevice);
+        enq_kernel(b, k_dt_batch, (n + 127) / 128, 128, 0, (const SimStatic*)b.d_static, (const DtJob*)b.d_dt, n);
         b.launches++;
     }
     queue_stages_batch(b, who, false);
@@ -556,16 +617,16 @@ int upload_mjobs(kg_batch& b, int t, const std::vector<int>& who) {
         hp[k] = total;
         total += (int)c.active.size() * per;
     }
-    CK(cudaMemcpyAsync(b.d_mjob + (size_t)t * b.cap, hj, who.size() * sizeof(MJob), cudaMemcpyHostToDevice, b.st));
-    CK(cudaMemcpyAsync(b.d_mpre + (size_t)t * (b.cap + 1), hp, who.size() * sizeof(int), cudaMemcpyHostToDevice, b.st));
+    enq_copy(b, b.d_mjob + (size_t)t * b.cap, hj, who.size() * sizeof(MJob), cudaMemcpyHostToDevice);
+    enq_copy(b, b.d_mpre + (size_t)t * (b.cap + 1), hp, who.size() * sizeof(int), cudaMemcpyHostToDevice);
     return total;
 }
 template <int K>
 void launch_m(kg_batch& b, int t, int n, int total, int stage = 0) {
     if (n == 0 || total == 0) return;
-    CK(kg_launch(k_m_batch<K>, std::min(total, b.grid_m), 256, 0, b.st, b.d_static, b.d_mjob + (size_t)t * b.cap,
-                                                             b.d_mpre + (size_t)t * (b.cap + 1), n, total, stage));
-    CK(cudaGetLastError());
+    enq_kernel(b, k_m_batch<K>, std::min(total, b.grid_m), 256, 0, (const SimStatic*)b.d_static,
+               (const MJob*)(b.d_mjob + (size_t)t * b.cap), (const int*)(b.d_mpre + (size_t)t * (b.cap + 1)), n, total,
+               stage);
     b.launches++;
 }
 
@@ -948,11 +1009,12 @@ int kg_batch_set_graphs(kg_batch* b, int32_t enable) {
     return KG_OK;
 }
 
-int kg_batch_graph_stats(kg_batch* b, int64_t out[3]) {
+int kg_batch_graph_stats(kg_batch* b, int64_t out[4]) {
     if (!b || !out) return KG_ERR_PARAM;
     out[0] = b->graph_launches;
     out[1] = b->graph_updates;
     out[2] = b->graph_instantiations;
+    out[3] = b->graph_replays;
     return KG_OK;
 }
 
