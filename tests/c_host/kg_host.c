@@ -2,7 +2,8 @@
  * library in place of Run (src/TimeStepper.f90:73-112): it reads a kg_params struct (raw
  * bytes, the header's layout), creates a context, places the sources, integrates to t_end
  * and prints the step statistics, the four volume sums and the sum of the free surface
- * over the active tiles.  Usage: kg_host PARAMS_FILE PRECISION */
+ * over the active tiles, read tile by tile and again in one call (kg_get_state).
+ * Usage: kg_host PARAMS_FILE PRECISION */
 #include <stdio.h>
 #include <stdlib.h>
 
@@ -53,8 +54,18 @@ int main(int argc, char** argv) {
         kg_get_tile_field(ctx, ids[k], 1, w);
         for (int c = 0; c < cells; ++c) sw += w[c];
     }
-    printf("ok %.17g %lld %lld %d %.17g %.17g %.17g %.17g %.17g\n", st.t, (long long)st.steps, (long long)st.rejected, n,
-           vol[0], vol[1], vol[2], vol[3], sw);
+    /* the same sum from the whole state in one call (kg_get_state) */
+    int32_t n2 = n;
+    int32_t* ids2 = (int32_t*)malloc(sizeof(int32_t) * (n > 0 ? n : 1));
+    double* state = (double*)malloc(sizeof(double) * 4 * (size_t)cells * (n > 0 ? n : 1));
+    double sw2 = 0.0;
+    if (kg_get_state(ctx, ids2, &n2, state, NULL) == KG_OK && n2 == n)
+        for (int k = 0; k < n; ++k)
+            for (int c = 0; c < cells; ++c) sw2 += state[(size_t)k * 4 * cells + c];
+    printf("ok %.17g %lld %lld %d %.17g %.17g %.17g %.17g %.17g %.17g\n", st.t, (long long)st.steps, (long long)st.rejected,
+           n, vol[0], vol[1], vol[2], vol[3], sw, sw2);
+    free(state);
+    free(ids2);
     free(w);
     free(ids);
     kg_destroy(ctx);

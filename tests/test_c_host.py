@@ -67,4 +67,4 @@ def test_c_host_matches_python(tmp_path):
     assert float(words[1]) == st.t and int(words[2]) == st.steps and int(words[3]) == st.rejected
     assert int(words[4]) == len(sim.active_tiles())
     assert [float(x) for x in words[5:9]] == list(vol)
-    assert float(words[9]) == sw
+    assert float(words[9]) == sw and float(words[10]) == sw
