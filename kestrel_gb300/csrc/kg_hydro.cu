@@ -43,6 +43,7 @@ struct __align__(16) HydroSmem {
     double w[NR], m1[NR], m2[NR], p[NR];
     double b0[NR], bt[NR], bx[NR], by[NR];
     double Hn[NR], rho[NR], u[NR], v[NR], psi[NR];
+    double gam[NR];     // gam of each loaded cell (a square root, taken once per pass)
     double lx[5][NLX];  // X slopes of (w, Hnpsi, u, v, rho), cells cx in [-1, BS], cy in [0, BS)
     double ly[5][NLX];  // Y slopes, cells cy in [-1, BS], cx in [0, BS)
     double fx[7][NFX];  // X-face fluxes: h(w, m1, m2, Hnpsi), g, p(m1), p(m2)
@@ -362,6 +363,8 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         double b0 = CT[plane(s, 4, 0, SC) + c], bt = CT[plane(s, 4, 1, SC) + c];
         double dbx = CT[plane(s, 4, 2, SC) + c], dby = CT[plane(s, 4, 3, SC) + c];
         sm.b0[r] = b0; sm.bt[r] = bt; sm.bx[r] = dbx; sm.by[r] = dby;
+        const double gam = gam_of(P.geo, dbx, dby);
+        sm.gam[r] = gam;
         if (A.kind[s] == SLOT_GHOST) {
             sm.w[r] = A.G9[plane(s, 9, 0, SC) + c];
             sm.m1[r] = A.G9[plane(s, 9, 1, SC) + c];
@@ -389,7 +392,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         }
         sm.w[r] = q[0]; sm.m1[r] = q[1]; sm.m2[r] = q[2]; sm.p[r] = q[3];
         double Hn, psi, rho, u, v;
-        desing(P, q[0], q[1], q[2], q[3], b0, bt, gam_of(P.geo, dbx, dby), Hn, psi, rho, u, v);
+        desing(P, q[0], q[1], q[2], q[3], b0, bt, gam, Hn, psi, rho, u, v);
         sm.Hn[r] = Hn; sm.psi[r] = psi; sm.rho[r] = rho; sm.u[r] = u; sm.v[r] = v;
     }
     __syncthreads();
@@ -505,7 +508,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
             }
             size_t fo = (size_t)slot * 5 * SFX + (size_t)j * (nX + 1) + fi;
             double b0f = FX[fo], btf = FX[fo + SFX], dbxf = FX[fo + 2 * (size_t)SFX], dbyf = FX[fo + 3 * (size_t)SFX];
-            double gamL = gam_of(P.geo, sm.bx[rL], sm.by[rL]), gamR = gam_of(P.geo, sm.bx[rR], sm.by[rR]);
+            double gamL = sm.gam[rL], gamR = sm.gam[rR];
             double out[7];
             face_flux(P, true, R, L, b0f, btf, dbxf, dbyf, gamL, gamR, dx, out, cfl);
             int fo2 = cy * (BS + 1) + fx;
@@ -573,7 +576,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
             }
             size_t fo = (size_t)slot * 5 * SFY + (size_t)fj * nX + i;
             double b0f = FY[fo], btf = FY[fo + SFY], dbxf = FY[fo + 2 * (size_t)SFY], dbyf = FY[fo + 3 * (size_t)SFY];
-            double gamL = gam_of(P.geo, sm.bx[rL], sm.by[rL]), gamR = gam_of(P.geo, sm.bx[rR], sm.by[rR]);
+            double gamL = sm.gam[rL], gamR = sm.gam[rR];
             double out[7];
             face_flux(P, false, R, L, b0f, btf, dbxf, dbyf, gamL, gamR, dy, out, cfl);
             int fo2 = fy * BS + cx;
@@ -598,7 +601,7 @@ __global__ void __launch_bounds__(NT) k_hydro(DevArrays A, const BlockDesc* __re
         int i = bd.x0 + cx, j = bd.y0 + cy, c = j * nX + i;
         int r = (cy + 2) * RG + (cx + 2);
         double b0 = sm.b0[r], bt = sm.bt[r], dbdx = sm.bx[r], dbdy = sm.by[r];
-        double gam = gam_of(P.geo, dbdx, dbdy);
+        double gam = sm.gam[r];
         double gXp1, gXp2, gYp1, gYp2;
         if (P.geo) {
             gXp1 = (1.0 + dbdy * dbdy) / gam;
