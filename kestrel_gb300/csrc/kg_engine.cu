@@ -259,13 +259,14 @@ void bind_constants(kg_ctx& c);
 
 // Device bytes of one slot: Q, E/I, CT/FX/FY/BV (two sets), UV, MS, EMD, B0S, G9, GE, MX,
 // the source-override Hn and rho planes, nbr/kind/has_source/tile_of_slot, and in the FP32
-// form TD/TF/TFX/TFY (two sets).
+// form TD/TF/TFX/TFY (two sets) and M0/MF.
 size_t slot_bytes(size_t nX, size_t nY, int prec) {
     size_t SC = nX * nY, SFX = (nX + 1) * nY, SFY = nX * (nY + 1), SV = (nX + 1) * (nY + 1), nE = std::max(nX, nY);
     return sizeof(double) * (4 * 4 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * SFX + 5 * SFY + 2 * SV) +
                              2 * SC + 5 * SC + SC + 2 * SC + 9 * SC + GE_COUNT * nE + 11 * SC + 2 * SC) +
            8 * sizeof(int) + 2 + sizeof(int) +
-           (prec == KG_PREC_FP32 ? 2 * (3 * sizeof(double) * SC + 6 * sizeof(float) * SC + 2 * sizeof(float) * (SFX + SFY))
+           (prec == KG_PREC_FP32 ? 2 * (3 * sizeof(double) * SC + 6 * sizeof(float) * SC + 2 * sizeof(float) * (SFX + SFY)) +
+                                       3 * sizeof(double) * SC + MF_COUNT * sizeof(float) * SC
                                  : 0);
 }
 size_t bytes_per_slot(const kg_ctx& c) { return slot_bytes((size_t)c.nX, (size_t)c.nY, c.prec); }
@@ -302,6 +303,10 @@ void ensure_cap(kg_ctx& c, int need) {
             grow_array(c.A.TFX[b], o * 2 * (size_t)c.SFX, n * 2 * (size_t)c.SFX, c.st);
             grow_array(c.A.TFY[b], o * 2 * (size_t)c.SFY, n * 2 * (size_t)c.SFY, c.st);
         }
+    }
+    if (c.prec == KG_PREC_FP32) {
+        grow_array(c.A.M0, o * 3 * SC, n * 3 * SC, c.st);
+        grow_array(c.A.MF, o * MF_COUNT * SC, n * MF_COUNT * SC, c.st);
     }
     grow_array(c.A.UV, o * 2 * SC, n * 2 * SC, c.st);
     grow_array(c.A.MS, o * 5 * SC, n * 5 * SC, c.st);
@@ -1735,7 +1740,7 @@ void free_ctx(kg_ctx* c) {
     cudaFree(c->d_tlist);
     cudaFree(c->d_gather);
     cudaFree(c->d_rb0);
-    void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.B0S, c->A.G9, c->A.GE, c->A.MX,
+    void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.B0S, c->A.M0, c->A.MF, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
                     c->d_vol, c->d_srcHn, c->d_srcRho, c->d_ckey, c->d_cex, c->d_src,
                     c->d_rslot, c->d_rcell, c->d_rwave};

@@ -14,6 +14,9 @@
 //   ghost data     G9[slot][9][nY][nX]        static u(1:9) of a ghost tile
 //                  GE[slot][12][nE]           its stale w reconstructions at the edges
 //   static slopes  B0S[slot][2][nY][nX]       b0 parts of the cell slopes (FP32-form M stages)
+//   M step start   M0[slot][3][nY][nX]        FP32 form: Hn, Hn gam, Hnpsi gam of the M input
+//                  MF[slot][8][nY][nX]        FP32 form (float): its psi; the stage's Hn, psi,
+//                                             rho, bt, dbdx, dbdy and E - D
 //   maxima         MX[slot][11][nY][nX]       Hnmax, umax, emax, dmax, psimax (value, time)
 //                                             and tfirst (src/Grid.f90:95-102)
 // FP32 form only (static per topography set, rebuilt when the set changes):
@@ -32,6 +35,8 @@
 
 namespace kg {
 
+// Planes of MF (FP32 form).
+enum MfPlane { MF_PSI0 = 0, MF_HN, MF_PSI, MF_RHO, MF_BT, MF_BX, MF_BY, MF_EMD, MF_COUNT };
 enum SlotKind : int8_t { SLOT_FREE = 0, SLOT_ACTIVE = 1, SLOT_GHOST = 2 };
 enum Nb { NB_W = 0, NB_E = 1, NB_N = 2, NB_S = 3, NB_SW = 4, NB_SE = 5, NB_NW = 6, NB_NE = 7 };
 // Ghost edge records (GE planes): uLimX(iw,1,:), uLimX(iw,nX,:), uLimY(iw,:,1),
@@ -69,6 +74,11 @@ struct DevArrays {
     double* MS;                // [slot][5][nY][nX] M-operator stage state: w, Hnpsi, Hn, psi, rho
     double* EMD;               // [slot][nY][nX] E - D of the current M stage (zero on ghosts)
     double* B0S;               // [slot][2][nY][nX] the static b0 parts of the cell slopes (FP32-form M stages)
+    double* M0;                // [slot][3][nY][nX] FP32 form: the M attempt's step-start Hn (unclamped),
+                               // Hn gam and Hnpsi gam (set by m_init, read by the stages and tests)
+    float* MF;                 // [slot][8][nY][nX] FP32 form (float): the step-start psi; the M stage's
+                               // Hn, psi, rho, bt, dbdx, dbdy as the closures and the vertex source read
+                               // them; the stage's E - D (zero on ghosts)
     double* TD[2];             // FP32 form topography factors (null in the FP64 form)
     float* TF[2];
     float* TFX[2];
@@ -124,6 +134,10 @@ struct RasterGeo {
 // the previous kernel of the stream drains (hiding the launch gap between the short
 // kernels of a step); it calls kg_dep_wait() before touching memory, which returns once
 // that kernel has completed and its writes are visible (immediately for a plain launch).
+// No kernel signals its dependents early (griddepcontrol.launch_dependents): the next
+// kernel's CTAs would then be placed on the SMs that the tail frees first, several per SM,
+// instead of spread over all SMs, which costs these FP64-pipe-bound kernels more than the
+// launch ramp it saves (measured: step 0.899 -> 0.921 ms).
 __device__ __forceinline__ void kg_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 #define KG_TRY_LAUNCH(x)                        \
     do {                                        \

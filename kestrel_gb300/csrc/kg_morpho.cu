@@ -29,6 +29,8 @@ namespace kg {
 constexpr int REDIST_THREADS = 512;
 
 __device__ __forceinline__ size_t mp(int slot, int nf, int f, int npl) { return ((size_t)slot * nf + f) * (size_t)npl; }
+// Plane f of the FP32 form's float stage planes (MF) of a slot.
+__device__ __forceinline__ float* mfp(const DevArrays& A, int slot, int f, int SC) { return A.MF + mp(slot, MF_COUNT, f, SC); }
 
 // FP32 form: 1/sqrt(x) from an FP32 seed and one Newton step (relative error about 1e-13,
 // far below the form's FP32 error), and the step-start gamma of a cell from the
@@ -83,21 +85,35 @@ __device__ __forceinline__ void m_init(const DevParams& P, const DevArrays& A, i
         double w = A.Q[qa][mp(s, 4, 0, SC) + c], p = A.Q[qa][mp(s, 4, 3, SC) + c];
         double gam = PLAIN ? gam_cached(P, A, tcur, s, c, ct[2], ct[3]) : gam_of(P.geo, ct[2], ct[3]);
         double Hn = compute_hn(w, ct[0], ct[1], gam);
+        if (PLAIN) {
+            // the step-start quantities every stage and test of the attempt reuses
+            double* Z = A.M0 + mp(s, 3, 0, SC) + c;
+            Z[0] = Hn;
+            Z[(size_t)SC] = Hn * gam;
+            Z[2 * (size_t)SC] = p * gam;
+        }
         if (Hn < 0.0) Hn = 0.0;
         double pp = p < 0.0 ? 0.0 : p;
-        double psi;
-        if (PLAIN) {
-            float Hf = (float)Hn, pf = (float)pp;
-            psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, (float)e2)), (float)P.maxPack);
-        } else {
-            psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
-        }
         double* M = A.MS + mp(s, 5, 0, SC) + c;
         M[0] = w;
         M[(size_t)SC] = p;
         M[2 * (size_t)SC] = Hn;
-        M[3 * (size_t)SC] = psi;
-        M[4 * (size_t)SC] = density(P, psi);
+        if (PLAIN) {
+            // the stage-0 inputs of the FP32 closures and of the vertex source, in float
+            float Hf = (float)Hn, pf = (float)pp;
+            float psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, (float)e2)), (float)P.maxPack);
+            mfp(A, s, MF_PSI0, SC)[c] = psi;
+            mfp(A, s, MF_HN, SC)[c] = Hf;
+            mfp(A, s, MF_PSI, SC)[c] = psi;
+            mfp(A, s, MF_RHO, SC)[c] = (float)density(P, (double)psi);
+            mfp(A, s, MF_BT, SC)[c] = (float)ct[1];
+            mfp(A, s, MF_BX, SC)[c] = (float)ct[2];
+            mfp(A, s, MF_BY, SC)[c] = (float)ct[3];
+        } else {
+            double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
+            M[3 * (size_t)SC] = psi;
+            M[4 * (size_t)SC] = density(P, psi);
+        }
     }
 }
 
@@ -129,14 +145,26 @@ __device__ __forceinline__ void m_emd(const DevParams& P, const DevParams32& F, 
             dry = below_pos(Hn, e) || below_pos(HnW, e) || below_pos(HnE, e) || below_pos(HnS, e) || below_pos(HnN, e);
         else
             dry = Hn < e || HnW < e || HnE < e || HnS < e || HnN < e;
-        if (!dry) {
-            R dbx = (R)CT[mp(s, 4, 2, SC) + c], dby = (R)CT[mp(s, 4, 3, SC) + c];
-            Pt<R> pt{(R)Hn, (R)A.UV[mp(s, 2, 0, SC) + c], (R)A.UV[mp(s, 2, 1, SC) + c], (R)A.MS[mp(s, 5, 3, SC) + c],
-                     (R)A.MS[mp(s, 5, 4, SC) + c], (R)CT[mp(s, 4, 1, SC) + c], dbx, dby, gam_of<R>(P.geo, dbx, dby)};
-            if constexpr (sizeof(R) == sizeof(float)) emd = (double)erosion_minus_deposition<R>(F, pt);
-            else emd = erosion_minus_deposition<R>(P, pt);
+        if constexpr (sizeof(R) == sizeof(float)) {
+            // the FP32 form: the stage's closure inputs from the float planes, E - D kept in float
+            float e = 0.f;
+            if (!dry) {
+                float dbx = mfp(A, s, MF_BX, SC)[c], dby = mfp(A, s, MF_BY, SC)[c];
+                Pt<float> pt{mfp(A, s, MF_HN, SC)[c], (float)A.UV[mp(s, 2, 0, SC) + c], (float)A.UV[mp(s, 2, 1, SC) + c],
+                             mfp(A, s, MF_PSI, SC)[c], mfp(A, s, MF_RHO, SC)[c], mfp(A, s, MF_BT, SC)[c], dbx, dby,
+                             gam_of<float>(P.geo, dbx, dby)};
+                e = erosion_minus_deposition<float>(F, pt);
+            }
+            mfp(A, s, MF_EMD, SC)[c] = e;
+        } else {
+            if (!dry) {
+                R dbx = (R)CT[mp(s, 4, 2, SC) + c], dby = (R)CT[mp(s, 4, 3, SC) + c];
+                Pt<R> pt{(R)Hn, (R)A.UV[mp(s, 2, 0, SC) + c], (R)A.UV[mp(s, 2, 1, SC) + c], (R)A.MS[mp(s, 5, 3, SC) + c],
+                         (R)A.MS[mp(s, 5, 4, SC) + c], (R)CT[mp(s, 4, 1, SC) + c], dbx, dby, gam_of<R>(P.geo, dbx, dby)};
+                emd = erosion_minus_deposition<R>(P, pt);
+            }
+            A.EMD[(size_t)s * SC + c] = emd;
         }
-        A.EMD[(size_t)s * SC + c] = emd;
     }
 }
 
@@ -214,20 +242,36 @@ __device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int
             mode = 2;
         }
         double x[4], y[4], e[4];
-        for (int q = 0; q < 4; ++q) e[q] = cellv(A, CT, cs[q], -1, ci[q], cj[q], nX, SC);
-        double kx = 0.0, ky = 0.0, ke;
+        double kx = 0.0, ky = 0.0, ke = 0.0;
+        float ddt32 = 0.f;
         if (PLAIN) {
-            // the slopes only matter where E - D is non-zero around the vertex
-            ke = (e[0] + e[1]) + (e[2] + e[3]);
-            if (ke != 0.0) {
+            // FP32 form: the four cells' E - D and slopes from the float stage planes (a ghost
+            // cell's E - D is zero and its slopes are the step-start factor cache's), summed
+            // in FP32; the slopes only matter where E - D is non-zero around the vertex.
+            float ef[4];
+            for (int q = 0; q < 4; ++q) ef[q] = cs[q] < 0 ? 0.f : mfp(A, cs[q], MF_EMD, SC)[cj[q] * nX + ci[q]];
+            float kef = (ef[0] + ef[1]) + (ef[2] + ef[3]);
+            if (kef != 0.f) {
+                float xf[4], yf[4];
                 for (int q = 0; q < 4; ++q) {
-                    x[q] = cellv(A, CT, cs[q], 2, ci[q], cj[q], nX, SC);
-                    y[q] = cellv(A, CT, cs[q], 3, ci[q], cj[q], nX, SC);
+                    int cc = cj[q] * nX + ci[q];
+                    if (cs[q] < 0) {
+                        xf[q] = 0.f;
+                        yf[q] = 0.f;
+                    } else if (A.kind[cs[q]] == SLOT_ACTIVE) {
+                        xf[q] = mfp(A, cs[q], MF_BX, SC)[cc];
+                        yf[q] = mfp(A, cs[q], MF_BY, SC)[cc];
+                    } else {
+                        xf[q] = A.TF[tcur][mp(cs[q], 6, 1, SC) + cc];
+                        yf[q] = A.TF[tcur][mp(cs[q], 6, 2, SC) + cc];
+                    }
                 }
-                kx = (x[0] + x[1]) + (x[2] + x[3]);
-                ky = (y[0] + y[1]) + (y[2] + y[3]);
+                float gx = 0.25f * ((xf[0] + xf[1]) + (xf[2] + xf[3])), gy = 0.25f * ((yf[0] + yf[1]) + (yf[2] + yf[3]));
+                float gam = P.geo ? sqrtf(1.f + gx * gx + gy * gy) : 1.f;
+                ddt32 = -0.25f * gam * kef * (float)P.invSolid;
             }
         } else {
+            for (int q = 0; q < 4; ++q) e[q] = cellv(A, CT, cs[q], -1, ci[q], cj[q], nX, SC);
             for (int q = 0; q < 4; ++q) {
                 x[q] = cellv(A, CT, cs[q], 2, ci[q], cj[q], nX, SC);
                 y[q] = cellv(A, CT, cs[q], 3, ci[q], cj[q], nX, SC);
@@ -243,14 +287,8 @@ __device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int
             // FP32 form: the rate in FP32 (its E - D terms come from FP32 closures), the
             // stage update as bt0 + a (bt_k - bt0 + dt ddt) in FP64, so a vertex with no
             // erosion or deposition around it keeps its bed exactly.
-            float ddt = 0.f;
-            if (ke != 0.0) {
-                float gx = 0.25f * (float)kx, gy = 0.25f * (float)ky;
-                float gam = P.geo ? sqrtf(1.f + gx * gx + gy * gy) : 1.f;
-                ddt = -0.25f * gam * (float)ke * (float)P.invSolid;
-            }
-            double inc = (btp - bt0) + dt * (double)ddt;
-            if (stage == 1) nb = bt0 + dt * (double)ddt;
+            double inc = (btp - bt0) + dt * (double)ddt32;
+            if (stage == 1) nb = bt0 + dt * (double)ddt32;
             else if (stage == 2) nb = bt0 + 0.25 * inc;
             else nb = bt0 + (2.0 / 3.0) * inc;
         } else {
@@ -310,9 +348,8 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
         A.CT[tnew][mp(s, 4, 2, SC) + c] = dbx;
         A.CT[tnew][mp(s, 4, 3, SC) + c] = dby;
         const double* C0 = A.CT[tcur];
-        double gamold, gamnew, ign = 1.0;
+        double gamold = 1.0, gamnew, ign = 1.0;
         if (PLAIN) {
-            gamold = gam_cached(P, A, tcur, s, c, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
             if (P.geo) {
                 double g2 = 1.0 + (dbx * dbx + dby * dby);
                 ign = rsqrt_nr(g2);
@@ -324,18 +361,32 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
             gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
             gamnew = gam_of(P.geo, dbx, dby);
         }
-        double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
-        double Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
         double db = btc - C0[mp(s, 4, 1, SC) + c];
         double w, Hnpsi, Hn, psi;
         if (PLAIN) {
-            w = (b0c + btc) + (Hn_old * gamold - db) * (ign * ign);
-            Hnpsi = (p0 * gamold - psib * db) * ign;
+            // Hn gam and Hnpsi gam of the step start from the attempt's cache (m_init)
+            const double* Z = A.M0 + mp(s, 3, 0, SC) + c;
+            w = (b0c + btc) + (Z[(size_t)SC] - db) * (ign * ign);
+            Hnpsi = (Z[2 * (size_t)SC] - psib * db) * ign;
             Hn = ((w - b0c) - btc) * gamnew;
             if (Hn < 0.0) Hn = 0.0;
             float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi;
-            psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, F.hThr2)), F.maxPack);
+            float psif = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, F.hThr2)), F.maxPack);
+            double* M = A.MS + mp(s, 5, 0, SC) + c;
+            M[0] = w;
+            M[(size_t)SC] = Hnpsi;
+            M[2 * (size_t)SC] = Hn;
+            // the stage's inputs of the FP32 closures and of the vertex source, in float
+            mfp(A, s, MF_HN, SC)[c] = Hf;
+            mfp(A, s, MF_PSI, SC)[c] = psif;
+            mfp(A, s, MF_RHO, SC)[c] = (float)density(P, (double)psif);
+            mfp(A, s, MF_BT, SC)[c] = (float)btc;
+            mfp(A, s, MF_BX, SC)[c] = (float)dbx;
+            mfp(A, s, MF_BY, SC)[c] = (float)dby;
+            return;
         } else {
+            double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
+            double Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
             w = -db / gamnew / gamnew;
             w = w + btc;
             w = w + Hn_old * gamold / gamnew / gamnew;
@@ -364,23 +415,28 @@ __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevA
                                                   double& Hn_old, double& Hn_new) {
     int SC = P.nX * P.nY;
     const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
-    double gamold = PLAIN ? gam_cached(P, A, tcur, s, c, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c])
-                          : gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
-    double gamnew = PLAIN ? gam_nr(P, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c])
-                          : gam_of(P.geo, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c]);
+    if (PLAIN) {
+        // the step-start Hn, Hn gam, Hnpsi gam and psi from the attempt's cache (m_init)
+        const double* Z = A.M0 + mp(s, 3, 0, SC) + c;
+        double gamnew = gam_nr(P, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c]);
+        Hn_old = Z[0];
+        Hn_new = compute_hn(A.MS[mp(s, 5, 0, SC) + c], C3[mp(s, 4, 0, SC) + c], C3[mp(s, 4, 1, SC) + c], gamnew);
+        deltaBt = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
+        psiold = (double)A.MF[(size_t)s * SC + c];
+        excess = -(Z[2 * (size_t)SC] * P.invSolid - deltaBt);
+        excess = mx(excess, -(Z[(size_t)SC] - deltaBt));
+        return;
+    }
+    double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+    double gamnew = gam_of(P.geo, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c]);
     double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
     Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
     Hn_new = compute_hn(A.MS[mp(s, 5, 0, SC) + c], C3[mp(s, 4, 0, SC) + c], C3[mp(s, 4, 1, SC) + c], gamnew);
     deltaBt = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
     // im0's solids fraction as the first hydraulic step left it
     double H0 = Hn_old < 0.0 ? 0.0 : Hn_old, pp = p0 < 0.0 ? 0.0 : p0, e2 = P.hThr * P.hThr;
-    if (PLAIN) {
-        float Hf = (float)H0, pf = (float)pp;
-        psiold = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, (float)e2)), (float)P.maxPack);
-    } else {
-        psiold = mn(2.0 * H0 * pp / (H0 * H0 + mx(H0 * H0, e2)), P.maxPack);
-    }
-    excess = PLAIN ? -(p0 * gamold * P.invSolid - deltaBt) : -(p0 * gamold / (1.0 - P.BedPorosity) - deltaBt);
+    psiold = mn(2.0 * H0 * pp / (H0 * H0 + mx(H0 * H0, e2)), P.maxPack);
+    excess = -(p0 * gamold / (1.0 - P.BedPorosity) - deltaBt);
     excess = mx(excess, -(Hn_old * gamold - deltaBt));
 }
 
@@ -481,23 +537,31 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
     double delta = 4.0 * corr / sum;
     const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
     size_t c = (size_t)j * nX + i;
-    double gamold = PLAIN ? gam_cached(P, A, tcur, s, c, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c])
-                          : gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
-    double w0 = A.Q[qa][mp(s, 4, 0, SC) + c];
-    double Hnold = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
-    if (Hnold < 0.0) Hnold = 0.0;
+    // Hg: the step-start Hn (clamped at 0) times gam; Hgp: Hnpsi gam / (1 - porosity).  The
+    // FP32 form takes both from the attempt's cache (m_init).
+    double Hg, Hgp;
+    if (PLAIN) {
+        const double* Z = A.M0 + mp(s, 3, 0, SC) + c;
+        Hg = Z[0] < 0.0 ? 0.0 : Z[(size_t)SC];
+        Hgp = Z[2 * (size_t)SC] * P.invSolid;
+    } else {
+        double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+        double w0 = A.Q[qa][mp(s, 4, 0, SC) + c];
+        double Hnold = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
+        if (Hnold < 0.0) Hnold = 0.0;
+        Hg = Hnold * gamold;
+        Hgp = A.Q[qa][mp(s, 4, 3, SC) + c] * gamold / (1.0 - P.BedPorosity);
+    }
     double db = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
     double tol = kEPS * A.MS[mp(s, 5, 0, SC) + c] * 10.0;
     double adjustment = 0.0;
-    double disc = PLAIN ? (Hnold * gamold - db) + corr : kahan3(Hnold * gamold, -db, corr);
+    double disc = PLAIN ? (Hg - db) + corr : kahan3(Hg, -db, corr);
     if (fabs(disc) < tol) {
-        adjustment = PLAIN ? (tol - Hnold * gamold) + db : kahan3(tol, -Hnold * gamold, db);
+        adjustment = PLAIN ? (tol - Hg) + db : kahan3(tol, -Hg, db);
         adjustment = adjustment * (4.0 / sum);
         adjustment = adjustment - delta;
         adjustment = mx(adjustment, 0.0);
     }
-    double Hgp = PLAIN ? A.Q[qa][mp(s, 4, 3, SC) + c] * gamold * P.invSolid
-                       : A.Q[qa][mp(s, 4, 3, SC) + c] * gamold / (1.0 - P.BedPorosity);
     tol = kEPS * 10.0;
     disc = PLAIN ? (Hgp - db) + corr : kahan3(Hgp, -db, corr);
     if (fabs(disc) < tol) {
@@ -558,11 +622,14 @@ __device__ __forceinline__ void redist_cells_of(const DevParams& P, const DevArr
 // copy of a ghost tile there, which only the last hydraulic RHS of the step would read).
 // Split in two so a warp can load the cell's step-start data (which the walk never
 // changes) while another lane is still correcting the vertices.
+// (The FP32 form loads the step-start Hn gam, clamped, and Hnpsi gam from the attempt's
+// cache into hg / pg instead of the step-start w, Hnpsi, b0 and slopes.)
 struct RedistCell {
     int ct, ci, cj;
     bool on;
-    double b0n, b00, bt0, bx0, by0, w0, p0;
+    double b0n, b00, bt0, bx0, by0, w0, p0, hg, pg;
 };
+template <bool PLAIN>
 __device__ __forceinline__ void redist_cell_load(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int ct, int ci,
                                                  int cj, RedistCell& r) {
     r.ct = ct; r.ci = ci; r.cj = cj;
@@ -572,6 +639,13 @@ __device__ __forceinline__ void redist_cell_load(const DevParams& P, const DevAr
     size_t cc = (size_t)cj * P.nX + ci;
     const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
     r.b0n = C3[mp(ct, 4, 0, SC) + cc];
+    if (PLAIN) {
+        const double* Z = A.M0 + mp(ct, 3, 0, SC) + cc;
+        r.bt0 = C0[mp(ct, 4, 1, SC) + cc];
+        r.hg = Z[0] < 0.0 ? 0.0 : Z[(size_t)SC];
+        r.pg = Z[2 * (size_t)SC];
+        return;
+    }
     r.b00 = C0[mp(ct, 4, 0, SC) + cc];
     r.bt0 = C0[mp(ct, 4, 1, SC) + cc];
     r.bx0 = C0[mp(ct, 4, 2, SC) + cc];
@@ -598,13 +672,10 @@ __device__ __forceinline__ void redist_cell_apply(const DevParams& P, const DevA
         A.CT[tnew][mp(r.ct, 4, 2, SC) + cc] = dbx;
         A.CT[tnew][mp(r.ct, 4, 3, SC) + cc] = dby;
         double dbc = btc - r.bt0;
-        double go = gam_cached(P, A, tcur, r.ct, (int)cc, r.bx0, r.by0);
         double ign = 1.0;
         if (P.geo) ign = rsqrt_nr(1.0 + (dbx * dbx + dby * dby));
-        double Hno = compute_hn(r.w0, r.b00, r.bt0, go);
-        if (Hno < 0.0) Hno = 0.0;
-        A.MS[mp(r.ct, 5, 0, SC) + cc] = (r.b0n + btc) + (Hno * go - dbc) * (ign * ign);
-        A.MS[mp(r.ct, 5, 1, SC) + cc] = (r.p0 * go - (1.0 - P.BedPorosity) * dbc) * ign;
+        A.MS[mp(r.ct, 5, 0, SC) + cc] = (r.b0n + btc) + (r.hg - dbc) * (ign * ign);
+        A.MS[mp(r.ct, 5, 1, SC) + cc] = (r.pg - (1.0 - P.BedPorosity) * dbc) * ign;
         return;
     }
     double c3[3];
@@ -624,7 +695,7 @@ template <bool PLAIN>
 __device__ __forceinline__ void redist_cell(const DevParams& P, const DevArrays& A, int qa, int tcur, int tnew, int ct, int ci,
                                             int cj) {
     RedistCell r;
-    redist_cell_load(P, A, qa, tcur, tnew, ct, ci, cj, r);
+    redist_cell_load<PLAIN>(P, A, qa, tcur, tnew, ct, ci, cj, r);
     redist_cell_apply<PLAIN>(P, A, tcur, tnew, r);
 }
 
@@ -767,7 +838,7 @@ __global__ void __launch_bounds__(32) k_m_redist_wave(DevArrays A, const int* __
 #pragma unroll
         for (int k = 0; k < 9; ++k)
             if (k == lane - 1) { mt = vt[k]; mi = vi[k]; mj = vj[k]; }
-        redist_cell_load(cP, A, qa, tcur, tnew, mt, mi, mj, r);
+        redist_cell_load<PLAIN>(cP, A, qa, tcur, tnew, mt, mi, mj, r);
     }
     int go = 0;
     if (lane == 0) {
