@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256) k_m_batch(const SimStatic* __restrict__ s
         int s = X.slots[pos];
         if (K == MK_INIT) {
             if (local == 0 && threadIdx.x < 2) J.flags[threadIdx.x] = 0;
-            m_init<true>(X.P, X.A, s, item, J.qa, J.tcur, J.tnew);
+            m_init<true>(X.P, X.F, X.A, s, item, J.qa, J.tcur, J.tnew);
         } else if (K == MK_EMD) {
             m_emd<float>(X.P, X.F, X.A, s, item, J.tnew);
         } else if (K == MK_BT) {

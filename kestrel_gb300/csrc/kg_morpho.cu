@@ -65,7 +65,8 @@ __device__ __forceinline__ double gam_nr(const DevParams& P, double bx, double b
 // Copy the step-start bed into the M set and fill the stage state of im0 (the state the
 // first hydraulic step produced).
 template <bool PLAIN>
-__device__ __forceinline__ void m_init(const DevParams& P, const DevArrays& A, int s, int item_, int qa, int tcur, int tnew) {
+__device__ __forceinline__ void m_init(const DevParams& P, const DevParams32& F, const DevArrays& A, int s, int item_, int qa,
+                                       int tcur, int tnew) {
     int SC = P.nX * P.nY, SV = (P.nX + 1) * (P.nY + 1);
     // b0 (vertex plane 0, cell plane 0) is static and both topography sets hold it: only
     // the bed change and the slopes are carried into the M set.
@@ -92,23 +93,27 @@ __device__ __forceinline__ void m_init(const DevParams& P, const DevArrays& A, i
             Z[(size_t)SC] = Hn * gam;
             Z[2 * (size_t)SC] = p * gam;
         }
-        if (Hn < 0.0) Hn = 0.0;
-        double pp = p < 0.0 ? 0.0 : p;
         double* M = A.MS + mp(s, 5, 0, SC) + c;
         M[0] = w;
         M[(size_t)SC] = p;
-        M[2 * (size_t)SC] = Hn;
+        // FP32 form: the stage depth is kept unclamped (the dry test reads its sign bit as a
+        // value below the threshold, and the tests read it as the new depth)
+        if (PLAIN) M[2 * (size_t)SC] = Hn;
+        if (Hn < 0.0) Hn = 0.0;
+        double pp = p < 0.0 ? 0.0 : p;
+        if (!PLAIN) M[2 * (size_t)SC] = Hn;
         if (PLAIN) {
             // the stage-0 inputs of the FP32 closures and of the vertex source, in float
             float Hf = (float)Hn, pf = (float)pp;
             float psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, (float)e2)), (float)P.maxPack);
+            // (the float slopes of the step-start bed are the factor cache's)
             mfp(A, s, MF_PSI0, SC)[c] = psi;
             mfp(A, s, MF_HN, SC)[c] = Hf;
             mfp(A, s, MF_PSI, SC)[c] = psi;
-            mfp(A, s, MF_RHO, SC)[c] = (float)density(P, (double)psi);
+            mfp(A, s, MF_RHO, SC)[c] = density<float>(F, psi);
             mfp(A, s, MF_BT, SC)[c] = (float)ct[1];
-            mfp(A, s, MF_BX, SC)[c] = (float)ct[2];
-            mfp(A, s, MF_BY, SC)[c] = (float)ct[3];
+            mfp(A, s, MF_BX, SC)[c] = A.TF[tcur][mp(s, 6, 1, SC) + c];
+            mfp(A, s, MF_BY, SC)[c] = A.TF[tcur][mp(s, 6, 2, SC) + c];
         } else {
             double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
             M[3 * (size_t)SC] = psi;
@@ -369,17 +374,17 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
             w = (b0c + btc) + (Z[(size_t)SC] - db) * (ign * ign);
             Hnpsi = (Z[2 * (size_t)SC] - psib * db) * ign;
             Hn = ((w - b0c) - btc) * gamnew;
-            if (Hn < 0.0) Hn = 0.0;
-            float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi;
-            float psif = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, F.hThr2)), F.maxPack);
             double* M = A.MS + mp(s, 5, 0, SC) + c;
             M[0] = w;
             M[(size_t)SC] = Hnpsi;
-            M[2 * (size_t)SC] = Hn;
+            M[2 * (size_t)SC] = Hn;  // unclamped (as m_init)
+            if (Hn < 0.0) Hn = 0.0;
+            float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi;
+            float psif = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, F.hThr2)), F.maxPack);
             // the stage's inputs of the FP32 closures and of the vertex source, in float
             mfp(A, s, MF_HN, SC)[c] = Hf;
             mfp(A, s, MF_PSI, SC)[c] = psif;
-            mfp(A, s, MF_RHO, SC)[c] = (float)density(P, (double)psif);
+            mfp(A, s, MF_RHO, SC)[c] = density<float>(F, psif);
             mfp(A, s, MF_BT, SC)[c] = (float)btc;
             mfp(A, s, MF_BX, SC)[c] = (float)dbx;
             mfp(A, s, MF_BY, SC)[c] = (float)dby;
@@ -409,7 +414,11 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
 
 // ExcessDeposition (src/Redistribute.f90:158-198) of cell (s, c) between im0 and im3.
 // PLAIN (the FP32 form) takes gamma from the factor cache / an FP32-seeded Newton step.
-template <bool PLAIN = false>
+// STAGE_HN (FP32 form, the check after the stages): the new depth is the stage's unclamped
+// depth, which m_cells formed with the same operations from the same w, bed and gamma (and
+// which m_init set for a cell no stage changed, one the check skips); the redistribution
+// walk, which changes cells after the stages, recomputes it.
+template <bool PLAIN = false, bool STAGE_HN = false>
 __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevArrays& A, int s, int c, int qa, int tcur,
                                                   int tnew, double& excess, double& deltaBt, double& psiold,
                                                   double& Hn_old, double& Hn_new) {
@@ -418,9 +427,13 @@ __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevA
     if (PLAIN) {
         // the step-start Hn, Hn gam, Hnpsi gam and psi from the attempt's cache (m_init)
         const double* Z = A.M0 + mp(s, 3, 0, SC) + c;
-        double gamnew = gam_nr(P, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c]);
         Hn_old = Z[0];
-        Hn_new = compute_hn(A.MS[mp(s, 5, 0, SC) + c], C3[mp(s, 4, 0, SC) + c], C3[mp(s, 4, 1, SC) + c], gamnew);
+        if (STAGE_HN) {
+            Hn_new = A.MS[mp(s, 5, 2, SC) + c];
+        } else {
+            double gamnew = gam_nr(P, C3[mp(s, 4, 2, SC) + c], C3[mp(s, 4, 3, SC) + c]);
+            Hn_new = compute_hn(A.MS[mp(s, 5, 0, SC) + c], C3[mp(s, 4, 0, SC) + c], C3[mp(s, 4, 1, SC) + c], gamnew);
+        }
         deltaBt = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
         psiold = (double)A.MF[(size_t)s * SC + c];
         excess = -(Z[2 * (size_t)SC] * P.invSolid - deltaBt);
@@ -461,7 +474,7 @@ __device__ __forceinline__ void m_check(const DevParams& P, const DevArrays& A, 
                 return;
         }
         double ex, dBt, psiold, Hn_old, Hn_new;
-        excess_deposition<PLAIN>(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Hn_old, Hn_new);
+        excess_deposition<PLAIN, PLAIN>(P, A, s, c, qa, tcur, tnew, ex, dBt, psiold, Hn_old, Hn_new);
         bool refine = false;
         if (ex > kEPS && dBt > kEPS && psiold > -kEPS) {
             if (Hn_old < P.EroCriticalHeight || fabs(Hn_new - Hn_old) < P.EroCriticalHeight) {
@@ -775,7 +788,7 @@ __global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restri
     kg_dep_wait();
     if (blockIdx.x == 0 && threadIdx.x < 2) ctl_flags[threadIdx.x] = 0;
     KG_TILE_ITEMS((cP.nX + 1) * (cP.nY + 1))
-    m_init<PLAIN>(cP, A, s, item_, qa, tcur, tnew);
+    m_init<PLAIN>(cP, cP32, A, s, item_, qa, tcur, tnew);
 }
 template <class R>
 __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
