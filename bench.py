@@ -360,9 +360,11 @@ def run_serve(args):
     srv = serve.Server(hbm_budget=args.budget_gb * 1e9, max_members=min(256, args.requests), keep_state=False)
     clocks = ClockSampler(0)
     clocks.start()
-    rep = srv.run(reqs)
-    clk = clocks.stop()
-    srv.close()
+    try:
+        rep = srv.run(reqs, max_wall_s=getattr(args, "serve_max_wall", None))
+    finally:
+        clk = clocks.stop()
+        srv.close()
     line = {"metric": "cell-updates/s", "value": rep["cell_updates_per_s"], "unit": "cell-updates/s", "n_gpus": 1,
             "steps": rep["batch_steps"], "warmup": 0, "ms_per_step": 1e3 * rep["makespan_s"] / max(rep["batch_steps"], 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -393,6 +395,7 @@ def extras_serve(args):
     import copy
     a = copy.copy(args)
     a.tend_min, a.tend_max = args.tend_min * args.serve_tend_scale, args.tend_max * args.serve_tend_scale
+    a.serve_max_wall = 300.0
     r = run_serve(a)
     rep = r["serve"]
     return {"workload": "serve_fp32", "requests": a.requests, "rate_per_s": a.rate,
@@ -405,7 +408,7 @@ def extras_serve(args):
                     f"{args.serve_tend_scale} so that the stream is served within the default run"}
 
 
-def run_sparse_window(args, t_window: float = 200.0, steps: int = 20):
+def run_sparse_window(args, t_window: float = 200.0, steps: int = 20, deadline_s=None):
     """The large sparse configuration (8192^2 cells in 16,384 tiles of 64^2, three seeded
     flux sources, Pouliquen drag, morphodynamics; FP32 form): an untimed spin-up to
     t_window (the active-tile count recorded every 20 s), then `steps` accepted steps
@@ -420,7 +423,7 @@ def run_sparse_window(args, t_window: float = 200.0, steps: int = 20):
     p, b0 = wl["params"]()
     t0 = time.perf_counter()
     sim = lib.simulation(p, precision=wl["prec"], b0=b0)
-    timeline = spin_up(sim, p, t_window, 20.0)
+    timeline = spin_up(sim, p, t_window, 20.0, deadline_s=deadline_s)
     spin_s = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -467,22 +470,33 @@ def reduce_replicas(seconds, cell_updates, dist=None, device="cpu"):
     return float(tt.item()), float(cc.item())
 
 
-def spin_up(sim, p, spin, every=None):
+def spin_up(sim, p, spin, every=None, deadline_s=None):
     """Untimed integration to t = spin; with `every`, the active-tile count is recorded at
-    each multiple of `every` seconds: [[t, active tiles, percent of all tiles], ...]."""
+    each multiple of `every` seconds: [[t, active tiles, percent of all tiles], ...] (and
+    printed to stderr as it goes).  With `deadline_s`, the integration runs step by step and
+    raises TimeoutError once that much wall time has passed (a secondary figure must not
+    hold up the bench line)."""
     out = []
     if spin <= 0.0:
         return out
-    if not every:
+    if not every and not deadline_s:
         sim.integrate_to(spin)
         return out
     total = p.nXtiles * p.nYtiles
-    t = 0.0
+    t, t0 = 0.0, time.perf_counter()
+    every = every or spin
     while t < spin:
         t = min(spin, t + every)
-        sim.integrate_to(t)
+        if deadline_s:
+            while sim.time[0] < t:
+                sim.step(t)
+                if time.perf_counter() - t0 > deadline_s:
+                    raise TimeoutError(f"spin-up reached t={sim.time[0]:.3f} s of {spin} s in {deadline_s:.0f} s of wall time")
+        else:
+            sim.integrate_to(t)
         n = len(sim.active_tiles())
         out.append([round(sim.time[0], 3), n, round(100.0 * n / total, 3)])
+        print(f"spin-up t={sim.time[0]:.1f} s: {n} active tiles, {time.perf_counter() - t0:.1f} s wall", file=sys.stderr, flush=True)
     return out
 
 
@@ -566,6 +580,65 @@ def run_dem(args):
                                 "cores": 1, "host_cores": os.cpu_count(), "kind": "port",
                                 "sample": f"oracle set-up: raster copy, sources and the heights of its {nt} active and ghost tiles, {secs:.2f} s"}
     print(json.dumps(line))
+
+
+def run_fp32_error(args):
+    """The FP32 form's depth error on the 2048^2 morphodynamic configuration against the
+    FP64 path, set beside the configuration's own sensitivity to its inputs: the FP64 path
+    run again with the hydrograph's peak inflow scaled by (1 + 2^-52) (one FP64 rounding)
+    and by (1 + 2^-24) (one FP32 rounding).  At each checkpoint every run is compared with
+    the unperturbed FP64 run over the tiles active in either (an inactive tile is dry):
+    relative L-inf of the depth Hn and its 99th percentile over the cells wet in either run,
+    both relative to the largest FP64 depth, with the accepted and refused step counts."""
+    import numpy as np
+    import torch
+    from kestrel_gb300 import abi, lib, workloads
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    times = [float(x) for x in args.error_times.split(",")]
+    runs = [("fp64", abi.PREC_FP64, 0.0), ("fp64_inflow_2^-52", abi.PREC_FP64, 2.0 ** -52),
+            ("fp64_inflow_2^-24", abi.PREC_FP64, 2.0 ** -24), ("fp32", abi.PREC_FP32, 0.0)]
+    sims, stats = {}, {}
+    for name, prec, eps in runs:
+        p, b0 = workloads.morpho_flux_2048()
+        p.sources[0].flux[1] = p.sources[0].flux[1] * (1.0 + eps)
+        sims[name] = lib.simulation(p, precision=prec, b0=b0)
+        stats[name] = [0, 0]
+    nX, nY = p.nXpertile, p.nYpertile
+
+    def depth(sim):
+        return {t: sim.field(t, 5) for t in sim.active_tiles()}
+
+    rows = []
+    t0 = time.perf_counter()
+    for tc in times:
+        hs = {}
+        for name, _, _ in runs:
+            st = sims[name].integrate_to(tc)
+            stats[name][0] += st.steps
+            stats[name][1] += st.rejected
+            hs[name] = depth(sims[name])
+        ref = hs["fp64"]
+        scale = max(float(np.max(np.abs(v))) for v in ref.values())
+        row = {"t": tc, "fp64_steps": stats["fp64"][0], "fp64_active_tiles": len(ref), "max_depth": scale}
+        zero = np.zeros((nY, nX))
+        for name, _, _ in runs[1:]:
+            h = hs[name]
+            tiles = sorted(set(ref) | set(h))
+            a = np.concatenate([ref.get(t, zero).ravel() for t in tiles])
+            b = np.concatenate([h.get(t, zero).ravel() for t in tiles])
+            d = np.abs(a - b)
+            wet = (a > 0) | (b > 0)
+            row[name] = {"linf": float(d.max() / scale), "p99": float(np.percentile(d[wet], 99) / scale) if wet.any() else 0.0,
+                         "steps": stats[name][0], "rejected": stats[name][1], "active_tiles": len(h)}
+        rows.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+    for s in sims.values():
+        s.close()
+    print(json.dumps({"workload": "fp32_error_2048",
+                      "desc": "depth of the FP32 form and of FP64 runs with the peak inflow scaled by (1 + 2^-52) and "
+                              "(1 + 2^-24), against the unperturbed FP64 run on the 2048^2 morphodynamic configuration; "
+                              "linf and p99 relative to the largest FP64 depth, over the tiles active in either run",
+                      "seconds": time.perf_counter() - t0, "checkpoints": rows}))
 
 
 def fp64_plain(args, wname, snapshot=None):
@@ -670,8 +743,19 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs (profiling runs)")
     ap.add_argument("--sparse-window", type=float, default=200.0,
                     help="sparse configuration beside the headline: spin-up end (s) of its timed window")
+    ap.add_argument("--fused-morpho", type=int, default=1,
+                    help="FP32 form: one launch per morphodynamic stage (1) or three (0); same results")
+    ap.add_argument("--dry-skip", type=int, default=1,
+                    help="FP32 form: skip the flux work of blocks with no water (1) or run every block (0)")
+    ap.add_argument("--error-times", default="5,10,20,40,80,120",
+                    help="fp32_error_2048: checkpoints (s) of the depth comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+
+    if args.workload == "fp32_error_2048":
+        if int(os.environ.get("RANK", "0")) != 0 or args.impl == "reference":
+            return
+        return run_fp32_error(args)
 
     if args.workload in ("ensemble_fp32", "serve_fp32") and args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
@@ -710,6 +794,8 @@ def main():
 
     # ---- device-timed throughput ----
     sim = lib.simulation(p, precision=wl["prec"], b0=b0)
+    L.kg_set_fused_morpho(sim.h, args.fused_morpho)
+    L.kg_set_dry_skip(sim.h, args.dry_skip)
     spin = wl.get("spinup", 0.0) if args.spinup is None else args.spinup
     timeline = spin_up(sim, p, spin, wl.get("timeline"))
     stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
@@ -866,7 +952,7 @@ def main():
     if args.workload == "morpho_flux_2048_fp32" and not args.no_extras:
         # the other forms of the metric on their own configurations, under their own keys
         # (secondary figures: an error in one never loses the headline line)
-        for key, fn in (("sparse_8192_fp32", lambda: run_sparse_window(args, t_window=args.sparse_window)),
+        for key, fn in (("sparse_8192_fp32", lambda: run_sparse_window(args, t_window=args.sparse_window, deadline_s=300.0)),
                         ("ensemble_fp32", lambda: extras_ensemble(args)),
                         ("serve_fp32", lambda: extras_serve(args))):
             try:

@@ -268,6 +268,18 @@ void* kg_stream(kg_ctx* ctx);
    No reference counterpart. */
 int  kg_set_kernel_timing(kg_ctx* ctx, int32_t enable);
 int  kg_get_kernel_time(kg_ctx* ctx, double* ms, int64_t* passes);
+/* FP32 form: run each stage of the morphodynamic operator (E - D, the vertex source and bed
+   update, the cell bed and w / Hnpsi update; MorphodynamicTimeStepper, src/TimeStepper.f90:
+   569-699) as one launch (enable, the default) or as three (0); the results are the same bit
+   for bit.  No effect on the FP64 form.  No reference counterpart. */
+int  kg_set_fused_morpho(kg_ctx* ctx, int32_t enable);
+/* FP32 form: skip the reconstruction, flux and RHS work of a 16 x 16 block whose cells and
+   two-cell halo hold no water (depth above the bed, Hnpsi and momenta all within
+   1e-4 heightThreshold) and no flux source, carrying its state forward with a zero RHS
+   (enable, the default), or run every block in full (0).  The difference is round-off of
+   the dry bed (face depths of order 1e-13 m).  No effect on the FP64 form, which always
+   runs every block as the reference does.  No reference counterpart. */
+int  kg_set_dry_skip(kg_ctx* ctx, int32_t enable);
 /* Redistribution work so far (RedistributeGrid, src/Redistribute.f90:203-244): the number
    of listed cells walked, the dependency waves they were run in and the walks.  No
    reference counterpart (the reference walks its list serially). */

@@ -56,6 +56,10 @@ cudaError_t launch_volume(const DevArrays& A, const int* d_slots, int n, int qcu
 cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int verts, int qa, int tcur, int tnew, int* ctl_flags,
                           bool fp32, cudaStream_t st);
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st);
+int m_stage32_blocks(int nX, int nY);
+cudaError_t launch_m_fused32(const DevArrays& A, const int* d_slots, int n, int nX, int nY, int qa, int tcur, int tnew,
+                             double dt_m, const double* dtp, int* ctl_flags, unsigned long long* keys, double* ex, int* ncand,
+                             int cap, cudaStream_t st);
 cudaError_t launch_m_bt(const DevArrays& A, const int* d_slots, int n, int verts, int tcur, int tnew, int stage, double dt,
                         const double* dtp, bool fp32, cudaStream_t st);
 cudaError_t launch_m_cells(const DevArrays& A, const int* d_slots, int n, int cells, int qa, int tcur, int tnew, bool fp32,
@@ -155,6 +159,7 @@ struct kg_ctx {
     int qcur = 0;                        // state buffer holding the solution (0..3)
     int tcur = 0;                        // topography set of the solution (0..1)
     int tdirty[2] = {2, 2};              // FP32 form factor cache of a set: 0 clean, 1 active tiles stale, 2 all stale
+    bool fused_m = true;                 // FP32 form: one launch per M stage (k_m_stage32)
     // Edge-band flags of the active tiles computed right after the last accepted hydraulic
     // step on its result (state buffer act_q, topography set act_t), so the next
     // CheckIfNearBoundaries needs no wait of its own; act_gen guards against host writes.
@@ -259,14 +264,14 @@ void bind_constants(kg_ctx& c);
 
 // Device bytes of one slot: Q, E/I, CT/FX/FY/BV (two sets), UV, MS, EMD, B0S, G9, GE, MX,
 // the source-override Hn and rho planes, nbr/kind/has_source/tile_of_slot, and in the FP32
-// form TD/TF/TFX/TFY (two sets) and M0/MF.
+// form TD/TF/TFX/TFY (two sets), M0/MF and BVA.
 size_t slot_bytes(size_t nX, size_t nY, int prec) {
     size_t SC = nX * nY, SFX = (nX + 1) * nY, SFY = nX * (nY + 1), SV = (nX + 1) * (nY + 1), nE = std::max(nX, nY);
     return sizeof(double) * (4 * 4 * SC + 2 * (4 * SC + SC + 4 * SC + 5 * SFX + 5 * SFY + 2 * SV) +
                              2 * SC + 5 * SC + SC + 2 * SC + 9 * SC + GE_COUNT * nE + 11 * SC + 2 * SC) +
            8 * sizeof(int) + 2 + sizeof(int) +
            (prec == KG_PREC_FP32 ? 2 * (3 * sizeof(double) * SC + 6 * sizeof(float) * SC + 2 * sizeof(float) * (SFX + SFY)) +
-                                       3 * sizeof(double) * SC + MF_COUNT * sizeof(float) * SC
+                                       3 * sizeof(double) * SC + MF_COUNT * sizeof(float) * SC + sizeof(double) * SV
                                  : 0);
 }
 size_t bytes_per_slot(const kg_ctx& c) { return slot_bytes((size_t)c.nX, (size_t)c.nY, c.prec); }
@@ -307,6 +312,7 @@ void ensure_cap(kg_ctx& c, int need) {
     if (c.prec == KG_PREC_FP32) {
         grow_array(c.A.M0, o * 3 * SC, n * 3 * SC, c.st);
         grow_array(c.A.MF, o * MF_COUNT * SC, n * MF_COUNT * SC, c.st);
+        grow_array(c.A.BVA, o * (size_t)c.SV, n * (size_t)c.SV, c.st);
     }
     grow_array(c.A.UV, o * 2 * SC, n * 2 * SC, c.st);
     grow_array(c.A.MS, o * 5 * SC, n * 5 * SC, c.st);
@@ -1163,14 +1169,6 @@ void queue_morpho(kg_ctx& c, double dt, const double* dtp, const int o[3], int t
     const bool fp32 = c.prec == KG_PREC_FP32;
     // The FP32 form's M kernels read gamma of the step-start topography from the cache.
     if (fp32 && c.tdirty[c.tcur]) refresh_topo32(c, c.tcur);
-    CK(launch_m_init(c.A, dl, n, c.SV, qa, c.tcur, tnew, c.d_mflags, fp32, c.st));
-    c.launches++;
-    for (int stage = 1; stage <= 3; ++stage) {
-        CK(launch_m_emd(c.A, dl, n, c.SC, tnew, fp32, c.st));
-        CK(launch_m_bt(c.A, dl, n, c.SV, c.tcur, tnew, stage, dt_m, dtp, fp32, c.st));
-        CK(launch_m_cells(c.A, dl, n, c.SC, qa, c.tcur, tnew, fp32, c.st));
-        c.launches += 3;
-    }
     int need = n * c.SC;
     if (need > c.cand_cap) {
         CK(cudaStreamSynchronize(c.st));
@@ -1182,8 +1180,23 @@ void queue_morpho(kg_ctx& c, double dt, const double* dtp, const int o[3], int t
         CK(cudaMalloc(&c.d_rcell, (size_t)c.cand_cap * sizeof(int)));
         CK(cudaMalloc(&c.d_rwave, ((size_t)c.cand_cap + 1) * sizeof(int)));
     }
-    CK(launch_m_check(c.A, dl, n, c.SC, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, fp32, c.st));
-    c.launches++;
+    if (fp32 && c.fused_m && m_stage32_blocks(c.nX, c.nY) > 0) {
+        // the FP32 form: init, then one launch per stage, the tests in the third
+        CK(launch_m_fused32(c.A, dl, n, c.nX, c.nY, qa, c.tcur, tnew, dt_m, dtp, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand,
+                            c.cand_cap, c.st));
+        c.launches += 4;
+    } else {
+        CK(launch_m_init(c.A, dl, n, c.SV, qa, c.tcur, tnew, c.d_mflags, fp32, c.st));
+        c.launches++;
+        for (int stage = 1; stage <= 3; ++stage) {
+            CK(launch_m_emd(c.A, dl, n, c.SC, tnew, fp32, c.st));
+            CK(launch_m_bt(c.A, dl, n, c.SV, c.tcur, tnew, stage, dt_m, dtp, fp32, c.st));
+            CK(launch_m_cells(c.A, dl, n, c.SC, qa, c.tcur, tnew, fp32, c.st));
+            c.launches += 3;
+        }
+        CK(launch_m_check(c.A, dl, n, c.SC, qa, c.tcur, tnew, c.d_mflags, c.d_ckey, c.d_cex, c.d_ncand, c.cand_cap, fp32, c.st));
+        c.launches++;
+    }
     int pre = std::min(c.cand_pre, c.cand_cap);
     if (pre > c.h_cand_cap) {
         CK(cudaStreamSynchronize(c.st));
@@ -1740,7 +1753,7 @@ void free_ctx(kg_ctx* c) {
     cudaFree(c->d_tlist);
     cudaFree(c->d_gather);
     cudaFree(c->d_rb0);
-    void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.B0S, c->A.M0, c->A.MF, c->A.G9, c->A.GE, c->A.MX,
+    void* ptrs[] = {c->A.UV, c->A.MS, c->A.EMD, c->A.B0S, c->A.M0, c->A.MF, c->A.BVA, c->A.G9, c->A.GE, c->A.MX,
                     c->A.nbr, c->A.kind, c->A.has_source, c->A.tile_of_slot, c->d_blocks, c->d_list, c->d_flags,
                     c->d_vol, c->d_srcHn, c->d_srcRho, c->d_ckey, c->d_cex, c->d_src,
                     c->d_rslot, c->d_rcell, c->d_rwave};
@@ -2230,6 +2243,21 @@ int kg_redistribution_stats(kg_ctx* c, int64_t* cells, int64_t* waves, int64_t* 
 }
 
 void* kg_stream(kg_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+int kg_set_fused_morpho(kg_ctx* c, int32_t enable) {
+    if (!c) return KG_ERR_PARAM;
+    c->fused_m = enable != 0;
+    return KG_OK;
+}
+
+int kg_set_dry_skip(kg_ctx* c, int32_t enable) {
+    if (!c) return KG_ERR_PARAM;
+    KG_GUARD(c, {
+        c->dp.no_dry_skip = enable ? 0 : 1;
+        if (g_const_owner == c) g_const_owner = nullptr;  // rewrite the constant bank before the next launch
+    });
+    return KG_OK;
+}
 
 int kg_set_kernel_timing(kg_ctx* c, int32_t enable) {
     if (!c) return KG_ERR_PARAM;

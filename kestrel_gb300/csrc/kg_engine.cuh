@@ -15,8 +15,10 @@
 //                  GE[slot][12][nE]           its stale w reconstructions at the edges
 //   static slopes  B0S[slot][2][nY][nX]       b0 parts of the cell slopes (FP32-form M stages)
 //   M step start   M0[slot][3][nY][nX]        FP32 form: Hn, Hn gam, Hnpsi gam of the M input
-//                  MF[slot][8][nY][nX]        FP32 form (float): its psi; the stage's Hn, psi,
-//                                             rho, bt, dbdx, dbdy and E - D
+//                  MF[slot][14][nY][nX]       FP32 form (float): its psi; the stage's Hn, psi,
+//                                             rho, bt, dbdx, dbdy and E - D; a second copy
+//                                             of the six stage planes (fused M stages)
+//                  BVA[slot][nY+1][nX+1]      FP32 form: a second copy of the vertex bt
 //   maxima         MX[slot][11][nY][nX]       Hnmax, umax, emax, dmax, psimax (value, time)
 //                                             and tfirst (src/Grid.f90:95-102)
 // FP32 form only (static per topography set, rebuilt when the set changes):
@@ -35,8 +37,11 @@
 
 namespace kg {
 
-// Planes of MF (FP32 form).
-enum MfPlane { MF_PSI0 = 0, MF_HN, MF_PSI, MF_RHO, MF_BT, MF_BX, MF_BY, MF_EMD, MF_COUNT };
+// Planes of MF (FP32 form).  The fused M stage (k_m_stage32) alternates the six stage
+// planes MF_HN..MF_BY with their copies MF_AHN..MF_ABY (plane + MF_ALT).
+enum MfPlane { MF_PSI0 = 0, MF_HN, MF_PSI, MF_RHO, MF_BT, MF_BX, MF_BY, MF_EMD,
+               MF_AHN, MF_APSI, MF_ARHO, MF_ABT, MF_ABX, MF_ABY, MF_COUNT };
+constexpr int MF_ALT = MF_AHN - MF_HN;
 enum SlotKind : int8_t { SLOT_FREE = 0, SLOT_ACTIVE = 1, SLOT_GHOST = 2 };
 enum Nb { NB_W = 0, NB_E = 1, NB_N = 2, NB_S = 3, NB_SW = 4, NB_SE = 5, NB_NW = 6, NB_NE = 7 };
 // Ghost edge records (GE planes): uLimX(iw,1,:), uLimX(iw,nX,:), uLimY(iw,:,1),
@@ -76,9 +81,12 @@ struct DevArrays {
     double* B0S;               // [slot][2][nY][nX] the static b0 parts of the cell slopes (FP32-form M stages)
     double* M0;                // [slot][3][nY][nX] FP32 form: the M attempt's step-start Hn (unclamped),
                                // Hn gam and Hnpsi gam (set by m_init, read by the stages and tests)
-    float* MF;                 // [slot][8][nY][nX] FP32 form (float): the step-start psi; the M stage's
+    float* MF;                 // [slot][14][nY][nX] FP32 form (float): the step-start psi; the M stage's
                                // Hn, psi, rho, bt, dbdx, dbdy as the closures and the vertex source read
-                               // them; the stage's E - D (zero on ghosts)
+                               // them; the stage's E - D (zero on ghosts); the second copy of the six
+                               // stage planes that the fused stages alternate with
+    double* BVA;               // [slot][nY+1][nX+1] FP32 form: the second copy of the M set's vertex bt
+                               // (the fused stages alternate between it and BV[tnew] plane 1)
     double* TD[2];             // FP32 form topography factors (null in the FP64 form)
     float* TF[2];
     float* TFX[2];

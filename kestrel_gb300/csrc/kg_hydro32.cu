@@ -187,6 +187,69 @@ __device__ __forceinline__ void face_flux32(const DevParams32& P, bool xdir, con
     out[6 * stride] = 0.5f * (dP2 + dM2);
 }
 
+// UpdateMaximum* on the state at the start of the step (src/TimeStepper.f90:519-524,
+// :1155-1303) for cell c of a slot, in the last pass of a step.
+__device__ __forceinline__ void update_maxima32(const DevArrays& A, const StepArgs& S, const StageTimes& Tm, const DevParams& P,
+                                                const DevParams32& F, int slot, int c) {
+    const int SC = P.nX * P.nY;
+    const double* q0p = A.Q[S.q_tc] + plane(slot, 4, 0, SC) + c;
+    const double* ct0 = A.CT[S.topo_tc] + plane(slot, 4, 0, SC) + c;
+    double btt = ct0[SC];
+    float bxt = (float)ct0[2 * (size_t)SC], byt = (float)ct0[3 * (size_t)SC];
+    float gamt = gam_of<float>(P.geo, bxt, byt);
+    float hpt = (float)((q0p[0] - ct0[0]) - btt);
+    float Hn, psi, rho, u, v;
+    const float* q0m = mom32(A.Q[S.q_tc], slot, SC);
+    desing32(F, hpt, gamt, q0m[c], q0m[SC + c], (float)q0p[3 * (size_t)SC], Hn, psi, rho, u, v);
+    double* M = A.MX + plane(slot, 11, 0, SC) + c;
+    double tt = Tm.t_max;
+    double Hnd = Hn, psid = psi;
+    if (Hnd > P.hThr) {
+        if (M[10 * (size_t)SC] == -1.0) M[10 * (size_t)SC] = tt;
+        if (Hnd > M[0]) { M[0] = Hnd; M[(size_t)SC] = tt; }
+    }
+    double spd = sqrtf(modu2_of<float>(P.geo, u, v, bxt, byt));
+    if ((spd > M[2 * (size_t)SC]) && (Hnd > P.hThr)) { M[2 * (size_t)SC] = spd; M[3 * (size_t)SC] = tt; }
+    if (btt < 0.0 && -btt > M[4 * (size_t)SC]) { M[4 * (size_t)SC] = -btt; M[5 * (size_t)SC] = tt; }
+    if (btt > 0.0 && btt > M[6 * (size_t)SC]) { M[6 * (size_t)SC] = btt; M[7 * (size_t)SC] = tt; }
+    if (Hnd > P.hThr && psid > M[8 * (size_t)SC]) { M[8 * (size_t)SC] = psid; M[9 * (size_t)SC] = tt; }
+}
+
+// A dry block's pass (see hydro32_block): the RHS stage writes a zero RHS, the RK stages
+// carry the block's input state (its own cells, as phase A loaded them) into their output
+// buffer, and the last stage also stores the velocities and updates the running maxima.
+__device__ __noinline__ void hydro32_dry_block(const DevArrays& A, const StepArgs& S, const StageTimes& Tm, const DevParams& P,
+                                                  const DevParams32& F, const BlockDesc bd, const Hydro32Smem& sm) {
+    const int nX = P.nX, SC = nX * P.nY;
+    const int bx = min(BS, nX - bd.x0), by = min(BS, P.nY - bd.y0);
+    const int tid = threadIdx.x, slot = bd.slot;
+    if (tid >= bx * by) return;
+    const int cx = tid % bx, cy = tid / bx, c = (bd.y0 + cy) * nX + (bd.x0 + cx);
+    const int r = (cy + 2) * RG + (cx + 2);
+    if (S.mode == MODE_RHS0) {
+        double* Ed = A.E[S.e_set] + plane(slot, 4, 0, SC) + c;
+        Ed[0] = 0.0;
+        Ed[3 * (size_t)SC] = 0.0;
+        float* Edm = mom32(A.E[S.e_set], slot, SC);
+        Edm[c] = 0.f;
+        Edm[SC + c] = 0.f;
+        imp32(A.I[S.e_set], slot, SC)[c] = 0.f;
+        return;
+    }
+    const int qo = S.mode == MODE_S1 ? S.q_s1 : S.mode == MODE_S2 ? S.q_s2 : S.q_out;
+    double* dst = A.Q[qo] + plane(slot, 4, 0, SC) + c;
+    dst[0] = sm.w[r];
+    dst[3 * (size_t)SC] = sm.p64[r];
+    float* dm = mom32(A.Q[qo], slot, SC);
+    dm[c] = sm.m1[r];
+    dm[SC + c] = sm.m2[r];
+    if (S.mode == MODE_S3) {
+        A.UV[plane(slot, 2, 0, SC) + c] = (double)sm.u[r];
+        A.UV[plane(slot, 2, 1, SC) + c] = (double)sm.v[r];
+        if (S.do_maxima) update_maxima32(A, S, Tm, P, F, slot, c);
+    }
+}
+
 // One BS x BS block of one tile through one pass (the body shared by the single-simulation
 // kernel, whose settings live in constant memory, and the batched kernel, whose settings
 // come from a per-simulation table).
@@ -209,6 +272,9 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
     const float dtf = (float)Tm.dt;
 
     // ---- A: load the cross-shaped region, FP64 depth, FP32 desingularisation ----
+    // `wet`: some region cell holds a depth, Hnpsi or momentum above F.dryEps (see below).
+    bool wet = false;
+    const float deps = F.dryEps;
     for (int r = tid; r < NR; r += NT) {
         int cx = r % RG - 2, cy = r / RG - 2;
         bool inX = (cy >= 0 && cy < by && cx >= -2 && cx < bx + 2);
@@ -235,6 +301,7 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             sm.v[r] = (float)A.G9[plane(s, 9, 6, SC) + c];
             sm.psi[r] = (float)A.G9[plane(s, 9, 7, SC) + c];
             sm.rho[r] = (float)A.G9[plane(s, 9, 8, SC) + c];
+            wet = wet || fabsf(sm.hp[r]) > deps || fabsf(sm.p[r]) > deps || fabsf(sm.m1[r]) > deps || fabsf(sm.m2[r]) > deps;
             continue;
         }
         double w, pp;
@@ -262,8 +329,21 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
         float Hn, psi, rho, u, v;
         desing32(F, hp, gam, m1, m2, (float)pp, Hn, psi, rho, u, v);
         sm.Hn[r] = Hn; sm.psi[r] = psi; sm.rho[r] = rho; sm.u[r] = u; sm.v[r] = v;
+        wet = wet || fabsf(hp) > deps || fabsf(sm.p[r]) > deps || fabsf(m1) > deps || fabsf(m2) > deps;
     }
-    __syncthreads();
+    // A dry block: no cell of the block or of its two-cell halo holds water (depth above
+    // the bed, Hnpsi and both momenta all within dryEps = 1e-4 heightThreshold) and the tile
+    // has no flux source.  Its faces then carry no flux beyond round-off of the bed
+    // interpolation (face depths of order 1e-13 m, momentum fluxes of order 1e-26), its
+    // closures are below the height threshold, and its cells' CFL terms exceed any dt, so
+    // the pass carries the block's state forward with a zero RHS instead of running the
+    // reconstruction, fluxes and RHS; the front of a flow is always at least two cells
+    // away from such a block, and a flow moves less than a cell per pass (CFL <= 1).
+    const bool src_tile = A.has_source[slot] != 0 && P.nSources >= 1;
+    if (!__syncthreads_or(wet || src_tile)) {
+        hydro32_dry_block(A, S, Tm, P, F, bd, sm);
+        return;
+    }
 
     // ---- B: limited slopes; reconstructed, corrected face-side depths of w in FP64 ----
     const int lim = P.limiter;
@@ -485,31 +565,7 @@ __device__ __forceinline__ void hydro32_block(const DevArrays& A, const StepArgs
             dst[3 * (size_t)SC] = sm.p64[r];
             A.UV[plane(slot, 2, 0, SC) + c] = (double)sm.u[r];
             A.UV[plane(slot, 2, 1, SC) + c] = (double)sm.v[r];
-            if (S.do_maxima) {
-                // UpdateMaximum* on the state at the start of the step
-                // (src/TimeStepper.f90:519-524, :1155-1303).
-                const double* q0p = A.Q[S.q_tc] + plane(slot, 4, 0, SC) + c;
-                const double* ct0 = A.CT[S.topo_tc] + plane(slot, 4, 0, SC) + c;
-                double btt = ct0[SC];
-                float bxt = (float)ct0[2 * (size_t)SC], byt = (float)ct0[3 * (size_t)SC];
-                float gamt = gam_of<float>(P.geo, bxt, byt);
-                float hpt = (float)((q0p[0] - ct0[0]) - btt);
-                float Hn, psi, rho, u, v;
-                const float* q0m = mom32(A.Q[S.q_tc], slot, SC);
-                desing32(F, hpt, gamt, q0m[c], q0m[SC + c], (float)q0p[3 * (size_t)SC], Hn, psi, rho, u, v);
-                double* M = A.MX + plane(slot, 11, 0, SC) + c;
-                double tt = Tm.t_max;
-                double Hnd = Hn, psid = psi;
-                if (Hnd > P.hThr) {
-                    if (M[10 * (size_t)SC] == -1.0) M[10 * (size_t)SC] = tt;
-                    if (Hnd > M[0]) { M[0] = Hnd; M[(size_t)SC] = tt; }
-                }
-                double spd = sqrtf(modu2_of<float>(P.geo, u, v, bxt, byt));
-                if ((spd > M[2 * (size_t)SC]) && (Hnd > P.hThr)) { M[2 * (size_t)SC] = spd; M[3 * (size_t)SC] = tt; }
-                if (btt < 0.0 && -btt > M[4 * (size_t)SC]) { M[4 * (size_t)SC] = -btt; M[5 * (size_t)SC] = tt; }
-                if (btt > 0.0 && btt > M[6 * (size_t)SC]) { M[6 * (size_t)SC] = btt; M[7 * (size_t)SC] = tt; }
-                if (Hnd > P.hThr && psid > M[8 * (size_t)SC]) { M[8 * (size_t)SC] = psid; M[9 * (size_t)SC] = tt; }
-            }
+            if (S.do_maxima) update_maxima32(A, S, Tm, P, F, slot, c);
         }
     }
 }

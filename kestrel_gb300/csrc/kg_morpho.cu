@@ -63,10 +63,12 @@ __device__ __forceinline__ double gam_nr(const DevParams& P, double bx, double b
 // per-member table.
 
 // Copy the step-start bed into the M set and fill the stage state of im0 (the state the
-// first hydraulic step produced).
-template <bool PLAIN>
+// first hydraulic step produced).  ALT (FP32 form, fused stages): the stage depth and the
+// six float stage planes go to their second copies, which the first fused stage reads.
+template <bool PLAIN, bool ALT = false>
 __device__ __forceinline__ void m_init(const DevParams& P, const DevParams32& F, const DevArrays& A, int s, int item_, int qa,
                                        int tcur, int tnew) {
+    constexpr int hn_plane = ALT ? 3 : 2, alt = ALT ? MF_ALT : 0;
     int SC = P.nX * P.nY, SV = (P.nX + 1) * (P.nY + 1);
     // b0 (vertex plane 0, cell plane 0) is static and both topography sets hold it: only
     // the bed change and the slopes are carried into the M set.
@@ -98,7 +100,7 @@ __device__ __forceinline__ void m_init(const DevParams& P, const DevParams32& F,
         M[(size_t)SC] = p;
         // FP32 form: the stage depth is kept unclamped (the dry test reads its sign bit as a
         // value below the threshold, and the tests read it as the new depth)
-        if (PLAIN) M[2 * (size_t)SC] = Hn;
+        if (PLAIN) M[hn_plane * (size_t)SC] = Hn;
         if (Hn < 0.0) Hn = 0.0;
         double pp = p < 0.0 ? 0.0 : p;
         if (!PLAIN) M[2 * (size_t)SC] = Hn;
@@ -108,12 +110,12 @@ __device__ __forceinline__ void m_init(const DevParams& P, const DevParams32& F,
             float psi = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, (float)e2)), (float)P.maxPack);
             // (the float slopes of the step-start bed are the factor cache's)
             mfp(A, s, MF_PSI0, SC)[c] = psi;
-            mfp(A, s, MF_HN, SC)[c] = Hf;
-            mfp(A, s, MF_PSI, SC)[c] = psi;
-            mfp(A, s, MF_RHO, SC)[c] = density<float>(F, psi);
-            mfp(A, s, MF_BT, SC)[c] = (float)ct[1];
-            mfp(A, s, MF_BX, SC)[c] = A.TF[tcur][mp(s, 6, 1, SC) + c];
-            mfp(A, s, MF_BY, SC)[c] = A.TF[tcur][mp(s, 6, 2, SC) + c];
+            mfp(A, s, MF_HN + alt, SC)[c] = Hf;
+            mfp(A, s, MF_PSI + alt, SC)[c] = psi;
+            mfp(A, s, MF_RHO + alt, SC)[c] = density<float>(F, psi);
+            mfp(A, s, MF_BT + alt, SC)[c] = (float)ct[1];
+            mfp(A, s, MF_BX + alt, SC)[c] = A.TF[tcur][mp(s, 6, 1, SC) + c];
+            mfp(A, s, MF_BY + alt, SC)[c] = A.TF[tcur][mp(s, 6, 2, SC) + c];
         } else {
             double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
             M[3 * (size_t)SC] = psi;
@@ -126,6 +128,88 @@ __device__ __forceinline__ void m_init(const DevParams& P, const DevParams32& F,
 // ghost tiles from their static data.
 __device__ __forceinline__ double stage_hn(const DevArrays& A, int s, int c, int SC) {
     return A.kind[s] == SLOT_GHOST ? A.G9[mp(s, 9, 4, SC) + c] : A.MS[mp(s, 5, 2, SC) + c];
+}
+
+// FP32 form, shared by the per-item bodies and the fused stage (k_m_stage32), so both form
+// every value with the same operations.  emd32: E - D of a wet cell (t, c) from its float
+// stage planes (plane + off: the first or second copy) and slopes dbx, dby.
+__device__ __forceinline__ float emd32(const DevParams& P, const DevParams32& F, const DevArrays& A, int t, int c, int SC,
+                                       int off, float dbx, float dby) {
+    Pt<float> pt{mfp(A, t, MF_HN + off, SC)[c], (float)A.UV[mp(t, 2, 0, SC) + c], (float)A.UV[mp(t, 2, 1, SC) + c],
+                 mfp(A, t, MF_PSI + off, SC)[c], mfp(A, t, MF_RHO + off, SC)[c], mfp(A, t, MF_BT + off, SC)[c], dbx, dby,
+                 gam_of<float>(P.geo, dbx, dby)};
+    return erosion_minus_deposition<float>(F, pt);
+}
+// d(bt)/dt at a vertex from the E - D and slopes of its four cells (south-west, north-west,
+// south-east, north-east), summed pairwise in FP32; the slopes only matter where E - D is
+// non-zero around the vertex.
+__device__ __forceinline__ float ddt32_vertex(const DevParams& P, const float ef[4], const float xf[4], const float yf[4]) {
+    float kef = (ef[0] + ef[1]) + (ef[2] + ef[3]);
+    if (kef == 0.f) return 0.f;
+    float gx = 0.25f * ((xf[0] + xf[1]) + (xf[2] + xf[3])), gy = 0.25f * ((yf[0] + yf[1]) + (yf[2] + yf[3]));
+    float gam = P.geo ? sqrtf(1.f + gx * gx + gy * gy) : 1.f;
+    return -0.25f * gam * kef * (float)P.invSolid;
+}
+// The clamped stage update of a vertex's bt: the rate in FP32 (its E - D terms come from
+// FP32 closures), the update as bt0 + a (bt_k - bt0 + dt ddt) in FP64, so a vertex with no
+// erosion or deposition around it keeps its bed exactly.
+__device__ __forceinline__ double bt32_stage(const DevParams& P, int stage, double bt0, double btp, double dt, float ddt32) {
+    // No E - D around the vertex and no change in the earlier stages: every stage formula
+    // gives bt0 + 0 (taken on the integer pipe: only -0 becomes +0).
+    if (ddt32 == 0.f && (stage == 1 || same_bits(btp, bt0)))
+        return mx(-P.EroDepth, same_bits(bt0, -0.0) ? 0.0 : bt0);
+    double inc = (btp - bt0) + dt * (double)ddt32;
+    double nb;
+    if (stage == 1) nb = bt0 + dt * (double)ddt32;
+    else if (stage == 2) nb = bt0 + 0.25 * inc;
+    else nb = bt0 + (2.0 / 3.0) * inc;
+    return mx(-P.EroDepth, nb);
+}
+// Cell c of slot s from its four new vertex bt values: the cell bed (static b0 parts from
+// the cache, bt terms summed pairwise, differences first), the conservative w / Hnpsi
+// update from the attempt's step-start cache with 1/gamma from an FP32-seeded Newton step,
+// and the stage's depth (kept unclamped in MS plane hn_plane) and float closure inputs
+// (planes + off).
+__device__ __forceinline__ void cell32_update(const DevParams& P, const DevParams32& F, const DevArrays& A, int s, int c, int tcur,
+                                              int tnew, double b00, double b10, double b01, double b11, int hn_plane, int off) {
+    const int SC = P.nX * P.nY;
+    const double psib = 1.0 - P.BedPorosity;
+    // b0 is static: the cell b0 (the compensated sum of the set-up) and the b0 parts of the
+    // slopes come from the cache; only the bt terms are summed here.
+    double b0c = A.CT[tcur][mp(s, 4, 0, SC) + c];
+    const double* B = A.B0S + mp(s, 2, 0, SC) + c;
+    double btc = 0.25 * ((b00 + b10) + (b01 + b11));
+    double dbx = B[0] + P.hdxR * ((b10 - b00) + (b11 - b01));
+    double dby = B[(size_t)SC] + P.hdyR * ((b01 - b00) + (b11 - b10));
+    A.CT[tnew][mp(s, 4, 1, SC) + c] = btc;
+    A.CT[tnew][mp(s, 4, 2, SC) + c] = dbx;
+    A.CT[tnew][mp(s, 4, 3, SC) + c] = dby;
+    double gamnew = 1.0, ign = 1.0;
+    if (P.geo) {
+        double g2 = 1.0 + (dbx * dbx + dby * dby);
+        ign = rsqrt_nr(g2);
+        gamnew = g2 * ign;
+    }
+    double db = btc - A.CT[tcur][mp(s, 4, 1, SC) + c];
+    // Hn gam and Hnpsi gam of the step start from the attempt's cache (m_init)
+    const double* Z = A.M0 + mp(s, 3, 0, SC) + c;
+    double w = (b0c + btc) + (Z[(size_t)SC] - db) * (ign * ign);
+    double Hnpsi = (Z[2 * (size_t)SC] - psib * db) * ign;
+    double Hn = ((w - b0c) - btc) * gamnew;
+    double* M = A.MS + mp(s, 5, 0, SC) + c;
+    M[0] = w;
+    M[(size_t)SC] = Hnpsi;
+    M[hn_plane * (size_t)SC] = Hn;  // unclamped (as m_init)
+    if (Hn < 0.0) Hn = 0.0;
+    float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi;
+    float psif = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, F.hThr2)), F.maxPack);
+    // the stage's inputs of the FP32 closures and of the vertex source, in float
+    mfp(A, s, MF_HN + off, SC)[c] = Hf;
+    mfp(A, s, MF_PSI + off, SC)[c] = psif;
+    mfp(A, s, MF_RHO + off, SC)[c] = density<float>(F, psif);
+    mfp(A, s, MF_BT + off, SC)[c] = (float)btc;
+    mfp(A, s, MF_BX + off, SC)[c] = (float)dbx;
+    mfp(A, s, MF_BY + off, SC)[c] = (float)dby;
 }
 
 // R = double: the FP64 drop-in; R = float: the FP32 form's closures (the depth test and
@@ -153,13 +237,7 @@ __device__ __forceinline__ void m_emd(const DevParams& P, const DevParams32& F, 
         if constexpr (sizeof(R) == sizeof(float)) {
             // the FP32 form: the stage's closure inputs from the float planes, E - D kept in float
             float e = 0.f;
-            if (!dry) {
-                float dbx = mfp(A, s, MF_BX, SC)[c], dby = mfp(A, s, MF_BY, SC)[c];
-                Pt<float> pt{mfp(A, s, MF_HN, SC)[c], (float)A.UV[mp(s, 2, 0, SC) + c], (float)A.UV[mp(s, 2, 1, SC) + c],
-                             mfp(A, s, MF_PSI, SC)[c], mfp(A, s, MF_RHO, SC)[c], mfp(A, s, MF_BT, SC)[c], dbx, dby,
-                             gam_of<float>(P.geo, dbx, dby)};
-                e = erosion_minus_deposition<float>(F, pt);
-            }
+            if (!dry) e = emd32(P, F, A, s, c, SC, 0, mfp(A, s, MF_BX, SC)[c], mfp(A, s, MF_BY, SC)[c]);
             mfp(A, s, MF_EMD, SC)[c] = e;
         } else {
             if (!dry) {
@@ -251,13 +329,10 @@ __device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int
         float ddt32 = 0.f;
         if (PLAIN) {
             // FP32 form: the four cells' E - D and slopes from the float stage planes (a ghost
-            // cell's E - D is zero and its slopes are the step-start factor cache's), summed
-            // in FP32; the slopes only matter where E - D is non-zero around the vertex.
-            float ef[4];
+            // cell's E - D is zero and its slopes are the step-start factor cache's).
+            float ef[4], xf[4] = {0.f, 0.f, 0.f, 0.f}, yf[4] = {0.f, 0.f, 0.f, 0.f};
             for (int q = 0; q < 4; ++q) ef[q] = cs[q] < 0 ? 0.f : mfp(A, cs[q], MF_EMD, SC)[cj[q] * nX + ci[q]];
-            float kef = (ef[0] + ef[1]) + (ef[2] + ef[3]);
-            if (kef != 0.f) {
-                float xf[4], yf[4];
+            if ((ef[0] + ef[1]) + (ef[2] + ef[3]) != 0.f) {
                 for (int q = 0; q < 4; ++q) {
                     int cc = cj[q] * nX + ci[q];
                     if (cs[q] < 0) {
@@ -271,10 +346,8 @@ __device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int
                         yf[q] = A.TF[tcur][mp(cs[q], 6, 2, SC) + cc];
                     }
                 }
-                float gx = 0.25f * ((xf[0] + xf[1]) + (xf[2] + xf[3])), gy = 0.25f * ((yf[0] + yf[1]) + (yf[2] + yf[3]));
-                float gam = P.geo ? sqrtf(1.f + gx * gx + gy * gy) : 1.f;
-                ddt32 = -0.25f * gam * kef * (float)P.invSolid;
             }
+            ddt32 = ddt32_vertex(P, ef, xf, yf);
         } else {
             for (int q = 0; q < 4; ++q) e[q] = cellv(A, CT, cs[q], -1, ci[q], cj[q], nX, SC);
             for (int q = 0; q < 4; ++q) {
@@ -289,13 +362,8 @@ __device__ __forceinline__ void m_bt(const DevParams& P, const DevArrays& A, int
         double btp = A.BV[tnew][mp(s, 2, 1, SV) + v];
         double nb;
         if (PLAIN) {
-            // FP32 form: the rate in FP32 (its E - D terms come from FP32 closures), the
-            // stage update as bt0 + a (bt_k - bt0 + dt ddt) in FP64, so a vertex with no
-            // erosion or deposition around it keeps its bed exactly.
-            double inc = (btp - bt0) + dt * (double)ddt32;
-            if (stage == 1) nb = bt0 + dt * (double)ddt32;
-            else if (stage == 2) nb = bt0 + 0.25 * inc;
-            else nb = bt0 + (2.0 / 3.0) * inc;
+            A.BV[tnew][mp(s, 2, 1, SV) + v] = bt32_stage(P, stage, bt0, btp, dt, ddt32);
+            return;
         } else {
             double gam = gam_of(P.geo, 0.25 * kx, 0.25 * ky);
             double ddt = -0.25 * gam / psib * ke;
@@ -331,78 +399,36 @@ __device__ __forceinline__ void m_cells(const DevParams& P, const DevParams32& F
                 same_bits(C3[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 2, SC) + c]) && same_bits(C3[mp(s, 4, 3, SC) + c], C0[mp(s, 4, 3, SC) + c]))
                 return;
         }
-        double b0c, btc, dbx, dby;
         if (PLAIN) {
-            // b0 is static: the cell b0 (the compensated sum of the set-up) and the b0 parts
-            // of the slopes come from the cache; only the bt terms are summed here.
-            b0c = A.CT[tcur][mp(s, 4, 0, SC) + c];
-            const double* B = A.B0S + mp(s, 2, 0, SC) + c;
-            btc = 0.25 * ((bt[v00] + bt[v10]) + (bt[v01] + bt[v11]));
-            dbx = B[0] + P.hdxR * ((bt[v10] - bt[v00]) + (bt[v11] - bt[v01]));
-            dby = B[(size_t)SC] + P.hdyR * ((bt[v01] - bt[v00]) + (bt[v11] - bt[v10]));
-        } else {
-            b0c = 0.25 * kahan4(b0[v00], b0[v10], b0[v01], b0[v11]);
-            btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
-            double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
-            double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
-            dbx = 0.5 * P.dxR * kahan8(ax);
-            dby = 0.5 * P.dyR * kahan8(ay);
+            cell32_update(P, F, A, s, c, tcur, tnew, bt[v00], bt[v10], bt[v01], bt[v11], 2, 0);
+            return;
         }
-        if (!PLAIN) A.CT[tnew][mp(s, 4, 0, SC) + c] = b0c;
+        double b0c = 0.25 * kahan4(b0[v00], b0[v10], b0[v01], b0[v11]);
+        double btc = 0.25 * kahan4(bt[v00], bt[v10], bt[v01], bt[v11]);
+        double ax[8] = {b0[v10], bt[v10], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v01], -bt[v01]};
+        double ay[8] = {b0[v01], bt[v01], -b0[v00], -bt[v00], b0[v11], bt[v11], -b0[v10], -bt[v10]};
+        double dbx = 0.5 * P.dxR * kahan8(ax);
+        double dby = 0.5 * P.dyR * kahan8(ay);
+        A.CT[tnew][mp(s, 4, 0, SC) + c] = b0c;
         A.CT[tnew][mp(s, 4, 1, SC) + c] = btc;
         A.CT[tnew][mp(s, 4, 2, SC) + c] = dbx;
         A.CT[tnew][mp(s, 4, 3, SC) + c] = dby;
         const double* C0 = A.CT[tcur];
-        double gamold = 1.0, gamnew, ign = 1.0;
-        if (PLAIN) {
-            if (P.geo) {
-                double g2 = 1.0 + (dbx * dbx + dby * dby);
-                ign = rsqrt_nr(g2);
-                gamnew = g2 * ign;
-            } else {
-                gamnew = 1.0;
-            }
-        } else {
-            gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
-            gamnew = gam_of(P.geo, dbx, dby);
-        }
+        double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
+        double gamnew = gam_of(P.geo, dbx, dby);
         double db = btc - C0[mp(s, 4, 1, SC) + c];
-        double w, Hnpsi, Hn, psi;
-        if (PLAIN) {
-            // Hn gam and Hnpsi gam of the step start from the attempt's cache (m_init)
-            const double* Z = A.M0 + mp(s, 3, 0, SC) + c;
-            w = (b0c + btc) + (Z[(size_t)SC] - db) * (ign * ign);
-            Hnpsi = (Z[2 * (size_t)SC] - psib * db) * ign;
-            Hn = ((w - b0c) - btc) * gamnew;
-            double* M = A.MS + mp(s, 5, 0, SC) + c;
-            M[0] = w;
-            M[(size_t)SC] = Hnpsi;
-            M[2 * (size_t)SC] = Hn;  // unclamped (as m_init)
-            if (Hn < 0.0) Hn = 0.0;
-            float Hf = (float)Hn, pf = Hnpsi < 0.0 ? 0.f : (float)Hnpsi;
-            float psif = fminf(2.f * Hf * pf / (Hf * Hf + fmaxf(Hf * Hf, F.hThr2)), F.maxPack);
-            // the stage's inputs of the FP32 closures and of the vertex source, in float
-            mfp(A, s, MF_HN, SC)[c] = Hf;
-            mfp(A, s, MF_PSI, SC)[c] = psif;
-            mfp(A, s, MF_RHO, SC)[c] = density<float>(F, psif);
-            mfp(A, s, MF_BT, SC)[c] = (float)btc;
-            mfp(A, s, MF_BX, SC)[c] = (float)dbx;
-            mfp(A, s, MF_BY, SC)[c] = (float)dby;
-            return;
-        } else {
-            double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
-            double Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
-            w = -db / gamnew / gamnew;
-            w = w + btc;
-            w = w + Hn_old * gamold / gamnew / gamnew;
-            w = w + b0c;
-            Hnpsi = -(psib)*db / gamnew;
-            Hnpsi = Hnpsi + p0 * gamold / gamnew;
-            Hn = compute_hn(w, b0c, btc, gamnew);
-            if (Hn < 0.0) Hn = 0.0;
-            double pp = Hnpsi < 0.0 ? 0.0 : Hnpsi;
-            psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
-        }
+        double w0 = A.Q[qa][mp(s, 4, 0, SC) + c], p0 = A.Q[qa][mp(s, 4, 3, SC) + c];
+        double Hn_old = compute_hn(w0, C0[mp(s, 4, 0, SC) + c], C0[mp(s, 4, 1, SC) + c], gamold);
+        double w = -db / gamnew / gamnew;
+        w = w + btc;
+        w = w + Hn_old * gamold / gamnew / gamnew;
+        w = w + b0c;
+        double Hnpsi = -(psib)*db / gamnew;
+        Hnpsi = Hnpsi + p0 * gamold / gamnew;
+        double Hn = compute_hn(w, b0c, btc, gamnew);
+        if (Hn < 0.0) Hn = 0.0;
+        double pp = Hnpsi < 0.0 ? 0.0 : Hnpsi;
+        double psi = mn(2.0 * Hn * pp / (Hn * Hn + mx(Hn * Hn, e2)), P.maxPack);
         double* M = A.MS + mp(s, 5, 0, SC) + c;
         M[0] = w;
         M[(size_t)SC] = Hnpsi;
@@ -782,13 +808,13 @@ __device__ __forceinline__ void m_finish(const DevParams& P, const DevArrays& A,
     (void)pos;
 
 // ctl_flags[0..1]: the M refine flag and the candidate count, zeroed here for k_m_check.
-template <bool PLAIN>
+template <bool PLAIN, bool ALT = false>
 __global__ void __launch_bounds__(256) k_m_init(DevArrays A, const int* __restrict__ slots, int qa, int tcur, int tnew,
                                                 int* ctl_flags) {
     kg_dep_wait();
     if (blockIdx.x == 0 && threadIdx.x < 2) ctl_flags[threadIdx.x] = 0;
     KG_TILE_ITEMS((cP.nX + 1) * (cP.nY + 1))
-    m_init<PLAIN>(cP, cP32, A, s, item_, qa, tcur, tnew);
+    m_init<PLAIN, ALT>(cP, cP32, A, s, item_, qa, tcur, tnew);
 }
 template <class R>
 __global__ void __launch_bounds__(256) k_m_emd(DevArrays A, const int* __restrict__ slots, int tnew) {
@@ -880,6 +906,146 @@ __global__ void __launch_bounds__(256) k_m_close(DevArrays A, const int* __restr
     m_close<PLAIN>(cP, A, slots[blockIdx.x / per], (blockIdx.x % per) * 256 + threadIdx.x, qa, tnew);
 }
 
+// ---- FP32 form: one launch per M stage (single simulation) ----
+// k_m_stage32<STAGE> runs a whole stage of M for one MSB x MSB block of cells of an active
+// tile, in place of the k_m_emd / k_m_bt / k_m_cells launches:
+//   0. the dry test of every cell within two cells of the block (the stage depth below the
+//      height threshold; ghost tiles from their static data, tiles never allocated dry);
+//   1. E - D (as m_emd) and the slopes of the block's cells and of the ring of cells around
+//      it, whichever of the eight neighbouring tiles they lie in (zero E - D outside active
+//      tiles, as the vertex source reads it);
+//   2. the vertex source and the clamped bed update (as m_bt) of the block's
+//      (MSB + 1)^2 vertices from those values in shared memory;
+//   3. the cell bed, the w / Hnpsi update and the stage variables (cell32_update) of the
+//      block's own cells from the new vertices in shared memory;
+//   4. after the third stage, the refinement tests (m_check) of its own cells.
+// The shared helpers form every value with the same operations on the same operands, so the
+// stages equal the three per-item launches (which the batched engine runs) bit for bit.
+// Each block reads the stage variables of cells that other blocks write in the same launch,
+// so those alternate between two copies from stage to stage: the stage depth (MS plane 2 /
+// 3), the six float stage planes (MF_HN.. / MF_AHN..) and the vertex bt (BV[tnew] plane 1 /
+// BVA).  m_init<true, true> fills the second copies; stages 1 and 3 read the second copies
+// and write the first, stage 2 the reverse, so the M result ends in the first copies, where
+// the tests, the redistribution walk and the closing launch read it (the vertex bt: stage 1
+// writes BV[tnew], stage 2 BVA, stage 3 BV[tnew]).  A cell whose bed did not change carries
+// its stage variables forward into the copy being written.
+constexpr int MSB = 16;
+struct MStageSmem {
+    unsigned char dry[MSB + 4][MSB + 4];
+    float ef[MSB + 2][MSB + 2], xf[MSB + 2][MSB + 2], yf[MSB + 2][MSB + 2];
+    double bt[MSB + 1][MSB + 1], bt0[MSB + 1][MSB + 1];
+};
+
+// Slot (-1: a tile never allocated) and cell index of tile-local cell (i, j) of tile s, which
+// may lie in one of the eight tiles around s: the column's tile (W / E) first, then its south
+// or north neighbour, as the vertex source and the redistribution walk reach corner tiles.
+// |i| and |j| stay within one tile of s (tiles of at least 2 x 2 cells).
+__device__ __forceinline__ int stage_cell_slot(const DevArrays& A, int s, int sW, int sE, int nX, int nY, int i, int j, int& c) {
+    int col = s;
+    if (i < 0) { col = sW; i += nX; }
+    else if (i >= nX) { col = sE; i -= nX; }
+    int t = col;
+    if (j < 0) { t = col < 0 ? -1 : A.nbr[col * 8 + NB_S]; j += nY; }
+    else if (j >= nY) { t = col < 0 ? -1 : A.nbr[col * 8 + NB_N]; j -= nY; }
+    c = j * nX + i;
+    return t;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256) k_m_stage32(DevArrays A, const int* __restrict__ slots, int nbt, int qa, int tcur, int tnew,
+                                                   double dt_m, const double* __restrict__ dtp, int* flags,
+                                                   unsigned long long* cand_key, double* cand_ex, int* ncand, int cand_cap) {
+    kg_dep_wait();
+    __shared__ MStageSmem sm;
+    const DevParams& P = cP;
+    const int nX = P.nX, nY = P.nY, SC = nX * nY, SV = (nX + 1) * (nY + 1);
+    const int pos = blockIdx.x / nbt, blk = blockIdx.x % nbt, nbx = (nX + MSB - 1) / MSB;
+    const int x0 = (blk % nbx) * MSB, y0 = (blk / nbx) * MSB;
+    const int bx = min(MSB, nX - x0), by = min(MSB, nY - y0);
+    const int s = slots[pos];
+    const int sW = A.nbr[s * 8 + NB_W], sE = A.nbr[s * 8 + NB_E];
+    const int tid = threadIdx.x;
+    // stages 1 and 3 read the second copies and write the first; stage 2 the reverse
+    constexpr bool RD_ALT = STAGE != 2;
+    constexpr int hn_rd = RD_ALT ? 3 : 2, hn_wr = RD_ALT ? 2 : 3;
+    constexpr int mf_rd = RD_ALT ? MF_ALT : 0, mf_wr = RD_ALT ? 0 : MF_ALT;
+    double* bt_rd = STAGE == 2 ? A.BV[tnew] + mp(s, 2, 1, SV) : A.BVA + (size_t)s * SV;
+    double* bt_wr = STAGE == 2 ? A.BVA + (size_t)s * SV : A.BV[tnew] + mp(s, 2, 1, SV);
+
+    // 0. dry flags of the (bx + 4) x (by + 4) box around the block
+    for (int k = tid; k < (bx + 4) * (by + 4); k += blockDim.x) {
+        const int cx = k % (bx + 4) - 2, cy = k / (bx + 4) - 2;
+        int c;
+        const int t = stage_cell_slot(A, s, sW, sE, nX, nY, x0 + cx, y0 + cy, c);
+        bool dry = true;
+        if (t >= 0) dry = below_pos(A.kind[t] == SLOT_GHOST ? A.G9[mp(t, 9, 4, SC) + c] : A.MS[mp(t, 5, hn_rd, SC) + c], P.hThr);
+        sm.dry[cy + 2][cx + 2] = dry;
+    }
+    __syncthreads();
+    // 1. E - D and slopes of the block's cells and the ring around them
+    for (int k = tid; k < (bx + 2) * (by + 2); k += blockDim.x) {
+        const int cx = k % (bx + 2) - 1, cy = k / (bx + 2) - 1;
+        int c;
+        const int t = stage_cell_slot(A, s, sW, sE, nX, nY, x0 + cx, y0 + cy, c);
+        float ef = 0.f, xf = 0.f, yf = 0.f;
+        if (t >= 0 && A.kind[t] == SLOT_ACTIVE) {
+            xf = mfp(A, t, MF_BX + mf_rd, SC)[c];
+            yf = mfp(A, t, MF_BY + mf_rd, SC)[c];
+            const int X = cx + 2, Y = cy + 2;
+            if (!(sm.dry[Y][X] || sm.dry[Y][X - 1] || sm.dry[Y][X + 1] || sm.dry[Y - 1][X] || sm.dry[Y + 1][X]))
+                ef = emd32(P, cP32, A, t, c, SC, mf_rd, xf, yf);
+        } else if (t >= 0) {
+            xf = A.TF[tcur][mp(t, 6, 1, SC) + c];
+            yf = A.TF[tcur][mp(t, 6, 2, SC) + c];
+        }
+        sm.ef[cy + 1][cx + 1] = ef;
+        sm.xf[cy + 1][cx + 1] = xf;
+        sm.yf[cy + 1][cx + 1] = yf;
+    }
+    __syncthreads();
+    // 2. the block's vertices: cells south-west, north-west, south-east, north-east of each
+    const double dt = dtp ? 2.0 * dtp[0] : dt_m;
+    for (int k = tid; k < (bx + 1) * (by + 1); k += blockDim.x) {
+        const int a = k % (bx + 1), b = k / (bx + 1);
+        const float ef[4] = {sm.ef[b][a], sm.ef[b + 1][a], sm.ef[b][a + 1], sm.ef[b + 1][a + 1]};
+        const float xf[4] = {sm.xf[b][a], sm.xf[b + 1][a], sm.xf[b][a + 1], sm.xf[b + 1][a + 1]};
+        const float yf[4] = {sm.yf[b][a], sm.yf[b + 1][a], sm.yf[b][a + 1], sm.yf[b + 1][a + 1]};
+        const int v = (y0 + b) * (nX + 1) + (x0 + a);
+        const double bt0 = A.BV[tcur][mp(s, 2, 1, SV) + v];
+        const double btp = STAGE == 1 ? bt0 : bt_rd[v];
+        const double nb = bt32_stage(P, STAGE, bt0, btp, dt, ddt32_vertex(P, ef, xf, yf));
+        bt_wr[v] = nb;
+        sm.bt[b][a] = nb;
+        sm.bt0[b][a] = bt0;
+    }
+    __syncthreads();
+    // 3. the block's own cells
+    if (tid < bx * by) {
+        const int cx = tid % bx, cy = tid / bx, c = (y0 + cy) * nX + (x0 + cx);
+        const double b00 = sm.bt[cy][cx], b10 = sm.bt[cy][cx + 1], b01 = sm.bt[cy + 1][cx], b11 = sm.bt[cy + 1][cx + 1];
+        const double *C0 = A.CT[tcur], *C3 = A.CT[tnew];
+        if (same_bits(b00, sm.bt0[cy][cx]) && same_bits(b10, sm.bt0[cy][cx + 1]) && same_bits(b01, sm.bt0[cy + 1][cx]) &&
+            same_bits(b11, sm.bt0[cy + 1][cx + 1]) && same_bits(C3[mp(s, 4, 1, SC) + c], C0[mp(s, 4, 1, SC) + c]) &&
+            same_bits(C3[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 2, SC) + c]) && same_bits(C3[mp(s, 4, 3, SC) + c], C0[mp(s, 4, 3, SC) + c])) {
+            // bed unchanged: the stage state carries forward
+            A.MS[mp(s, 5, hn_wr, SC) + c] = A.MS[mp(s, 5, hn_rd, SC) + c];
+#pragma unroll
+            for (int f = MF_HN; f <= MF_BY; ++f) mfp(A, s, f + mf_wr, SC)[c] = mfp(A, s, f + mf_rd, SC)[c];
+        } else {
+            cell32_update(P, cP32, A, s, c, tcur, tnew, b00, b10, b01, b11, hn_wr, mf_wr);
+        }
+        // 4. the refinement tests after the last stage (the cell's own values, written above)
+        if (STAGE == 3) m_check<true>(P, A, s, c, pos, qa, tcur, tnew, flags, cand_key, cand_ex, ncand, cand_cap);
+    }
+}
+
+// Blocks of the fused stage per tile; 0 when the tiles are too small for its two-cell halo
+// (the three per-item launches run then).
+int m_stage32_blocks(int nX, int nY) {
+    if (nX < 2 || nY < 2) return 0;
+    return ((nX + MSB - 1) / MSB) * ((nY + MSB - 1) / MSB);
+}
+
 // ---- host launchers (cells/verts: items per tile) ----
 static inline int per_of(int items) { return (items + 255) / 256; }
 
@@ -888,6 +1054,20 @@ cudaError_t launch_m_init(const DevArrays& A, const int* d_slots, int n, int ver
     if (n <= 0) return cudaSuccess;
     if (fp32) KG_TRY_LAUNCH(kg_launch(k_m_init<true>, n * per_of(verts), 256, 0, st, A, d_slots, qa, tcur, tnew, ctl_flags));
     else KG_TRY_LAUNCH(kg_launch(k_m_init<false>, n * per_of(verts), 256, 0, st, A, d_slots, qa, tcur, tnew, ctl_flags));
+    return cudaGetLastError();
+}
+// The FP32 form's fused M attempt up to its tests: init into the second copies of the stage
+// planes, then one k_m_stage32 launch per stage (the third runs the tests).
+cudaError_t launch_m_fused32(const DevArrays& A, const int* d_slots, int n, int nX, int nY, int qa, int tcur, int tnew,
+                             double dt_m, const double* dtp, int* ctl_flags, unsigned long long* keys, double* ex, int* ncand,
+                             int cap, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int nbt = m_stage32_blocks(nX, nY);
+    if (nbt <= 0) return cudaErrorInvalidValue;
+    KG_TRY_LAUNCH(kg_launch(k_m_init<true, true>, n * per_of((nX + 1) * (nY + 1)), 256, 0, st, A, d_slots, qa, tcur, tnew, ctl_flags));
+    KG_TRY_LAUNCH(kg_launch(k_m_stage32<1>, n * nbt, 256, 0, st, A, d_slots, nbt, qa, tcur, tnew, dt_m, dtp, ctl_flags, keys, ex, ncand, cap));
+    KG_TRY_LAUNCH(kg_launch(k_m_stage32<2>, n * nbt, 256, 0, st, A, d_slots, nbt, qa, tcur, tnew, dt_m, dtp, ctl_flags, keys, ex, ncand, cap));
+    KG_TRY_LAUNCH(kg_launch(k_m_stage32<3>, n * nbt, 256, 0, st, A, d_slots, nbt, qa, tcur, tnew, dt_m, dtp, ctl_flags, keys, ex, ncand, cap));
     return cudaGetLastError();
 }
 cudaError_t launch_m_emd(const DevArrays& A, const int* d_slots, int n, int cells, int tnew, bool fp32, cudaStream_t st) {

@@ -32,6 +32,7 @@ struct DevParams {
     double cfl, maxdt, diffusiveTimeScale;
     double invSolid;  // 1 / (1 - BedPorosity), for the FP32 form's multiplications
     double hdxR, hdyR;  // 0.5 / dx, 0.5 / dy
+    int no_dry_skip;    // FP32 form: run every block of a pass in full (kg_set_dry_skip(ctx, 0))
 };
 
 // The same settings in FP32 for the FP32 form's arithmetic (a conversion from FP64 is an
@@ -52,6 +53,7 @@ struct DevParams32 {
 #undef KG_F
 #undef KG_I
     float hThr2;
+    float dryEps;  // FP32 form: depth, Hnpsi and momentum magnitude below which a block counts as dry
 };
 inline DevParams32 params32(const DevParams& d) {
     DevParams32 f{};
@@ -62,6 +64,7 @@ inline DevParams32 params32(const DevParams& d) {
 #undef KG_F
 #undef KG_I
     f.hThr2 = (float)(d.hThr * d.hThr);
+    f.dryEps = d.no_dry_skip ? -1.f : (float)(1e-4 * d.hThr);  // -1: no block counts as dry
     return f;
 }
 

@@ -31,6 +31,10 @@ def load(auto_build: bool = True):
     lib.kg_stream.restype = C.c_void_p
     lib.kg_set_kernel_timing.argtypes = [C.c_void_p, C.c_int32]
     lib.kg_set_kernel_timing.restype = C.c_int
+    lib.kg_set_fused_morpho.argtypes = [C.c_void_p, C.c_int32]
+    lib.kg_set_fused_morpho.restype = C.c_int
+    lib.kg_set_dry_skip.argtypes = [C.c_void_p, C.c_int32]
+    lib.kg_set_dry_skip.restype = C.c_int
     lib.kg_get_kernel_time.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     lib.kg_get_kernel_time.restype = C.c_int
     lib.kg_get_counters.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]

@@ -68,9 +68,10 @@ class Server:
         self.clock = clock
         self.keep_state = keep_state
 
-    def run(self, requests: list[Request]) -> dict:
+    def run(self, requests: list[Request], max_wall_s: float | None = None) -> dict:
         """Serve the requests (arrival times in seconds from now) to completion; returns the
-        report (latencies, throughput, occupancy)."""
+        report (latencies, throughput, occupancy).  With max_wall_s, raises TimeoutError
+        once the stream has taken that long."""
         b, L = self.batch, self.batch.L
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         queue: collections.deque = collections.deque()
@@ -100,6 +101,9 @@ class Server:
                 if pending:
                     time.sleep(max(0.0, min(pending[0].arrival - (self.clock() - t0), 0.05)))
                 continue
+            if max_wall_s is not None and self.clock() - t0 > max_wall_s:
+                raise TimeoutError(f"{len(running) + len(queue) + len(pending)} of {len(requests)} requests unfinished "
+                                   f"after {max_wall_s:.0f} s")
             b.step()
             steps += 1
             occupancy.append(len(running))

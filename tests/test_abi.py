@@ -197,7 +197,8 @@ def test_slot_bytes_follow_the_layout(nx, ny):
                + 2 * SC)                                    # source-override Hn and rho
     ints = 8 + 1                                            # nbr[8], tile_of_slot
     fp32 = (2 * (3 * SC * 8 + 6 * SC * 4 + 2 * (SFX + SFY) * 4)  # TD, TF, TFX, TFY: two sets
-            + 3 * SC * 8 + 8 * SC * 4)                           # M0, MF: the M attempt's step start and stage
+            + 3 * SC * 8 + 14 * SC * 4                           # M0, MF: the M attempt's step start and stage
+            + SV * 8)                                            # BVA: the second copy of the vertex bt
     base = 8 * doubles + 4 * ints + 2                       # + kind, has_source bytes
     assert L.kg_slot_bytes(nx, ny, abi.PREC_FP64) == base
     assert L.kg_slot_bytes(nx, ny, abi.PREC_FP32) == base + fp32

@@ -169,3 +169,76 @@ def test_fp32_state_round_trip():
     g.set_field(tile, 2, new)
     assert np.array_equal(g.field(tile, 2), new)
     assert np.array_equal(g.field(tile, 3), m2) and np.array_equal(g.field(tile, 1), w0)
+
+
+def _fused_case(name):
+    from kestrel_gb300 import config, workloads
+    if name == "periodic_morpho":
+        import test_gpu_edges
+        return config.parse(test_gpu_edges.PERIODIC_MORPHO).params, None
+    if name == "window":
+        return workloads.morpho_flux_window(tend=3.0)
+    return cases.ref_input(name, tend={"cap_morpho_2d": 1.0, "flux_morpho_2d": 2.0}[name], nout=1), None
+
+
+@pytest.mark.parametrize("name", ["cap_morpho_2d", "flux_morpho_2d", "periodic_morpho", "window"])
+def test_fp32_fused_morpho_stages_match_three_launches(name):
+    """The FP32 form runs each stage of the morphodynamic operator as one launch (E - D of a
+    16 x 16 block and the ring of cells around it, the vertex source and bed update, then the
+    cell bed and w / Hnpsi update, from shared memory; the refinement tests in the third).
+    With kg_set_fused_morpho(0) the same stage runs as the per-item E - D, vertex and cell
+    launches.  Both end in the same state bit for bit, with the same accepted and refused
+    steps and redistribution walks: on 50^2 tiles (partial blocks), on 8^2 tiles of a
+    periodic domain whose diagonal tiles are missing, and on the 2048^2 configuration's
+    terrain window in 32^2 tiles."""
+    p, b0 = _fused_case(name)
+    L = lib.load()
+    runs = []
+    for fused in (1, 0):
+        s = fp32(p, b0=b0)
+        assert L.kg_set_fused_morpho(s.h, fused) == abi.KG_OK
+        st = s.run()
+        state = {t: [s.field(t, f).copy() for f in (1, 2, 3, 4, 5, 11)] + [s.vertex(t, 1).copy()] for t in s.active_tiles()}
+        runs.append((st.steps, st.rejected, s.time[0], s.redistribution_stats(), s.ghost_tiles(), state,
+                     L.kg_kernel_launches(s.h)))
+        s.close()
+    a, b = runs
+    assert a[:5] == b[:5], (a[:5], b[:5])
+    assert a[5].keys() == b[5].keys()
+    for t in a[5]:
+        for x, y in zip(a[5][t], b[5][t]):
+            assert np.array_equal(x, y), t
+    assert a[6] < b[6]  # fewer launches with the fused stages
+
+
+@pytest.mark.parametrize("name,tend", [("flux_hydro_2d", 3.0), ("cap_morpho_2d", 1.0), ("window", 5.0)])
+def test_fp32_dry_skip_matches_full_blocks(name, tend):
+    """The FP32 form skips the reconstruction, flux and RHS work of a block whose cells and
+    two-cell halo hold no water (kg_set_dry_skip, on by default) and carries its state
+    forward.  The full computation of such a block changes it only by round-off of the dry
+    bed, so both runs take the same accepted and refused steps, activate the same tiles and
+    end within 1e-8 of the largest depth (w, Hn) and 1e-6 of the largest momentum of each
+    other; the FP32 error bounds against the oracle above hold with the skip on."""
+    if name == "window":
+        from kestrel_gb300 import workloads
+        p, b0 = workloads.morpho_flux_window(tend=tend)
+    else:
+        p, b0 = cases.ref_input(name, tend=tend, nout=1), None
+    L = lib.load()
+    runs = []
+    for skip in (1, 0):
+        s = fp32(p, b0=b0)
+        assert L.kg_set_dry_skip(s.h, skip) == abi.KG_OK
+        st = s.run()
+        runs.append((st.steps, st.rejected, s.active_tiles(), s.ghost_tiles(),
+                     {t: [s.field(t, f).copy() for f in (1, 2, 3, 5)] for t in s.active_tiles()}))
+        s.close()
+    a, b = runs
+    assert a[:4] == b[:4], (a[:2], b[:2])
+    depth = max(float(np.max(np.abs(v[3]))) for v in b[4].values())
+    mom = max(max(float(np.max(np.abs(v[1]))), float(np.max(np.abs(v[2])))) for v in b[4].values())
+    for t in a[4]:
+        x, y = a[4][t], b[4][t]
+        assert np.max(np.abs(x[0] - y[0])) <= 1e-8 * depth, t
+        assert np.max(np.abs(x[3] - y[3])) <= 1e-8 * depth, t
+        assert np.max(np.abs(x[1] - y[1])) <= 1e-6 * mom and np.max(np.abs(x[2] - y[2])) <= 1e-6 * mom, t
