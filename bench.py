@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import faulthandler
 import json
 import os
 import re
@@ -357,7 +358,8 @@ def run_serve(args):
     reqs = [serve.Request(arrival=t, params=p, b0=b0, desc=d) for t, p, b0, d in
             workloads.serve_requests(args.requests, rate=args.rate, tend_range=(args.tend_min, args.tend_max),
                                      tiles=lambda side: autotune.tile_for(side, tuned))]
-    srv = serve.Server(hbm_budget=args.budget_gb * 1e9, max_members=min(256, args.requests), keep_state=False)
+    srv = serve.Server(hbm_budget=args.budget_gb * 1e9, max_members=min(256, args.requests), keep_state=False,
+                       graphs=bool(args.batch_graphs))
     clocks = ClockSampler(0)
     clocks.start()
     try:
@@ -408,6 +410,29 @@ def extras_serve(args):
                     f"{args.serve_tend_scale} so that the stream is served within the default run"}
 
 
+EXTRAS = {"sparse_8192_fp32": lambda a: run_sparse_window(a, t_window=a.sparse_window, deadline_s=240.0),
+          "ensemble_fp32": lambda a: extras_ensemble(a),
+          "serve_fp32": lambda a: extras_serve(a)}
+
+
+def run_extra(key: str, args, timeout_s: float = 600.0):
+    """One secondary figure beside the headline, run as `bench.py --extra key` in a child
+    process; returns its JSON, or {"error": ...} when it fails, crashes or runs out of time."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--extra", key, "--sparse-window", str(args.sparse_window),
+           "--members", str(args.members), "--requests", str(args.requests), "--rate", str(args.rate),
+           "--tend-min", str(args.tend_min), "--tend-max", str(args.tend_max), "--budget-gb", str(args.budget_gb),
+           "--serve-tend-scale", str(args.serve_tend_scale), "--batch-graphs", str(args.batch_graphs)]
+    try:
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=timeout_s)
+    except subprocess.TimeoutExpired:
+        return {"error": f"no result within {timeout_s:.0f} s"}
+    sys.stderr.write(r.stderr)
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    if r.returncode == 0 and lines:
+        return json.loads(lines[-1])
+    return {"error": f"exit code {r.returncode}", "stderr_tail": r.stderr[-600:]}
+
+
 def run_sparse_window(args, t_window: float = 200.0, steps: int = 20, deadline_s=None):
     """The large sparse configuration (8192^2 cells in 16,384 tiles of 64^2, three seeded
     flux sources, Pouliquen drag, morphodynamics; FP32 form): an untimed spin-up to
@@ -423,7 +448,14 @@ def run_sparse_window(args, t_window: float = 200.0, steps: int = 20, deadline_s
     p, b0 = wl["params"]()
     t0 = time.perf_counter()
     sim = lib.simulation(p, precision=wl["prec"], b0=b0)
-    timeline = spin_up(sim, p, t_window, 20.0, deadline_s=deadline_s)
+    try:
+        timeline = spin_up(sim, p, t_window, 20.0, deadline_s=deadline_s)
+    except TimeoutError as e:
+        n_st = (C.c_int64 * 3)()
+        L.kg_get_counters(sim.h, n_st)
+        sim.close()
+        return {"workload": "sparse_8192_fp32", "error": str(e), "active_timeline": getattr(e, "timeline", None),
+                "steps_accepted_refused": [n_st[0], n_st[1]]}
     spin_s = time.perf_counter() - t0
     stream = torch.cuda.ExternalStream(L.kg_stream(sim.h))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -491,7 +523,11 @@ def spin_up(sim, p, spin, every=None, deadline_s=None):
             while sim.time[0] < t:
                 sim.step(t)
                 if time.perf_counter() - t0 > deadline_s:
-                    raise TimeoutError(f"spin-up reached t={sim.time[0]:.3f} s of {spin} s in {deadline_s:.0f} s of wall time")
+                    n = len(sim.active_tiles())
+                    out.append([round(sim.time[0], 3), n, round(100.0 * n / total, 3)])
+                    e = TimeoutError(f"spin-up reached t={sim.time[0]:.3f} s of {spin} s in {deadline_s:.0f} s of wall time")
+                    e.timeline = out
+                    raise e
         else:
             sim.integrate_to(t)
         n = len(sim.active_tiles())
@@ -720,6 +756,7 @@ def fp64_plain(args, wname, snapshot=None):
 
 
 def main():
+    faulthandler.enable()  # a native crash prints the Python stack to stderr
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
@@ -749,8 +786,16 @@ def main():
                     help="FP32 form: skip the flux work of blocks with no water (1) or run every block (0)")
     ap.add_argument("--error-times", default="5,10,20,40,80,120",
                     help="fp32_error_2048: checkpoints (s) of the depth comparison")
+    ap.add_argument("--extra", default=None, choices=sorted(EXTRAS), help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+
+    if args.extra:  # one secondary figure, in the child process run_extra starts
+        try:
+            print(json.dumps(EXTRAS[args.extra](args)))
+        except Exception as e:
+            print(json.dumps({"error": repr(e)}))
+        return
 
     if args.workload == "fp32_error_2048":
         if int(os.environ.get("RANK", "0")) != 0 or args.impl == "reference":
@@ -950,15 +995,11 @@ def main():
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(p, b0, snapshot=snapshot)
     if args.workload == "morpho_flux_2048_fp32" and not args.no_extras:
-        # the other forms of the metric on their own configurations, under their own keys
-        # (secondary figures: an error in one never loses the headline line)
-        for key, fn in (("sparse_8192_fp32", lambda: run_sparse_window(args, t_window=args.sparse_window, deadline_s=300.0)),
-                        ("ensemble_fp32", lambda: extras_ensemble(args)),
-                        ("serve_fp32", lambda: extras_serve(args))):
-            try:
-                line[key] = fn()
-            except Exception as e:
-                line[key] = {"error": repr(e)}
+        # the other forms of the metric on their own configurations, under their own keys;
+        # each runs in a process of its own, so an error or a crash in one never loses the
+        # headline line
+        for key in ("sparse_8192_fp32", "ensemble_fp32", "serve_fp32"):
+            line[key] = run_extra(key, args)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

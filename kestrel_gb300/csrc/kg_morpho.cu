@@ -462,8 +462,14 @@ __device__ __forceinline__ void excess_deposition(const DevParams& P, const DevA
         }
         deltaBt = C3[mp(s, 4, 1, SC) + c] - C0[mp(s, 4, 1, SC) + c];
         psiold = (double)A.MF[(size_t)s * SC + c];
-        excess = -(Z[2 * (size_t)SC] * P.invSolid - deltaBt);
-        excess = mx(excess, -(Z[(size_t)SC] - deltaBt));
+        // The deposition of this attempt is limited by the solids and depth the cell holds,
+        // taken at 0 where they are negative: next to deep flows the FP32 fluxes leave
+        // round-off of order 1e-9 in thin cells, which can make Hnpsi or the depth slightly
+        // negative, and a deficit the attempt did not cause is not excess deposition (M could
+        // never remove it, and refining dt would not shrink it).  Where both are >= 0 this is
+        // the reference's formula.
+        excess = -(mx(Z[2 * (size_t)SC], 0.0) * P.invSolid - deltaBt);
+        excess = mx(excess, -(mx(Z[(size_t)SC], 0.0) - deltaBt));
         return;
     }
     double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
@@ -582,7 +588,7 @@ __device__ bool redistribute_cell(const DevParams& P, const DevArrays& A, int qa
     if (PLAIN) {
         const double* Z = A.M0 + mp(s, 3, 0, SC) + c;
         Hg = Z[0] < 0.0 ? 0.0 : Z[(size_t)SC];
-        Hgp = Z[2 * (size_t)SC] * P.invSolid;
+        Hgp = mx(Z[2 * (size_t)SC], 0.0) * P.invSolid;  // as the excess test: negative solids taken at 0
     } else {
         double gamold = gam_of(P.geo, C0[mp(s, 4, 2, SC) + c], C0[mp(s, 4, 3, SC) + c]);
         double w0 = A.Q[qa][mp(s, 4, 0, SC) + c];

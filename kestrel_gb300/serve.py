@@ -61,9 +61,10 @@ def extract(sim) -> dict:
 
 
 class Server:
-    def __init__(self, hbm_budget: float = 150e9, max_members: int = 256, clock=time.perf_counter, keep_state: bool = True):
+    def __init__(self, hbm_budget: float = 150e9, max_members: int = 256, clock=time.perf_counter, keep_state: bool = True,
+                 graphs: bool = True):
         self.budget = float(hbm_budget)
-        self.batch = Batch(max_members)
+        self.batch = Batch(max_members, graphs=graphs)
         self.max_members = max_members
         self.clock = clock
         self.keep_state = keep_state
