@@ -728,9 +728,7 @@ def fp64_plain(args, wname, snapshot=None):
         st = sim.step(p.tend)
         cu_e += st.cell_updates
         n_e += st.steps
-    for t in sim.active_tiles():
-        for f in (1, 2, 3, 4):
-            sim.field(t, f)
+    sim.get_state()  # the conserved fields and bed change of every active tile, one call
     e2e_s = time.perf_counter() - t0
     xb1 = (C.c_int64 * 2)()
     L.kg_get_transfer_bytes(sim.h, xb1)
@@ -745,7 +743,8 @@ def fp64_plain(args, wname, snapshot=None):
            "active_tiles_end": active, "pass_ms": pass_ms,
            "e2e": {"value": cu_e / e2e_s if e2e_s > 0 else None, "unit": "cell-updates/s",
                    "h2d_bytes_per_step": (xb1[0] - xb0[0]) / max(n_e, 1), "d2h_bytes_per_step": (xb1[1] - xb0[1]) / max(n_e, 1),
-                   "note": f"host clock around {n_e} further kg_step calls, then the read-back of the conserved fields"}}
+                   "note": f"host clock around {n_e} further kg_step calls, then the read-back of the conserved fields "
+                           f"and bed change (kg_get_state)"}}
     try:  # the FP64 pass against its FP64 pipe; the clock is the GPU's maximum (not sampled here)
         cells = cu / max(n, 1) / (2.0 if p.MorphodynamicsOn else 1.0)
         n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
@@ -923,10 +922,10 @@ def main():
             n2 += st.steps
             if sim2.time[0] >= p.tend:
                 break
-        fields_bytes = 0
-        for t in sim2.active_tiles():
-            for f in (1, 2, 3, 4):
-                fields_bytes += sim2.field(t, f).nbytes
+        # the state a host reads back at the end: every active tile's conserved fields and
+        # vertex bed change in one call (kg_get_state: one gather, one copy per array)
+        _, st_fields, st_bt, _ = sim2.get_state()
+        fields_bytes = st_fields.nbytes + st_bt.nbytes
         t1 = time.perf_counter()
         xb1 = (C.c_int64 * 2)()
         L.kg_get_transfer_bytes(sim2.h, xb1)
@@ -964,7 +963,8 @@ def main():
         "e2e": {"value": cu2 / e2e_s if e2e_s > 0 else None, "unit": "cell-updates/s", "h2d_bytes_per_step": (xb1[0] - xb0[0]) / max(n2, 1),
                 "d2h_bytes_per_step": (xb1[1] - xb0[1]) / max(n2, 1),
                 "note": f"host clock around {n2} kg_step calls after the same spin-up, then the read-back of the "
-                        f"conserved fields ({fields_bytes} B, counted in d2h)"},
+                        f"conserved fields and bed change of every active tile with kg_get_state ({fields_bytes} B, "
+                        f"counted in d2h)"},
         "e2e_job": {"value": cu_job / job_s if job_s > 0 else None, "unit": "cell-updates/s", "seconds": job_s,
                     "note": "kg_create with the settings and bed grid uploaded, spin-up, warm-up and the same steps, "
                             "final read-back"},
