@@ -378,7 +378,7 @@ def run_serve(args):
 
 
 def extras_ensemble(args):
-    """configs[3] beside the headline: the batched ensemble of --members members, its
+    """The batched ensemble beside the headline: --members members (128^2-1024^2), its
     device-timed and host-clock throughput and round shape."""
     import copy
     a = copy.copy(args)
@@ -391,7 +391,7 @@ def extras_ensemble(args):
 
 
 def extras_serve(args):
-    """configs[4] beside the headline: the served request stream (Poisson arrivals at
+    """The served request stream beside the headline (Poisson arrivals at
     --rate per s, sides 256-2048, HBM budget --budget-gb), with the end times scaled by
     --serve-tend-scale so that the whole stream is served within the default run."""
     import copy
