@@ -338,13 +338,13 @@ struct SegGuard {
 // Room for `total` edge-band words (grown before a capture starts: no allocation inside one).
 void ensure_actout(kg_batch& b, int total) {
     if (total <= b.actout_cap) return;
+    const int cap = std::max(total, 2 * b.actout_cap);  // grows geometrically: few reallocations
     batch_sync(b);
     if (b.d_actout) CK(cudaFree(b.d_actout));
     if (b.h_actout) CK(cudaFreeHost(b.h_actout));
     b.d_actout = nullptr;
     b.h_actout = nullptr;
     b.actout_cap = 0;
-    int cap = std::max(total, 2 * b.actout_cap);
     CK(cudaMalloc(&b.d_actout, (size_t)cap * sizeof(int)));
     CK(cudaMallocHost(&b.h_actout, (size_t)cap * sizeof(int)));
     b.actout_cap = cap;
