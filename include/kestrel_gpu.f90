@@ -170,6 +170,18 @@ module kestrel_gpu
          type(c_ptr), value :: ctx
          real(c_double) :: t, dt
       end function
+      ! FP32 form: each morphodynamic stage as one launch (1, default) or three (0)
+      integer(c_int) function kg_set_fused_morpho(ctx, enable) bind(C, name="kg_set_fused_morpho")
+         import :: c_int, c_int32_t, c_ptr
+         type(c_ptr), value :: ctx
+         integer(c_int32_t), value :: enable
+      end function
+      ! FP32 form: skip the flux work of blocks with no water (1, default) or not (0)
+      integer(c_int) function kg_set_dry_skip(ctx, enable) bind(C, name="kg_set_dry_skip")
+         import :: c_int, c_int32_t, c_ptr
+         type(c_ptr), value :: ctx
+         integer(c_int32_t), value :: enable
+      end function
       subroutine kg_destroy(ctx) bind(C, name="kg_destroy")
          import :: c_ptr
          type(c_ptr), value :: ctx
