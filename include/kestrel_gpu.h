@@ -271,7 +271,8 @@ int  kg_get_kernel_time(kg_ctx* ctx, double* ms, int64_t* passes);
 /* FP32 form: run each stage of the morphodynamic operator (E - D, the vertex source and bed
    update, the cell bed and w / Hnpsi update; MorphodynamicTimeStepper, src/TimeStepper.f90:
    569-699) as one launch (enable, the default) or as three (0); the results are the same bit
-   for bit.  No effect on the FP64 form.  No reference counterpart. */
+   for bit.  No effect on the FP64 form or on batch members (the batched engine runs the
+   three launches, with the same results).  No reference counterpart. */
 int  kg_set_fused_morpho(kg_ctx* ctx, int32_t enable);
 /* FP32 form: skip the reconstruction, flux and RHS work of a 16 x 16 block whose cells and
    two-cell halo hold no water (depth above the bed, Hnpsi and momenta all within
